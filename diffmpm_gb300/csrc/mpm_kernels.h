@@ -1,0 +1,73 @@
+// Host-side launchers of the MPM kernels (implemented in mpm_kernels.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "mpm_types.h"
+
+namespace mpm {
+
+struct StepConfig {
+    bool usl;          // scheme: USL (else USF)
+    bool reinit;       // solve_jit semantics: volume/mass reset each step
+    bool traction;     // particle tractions present
+};
+
+// One explicit step = three launches over the tile list.
+cudaError_t launch_nodal_kinematics(const StepConfig& c, const SimDev* sims, const int4* tiles,
+                                    int ntiles, Control* ctl, cudaStream_t s);
+cudaError_t launch_forces(const StepConfig& c, const SimDev* sims, const int4* tiles, int ntiles,
+                          Control* ctl, cudaStream_t s);
+cudaError_t launch_particle_kinematics(const StepConfig& c, const SimDev* sims, const int4* tiles,
+                                       int ntiles, Control* ctl, cudaStream_t s);
+
+// Re-sort of one simulation's particles by current cell, stable in storage order.
+struct SortScratch {
+    int* count;        // ncell + 1 (last bucket: particles outside the mesh)
+    int* cursor;       // ncell + 1
+    int* key;          // np
+    int* perm;         // np
+    int* block_sums;   // ceil((ncell + 2) / 1024) + 1
+};
+cudaError_t launch_resort_keys(const SimDev* sim, int np, int nx, int ny, float hx, float hy,
+                               const SortScratch& w, Control* ctl, cudaStream_t s);
+cudaError_t launch_exclusive_scan(const int* in, int* out, int n, int* block_sums, cudaStream_t s);
+cudaError_t launch_resort_place(int np, const int* start, const SortScratch& w, cudaStream_t s);
+cudaError_t launch_resort_segsort(int nbucket, const int* start, const SortScratch& w,
+                                  cudaStream_t s);
+
+// dst[i] = src[perm[i]] for 4-byte and 1-byte elements.
+cudaError_t launch_gather_u32(const uint32_t* src, uint32_t* dst, const int* perm, int n,
+                              cudaStream_t s);
+cudaError_t launch_gather_u8(const uint8_t* src, uint8_t* dst, const int* perm, int n,
+                             cudaStream_t s);
+cudaError_t launch_gather_pair_u32(const uint32_t* src, uint32_t* dst, const int* perm, int n,
+                                   cudaStream_t s);
+cudaError_t launch_gather_pair_u8(const uint8_t* src, uint8_t* dst, const int* perm, int n,
+                                  cudaStream_t s);
+
+// Solve-semantics volume set-up after a sort (V = V_el / count, m = V rho, size = sqrt V).
+cudaError_t launch_setup_volume(const SimDev* sim, int np, int parity, cudaStream_t s);
+
+// Field transfer between original order (AoS, ncomp per particle) and storage order (SoA).
+// comp_ptrs: device array of ncomp float* (storage order); pid: storage -> original.
+cudaError_t launch_scatter_out(const float* const* comp_ptrs, int ncomp, const int* pid, int np,
+                               float* out, cudaStream_t s);
+cudaError_t launch_gather_in(float* const* comp_ptrs, int ncomp, const int* pid, int np,
+                             const float* in, cudaStream_t s);
+cudaError_t launch_gather_in_u8(uint8_t* dst, const int* pid, int np, const int32_t* in,
+                                cudaStream_t s);
+cudaError_t launch_scatter_out_u8(const uint8_t* src, const int* pid, int np, int32_t* out,
+                                  cudaStream_t s);
+
+// Derived per-particle outputs in original order: element id, volume, mass
+// (solve_jit semantics: the volume set-up at the current positions), momentum.
+cudaError_t launch_derived_out(const SimDev* sim, int np, int parity, bool reinit, int what,
+                               const int* pid, void* out, cudaStream_t s);
+
+// Interleave / de-interleave nodal vectors.
+cudaError_t launch_interleave2(const float* a, const float* b, int n, float* out, cudaStream_t s);
+cudaError_t launch_deinterleave2(const float* in, int n, float* a, float* b, cudaStream_t s);
+cudaError_t launch_node_momentum(const float* m, const float* vx, const float* vy, int n,
+                                 float* out, cudaStream_t s);
+
+}  // namespace mpm

@@ -1,0 +1,97 @@
+// Device-visible simulation descriptor shared by the kernels and the host driver.
+//
+// Layout in HBM (one simulation; a batch is an array of these):
+//   particles  SoA float32 in cell-sorted storage order.  Fields that a tile
+//              reads for its one-cell halo while the owner tile rewrites them
+//              (stress, density, volumetric strain, volume) are ping-pong
+//              pairs indexed by the step parity; the rest are single arrays.
+//   cells      cstart[Ne+1]: storage range of each sort-cell (cell at the last
+//              re-sort); cflag[Ne]: 1 when a particle stored in the sort-cell
+//              is currently in another cell.
+//   nodes      mass, velocity after the nodal-kinematics phase (nva*),
+//              velocity and acceleration after the nodal update (nvb*, na*),
+//              a 16-bit constraint code per node.
+#pragma once
+#include <stdint.h>
+
+namespace mpm {
+
+constexpr int TILE_CX = 32;              // cells per tile row (one warp)
+constexpr int TILE_CY = 16;              // cell rows per tile
+constexpr int TILE_NX = TILE_CX - 1;     // nodes owned per tile row
+constexpr int TILE_NY = TILE_CY - 1;     // node rows owned per tile
+constexpr int TILE_THREADS = TILE_CX * TILE_CY;
+
+enum StatusBits : int {
+    ST_OUT_OF_MESH = 1,     // a particle left the mesh
+    ST_DRIFT_VIOLATION = 2, // a particle is more than one cell from its sort-cell
+    ST_DRIFTED = 4,         // some particle is in a cell other than its sort-cell
+    ST_TRACTION_CONFLICT = 8
+};
+
+enum MatType : int { MAT_LINEAR_ELASTIC = 0, MAT_SIMPLE = 1, MAT_NEWTONIAN = 2 };
+
+struct MatDev {
+    int type;
+    float a1, a2, G;       // LinearElastic D-matrix entries (host float64 -> float32)
+    float c1, c2, c3;      // a1, a2, G per unit Young's modulus (per-particle E)
+    float E;               // SimpleMaterial
+    float K, mu, twomu;    // Newtonian
+    float density;
+};
+
+struct SimDev {
+    // mesh
+    int nx, ny;
+    float hx, hy;
+    float vol_el;          // element volume (reference formula, float32)
+    float dt;
+    float gx, gy;
+    int tiles_x, tiles_y;
+    int np;
+    int velocity_update;
+    // particles (storage order)
+    float *x, *y, *vx, *vy;
+    float *sxx[2], *syy[2], *szz[2], *sxy[2];
+    float *exx, *eyy, *exy;
+    float *rho[2], *vsc[2];
+    float *vol[2];         // persistent volume (solve semantics only)
+    float *mass;           // persistent mass (solve semantics only)
+    float *psize;          // persistent size (solve semantics with tractions only)
+    uint8_t *mat;
+    float *E;              // per-particle Young's modulus or null
+    int8_t *tr_fn;         // [2 per particle] 0 none, 1 Unit, k+2 table k; null if no tractions
+    float *tr_tau;         // [2 per particle]
+    int *pid;              // storage index -> original particle index
+    // cells
+    int *cstart;
+    uint8_t *cflag;
+    // nodes
+    float *nm;
+    float *nvax, *nvay;
+    float *nvbx, *nvby;
+    float *nax, *nay;
+    uint16_t *ncons;       // low byte: dir-0 velocity slot+1, high byte: dir-1 slot+1
+    const float *cons_vel; // constraint velocity table
+    const int *cnf_ptr;    // CSR per node into the nodal-force entries (null if none)
+    const int8_t *cnf_dir;
+    const float *cnf_val;
+    const int8_t *cnf_fn;  // 1 Unit, k+2 table k
+    // time functions
+    int nfn;
+    const int *fn_off;     // nfn+1 offsets
+    const float *fn_x, *fn_y;
+    // materials
+    int nmat;
+    const MatDev *mats;
+};
+
+// Per-batch control block.
+struct Control {
+    int step;              // step counter i (t = i * dt)
+    int status;            // StatusBits
+    unsigned int done;     // finished-block counter of the last-block pattern
+    int pad;
+};
+
+}  // namespace mpm

@@ -1,0 +1,238 @@
+"""GPU-resident simulation: the Python face of one C handle.
+
+``Simulation`` owns one ``MpmHandle`` (include/diffmpm_gb300.h).  Arrays passed
+in or out may be NumPy arrays (host memory; the library copies) or CUDA torch
+tensors (device memory on the handle's GPU; used in place, ordered on torch's
+current stream).  All arithmetic runs in the CUDA library.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Sequence
+
+import numpy as np
+
+from . import _lib
+from .functions import Linear, Unit
+
+_FIELD_NCOMP = {"loc": "ndim", "velocity": "ndim", "momentum": "ndim", "stress": 6, "strain": 6}
+_INT_FIELDS = ("material_id", "element_ids")
+
+
+def _is_cuda_tensor(a) -> bool:
+    return type(a).__module__.startswith("torch") and getattr(a, "is_cuda", False)
+
+
+def _stream_for(a):
+    if _is_cuda_tensor(a):
+        import torch
+        return C.c_void_p(torch.cuda.current_stream(a.device).cuda_stream)
+    return None
+
+
+def _in_arg(a, dtype, count):
+    """(pointer, on_device, keepalive) for an input of ``count`` elements."""
+    if _is_cuda_tensor(a):
+        import torch
+        want = torch.float32 if dtype == np.float32 else torch.int32
+        if a.dtype != want or not a.is_contiguous() or a.numel() != count:
+            raise ValueError(f"expected a contiguous {want} tensor of {count} elements")
+        return C.c_void_p(a.data_ptr()), 1, a
+    arr = np.ascontiguousarray(np.asarray(a, dtype=dtype).reshape(-1))
+    if arr.size != count:
+        raise ValueError(f"expected {count} values, found {arr.size}")
+    return _lib.ptr(arr), 0, arr
+
+
+class Simulation:
+    """One explicit-MPM simulation on the current CUDA device.
+
+    Parameters mirror Quadrilateral4Node (nelements, el_len, constraints,
+    concentrated_nodal_forces) and MPMExplicit (dt, scheme, velocity_update);
+    ``reinit_each_step`` selects solve_jit semantics (True) or solve semantics.
+    ``functions`` lists the Linear time functions that forces and tractions
+    may refer to.
+    """
+
+    def __init__(self, nelements, el_len, dt, *, scheme="usf", velocity_update=False,
+                 reinit_each_step=True, gravity=(0.0, 0.0), constraints=(), functions=(),
+                 nodal_forces=(), materials=(), ndim=2):
+        self._lib = _lib.load()
+        self._h = C.c_void_p()
+        if scheme not in ("usf", "usl"):
+            raise ValueError(f"Please select scheme from ('usf', 'usl'). Found {scheme}")
+        nel = np.asarray(nelements, dtype=np.int64).reshape(-1)
+        el = np.broadcast_to(np.asarray(el_len, dtype=np.float64).reshape(-1), (2,))
+        self.ndim = ndim
+        self.nelements = (int(nel[0]), int(nel[1]) if nel.size > 1 else 1)
+        self.nnodes = (self.nelements[0] + 1) * (self.nelements[1] + 1)
+        self.functions = [f for f in functions if isinstance(f, Linear)]
+        self._fn_index = {id(f): k for k, f in enumerate(self.functions)}
+        g = np.broadcast_to(np.asarray(gravity, dtype=np.float64).reshape(-1), (2,))
+
+        d = _lib.MpmDesc()
+        d.ndim = ndim
+        d.nelements[0], d.nelements[1] = self.nelements
+        d.el_len[0], d.el_len[1] = float(el[0]), float(el[1])
+        d.scheme = _lib.USF if scheme == "usf" else _lib.USL
+        d.velocity_update = int(bool(velocity_update))
+        d.reinit_each_step = int(bool(reinit_each_step))
+        d.dt = float(dt)
+        d.gravity[0], d.gravity[1] = float(g[0]), float(g[1])
+        keep = []
+
+        def arr(values, dtype, ctype):
+            a = np.ascontiguousarray(np.asarray(values, dtype=dtype).reshape(-1))
+            keep.append(a)
+            return a.ctypes.data_as(C.POINTER(ctype))
+
+        cn, cd, cv = [], [], []
+        for ids, con in constraints:
+            ids = np.asarray(ids, dtype=np.int64).reshape(-1)
+            cn.extend(ids.tolist())
+            cd.extend([con.dir] * ids.size)
+            cv.extend([float(con.velocity)] * ids.size)
+        d.n_constraints = len(cn)
+        d.constraint_node = arr(cn, np.int32, C.c_int32)
+        d.constraint_dir = arr(cd, np.int32, C.c_int32)
+        d.constraint_velocity = arr(cv, np.float64, C.c_double)
+
+        d.n_functions = len(self.functions)
+        d.function_npoints = arr([f.xvalues.size for f in self.functions], np.int32, C.c_int32)
+        d.function_x = arr(np.concatenate([f.xvalues for f in self.functions]) if self.functions else [],
+                           np.float64, C.c_double)
+        d.function_y = arr(np.concatenate([f.fxvalues for f in self.functions]) if self.functions else [],
+                           np.float64, C.c_double)
+
+        fnode, fdir, fval, ffn = [], [], [], []
+        for f in nodal_forces:
+            ids = np.asarray(f.node_ids, dtype=np.int64).reshape(-1)
+            fnode.extend(ids.tolist())
+            fdir.extend([int(f.dir)] * ids.size)
+            fval.extend([float(f.force)] * ids.size)
+            ffn.extend([self.function_code(f.function)] * ids.size)
+        d.n_nodal_forces = len(fnode)
+        d.nodal_force_node = arr(fnode, np.int32, C.c_int32)
+        d.nodal_force_dir = arr(fdir, np.int32, C.c_int32)
+        d.nodal_force_value = arr(fval, np.float64, C.c_double)
+        d.nodal_force_function = arr(ffn, np.int32, C.c_int32)
+
+        mats = (_lib.MpmMaterial * max(1, len(materials)))()
+        for i, m in enumerate(materials):
+            mats[i] = m.to_c()
+        d.n_materials = len(materials)
+        d.materials = mats
+        self.materials = list(materials)
+        rc = self._lib.mpm_create(C.byref(d), C.byref(self._h))
+        if rc != _lib.MPM_OK:
+            self._h = C.c_void_p()
+            _lib.check(rc, None)
+        self.n = -1
+
+    # ------------------------------------------------------------------
+    def function_code(self, fn) -> int:
+        if fn is None or isinstance(fn, Unit):
+            return -1
+        if id(fn) not in self._fn_index:
+            raise ValueError("time function was not registered with the simulation")
+        return self._fn_index[id(fn)]
+
+    def _ok(self, rc):
+        _lib.check(rc, self._h)
+
+    def close(self):
+        if self._h:
+            self._lib.mpm_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def ncomp(self, field) -> int:
+        n = _FIELD_NCOMP.get(field, 1)
+        return self.ndim if n == "ndim" else n
+
+    # ------------------------------------------------------------------
+    def set_particles(self, loc, material_id=None):
+        """Set the population at ``loc`` (n, ndim); every other field takes the
+        reference's initial value (diffmpm/particle.py:53-71)."""
+        n = int(np.prod(np.shape(loc))) // self.ndim if not _is_cuda_tensor(loc) else loc.numel() // self.ndim
+        p, dev, keep = _in_arg(loc, np.float32, n * self.ndim)
+        mp, mdev, mkeep = (None, dev, None) if material_id is None else _in_arg(material_id, np.int32, n)
+        if material_id is not None and mdev != dev:
+            raise ValueError("loc and material_id must both be host arrays or both CUDA tensors")
+        self._ok(self._lib.mpm_set_particles(self._h, n, p, mp, dev, _stream_for(loc)))
+        self.n = n
+
+    def write(self, field, values):
+        dtype = np.int32 if field in _INT_FIELDS else np.float32
+        p, dev, keep = _in_arg(values, dtype, self.n * self.ncomp(field))
+        self._ok(self._lib.mpm_write_field(self._h, _lib.FIELD[field], p, dev, _stream_for(values)))
+
+    def read(self, field, out=None):
+        """Field in original particle order, shape (n, ncomp) (or (n,))."""
+        nc = self.ncomp(field)
+        dtype = np.int32 if field in _INT_FIELDS else np.float32
+        if out is None:
+            out = np.empty((self.n, nc) if nc > 1 else (self.n,), dtype=dtype)
+        if _is_cuda_tensor(out):
+            p, dev = C.c_void_p(out.data_ptr()), 1
+        else:
+            p, dev = _lib.ptr(out), 0
+        self._ok(self._lib.mpm_read_field(self._h, _lib.FIELD[field], p, dev, _stream_for(out)))
+        return out
+
+    def set_tractions(self, pids, dirs, values, functions):
+        """Particle tractions: entry k adds f_k(t) * values[k] * V / size in
+        direction dirs[k] of particle pids[k] (diffmpm/particle.py:329-343)."""
+        pids = np.ascontiguousarray(np.asarray(pids, dtype=np.int64).reshape(-1))
+        dirs = np.ascontiguousarray(np.asarray(dirs, dtype=np.int32).reshape(-1))
+        vals = np.ascontiguousarray(np.asarray(values, dtype=np.float64).reshape(-1))
+        fns = np.ascontiguousarray(np.asarray([self.function_code(f) for f in functions],
+                                              dtype=np.int32).reshape(-1))
+        self._ok(self._lib.mpm_set_tractions(self._h, int(pids.size), _lib.ptr(pids), _lib.ptr(dirs),
+                                             _lib.ptr(vals), _lib.ptr(fns), None))
+
+    def read_nodal(self, field, out=None):
+        nc = 1 if field == "mass" else 2
+        if out is None:
+            out = np.empty((self.nnodes, nc) if nc > 1 else (self.nnodes,), dtype=np.float32)
+        dev = 1 if _is_cuda_tensor(out) else 0
+        p = C.c_void_p(out.data_ptr()) if dev else _lib.ptr(out)
+        self._ok(self._lib.mpm_read_nodal_field(self._h, _lib.NODAL_FIELD[field], p, dev, _stream_for(out)))
+        return out
+
+    def write_nodal(self, field, values):
+        nc = 1 if field == "mass" else 2
+        p, dev, keep = _in_arg(values, np.float32, self.nnodes * nc)
+        self._ok(self._lib.mpm_write_nodal_field(self._h, _lib.NODAL_FIELD[field], p, dev, _stream_for(values)))
+
+    def initialize(self, stream=None):
+        self._ok(self._lib.mpm_initialize(self._h, stream))
+
+    def step(self, nsteps=1, stream=None):
+        self._ok(self._lib.mpm_step(self._h, int(nsteps), stream))
+
+    def run_phase(self, phase, stream=None):
+        self._ok(self._lib.mpm_run_phase(self._h, _lib.PHASE[phase], stream))
+
+    @property
+    def step_index(self) -> int:
+        v = C.c_int64()
+        self._ok(self._lib.mpm_get_step(self._h, C.byref(v)))
+        return v.value
+
+    @step_index.setter
+    def step_index(self, value):
+        self._ok(self._lib.mpm_set_step(self._h, int(value)))
+
+    def set_block_steps(self, n):
+        self._ok(self._lib.mpm_set_block_steps(self._h, int(n)))
+
+    def counters(self):
+        a, b = C.c_int64(), C.c_int64()
+        self._ok(self._lib.mpm_get_counters(self._h, C.byref(a), C.byref(b)))
+        return {"resorts": a.value, "rollbacks": b.value}

@@ -1,0 +1,195 @@
+"""Explicit MPM driver with the reference's surface (diffmpm/solver.py:19-222).
+
+``MPMExplicit(mesh, dt, scheme, velocity_update, sim_steps, out_steps, out_dir,
+writer_func)`` with ``solve_jit(gravity)`` and ``solve(gravity)``.  Every step
+runs in the CUDA library (engine.Simulation); the Python objects hold the
+initial state, as the reference's pytrees do.
+
+* ``solve_jit`` is pure like the reference's: it starts from the objects'
+  state, advances ``sim_steps`` steps with the per-step volume/mass set-up of
+  the reference's ``lax.fori_loop`` (solver.py:100-111, 213), calls
+  ``writer_func((arrays, i), None, out_dir=..., max_steps=...)`` after step i
+  when ``i % out_steps == 0`` (solver.py:203-210) and returns the final
+  ``{"loc", "velocity", "stress", "strain"}`` (solver.py:214-222).
+* ``solve`` runs without the per-step set-up, records every step
+  (solver.py:116-157) and leaves the final state in the objects.
+"""
+from __future__ import annotations
+
+from collections import defaultdict
+
+import numpy as np
+
+from .engine import Simulation
+from .functions import Linear
+
+_schemes = ("usf", "usl")
+
+
+class MPMExplicit:
+    __particle_props = ("loc", "velocity", "stress", "strain")
+
+    def __init__(self, mesh, dt, scheme="usf", velocity_update=False, sim_steps=1, out_steps=1,
+                 out_dir="results/", writer_func=None):
+        if scheme not in _schemes:
+            raise ValueError(f"Please select scheme from {_schemes}. Found {scheme}")
+        self.mesh = mesh
+        self.dt = dt
+        self.scheme = scheme
+        self.velocity_update = velocity_update
+        self.sim_steps = sim_steps
+        self.out_steps = out_steps
+        self.out_dir = out_dir
+        self.writer_func = writer_func
+        self._sims = {}
+        # the constructor's volume set-up (solver.py:81-85), run on the GPU
+        sim = self.simulation(np.zeros(2), reinit=True)
+        self._upload(sim)
+        sim.initialize()
+        self._pull_setup(sim)
+
+    # ------------------------------------------------------------------
+    def _population(self):
+        sets = self.mesh.particles
+        mats, mat_index = [], {}
+        for p in sets:
+            for m in p.materials:
+                if id(m) not in mat_index:
+                    mat_index[id(m)] = len(mats)
+                    mats.append(m)
+        offsets = np.cumsum([0] + [len(p) for p in sets])
+        return sets, mats, mat_index, offsets
+
+    def _functions(self):
+        fns = []
+        for f in list(self.mesh.elements.concentrated_nodal_forces) + list(self.mesh.particle_tractions):
+            if isinstance(f.function, Linear) and all(f.function is not g for g in fns):
+                fns.append(f.function)
+        return fns
+
+    def simulation(self, gravity, reinit=True) -> Simulation:
+        """The GPU simulation for this configuration (cached per gravity/mode)."""
+        g = np.broadcast_to(np.asarray(gravity, dtype=np.float64).reshape(-1), (2,))
+        key = (float(g[0]), float(g[1]), bool(reinit))
+        if key not in self._sims:
+            el = self.mesh.elements
+            _, mats, _, _ = self._population()
+            self._sims[key] = Simulation(
+                el.nelements, el.el_len, self.dt, scheme=self.scheme,
+                velocity_update=self.velocity_update, reinit_each_step=reinit, gravity=g,
+                constraints=el.constraints, functions=self._functions(),
+                nodal_forces=el.concentrated_nodal_forces, materials=mats,
+                ndim=getattr(el, "ndim", 2))
+        return self._sims[key]
+
+    def _upload(self, sim: Simulation):
+        sets, mats, mat_index, offsets = self._population()
+        ndim = sim.ndim
+        loc = np.concatenate([p.loc.reshape(len(p), ndim) for p in sets])
+        mids = np.concatenate([np.asarray([mat_index[id(p.materials[k])] for k in p.material_ids],
+                                          dtype=np.int32).reshape(-1) for p in sets])
+        sim.set_particles(loc, mids)
+        sim.write("velocity", np.concatenate([p.velocity.reshape(len(p), ndim) for p in sets]))
+        sim.write("stress", np.concatenate([p.stress.reshape(len(p), 6) for p in sets]))
+        sim.write("strain", np.concatenate([p.strain.reshape(len(p), 6) for p in sets]))
+        sim.write("density", np.concatenate([p.density.reshape(-1) for p in sets]))
+        sim.write("volumetric_strain_centroid",
+                  np.concatenate([p.volumetric_strain_centroid.reshape(-1) for p in sets]))
+        if any(p.youngs_modulus is not None for p in sets):
+            E = []
+            for p in sets:
+                if p.youngs_modulus is not None:
+                    E.append(p.youngs_modulus)
+                else:
+                    E.append(np.full(len(p), -1.0, dtype=np.float32))
+            sim.write("youngs_modulus", np.concatenate(E))
+        sim.write_nodal("velocity", self.mesh.elements.nodes.velocity.reshape(-1, ndim))
+        pids, dirs, vals, fns = [], [], [], []
+        for pt in self.mesh.particle_tractions:
+            psets = pt.pset if isinstance(pt.pset, (list, tuple, np.ndarray)) else [pt.pset]
+            ids = np.asarray(pt.pids, dtype=np.int64).reshape(-1)
+            for s in psets:
+                pids.extend((offsets[int(s)] + ids).tolist())
+                dirs.extend([int(pt.dir)] * ids.size)
+                vals.extend([float(pt.traction)] * ids.size)
+                fns.extend([pt.function] * ids.size)
+        if pids:
+            sim.set_tractions(pids, dirs, vals, fns)
+
+    def _pull_setup(self, sim: Simulation):
+        sets, _, _, offsets = self._population()
+        e = sim.read("element_ids")
+        vol = sim.read("volume")
+        mass = sim.read("mass")
+        ndim = sim.ndim
+        for k, p in enumerate(sets):
+            sl = slice(offsets[k], offsets[k + 1])
+            p.element_ids = e[sl].copy()
+            p.volume = vol[sl].reshape(-1, 1, 1).copy()
+            p.mass = mass[sl].reshape(-1, 1, 1).copy()
+            p.size = np.broadcast_to(np.sqrt(p.volume), p.loc.shape).astype(np.float32).copy()
+        self.mesh.elements.volume[:] = self._element_volume()
+
+    def _element_volume(self):
+        """Element volume by the reference's formula (element.py:903-909), the
+        value the library uses."""
+        el = self.mesh.elements
+        a = c = np.float32(el.el_len[1])
+        b = d = np.float32(el.el_len[0])
+        p = q = np.sqrt(a * a + b * b)
+        t = a * a + c * c - b * b - d * d
+        return np.float32(0.25) * np.sqrt(np.float32(4) * p * p * q * q - t * t)
+
+    def _arrays(self, sim: Simulation, squeeze_each=True):
+        sets, _, _, offsets = self._population()
+        out = {}
+        for name in self.__particle_props:
+            a = sim.read(name)
+            per = []
+            for k, p in enumerate(sets):
+                v = a[offsets[k]:offsets[k + 1]]
+                shape = (len(p), 1, sim.ndim) if name in ("loc", "velocity") else (len(p), 6, 1)
+                v = v.reshape(shape)
+                per.append(v.squeeze() if squeeze_each else v)
+            out[name] = np.array(per)
+        return out
+
+    # ------------------------------------------------------------------
+    def solve_jit(self, gravity) -> dict:
+        sim = self.simulation(gravity, reinit=True)
+        self._upload(sim)
+        sim.initialize()
+        done = 0
+        if self.writer_func is not None:
+            for i in range(0, self.sim_steps, self.out_steps):
+                sim.step(i + 1 - done)
+                done = i + 1
+                self.writer_func((self._arrays(sim), i), None, out_dir=self.out_dir,
+                                 max_steps=self.sim_steps)
+        sim.step(self.sim_steps - done)
+        return {k: v.squeeze() for k, v in self._arrays(sim, squeeze_each=False).items()}
+
+    def solve(self, gravity) -> dict:
+        sim = self.simulation(gravity, reinit=False)
+        self._upload(sim)
+        sim.initialize()
+        sets, _, _, offsets = self._population()
+        result = defaultdict(list)
+        for _ in range(self.sim_steps):
+            sim.step(1)
+            loc, vel = sim.read("loc"), sim.read("velocity")
+            stress, strain = sim.read("stress"), sim.read("strain")
+            for k, p in enumerate(sets):
+                sl = slice(offsets[k], offsets[k + 1])
+                result["position"].append(loc[sl].reshape(-1, 1, sim.ndim))
+                result["velocity"].append(vel[sl].reshape(-1, 1, sim.ndim))
+                result["stress"].append(stress[sl, :2])
+                result["strain"].append(strain[sl, :2])
+        for k, p in enumerate(sets):
+            sl = slice(offsets[k], offsets[k + 1])
+            p.loc = sim.read("loc")[sl].reshape(p.loc.shape)
+            p.velocity = sim.read("velocity")[sl].reshape(p.velocity.shape)
+            p.stress = sim.read("stress")[sl].reshape(p.stress.shape)
+            p.strain = sim.read("strain")[sl].reshape(p.strain.shape)
+            p.density = sim.read("density")[sl].reshape(p.density.shape)
+        return {k: np.asarray(v) for k, v in result.items()}

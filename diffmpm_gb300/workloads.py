@@ -1,0 +1,116 @@
+"""Synthetic workloads of the benchmark configurations.
+
+Each builder returns ``(solver, gravity, info)`` for an API module ``api`` that
+exposes the reference's class names (this package, or any restatement with the
+same surface), so that the same input can be built for two implementations.
+Inputs are seeded (NumPy PCG64); no dataset is involved.
+
+* ``plain_small``  10 x 10 Q4 mesh on [0,1]^2, 2 x 2 Gauss-point particles in
+  the cells covering [0.2, 0.8]^2 (144 particles), LinearElastic E=1e4,
+  nu=0.3, rho=1000, gravity (0, -9.81), nodes at y=0 fixed in x and y,
+  dt=1e-4, USF, 1000 steps.
+* ``plain_scaleup``  n x n mesh (n=1024 at full size) on [0,1]^2, 4 Gauss-point
+  particles per cell filling x in [0, 0.5], y in [0, 1], jittered uniformly by
+  +-0.1 h per component, LinearElastic E=1e6, nu=0.25, rho=2000, gravity,
+  roller walls (x fixed at x=0 and x=1), bottom fixed, dt=1e-6, 500 steps,
+  USF or USL.
+* ``mixed_large``  n x n mesh (n=4096 at full size), an elastic block
+  x in [0.125, 0.375] and a Newtonian block x in [0.625, 0.875], both
+  y in [0, 0.5], 4 Gauss points per cell, elastic E=5e6, nu=0.3, rho=1800,
+  fluid K=2e6, mu=1e-3, rho=1000, initial velocities N(0, 0.01^2), gravity,
+  roller walls and fixed bottom, USL, dt=2e-7, 200 steps.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+GAUSS = 1.0 / (2.0 * np.sqrt(3.0))   # Gauss offset from the cell centre, in cells
+
+
+def gauss_points(i0, i1, j0, j1, h):
+    """Particles at the 2 x 2 Gauss points of cells [i0,i1) x [j0,j1) (float64),
+    ordered cell by cell (row-major), 4 per cell."""
+    ii, jj = np.meshgrid(np.arange(i0, i1), np.arange(j0, j1), indexing="xy")
+    cx = (ii.reshape(-1) + 0.5) * h
+    cy = (jj.reshape(-1) + 0.5) * h
+    off = np.array([[-GAUSS, -GAUSS], [GAUSS, -GAUSS], [-GAUSS, GAUSS], [GAUSS, GAUSS]]) * h
+    pts = np.stack([cx, cy], axis=-1)[:, None, :] + off[None, :, :]
+    return pts.reshape(-1, 2)
+
+
+def _node_ids(n_x, n_y, pred):
+    ii, jj = np.meshgrid(np.arange(n_x + 1), np.arange(n_y + 1), indexing="xy")
+    ii, jj = ii.reshape(-1), jj.reshape(-1)
+    return np.nonzero(pred(ii, jj))[0].astype(np.int64)
+
+
+def _mesh(api, n, h, constraints, kw):
+    return api.Quadrilateral4Node((n, n), n * n, (h, h), constraints, **kw)
+
+
+def plain_small(api, sim_steps=1000, dt=1e-4, velocity=None, velocity_update=False, **kw):
+    n, h = 10, 0.1
+    pts = gauss_points(2, 8, 2, 8, h)
+    mat = api.LinearElastic({"density": 1000, "youngs_modulus": 1e4, "poisson_ratio": 0.3})
+    bottom = _node_ids(n, n, lambda i, j: j == 0)
+    cons = [(bottom, api.Constraint(0, 0.0)), (bottom, api.Constraint(1, 0.0))]
+    el = _mesh(api, n, h, cons, kw)
+    ps = api.Particles(pts.reshape(-1, 1, 2), mat, np.zeros(len(pts), dtype=np.int32), **kw)
+    if velocity is not None:
+        ps.velocity[:] = np.asarray(velocity, dtype=np.float64).reshape(1, 1, 2)
+    mesh = api.Mesh2D({"particles": [ps], "elements": el, "particle_surface_traction": []})
+    solver = api.MPMExplicit(mesh, dt, scheme="usf", velocity_update=velocity_update,
+                             sim_steps=sim_steps)
+    return solver, np.array([0.0, -9.81]), {"workload": "plain_small", "n": n, "np": len(pts)}
+
+
+def _rollers_and_bottom(api, n):
+    walls = _node_ids(n, n, lambda i, j: (i == 0) | (i == n))
+    bottom = _node_ids(n, n, lambda i, j: j == 0)
+    return [(walls, api.Constraint(0, 0.0)), (bottom, api.Constraint(0, 0.0)),
+            (bottom, api.Constraint(1, 0.0))]
+
+
+def plain_scaleup(api, n=1024, scheme="usf", sim_steps=500, seed=2024, rows=None, **kw):
+    """``rows`` keeps only the particles of the first ``rows`` cell rows (a
+    bounded sample of the same workload on the same mesh)."""
+    h = 1.0 / n
+    pts = gauss_points(0, n // 2, 0, n if rows is None else rows, h)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    pts = pts + rng.uniform(-0.1 * h, 0.1 * h, size=pts.shape)
+    mat = api.LinearElastic({"density": 2000, "youngs_modulus": 1e6, "poisson_ratio": 0.25})
+    el = _mesh(api, n, h, _rollers_and_bottom(api, n), kw)
+    ps = api.Particles(pts.reshape(-1, 1, 2), mat, np.zeros(len(pts), dtype=np.int32), **kw)
+    mesh = api.Mesh2D({"particles": [ps], "elements": el, "particle_surface_traction": []})
+    solver = api.MPMExplicit(mesh, 1e-6, scheme=scheme, velocity_update=False, sim_steps=sim_steps)
+    return solver, np.array([0.0, -9.81]), {"workload": f"plain_scaleup_{scheme}", "n": n,
+                                             "np": len(pts), "seed": seed}
+
+
+def mixed_large(api, n=4096, sim_steps=200, seed=7, **kw):
+    h = 1.0 / n
+    a0, a1 = int(round(0.125 * n)), int(round(0.375 * n))
+    b0, b1 = int(round(0.625 * n)), int(round(0.875 * n))
+    top = int(round(0.5 * n))
+    elastic = gauss_points(a0, a1, 0, top, h)
+    fluid = gauss_points(b0, b1, 0, top, h)
+    pts = np.concatenate([elastic, fluid])
+    mid = np.concatenate([np.zeros(len(elastic), np.int32), np.ones(len(fluid), np.int32)])
+    mats = [api.LinearElastic({"density": 1800, "youngs_modulus": 5e6, "poisson_ratio": 0.3}),
+            api.Newtonian({"density": 1000, "bulk_modulus": 2e6, "dynamic_viscosity": 1e-3})]
+    rng = np.random.Generator(np.random.PCG64(seed))
+    vel = rng.normal(0.0, 0.01, size=pts.shape)
+    el = _mesh(api, n, h, _rollers_and_bottom(api, n), kw)
+    ps = api.Particles(pts.reshape(-1, 1, 2), mats, np.zeros(len(pts), dtype=np.int32),
+                       material_ids=mid, **kw)
+    ps.velocity[:] = vel.reshape(-1, 1, 2)
+    mesh = api.Mesh2D({"particles": [ps], "elements": el, "particle_surface_traction": []})
+    solver = api.MPMExplicit(mesh, 2e-7, scheme="usl", velocity_update=False, sim_steps=sim_steps)
+    return solver, np.array([0.0, -9.81]), {"workload": "mixed_large", "n": n, "np": len(pts),
+                                             "seed": seed}
+
+
+def particle_steps_bytes(np_, nn):
+    """Algorithmic bytes of one step: 104 B of particle state read and written
+    once per particle plus 72 B per node (the minimal unique float32 traffic)."""
+    return 104.0 * np_ + 72.0 * nn

@@ -1,0 +1,200 @@
+/*
+ * diffmpm_gb300 -- C ABI of the GB300 (sm_103a) explicit MPM step.
+ *
+ * This library replaces the explicit time step of geoelements/diffmpm
+ * (diffmpm/solver.py, scheme.py, mesh.py, element.py, particle.py,
+ * material.py, constraint.py, forces.py, functions.py).  The reference has no
+ * foreign-function interface: its step is composed by string method dispatch
+ * (diffmpm/mesh.py:31-58) in the order of diffmpm/scheme.py:22-67.  Each entry
+ * point below names the reference interface it stands in for.
+ *
+ * Conventions
+ *   - Every function returns an MpmStatus (0 = success).  mpm_last_error()
+ *     gives a message for the last failure on a handle.
+ *   - Buffers are caller-owned.  `on_device` = 1 means the pointer is device
+ *     memory on the handle's GPU; 0 means host memory (the copy is done and
+ *     synchronised inside the call).  The handle owns all simulation state
+ *     and scratch (particle and nodal arrays, sort buffers, snapshots).
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default
+ *     stream).  Calls are stream-ordered; one handle per host thread.
+ *   - Particle arrays use the reference's layouts flattened row-major:
+ *     loc/velocity (n, ndim), stress/strain Voigt (n, 6) in the order
+ *     [xx, yy, zz, xy, yz, xz], scalars (n).  Reads return the original
+ *     particle order whatever the internal (cell-sorted) order is.
+ *   - Arithmetic is float32 throughout, as the reference's JAX default.
+ */
+#ifndef DIFFMPM_GB300_H
+#define DIFFMPM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MPM_ABI_VERSION 1
+
+typedef struct MpmHandle MpmHandle;
+
+typedef enum MpmStatus {
+    MPM_OK = 0,
+    MPM_ERR_INVALID = 1,      /* bad argument, shape or value (reference: ValueError/KeyError) */
+    MPM_ERR_CUDA = 2,         /* a CUDA runtime call failed */
+    MPM_ERR_OUT_OF_MESH = 3,  /* a particle left the mesh (reference: silent wrap/clamp ids) */
+    MPM_ERR_CFL = 4,          /* a particle crossed more than one cell in one step */
+    MPM_ERR_UNSUPPORTED = 5,  /* configuration this build does not implement */
+    MPM_ERR_STATE = 6,        /* call out of order (e.g. step before initialize) */
+    MPM_ERR_NOMEM = 7         /* device allocation failed */
+} MpmStatus;
+
+typedef enum MpmMaterialType {
+    MPM_LINEAR_ELASTIC = 0,   /* diffmpm/material.py:54-116 */
+    MPM_SIMPLE = 1,           /* diffmpm/material.py:119-131 */
+    MPM_NEWTONIAN = 2         /* build definition; no counterpart in the reference */
+} MpmMaterialType;
+
+typedef struct MpmMaterial {
+    int type;                 /* MpmMaterialType */
+    double density;
+    double youngs_modulus;    /* LinearElastic */
+    double poisson_ratio;     /* LinearElastic */
+    double E;                 /* SimpleMaterial */
+    double bulk_modulus;      /* Newtonian */
+    double dynamic_viscosity; /* Newtonian */
+} MpmMaterial;
+
+typedef enum MpmScheme { MPM_USF = 0, MPM_USL = 1 } MpmScheme;
+
+/* Simulation description: the arguments of Quadrilateral4Node / Linear1D
+ * (diffmpm/element.py:358-412, 626-690), MPMExplicit (diffmpm/solver.py:24-80),
+ * Constraint (diffmpm/constraint.py:7-20), NodalForce (diffmpm/forces.py:9-18),
+ * Linear/Unit (diffmpm/functions.py:16-49) and the material classes. */
+typedef struct MpmDesc {
+    int ndim;                      /* 2 = Quadrilateral4Node (1 reserved for Linear1D) */
+    int nelements[2];              /* nx, ny */
+    double el_len[2];              /* hx, hy (converted to float32 like jnp.asarray) */
+    int scheme;                    /* MpmScheme */
+    int velocity_update;           /* 0/1 (diffmpm/particle.py:235-245) */
+    int reinit_each_step;          /* 1: solve_jit semantics (volume/mass reset each step,
+                                      diffmpm/solver.py:81-85,100-111); 0: solve semantics */
+    double dt;
+    double gravity[2];
+    /* velocity constraints, flattened (node, dir, velocity), applied in order */
+    int n_constraints;
+    const int32_t* constraint_node;
+    const int32_t* constraint_dir;
+    const double* constraint_velocity;
+    /* piecewise-linear time functions; table k holds function_npoints[k] points */
+    int n_functions;
+    const int32_t* function_npoints;
+    const double* function_x;
+    const double* function_y;
+    /* concentrated nodal forces, flattened (node, dir, force, function); function
+       -1 = Unit, k >= 0 = table k.  Applied in list order. */
+    int n_nodal_forces;
+    const int32_t* nodal_force_node;
+    const int32_t* nodal_force_dir;
+    const double* nodal_force_value;
+    const int32_t* nodal_force_function;
+    int n_materials;
+    const MpmMaterial* materials;
+} MpmDesc;
+
+/* Particle fields (mpm_write_field / mpm_read_field). */
+typedef enum MpmField {
+    MPM_FIELD_LOC = 0,            /* float (n, ndim) */
+    MPM_FIELD_VELOCITY = 1,       /* float (n, ndim) */
+    MPM_FIELD_STRESS = 2,         /* float (n, 6) */
+    MPM_FIELD_STRAIN = 3,         /* float (n, 6) */
+    MPM_FIELD_DENSITY = 4,        /* float (n) */
+    MPM_FIELD_VOLUME = 5,         /* float (n) */
+    MPM_FIELD_MASS = 6,           /* float (n) */
+    MPM_FIELD_VSC = 7,            /* float (n) volumetric_strain_centroid */
+    MPM_FIELD_MATERIAL_ID = 8,    /* int32 (n) */
+    MPM_FIELD_YOUNGS_MODULUS = 9, /* float (n) per-particle E (LinearElastic), write enables it */
+    MPM_FIELD_ELEMENT_ID = 10,    /* int32 (n), read only */
+    MPM_FIELD_MOMENTUM = 11       /* float (n, ndim), read only: mass * velocity */
+} MpmField;
+
+/* Nodal fields (mpm_read_nodal_field / mpm_write_nodal_field). */
+typedef enum MpmNodalField {
+    MPM_NODE_MASS = 0,            /* float (Nn) */
+    MPM_NODE_VELOCITY = 1,        /* float (Nn, ndim) */
+    MPM_NODE_ACCELERATION = 2,    /* float (Nn, ndim) */
+    MPM_NODE_MOMENTUM = 3         /* float (Nn, ndim), read only: mass * velocity */
+} MpmNodalField;
+
+/* Phases for mpm_run_phase (test and debugging entry). */
+typedef enum MpmPhase {
+    MPM_PHASE_NODAL_KINEMATICS = 0, /* scheme.py:22-29 (+ the step's volume reset) */
+    MPM_PHASE_FORCES = 1,           /* USF: scheme.py:31-56 + element.py:305-329; USL: scheme.py:37-56 + element.py:305-329 */
+    MPM_PHASE_PARTICLE_KINEMATICS = 2 /* particle.py:208-247 (USL: + scheme.py:31-35) */
+} MpmPhase;
+
+/* Library ABI version (MPM_ABI_VERSION). */
+int mpm_abi_version(void);
+
+/* Create a simulation on the current CUDA device.
+ * Replaces Quadrilateral4Node.__init__ (diffmpm/element.py:626-690) and the
+ * configuration part of MPMExplicit.__init__ (diffmpm/solver.py:24-80). */
+int mpm_create(const MpmDesc* desc, MpmHandle** out);
+
+/* Free every device buffer of the handle. */
+int mpm_destroy(MpmHandle* h);
+
+/* Message of the last failure on `h` (or of the last failed mpm_create when h is NULL). */
+const char* mpm_last_error(const MpmHandle* h);
+
+/* Set the particle population: `n` particles at `loc` (n, ndim) with material
+ * ids (NULL = all 0).  Every other field takes the reference's initial value
+ * (diffmpm/particle.py:53-71: zero velocity/stress/strain, density from the
+ * material).  Replaces Particles.__init__ (diffmpm/particle.py:16-91). */
+int mpm_set_particles(MpmHandle* h, int64_t n, const float* loc, const int32_t* material_id,
+                      int on_device, void* stream);
+
+/* Overwrite one particle field (original particle order). */
+int mpm_write_field(MpmHandle* h, int field, const void* src, int on_device, void* stream);
+
+/* Read one particle field in original particle order.  Replaces the output
+ * assembly of MPMExplicit.solve_jit (diffmpm/solver.py:214-222). */
+int mpm_read_field(MpmHandle* h, int field, void* dst, int on_device, void* stream);
+
+/* Particle tractions (diffmpm/forces.py:26-41, mesh.py:60-77): `n` entries
+ * (particle id, dir, traction, function: -1 Unit, k table k).  Replaces any
+ * previous list. */
+int mpm_set_tractions(MpmHandle* h, int n, const int64_t* pid, const int32_t* dir,
+                      const double* traction, const int32_t* function, void* stream);
+
+/* Nodal state access (diffmpm/node.py:64-71). */
+int mpm_read_nodal_field(MpmHandle* h, int field, float* dst, int on_device, void* stream);
+int mpm_write_nodal_field(MpmHandle* h, int field, const float* src, int on_device, void* stream);
+
+/* Sort particles by cell and run the volume set-up: element ids, element
+ * volume, particle volume/size/mass (diffmpm/solver.py:81-85).  Must follow
+ * mpm_set_particles before the first step. */
+int mpm_initialize(MpmHandle* h, void* stream);
+
+/* Advance `nsteps` explicit steps.  Replaces the body of solve_jit's
+ * lax.fori_loop (diffmpm/solver.py:179-213) or of solve's loop
+ * (diffmpm/solver.py:144-149), per desc.reinit_each_step. */
+int mpm_step(MpmHandle* h, int nsteps, void* stream);
+
+/* Step counter i (t = i * dt in the time functions, diffmpm/scheme.py:52-54). */
+int mpm_get_step(const MpmHandle* h, int64_t* step);
+int mpm_set_step(MpmHandle* h, int64_t step);
+
+/* Run one phase of one step (for tests).  Steps that use this must run the
+ * three phases in order. */
+int mpm_run_phase(MpmHandle* h, int phase, void* stream);
+
+/* Steps per captured CUDA graph (default 100). */
+int mpm_set_block_steps(MpmHandle* h, int steps);
+
+/* Number of particle re-sorts and rolled-back step blocks so far. */
+int mpm_get_counters(const MpmHandle* h, int64_t* resorts, int64_t* rollbacks);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DIFFMPM_GB300_H */

@@ -1,3 +1,4 @@
+import ctypes
 import sys
 from pathlib import Path
 
@@ -13,3 +14,30 @@ if str(TESTS) not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+def _have_gpu() -> bool:
+    try:
+        cuda = ctypes.CDLL("libcuda.so.1")
+    except OSError:
+        return False
+    if cuda.cuInit(0) != 0:
+        return False
+    n = ctypes.c_int(0)
+    return cuda.cuDeviceGetCount(ctypes.byref(n)) == 0 and n.value > 0
+
+
+def pytest_collection_modifyitems(config, items):
+    gpu_items = [it for it in items if it.get_closest_marker("gpu")]
+    if gpu_items and not _have_gpu():
+        skip = pytest.mark.skip(reason="no CUDA GPU on this machine")
+        for it in gpu_items:
+            it.add_marker(skip)
+
+
+@pytest.fixture(scope="session")
+def built():
+    """Build (if stale) and load the CUDA library."""
+    import __graft_entry__
+    __graft_entry__.build()
+    return True

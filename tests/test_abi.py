@@ -1,0 +1,89 @@
+"""The C ABI library: builds for sm_103a, loads, and exports every entry point
+that include/diffmpm_gb300.h declares (no GPU needed)."""
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+HEADER = ROOT / "include" / "diffmpm_gb300.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(mpm_\w+)\s*\(", text, re.M)))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    assert "mpm_create" in names and "mpm_step" in names and len(names) >= 15
+
+
+def test_library_exports_every_declared_symbol(built):
+    from diffmpm_gb300 import _lib
+    lib = _lib.load()
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+    bound = {name for name, _, _ in _lib.SIGNATURES}
+    assert set(declared_functions()) == bound
+
+
+def test_abi_version(built):
+    from diffmpm_gb300 import _lib
+    assert _lib.load().mpm_abi_version() == 1
+
+
+def test_create_rejects_bad_scheme_without_gpu(built):
+    # argument validation happens before any device call
+    from diffmpm_gb300 import _lib
+    lib = _lib.load()
+    d = _lib.MpmDesc()
+    d.ndim = 2
+    d.nelements[0] = d.nelements[1] = 2
+    d.el_len[0] = d.el_len[1] = 0.5
+    d.scheme = 7
+    h = ctypes.c_void_p()
+    rc = lib.mpm_create(ctypes.byref(d), ctypes.byref(h))
+    assert rc == 1
+    assert b"scheme" in lib.mpm_last_error(None)
+
+
+def test_create_rejects_linear1d_as_unsupported(built):
+    from diffmpm_gb300 import _lib
+    lib = _lib.load()
+    d = _lib.MpmDesc()
+    d.ndim = 1
+    h = ctypes.c_void_p()
+    assert lib.mpm_create(ctypes.byref(d), ctypes.byref(h)) == 5
+
+
+def test_library_is_sm103a(built):
+    from diffmpm_gb300 import _lib
+    data = _lib.LIB_PATH.read_bytes()
+    assert b"sm_103a" in data
+
+
+def test_python_api_mirrors_reference_names():
+    import diffmpm_gb300 as D
+    for name in ("Mesh2D", "Particles", "Quadrilateral4Node", "MPMExplicit", "LinearElastic",
+                 "SimpleMaterial", "Newtonian", "Constraint", "NodalForce", "ParticleTraction",
+                 "Unit", "Linear", "Linear1D", "Mesh1D"):
+        assert hasattr(D, name)
+
+
+def test_invalid_scheme_raises_value_error():
+    import numpy as np
+    import diffmpm_gb300 as D
+    mat = D.LinearElastic({"density": 1, "youngs_modulus": 1, "poisson_ratio": 0})
+    el = D.Quadrilateral4Node((1, 1), 1, (1.0, 1.0), [])
+    ps = D.Particles(np.full((1, 1, 2), 0.5), mat, np.zeros(1))
+    mesh = D.Mesh2D({"particles": [ps], "elements": el})
+    with pytest.raises(ValueError):
+        D.MPMExplicit(mesh, 0.1, scheme="abc")
+
+
+def test_missing_material_property_raises_key_error():
+    import diffmpm_gb300 as D
+    with pytest.raises(KeyError):
+        D.LinearElastic({"density": 1, "youngs_modulus": 1})
