@@ -228,26 +228,20 @@ def run_ours(args, world, rank, local):
     value = world * np_ * args.steps / (ms / 1000.0)
     counters = sim.counters()
 
-    # per-phase kernel time (CUDA events on the launching stream)
-    names = ["nodal_kinematics", "forces", "particle_kinematics"]
-    acc = {k: 0.0 for k in names}
-    for _ in range(args.phase_steps):
-        for k in names:
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            sim.run_phase(k)
-            b.record(stream)
-            torch.cuda.synchronize()
-            acc[k] += a.elapsed_time(b)
-    avg = {k: acc[k] / args.phase_steps for k in names}
+    # per-phase kernel time: CUDA events recorded between back-to-back launches
+    # of the phase kernels on the launching stream
+    tot = sim.time_phases(args.phase_steps)
+    avg = {k: v / args.phase_steps for k, v in tot.items()}
     top = max(avg, key=avg.get)
     pb = phase_bytes(np_, nn, args.scheme)
     peak, peak_kind = measured_peak()
     achieved = pb[top] / (avg[top] / 1000.0) / 1e9
-    traffic = None
-    tf = ROOT / "profiles" / f"traffic_{top}_plain_scaleup_{args.scheme}.json"
+    traffic = None   # DRAM bytes of one launch from the committed ncu summary
+    tf = ROOT / "profiles" / f"k_{top}_plain_scaleup_{args.scheme}.md"
     if tf.exists():
-        traffic = json.loads(tf.read_text()).get("bytes_per_launch")
+        for line in tf.read_text().splitlines():
+            if line.startswith("dram bytes per launch:"):
+                traffic = int(line.split(":")[1])
 
     # end to end through the public API with host buffers: upload, set-up,
     # K steps, read back loc/velocity/stress/strain (solve_jit's outputs)

@@ -83,6 +83,7 @@ SIGNATURES = [
     ("mpm_get_step", C.c_int, [_VP, C.POINTER(C.c_int64)]),
     ("mpm_set_step", C.c_int, [_VP, C.c_int64]),
     ("mpm_run_phase", C.c_int, [_VP, C.c_int, _VP]),
+    ("mpm_time_phases", C.c_int, [_VP, C.c_int, _VP, _VP]),
     ("mpm_set_block_steps", C.c_int, [_VP, C.c_int]),
     ("mpm_get_counters", C.c_int, [_VP, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
 ]

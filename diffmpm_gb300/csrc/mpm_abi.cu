@@ -166,7 +166,13 @@ float element_volume(float hx, float hy) {
     return 0.25f * std::sqrt(x);
 }
 
+void drop_graphs(MpmHandle* h) {
+    for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+    h->graphs.clear();
+}
+
 int upload_desc(MpmHandle* h) {
+    drop_graphs(h);
     CK(h, cudaMemcpy(h->ds, &h->hs, sizeof(SimDev), cudaMemcpyHostToDevice));
     return MPM_OK;
 }
@@ -269,6 +275,7 @@ int resort(MpmHandle* h, cudaStream_t s) {
     h->cs_cur ^= 1;
     CK(h, cudaMemsetAsync(h->cflag, 0, h->ncell, s));
     bind_particles(h);
+    drop_graphs(h);   // the step graphs hold the descriptor by value
     CK(h, cudaMemcpyAsync(h->ds, &h->hs, sizeof(SimDev), cudaMemcpyHostToDevice, s));
     h->needs_resort = false;
     h->resorts++;
@@ -312,9 +319,9 @@ StepConfig step_config(const MpmHandle* h) {
 int launch_phase(MpmHandle* h, int phase, cudaStream_t s) {
     const StepConfig c = step_config(h);
     cudaError_t e = cudaSuccess;
-    if (phase == 0) e = launch_nodal_kinematics(c, h->ds, h->dtiles, h->ntiles, h->ctl, s);
-    else if (phase == 1) e = launch_forces(c, h->ds, h->dtiles, h->ntiles, h->ctl, s);
-    else e = launch_particle_kinematics(c, h->ds, h->dtiles, h->ntiles, h->ctl, s);
+    if (phase == 0) e = launch_nodal_kinematics(c, h->hs, h->dtiles, h->ntiles, h->ctl, s);
+    else if (phase == 1) e = launch_forces(c, h->hs, h->dtiles, h->ntiles, h->ctl, s);
+    else e = launch_particle_kinematics(c, h->hs, h->dtiles, h->ntiles, h->ctl, s);
     CK(h, e);
     return MPM_OK;
 }
@@ -325,10 +332,7 @@ int launch_steps(MpmHandle* h, int n, cudaStream_t s) {
     return MPM_OK;
 }
 
-void drop_graphs(MpmHandle* h) {
-    for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
-    h->graphs.clear();
-}
+
 
 int run_graph(MpmHandle* h, int n, cudaStream_t s) {
     if (h->graphs_trac != h->has_trac) {
@@ -928,6 +932,7 @@ int mpm_set_tractions(MpmHandle* h, int n, const int64_t* pid, const int32_t* di
     CK(h, launch_gather_pair_u8(reinterpret_cast<const uint8_t*>(st8), reinterpret_cast<uint8_t*>(p.tr_fn), p.pid, (int)np, s));
     h->has_trac = true;
     bind_particles(h);
+    drop_graphs(h);
     CK(h, cudaMemcpyAsync(h->ds, &h->hs, sizeof(SimDev), cudaMemcpyHostToDevice, s));
     return sync(h, s);
 }
@@ -1070,6 +1075,40 @@ int mpm_set_step(MpmHandle* h, int64_t step) {
     h->step = step;
     h->h_ctl->step = (int)step;
     CK(h, cudaMemcpy(&h->ctl->step, &h->h_ctl->step, sizeof(int), cudaMemcpyHostToDevice));
+    return MPM_OK;
+}
+
+int mpm_time_phases(MpmHandle* h, int nsteps, float* ms_out, void* stream) {
+    if (!h || !ms_out || nsteps < 1) return MPM_ERR_INVALID;
+    if (!h->initialized) return fail(h, MPM_ERR_STATE, "initialize first");
+    cudaStream_t s = S(stream);
+    if (h->needs_resort) TRY(resort(h, s));
+    std::vector<cudaEvent_t> ev((size_t)3 * nsteps + 1);
+    for (auto& e : ev) CK(h, cudaEventCreate(&e));
+    int r = MPM_OK;
+    CK(h, cudaEventRecord(ev[0], s));
+    for (int i = 0; i < nsteps && r == MPM_OK; ++i)
+        for (int p = 0; p < 3 && r == MPM_OK; ++p) {
+            r = launch_phase(h, p, s);
+            if (r == MPM_OK) CK(h, cudaEventRecord(ev[3 * i + p + 1], s));
+        }
+    CK(h, cudaStreamSynchronize(s));
+    for (int p = 0; p < 3; ++p) ms_out[p] = 0.0f;
+    if (r == MPM_OK)
+        for (int i = 0; i < nsteps; ++i)
+            for (int p = 0; p < 3; ++p) {
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, ev[3 * i + p], ev[3 * i + p + 1]);
+                ms_out[p] += ms;
+            }
+    for (auto& e : ev) cudaEventDestroy(e);
+    TRY(r);
+    h->step += nsteps;
+    TRY(read_ctl(h, s));
+    int st = 0;
+    TRY(check_status(h, st));
+    h->needs_resort = (st & (ST_DRIFTED | ST_DRIFT_VIOLATION)) != 0;
+    TRY(clear_status(h, s));
     return MPM_OK;
 }
 

@@ -89,63 +89,317 @@ __device__ __forceinline__ void apply_constraint(const SimDev& S, uint16_t code,
 }
 
 // ---------------------------------------------------------------------------
+// Tile streaming.
+//
+// Fast path (no drift flag set on the 34 x 18 sort-cells around the tile, so
+// every particle of the tile is in its sort-cell): warp w streams the
+// contiguous storage range of cell row w, one particle per lane (coalesced
+// loads and stores).  A particle's cell is found from its storage index by a
+// binary search of the row's cell starts, and the cell geometry comes from
+// per-tile tables, so no division or locate runs per particle.  The particle's
+// NQ corner contributions go to shared-memory slots; lane l then adds, in
+// storage order, the slots of the particles of its own cell (c0x + l, row w)
+// to that cell's partials.
+// Slow path (some neighbouring particle drifted): each thread visits the
+// particles currently in its cell with visit_cell.  Both paths use the same
+// per-particle function and the same per-cell values and add in the same order
+// (storage order within the cell), so on an undrifted tile they give bitwise
+// the same partials.
+// ---------------------------------------------------------------------------
+constexpr int HALO_W = TILE_CX + 2;   // sort-cells checked for drift: [c0x-1, c0x+33)
+constexpr int HALO_H = TILE_CY + 2;   //                               [c0y-1, c0y+17)
+constexpr int GEO_C = TILE_CX + 3;    // geometry table columns k <-> cell c0x - 1 + k
+constexpr int GEO_R = TILE_CY + 3;    // geometry table rows    k <-> cell c0y - 1 + k
+
+// Per-tile cell geometry: bounds, centre and 2/width of columns and rows, formed
+// exactly as cell_geo forms them.
+struct TileGeo {
+    float x0[GEO_C], x1[GEO_C], cx[GEO_C], rx[GEO_C];
+    float y0[GEO_R], y1[GEO_R], cy[GEO_R], ry[GEO_R];
+};
+
+__device__ __forceinline__ void build_geo(const SimDev& S, int c0x, int c0y, TileGeo& G) {
+    const int t = threadIdx.x;
+    if (t < GEO_C) {
+        const int i = c0x - 1 + t;
+        const float a = node_coord(i, S.hx), b = node_coord(i + 1, S.hx);
+        G.x0[t] = a;
+        G.x1[t] = b;
+        G.cx[t] = fm(fa(a, b), 0.5f);
+        G.rx[t] = fdv(2.0f, fs(b, a));
+    } else if (t >= 64 && t < 64 + GEO_R) {
+        const int k = t - 64, j = c0y - 1 + k;
+        const float a = node_coord(j, S.hy), b = node_coord(j + 1, S.hy);
+        G.y0[k] = a;
+        G.y1[k] = b;
+        G.cy[k] = fm(fa(a, b), 0.5f);
+        G.ry[k] = fdv(2.0f, fs(b, a));
+    }
+}
+
+__device__ __forceinline__ CellGeo geo_of(const TileGeo& G, int kc, int kr) {
+    CellGeo g;
+    g.x0 = G.x0[kc];
+    g.x1 = G.x1[kc];
+    g.cx = G.cx[kc];
+    g.rx = G.rx[kc];
+    g.y0 = G.y0[kr];
+    g.y1 = G.y1[kr];
+    g.cy = G.cy[kr];
+    g.ry = G.ry[kr];
+    return g;
+}
+
+// Load the 33 cell starts of row cj for cells c0x .. c0x+32 (clamped to the
+// mesh so that cells outside it have empty ranges) into cs[0..32].
+__device__ __forceinline__ void load_row_starts(const SimDev& S, int c0x, int cj, int* cs,
+                                                int lane) {
+    if (cj < 0 || cj >= S.ny) {
+        cs[lane] = 0;
+        if (lane == 0) cs[32] = 0;
+        return;
+    }
+    const int base = cj * S.nx;
+    const int col = min(max(c0x + lane, 0), S.nx);
+    cs[lane] = S.cstart[base + col];
+    if (lane == 0) cs[32] = S.cstart[base + min(max(c0x + 32, 0), S.nx)];
+}
+
+// The cell l in [0, last] whose range [cs[l], cs[l+1]) holds storage index q
+// (the last l with cs[l] <= q; q lies in [cs[0], cs[last+1])).
+__device__ __forceinline__ int cell_of(const int* cs, int last, int q) {
+    int lo = 0, hi = last;
+    #pragma unroll 1
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (cs[mid] <= q) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// True when any sort-cell around the tile has its drift flag set.
+__device__ __forceinline__ bool tile_drifted(const SimDev& S, int c0x, int c0y) {
+    int any = 0;
+    for (int idx = threadIdx.x; idx < HALO_W * HALO_H; idx += TILE_THREADS) {
+        const int si = c0x - 1 + idx % HALO_W, sj = c0y - 1 + idx / HALO_W;
+        if (si >= 0 && si < S.nx && sj >= 0 && sj < S.ny) any |= S.cflag[sj * S.nx + si];
+    }
+    return __syncthreads_or(any) != 0;
+}
+
+// Per-particle contributions of phase 1 to the 4 corners of its cell:
+// [m N_k, N_k (m vx), N_k (m vy)] (element.py:138-152, 170-189).
+template <bool REINIT>
+__device__ __forceinline__ void mass_contrib(const SimDev& S, int q, const CellGeo& g, float V0,
+                                             const float* __restrict__ rho, float* c) {
+    const float mp = REINIT ? fm(V0, rho[q]) : S.mass[q];
+    const float xi = natural(S.x[q], g.cx, g.rx);
+    const float eta = natural(S.y[q], g.cy, g.ry);
+    float N[4];
+    shape4(xi, eta, N);
+    const float pvx = fm(mp, S.vx[q]), pvy = fm(mp, S.vy[q]);
+    #pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        c[k] = fm(mp, N[k]);
+        c[4 + k] = fm(N[k], pvx);
+        c[8 + k] = fm(N[k], pvy);
+    }
+}
+
+// Particle traction t_p[d] = f(t) tau_d V / size (diffmpm/mesh.py:60-77,
+// particle.py:329-343), added to the external-force contributions.
+template <bool TRAC>
+__device__ __forceinline__ void add_traction(const SimDev& S, int q, float t, float V, float size,
+                                             const float N[4], float* cex, float* cey) {
+    if constexpr (TRAC) {
+        #pragma unroll
+        for (int d = 0; d < 2; ++d) {
+            const int code = S.tr_fn[2 * q + d];
+            if (!code) continue;
+            const float tv = fm(fn_value(S, code, t), S.tr_tau[2 * q + d]);
+            const float tr = fdv(fm(tv, V), size);
+            #pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (d == 0) cex[k] = fa(cex[k], fm(N[k], tr));
+                else cey[k] = fa(cey[k], fm(N[k], tr));
+            }
+        }
+    }
+}
+
+// Per-cell values of phase 2: the volume set-up V0 = V_el / count and
+// size0 = sqrt(V0) (particle.py:169-178), and (USF) dt times the centroid
+// volumetric strain rate from the cell's nodal velocities (particle.py:270-279).
+template <bool USL, bool REINIT>
+__device__ __forceinline__ void force_cell_values(const SimDev& S, int cnt, const CellGeo& g,
+                                                  const float nvx[4], const float nvy[4],
+                                                  float& V0, float& size0, float& dvol) {
+    V0 = 0.0f;
+    size0 = 1.0f;
+    if (REINIT) {
+        if (cnt) V0 = fdv(S.vol_el, (float)cnt);
+        size0 = sqrtf(V0);
+    }
+    dvol = 0.0f;
+    if (!USL) {
+        float Gcx[4], Gcy[4], c0, c1, c3;
+        dshape4(0.0f, 0.0f, g.rx, g.ry, Gcx, Gcy);
+        strain_rate4(Gcx, Gcy, nvx, nvy, c0, c1, c3);
+        dvol = fm(S.dt, fa(c0, c1));
+    }
+}
+
+// Per-particle work of phase 2: USF strain/volume/stress update (written back
+// when `write`) and the contributions [fint x, fint y, fext x, fext y] x 4
+// corners (element.py:236-303, 842-901).
+template <bool USL, bool REINIT, bool TRAC>
+__device__ __forceinline__ void force_contrib(const SimDev& S, int q, const CellGeo& g, float V0,
+                                              float size0, const float nvx[4], const float nvy[4],
+                                              float dvol, int parity, float t, bool write,
+                                              float* c) {
+    const int next = parity ^ 1;
+    const float xi = natural(S.x[q], g.cx, g.rx);
+    const float eta = natural(S.y[q], g.cy, g.ry);
+    float N[4], Gx[4], Gy[4];
+    shape4(xi, eta, N);
+    dshape4(xi, eta, g.rx, g.ry, Gx, Gy);
+    PState p;
+    p.sxx = S.sxx[parity][q];
+    p.syy = S.syy[parity][q];
+    p.szz = S.szz[parity][q];
+    p.sxy = S.sxy[parity][q];
+    p.rho = S.rho[parity][q];
+    const float mp = REINIT ? fm(V0, p.rho) : S.mass[q];
+    float V = REINIT ? V0 : S.vol[parity][q];
+    if (!USL) {
+        float r0, r1, r3;
+        strain_rate4(Gx, Gy, nvx, nvy, r0, r1, r3);
+        p.exx = S.exx[q];
+        p.eyy = S.eyy[q];
+        p.exy = S.exy[q];
+        p.vsc = S.vsc[parity][q];
+        const MatDev& M = S.mats[S.mat[q]];
+        const float Ep = S.E ? S.E[q] : -1.0f;
+        V = fm(V, strain_stress_update(M, Ep, S.dt, r0, r1, r3, dvol, p));
+        if (write) {
+            S.sxx[next][q] = p.sxx;
+            S.syy[next][q] = p.syy;
+            S.szz[next][q] = p.szz;
+            S.sxy[next][q] = p.sxy;
+            S.exx[q] = p.exx;
+            S.eyy[q] = p.eyy;
+            S.exy[q] = p.exy;
+            S.rho[next][q] = p.rho;
+            S.vsc[next][q] = p.vsc;
+            if (!REINIT) S.vol[next][q] = V;
+        }
+    }
+    const float nV = -V;
+    const float mgx = fm(mp, S.gx), mgy = fm(mp, S.gy);
+    #pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float fx = fa(fm(Gx[k], p.sxx), fm(Gy[k], p.sxy));
+        const float fy = fa(fm(Gy[k], p.syy), fm(Gx[k], p.sxy));
+        c[k] = fm(nV, fx);
+        c[4 + k] = fm(nV, fy);
+        c[8 + k] = fm(N[k], mgx);
+        c[12 + k] = fm(N[k], mgy);
+    }
+    add_traction<TRAC>(S, q, t, V, REINIT ? size0 : (S.psize ? S.psize[q] : 1.0f), N, c + 8, c + 12);
+}
+
+// Fast-path accumulation of one chunk: lane `lx` adds, in storage order, the
+// slots of its cell's particles that lie in [base, base + 32) to s_c[.][tid].
+template <int NQ>
+__device__ __forceinline__ void add_chunk(float (*s_c)[TILE_THREADS], const float (*slot)[32],
+                                          int tid, int cb, int ce, int base) {
+    const int lo = max(cb, base), hi = min(ce, base + 32);
+    if (lo >= hi) return;
+    float acc[NQ];
+    #pragma unroll
+    for (int k = 0; k < NQ; ++k) acc[k] = s_c[k][tid];
+    #pragma unroll 1
+    for (int qq = lo; qq < hi; ++qq) {
+        #pragma unroll
+        for (int k = 0; k < NQ; ++k) acc[k] = fa(acc[k], slot[k][qq - base]);
+    }
+    #pragma unroll
+    for (int k = 0; k < NQ; ++k) s_c[k][tid] = acc[k];
+}
+
+// ---------------------------------------------------------------------------
 // Phase 1: nodal kinematics (diffmpm/scheme.py:22-29) with the step's volume
 // set-up (diffmpm/solver.py:81-85 via tree_unflatten, solver.py:100-111).
 //   P2G of mass and momentum (element.py:122-189), nodal velocity
 //   (element.py:191-202), velocity constraints (element.py:331-334).
 // ---------------------------------------------------------------------------
 template <bool REINIT>
-__global__ void __launch_bounds__(TILE_THREADS)
-k_nodal_kinematics(const SimDev* __restrict__ sims, const int4* __restrict__ tiles,
+__global__ void __launch_bounds__(TILE_THREADS, 2)
+k_nodal_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
                    Control* __restrict__ ctl) {
-    __shared__ float s_m[4][TILE_THREADS];
-    __shared__ float s_px[4][TILE_THREADS];
-    __shared__ float s_py[4][TILE_THREADS];
+    constexpr int NQ = 12;
+    __shared__ float s_c[NQ][TILE_THREADS];            // [m, px, py] x corner, per cell
+    __shared__ float s_slot[TILE_CY][NQ][32];          // per-warp particle contributions
+    __shared__ int s_cs[TILE_CY][33];
+    __shared__ float s_V0[TILE_CY][32];
+    __shared__ TileGeo G;
     const int4 T = tiles[blockIdx.x];
-    const SimDev& S = sims[T.x];
     const int parity = load_step(ctl) & 1;
     const int tid = threadIdx.x, lx = tid & (TILE_CX - 1), ly = tid / TILE_CX;
     const int c0x = T.y * TILE_NX - 1, c0y = T.z * TILE_NY - 1;
     const int ci = c0x + lx, cj = c0y + ly;
+    const float* __restrict__ rho = S.rho[parity];
+    #pragma unroll
+    for (int k = 0; k < NQ; ++k) s_c[k][tid] = 0.0f;
+    load_row_starts(S, c0x, cj, s_cs[ly], lx);
+    build_geo(S, c0x, c0y, G);
+    const bool slow = tile_drifted(S, c0x, c0y);   // (also a block barrier)
 
-    float m[4] = {0.f, 0.f, 0.f, 0.f}, px[4] = {0.f, 0.f, 0.f, 0.f}, py[4] = {0.f, 0.f, 0.f, 0.f};
-    if (ci >= 0 && ci < S.nx && cj >= 0 && cj < S.ny) {
-        const CellGeo g = cell_geo(ci, cj, S.hx, S.hy);
-        const float* __restrict__ rho = S.rho[parity];
+    if (!slow) {
+        const int* cs = s_cs[ly];
+        const int rb = cs[0], re = cs[32];
+        const int cb = cs[lx], ce = cs[lx + 1];
+        if (REINIT) s_V0[ly][lx] = ce > cb ? fdv(S.vol_el, (float)(ce - cb)) : 0.0f;
+        __syncwarp();
+        const int kr = ly + 1;
+        #pragma unroll 1
+        for (int base = rb; base < re; base += 32) {
+            const int q = base + lx;
+            if (q < re) {
+                const int l = cell_of(cs, 31, q);
+                const CellGeo g = geo_of(G, l + 1, kr);
+                float c[NQ];
+                mass_contrib<REINIT>(S, q, g, REINIT ? s_V0[ly][l] : 0.0f, rho, c);
+                #pragma unroll
+                for (int k = 0; k < NQ; ++k) s_slot[ly][k][lx] = c[k];
+            }
+            __syncwarp();
+            add_chunk<NQ>(s_c, s_slot[ly], tid, cb, ce, base);
+            __syncwarp();
+        }
+    } else if (ci >= 0 && ci < S.nx && cj >= 0 && cj < S.ny) {
+        const CellGeo g = geo_of(G, lx + 1, ly + 1);
         float V0 = 0.0f;
         if (REINIT) {
             const int cnt = count_cell(S, ci, cj, g);
-            if (cnt) V0 = fdv(S.vol_el, (float)cnt);   // particle.py:169-178
+            if (cnt) V0 = fdv(S.vol_el, (float)cnt);
         }
         visit_cell(S, ci, cj, g, [&](int q) {
-            const float mp = REINIT ? fm(V0, rho[q]) : S.mass[q];
-            const float xi = natural(S.x[q], g.cx, g.rx);
-            const float eta = natural(S.y[q], g.cy, g.ry);
-            float N[4];
-            shape4(xi, eta, N);
-            const float pvx = fm(mp, S.vx[q]), pvy = fm(mp, S.vy[q]);
+            float c[NQ];
+            mass_contrib<REINIT>(S, q, g, V0, rho, c);
             #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                m[k] = fa(m[k], fm(mp, N[k]));
-                px[k] = fa(px[k], fm(N[k], pvx));
-                py[k] = fa(py[k], fm(N[k], pvy));
-            }
+            for (int k = 0; k < NQ; ++k) s_c[k][tid] = fa(s_c[k][tid], c[k]);
         });
-    }
-    #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        s_m[k][tid] = m[k];
-        s_px[k][tid] = px[k];
-        s_py[k][tid] = py[k];
     }
     __syncthreads();
     if (lx < TILE_NX && ly < TILE_NY) {
         const int I = c0x + 1 + lx, J = c0y + 1 + ly;
         if (I <= S.nx && J <= S.ny) {
             const int n = J * (S.nx + 1) + I;
-            const float mass = node_sum(s_m, tid);
-            const float pxn = flush(node_sum(s_px, tid));
-            const float pyn = flush(node_sum(s_py, tid));
+            const float mass = node_sum(s_c + 0, tid);
+            const float pxn = flush(node_sum(s_c + 4, tid));
+            const float pyn = flush(node_sum(s_c + 8, tid));
             float vx, vy;
             if (mass == 0.0f) {
                 vx = S.nvbx[n];
@@ -164,31 +418,10 @@ k_nodal_kinematics(const SimDev* __restrict__ sims, const int4* __restrict__ til
     }
 }
 
-// Particle traction t_p[d] = f(t) tau_d V / size (diffmpm/mesh.py:60-77,
-// particle.py:329-343), accumulated into the body-force partials.
-template <bool TRAC>
-__device__ __forceinline__ void add_traction(const SimDev& S, int q, float t, float V, float size,
-                                             const float N[4], float fex[4], float fey[4]) {
-    if constexpr (TRAC) {
-    #pragma unroll
-    for (int d = 0; d < 2; ++d) {
-        const int code = S.tr_fn[2 * q + d];
-        if (!code) continue;
-        const float tv = fm(fn_value(S, code, t), S.tr_tau[2 * q + d]);
-        const float tr = fdv(fm(tv, V), size);
-        #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            if (d == 0) fex[k] = fa(fex[k], fm(N[k], tr));
-            else fey[k] = fa(fey[k], fm(N[k], tr));
-        }
-    }
-    }
-}
-
 // Nodal update shared by both schemes: concentrated forces (element.py:270-284),
 // a = nan_to_num(f/m), v += a dt, constraints, flush (element.py:305-329).
 __device__ __forceinline__ void nodal_update(const SimDev& S, int n, float t, float fix, float fiy,
-                                             float fex, float fey) {
+                                             float fex, float fey, float v0x, float v0y) {
     if (S.cnf_ptr) {
         const int b = S.cnf_ptr[n], e = S.cnf_ptr[n + 1];
         #pragma unroll 1
@@ -203,8 +436,8 @@ __device__ __forceinline__ void nodal_update(const SimDev& S, int n, float t, fl
     const float mass = S.nm[n];
     float ax = nan_to_num(fdv(tx, mass));
     float ay = nan_to_num(fdv(ty, mass));
-    float vx = fa(S.nvax[n], fm(ax, S.dt));
-    float vy = fa(S.nvay[n], fm(ay, S.dt));
+    float vx = fa(v0x, fm(ax, S.dt));
+    float vy = fa(v0y, fm(ay, S.dt));
     apply_constraint(S, S.ncons[n], vx, vy, &ax, &ay);
     S.nvbx[n] = flush(vx);
     S.nvby[n] = flush(vy);
@@ -220,122 +453,109 @@ __device__ __forceinline__ void nodal_update(const SimDev& S, int n, float t, fl
 // Phase 2 (USL): forces and nodal update only; the stress update runs after
 // G2P (scheme.py:127-133).
 // ---------------------------------------------------------------------------
+constexpr int NV_W = TILE_CX + 1;   // node tile of the R cells: [c0x, c0x+33) x [c0y, c0y+17)
+constexpr int NV_H = TILE_CY + 1;
+
 template <bool USL, bool REINIT, bool TRAC>
-__global__ void __launch_bounds__(TILE_THREADS)
-k_forces(const SimDev* __restrict__ sims, const int4* __restrict__ tiles,
+__global__ void __launch_bounds__(TILE_THREADS, 2)
+k_forces(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
          Control* __restrict__ ctl) {
-    __shared__ float s_f[4][4][TILE_THREADS];   // [fint x, fint y, fext x, fext y][corner][cell]
+    constexpr int NQ = 16;
+    __shared__ float s_c[NQ][TILE_THREADS];            // [fint x, fint y, fext x, fext y] x corner
+    __shared__ float s_slot[TILE_CY][NQ][32];
+    __shared__ int s_cs[TILE_CY][33];
+    __shared__ float s_V0[TILE_CY][32], s_size0[TILE_CY][32], s_dvol[TILE_CY][32];
+    __shared__ float s_vx[NV_W * NV_H], s_vy[NV_W * NV_H];
+    __shared__ TileGeo G;
     const int4 T = tiles[blockIdx.x];
-    const SimDev& S = sims[T.x];
     const int step = load_step(ctl);
-    const int parity = step & 1, next = parity ^ 1;
+    const int parity = step & 1;
     const float t = step_time(step, S.dt);
     const int tid = threadIdx.x, lx = tid & (TILE_CX - 1), ly = tid / TILE_CX;
     const int c0x = T.y * TILE_NX - 1, c0y = T.z * TILE_NY - 1;
     const int ci = c0x + lx, cj = c0y + ly;
-    const bool owned = lx >= 1 && ly >= 1;
-
-    float fix[4] = {0.f, 0.f, 0.f, 0.f}, fiy[4] = {0.f, 0.f, 0.f, 0.f};
-    float fex[4] = {0.f, 0.f, 0.f, 0.f}, fey[4] = {0.f, 0.f, 0.f, 0.f};
-    if (ci >= 0 && ci < S.nx && cj >= 0 && cj < S.ny) {
-        const CellGeo g = cell_geo(ci, cj, S.hx, S.hy);
-        float V0 = 0.0f, size0 = 1.0f;
-        if (REINIT) {
-            const int cnt = count_cell(S, ci, cj, g);
-            if (cnt) V0 = fdv(S.vol_el, (float)cnt);
-            size0 = sqrtf(V0);
-        }
-        float nvx[4], nvy[4], dvol = 0.0f;
-        if (!USL) {
-            int ids[4];
-            cell_nodes(S, ci, cj, ids);
-            #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                nvx[k] = S.nvax[ids[k]];
-                nvy[k] = S.nvay[ids[k]];
-            }
-            // centroid strain rate (xi = eta = 0), particle.py:270-279
-            float Gcx[4], Gcy[4], c0, c1, c3;
-            dshape4(0.0f, 0.0f, g.rx, g.ry, Gcx, Gcy);
-            strain_rate4(Gcx, Gcy, nvx, nvy, c0, c1, c3);
-            dvol = fm(S.dt, fa(c0, c1));
-        }
-        const float* __restrict__ sxx = S.sxx[parity];
-        const float* __restrict__ syy = S.syy[parity];
-        const float* __restrict__ szz = S.szz[parity];
-        const float* __restrict__ sxy = S.sxy[parity];
-        const float* __restrict__ rho = S.rho[parity];
-        const float* __restrict__ vsc = S.vsc[parity];
-        visit_cell(S, ci, cj, g, [&](int q) {
-            const float xi = natural(S.x[q], g.cx, g.rx);
-            const float eta = natural(S.y[q], g.cy, g.ry);
-            float N[4], Gx[4], Gy[4];
-            shape4(xi, eta, N);
-            dshape4(xi, eta, g.rx, g.ry, Gx, Gy);
-            PState p;
-            p.sxx = sxx[q];
-            p.syy = syy[q];
-            p.szz = szz[q];
-            p.sxy = sxy[q];
-            p.rho = rho[q];
-            const float mp = REINIT ? fm(V0, p.rho) : S.mass[q];
-            float V = REINIT ? V0 : S.vol[parity][q];
-            if (!USL) {
-                float r0, r1, r3;
-                strain_rate4(Gx, Gy, nvx, nvy, r0, r1, r3);
-                p.exx = S.exx[q];
-                p.eyy = S.eyy[q];
-                p.exy = S.exy[q];
-                p.vsc = vsc[q];
-                const MatDev M = S.mats[S.mat[q]];
-                const float Ep = S.E ? S.E[q] : -1.0f;
-                V = fm(V, strain_stress_update(M, Ep, S.dt, r0, r1, r3, dvol, p));
-                if (owned) {
-                    S.sxx[next][q] = p.sxx;
-                    S.syy[next][q] = p.syy;
-                    S.szz[next][q] = p.szz;
-                    S.sxy[next][q] = p.sxy;
-                    S.exx[q] = p.exx;
-                    S.eyy[q] = p.eyy;
-                    S.exy[q] = p.exy;
-                    S.rho[next][q] = p.rho;
-                    S.vsc[next][q] = p.vsc;
-                    if (!REINIT) S.vol[next][q] = V;
-                }
-            }
-            // internal force (element.py:868-878)
-            const float nV = -V;
-            #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const float fx = fa(fm(Gx[k], p.sxx), fm(Gy[k], p.sxy));
-                const float fy = fa(fm(Gy[k], p.syy), fm(Gx[k], p.sxy));
-                fix[k] = fa(fix[k], fm(nV, fx));
-                fiy[k] = fa(fiy[k], fm(nV, fy));
-            }
-            // body force (element.py:252-256)
-            const float mgx = fm(mp, S.gx), mgy = fm(mp, S.gy);
-            #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                fex[k] = fa(fex[k], fm(N[k], mgx));
-                fey[k] = fa(fey[k], fm(N[k], mgy));
-            }
-            add_traction<TRAC>(S, q, t, V, REINIT ? size0 : (S.psize ? S.psize[q] : 1.0f), N,
-                               fex, fey);
-        });
-    }
     #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        s_f[0][k][tid] = fix[k];
-        s_f[1][k][tid] = fiy[k];
-        s_f[2][k][tid] = fex[k];
-        s_f[3][k][tid] = fey[k];
+    for (int k = 0; k < NQ; ++k) s_c[k][tid] = 0.0f;
+    load_row_starts(S, c0x, cj, s_cs[ly], lx);
+    build_geo(S, c0x, c0y, G);
+    for (int idx = tid; idx < NV_W * NV_H; idx += TILE_THREADS) {
+        const int I = c0x + idx % NV_W, J = c0y + idx / NV_W;
+        float vx = 0.0f, vy = 0.0f;
+        if (I >= 0 && I <= S.nx && J >= 0 && J <= S.ny) {
+            const int n = J * (S.nx + 1) + I;
+            vx = S.nvax[n];
+            vy = S.nvay[n];
+        }
+        s_vx[idx] = vx;
+        s_vy[idx] = vy;
+    }
+    const bool slow = tile_drifted(S, c0x, c0y);   // (also a block barrier)
+
+    auto cell_velocities = [&](int li, int lj, float* vx, float* vy) {
+        const int a = lj * NV_W + li;
+        const int id[4] = {a, a + 1, a + NV_W + 1, a + NV_W};
+        #pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            vx[k] = s_vx[id[k]];
+            vy[k] = s_vy[id[k]];
+        }
+    };
+
+    if (!slow) {
+        const int* cs = s_cs[ly];
+        const int rb = cs[0], re = cs[32];
+        const int cb = cs[lx], ce = cs[lx + 1];
+        {
+            // per-cell values, one lane per cell of the row
+            float nvx[4], nvy[4], V0, size0, dvol;
+            if (!USL) cell_velocities(lx, ly, nvx, nvy);
+            force_cell_values<USL, REINIT>(S, ce - cb, geo_of(G, lx + 1, ly + 1), nvx, nvy, V0,
+                                           size0, dvol);
+            s_V0[ly][lx] = V0;
+            s_size0[ly][lx] = size0;
+            s_dvol[ly][lx] = dvol;
+        }
+        __syncwarp();
+        const int kr = ly + 1;
+        #pragma unroll 1
+        for (int base = rb; base < re; base += 32) {
+            const int q = base + lx;
+            if (q < re) {
+                const int l = cell_of(cs, 31, q);
+                float nvx[4], nvy[4];
+                if (!USL) cell_velocities(l, ly, nvx, nvy);
+                float c[NQ];
+                force_contrib<USL, REINIT, TRAC>(S, q, geo_of(G, l + 1, kr), s_V0[ly][l],
+                                                 s_size0[ly][l], nvx, nvy, s_dvol[ly][l], parity,
+                                                 t, l >= 1 && ly >= 1, c);
+                #pragma unroll
+                for (int k = 0; k < NQ; ++k) s_slot[ly][k][lx] = c[k];
+            }
+            __syncwarp();
+            add_chunk<NQ>(s_c, s_slot[ly], tid, cb, ce, base);
+            __syncwarp();
+        }
+    } else if (ci >= 0 && ci < S.nx && cj >= 0 && cj < S.ny) {
+        const CellGeo g = geo_of(G, lx + 1, ly + 1);
+        const int cnt = REINIT ? count_cell(S, ci, cj, g) : 0;
+        float nvx[4], nvy[4], V0, size0, dvol;
+        if (!USL) cell_velocities(lx, ly, nvx, nvy);
+        force_cell_values<USL, REINIT>(S, cnt, g, nvx, nvy, V0, size0, dvol);
+        const bool own = lx >= 1 && ly >= 1;
+        visit_cell(S, ci, cj, g, [&](int q) {
+            float c[NQ];
+            force_contrib<USL, REINIT, TRAC>(S, q, g, V0, size0, nvx, nvy, dvol, parity, t, own, c);
+            #pragma unroll
+            for (int k = 0; k < NQ; ++k) s_c[k][tid] = fa(s_c[k][tid], c[k]);
+        });
     }
     __syncthreads();
     if (lx < TILE_NX && ly < TILE_NY) {
         const int I = c0x + 1 + lx, J = c0y + 1 + ly;
         if (I <= S.nx && J <= S.ny) {
-            nodal_update(S, J * (S.nx + 1) + I, t, node_sum(s_f[0], tid), node_sum(s_f[1], tid),
-                         node_sum(s_f[2], tid), node_sum(s_f[3], tid));
+            const int a = (ly + 1) * NV_W + lx + 1;   // node (I, J) in the node tile
+            nodal_update(S, J * (S.nx + 1) + I, t, node_sum(s_c + 0, tid), node_sum(s_c + 4, tid),
+                         node_sum(s_c + 8, tid), node_sum(s_c + 12, tid), s_vx[a], s_vy[a]);
         }
     }
 }
@@ -344,127 +564,195 @@ k_forces(const SimDev* __restrict__ sims, const int4* __restrict__ tiles,
 // Phase 3: G2P (diffmpm/particle.py:208-247): v_hat = sum N v_i,
 // a_hat = sum N a_i, v_p = v_hat or v_p + a_hat dt, x_p += v_hat dt.  USL adds
 // the strain/volume/stress update at the step's natural coordinates with the
-// updated nodal velocities (scheme.py:127-133).  Thread per owned sort-cell.
+// updated nodal velocities (scheme.py:127-133).  Warp w streams the particles
+// of the owned sort-cells of row w + 1 (one particle per lane) against a
+// shared-memory tile of the nodal velocity and acceleration, and records per
+// sort-cell whether a particle now lies in another cell (the drift flags).
 // ---------------------------------------------------------------------------
+constexpr int G_W = TILE_CX + 2;   // node tile [c0x, c0x+34) x [c0y, c0y+18)
+constexpr int G_H = TILE_CY + 2;
+
+// New cell along one axis for a coordinate that was in table column k (cell
+// c = base + k): same, or a neighbour by one, decided against the tabulated
+// bounds; otherwise a full locate.
+__device__ __forceinline__ int moved_axis(float x, const float* lo, const float* hi, int k,
+                                          int nk, int c, float h, int n) {
+    if (x >= lo[k] && x < hi[k]) return c;
+    if (x >= hi[k] && k + 1 < nk && x < hi[k + 1]) return c + 1;
+    if (x < lo[k] && k >= 1 && x >= lo[k - 1]) return c - 1;
+    return locate_axis(x, h, n);
+}
+
 template <bool USL, bool REINIT>
-__global__ void __launch_bounds__(TILE_THREADS)
-k_particle_kinematics(const SimDev* __restrict__ sims, const int4* __restrict__ tiles,
+__global__ void __launch_bounds__(TILE_THREADS, 2)
+k_particle_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
                       Control* __restrict__ ctl) {
+    __shared__ float s_vx[G_W * G_H], s_vy[G_W * G_H], s_ax[G_W * G_H], s_ay[G_W * G_H];
+    __shared__ int s_cs[TILE_CY][33];
+    __shared__ int s_sf[TILE_CY][32];     // drift flag of the sort-cell at the start of the step
+    __shared__ int s_flag[TILE_CY][32];   // drift flag after this step
+    __shared__ int s_status;
+    __shared__ TileGeo G;
     const int4 T = tiles[blockIdx.x];
-    const SimDev& S = sims[T.x];
     const int step = load_step(ctl);
     const int parity = step & 1, next = parity ^ 1;
-    const int tid = threadIdx.x, lx = tid & (TILE_CX - 1), ly = tid / TILE_CX;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid / 32;
+    const int c0x = T.y * TILE_NX - 1, c0y = T.z * TILE_NY - 1;
+    const float dt = S.dt;
+    if (tid == 0) s_status = 0;
+    for (int idx = tid; idx < G_W * G_H; idx += TILE_THREADS) {
+        const int I = c0x + idx % G_W, J = c0y + idx / G_W;
+        float vx = 0.0f, vy = 0.0f, ax = 0.0f, ay = 0.0f;
+        if (I >= 0 && I <= S.nx && J >= 0 && J <= S.ny) {
+            const int n = J * (S.nx + 1) + I;
+            vx = S.nvbx[n];
+            vy = S.nvby[n];
+            ax = S.nax[n];
+            ay = S.nay[n];
+        }
+        s_vx[idx] = vx;
+        s_vy[idx] = vy;
+        s_ax[idx] = ax;
+        s_ay[idx] = ay;
+    }
+    build_geo(S, c0x, c0y, G);
+    // row w + 1 of the tile: owned sort-cells c0x+1 .. c0x+31 -> starts cs[0..31]
+    const int sj = c0y + 1 + w;
+    const bool row_ok = w < TILE_NY && sj < S.ny;
+    if (row_ok) {
+        const int col = min(c0x + 1 + lane, S.nx);
+        s_cs[w][lane] = S.cstart[sj * S.nx + col];
+        s_sf[w][lane] = col < S.nx ? S.cflag[sj * S.nx + col] : 0;
+    }
+    s_flag[w][lane] = 0;
+    __syncthreads();
     int status = 0;
-    if (lx < TILE_NX && ly < TILE_NY) {
-        const int si = T.y * TILE_NX + lx, sj = T.z * TILE_NY + ly;
-        if (si < S.nx && sj < S.ny) {
-            const int s = sj * S.nx + si;
-            const int b = S.cstart[s], e = S.cstart[s + 1];
-            const bool flagged = S.cflag[s] != 0;
-            bool drifted = false;
-            int cci = -1, ccj = -1;
-            CellGeo g;
-            float nvx[4], nvy[4], nax[4], nay[4], dvol = 0.0f, V0 = 0.0f;
-            const float dt = S.dt;
-            #pragma unroll 1
-            for (int q = b; q < e; ++q) {
-                const float x = S.x[q], y = S.y[q];
-                int ci = si, cj = sj;
-                if (flagged) {
-                    ci = locate_axis(x, S.hx, S.nx);
-                    cj = locate_axis(y, S.hy, S.ny);
-                    if (ci < 0 || ci >= S.nx || cj < 0 || cj >= S.ny) {
-                        status |= ST_OUT_OF_MESH;
-                        continue;
-                    }
-                }
-                if (ci != cci || cj != ccj) {
-                    cci = ci;
-                    ccj = cj;
-                    g = cell_geo(ci, cj, S.hx, S.hy);
-                    int ids[4];
-                    cell_nodes(S, ci, cj, ids);
-                    #pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        nvx[k] = S.nvbx[ids[k]];
-                        nvy[k] = S.nvby[ids[k]];
-                        nax[k] = S.nax[ids[k]];
-                        nay[k] = S.nay[ids[k]];
-                    }
-                    if (USL) {
-                        float Gcx[4], Gcy[4], c0, c1, c3;
-                        dshape4(0.0f, 0.0f, g.rx, g.ry, Gcx, Gcy);
-                        strain_rate4(Gcx, Gcy, nvx, nvy, c0, c1, c3);
-                        dvol = fm(dt, fa(c0, c1));
-                    }
-                }
-                const float xi = natural(x, g.cx, g.rx);
-                const float eta = natural(y, g.cy, g.ry);
-                float N[4];
-                shape4(xi, eta, N);
-                const float vhx = dot4(N, nvx), vhy = dot4(N, nvy);
-                float vx, vy;
-                if (S.velocity_update) {
-                    vx = vhx;
-                    vy = vhy;
-                } else {
-                    vx = fa(S.vx[q], fm(dot4(N, nax), dt));
-                    vy = fa(S.vy[q], fm(dot4(N, nay), dt));
-                }
-                const float xn = fa(x, fm(vhx, dt)), yn = fa(y, fm(vhy, dt));
-                S.x[q] = xn;
-                S.y[q] = yn;
-                S.vx[q] = vx;
-                S.vy[q] = vy;
-                if (USL) {
-                    float Gx[4], Gy[4], r0, r1, r3;
-                    dshape4(xi, eta, g.rx, g.ry, Gx, Gy);
-                    strain_rate4(Gx, Gy, nvx, nvy, r0, r1, r3);
-                    PState p;
-                    p.sxx = S.sxx[parity][q];
-                    p.syy = S.syy[parity][q];
-                    p.szz = S.szz[parity][q];
-                    p.sxy = S.sxy[parity][q];
-                    p.exx = S.exx[q];
-                    p.eyy = S.eyy[q];
-                    p.exy = S.exy[q];
-                    p.rho = S.rho[parity][q];
-                    p.vsc = S.vsc[parity][q];
-                    const MatDev M = S.mats[S.mat[q]];
-                    const float Ep = S.E ? S.E[q] : -1.0f;
-                    const float f = strain_stress_update(M, Ep, dt, r0, r1, r3, dvol, p);
-                    S.sxx[next][q] = p.sxx;
-                    S.syy[next][q] = p.syy;
-                    S.szz[next][q] = p.szz;
-                    S.sxy[next][q] = p.sxy;
-                    S.exx[q] = p.exx;
-                    S.eyy[q] = p.eyy;
-                    S.exy[q] = p.exy;
-                    S.rho[next][q] = p.rho;
-                    S.vsc[next][q] = p.vsc;
-                    if (!REINIT) S.vol[next][q] = fm(S.vol[parity][q], f);
-                    (void)V0;
-                }
-                const int ni = locate_axis(xn, S.hx, S.nx), nj = locate_axis(yn, S.hy, S.ny);
-                if (ni < 0 || ni >= S.nx || nj < 0 || nj >= S.ny) {
+    if (row_ok) {
+        const int* cs = s_cs[w];
+        const int rb = cs[0], re = cs[31];
+        #pragma unroll 1
+        for (int base = rb; base < re; base += 32) {
+            const int q = base + lane;
+            if (q >= re) continue;
+            const int l = cell_of(cs, 30, q);   // sort-cell c0x + 1 + l
+            const int si = c0x + 1 + l;
+            const float x = S.x[q], y = S.y[q];
+            int ci = si, cj = sj;
+            if (s_sf[w][l]) {
+                ci = locate_axis(x, S.hx, S.nx);
+                cj = locate_axis(y, S.hy, S.ny);
+                if (ci < 0 || ci >= S.nx || cj < 0 || cj >= S.ny) {
                     status |= ST_OUT_OF_MESH;
-                } else {
-                    const int d = max(abs(ni - si), abs(nj - sj));
-                    if (d >= 1) drifted = true;
-                    if (d > 1) status |= ST_DRIFT_VIOLATION;
+                    s_flag[w][l] = 1;
+                    continue;
                 }
             }
-            S.cflag[s] = drifted ? 1 : 0;
-            if (drifted) status |= ST_DRIFTED;
+            const int kc = ci - c0x + 1, kr = cj - c0y + 1;   // geometry table indices
+            const bool in_tile = kc >= 0 && kc < GEO_C && kr >= 0 && kr < GEO_R;
+            const CellGeo g = in_tile ? geo_of(G, kc, kr) : cell_geo(ci, cj, S.hx, S.hy);
+            float nvx[4], nvy[4], nax[4], nay[4];
+            const int li = ci - c0x, lj = cj - c0y;
+            if (li >= 0 && li + 1 < G_W && lj >= 0 && lj + 1 < G_H) {
+                const int a = lj * G_W + li;
+                const int id[4] = {a, a + 1, a + G_W + 1, a + G_W};
+                #pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    nvx[k] = s_vx[id[k]];
+                    nvy[k] = s_vy[id[k]];
+                    nax[k] = s_ax[id[k]];
+                    nay[k] = s_ay[id[k]];
+                }
+            } else {
+                int ids[4];
+                cell_nodes(S, ci, cj, ids);
+                #pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    nvx[k] = S.nvbx[ids[k]];
+                    nvy[k] = S.nvby[ids[k]];
+                    nax[k] = S.nax[ids[k]];
+                    nay[k] = S.nay[ids[k]];
+                }
+            }
+            const float xi = natural(x, g.cx, g.rx);
+            const float eta = natural(y, g.cy, g.ry);
+            float N[4];
+            shape4(xi, eta, N);
+            const float vhx = dot4(N, nvx), vhy = dot4(N, nvy);
+            float vx, vy;
+            if (S.velocity_update) {
+                vx = vhx;
+                vy = vhy;
+            } else {
+                vx = fa(S.vx[q], fm(dot4(N, nax), dt));
+                vy = fa(S.vy[q], fm(dot4(N, nay), dt));
+            }
+            const float xn = fa(x, fm(vhx, dt)), yn = fa(y, fm(vhy, dt));
+            S.x[q] = xn;
+            S.y[q] = yn;
+            S.vx[q] = vx;
+            S.vy[q] = vy;
+            if (USL) {
+                float Gcx[4], Gcy[4], c0, c1, c3;
+                dshape4(0.0f, 0.0f, g.rx, g.ry, Gcx, Gcy);
+                strain_rate4(Gcx, Gcy, nvx, nvy, c0, c1, c3);
+                const float dvol = fm(dt, fa(c0, c1));
+                float Gx[4], Gy[4], r0, r1, r3;
+                dshape4(xi, eta, g.rx, g.ry, Gx, Gy);
+                strain_rate4(Gx, Gy, nvx, nvy, r0, r1, r3);
+                PState p;
+                p.sxx = S.sxx[parity][q];
+                p.syy = S.syy[parity][q];
+                p.szz = S.szz[parity][q];
+                p.sxy = S.sxy[parity][q];
+                p.exx = S.exx[q];
+                p.eyy = S.eyy[q];
+                p.exy = S.exy[q];
+                p.rho = S.rho[parity][q];
+                p.vsc = S.vsc[parity][q];
+                const MatDev& M = S.mats[S.mat[q]];
+                const float Ep = S.E ? S.E[q] : -1.0f;
+                const float f = strain_stress_update(M, Ep, dt, r0, r1, r3, dvol, p);
+                S.sxx[next][q] = p.sxx;
+                S.syy[next][q] = p.syy;
+                S.szz[next][q] = p.szz;
+                S.sxy[next][q] = p.sxy;
+                S.exx[q] = p.exx;
+                S.eyy[q] = p.eyy;
+                S.exy[q] = p.exy;
+                S.rho[next][q] = p.rho;
+                S.vsc[next][q] = p.vsc;
+                if (!REINIT) S.vol[next][q] = fm(S.vol[parity][q], f);
+            }
+            int ni, nj;
+            if (in_tile) {
+                ni = moved_axis(xn, G.x0, G.x1, kc, GEO_C, ci, S.hx, S.nx);
+                nj = moved_axis(yn, G.y0, G.y1, kr, GEO_R, cj, S.hy, S.ny);
+            } else {
+                ni = locate_axis(xn, S.hx, S.nx);
+                nj = locate_axis(yn, S.hy, S.ny);
+            }
+            if (ni < 0 || ni >= S.nx || nj < 0 || nj >= S.ny) {
+                status |= ST_OUT_OF_MESH;
+                s_flag[w][l] = 1;
+            } else {
+                const int d = max(abs(ni - si), abs(nj - sj));
+                if (d >= 1) s_flag[w][l] = 1;
+                if (d > 1) status |= ST_DRIFT_VIOLATION;
+            }
+        }
+    }
+    __syncwarp();
+    if (row_ok && lane < TILE_NX) {
+        const int si = c0x + 1 + lane;
+        if (si < S.nx) {
+            const int f = s_flag[w][lane];
+            S.cflag[sj * S.nx + si] = (uint8_t)f;
+            if (f) status |= ST_DRIFTED;
         }
     }
     // block-wide OR of the status bits, then one atomic per CTA
     status = __reduce_or_sync(0xffffffffu, status);
-    __shared__ int s_status;
-    if (tid == 0) s_status = 0;
-    __syncthreads();
-    if ((tid & 31) == 0 && status) atomicOr(&s_status, status);
+    if (lane == 0 && status) atomicOr(&s_status, status);
     __syncthreads();
     if (tid == 0) {
         if (s_status) atomicOr(&ctl->status, s_status);
@@ -482,40 +770,40 @@ k_particle_kinematics(const SimDev* __restrict__ sims, const int4* __restrict__ 
 // ---------------------------------------------------------------------------
 // Launchers
 // ---------------------------------------------------------------------------
-cudaError_t launch_nodal_kinematics(const StepConfig& c, const SimDev* sims, const int4* tiles,
+cudaError_t launch_nodal_kinematics(const StepConfig& c, const SimDev& S, const int4* tiles,
                                     int ntiles, Control* ctl, cudaStream_t s) {
-    if (c.reinit) k_nodal_kinematics<true><<<ntiles, TILE_THREADS, 0, s>>>(sims, tiles, ctl);
-    else k_nodal_kinematics<false><<<ntiles, TILE_THREADS, 0, s>>>(sims, tiles, ctl);
+    if (c.reinit) k_nodal_kinematics<true><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl);
+    else k_nodal_kinematics<false><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl);
     return cudaGetLastError();
 }
 
 template <bool USL, bool REINIT>
-static void forces_trac(bool trac, const SimDev* sims, const int4* tiles, int ntiles, Control* ctl,
+static void forces_trac(bool trac, const SimDev& S, const int4* tiles, int ntiles, Control* ctl,
                         cudaStream_t s) {
-    if (trac) k_forces<USL, REINIT, true><<<ntiles, TILE_THREADS, 0, s>>>(sims, tiles, ctl);
-    else k_forces<USL, REINIT, false><<<ntiles, TILE_THREADS, 0, s>>>(sims, tiles, ctl);
+    if (trac) k_forces<USL, REINIT, true><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl);
+    else k_forces<USL, REINIT, false><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl);
 }
 
-cudaError_t launch_forces(const StepConfig& c, const SimDev* sims, const int4* tiles, int ntiles,
+cudaError_t launch_forces(const StepConfig& c, const SimDev& S, const int4* tiles, int ntiles,
                           Control* ctl, cudaStream_t s) {
     if (c.usl) {
-        if (c.reinit) forces_trac<true, true>(c.traction, sims, tiles, ntiles, ctl, s);
-        else forces_trac<true, false>(c.traction, sims, tiles, ntiles, ctl, s);
+        if (c.reinit) forces_trac<true, true>(c.traction, S, tiles, ntiles, ctl, s);
+        else forces_trac<true, false>(c.traction, S, tiles, ntiles, ctl, s);
     } else {
-        if (c.reinit) forces_trac<false, true>(c.traction, sims, tiles, ntiles, ctl, s);
-        else forces_trac<false, false>(c.traction, sims, tiles, ntiles, ctl, s);
+        if (c.reinit) forces_trac<false, true>(c.traction, S, tiles, ntiles, ctl, s);
+        else forces_trac<false, false>(c.traction, S, tiles, ntiles, ctl, s);
     }
     return cudaGetLastError();
 }
 
-cudaError_t launch_particle_kinematics(const StepConfig& c, const SimDev* sims, const int4* tiles,
+cudaError_t launch_particle_kinematics(const StepConfig& c, const SimDev& S, const int4* tiles,
                                        int ntiles, Control* ctl, cudaStream_t s) {
     if (c.usl) {
-        if (c.reinit) k_particle_kinematics<true, true><<<ntiles, TILE_THREADS, 0, s>>>(sims, tiles, ctl);
-        else k_particle_kinematics<true, false><<<ntiles, TILE_THREADS, 0, s>>>(sims, tiles, ctl);
+        if (c.reinit) k_particle_kinematics<true, true><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl);
+        else k_particle_kinematics<true, false><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl);
     } else {
-        if (c.reinit) k_particle_kinematics<false, true><<<ntiles, TILE_THREADS, 0, s>>>(sims, tiles, ctl);
-        else k_particle_kinematics<false, false><<<ntiles, TILE_THREADS, 0, s>>>(sims, tiles, ctl);
+        if (c.reinit) k_particle_kinematics<false, true><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl);
+        else k_particle_kinematics<false, false><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl);
     }
     return cudaGetLastError();
 }

@@ -12,12 +12,14 @@ struct StepConfig {
     bool traction;     // particle tractions present
 };
 
-// One explicit step = three launches over the tile list.
-cudaError_t launch_nodal_kinematics(const StepConfig& c, const SimDev* sims, const int4* tiles,
+// One explicit step = three launches over the tile list.  The descriptor is
+// passed by value (a __grid_constant__ kernel parameter), so a captured graph
+// holds the descriptor current at capture time.
+cudaError_t launch_nodal_kinematics(const StepConfig& c, const SimDev& S, const int4* tiles,
                                     int ntiles, Control* ctl, cudaStream_t s);
-cudaError_t launch_forces(const StepConfig& c, const SimDev* sims, const int4* tiles, int ntiles,
+cudaError_t launch_forces(const StepConfig& c, const SimDev& S, const int4* tiles, int ntiles,
                           Control* ctl, cudaStream_t s);
-cudaError_t launch_particle_kinematics(const StepConfig& c, const SimDev* sims, const int4* tiles,
+cudaError_t launch_particle_kinematics(const StepConfig& c, const SimDev& S, const int4* tiles,
                                        int ntiles, Control* ctl, cudaStream_t s);
 
 // Re-sort of one simulation's particles by current cell, stable in storage order.

@@ -229,6 +229,13 @@ class Simulation:
     def step_index(self, value):
         self._ok(self._lib.mpm_set_step(self._h, int(value)))
 
+    def time_phases(self, nsteps, stream=None):
+        """Advance ``nsteps`` steps and return the device milliseconds spent in
+        each phase kernel, {"nodal_kinematics", "forces", "particle_kinematics"}."""
+        ms = (C.c_float * 3)()
+        self._ok(self._lib.mpm_time_phases(self._h, int(nsteps), ms, stream))
+        return dict(zip(_lib.PHASE, list(ms)))
+
     def set_block_steps(self, n):
         self._ok(self._lib.mpm_set_block_steps(self._h, int(n)))
 

@@ -187,6 +187,12 @@ int mpm_set_step(MpmHandle* h, int64_t step);
  * three phases in order. */
 int mpm_run_phase(MpmHandle* h, int phase, void* stream);
 
+/* Advance `nsteps` steps launching the three phase kernels directly (no graph)
+ * with CUDA events between them, and return the summed device time of each
+ * phase in ms_out[0..2] (nodal kinematics, forces, particle kinematics).  For
+ * measurement; the state advances as with mpm_step. */
+int mpm_time_phases(MpmHandle* h, int nsteps, float* ms_out, void* stream);
+
 /* Steps per captured CUDA graph (default 100). */
 int mpm_set_block_steps(MpmHandle* h, int steps);
 

@@ -1,0 +1,221 @@
+"""Differentiable float64 restatement of the explicit MPM step -- TEST INFRASTRUCTURE.
+
+A PyTorch (CPU, float64) restatement of the same step as ``oracle.mpm_oracle``
+(and of the reference's diffmpm step it restates), written so that autograd
+gives the exact discrete gradient of a loss with respect to the per-particle
+Young's modulus and the initial particle state.  It is the gradient oracle of
+the hand-written CUDA adjoint; ``tests/test_oracle_torch.py`` checks that its
+forward agrees with the NumPy oracle run in float64, and the adjoint tests also
+check it against central finite differences of that oracle.
+
+Scope: Quadrilateral4Node mesh, USF or USL, the per-step volume set-up of
+``solve_jit`` (diffmpm/solver.py:81-85, 100-111), LinearElastic (per-particle E
+or the material's) and SimpleMaterial, gravity, velocity constraints,
+concentrated nodal forces.  Particle cell ids and counts are piecewise constant
+in the positions and carry no gradient; so are the flush-to-zero masks.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from .mpm_oracle import le_coefficients
+
+FLUSH = 1e-12
+
+
+def _flush(a):
+    return torch.where(a.abs() < FLUSH, torch.zeros_like(a), a)
+
+
+class TorchMPM:
+    """One simulation: mesh, materials, boundary conditions; ``run`` advances a
+    state dict of tensors ``x (N,2), v (N,2), sig (N,4: xx yy zz xy),
+    eps (N,3: xx yy xy), rho (N,), vsc (N,)`` and the persistent nodal velocity."""
+
+    def __init__(self, nx, ny, hx, hy, dt, gravity, constraints, materials, mat_ids,
+                 scheme="usf", velocity_update=False, nodal_forces=()):
+        self.nx, self.ny = nx, ny
+        f = torch.float64
+        self.hx, self.hy = float(hx), float(hy)
+        self.node_x = torch.arange(nx + 1, dtype=f) * self.hx
+        self.node_y = torch.arange(ny + 1, dtype=f) * self.hy
+        self.dt = float(dt)
+        self.g = torch.tensor(np.broadcast_to(np.asarray(gravity, float).reshape(-1), (2,)), dtype=f)
+        nn = (nx + 1) * (ny + 1)
+        self.nn = nn
+        # constraint masks/values in application order: last one wins per (node, dir)
+        self.cmask = torch.zeros(nn, 2, dtype=torch.bool)
+        self.cval = torch.zeros(nn, 2, dtype=f)
+        for ids, d, vel in constraints:
+            ids = torch.as_tensor(np.asarray(ids, dtype=np.int64).reshape(-1))
+            self.cmask[ids, d] = True
+            self.cval[ids, d] = float(vel)
+        self.cnf = [(torch.as_tensor(np.asarray(ids, dtype=np.int64).reshape(-1)), d, float(F), fn)
+                    for ids, d, F, fn in nodal_forces]
+        a, b, c = self.hy, self.hx, self.hy
+        p = np.sqrt(a * a + b * b)
+        t = a * a + c * c - b * b - b * b
+        self.vol_el = 0.25 * np.sqrt(4 * p * p * p * p - t * t)
+        self.scheme = scheme
+        self.velocity_update = velocity_update
+        self.mat_ids = torch.as_tensor(np.asarray(mat_ids, dtype=np.int64))
+        self.materials = materials
+
+    # ------------------------------------------------------------------
+    def _locate(self, x):
+        with torch.no_grad():
+            i = torch.searchsorted(self.node_x, x[:, 0].contiguous(), right=True) - 1
+            j = torch.searchsorted(self.node_y, x[:, 1].contiguous(), right=True) - 1
+        if ((i < 0) | (i >= self.nx) | (j < 0) | (j >= self.ny)).any():
+            raise ValueError("particle outside the mesh")
+        return i, j
+
+    def _geometry(self, x):
+        i, j = self._locate(x)
+        e = j * self.nx + i
+        x0, x1 = self.node_x[i], self.node_x[i + 1]
+        y0, y1 = self.node_y[j], self.node_y[j + 1]
+        rx, ry = 2.0 / (x1 - x0), 2.0 / (y1 - y0)
+        xi = (x[:, 0] - (x0 + x1) / 2) * rx
+        eta = (x[:, 1] - (y0 + y1) / 2) * ry
+        ll = j * (self.nx + 1) + i
+        ids = torch.stack([ll, ll + 1, ll + self.nx + 2, ll + self.nx + 1], dim=1)
+        a, b, c, d = 1 - xi, 1 + xi, 1 - eta, 1 + eta
+        N = torch.stack([0.25 * a * c, 0.25 * b * c, 0.25 * b * d, 0.25 * a * d], dim=1)
+        Gx = torch.stack([-0.25 * c, 0.25 * c, 0.25 * d, -0.25 * d], dim=1) * rx[:, None]
+        Gy = torch.stack([-0.25 * a, -0.25 * b, 0.25 * b, 0.25 * a], dim=1) * ry[:, None]
+        Gcx = torch.stack([-0.25 * rx, 0.25 * rx, 0.25 * rx, -0.25 * rx], dim=1)
+        Gcy = torch.stack([-0.25 * ry, -0.25 * ry, 0.25 * ry, 0.25 * ry], dim=1)
+        return e, ids, N, Gx, Gy, Gcx, Gcy
+
+    def _scatter(self, ids, vals):
+        out = torch.zeros((self.nn,) + vals.shape[2:], dtype=vals.dtype)
+        return out.index_add(0, ids.reshape(-1), vals.reshape((-1,) + vals.shape[2:]))
+
+    def _constrain(self, v, a=None):
+        v = torch.where(self.cmask, self.cval, v)
+        if a is not None:
+            a = torch.where(self.cmask, torch.zeros_like(a), a)
+        return v, a
+
+    def _stress(self, s, E, sr, dvol, vsc_new):
+        """Stress update of particle.py:315-322 for the particle's material."""
+        dt = self.dt
+        d0, d1, d3 = sr[:, 0] * dt, sr[:, 1] * dt, sr[:, 2] * dt
+        out = s.clone()
+        for k, mat in enumerate(self.materials):
+            sel = self.mat_ids == k
+            if not bool(sel.any()):
+                continue
+            kind = type(mat).__name__
+            if kind == "LinearElastic":
+                c1, c2, c3 = le_coefficients(float(mat.properties["poisson_ratio"]))
+                Ek = E[sel] if E is not None else torch.full((int(sel.sum()),),
+                                                             float(mat.properties["youngs_modulus"]),
+                                                             dtype=torch.float64)
+                a1, a2, G = Ek * c1, Ek * c2, Ek * c3
+                ds = torch.stack([a1 * d0[sel] + a2 * d1[sel], a2 * d0[sel] + a1 * d1[sel],
+                                  a2 * d0[sel] + a2 * d1[sel], G * d3[sel]], dim=1)
+            elif kind == "SimpleMaterial":
+                Es = float(mat.properties["E"])
+                ds = torch.stack([d0[sel] * Es, d1[sel] * Es, torch.zeros_like(d0[sel]),
+                                  d3[sel] * Es], dim=1)
+            else:
+                raise NotImplementedError(kind)
+            out = out.index_put((sel.nonzero()[:, 0],), s[sel] + ds)
+        return out
+
+    def _strain(self, st, Gx, Gy, ids, vn, Gcx, Gcy):
+        vx, vy = vn[ids, 0], vn[ids, 1]
+        r0 = _flush((Gx * vx).sum(1))
+        r1 = _flush((Gy * vy).sum(1))
+        r3 = _flush((Gx * vy).sum(1) + (Gy * vx).sum(1))
+        c0 = _flush((Gcx * vx).sum(1))
+        c1 = _flush((Gcy * vy).sum(1))
+        dvol = self.dt * (c0 + c1)
+        return torch.stack([r0, r1, r3], dim=1), dvol
+
+    def step(self, st, i, E=None):
+        """One solve_jit step (R0 + scheme), returns the new state dict."""
+        x, v, s, eps, rho, vsc, nvo = (st[k] for k in ("x", "v", "sig", "eps", "rho", "vsc", "nv"))
+        e, ids, N, Gx, Gy, Gcx, Gcy = self._geometry(x)
+        with torch.no_grad():
+            cnt = torch.bincount(e, minlength=self.nx * self.ny).to(torch.float64)
+        V0 = self.vol_el / cnt[e]
+        m = V0 * rho
+        M = self._scatter(ids, m[:, None] * N)
+        P = _flush(self._scatter(ids, (N[:, :, None] * (m[:, None] * v)[:, None, :])))
+        safeM = torch.where(M == 0, torch.ones_like(M), M)
+        vn = torch.where((M == 0)[:, None], nvo, P / safeM[:, None])
+        vn, _ = self._constrain(_flush(vn))
+        out = dict(st)
+        V = V0
+        if self.scheme == "usf":
+            sr, dvol = self._strain(st, Gx, Gy, ids, vn, Gcx, Gcy)
+            vsc = vsc + dvol
+            s = self._stress(s, E, sr, dvol, vsc)
+            eps = eps + sr * self.dt
+            V = V0 * (1 + dvol)
+            rho = rho / (1 + dvol)
+        fx = Gx * s[:, 0:1] + Gy * s[:, 3:4]
+        fy = Gy * s[:, 1:2] + Gx * s[:, 3:4]
+        fint = self._scatter(ids, torch.stack([-V[:, None] * fx, -V[:, None] * fy], dim=2))
+        fext = self._scatter(ids, N[:, :, None] * (m[:, None] * self.g[None, :])[:, None, :])
+        t = float(np.float64(i) * self.dt)
+        for nid, d, F, fn in self.cnf:
+            fval = 1.0 if fn is None else float(np.interp(t, fn.xvalues, fn.fxvalues))
+            col = torch.zeros(self.nn, 2, dtype=torch.float64)
+            col[:, d] = torch.zeros(self.nn, dtype=torch.float64).index_add(
+                0, nid, torch.full((nid.numel(),), fval * F, dtype=torch.float64))
+            fext = fext + col
+        tot = fint + fext
+        a = torch.where((M == 0)[:, None], torch.zeros_like(tot), tot / safeM[:, None])
+        vb = vn + a * self.dt
+        vb, a = self._constrain(vb, a)
+        vb, a = _flush(vb), _flush(a)
+        vhat = (N[:, :, None] * vb[ids]).sum(1)
+        ahat = (N[:, :, None] * a[ids]).sum(1)
+        vp = vhat if self.velocity_update else v + ahat * self.dt
+        xp = x + vhat * self.dt
+        if self.scheme == "usl":
+            sr, dvol = self._strain(st, Gx, Gy, ids, vb, Gcx, Gcy)
+            vsc = vsc + dvol
+            s = self._stress(s, E, sr, dvol, vsc)
+            eps = eps + sr * self.dt
+            rho = rho / (1 + dvol)
+        out.update(x=xp, v=vp, sig=s, eps=eps, rho=rho, vsc=vsc, nv=vb)
+        return out
+
+    def run(self, st, nsteps, E=None, start=0):
+        for i in range(start, start + nsteps):
+            st = self.step(st, i, E)
+        return st
+
+
+def from_solver(solver, gravity):
+    """TorchMPM and initial state dict from a float64 ``oracle.mpm_oracle``
+    MPMExplicit built for one particle set."""
+    el = solver.mesh.elements
+    ps = solver.mesh.particles[0]
+    nx, ny = el.nelements
+    cons = [(ids, c.dir, c.velocity) for ids, c in el.constraints]
+    nfs = [(f.node_ids, f.dir, f.force, None if type(f.function).__name__ == "Unit" else f.function)
+           for f in el.concentrated_nodal_forces]
+    sim = TorchMPM(nx, ny, float(el.el_len[0]), float(el.el_len[1]), solver.dt, gravity, cons,
+                   ps.materials, ps.material_ids, scheme=solver.scheme,
+                   velocity_update=solver.velocity_update, nodal_forces=nfs)
+    f = torch.float64
+    n = len(ps)
+    s = ps.stress.reshape(n, 6)
+    e = ps.strain.reshape(n, 6)
+    st = {
+        "x": torch.tensor(ps.loc.reshape(n, 2), dtype=f),
+        "v": torch.tensor(ps.velocity.reshape(n, 2), dtype=f),
+        "sig": torch.tensor(np.stack([s[:, 0], s[:, 1], s[:, 2], s[:, 3]], 1), dtype=f),
+        "eps": torch.tensor(np.stack([e[:, 0], e[:, 1], e[:, 3]], 1), dtype=f),
+        "rho": torch.tensor(ps.density.reshape(n), dtype=f),
+        "vsc": torch.tensor(ps.volumetric_strain_centroid.reshape(n), dtype=f),
+        "nv": torch.tensor(el.nodes.velocity.reshape(-1, 2), dtype=f),
+    }
+    return sim, st

@@ -1,0 +1,72 @@
+"""The float64 torch restatement (the gradient oracle) against the NumPy oracle.
+
+Its forward must equal the NumPy oracle run in float64, and its autograd
+gradient must agree with central finite differences of that oracle.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from diffmpm_gb300 import workloads
+from oracle import mpm_oracle as O
+from oracle import mpm_torch as T
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.mark.parametrize("scheme", ["usf", "usl"])
+def test_forward_matches_numpy_oracle(scheme):
+    o, g, _ = workloads.plain_scaleup(O, n=16, scheme=scheme, sim_steps=6, dtype=np.float64)
+    sim, st = T.from_solver(o, g)
+    for i in range(6):
+        o.step(i, g)
+        st = sim.step(st, i)
+    p = o.mesh.particles[0]
+    assert rel(st["x"].numpy(), p.loc.reshape(-1, 2)) < 1e-14
+    assert rel(st["v"].numpy(), p.velocity.reshape(-1, 2)) < 1e-14
+    assert rel(st["sig"].numpy(), p.stress.reshape(-1, 6)[:, :4]) < 1e-14
+    assert rel(st["rho"].numpy(), p.density.reshape(-1)) < 1e-14
+
+
+def test_forward_matches_with_motion():
+    o, g, _ = workloads.plain_small(O, sim_steps=30, dt=2e-3, velocity=(0.6, 0.25), dtype=np.float64)
+    sim, st = T.from_solver(o, g)
+    for i in range(30):
+        o.step(i, g)
+        st = sim.step(st, i)
+    p = o.mesh.particles[0]
+    assert rel(st["x"].numpy(), p.loc.reshape(-1, 2)) < 1e-13
+    assert rel(st["v"].numpy(), p.velocity.reshape(-1, 2)) < 1e-12
+
+
+def _loss_from(st, target):
+    return ((st["x"] - target) ** 2).sum(1).mean()
+
+
+def test_autograd_matches_finite_differences():
+    """dL/dE of L = mean |x_K - x_target|^2 w.r.t. a per-particle E field."""
+    n, steps = 12, 30
+    o, g, info = workloads.plain_scaleup(O, n=n, sim_steps=steps, dtype=np.float64)
+    # a stiff, fast-responding variant: larger dt so the field matters in 30 steps
+    o.dt = 2e-4
+    o.mpm_scheme.dt = 2e-4
+    sim, st0 = T.from_solver(o, g)
+    rng = np.random.Generator(np.random.PCG64(3))
+    E0 = 1e6 * np.exp(0.5 * rng.normal(size=info["np"]))
+    target = st0["x"].detach() + 1e-4
+    E = torch.tensor(E0, dtype=torch.float64, requires_grad=True)
+    L = _loss_from(sim.run(dict(st0), steps, E=E), target)
+    L.backward()
+    grad = E.grad.numpy()
+    u = rng.normal(size=info["np"])
+    h = 1e-3 * np.linalg.norm(E0) / np.linalg.norm(u)
+
+    def loss(Ev):
+        with torch.no_grad():
+            return float(_loss_from(sim.run(dict(st0), steps, E=torch.tensor(Ev)), target))
+
+    fd = (loss(E0 + h * u) - loss(E0 - h * u)) / (2 * h)
+    assert abs(fd - grad @ u) <= 1e-5 * abs(fd) + 1e-30, (fd, grad @ u)
