@@ -497,6 +497,8 @@ int copy_passive(MpmHandle* h, int field, float* aos, bool to_aos, cudaStream_t 
 
 }  // namespace
 
+void mpm::set_thread_error(const std::string& msg) { g_create_error = msg; }
+
 extern "C" {
 
 int mpm_abi_version(void) { return MPM_ABI_VERSION; }

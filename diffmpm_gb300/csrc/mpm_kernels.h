@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string>
 #include "mpm_types.h"
 
 namespace mpm {
@@ -71,5 +72,8 @@ cudaError_t launch_interleave2(const float* a, const float* b, int n, float* out
 cudaError_t launch_deinterleave2(const float* in, int n, float* a, float* b, cudaStream_t s);
 cudaError_t launch_node_momentum(const float* m, const float* vx, const float* vy, int n,
                                  float* out, cudaStream_t s);
+
+// Set the calling thread's message returned by mpm_last_error(NULL).
+void set_thread_error(const std::string& msg);
 
 }  // namespace mpm

@@ -199,6 +199,28 @@ int mpm_set_block_steps(MpmHandle* h, int steps);
 /* Number of particle re-sorts and rolled-back step blocks so far. */
 int mpm_get_counters(const MpmHandle* h, int64_t* resorts, int64_t* rollbacks);
 
+/* Largest mesh (nx * ny elements) mpm_volume_setup_noalloc accepts. */
+#define MPM_NOALLOC_MAX_ELEMENTS (1 << 20)
+
+/* Particle volume set-up that allocates no device memory.  No counterpart in
+ * the reference: it is the no-allocation form of this library's set-up
+ * (element id, V = V_el / particles in the element, mass = V * density, the
+ * values mpm_initialize and mpm_read_field(ELEMENT_ID / VOLUME / MASS) give),
+ * for callers that cannot call cudaMalloc -- a JAX/XLA FFI handler, whose
+ * buffers come from XLA's allocator, or an application whose framework owns the
+ * device memory pool.  All pointers are device memory: loc (n, 2), density (n)
+ * in; element_id (n; -1 outside the mesh), volume (n), mass (n) out.
+ * The per-element counters live in a fixed 4 MiB device array, so the mesh may
+ * have at most MPM_NOALLOC_MAX_ELEMENTS elements (larger meshes return
+ * MPM_ERR_INVALID).  That array stays resident on every GPU that loads the
+ * library.  The first call on a device (with that device current) looks up
+ * the array's address; make that first call before any stream capture.  All
+ * calls share the array, so calls that overlap on the GPU race; order them.
+ * Errors are reported through mpm_last_error(NULL). */
+int mpm_volume_setup_noalloc(int nx, int ny, double hx, double hy, int64_t n, const float* loc,
+                             const float* density, int32_t* element_id, float* volume,
+                             float* mass, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
