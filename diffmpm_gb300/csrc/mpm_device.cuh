@@ -16,6 +16,19 @@ __device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); 
 __device__ __forceinline__ float fs(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float fdv(float a, float b) { return __fdiv_rn(a, b); }
 
+// Asynchronous 4-byte global -> shared copies (cp.async), committed in groups.
+__device__ __forceinline__ void cp_async4(void* smem_dst, const void* gmem_src) {
+    const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
 // where(|a| < 1e-12, 0, a) (diffmpm/element.py:185-189, particle.py:310-312)
 __device__ __forceinline__ float flush(float a) { return fabsf(a) < 1e-12f ? 0.0f : a; }
 

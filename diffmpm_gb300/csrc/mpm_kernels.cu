@@ -71,7 +71,9 @@ __device__ __forceinline__ void cell_nodes(const SimDev& S, int ci, int cj, int 
 // Sum of the four cell-corner partials meeting at the node of thread `tid`
 // (node = lower-left corner of cell tid + 33): cell (I-1,J-1) corner 2,
 // cell (I,J-1) corner 3, cell (I-1,J) corner 1, cell (I,J) corner 0.
-__device__ __forceinline__ float node_sum(const float (*s)[TILE_THREADS], int tid) {
+constexpr int SC_STRIDE = TILE_THREADS + 1;   // per-quantity row of the cell-corner partials
+
+__device__ __forceinline__ float node_sum(const float (*s)[SC_STRIDE], int tid) {
     return fa(fa(fa(s[2][tid], s[3][tid + 1]), s[1][tid + TILE_CX]), s[0][tid + TILE_CX + 1]);
 }
 
@@ -93,13 +95,15 @@ __device__ __forceinline__ void apply_constraint(const SimDev& S, uint16_t code,
 //
 // Fast path (no drift flag set on the 34 x 18 sort-cells around the tile, so
 // every particle of the tile is in its sort-cell): warp w streams the
-// contiguous storage range of cell row w, one particle per lane (coalesced
-// loads and stores).  A particle's cell is found from its storage index by a
-// binary search of the row's cell starts, and the cell geometry comes from
-// per-tile tables, so no division or locate runs per particle.  The particle's
-// NQ corner contributions go to shared-memory slots; lane l then adds, in
-// storage order, the slots of the particles of its own cell (c0x + l, row w)
-// to that cell's partials.
+// contiguous storage range of cell row w in chunks of 32 particles, one
+// particle per lane.  The chunks are staged into shared memory with cp.async
+// copies issued several chunks ahead, so a warp keeps DEPTH-1 chunks of loads
+// in flight while it computes.  A particle's cell is found from its storage
+// index by a binary search of the row's cell starts, and the cell geometry
+// comes from per-tile tables, so no division or locate runs per particle.  The
+// particle's NQ corner contributions go to shared-memory slots; lane l then
+// adds, in storage order, the slots of the particles of its own cell
+// (c0x + l, row w) to that cell's partials.
 // Slow path (some neighbouring particle drifted): each thread visits the
 // particles currently in its cell with visit_cell.  Both paths use the same
 // per-particle function and the same per-cell values and add in the same order
@@ -188,20 +192,48 @@ __device__ __forceinline__ bool tile_drifted(const SimDev& S, int c0x, int c0y) 
     return __syncthreads_or(any) != 0;
 }
 
+// Per-warp staging of the chunks of a row: chunk c of [rb, re) holds storage
+// indices rb + 32c + lane; field f of it lands in buf[c % DEPTH][f][lane].
+template <int NF, int DEPTH>
+struct RowStage {
+    float (*buf)[NF][32];
+    const float* src[NF];
+    int rb, re, nch, lane;
+
+    __device__ __forceinline__ void issue(int c) {
+        const int q = rb + 32 * c + lane;
+        if (c < nch && q < re) {
+            #pragma unroll
+            for (int f = 0; f < NF; ++f)
+                if (src[f]) cp_async4(&buf[c % DEPTH][f][lane], src[f] + q);
+        }
+        cp_async_commit();
+    }
+    __device__ __forceinline__ void prime() {
+        #pragma unroll
+        for (int c = 0; c < DEPTH - 1; ++c) issue(c);
+    }
+    // Issue chunk c + DEPTH - 1 and wait until chunk c has landed.
+    __device__ __forceinline__ const float (*advance(int c))[32] {
+        issue(c + DEPTH - 1);
+        cp_async_wait<DEPTH - 1>();
+        return buf[c % DEPTH];
+    }
+};
+
 // Per-particle contributions of phase 1 to the 4 corners of its cell:
-// [m N_k, N_k (m vx), N_k (m vy)] (element.py:138-152, 170-189).
-template <bool REINIT>
-__device__ __forceinline__ void mass_contrib(const SimDev& S, int q, const CellGeo& g, float V0,
-                                             const float* __restrict__ rho, float* c) {
-    const float mp = REINIT ? fm(V0, rho[q]) : S.mass[q];
-    const float xi = natural(S.x[q], g.cx, g.rx);
-    const float eta = natural(S.y[q], g.cy, g.ry);
+// [m N_k, N_k (m vx), N_k (m vy)] (element.py:138-152, 170-189).  `m` is the
+// particle mass (V0 rho under the per-step volume set-up).
+__device__ __forceinline__ void mass_contrib(float x, float y, float vx, float vy, float m,
+                                             float cx, float rx, float cy, float ry, float* c) {
+    const float xi = natural(x, cx, rx);
+    const float eta = natural(y, cy, ry);
     float N[4];
     shape4(xi, eta, N);
-    const float pvx = fm(mp, S.vx[q]), pvy = fm(mp, S.vy[q]);
+    const float pvx = fm(m, vx), pvy = fm(m, vy);
     #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        c[k] = fm(mp, N[k]);
+        c[k] = fm(m, N[k]);
         c[4 + k] = fm(N[k], pvx);
         c[8 + k] = fm(N[k], pvy);
     }
@@ -250,35 +282,59 @@ __device__ __forceinline__ void force_cell_values(const SimDev& S, int cnt, cons
     }
 }
 
+// Staged inputs of one particle in phase 2.
+struct ForceIn {
+    float x, y, sxx, syy, szz, sxy, rho, vol;
+};
+
+enum ForceField { FF_X, FF_Y, FF_SXX, FF_SYY, FF_SZZ, FF_SXY, FF_RHO, FF_VOL, FF_N };
+
+__device__ __forceinline__ ForceIn force_in_global(const SimDev& S, int q, int parity,
+                                                   bool reinit) {
+    ForceIn in;
+    in.x = S.x[q];
+    in.y = S.y[q];
+    in.sxx = S.sxx[parity][q];
+    in.syy = S.syy[parity][q];
+    in.szz = S.szz[parity][q];
+    in.sxy = S.sxy[parity][q];
+    in.rho = S.rho[parity][q];
+    in.vol = reinit ? 0.0f : S.vol[parity][q];
+    return in;
+}
+
 // Per-particle work of phase 2: USF strain/volume/stress update (written back
-// when `write`) and the contributions [fint x, fint y, fext x, fext y] x 4
-// corners (element.py:236-303, 842-901).
+// when `write`) and the total-force contributions [f x, f y] x 4 corners,
+// internal plus external force (element.py:236-303, 842-901).
 template <bool USL, bool REINIT, bool TRAC>
-__device__ __forceinline__ void force_contrib(const SimDev& S, int q, const CellGeo& g, float V0,
-                                              float size0, const float nvx[4], const float nvy[4],
-                                              float dvol, int parity, float t, bool write,
-                                              float* c) {
+__device__ __forceinline__ void force_contrib(const SimDev& S, int q, const ForceIn& in, float cx,
+                                              float rx, float cy, float ry, float V0, float size0,
+                                              const float nvx[4], const float nvy[4], float dvol,
+                                              int parity, float t, bool write, float* c) {
     const int next = parity ^ 1;
-    const float xi = natural(S.x[q], g.cx, g.rx);
-    const float eta = natural(S.y[q], g.cy, g.ry);
-    float N[4], Gx[4], Gy[4];
-    shape4(xi, eta, N);
-    dshape4(xi, eta, g.rx, g.ry, Gx, Gy);
     PState p;
-    p.sxx = S.sxx[parity][q];
-    p.syy = S.syy[parity][q];
-    p.szz = S.szz[parity][q];
-    p.sxy = S.sxy[parity][q];
-    p.rho = S.rho[parity][q];
-    const float mp = REINIT ? fm(V0, p.rho) : S.mass[q];
-    float V = REINIT ? V0 : S.vol[parity][q];
     if (!USL) {
-        float r0, r1, r3;
-        strain_rate4(Gx, Gy, nvx, nvy, r0, r1, r3);
+        // state updated but not needed for the forces: loaded early, used late
         p.exx = S.exx[q];
         p.eyy = S.eyy[q];
         p.exy = S.exy[q];
         p.vsc = S.vsc[parity][q];
+    }
+    const float xi = natural(in.x, cx, rx);
+    const float eta = natural(in.y, cy, ry);
+    float N[4], Gx[4], Gy[4];
+    shape4(xi, eta, N);
+    dshape4(xi, eta, rx, ry, Gx, Gy);
+    p.sxx = in.sxx;
+    p.syy = in.syy;
+    p.szz = in.szz;
+    p.sxy = in.sxy;
+    p.rho = in.rho;
+    const float mp = REINIT ? fm(V0, p.rho) : S.mass[q];
+    float V = REINIT ? V0 : in.vol;
+    if (!USL) {
+        float r0, r1, r3;
+        strain_rate4(Gx, Gy, nvx, nvy, r0, r1, r3);
         const MatDev& M = S.mats[S.mat[q]];
         const float Ep = S.E ? S.E[q] : -1.0f;
         V = fm(V, strain_stress_update(M, Ep, S.dt, r0, r1, r3, dvol, p));
@@ -301,31 +357,32 @@ __device__ __forceinline__ void force_contrib(const SimDev& S, int q, const Cell
     for (int k = 0; k < 4; ++k) {
         const float fx = fa(fm(Gx[k], p.sxx), fm(Gy[k], p.sxy));
         const float fy = fa(fm(Gy[k], p.syy), fm(Gx[k], p.sxy));
-        c[k] = fm(nV, fx);
-        c[4 + k] = fm(nV, fy);
-        c[8 + k] = fm(N[k], mgx);
-        c[12 + k] = fm(N[k], mgy);
+        c[k] = fa(fm(nV, fx), fm(N[k], mgx));
+        c[4 + k] = fa(fm(nV, fy), fm(N[k], mgy));
     }
-    add_traction<TRAC>(S, q, t, V, REINIT ? size0 : (S.psize ? S.psize[q] : 1.0f), N, c + 8, c + 12);
+    add_traction<TRAC>(S, q, t, V, REINIT ? size0 : (S.psize ? S.psize[q] : 1.0f), N, c, c + 4);
 }
 
-// Fast-path accumulation of one chunk: lane `lx` adds, in storage order, the
-// slots of its cell's particles that lie in [base, base + 32) to s_c[.][tid].
+// Fast-path accumulation of one chunk [base, min(base + 32, re)) of row `row`
+// holding cells c_lo .. c_hi of the row: the warp's lanes share the
+// (cell, quantity) pairs, and each pair adds its cell's slots in storage order.
+constexpr int SLOT_STRIDE = 33;
+
 template <int NQ>
-__device__ __forceinline__ void add_chunk(float (*s_c)[TILE_THREADS], const float (*slot)[32],
-                                          int tid, int cb, int ce, int base) {
-    const int lo = max(cb, base), hi = min(ce, base + 32);
-    if (lo >= hi) return;
-    float acc[NQ];
-    #pragma unroll
-    for (int k = 0; k < NQ; ++k) acc[k] = s_c[k][tid];
+__device__ __forceinline__ void accumulate_chunk(float (*s_c)[SC_STRIDE],
+                                                 const float (*slot)[SLOT_STRIDE], const int* cs,
+                                                 int base, int end, int c_lo, int c_hi, int lane,
+                                                 int row) {
+    const int npairs = (c_hi - c_lo + 1) * NQ;
     #pragma unroll 1
-    for (int qq = lo; qq < hi; ++qq) {
-        #pragma unroll
-        for (int k = 0; k < NQ; ++k) acc[k] = fa(acc[k], slot[k][qq - base]);
+    for (int p = lane; p < npairs; p += 32) {
+        const int cell = c_lo + p / NQ, k = p % NQ;
+        const int lo = max(cs[cell], base), hi = min(cs[cell + 1], end);
+        float acc = s_c[k][row * 32 + cell];
+        #pragma unroll 1
+        for (int qq = lo; qq < hi; ++qq) acc = fa(acc, slot[k][qq - base]);
+        s_c[k][row * 32 + cell] = acc;
     }
-    #pragma unroll
-    for (int k = 0; k < NQ; ++k) s_c[k][tid] = acc[k];
 }
 
 // ---------------------------------------------------------------------------
@@ -334,13 +391,17 @@ __device__ __forceinline__ void add_chunk(float (*s_c)[TILE_THREADS], const floa
 //   P2G of mass and momentum (element.py:122-189), nodal velocity
 //   (element.py:191-202), velocity constraints (element.py:331-334).
 // ---------------------------------------------------------------------------
+constexpr int K1_DEPTH = 4;
+constexpr int K1_NF = 5;   // x, y, vx, vy, rho (solve_jit) or mass (solve)
+
 template <bool REINIT>
 __global__ void __launch_bounds__(TILE_THREADS, 2)
 k_nodal_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
                    Control* __restrict__ ctl) {
     constexpr int NQ = 12;
-    __shared__ float s_c[NQ][TILE_THREADS];            // [m, px, py] x corner, per cell
-    __shared__ float s_slot[TILE_CY][NQ][32];          // per-warp particle contributions
+    __shared__ float s_c[NQ][SC_STRIDE];               // [m, px, py] x corner, per cell
+    __shared__ float s_slot[TILE_CY][NQ][SLOT_STRIDE]; // per-warp particle contributions
+    __shared__ float s_stage[TILE_CY][K1_DEPTH][K1_NF][32];
     __shared__ int s_cs[TILE_CY][33];
     __shared__ float s_V0[TILE_CY][32];
     __shared__ TileGeo G;
@@ -350,6 +411,9 @@ k_nodal_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__ ti
     const int c0x = T.y * TILE_NX - 1, c0y = T.z * TILE_NY - 1;
     const int ci = c0x + lx, cj = c0y + ly;
     const float* __restrict__ rho = S.rho[parity];
+    const bool node_ok = lx < TILE_NX && ly < TILE_NY && c0x + 1 + lx <= S.nx && c0y + 1 + ly <= S.ny;
+    const int node = (c0y + 1 + ly) * (S.nx + 1) + c0x + 1 + lx;
+    const uint16_t ncons = node_ok ? S.ncons[node] : 0;   // node-phase input, fetched early
     #pragma unroll
     for (int k = 0; k < NQ; ++k) s_c[k][tid] = 0.0f;
     load_row_starts(S, c0x, cj, s_cs[ly], lx);
@@ -360,22 +424,30 @@ k_nodal_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__ ti
         const int* cs = s_cs[ly];
         const int rb = cs[0], re = cs[32];
         const int cb = cs[lx], ce = cs[lx + 1];
+        RowStage<K1_NF, K1_DEPTH> st{s_stage[ly], {S.x, S.y, S.vx, S.vy, REINIT ? rho : S.mass},
+                                     rb, re, (re - rb + 31) / 32, lx};
+        st.prime();
         if (REINIT) s_V0[ly][lx] = ce > cb ? fdv(S.vol_el, (float)(ce - cb)) : 0.0f;
+        const float cy = G.cy[ly + 1], ry = G.ry[ly + 1];   // row geometry (warp-uniform)
         __syncwarp();
-        const int kr = ly + 1;
         #pragma unroll 1
-        for (int base = rb; base < re; base += 32) {
-            const int q = base + lx;
+        for (int c = 0; c < st.nch; ++c) {
+            const float (*b)[32] = st.advance(c);
+            const int base = rb + 32 * c, q = base + lx, end = min(base + 32, re);
+            int l = -1;
             if (q < re) {
-                const int l = cell_of(cs, 31, q);
-                const CellGeo g = geo_of(G, l + 1, kr);
-                float c[NQ];
-                mass_contrib<REINIT>(S, q, g, REINIT ? s_V0[ly][l] : 0.0f, rho, c);
+                l = cell_of(cs, 31, q);
+                const float m = REINIT ? fm(s_V0[ly][l], b[4][lx]) : b[4][lx];
+                float cc[NQ];
+                mass_contrib(b[0][lx], b[1][lx], b[2][lx], b[3][lx], m, G.cx[l + 1], G.rx[l + 1],
+                             cy, ry, cc);
                 #pragma unroll
-                for (int k = 0; k < NQ; ++k) s_slot[ly][k][lx] = c[k];
+                for (int k = 0; k < NQ; ++k) s_slot[ly][k][lx] = cc[k];
             }
+            const int c_lo = __shfl_sync(0xffffffffu, l, 0);
+            const int c_hi = __shfl_sync(0xffffffffu, l, end - 1 - base);
             __syncwarp();
-            add_chunk<NQ>(s_c, s_slot[ly], tid, cb, ce, base);
+            accumulate_chunk<NQ>(s_c, s_slot[ly], cs, base, end, c_lo, c_hi, lx, ly);
             __syncwarp();
         }
     } else if (ci >= 0 && ci < S.nx && cj >= 0 && cj < S.ny) {
@@ -386,59 +458,56 @@ k_nodal_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__ ti
             if (cnt) V0 = fdv(S.vol_el, (float)cnt);
         }
         visit_cell(S, ci, cj, g, [&](int q) {
-            float c[NQ];
-            mass_contrib<REINIT>(S, q, g, V0, rho, c);
+            const float m = REINIT ? fm(V0, rho[q]) : S.mass[q];
+            float cc[NQ];
+            mass_contrib(S.x[q], S.y[q], S.vx[q], S.vy[q], m, g.cx, g.rx, g.cy, g.ry, cc);
             #pragma unroll
-            for (int k = 0; k < NQ; ++k) s_c[k][tid] = fa(s_c[k][tid], c[k]);
+            for (int k = 0; k < NQ; ++k) s_c[k][tid] = fa(s_c[k][tid], cc[k]);
         });
     }
     __syncthreads();
-    if (lx < TILE_NX && ly < TILE_NY) {
-        const int I = c0x + 1 + lx, J = c0y + 1 + ly;
-        if (I <= S.nx && J <= S.ny) {
-            const int n = J * (S.nx + 1) + I;
-            const float mass = node_sum(s_c + 0, tid);
-            const float pxn = flush(node_sum(s_c + 4, tid));
-            const float pyn = flush(node_sum(s_c + 8, tid));
-            float vx, vy;
-            if (mass == 0.0f) {
-                vx = S.nvbx[n];
-                vy = S.nvby[n];
-            } else {
-                vx = fdv(pxn, mass);
-                vy = fdv(pyn, mass);
-            }
-            vx = flush(vx);
-            vy = flush(vy);
-            apply_constraint(S, S.ncons[n], vx, vy, nullptr, nullptr);
-            S.nm[n] = mass;
-            S.nvax[n] = vx;
-            S.nvay[n] = vy;
+    if (node_ok) {
+        const float mass = node_sum(s_c + 0, tid);
+        const float pxn = flush(node_sum(s_c + 4, tid));
+        const float pyn = flush(node_sum(s_c + 8, tid));
+        float vx, vy;
+        if (mass == 0.0f) {
+            vx = S.nvbx[node];
+            vy = S.nvby[node];
+        } else {
+            vx = fdv(pxn, mass);
+            vy = fdv(pyn, mass);
         }
+        vx = flush(vx);
+        vy = flush(vy);
+        apply_constraint(S, ncons, vx, vy, nullptr, nullptr);
+        S.nm[node] = mass;
+        S.nvax[node] = vx;
+        S.nvay[node] = vy;
     }
 }
 
 // Nodal update shared by both schemes: concentrated forces (element.py:270-284),
 // a = nan_to_num(f/m), v += a dt, constraints, flush (element.py:305-329).
-__device__ __forceinline__ void nodal_update(const SimDev& S, int n, float t, float fix, float fiy,
-                                             float fex, float fey, float v0x, float v0y) {
+// (fx, fy) is the summed internal plus external force of the particles.
+__device__ __forceinline__ void nodal_update(const SimDev& S, int n, float t, float fx, float fy,
+                                             float v0x, float v0y, float mass, uint16_t ncons) {
     if (S.cnf_ptr) {
         const int b = S.cnf_ptr[n], e = S.cnf_ptr[n + 1];
         #pragma unroll 1
         for (int k = b; k < e; ++k) {
             const float val = fm(fn_value(S, S.cnf_fn[k], t), S.cnf_val[k]);
-            if (S.cnf_dir[k] == 0) fex = fa(fex, val);
-            else fey = fa(fey, val);
+            if (S.cnf_dir[k] == 0) fx = fa(fx, val);
+            else fy = fa(fy, val);
         }
     }
-    const float tx = fa(fa(fix, fex), 0.0f);
-    const float ty = fa(fa(fiy, fey), 0.0f);
-    const float mass = S.nm[n];
+    const float tx = fa(fx, 0.0f);   // + f_damp (zero, node.py:71)
+    const float ty = fa(fy, 0.0f);
     float ax = nan_to_num(fdv(tx, mass));
     float ay = nan_to_num(fdv(ty, mass));
     float vx = fa(v0x, fm(ax, S.dt));
     float vy = fa(v0y, fm(ay, S.dt));
-    apply_constraint(S, S.ncons[n], vx, vy, &ax, &ay);
+    apply_constraint(S, ncons, vx, vy, &ax, &ay);
     S.nvbx[n] = flush(vx);
     S.nvby[n] = flush(vy);
     S.nax[n] = flush(ax);
@@ -455,14 +524,16 @@ __device__ __forceinline__ void nodal_update(const SimDev& S, int n, float t, fl
 // ---------------------------------------------------------------------------
 constexpr int NV_W = TILE_CX + 1;   // node tile of the R cells: [c0x, c0x+33) x [c0y, c0y+17)
 constexpr int NV_H = TILE_CY + 1;
+constexpr int K2_DEPTH = 2;
 
 template <bool USL, bool REINIT, bool TRAC>
 __global__ void __launch_bounds__(TILE_THREADS, 2)
 k_forces(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
          Control* __restrict__ ctl) {
-    constexpr int NQ = 16;
-    __shared__ float s_c[NQ][TILE_THREADS];            // [fint x, fint y, fext x, fext y] x corner
-    __shared__ float s_slot[TILE_CY][NQ][32];
+    constexpr int NQ = 8;
+    __shared__ float s_c[NQ][SC_STRIDE];               // [f x, f y] x corner, per cell
+    __shared__ float s_slot[TILE_CY][NQ][SLOT_STRIDE];
+    __shared__ float s_stage[TILE_CY][K2_DEPTH][FF_N][32];
     __shared__ int s_cs[TILE_CY][33];
     __shared__ float s_V0[TILE_CY][32], s_size0[TILE_CY][32], s_dvol[TILE_CY][32];
     __shared__ float s_vx[NV_W * NV_H], s_vy[NV_W * NV_H];
@@ -474,6 +545,11 @@ k_forces(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
     const int tid = threadIdx.x, lx = tid & (TILE_CX - 1), ly = tid / TILE_CX;
     const int c0x = T.y * TILE_NX - 1, c0y = T.z * TILE_NY - 1;
     const int ci = c0x + lx, cj = c0y + ly;
+    const bool node_ok = lx < TILE_NX && ly < TILE_NY && c0x + 1 + lx <= S.nx && c0y + 1 + ly <= S.ny;
+    const int node = (c0y + 1 + ly) * (S.nx + 1) + c0x + 1 + lx;
+    // node-phase inputs, fetched early
+    const float nmass = node_ok ? S.nm[node] : 0.0f;
+    const uint16_t ncons = node_ok ? S.ncons[node] : 0;
     #pragma unroll
     for (int k = 0; k < NQ; ++k) s_c[k][tid] = 0.0f;
     load_row_starts(S, c0x, cj, s_cs[ly], lx);
@@ -505,6 +581,11 @@ k_forces(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
         const int* cs = s_cs[ly];
         const int rb = cs[0], re = cs[32];
         const int cb = cs[lx], ce = cs[lx + 1];
+        RowStage<FF_N, K2_DEPTH> st{s_stage[ly],
+                                    {S.x, S.y, S.sxx[parity], S.syy[parity], S.szz[parity],
+                                     S.sxy[parity], S.rho[parity], REINIT ? nullptr : S.vol[parity]},
+                                    rb, re, (re - rb + 31) / 32, lx};
+        st.prime();
         {
             // per-cell values, one lane per cell of the row
             float nvx[4], nvy[4], V0, size0, dvol;
@@ -515,24 +596,37 @@ k_forces(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
             s_size0[ly][lx] = size0;
             s_dvol[ly][lx] = dvol;
         }
+        const float cy = G.cy[ly + 1], ry = G.ry[ly + 1];   // row geometry (warp-uniform)
         __syncwarp();
-        const int kr = ly + 1;
         #pragma unroll 1
-        for (int base = rb; base < re; base += 32) {
-            const int q = base + lx;
+        for (int c = 0; c < st.nch; ++c) {
+            const float (*b)[32] = st.advance(c);
+            const int base = rb + 32 * c, q = base + lx, end = min(base + 32, re);
+            int l = -1;
             if (q < re) {
-                const int l = cell_of(cs, 31, q);
+                l = cell_of(cs, 31, q);
                 float nvx[4], nvy[4];
                 if (!USL) cell_velocities(l, ly, nvx, nvy);
-                float c[NQ];
-                force_contrib<USL, REINIT, TRAC>(S, q, geo_of(G, l + 1, kr), s_V0[ly][l],
-                                                 s_size0[ly][l], nvx, nvy, s_dvol[ly][l], parity,
-                                                 t, l >= 1 && ly >= 1, c);
+                ForceIn in;
+                in.x = b[FF_X][lx];
+                in.y = b[FF_Y][lx];
+                in.sxx = b[FF_SXX][lx];
+                in.syy = b[FF_SYY][lx];
+                in.szz = b[FF_SZZ][lx];
+                in.sxy = b[FF_SXY][lx];
+                in.rho = b[FF_RHO][lx];
+                in.vol = REINIT ? 0.0f : b[FF_VOL][lx];
+                float cc[NQ];
+                force_contrib<USL, REINIT, TRAC>(S, q, in, G.cx[l + 1], G.rx[l + 1], cy, ry,
+                                                 s_V0[ly][l], s_size0[ly][l], nvx, nvy,
+                                                 s_dvol[ly][l], parity, t, l >= 1 && ly >= 1, cc);
                 #pragma unroll
-                for (int k = 0; k < NQ; ++k) s_slot[ly][k][lx] = c[k];
+                for (int k = 0; k < NQ; ++k) s_slot[ly][k][lx] = cc[k];
             }
+            const int c_lo = __shfl_sync(0xffffffffu, l, 0);
+            const int c_hi = __shfl_sync(0xffffffffu, l, end - 1 - base);
             __syncwarp();
-            add_chunk<NQ>(s_c, s_slot[ly], tid, cb, ce, base);
+            accumulate_chunk<NQ>(s_c, s_slot[ly], cs, base, end, c_lo, c_hi, lx, ly);
             __syncwarp();
         }
     } else if (ci >= 0 && ci < S.nx && cj >= 0 && cj < S.ny) {
@@ -543,20 +637,19 @@ k_forces(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
         force_cell_values<USL, REINIT>(S, cnt, g, nvx, nvy, V0, size0, dvol);
         const bool own = lx >= 1 && ly >= 1;
         visit_cell(S, ci, cj, g, [&](int q) {
-            float c[NQ];
-            force_contrib<USL, REINIT, TRAC>(S, q, g, V0, size0, nvx, nvy, dvol, parity, t, own, c);
+            float cc[NQ];
+            force_contrib<USL, REINIT, TRAC>(S, q, force_in_global(S, q, parity, REINIT), g.cx,
+                                             g.rx, g.cy, g.ry, V0, size0, nvx, nvy, dvol, parity,
+                                             t, own, cc);
             #pragma unroll
-            for (int k = 0; k < NQ; ++k) s_c[k][tid] = fa(s_c[k][tid], c[k]);
+            for (int k = 0; k < NQ; ++k) s_c[k][tid] = fa(s_c[k][tid], cc[k]);
         });
     }
     __syncthreads();
-    if (lx < TILE_NX && ly < TILE_NY) {
-        const int I = c0x + 1 + lx, J = c0y + 1 + ly;
-        if (I <= S.nx && J <= S.ny) {
-            const int a = (ly + 1) * NV_W + lx + 1;   // node (I, J) in the node tile
-            nodal_update(S, J * (S.nx + 1) + I, t, node_sum(s_c + 0, tid), node_sum(s_c + 4, tid),
-                         node_sum(s_c + 8, tid), node_sum(s_c + 12, tid), s_vx[a], s_vy[a]);
-        }
+    if (node_ok) {
+        const int a = (ly + 1) * NV_W + lx + 1;   // node (I, J) in the node tile
+        nodal_update(S, node, t, node_sum(s_c + 0, tid), node_sum(s_c + 4, tid), s_vx[a], s_vy[a],
+                     nmass, ncons);
     }
 }
 
@@ -565,9 +658,10 @@ k_forces(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
 // a_hat = sum N a_i, v_p = v_hat or v_p + a_hat dt, x_p += v_hat dt.  USL adds
 // the strain/volume/stress update at the step's natural coordinates with the
 // updated nodal velocities (scheme.py:127-133).  Warp w streams the particles
-// of the owned sort-cells of row w + 1 (one particle per lane) against a
-// shared-memory tile of the nodal velocity and acceleration, and records per
-// sort-cell whether a particle now lies in another cell (the drift flags).
+// of the owned sort-cells of row w + 1 (one particle per lane, staged with
+// cp.async) against a shared-memory tile of the nodal velocity and
+// acceleration, and records per sort-cell whether a particle now lies in
+// another cell (the drift flags).
 // ---------------------------------------------------------------------------
 constexpr int G_W = TILE_CX + 2;   // node tile [c0x, c0x+34) x [c0y, c0y+18)
 constexpr int G_H = TILE_CY + 2;
@@ -583,11 +677,22 @@ __device__ __forceinline__ int moved_axis(float x, const float* lo, const float*
     return locate_axis(x, h, n);
 }
 
+enum G2PField { GF_X, GF_Y, GF_VX, GF_VY, GF_SXX, GF_SYY, GF_SZZ, GF_SXY, GF_EXX, GF_EYY,
+                GF_EXY, GF_RHO, GF_VSC, GF_VOL, GF_N };
+
+template <bool USL>
+struct G2PStage {
+    static constexpr int NF = USL ? GF_N : 4;
+    static constexpr int DEPTH = USL ? 2 : 4;
+};
+
 template <bool USL, bool REINIT>
 __global__ void __launch_bounds__(TILE_THREADS, 2)
 k_particle_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
                       Control* __restrict__ ctl) {
+    constexpr int NF = G2PStage<USL>::NF, DEPTH = G2PStage<USL>::DEPTH;
     __shared__ float s_vx[G_W * G_H], s_vy[G_W * G_H], s_ax[G_W * G_H], s_ay[G_W * G_H];
+    __shared__ float s_stage[TILE_CY][DEPTH][NF][32];
     __shared__ int s_cs[TILE_CY][33];
     __shared__ int s_sf[TILE_CY][32];     // drift flag of the sort-cell at the start of the step
     __shared__ int s_flag[TILE_CY][32];   // drift flag after this step
@@ -599,6 +704,39 @@ k_particle_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__
     const int tid = threadIdx.x, lane = tid & 31, w = tid / 32;
     const int c0x = T.y * TILE_NX - 1, c0y = T.z * TILE_NY - 1;
     const float dt = S.dt;
+    // row w + 1 of the tile: owned sort-cells c0x+1 .. c0x+31 -> starts cs[0..31]
+    const int sj = c0y + 1 + w;
+    const bool row_ok = w < TILE_NY && sj < S.ny;
+    int rb = 0, re = 0;
+    if (row_ok) {
+        const int col = min(c0x + 1 + lane, S.nx);
+        s_cs[w][lane] = S.cstart[sj * S.nx + col];
+        s_sf[w][lane] = col < S.nx ? S.cflag[sj * S.nx + col] : 0;
+    }
+    s_flag[w][lane] = 0;
+    __syncwarp();
+    if (row_ok) {
+        rb = s_cs[w][0];
+        re = s_cs[w][31];
+    }
+    RowStage<NF, DEPTH> st{s_stage[w], {}, rb, re, (re - rb + 31) / 32, lane};
+    st.src[GF_X] = S.x;
+    st.src[GF_Y] = S.y;
+    st.src[GF_VX] = S.vx;
+    st.src[GF_VY] = S.vy;
+    if constexpr (USL) {
+        st.src[GF_SXX] = S.sxx[parity];
+        st.src[GF_SYY] = S.syy[parity];
+        st.src[GF_SZZ] = S.szz[parity];
+        st.src[GF_SXY] = S.sxy[parity];
+        st.src[GF_EXX] = S.exx;
+        st.src[GF_EYY] = S.eyy;
+        st.src[GF_EXY] = S.exy;
+        st.src[GF_RHO] = S.rho[parity];
+        st.src[GF_VSC] = S.vsc[parity];
+        st.src[GF_VOL] = REINIT ? nullptr : S.vol[parity];
+    }
+    st.prime();
     if (tid == 0) s_status = 0;
     for (int idx = tid; idx < G_W * G_H; idx += TILE_THREADS) {
         const int I = c0x + idx % G_W, J = c0y + idx / G_W;
@@ -616,131 +754,121 @@ k_particle_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__
         s_ay[idx] = ay;
     }
     build_geo(S, c0x, c0y, G);
-    // row w + 1 of the tile: owned sort-cells c0x+1 .. c0x+31 -> starts cs[0..31]
-    const int sj = c0y + 1 + w;
-    const bool row_ok = w < TILE_NY && sj < S.ny;
-    if (row_ok) {
-        const int col = min(c0x + 1 + lane, S.nx);
-        s_cs[w][lane] = S.cstart[sj * S.nx + col];
-        s_sf[w][lane] = col < S.nx ? S.cflag[sj * S.nx + col] : 0;
-    }
-    s_flag[w][lane] = 0;
     __syncthreads();
     int status = 0;
-    if (row_ok) {
-        const int* cs = s_cs[w];
-        const int rb = cs[0], re = cs[31];
-        #pragma unroll 1
-        for (int base = rb; base < re; base += 32) {
-            const int q = base + lane;
-            if (q >= re) continue;
-            const int l = cell_of(cs, 30, q);   // sort-cell c0x + 1 + l
-            const int si = c0x + 1 + l;
-            const float x = S.x[q], y = S.y[q];
-            int ci = si, cj = sj;
-            if (s_sf[w][l]) {
-                ci = locate_axis(x, S.hx, S.nx);
-                cj = locate_axis(y, S.hy, S.ny);
-                if (ci < 0 || ci >= S.nx || cj < 0 || cj >= S.ny) {
-                    status |= ST_OUT_OF_MESH;
-                    s_flag[w][l] = 1;
-                    continue;
-                }
-            }
-            const int kc = ci - c0x + 1, kr = cj - c0y + 1;   // geometry table indices
-            const bool in_tile = kc >= 0 && kc < GEO_C && kr >= 0 && kr < GEO_R;
-            const CellGeo g = in_tile ? geo_of(G, kc, kr) : cell_geo(ci, cj, S.hx, S.hy);
-            float nvx[4], nvy[4], nax[4], nay[4];
-            const int li = ci - c0x, lj = cj - c0y;
-            if (li >= 0 && li + 1 < G_W && lj >= 0 && lj + 1 < G_H) {
-                const int a = lj * G_W + li;
-                const int id[4] = {a, a + 1, a + G_W + 1, a + G_W};
-                #pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    nvx[k] = s_vx[id[k]];
-                    nvy[k] = s_vy[id[k]];
-                    nax[k] = s_ax[id[k]];
-                    nay[k] = s_ay[id[k]];
-                }
-            } else {
-                int ids[4];
-                cell_nodes(S, ci, cj, ids);
-                #pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    nvx[k] = S.nvbx[ids[k]];
-                    nvy[k] = S.nvby[ids[k]];
-                    nax[k] = S.nax[ids[k]];
-                    nay[k] = S.nay[ids[k]];
-                }
-            }
-            const float xi = natural(x, g.cx, g.rx);
-            const float eta = natural(y, g.cy, g.ry);
-            float N[4];
-            shape4(xi, eta, N);
-            const float vhx = dot4(N, nvx), vhy = dot4(N, nvy);
-            float vx, vy;
-            if (S.velocity_update) {
-                vx = vhx;
-                vy = vhy;
-            } else {
-                vx = fa(S.vx[q], fm(dot4(N, nax), dt));
-                vy = fa(S.vy[q], fm(dot4(N, nay), dt));
-            }
-            const float xn = fa(x, fm(vhx, dt)), yn = fa(y, fm(vhy, dt));
-            S.x[q] = xn;
-            S.y[q] = yn;
-            S.vx[q] = vx;
-            S.vy[q] = vy;
-            if (USL) {
-                float Gcx[4], Gcy[4], c0, c1, c3;
-                dshape4(0.0f, 0.0f, g.rx, g.ry, Gcx, Gcy);
-                strain_rate4(Gcx, Gcy, nvx, nvy, c0, c1, c3);
-                const float dvol = fm(dt, fa(c0, c1));
-                float Gx[4], Gy[4], r0, r1, r3;
-                dshape4(xi, eta, g.rx, g.ry, Gx, Gy);
-                strain_rate4(Gx, Gy, nvx, nvy, r0, r1, r3);
-                PState p;
-                p.sxx = S.sxx[parity][q];
-                p.syy = S.syy[parity][q];
-                p.szz = S.szz[parity][q];
-                p.sxy = S.sxy[parity][q];
-                p.exx = S.exx[q];
-                p.eyy = S.eyy[q];
-                p.exy = S.exy[q];
-                p.rho = S.rho[parity][q];
-                p.vsc = S.vsc[parity][q];
-                const MatDev& M = S.mats[S.mat[q]];
-                const float Ep = S.E ? S.E[q] : -1.0f;
-                const float f = strain_stress_update(M, Ep, dt, r0, r1, r3, dvol, p);
-                S.sxx[next][q] = p.sxx;
-                S.syy[next][q] = p.syy;
-                S.szz[next][q] = p.szz;
-                S.sxy[next][q] = p.sxy;
-                S.exx[q] = p.exx;
-                S.eyy[q] = p.eyy;
-                S.exy[q] = p.exy;
-                S.rho[next][q] = p.rho;
-                S.vsc[next][q] = p.vsc;
-                if (!REINIT) S.vol[next][q] = fm(S.vol[parity][q], f);
-            }
-            int ni, nj;
-            if (in_tile) {
-                ni = moved_axis(xn, G.x0, G.x1, kc, GEO_C, ci, S.hx, S.nx);
-                nj = moved_axis(yn, G.y0, G.y1, kr, GEO_R, cj, S.hy, S.ny);
-            } else {
-                ni = locate_axis(xn, S.hx, S.nx);
-                nj = locate_axis(yn, S.hy, S.ny);
-            }
-            if (ni < 0 || ni >= S.nx || nj < 0 || nj >= S.ny) {
+    const int* cs = s_cs[w];
+    #pragma unroll 1
+    for (int c = 0; c < st.nch; ++c) {
+        const float (*b)[32] = st.advance(c);
+        const int q = rb + 32 * c + lane;
+        if (q >= re) continue;
+        const int l = cell_of(cs, 30, q);   // sort-cell c0x + 1 + l
+        const int si = c0x + 1 + l;
+        const float x = b[GF_X][lane], y = b[GF_Y][lane];
+        int ci = si, cj = sj;
+        if (s_sf[w][l]) {
+            ci = locate_axis(x, S.hx, S.nx);
+            cj = locate_axis(y, S.hy, S.ny);
+            if (ci < 0 || ci >= S.nx || cj < 0 || cj >= S.ny) {
                 status |= ST_OUT_OF_MESH;
                 s_flag[w][l] = 1;
-            } else {
-                const int d = max(abs(ni - si), abs(nj - sj));
-                if (d >= 1) s_flag[w][l] = 1;
-                if (d > 1) status |= ST_DRIFT_VIOLATION;
+                continue;
             }
         }
+        const int kc = ci - c0x + 1, kr = cj - c0y + 1;   // geometry table indices
+        const bool in_tile = kc >= 0 && kc < GEO_C && kr >= 0 && kr < GEO_R;
+        const CellGeo g = in_tile ? geo_of(G, kc, kr) : cell_geo(ci, cj, S.hx, S.hy);
+        float nvx[4], nvy[4], nax[4], nay[4];
+        const int li = ci - c0x, lj = cj - c0y;
+        if (li >= 0 && li + 1 < G_W && lj >= 0 && lj + 1 < G_H) {
+            const int a = lj * G_W + li;
+            const int id[4] = {a, a + 1, a + G_W + 1, a + G_W};
+            #pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                nvx[k] = s_vx[id[k]];
+                nvy[k] = s_vy[id[k]];
+                nax[k] = s_ax[id[k]];
+                nay[k] = s_ay[id[k]];
+            }
+        } else {
+            int ids[4];
+            cell_nodes(S, ci, cj, ids);
+            #pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                nvx[k] = S.nvbx[ids[k]];
+                nvy[k] = S.nvby[ids[k]];
+                nax[k] = S.nax[ids[k]];
+                nay[k] = S.nay[ids[k]];
+            }
+        }
+        const float xi = natural(x, g.cx, g.rx);
+        const float eta = natural(y, g.cy, g.ry);
+        float N[4];
+        shape4(xi, eta, N);
+        const float vhx = dot4(N, nvx), vhy = dot4(N, nvy);
+        float vx, vy;
+        if (S.velocity_update) {
+            vx = vhx;
+            vy = vhy;
+        } else {
+            vx = fa(b[GF_VX][lane], fm(dot4(N, nax), dt));
+            vy = fa(b[GF_VY][lane], fm(dot4(N, nay), dt));
+        }
+        const float xn = fa(x, fm(vhx, dt)), yn = fa(y, fm(vhy, dt));
+        S.x[q] = xn;
+        S.y[q] = yn;
+        S.vx[q] = vx;
+        S.vy[q] = vy;
+        if constexpr (USL) {
+            float Gcx[4], Gcy[4], c0, c1, c3;
+            dshape4(0.0f, 0.0f, g.rx, g.ry, Gcx, Gcy);
+            strain_rate4(Gcx, Gcy, nvx, nvy, c0, c1, c3);
+            const float dvol = fm(dt, fa(c0, c1));
+            float Gx[4], Gy[4], r0, r1, r3;
+            dshape4(xi, eta, g.rx, g.ry, Gx, Gy);
+            strain_rate4(Gx, Gy, nvx, nvy, r0, r1, r3);
+            PState p;
+            p.sxx = b[GF_SXX][lane];
+            p.syy = b[GF_SYY][lane];
+            p.szz = b[GF_SZZ][lane];
+            p.sxy = b[GF_SXY][lane];
+            p.exx = b[GF_EXX][lane];
+            p.eyy = b[GF_EYY][lane];
+            p.exy = b[GF_EXY][lane];
+            p.rho = b[GF_RHO][lane];
+            p.vsc = b[GF_VSC][lane];
+            const MatDev& M = S.mats[S.mat[q]];
+            const float Ep = S.E ? S.E[q] : -1.0f;
+            const float f = strain_stress_update(M, Ep, dt, r0, r1, r3, dvol, p);
+            S.sxx[next][q] = p.sxx;
+            S.syy[next][q] = p.syy;
+            S.szz[next][q] = p.szz;
+            S.sxy[next][q] = p.sxy;
+            S.exx[q] = p.exx;
+            S.eyy[q] = p.eyy;
+            S.exy[q] = p.exy;
+            S.rho[next][q] = p.rho;
+            S.vsc[next][q] = p.vsc;
+            if (!REINIT) S.vol[next][q] = fm(b[GF_VOL][lane], f);
+        }
+        int ni, nj;
+        if (in_tile) {
+            ni = moved_axis(xn, G.x0, G.x1, kc, GEO_C, ci, S.hx, S.nx);
+            nj = moved_axis(yn, G.y0, G.y1, kr, GEO_R, cj, S.hy, S.ny);
+        } else {
+            ni = locate_axis(xn, S.hx, S.nx);
+            nj = locate_axis(yn, S.hy, S.ny);
+        }
+        if (ni < 0 || ni >= S.nx || nj < 0 || nj >= S.ny) {
+            status |= ST_OUT_OF_MESH;
+            s_flag[w][l] = 1;
+        } else {
+            const int d = max(abs(ni - si), abs(nj - sj));
+            if (d >= 1) s_flag[w][l] = 1;
+            if (d > 1) status |= ST_DRIFT_VIOLATION;
+        }
     }
+    cp_async_wait<0>();
     __syncwarp();
     if (row_ok && lane < TILE_NX) {
         const int si = c0x + 1 + lane;
@@ -770,18 +898,42 @@ k_particle_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__
 // ---------------------------------------------------------------------------
 // Launchers
 // ---------------------------------------------------------------------------
+// The step kernels use 50-110 KB of shared memory per CTA and are sized for two
+// CTAs per SM: ask for the largest shared-memory carveout once per kernel.
+template <class K>
+static void prefer_shared(K kernel) {
+    static bool done = false;
+    if (!done) {
+        cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
+        done = true;
+    }
+}
+
+template <bool REINIT>
+static void nodal_kinematics(const SimDev& S, const int4* tiles, int ntiles, Control* ctl,
+                             cudaStream_t s) {
+    prefer_shared(k_nodal_kinematics<REINIT>);
+    k_nodal_kinematics<REINIT><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl);
+}
+
 cudaError_t launch_nodal_kinematics(const StepConfig& c, const SimDev& S, const int4* tiles,
                                     int ntiles, Control* ctl, cudaStream_t s) {
-    if (c.reinit) k_nodal_kinematics<true><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl);
-    else k_nodal_kinematics<false><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl);
+    if (c.reinit) nodal_kinematics<true>(S, tiles, ntiles, ctl, s);
+    else nodal_kinematics<false>(S, tiles, ntiles, ctl, s);
     return cudaGetLastError();
 }
 
 template <bool USL, bool REINIT>
 static void forces_trac(bool trac, const SimDev& S, const int4* tiles, int ntiles, Control* ctl,
                         cudaStream_t s) {
-    if (trac) k_forces<USL, REINIT, true><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl);
-    else k_forces<USL, REINIT, false><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl);
+    if (trac) {
+        prefer_shared(k_forces<USL, REINIT, true>);
+        k_forces<USL, REINIT, true><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl);
+    } else {
+        prefer_shared(k_forces<USL, REINIT, false>);
+        k_forces<USL, REINIT, false><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl);
+    }
 }
 
 cudaError_t launch_forces(const StepConfig& c, const SimDev& S, const int4* tiles, int ntiles,
@@ -796,14 +948,21 @@ cudaError_t launch_forces(const StepConfig& c, const SimDev& S, const int4* tile
     return cudaGetLastError();
 }
 
+template <bool USL, bool REINIT>
+static void particle_kinematics(const SimDev& S, const int4* tiles, int ntiles, Control* ctl,
+                                cudaStream_t s) {
+    prefer_shared(k_particle_kinematics<USL, REINIT>);
+    k_particle_kinematics<USL, REINIT><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl);
+}
+
 cudaError_t launch_particle_kinematics(const StepConfig& c, const SimDev& S, const int4* tiles,
                                        int ntiles, Control* ctl, cudaStream_t s) {
     if (c.usl) {
-        if (c.reinit) k_particle_kinematics<true, true><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl);
-        else k_particle_kinematics<true, false><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl);
+        if (c.reinit) particle_kinematics<true, true>(S, tiles, ntiles, ctl, s);
+        else particle_kinematics<true, false>(S, tiles, ntiles, ctl, s);
     } else {
-        if (c.reinit) k_particle_kinematics<false, true><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl);
-        else k_particle_kinematics<false, false><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl);
+        if (c.reinit) particle_kinematics<false, true>(S, tiles, ntiles, ctl, s);
+        else particle_kinematics<false, false>(S, tiles, ntiles, ctl, s);
     }
     return cudaGetLastError();
 }
