@@ -86,6 +86,8 @@ SIGNATURES = [
     ("mpm_time_phases", C.c_int, [_VP, C.c_int, _VP, _VP]),
     ("mpm_set_block_steps", C.c_int, [_VP, C.c_int]),
     ("mpm_get_counters", C.c_int, [_VP, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    ("mpm_record", C.c_int, [_VP, C.c_int, C.c_int, _VP]),
+    ("mpm_adjoint", C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, C.c_int, _VP]),
     ("mpm_volume_setup_noalloc", C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_int64,
                                            _VP, _VP, _VP, _VP, _VP, _VP]),
 ]

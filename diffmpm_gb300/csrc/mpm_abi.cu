@@ -17,9 +17,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/diffmpm_gb300.h"
-#include "mpm_kernels.h"
-#include "mpm_types.h"
+#include "mpm_handle.h"
 
 using namespace mpm;
 
@@ -27,83 +25,10 @@ namespace {
 
 thread_local std::string g_create_error;
 
-struct PSet {
-    float *x = nullptr, *y = nullptr, *vx = nullptr, *vy = nullptr;
-    float *sxx[2] = {}, *syy[2] = {}, *szz[2] = {}, *sxy[2] = {};
-    float *exx = nullptr, *eyy = nullptr, *exy = nullptr;
-    float *rho[2] = {}, *vsc[2] = {}, *vol[2] = {};
-    float *mass = nullptr, *psize = nullptr, *E = nullptr, *tr_tau = nullptr;
-    uint8_t* mat = nullptr;
-    int8_t* tr_fn = nullptr;
-    int* pid = nullptr;
-};
-
 }  // namespace
 
-struct MpmHandle {
-    int device = 0;
-    // configuration
-    int ndim = 2, nx = 0, ny = 0;
-    float hx = 0, hy = 0, dt = 0, gx = 0, gy = 0, vol_el = 0;
-    bool usl = false, reinit = true;
-    int velocity_update = 0;
-    int nmat = 0;
-    std::vector<MatDev> mats;
-    // device tables
-    MatDev* d_mats = nullptr;
-    float* d_cons_vel = nullptr;
-    uint16_t* d_ncons = nullptr;
-    int* d_cnf_ptr = nullptr;
-    int8_t* d_cnf_dir = nullptr;
-    float* d_cnf_val = nullptr;
-    int8_t* d_cnf_fn = nullptr;
-    int nfn = 0;
-    int* d_fn_off = nullptr;
-    float *d_fn_x = nullptr, *d_fn_y = nullptr;
-    // nodes
-    int nn = 0;
-    float *nm = nullptr, *nvax = nullptr, *nvay = nullptr, *nvbx = nullptr, *nvby = nullptr;
-    float *nax = nullptr, *nay = nullptr;
-    // cells
-    int ncell = 0;
-    int* cstart[2] = {};
-    int cs_cur = 0;
-    uint8_t* cflag = nullptr;
-    SortScratch sw{};
-    // particles
-    int64_t np = -1;
-    PSet ps[2];
-    int pcur = 0;
-    float* passive = nullptr;   // original order, 5 per particle: s_yz s_xz e_zz e_yz e_xz
-    bool has_trac = false, has_E = false;
-    // snapshot of the mutable state at a block start
-    std::vector<float*> snap_f;
-    uint8_t* snap_cflag = nullptr;
-    float *snap_nvbx = nullptr, *snap_nvby = nullptr;
-    // descriptors
-    SimDev hs{};
-    SimDev* ds = nullptr;
-    Control* ctl = nullptr;
-    Control* h_ctl = nullptr;   // pinned mirror
-    int4* dtiles = nullptr;
-    int ntiles = 0;
-    int64_t step = 0;
-    // staging and pointer tables
-    void* stage = nullptr;
-    size_t stage_bytes = 0;
-    float** d_ptrs = nullptr;
-    // graphs
-    cudaStream_t cap = nullptr;
-    std::map<int, cudaGraphExec_t> graphs;
-    bool graphs_trac = false;
-    bool initialized = false, needs_resort = false;
-    int block_steps = 100;
-    int64_t resorts = 0, rollbacks = 0;
-    std::vector<void*> allocs;
-    std::string err;
-};
-
-namespace {
+namespace mpm {
+namespace host {
 
 int fail(MpmHandle* h, int code, const char* fmt, ...) {
     char buf[512];
@@ -116,34 +41,6 @@ int fail(MpmHandle* h, int code, const char* fmt, ...) {
     return code;
 }
 
-#define CK(h, call)                                                                          \
-    do {                                                                                     \
-        cudaError_t e_ = (call);                                                             \
-        if (e_ != cudaSuccess)                                                               \
-            return fail(h, e_ == cudaErrorMemoryAllocation ? MPM_ERR_NOMEM : MPM_ERR_CUDA,   \
-                        "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
-    } while (0)
-
-#define TRY(x)                   \
-    do {                         \
-        int r_ = (x);            \
-        if (r_ != MPM_OK) return r_; \
-    } while (0)
-
-template <class T>
-int dalloc(MpmHandle* h, T** p, size_t count) {
-    *p = nullptr;
-    if (count == 0) count = 1;
-    void* v = nullptr;
-    cudaError_t e = cudaMalloc(&v, count * sizeof(T));
-    if (e != cudaSuccess)
-        return fail(h, MPM_ERR_NOMEM, "cudaMalloc(%zu bytes): %s", count * sizeof(T),
-                    cudaGetErrorString(e));
-    h->allocs.push_back(v);
-    *p = static_cast<T*>(v);
-    return MPM_OK;
-}
-
 void dfree(MpmHandle* h, void* p) {
     if (!p) return;
     for (size_t i = 0; i < h->allocs.size(); ++i) {
@@ -154,8 +51,6 @@ void dfree(MpmHandle* h, void* p) {
     }
     cudaFree(p);
 }
-
-inline cudaStream_t S(void* s) { return static_cast<cudaStream_t>(s); }
 
 // Element volume by the reference's formula in float32 (diffmpm/element.py:903-909).
 float element_volume(float hx, float hy) {
@@ -250,6 +145,7 @@ int resort(MpmHandle* h, cudaStream_t s) {
         return MPM_OK;
     }
     const int np = (int)h->np, nb = h->ncell + 1;
+    adjoint_note_resort(h);
     SortScratch& w = h->sw;
     CK(h, cudaMemsetAsync(w.count, 0, sizeof(int) * nb, s));
     CK(h, cudaMemsetAsync(w.cursor, 0, sizeof(int) * nb, s));
@@ -495,7 +391,10 @@ int copy_passive(MpmHandle* h, int field, float* aos, bool to_aos, cudaStream_t 
     return MPM_OK;
 }
 
-}  // namespace
+}  // namespace host
+}  // namespace mpm
+
+using namespace mpm::host;
 
 void mpm::set_thread_error(const std::string& msg) { g_create_error = msg; }
 
@@ -741,6 +640,7 @@ int mpm_create(const MpmDesc* d, MpmHandle** out) {
 
 int mpm_destroy(MpmHandle* h) {
     if (!h) return MPM_OK;
+    mpm::adjoint_free(h);
     drop_graphs(h);
     if (h->cap) cudaStreamDestroy(h->cap);
     for (void* p : h->allocs) cudaFree(p);
@@ -753,6 +653,7 @@ int mpm_destroy(MpmHandle* h) {
 int mpm_set_particles(MpmHandle* h, int64_t n, const float* loc, const int32_t* material_id,
                       int on_device, void* stream) {
     if (!h) return MPM_ERR_INVALID;
+    h->gen++;
     if (n < 0 || n > ((int64_t)1 << 31) - 1) return fail(h, MPM_ERR_INVALID, "particle count out of range");
     if (n > 0 && !loc) return fail(h, MPM_ERR_INVALID, "loc is null");
     cudaStream_t s = S(stream);
@@ -810,6 +711,7 @@ int mpm_set_particles(MpmHandle* h, int64_t n, const float* loc, const int32_t* 
 
 int mpm_write_field(MpmHandle* h, int field, const void* src, int on_device, void* stream) {
     if (!h) return MPM_ERR_INVALID;
+    h->gen++;
     if (h->np < 0) return fail(h, MPM_ERR_STATE, "set particles first");
     if (h->np == 0) return MPM_OK;
     if (!src) return fail(h, MPM_ERR_INVALID, "null source");
@@ -894,6 +796,7 @@ int mpm_read_field(MpmHandle* h, int field, void* dst, int on_device, void* stre
 int mpm_set_tractions(MpmHandle* h, int n, const int64_t* pid, const int32_t* dir,
                       const double* traction, const int32_t* function, void* stream) {
     if (!h) return MPM_ERR_INVALID;
+    h->gen++;
     if (h->np < 0) return fail(h, MPM_ERR_STATE, "set particles first");
     const int64_t np = h->np;
     cudaStream_t s = S(stream);
@@ -960,6 +863,7 @@ int mpm_read_nodal_field(MpmHandle* h, int field, float* dst, int on_device, voi
 
 int mpm_write_nodal_field(MpmHandle* h, int field, const float* src, int on_device, void* stream) {
     if (!h || !src) return MPM_ERR_INVALID;
+    h->gen++;
     cudaStream_t s = S(stream);
     const int nc = field == MPM_NODE_MASS ? 1 : 2;
     const void* d = nullptr;
@@ -974,6 +878,7 @@ int mpm_write_nodal_field(MpmHandle* h, int field, const float* src, int on_devi
 
 int mpm_initialize(MpmHandle* h, void* stream) {
     if (!h) return MPM_ERR_INVALID;
+    h->gen++;
     if (h->np < 0) return fail(h, MPM_ERR_STATE, "set particles first");
     cudaStream_t s = S(stream);
     TRY(clear_status(h, s));
@@ -988,6 +893,7 @@ int mpm_initialize(MpmHandle* h, void* stream) {
 
 int mpm_run_phase(MpmHandle* h, int phase, void* stream) {
     if (!h) return MPM_ERR_INVALID;
+    h->gen++;
     if (!h->initialized) return fail(h, MPM_ERR_STATE, "initialize first");
     if (phase < 0 || phase > 2) return fail(h, MPM_ERR_INVALID, "phase must be 0, 1 or 2");
     cudaStream_t s = S(stream);
@@ -1008,6 +914,7 @@ int mpm_run_phase(MpmHandle* h, int phase, void* stream) {
 
 int mpm_step(MpmHandle* h, int nsteps, void* stream) {
     if (!h) return MPM_ERR_INVALID;
+    h->gen++;
     if (!h->initialized) return fail(h, MPM_ERR_STATE, "initialize first");
     if (nsteps < 0) return fail(h, MPM_ERR_INVALID, "nsteps must be >= 0");
     if (h->np <= 0) {
@@ -1059,6 +966,7 @@ int mpm_get_step(const MpmHandle* h, int64_t* step) {
 
 int mpm_set_step(MpmHandle* h, int64_t step) {
     if (!h || step < 0 || step > 0x7fffffff) return MPM_ERR_INVALID;
+    h->gen++;
     if ((step & 1) != (h->step & 1) && h->np > 0) {
         // keep the current ping-pong data addressed by the new parity
         for (int k = 0; k < 2; ++k) {
@@ -1082,6 +990,7 @@ int mpm_set_step(MpmHandle* h, int64_t step) {
 
 int mpm_time_phases(MpmHandle* h, int nsteps, float* ms_out, void* stream) {
     if (!h || !ms_out || nsteps < 1) return MPM_ERR_INVALID;
+    h->gen++;
     if (!h->initialized) return fail(h, MPM_ERR_STATE, "initialize first");
     cudaStream_t s = S(stream);
     if (h->needs_resort) TRY(resort(h, s));

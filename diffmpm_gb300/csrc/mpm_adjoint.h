@@ -1,0 +1,72 @@
+// Reverse (adjoint) passes of the explicit MPM step, USF with the per-step
+// volume set-up of solve_jit (diffmpm/solver.py:81-85, 100-111, 179-213).
+//
+// The reverse of one step runs four launches over the step's tape (the
+// particle state at the step start and the nodal values the forward step
+// produced), in the reverse order of the forward phases:
+//   1. node pass      transposed G2P (v-hat, a-hat adjoints gathered to the
+//                     nodes) and the reverse nodal update (a = f/m, v += a dt,
+//                     constraints, flush); also the per-cell particle counts
+//   2. particle pass  reverse of the forces (internal + external) and of the
+//                     USF strain, volume, density and stress update
+//   3. node pass      transposed strain-rate gather (nodal-velocity adjoint)
+//                     and the reverse nodal velocity p/m with constraints
+//   4. particle pass  reverse of the mass and momentum P2G
+// Every node sum is formed in a fixed order (the four cells around the node,
+// particles of a cell in storage order), so the adjoint is deterministic.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "mpm_types.h"
+
+namespace mpm {
+
+// Everything one reverse step reads and writes; passed by value.
+struct AdjStep {
+    // mesh and run constants
+    int nx, ny, np;
+    float hx, hy, dt, vol_el, gx, gy;
+    int velocity_update;
+    const uint16_t* ncons;
+    const MatDev* mats;
+    // sort epoch of the step: cell starts, material ids and per-particle E
+    const int* cstart;
+    const uint8_t* mat;
+    const float* E;
+    // tape: particle state at the step start (storage order), drift flags,
+    // nodal mass, velocity after phase 1 (vA), velocity and acceleration after
+    // the nodal update (vB, aB)
+    const float *x, *y, *vx, *vy, *sxx, *syy, *szz, *sxy, *rho;
+    const uint8_t* cflag;
+    const float *nm, *nvax, *nvay, *nvbx, *nvby, *nax, *nay;
+    // adjoint of the particle state (in: end of step; out: start of step) and
+    // the accumulated dL/dE per particle
+    float *lx, *ly, *lvx, *lvy, *lsxx, *lsyy, *lszz, *lsxy, *lrho, *lE;
+    // per-particle adjoints of the strain rates and centroid rates (pass 2 -> 3)
+    float *r0b, *r1b, *r3b, *c0b, *c1b;
+    // nodal adjoints: force, mass and phase-1 velocity from the nodal update
+    // (pass 1 -> 2, 3), momentum and total mass (pass 3 -> 4)
+    float *fbx, *fby, *mb, *vabx, *vaby;
+    float *qbx, *qby, *mbt;
+    int* cnt;              // particles per cell at the step start (pass 1 -> 2, 4)
+};
+
+cudaError_t launch_rev_nodal_update(const AdjStep& A, cudaStream_t s);
+cudaError_t launch_rev_forces(const AdjStep& A, cudaStream_t s);
+cudaError_t launch_rev_nodal_kinematics(const AdjStep& A, cudaStream_t s);
+cudaError_t launch_rev_mass_momentum(const AdjStep& A, cudaStream_t s);
+
+// *mismatch += number of i < n with a[i] != b[i] bitwise (4-byte words).
+cudaError_t launch_count_mismatch(const void* a, const void* b, int n, int* mismatch,
+                                  cudaStream_t s);
+
+// dst[k][i] = src[k][i] for k < count (count <= 9), i < n.
+struct CopyJob {
+    const void* src[9];
+    void* dst[9];
+    int count;
+    int n;
+};
+cudaError_t launch_copy_f32(const CopyJob& j, cudaStream_t s);
+
+}  // namespace mpm

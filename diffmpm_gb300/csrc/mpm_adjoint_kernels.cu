@@ -1,0 +1,442 @@
+// Reverse passes of the explicit MPM step (USF, per-step volume set-up).
+//
+// Notation of the forward step, particle p in cell c with corners k = 0..3
+// (diffmpm/element.py, particle.py; the step order of diffmpm/scheme.py:22-67):
+//   m    = V0 rho,           V0 = V_el / count(c)            (solver.py:81-85)
+//   M_n  = sum N m,  P_n = flush(sum N m v),  vA = C(flush(P / M))
+//   r    = flush(G^T vA) (xx, yy, xy),  c = flush(Gc^T vA),  dvol = dt (c0 + c1)
+//   sig' = sig + D(E) r dt,  V = V0 (1 + dvol),  rho' = rho / (1 + dvol)
+//   F_n  = sum -V (Gx sxx' + Gy sxy', Gy syy' + Gx sxy') + N m g
+//   a    = F / M,  vB = flush(C(vA + a dt)),  aB = flush(C0(a))
+//   v'   = velocity_update ? sum N vB : v + dt sum N aB,  x' = x + dt sum N vB
+// C sets constrained velocity components, C0 zeroes constrained accelerations.
+// flush(a) = 0 for |a| < 1e-12, so its derivative is 0 there and 1 elsewhere:
+// a component that is exactly 0 after the flush passes no adjoint.  Cell ids,
+// counts and masks are piecewise constant in the positions and pass none.
+// The velocity a node with zero mass keeps from the previous step only
+// reaches particles whose shape function at that node is exactly zero, so its
+// dependence is dropped.
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "mpm_adjoint.h"
+#include "mpm_device.cuh"
+
+namespace mpm {
+
+namespace {
+
+constexpr int NODE_THREADS = 256;
+constexpr int PART_THREADS = 256;
+
+// Particles currently in cell (ci, cj) at the step start, in the order of the
+// forward gathers: the cell's own sort-cell, and neighbouring sort-cells whose
+// drift flag is set (positions tested).
+template <class F>
+__device__ __forceinline__ void visit_tape_cell(const AdjStep& A, int ci, int cj, const CellGeo& g,
+                                                F&& f) {
+    #pragma unroll 1
+    for (int dj = -1; dj <= 1; ++dj) {
+        const int sj = cj + dj;
+        if (sj < 0 || sj >= A.ny) continue;
+        #pragma unroll 1
+        for (int di = -1; di <= 1; ++di) {
+            const int si = ci + di;
+            if (si < 0 || si >= A.nx) continue;
+            const int s = sj * A.nx + si;
+            const bool flagged = A.cflag[s] != 0;
+            if (!(di == 0 && dj == 0) && !flagged) continue;
+            const int b = A.cstart[s], e = A.cstart[s + 1];
+            #pragma unroll 1
+            for (int q = b; q < e; ++q) {
+                if (flagged && !in_cell(g, A.x[q], A.y[q])) continue;
+                f(q);
+            }
+        }
+    }
+}
+
+// Shape function and gradient of corner k alone, with the same roundings as
+// shape4 / dshape4.
+__device__ __forceinline__ void corner_shape(int k, float xi, float eta, float rx, float ry,
+                                             float& N, float& Gx, float& Gy) {
+    const bool px = k == 1 || k == 2, py = k >= 2;
+    const float sx = px ? fa(1.0f, xi) : fs(1.0f, xi);
+    const float sy = py ? fa(1.0f, eta) : fs(1.0f, eta);
+    N = fm(fm(0.25f, sx), sy);
+    Gx = fm(fm(px ? 0.25f : -0.25f, sy), rx);
+    Gy = fm(fm(py ? 0.25f : -0.25f, sx), ry);
+}
+
+// Cell (ci, cj) and corner index of the node (I, J) for the four cells around
+// it, in the fixed order c = 0..3: (I-1, J-1) corner 2, (I, J-1) corner 3,
+// (I-1, J) corner 1, (I, J) corner 0.
+__device__ __forceinline__ int corner_of(int c) { return c == 0 ? 2 : c == 1 ? 3 : c == 2 ? 1 : 0; }
+
+__device__ __forceinline__ void particle_cell(const AdjStep& A, float x, float y, int& ci, int& cj) {
+    ci = min(max(locate_axis(x, A.hx, A.nx), 0), A.nx - 1);
+    cj = min(max(locate_axis(y, A.hy, A.ny), 0), A.ny - 1);
+}
+
+// Adjoint seeds of G2P: (v-hat bar, a-hat bar) of particle q.
+__device__ __forceinline__ void g2p_seeds(const AdjStep& A, int q, float& gx, float& gy,
+                                          float& hx, float& hy) {
+    const float lvx = A.lvx[q], lvy = A.lvy[q];
+    gx = fm(A.lx[q], A.dt);
+    gy = fm(A.ly[q], A.dt);
+    if (A.velocity_update) {
+        gx = fa(gx, lvx);
+        gy = fa(gy, lvy);
+        hx = 0.0f;
+        hy = 0.0f;
+    } else {
+        hx = fm(lvx, A.dt);
+        hy = fm(lvy, A.dt);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Pass 1: transposed G2P and reverse nodal update (element.py:305-329,
+// particle.py:208-247).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(NODE_THREADS)
+k_rev_nodal_update(const __grid_constant__ AdjStep A) {
+    const int nxn = A.nx + 1;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nxn * (A.ny + 1)) return;
+    const int I = n % nxn, J = n / nxn;
+    float vbx = 0.0f, vby = 0.0f, abx = 0.0f, aby = 0.0f;
+    #pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
+        const int ci = I - 1 + (c & 1), cj = J - 1 + (c >> 1);
+        if (ci < 0 || ci >= A.nx || cj < 0 || cj >= A.ny) continue;
+        const int k = corner_of(c);
+        const CellGeo g = cell_geo(ci, cj, A.hx, A.hy);
+        int cnt = 0;
+        visit_tape_cell(A, ci, cj, g, [&](int q) {
+            float N, Gx, Gy;
+            corner_shape(k, natural(A.x[q], g.cx, g.rx), natural(A.y[q], g.cy, g.ry), g.rx, g.ry,
+                         N, Gx, Gy);
+            float gx, gy, hx, hy;
+            g2p_seeds(A, q, gx, gy, hx, hy);
+            vbx = fa(vbx, fm(N, gx));
+            vby = fa(vby, fm(N, gy));
+            abx = fa(abx, fm(N, hx));
+            aby = fa(aby, fm(N, hy));
+            ++cnt;
+        });
+        if (c == 3) A.cnt[cj * A.nx + ci] = cnt;
+    }
+    float fbx = 0.0f, fby = 0.0f, mb = 0.0f, wbx = 0.0f, wby = 0.0f;
+    const float M = A.nm[n];
+    if (M != 0.0f) {
+        const uint16_t code = A.ncons[n];
+        const bool cx = (code & 0xff) != 0, cy = (code >> 8) != 0;
+        const float vBx = A.nvbx[n], vBy = A.nvby[n], aBx = A.nax[n], aBy = A.nay[n];
+        // vB = flush(C(vA + a dt)), aB = flush(C0(a))
+        wbx = (cx || vBx == 0.0f) ? 0.0f : vbx;
+        wby = (cy || vBy == 0.0f) ? 0.0f : vby;
+        const float ax = fa((cx || aBx == 0.0f) ? 0.0f : abx, fm(wbx, A.dt));
+        const float ay = fa((cy || aBy == 0.0f) ? 0.0f : aby, fm(wby, A.dt));
+        // a = F / M
+        fbx = fdv(ax, M);
+        fby = fdv(ay, M);
+        mb = -fdv(fa(fm(ax, aBx), fm(ay, aBy)), M);
+    }
+    A.fbx[n] = fbx;
+    A.fby[n] = fby;
+    A.mb[n] = mb;
+    A.vabx[n] = wbx;
+    A.vaby[n] = wby;
+}
+
+// ---------------------------------------------------------------------------
+// Pass 2: reverse of the forces (element.py:236-268, 842-901) and of the USF
+// strain / volume / stress update (particle.py:249-327, material.py:113-131).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(PART_THREADS)
+k_rev_forces(const __grid_constant__ AdjStep A) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= A.np) return;
+    const float x = A.x[q], y = A.y[q];
+    int ci, cj;
+    particle_cell(A, x, y, ci, cj);
+    const CellGeo g = cell_geo(ci, cj, A.hx, A.hy);
+    const float xi = natural(x, g.cx, g.rx), eta = natural(y, g.cy, g.ry);
+    float N[4], Gx[4], Gy[4], Gcx[4], Gcy[4];
+    shape4(xi, eta, N);
+    dshape4(xi, eta, g.rx, g.ry, Gx, Gy);
+    dshape4(0.0f, 0.0f, g.rx, g.ry, Gcx, Gcy);
+    const int ll = cj * (A.nx + 1) + ci;
+    const int ids[4] = {ll, ll + 1, ll + A.nx + 2, ll + A.nx + 1};
+    float vAx[4], vAy[4], vBx[4], vBy[4], aBx[4], aBy[4], fbx[4], fby[4];
+    #pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        vAx[k] = A.nvax[ids[k]];
+        vAy[k] = A.nvay[ids[k]];
+        vBx[k] = A.nvbx[ids[k]];
+        vBy[k] = A.nvby[ids[k]];
+        aBx[k] = A.nax[ids[k]];
+        aBy[k] = A.nay[ids[k]];
+        fbx[k] = A.fbx[ids[k]];
+        fby[k] = A.fby[ids[k]];
+    }
+    const int cnt = A.cnt[cj * A.nx + ci];
+    const float V0 = cnt ? fdv(A.vol_el, (float)cnt) : 0.0f;
+    const float rho0 = A.rho[q];
+    const float m = fm(V0, rho0);
+
+    // forward recomputation of the stress update
+    PState p{};
+    p.sxx = A.sxx[q];
+    p.syy = A.syy[q];
+    p.szz = A.szz[q];
+    p.sxy = A.sxy[q];
+    p.rho = rho0;
+    float r0, r1, r3, c0, c1, c3;
+    strain_rate4(Gx, Gy, vAx, vAy, r0, r1, r3);
+    strain_rate4(Gcx, Gcy, vAx, vAy, c0, c1, c3);
+    const float dvol = fm(A.dt, fa(c0, c1));
+    const MatDev& mat = A.mats[A.mat[q]];
+    const float Ep = A.E ? A.E[q] : -1.0f;
+    const float f = strain_stress_update(mat, Ep, A.dt, r0, r1, r3, dvol, p);
+    const float V = fm(V0, f);
+
+    // G2P (x' = x + dt v-hat, v' from v-hat or a-hat): shape-function adjoints
+    float gx, gy, hx, hy;
+    g2p_seeds(A, q, gx, gy, hx, hy);
+    float Nb[4], Gxb[4], Gyb[4];
+    float mb = 0.0f, Vb = 0.0f, fsxx = 0.0f, fsyy = 0.0f, fsxy = 0.0f;
+    #pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float fg = fa(fm(fbx[k], A.gx), fm(fby[k], A.gy));   // F-bar . g
+        Nb[k] = fa(fa(fa(fm(gx, vBx[k]), fm(gy, vBy[k])), fa(fm(hx, aBx[k]), fm(hy, aBy[k]))),
+                   fm(m, fg));
+        mb = fa(mb, fm(N[k], fg));
+        const float fx = fa(fm(Gx[k], p.sxx), fm(Gy[k], p.sxy));
+        const float fy = fa(fm(Gy[k], p.syy), fm(Gx[k], p.sxy));
+        Vb = fs(Vb, fa(fm(fbx[k], fx), fm(fby[k], fy)));
+        fsxx = fa(fsxx, fm(fbx[k], Gx[k]));
+        fsyy = fa(fsyy, fm(fby[k], Gy[k]));
+        fsxy = fa(fsxy, fa(fm(fbx[k], Gy[k]), fm(fby[k], Gx[k])));
+        Gxb[k] = -fm(V, fa(fm(fbx[k], p.sxx), fm(fby[k], p.sxy)));
+        Gyb[k] = -fm(V, fa(fm(fbx[k], p.sxy), fm(fby[k], p.syy)));
+    }
+    // stress adjoint at the end of the forces: loss/next-step part + force part
+    const float sbxx = fs(A.lsxx[q], fm(V, fsxx));
+    const float sbyy = fs(A.lsyy[q], fm(V, fsyy));
+    const float sbzz = A.lszz[q];
+    const float sbxy = fs(A.lsxy[q], fm(V, fsxy));
+
+    // reverse of sig' = sig + D r dt
+    const float d0 = fm(r0, A.dt), d1 = fm(r1, A.dt), d3 = fm(r3, A.dt);
+    float d0b = 0.0f, d1b = 0.0f, d3b = 0.0f, Eb = 0.0f;
+    if (mat.type == MAT_LINEAR_ELASTIC) {
+        float a1 = mat.a1, a2 = mat.a2, G = mat.G;
+        if (Ep >= 0.0f) {
+            a1 = fm(Ep, mat.c1);
+            a2 = fm(Ep, mat.c2);
+            G = fm(Ep, mat.c3);
+        }
+        d0b = fa(fa(fm(a1, sbxx), fm(a2, sbyy)), fm(a2, sbzz));
+        d1b = fa(fa(fm(a2, sbxx), fm(a1, sbyy)), fm(a2, sbzz));
+        d3b = fm(G, sbxy);
+        Eb = fa(fa(fm(mat.c1, fa(fm(d0, sbxx), fm(d1, sbyy))),
+                   fm(mat.c2, fa(fa(fm(d1, sbxx), fm(d0, sbyy)), fm(fa(d0, d1), sbzz)))),
+                fm(mat.c3, fm(d3, sbxy)));
+    } else if (mat.type == MAT_SIMPLE) {
+        d0b = fm(mat.E, sbxx);
+        d1b = fm(mat.E, sbyy);
+        d3b = fm(mat.E, sbxy);
+        Eb = fa(fa(fm(d0, sbxx), fm(d1, sbyy)), fm(d3, sbxy));
+    }
+    const float r0b = r0 != 0.0f ? fm(d0b, A.dt) : 0.0f;
+    const float r1b = r1 != 0.0f ? fm(d1b, A.dt) : 0.0f;
+    const float r3b = r3 != 0.0f ? fm(d3b, A.dt) : 0.0f;
+
+    // reverse of V = V0 (1 + dvol), rho' = rho / (1 + dvol), m = V0 rho
+    const float lrho = A.lrho[q];
+    const float fb = fs(fm(Vb, V0), fdv(fm(lrho, p.rho), f));
+    const float rhob = fa(fdv(lrho, f), fm(V0, mb));
+    const float c0b = c0 != 0.0f ? fm(fb, A.dt) : 0.0f;
+    const float c1b = c1 != 0.0f ? fm(fb, A.dt) : 0.0f;
+
+    // strain-rate part of the gradient adjoints
+    float xb = A.lx[q], yb = A.ly[q];
+    float gyb = 0.0f, gxb = 0.0f;
+    #pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float gxk = fa(Gxb[k], fa(fm(r0b, vAx[k]), fm(r3b, vAy[k])));
+        const float gyk = fa(Gyb[k], fa(fm(r1b, vAy[k]), fm(r3b, vAx[k])));
+        const float sgn = (k & 1) ? -1.0f : 1.0f;   // d Gx_k / d eta, d Gy_k / d xi: + - + -
+        gxb = fa(gxb, fm(sgn, gxk));
+        gyb = fa(gyb, fm(sgn, gyk));
+        xb = fa(xb, fm(Nb[k], Gx[k]));
+        yb = fa(yb, fm(Nb[k], Gy[k]));
+    }
+    const float rxy = fm(fm(0.25f, g.rx), g.ry);
+    xb = fa(xb, fm(rxy, gyb));
+    yb = fa(yb, fm(rxy, gxb));
+
+    A.lx[q] = xb;
+    A.ly[q] = yb;
+    A.lsxx[q] = sbxx;
+    A.lsyy[q] = sbyy;
+    A.lszz[q] = sbzz;
+    A.lsxy[q] = sbxy;
+    A.lrho[q] = rhob;
+    A.lE[q] = fa(A.lE[q], Eb);
+    A.r0b[q] = r0b;
+    A.r1b[q] = r1b;
+    A.r3b[q] = r3b;
+    A.c0b[q] = c0b;
+    A.c1b[q] = c1b;
+}
+
+// ---------------------------------------------------------------------------
+// Pass 3: transposed strain-rate gather and reverse nodal velocity
+// (element.py:191-202, 331-334; particle.py:281-313).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(NODE_THREADS)
+k_rev_nodal_kinematics(const __grid_constant__ AdjStep A) {
+    const int nxn = A.nx + 1;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nxn * (A.ny + 1)) return;
+    const int I = n % nxn, J = n / nxn;
+    float vbx = A.vabx[n], vby = A.vaby[n];
+    #pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
+        const int ci = I - 1 + (c & 1), cj = J - 1 + (c >> 1);
+        if (ci < 0 || ci >= A.nx || cj < 0 || cj >= A.ny) continue;
+        const int k = corner_of(c);
+        const CellGeo g = cell_geo(ci, cj, A.hx, A.hy);
+        float Nc, Gcx, Gcy;
+        corner_shape(k, 0.0f, 0.0f, g.rx, g.ry, Nc, Gcx, Gcy);
+        visit_tape_cell(A, ci, cj, g, [&](int q) {
+            float N, Gx, Gy;
+            corner_shape(k, natural(A.x[q], g.cx, g.rx), natural(A.y[q], g.cy, g.ry), g.rx, g.ry,
+                         N, Gx, Gy);
+            const float r0b = A.r0b[q], r1b = A.r1b[q], r3b = A.r3b[q];
+            vbx = fa(vbx, fa(fa(fm(Gx, r0b), fm(Gy, r3b)), fm(Gcx, A.c0b[q])));
+            vby = fa(vby, fa(fa(fm(Gy, r1b), fm(Gx, r3b)), fm(Gcy, A.c1b[q])));
+        });
+    }
+    float qbx = 0.0f, qby = 0.0f, mbt = A.mb[n];
+    const float M = A.nm[n];
+    if (M != 0.0f) {
+        const uint16_t code = A.ncons[n];
+        const bool cx = (code & 0xff) != 0, cy = (code >> 8) != 0;
+        const float vAx = A.nvax[n], vAy = A.nvay[n];
+        // vA = C(flush(P / M)), P = flush(sum N m v)
+        const float ubx = (cx || vAx == 0.0f) ? 0.0f : vbx;
+        const float uby = (cy || vAy == 0.0f) ? 0.0f : vby;
+        qbx = fdv(ubx, M);
+        qby = fdv(uby, M);
+        mbt = fs(mbt, fdv(fa(fm(ubx, vAx), fm(uby, vAy)), M));
+    }
+    A.qbx[n] = qbx;
+    A.qby[n] = qby;
+    A.mbt[n] = mbt;
+}
+
+// ---------------------------------------------------------------------------
+// Pass 4: reverse of the mass and momentum P2G (element.py:122-189) and of
+// m = V0 rho (particle.py:158-178).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(PART_THREADS)
+k_rev_mass_momentum(const __grid_constant__ AdjStep A) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= A.np) return;
+    const float x = A.x[q], y = A.y[q];
+    int ci, cj;
+    particle_cell(A, x, y, ci, cj);
+    const CellGeo g = cell_geo(ci, cj, A.hx, A.hy);
+    const float xi = natural(x, g.cx, g.rx), eta = natural(y, g.cy, g.ry);
+    float N[4], Gx[4], Gy[4];
+    shape4(xi, eta, N);
+    dshape4(xi, eta, g.rx, g.ry, Gx, Gy);
+    const int ll = cj * (A.nx + 1) + ci;
+    const int ids[4] = {ll, ll + 1, ll + A.nx + 2, ll + A.nx + 1};
+    const int cnt = A.cnt[cj * A.nx + ci];
+    const float V0 = cnt ? fdv(A.vol_el, (float)cnt) : 0.0f;
+    const float m = fm(V0, A.rho[q]);
+    const float vx = A.vx[q], vy = A.vy[q];
+    float mb = 0.0f, sqx = 0.0f, sqy = 0.0f, xb = A.lx[q], yb = A.ly[q];
+    #pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float qx = A.qbx[ids[k]], qy = A.qby[ids[k]];
+        const float t = fa(fa(fm(qx, vx), fm(qy, vy)), A.mbt[ids[k]]);
+        mb = fa(mb, fm(N[k], t));
+        sqx = fa(sqx, fm(N[k], qx));
+        sqy = fa(sqy, fm(N[k], qy));
+        const float nb = fm(m, t);
+        xb = fa(xb, fm(nb, Gx[k]));
+        yb = fa(yb, fm(nb, Gy[k]));
+    }
+    const float lvx = A.velocity_update ? 0.0f : A.lvx[q];
+    const float lvy = A.velocity_update ? 0.0f : A.lvy[q];
+    A.lvx[q] = fa(lvx, fm(m, sqx));
+    A.lvy[q] = fa(lvy, fm(m, sqy));
+    A.lrho[q] = fa(A.lrho[q], fm(V0, mb));
+    A.lx[q] = xb;
+    A.ly[q] = yb;
+}
+
+__global__ void k_copy_f32(const __grid_constant__ CopyJob j) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= j.n) return;
+    #pragma unroll 1
+    for (int k = 0; k < j.count; ++k)
+        static_cast<float*>(j.dst[k])[i] = static_cast<const float*>(j.src[k])[i];
+}
+
+__global__ void k_count_mismatch(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b,
+                                 int n, int* __restrict__ mismatch) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool diff = i < n && a[i] != b[i];
+    const int c = __syncthreads_count(diff);
+    if (threadIdx.x == 0 && c) atomicAdd(mismatch, c);
+}
+
+inline int blocks_for(int n, int t) { return (n + t - 1) / t; }
+
+}  // namespace
+
+cudaError_t launch_rev_nodal_update(const AdjStep& A, cudaStream_t s) {
+    const int nn = (A.nx + 1) * (A.ny + 1);
+    k_rev_nodal_update<<<blocks_for(nn, NODE_THREADS), NODE_THREADS, 0, s>>>(A);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rev_forces(const AdjStep& A, cudaStream_t s) {
+    if (A.np <= 0) return cudaSuccess;
+    k_rev_forces<<<blocks_for(A.np, PART_THREADS), PART_THREADS, 0, s>>>(A);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rev_nodal_kinematics(const AdjStep& A, cudaStream_t s) {
+    const int nn = (A.nx + 1) * (A.ny + 1);
+    k_rev_nodal_kinematics<<<blocks_for(nn, NODE_THREADS), NODE_THREADS, 0, s>>>(A);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rev_mass_momentum(const AdjStep& A, cudaStream_t s) {
+    if (A.np <= 0) return cudaSuccess;
+    k_rev_mass_momentum<<<blocks_for(A.np, PART_THREADS), PART_THREADS, 0, s>>>(A);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_count_mismatch(const void* a, const void* b, int n, int* mismatch,
+                                  cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_count_mismatch<<<blocks_for(n, 256), 256, 0, s>>>(static_cast<const uint32_t*>(a),
+                                                         static_cast<const uint32_t*>(b), n, mismatch);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_copy_f32(const CopyJob& j, cudaStream_t s) {
+    if (j.n <= 0 || j.count <= 0) return cudaSuccess;
+    k_copy_f32<<<blocks_for(j.n, 256), 256, 0, s>>>(j);
+    return cudaGetLastError();
+}
+
+}  // namespace mpm

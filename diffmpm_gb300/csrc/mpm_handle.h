@@ -1,0 +1,159 @@
+// Host-side state of one simulation handle and the driver helpers shared by
+// the forward step (mpm_abi.cu) and the adjoint (mpm_adjoint.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/diffmpm_gb300.h"
+#include "mpm_kernels.h"
+#include "mpm_types.h"
+
+namespace mpm {
+
+// One buffer set of the cell-sorted particle arrays (a re-sort gathers into
+// the other set and swaps).
+struct PSet {
+    float *x = nullptr, *y = nullptr, *vx = nullptr, *vy = nullptr;
+    float *sxx[2] = {}, *syy[2] = {}, *szz[2] = {}, *sxy[2] = {};
+    float *exx = nullptr, *eyy = nullptr, *exy = nullptr;
+    float *rho[2] = {}, *vsc[2] = {}, *vol[2] = {};
+    float *mass = nullptr, *psize = nullptr, *E = nullptr, *tr_tau = nullptr;
+    uint8_t* mat = nullptr;
+    int8_t* tr_fn = nullptr;
+    int* pid = nullptr;
+};
+
+struct AdjointState;   // checkpoints, tape and adjoint arrays (mpm_adjoint.cu)
+
+}  // namespace mpm
+
+struct MpmHandle {
+    int device = 0;
+    // configuration
+    int ndim = 2, nx = 0, ny = 0;
+    float hx = 0, hy = 0, dt = 0, gx = 0, gy = 0, vol_el = 0;
+    bool usl = false, reinit = true;
+    int velocity_update = 0;
+    int nmat = 0;
+    std::vector<mpm::MatDev> mats;
+    // device tables
+    mpm::MatDev* d_mats = nullptr;
+    float* d_cons_vel = nullptr;
+    uint16_t* d_ncons = nullptr;
+    int* d_cnf_ptr = nullptr;
+    int8_t* d_cnf_dir = nullptr;
+    float* d_cnf_val = nullptr;
+    int8_t* d_cnf_fn = nullptr;
+    int nfn = 0;
+    int* d_fn_off = nullptr;
+    float *d_fn_x = nullptr, *d_fn_y = nullptr;
+    // nodes
+    int nn = 0;
+    float *nm = nullptr, *nvax = nullptr, *nvay = nullptr, *nvbx = nullptr, *nvby = nullptr;
+    float *nax = nullptr, *nay = nullptr;
+    // cells
+    int ncell = 0;
+    int* cstart[2] = {};
+    int cs_cur = 0;
+    uint8_t* cflag = nullptr;
+    mpm::SortScratch sw{};
+    // particles
+    int64_t np = -1;
+    mpm::PSet ps[2];
+    int pcur = 0;
+    float* passive = nullptr;   // original order, 5 per particle: s_yz s_xz e_zz e_yz e_xz
+    bool has_trac = false, has_E = false;
+    // snapshot of the mutable state at a block start
+    std::vector<float*> snap_f;
+    uint8_t* snap_cflag = nullptr;
+    float *snap_nvbx = nullptr, *snap_nvby = nullptr;
+    // descriptors
+    mpm::SimDev hs{};
+    mpm::SimDev* ds = nullptr;
+    mpm::Control* ctl = nullptr;
+    mpm::Control* h_ctl = nullptr;   // pinned mirror
+    int4* dtiles = nullptr;
+    int ntiles = 0;
+    int64_t step = 0;
+    // staging and pointer tables
+    void* stage = nullptr;
+    size_t stage_bytes = 0;
+    float** d_ptrs = nullptr;
+    // graphs
+    cudaStream_t cap = nullptr;
+    std::map<int, cudaGraphExec_t> graphs;
+    bool graphs_trac = false;
+    bool initialized = false, needs_resort = false;
+    int block_steps = 100;
+    int64_t resorts = 0, rollbacks = 0;
+    // differentiation (null until mpm_record); gen counts state changes
+    mpm::AdjointState* adj = nullptr;
+    uint64_t gen = 0;
+    std::vector<void*> allocs;
+    std::string err;
+};
+
+namespace mpm {
+namespace host {
+
+int fail(MpmHandle* h, int code, const char* fmt, ...);
+
+#define CK(h, call)                                                                          \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess)                                                               \
+            return ::mpm::host::fail(h, e_ == cudaErrorMemoryAllocation ? MPM_ERR_NOMEM      \
+                                                                        : MPM_ERR_CUDA,      \
+                                     "%s: %s (%s:%d)", #call, cudaGetErrorString(e_),        \
+                                     __FILE__, __LINE__);                                    \
+    } while (0)
+
+#define TRY(x)                       \
+    do {                             \
+        int r_ = (x);                \
+        if (r_ != MPM_OK) return r_; \
+    } while (0)
+
+template <class T>
+int dalloc(MpmHandle* h, T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    void* v = nullptr;
+    cudaError_t e = cudaMalloc(&v, count * sizeof(T));
+    if (e != cudaSuccess)
+        return fail(h, MPM_ERR_NOMEM, "cudaMalloc(%zu bytes): %s", count * sizeof(T),
+                    cudaGetErrorString(e));
+    h->allocs.push_back(v);
+    *p = static_cast<T*>(v);
+    return MPM_OK;
+}
+
+void dfree(MpmHandle* h, void* p);
+inline cudaStream_t S(void* s) { return static_cast<cudaStream_t>(s); }
+
+void drop_graphs(MpmHandle* h);
+int upload_desc(MpmHandle* h);
+void bind_particles(MpmHandle* h);
+int parity(const MpmHandle* h);
+std::vector<float**> movable_f32(MpmHandle* h, PSet& p, bool for_snapshot);
+int ensure_stage(MpmHandle* h, size_t bytes);
+int sync(MpmHandle* h, cudaStream_t s);
+int read_ctl(MpmHandle* h, cudaStream_t s);
+int clear_status(MpmHandle* h, cudaStream_t s);
+int resort(MpmHandle* h, cudaStream_t s);
+int launch_steps(MpmHandle* h, int n, cudaStream_t s);
+int check_status(MpmHandle* h, int& st);
+int to_device(MpmHandle* h, const void* src, size_t bytes, int on_device, cudaStream_t s,
+              const void** dsrc);
+
+}  // namespace host
+
+// Adjoint bookkeeping (mpm_adjoint.cu): release the adjoint state of a handle;
+// note a re-sort at the current step while mpm_record runs.
+void adjoint_free(MpmHandle* h);
+void adjoint_note_resort(MpmHandle* h);
+
+}  // namespace mpm

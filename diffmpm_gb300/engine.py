@@ -243,3 +243,40 @@ class Simulation:
         a, b = C.c_int64(), C.c_int64()
         self._ok(self._lib.mpm_get_counters(self._h, C.byref(a), C.byref(b)))
         return {"resorts": a.value, "rollbacks": b.value}
+
+    # ------------------------------------------------------------------
+    def record(self, nsteps, checkpoint_steps=100, stream=None):
+        """Advance ``nsteps`` steps keeping a checkpoint every
+        ``checkpoint_steps`` steps for :meth:`adjoint`."""
+        self._ok(self._lib.mpm_record(self._h, int(nsteps), int(checkpoint_steps), stream))
+
+    def adjoint(self, dl_dloc, dl_dvel=None, *, want=("youngs_modulus", "loc", "velocity")):
+        """Reverse of the last :meth:`record` for seeds dL/dx_end (n, 2) and
+        dL/dv_end (n, 2, optional), original particle order.  Returns a dict
+        with the requested gradients at the recorded start: "youngs_modulus"
+        (n,), "loc" (n, 2), "velocity" (n, 2).  Seeds and outputs are NumPy
+        arrays, or CUDA tensors (then the outputs are CUDA tensors too)."""
+        n = self.n
+        p, dev, keep = _in_arg(dl_dloc, np.float32, n * 2)
+        pv, keepv = None, None
+        if dl_dvel is not None:
+            pv, vdev, keepv = _in_arg(dl_dvel, np.float32, n * 2)
+            if vdev != dev:
+                raise ValueError("seeds must both be host arrays or both CUDA tensors")
+        shapes = {"youngs_modulus": (n,), "loc": (n, 2), "velocity": (n, 2)}
+        out = {}
+        for k in want:
+            if dev:
+                import torch
+                out[k] = torch.empty(shapes[k], dtype=torch.float32, device=dl_dloc.device)
+            else:
+                out[k] = np.empty(shapes[k], dtype=np.float32)
+
+        def optr(k):
+            if k not in out:
+                return None
+            return C.c_void_p(out[k].data_ptr()) if dev else _lib.ptr(out[k])
+
+        self._ok(self._lib.mpm_adjoint(self._h, p, pv, optr("youngs_modulus"), optr("loc"),
+                                       optr("velocity"), dev, _stream_for(dl_dloc)))
+        return out

@@ -14,6 +14,10 @@ Inputs are seeded (NumPy PCG64); no dataset is involved.
   +-0.1 h per component, LinearElastic E=1e6, nu=0.25, rho=2000, gravity,
   roller walls (x fixed at x=0 and x=1), bottom fixed, dt=1e-6, 500 steps,
   USF or USL.
+* ``differentiation``  n x n mesh (n=256 at full size), 4 Gauss-point particles
+  per cell in the cells whose centres lie in [0.1, 0.9] x [0, 0.6] (125,664
+  particles at n=256), per-particle Young's modulus 1e6 exp(0.5 z), z ~ N(0,1)
+  seeded, nu=0.3, rho=1000, gravity, bottom fixed, USF, dt=5e-6, 2000 steps.
 * ``mixed_large``  n x n mesh (n=4096 at full size), an elastic block
   x in [0.125, 0.375] and a Newtonian block x in [0.625, 0.875], both
   y in [0, 0.5], 4 Gauss points per cell, elastic E=5e6, nu=0.3, rho=1800,
@@ -85,6 +89,37 @@ def plain_scaleup(api, n=1024, scheme="usf", sim_steps=500, seed=2024, rows=None
     solver = api.MPMExplicit(mesh, 1e-6, scheme=scheme, velocity_update=False, sim_steps=sim_steps)
     return solver, np.array([0.0, -9.81]), {"workload": f"plain_scaleup_{scheme}", "n": n,
                                              "np": len(pts), "seed": seed}
+
+
+def youngs_field(npart, seed, median=1e6, sigma_log=0.5):
+    """Log-normal per-particle Young's modulus, median * exp(sigma_log z)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return median * np.exp(sigma_log * rng.normal(size=npart))
+
+
+def differentiation(api, n=256, sim_steps=2000, dt=5e-6, seed=101, velocity=None, E=None, **kw):
+    """``E`` overrides the seeded field; ``velocity`` sets the initial particle
+    velocity (used by small test variants to make particles change cell): a
+    2-vector for all particles, or a function of the (n, 2) positions."""
+    h = 1.0 / n
+    i0 = int(np.ceil(0.1 * n - 0.5))
+    i1 = int(np.floor(0.9 * n - 0.5)) + 1
+    j1 = int(np.floor(0.6 * n - 0.5)) + 1
+    pts = gauss_points(i0, i1, 0, j1, h)
+    E = youngs_field(len(pts), seed) if E is None else np.asarray(E, dtype=np.float64)
+    mat = api.LinearElastic({"density": 1000, "youngs_modulus": 1e6, "poisson_ratio": 0.3})
+    bottom = _node_ids(n, n, lambda i, j: j == 0)
+    cons = [(bottom, api.Constraint(0, 0.0)), (bottom, api.Constraint(1, 0.0))]
+    el = _mesh(api, n, h, cons, kw)
+    ps = api.Particles(pts.reshape(-1, 1, 2), mat, np.zeros(len(pts), dtype=np.int32),
+                       youngs_modulus=E, **kw)
+    if velocity is not None:
+        v = velocity(pts) if callable(velocity) else velocity
+        ps.velocity[:] = np.broadcast_to(np.asarray(v, dtype=np.float64), pts.shape).reshape(-1, 1, 2)
+    mesh = api.Mesh2D({"particles": [ps], "elements": el, "particle_surface_traction": []})
+    solver = api.MPMExplicit(mesh, dt, scheme="usf", velocity_update=False, sim_steps=sim_steps)
+    return solver, np.array([0.0, -9.81]), {"workload": "differentiation", "n": n, "np": len(pts),
+                                             "seed": seed, "E": E}
 
 
 def mixed_large(api, n=4096, sim_steps=200, seed=7, **kw):

@@ -199,6 +199,30 @@ int mpm_set_block_steps(MpmHandle* h, int steps);
 /* Number of particle re-sorts and rolled-back step blocks so far. */
 int mpm_get_counters(const MpmHandle* h, int64_t* resorts, int64_t* rollbacks);
 
+/* Differentiation.  The reference differentiates solve_jit with jax.grad
+ * (examples/optim_1d.py:33-41,55 takes jax.value_and_grad of a loss of the
+ * final positions); these two calls are the hand-written reverse of the same
+ * steps, for the USF scheme with the per-step volume set-up
+ * (reinit_each_step = 1), LinearElastic or SimpleMaterial, without particle
+ * tractions (other configurations return MPM_ERR_UNSUPPORTED).
+ *
+ * mpm_record advances `nsteps` steps like mpm_step and keeps a checkpoint of
+ * the full state every `checkpoint_steps` steps (and at the end). */
+int mpm_record(MpmHandle* h, int nsteps, int checkpoint_steps, void* stream);
+
+/* Gradient of a loss L(x_end, v_end) through the steps of the last
+ * mpm_record, given dL/dx_end (n, 2) and dL/dv_end (n, 2; NULL = zero) in
+ * original particle order.  Writes, in original particle order, any of
+ * dL/dE (n; per-particle Young's modulus, or the material's modulus counted
+ * per particle: the sum over a material's particles is dL/dE of that
+ * material), dL/dx_0 (n, 2) and dL/dv_0 (n, 2) at the recorded start; NULL
+ * outputs are skipped.  Each segment between checkpoints is re-run to rebuild
+ * its per-step tape.  The handle is left at the recorded end state, so the
+ * call may be repeated with other seeds; any call that changes the state
+ * (step, write, set) in between makes it return MPM_ERR_STATE. */
+int mpm_adjoint(MpmHandle* h, const float* dl_dloc, const float* dl_dvel, float* dl_dE,
+                float* dl_dloc0, float* dl_dvel0, int on_device, void* stream);
+
 /* Largest mesh (nx * ny elements) mpm_volume_setup_noalloc accepts. */
 #define MPM_NOALLOC_MAX_ELEMENTS (1 << 20)
 

@@ -1,6 +1,6 @@
-"""Differentiable float64 restatement of the explicit MPM step -- TEST INFRASTRUCTURE.
+"""Differentiable restatement of the explicit MPM step -- TEST INFRASTRUCTURE.
 
-A PyTorch (CPU, float64) restatement of the same step as ``oracle.mpm_oracle``
+A PyTorch (CPU, float64 or float32) restatement of the same step as ``oracle.mpm_oracle``
 (and of the reference's diffmpm step it restates), written so that autograd
 gives the exact discrete gradient of a loss with respect to the per-particle
 Young's modulus and the initial particle state.  It is the gradient oracle of
@@ -13,6 +13,13 @@ Scope: Quadrilateral4Node mesh, USF or USL, the per-step volume set-up of
 or the material's) and SimpleMaterial, gravity, velocity constraints,
 concentrated nodal forces.  Particle cell ids and counts are piecewise constant
 in the positions and carry no gradient; so are the flush-to-zero masks.
+
+The float32 form is the gradient oracle of the float32 GPU adjoint: the
+reference's flush |a| < 1e-12 -> 0 has zero derivative, and a quantity that is
+zero in exact arithmetic (the strain rate of a uniform velocity field) lands
+below the threshold in float64 round-off (~1e-16) but above it in float32
+(~1e-6), so float32 and float64 programs can differ in which paths carry
+gradient.  Against float32 autograd the masks agree.
 """
 from __future__ import annotations
 
@@ -34,12 +41,14 @@ class TorchMPM:
     eps (N,3: xx yy xy), rho (N,), vsc (N,)`` and the persistent nodal velocity."""
 
     def __init__(self, nx, ny, hx, hy, dt, gravity, constraints, materials, mat_ids,
-                 scheme="usf", velocity_update=False, nodal_forces=()):
+                 scheme="usf", velocity_update=False, nodal_forces=(), dtype=torch.float64):
         self.nx, self.ny = nx, ny
-        f = torch.float64
+        f = self.dtype = dtype
         self.hx, self.hy = float(hx), float(hy)
-        self.node_x = torch.arange(nx + 1, dtype=f) * self.hx
-        self.node_y = torch.arange(ny + 1, dtype=f) * self.hy
+        # node coordinates as the reference forms them: float(i) * h in the
+        # working precision (diffmpm/element.py:669-679)
+        self.node_x = torch.arange(nx + 1, dtype=f) * torch.tensor(self.hx, dtype=f)
+        self.node_y = torch.arange(ny + 1, dtype=f) * torch.tensor(self.hy, dtype=f)
         self.dt = float(dt)
         self.g = torch.tensor(np.broadcast_to(np.asarray(gravity, float).reshape(-1), (2,)), dtype=f)
         nn = (nx + 1) * (ny + 1)
@@ -113,7 +122,7 @@ class TorchMPM:
                 c1, c2, c3 = le_coefficients(float(mat.properties["poisson_ratio"]))
                 Ek = E[sel] if E is not None else torch.full((int(sel.sum()),),
                                                              float(mat.properties["youngs_modulus"]),
-                                                             dtype=torch.float64)
+                                                             dtype=self.dtype)
                 a1, a2, G = Ek * c1, Ek * c2, Ek * c3
                 ds = torch.stack([a1 * d0[sel] + a2 * d1[sel], a2 * d0[sel] + a1 * d1[sel],
                                   a2 * d0[sel] + a2 * d1[sel], G * d3[sel]], dim=1)
@@ -141,7 +150,7 @@ class TorchMPM:
         x, v, s, eps, rho, vsc, nvo = (st[k] for k in ("x", "v", "sig", "eps", "rho", "vsc", "nv"))
         e, ids, N, Gx, Gy, Gcx, Gcy = self._geometry(x)
         with torch.no_grad():
-            cnt = torch.bincount(e, minlength=self.nx * self.ny).to(torch.float64)
+            cnt = torch.bincount(e, minlength=self.nx * self.ny).to(self.dtype)
         V0 = self.vol_el / cnt[e]
         m = V0 * rho
         M = self._scatter(ids, m[:, None] * N)
@@ -165,9 +174,9 @@ class TorchMPM:
         t = float(np.float64(i) * self.dt)
         for nid, d, F, fn in self.cnf:
             fval = 1.0 if fn is None else float(np.interp(t, fn.xvalues, fn.fxvalues))
-            col = torch.zeros(self.nn, 2, dtype=torch.float64)
-            col[:, d] = torch.zeros(self.nn, dtype=torch.float64).index_add(
-                0, nid, torch.full((nid.numel(),), fval * F, dtype=torch.float64))
+            col = torch.zeros(self.nn, 2, dtype=self.dtype)
+            col[:, d] = torch.zeros(self.nn, dtype=self.dtype).index_add(
+                0, nid, torch.full((nid.numel(),), fval * F, dtype=self.dtype))
             fext = fext + col
         tot = fint + fext
         a = torch.where((M == 0)[:, None], torch.zeros_like(tot), tot / safeM[:, None])
@@ -193,9 +202,10 @@ class TorchMPM:
         return st
 
 
-def from_solver(solver, gravity):
-    """TorchMPM and initial state dict from a float64 ``oracle.mpm_oracle``
-    MPMExplicit built for one particle set."""
+def from_solver(solver, gravity, dtype=torch.float64):
+    """TorchMPM and initial state dict from an ``oracle.mpm_oracle``
+    MPMExplicit built for one particle set (float64, or float32 with
+    ``dtype=torch.float32`` for the float32 discrete program)."""
     el = solver.mesh.elements
     ps = solver.mesh.particles[0]
     nx, ny = el.nelements
@@ -204,8 +214,8 @@ def from_solver(solver, gravity):
            for f in el.concentrated_nodal_forces]
     sim = TorchMPM(nx, ny, float(el.el_len[0]), float(el.el_len[1]), solver.dt, gravity, cons,
                    ps.materials, ps.material_ids, scheme=solver.scheme,
-                   velocity_update=solver.velocity_update, nodal_forces=nfs)
-    f = torch.float64
+                   velocity_update=solver.velocity_update, nodal_forces=nfs, dtype=dtype)
+    f = dtype
     n = len(ps)
     s = ps.stress.reshape(n, 6)
     e = ps.strain.reshape(n, 6)

@@ -1,0 +1,211 @@
+"""NumPy float64 restatement of the hand-written adjoint -- TEST INFRASTRUCTURE.
+
+The four reverse passes of diffmpm_gb300/csrc/mpm_adjoint_kernels.cu written
+out with NumPy scatters, over a float64 forward that keeps the same tape (the
+particle state at each step start, nodal mass, vA, vB, aB).  The CPU tests
+check that this restatement equals torch autograd of ``oracle.mpm_torch``, so
+the derivation the CUDA kernels implement is pinned without a GPU; the GPU
+tests then compare the kernels with autograd directly.
+
+Scope as the CUDA adjoint: USF, per-step volume set-up, LinearElastic with a
+per-particle E, gravity, velocity constraints.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from oracle.mpm_oracle import le_coefficients
+
+FLUSH = 1e-12
+
+
+def flush(a):
+    return np.where(np.abs(a) < FLUSH, 0.0, a)
+
+
+class Restated:
+    def __init__(self, tsim):
+        """``tsim``: an ``oracle.mpm_torch.TorchMPM`` (mesh, constraints, material)."""
+        self.nx, self.ny = tsim.nx, tsim.ny
+        self.node_x = tsim.node_x.numpy()
+        self.node_y = tsim.node_y.numpy()
+        self.dt = tsim.dt
+        self.g = tsim.g.numpy()
+        self.cmask = tsim.cmask.numpy()
+        self.cval = tsim.cval.numpy()
+        self.vol_el = float(tsim.vol_el)
+        self.nn = tsim.nn
+        self.vu = bool(tsim.velocity_update)
+        assert tsim.scheme == "usf" and len(tsim.materials) == 1
+        self.c1, self.c2, self.c3 = le_coefficients(float(tsim.materials[0].properties["poisson_ratio"]))
+
+    def geometry(self, x):
+        i = np.searchsorted(self.node_x, x[:, 0], side="right") - 1
+        j = np.searchsorted(self.node_y, x[:, 1], side="right") - 1
+        x0, x1 = self.node_x[i], self.node_x[i + 1]
+        y0, y1 = self.node_y[j], self.node_y[j + 1]
+        rx, ry = 2.0 / (x1 - x0), 2.0 / (y1 - y0)
+        xi = (x[:, 0] - (x0 + x1) / 2) * rx
+        eta = (x[:, 1] - (y0 + y1) / 2) * ry
+        ll = j * (self.nx + 1) + i
+        ids = np.stack([ll, ll + 1, ll + self.nx + 2, ll + self.nx + 1], 1)
+        a, b, c, d = 1 - xi, 1 + xi, 1 - eta, 1 + eta
+        N = np.stack([0.25 * a * c, 0.25 * b * c, 0.25 * b * d, 0.25 * a * d], 1)
+        Gx = np.stack([-0.25 * c, 0.25 * c, 0.25 * d, -0.25 * d], 1) * rx[:, None]
+        Gy = np.stack([-0.25 * a, -0.25 * b, 0.25 * b, 0.25 * a], 1) * ry[:, None]
+        Gcx = np.stack([-0.25 * rx, 0.25 * rx, 0.25 * rx, -0.25 * rx], 1)
+        Gcy = np.stack([-0.25 * ry, -0.25 * ry, 0.25 * ry, 0.25 * ry], 1)
+        e = j * self.nx + i
+        return dict(e=e, ids=ids, N=N, Gx=Gx, Gy=Gy, Gcx=Gcx, Gcy=Gcy, rx=rx, ry=ry)
+
+    def scatter(self, ids, vals):
+        out = np.zeros((self.nn,) + vals.shape[2:])
+        np.add.at(out, ids.reshape(-1), vals.reshape((-1,) + vals.shape[2:]))
+        return out
+
+    # ------------------------------------------------------------------
+    def forward(self, st, E):
+        """One step; returns (new state, tape).  State: x (n,2), v (n,2),
+        sig (n,4: xx yy zz xy), rho (n,), nv (nn,2)."""
+        x, v, s, rho, nvo = st["x"], st["v"], st["sig"], st["rho"], st["nv"]
+        G = self.geometry(x)
+        ids, N, Gx, Gy = G["ids"], G["N"], G["Gx"], G["Gy"]
+        cnt = np.bincount(G["e"], minlength=self.nx * self.ny).astype(float)
+        V0 = self.vol_el / cnt[G["e"]]
+        m = V0 * rho
+        M = self.scatter(ids, m[:, None] * N)
+        P = flush(self.scatter(ids, N[:, :, None] * (m[:, None] * v)[:, None, :]))
+        safe = np.where(M == 0, 1.0, M)
+        vA = np.where((M == 0)[:, None], nvo, P / safe[:, None])
+        vA = np.where(self.cmask, self.cval, flush(vA))
+        vx, vy = vA[ids, 0], vA[ids, 1]
+        r0 = flush((Gx * vx).sum(1))
+        r1 = flush((Gy * vy).sum(1))
+        r3 = flush((Gx * vy).sum(1) + (Gy * vx).sum(1))
+        c0 = flush((G["Gcx"] * vx).sum(1))
+        c1 = flush((G["Gcy"] * vy).sum(1))
+        dvol = self.dt * (c0 + c1)
+        d0, d1, d3 = r0 * self.dt, r1 * self.dt, r3 * self.dt
+        a1, a2, Gm = E * self.c1, E * self.c2, E * self.c3
+        s2 = s + np.stack([a1 * d0 + a2 * d1, a2 * d0 + a1 * d1, a2 * d0 + a2 * d1, Gm * d3], 1)
+        f = 1 + dvol
+        V = V0 * f
+        rho2 = rho / f
+        fx = Gx * s2[:, 0:1] + Gy * s2[:, 3:4]
+        fy = Gy * s2[:, 1:2] + Gx * s2[:, 3:4]
+        F = self.scatter(ids, np.stack([-V[:, None] * fx, -V[:, None] * fy], 2))
+        F = F + self.scatter(ids, N[:, :, None] * (m[:, None] * self.g[None, :])[:, None, :])
+        a = np.where((M == 0)[:, None], 0.0, F / safe[:, None])
+        vB = vA + a * self.dt
+        vB = flush(np.where(self.cmask, self.cval, vB))
+        aB = flush(np.where(self.cmask, 0.0, a))
+        vhat = (N[:, :, None] * vB[ids]).sum(1)
+        ahat = (N[:, :, None] * aB[ids]).sum(1)
+        v2 = vhat if self.vu else v + ahat * self.dt
+        x2 = x + vhat * self.dt
+        tape = dict(x=x, v=v, sig=s, rho=rho, M=M, vA=vA, vB=vB, aB=aB)
+        return dict(x=x2, v=v2, sig=s2, rho=rho2, nv=vB), tape
+
+    # ------------------------------------------------------------------
+    def reverse(self, tape, lam, E):
+        """Reverse of one step: ``lam`` (x, v, sig, rho adjoints of the step's
+        end state) -> adjoints of its start state; returns (lam, dL/dE part)."""
+        dt = self.dt
+        x, v, s, rho = tape["x"], tape["v"], tape["sig"], tape["rho"]
+        M, vA, vB, aB = tape["M"], tape["vA"], tape["vB"], tape["aB"]
+        G = self.geometry(x)
+        ids, N, Gx, Gy, Gcx, Gcy = G["ids"], G["N"], G["Gx"], G["Gy"], G["Gcx"], G["Gcy"]
+        live = (M != 0)[:, None]
+        safe = np.where(M == 0, 1.0, M)
+        # pass 1: transposed G2P, reverse nodal update
+        gh = lam["x"] * dt + (lam["v"] if self.vu else 0.0)
+        hh = np.zeros_like(gh) if self.vu else lam["v"] * dt
+        vBb = self.scatter(ids, N[:, :, None] * gh[:, None, :])
+        aBb = self.scatter(ids, N[:, :, None] * hh[:, None, :])
+        wb = np.where(self.cmask | (vB == 0), 0.0, vBb) * live
+        ab = (np.where(self.cmask | (aB == 0), 0.0, aBb) + wb * dt) * live
+        Fb = ab / safe[:, None]
+        Mb = -(ab * aB).sum(1) / safe
+        # pass 2: forces and stress update
+        cnt = np.bincount(G["e"], minlength=self.nx * self.ny).astype(float)
+        V0 = self.vol_el / cnt[G["e"]]
+        m = V0 * rho
+        vx, vy = vA[ids, 0], vA[ids, 1]
+        r0 = flush((Gx * vx).sum(1))
+        r1 = flush((Gy * vy).sum(1))
+        r3 = flush((Gx * vy).sum(1) + (Gy * vx).sum(1))
+        c0 = flush((Gcx * vx).sum(1))
+        c1 = flush((Gcy * vy).sum(1))
+        dvol = dt * (c0 + c1)
+        d0, d1, d3 = r0 * dt, r1 * dt, r3 * dt
+        a1, a2, Gm = E * self.c1, E * self.c2, E * self.c3
+        s2 = s + np.stack([a1 * d0 + a2 * d1, a2 * d0 + a1 * d1, a2 * d0 + a2 * d1, Gm * d3], 1)
+        f = 1 + dvol
+        V = V0 * f
+        rho2 = rho / f
+        fbx, fby = Fb[ids, 0], Fb[ids, 1]
+        fg = fbx * self.g[0] + fby * self.g[1]
+        Nb = (gh[:, None, 0] * vB[ids, 0] + gh[:, None, 1] * vB[ids, 1]
+              + hh[:, None, 0] * aB[ids, 0] + hh[:, None, 1] * aB[ids, 1] + m[:, None] * fg)
+        mb = (N * fg).sum(1)
+        fx = Gx * s2[:, 0:1] + Gy * s2[:, 3:4]
+        fy = Gy * s2[:, 1:2] + Gx * s2[:, 3:4]
+        Vb = -(fbx * fx + fby * fy).sum(1)
+        sb = lam["sig"].copy()
+        sb[:, 0] -= V * (fbx * Gx).sum(1)
+        sb[:, 1] -= V * (fby * Gy).sum(1)
+        sb[:, 3] -= V * (fbx * Gy + fby * Gx).sum(1)
+        Gxb = -V[:, None] * (fbx * s2[:, 0:1] + fby * s2[:, 3:4])
+        Gyb = -V[:, None] * (fbx * s2[:, 3:4] + fby * s2[:, 1:2])
+        d0b = a1 * sb[:, 0] + a2 * sb[:, 1] + a2 * sb[:, 2]
+        d1b = a2 * sb[:, 0] + a1 * sb[:, 1] + a2 * sb[:, 2]
+        d3b = Gm * sb[:, 3]
+        Eb = (self.c1 * (d0 * sb[:, 0] + d1 * sb[:, 1])
+              + self.c2 * (d1 * sb[:, 0] + d0 * sb[:, 1] + (d0 + d1) * sb[:, 2])
+              + self.c3 * d3 * sb[:, 3])
+        r0b = np.where(r0 != 0, d0b * dt, 0.0)
+        r1b = np.where(r1 != 0, d1b * dt, 0.0)
+        r3b = np.where(r3 != 0, d3b * dt, 0.0)
+        fb = Vb * V0 - lam["rho"] * rho2 / f
+        rhob = lam["rho"] / f + V0 * mb
+        c0b = np.where(c0 != 0, fb * dt, 0.0)
+        c1b = np.where(c1 != 0, fb * dt, 0.0)
+        Gxb = Gxb + r0b[:, None] * vx + r3b[:, None] * vy
+        Gyb = Gyb + r1b[:, None] * vy + r3b[:, None] * vx
+        sgn = np.array([1.0, -1.0, 1.0, -1.0])
+        rxy = 0.25 * G["rx"] * G["ry"]
+        xb = lam["x"].copy()
+        xb[:, 0] += (Nb * Gx).sum(1) + rxy * (Gyb * sgn).sum(1)
+        xb[:, 1] += (Nb * Gy).sum(1) + rxy * (Gxb * sgn).sum(1)
+        # pass 3: transposed strain-rate gather, reverse nodal velocity
+        vAb = wb + self.scatter(ids, np.stack([Gx * r0b[:, None] + Gy * r3b[:, None] + Gcx * c0b[:, None],
+                                               Gy * r1b[:, None] + Gx * r3b[:, None] + Gcy * c1b[:, None]], 2))
+        ub = np.where(self.cmask | (vA == 0), 0.0, vAb) * live
+        Qb = ub / safe[:, None]
+        Mbt = Mb - (ub * vA).sum(1) / safe
+        # pass 4: mass and momentum P2G
+        t = Qb[ids, 0] * v[:, None, 0] + Qb[ids, 1] * v[:, None, 1] + Mbt[ids]
+        mb2 = (N * t).sum(1)
+        vb = (0.0 if self.vu else lam["v"]) + m[:, None] * np.stack(
+            [(N * Qb[ids, 0]).sum(1), (N * Qb[ids, 1]).sum(1)], 1)
+        rhob = rhob + V0 * mb2
+        xb[:, 0] += (m[:, None] * t * Gx).sum(1)
+        xb[:, 1] += (m[:, None] * t * Gy).sum(1)
+        return dict(x=xb, v=vb, sig=sb, rho=rhob), Eb
+
+    def gradient(self, st0, E, nsteps, dl_dx, dl_dv=None):
+        """Forward ``nsteps`` steps keeping every tape, then the reverse sweep;
+        returns dict(E, x, v) of gradients at the start."""
+        tapes, st = [], dict(st0)
+        for _ in range(nsteps):
+            st, tp = self.forward(st, E)
+            tapes.append(tp)
+        n = st0["x"].shape[0]
+        dt = st0["x"].dtype
+        lam = dict(x=np.array(dl_dx, dt), v=np.zeros((n, 2), dt) if dl_dv is None else np.array(dl_dv, dt),
+                   sig=np.zeros((n, 4), dt), rho=np.zeros(n, dt))
+        gE = np.zeros(n, dt)
+        for tp in reversed(tapes):
+            lam, Eb = self.reverse(tp, lam, E)
+            gE += Eb
+        return dict(E=gE, x=lam["x"], v=lam["v"]), st

@@ -1,0 +1,199 @@
+"""The CUDA adjoint (mpm_record / mpm_adjoint) against the gradient oracle.
+
+The oracle is torch autograd of the restatement in oracle.mpm_torch, whose
+float64 gradient is checked against central finite differences on the CPU
+(tests/test_oracle_torch.py) and whose reverse passes equal the hand-derived
+ones (tests/test_adjoint_restated.py).  The GPU adjoint is the exact adjoint
+of the float32 program, so it is compared with float32 autograd (normwise
+relative error <= 1e-3); against float64 autograd it must be within 1e-3 or
+as close as float32 autograd is (within 3x) -- the float32 program's own
+conditioning (the position gradient under velocity_update differs from
+float64 by ~3e-3 in float32 autograd too).
+The initial velocity field is sheared: under a uniform velocity the strain
+rates are zero in exact arithmetic, and whether the reference's flush
+(|a| < 1e-12 -> 0, zero derivative) blocks them then depends on round-off
+ties (see oracle/mpm_torch.py), which makes the velocity gradient of that
+degenerate input differ between any two summation orders.  A central finite
+difference of the float64 oracle checks a directional derivative in E.
+"""
+import numpy as np
+import pytest
+
+import diffmpm_gb300 as D
+from diffmpm_gb300 import workloads
+from oracle import mpm_oracle as O
+
+torch = pytest.importorskip("torch")
+from oracle import mpm_torch as T  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+GRAD_TOL = 1e-3
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def sheared(p):
+    """Initial velocity (1.5 + 0.4 x + 0.8 y, 0.6 + 0.5 x - 0.3 y): particles
+    change cell, and every strain rate is far from the flush threshold."""
+    return np.stack([1.5 + 0.4 * p[:, 0] + 0.8 * p[:, 1], 0.6 + 0.5 * p[:, 0] - 0.3 * p[:, 1]],
+                    axis=1)
+
+
+CASE = dict(n=16, sim_steps=24, dt=1e-3, velocity=sheared)
+
+
+def gpu_sim(vu=False, block=None, **kw):
+    args = dict(CASE, **kw)
+    gs, g, info = workloads.differentiation(D, **args)
+    gs.velocity_update = vu
+    sim = gs.simulation(g, reinit=True)
+    gs._upload(sim)
+    sim.initialize()
+    if block:
+        sim.set_block_steps(block)
+    return gs, sim, g, info
+
+
+def seeds(n, seed=5):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return rng.normal(size=(n, 2)).astype(np.float32), rng.normal(size=(n, 2)).astype(np.float32)
+
+
+def autograd_ref(vu, W, U, dtype=torch.float32, **kw):
+    """Gradients of L = <W, x_end> + <U, v_end> by autograd of the oracle in
+    ``dtype`` (float32: the same discrete program as the GPU)."""
+    args = dict(CASE, **kw)
+    npd = np.float32 if dtype == torch.float32 else np.float64
+    o, g, info = workloads.differentiation(O, dtype=npd, **args)
+    o.velocity_update = vu
+    o.mpm_scheme.velocity_update = vu
+    tsim, st0 = T.from_solver(o, g, dtype=dtype)
+    Et = torch.tensor(info["E"], dtype=dtype, requires_grad=True)
+    x0 = st0["x"].clone().requires_grad_(True)
+    v0 = st0["v"].clone().requires_grad_(True)
+    end = tsim.run(dict(st0, x=x0, v=v0), args["sim_steps"], E=Et)
+    L = (end["x"] * torch.tensor(W, dtype=dtype)).sum() + (end["v"] * torch.tensor(U, dtype=dtype)).sum()
+    L.backward()
+    return {"youngs_modulus": Et.grad.numpy(), "loc": x0.grad.numpy(), "velocity": v0.grad.numpy(),
+            "x_end": end["x"].detach().numpy()}
+
+
+@pytest.mark.parametrize("vu", [False, True])
+def test_adjoint_matches_autograd(built, vu):
+    gs, sim, g, info = gpu_sim(vu)
+    W, U = seeds(info["np"])
+    sim.record(CASE["sim_steps"], 10)
+    x_end = sim.read("loc")
+    got = sim.adjoint(W, U)
+    ref = autograd_ref(vu, W, U)
+    ref64 = autograd_ref(vu, W, U, dtype=torch.float64)
+    fwd = rel(x_end, ref64["x_end"])
+    assert fwd < 1e-5
+    for k in ("youngs_modulus", "loc", "velocity"):
+        e, e64 = rel(got[k], ref[k]), rel(got[k], ref64[k])
+        # as close to float64 as float32 autograd itself is (within 3x)
+        assert e < GRAD_TOL and e64 <= max(GRAD_TOL, 3.0 * rel(ref[k], ref64[k])), (k, e, e64)
+
+
+def test_adjoint_checkpoint_interval_and_repeat(built):
+    """Every re-run segment reproduces the recorded run bit for bit (the
+    adjoint checks this itself and raises otherwise); a repeated call (the
+    handle is left at the recorded end) gives the same bits; and the gradient
+    hardly depends on the checkpoint interval (the interval splits the step
+    blocks, which moves the re-sorts and so the order of float32 sums)."""
+    outs = []
+    for K in (1, 7, CASE["sim_steps"]):
+        gs, sim, g, info = gpu_sim()
+        W, U = seeds(info["np"])
+        sim.record(CASE["sim_steps"], K)
+        outs.append(sim.adjoint(W, U))
+        again = sim.adjoint(W, U)
+        for k in again:
+            assert np.array_equal(again[k], outs[-1][k]), (K, k)
+    for o in outs[1:]:
+        for k in o:
+            assert rel(o[k], outs[0][k]) < 1e-5, k
+
+
+def test_adjoint_across_resorts(built):
+    """Short step blocks re-sort the particles between blocks; the recorded
+    re-sorts are replayed and the adjoint arrays permuted across them."""
+    gs, sim, g, info = gpu_sim(block=3)
+    W, U = seeds(info["np"])
+    before = sim.counters()["resorts"]
+    sim.record(CASE["sim_steps"], 10)
+    assert sim.counters()["resorts"] > before + 1
+    a = sim.adjoint(W, U)
+    ref = autograd_ref(False, W, U)
+    for k in a:
+        assert rel(a[k], ref[k]) < GRAD_TOL, k
+
+
+def test_autograd_function(built):
+    from diffmpm_gb300.autograd import explicit_run
+    gs, g, info = workloads.differentiation(D, **CASE)
+    n = info["np"]
+    W, U = seeds(n, 9)
+    dev = torch.device("cuda:0")
+    E = torch.tensor(info["E"], dtype=torch.float32, device=dev, requires_grad=True)
+    v0 = torch.tensor(gs.mesh.particles[0].velocity.reshape(n, 2), device=dev, requires_grad=True)
+    x, v = explicit_run(gs, g, E, velocity=v0, checkpoint_steps=8)
+    L = (x * torch.tensor(W, device=dev)).sum() + (v * torch.tensor(U, device=dev)).sum()
+    L.backward()
+    sim = gs.simulation(g, reinit=True)
+    direct = sim.adjoint(W, U)
+    assert np.array_equal(E.grad.cpu().numpy(), direct["youngs_modulus"])
+    assert np.array_equal(v0.grad.cpu().numpy(), direct["velocity"])
+
+
+def test_adjoint_directional_derivative_vs_finite_differences(built):
+    """<dL/dE, u> from the GPU against a central difference of the float64
+    oracle, L = mean |x_end - x_target|^2 (the differentiation workload's loss)
+    on a 32 x 32 mesh for 40 steps."""
+    kw = dict(n=32, sim_steps=40, dt=2e-4, velocity=(0.5, 0.0))
+    gs, sim, g, info = gpu_sim(**kw)
+    n = info["np"]
+    rng = np.random.Generator(np.random.PCG64(21))
+    o, g64, info64 = workloads.differentiation(O, dtype=np.float64, **dict(CASE, **kw))
+    tsim, st0 = T.from_solver(o, g64)
+    target = st0["x"].numpy() + rng.normal(scale=1e-3, size=(n, 2))
+    sim.record(kw["sim_steps"], 16)
+    x_end = sim.read("loc").astype(np.float64)
+    dl_dx = (2.0 / n) * (x_end - target)
+    grad = sim.adjoint(dl_dx.astype(np.float32), want=("youngs_modulus",))["youngs_modulus"]
+    E0 = info64["E"]
+    u = rng.normal(size=n) * E0
+    h = 1e-4
+
+    def loss(Ev):
+        with torch.no_grad():
+            end = tsim.run(dict(st0), kw["sim_steps"], E=torch.tensor(Ev))
+        return float(((end["x"].numpy() - target) ** 2).sum(1).mean())
+
+    fd = (loss(E0 + h * u) - loss(E0 - h * u)) / (2 * h)
+    gd = float(np.dot(grad.astype(np.float64), u))
+    assert abs(gd - fd) <= GRAD_TOL * abs(fd), (gd, fd)
+
+
+def test_adjoint_rejects_unsupported(built):
+    gs, g, info = workloads.plain_scaleup(D, n=16, scheme="usl", sim_steps=2)
+    sim = gs.simulation(g, reinit=True)
+    gs._upload(sim)
+    sim.initialize()
+    with pytest.raises(D.MpmError) as e:
+        sim.record(2, 1)
+    assert e.value.code == 5
+    gs, sim, g, info = gpu_sim()
+    with pytest.raises(D.MpmError) as e:
+        sim.adjoint(np.zeros((info["np"], 2), np.float32))
+    assert e.value.code == 6
+    sim.record(4, 2)
+    sim.step(1)
+    with pytest.raises(D.MpmError) as e:
+        sim.adjoint(np.zeros((info["np"], 2), np.float32))
+    assert e.value.code == 6
