@@ -6,7 +6,7 @@ Quadrilateral4Node, MPMExplicit, ...).  Every step runs in the CUDA library
 """
 from .constraint import Constraint
 from .element import Linear1D, Quadrilateral4Node
-from .engine import Simulation
+from .engine import Batch, Simulation
 from .forces import NodalForce, ParticleTraction
 from .functions import Linear, Unit
 from .material import LinearElastic, Newtonian, SimpleMaterial
@@ -17,7 +17,7 @@ from .solver import MPMExplicit
 from ._lib import MpmError, OutOfMeshError
 
 __all__ = [
-    "Constraint", "Linear1D", "Quadrilateral4Node", "Simulation", "NodalForce",
+    "Batch", "Constraint", "Linear1D", "Quadrilateral4Node", "Simulation", "NodalForce",
     "ParticleTraction", "Linear", "Unit", "LinearElastic", "Newtonian", "SimpleMaterial",
     "Mesh1D", "Mesh2D", "Nodes", "Particles", "MPMExplicit", "MpmError", "OutOfMeshError",
 ]

@@ -86,8 +86,16 @@ SIGNATURES = [
     ("mpm_time_phases", C.c_int, [_VP, C.c_int, _VP, _VP]),
     ("mpm_set_block_steps", C.c_int, [_VP, C.c_int]),
     ("mpm_get_counters", C.c_int, [_VP, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    ("mpm_set_gravity", C.c_int, [_VP, C.c_double, C.c_double]),
     ("mpm_record", C.c_int, [_VP, C.c_int, C.c_int, _VP]),
     ("mpm_adjoint", C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, C.c_int, _VP]),
+    ("mpm_batch_create", C.c_int, [C.POINTER(_VP), C.c_int, C.POINTER(_VP)]),
+    ("mpm_batch_destroy", C.c_int, [_VP]),
+    ("mpm_batch_last_error", C.c_char_p, [_VP]),
+    ("mpm_batch_size", C.c_int, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    ("mpm_batch_step", C.c_int, [_VP, C.c_int, _VP]),
+    ("mpm_batch_set_block_steps", C.c_int, [_VP, C.c_int]),
+    ("mpm_batch_autotune", C.c_int, [_VP, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float), _VP]),
     ("mpm_volume_setup_noalloc", C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_int64,
                                            _VP, _VP, _VP, _VP, _VP, _VP]),
 ]
@@ -115,6 +123,14 @@ def load():
 def check(code, handle=None):
     if code != MPM_OK:
         msg = load().mpm_last_error(handle).decode(errors="replace")
+        if code == 3:
+            raise OutOfMeshError(code, msg)
+        raise MpmError(code, msg)
+
+
+def check_batch(code, batch=None):
+    if code != MPM_OK:
+        msg = load().mpm_batch_last_error(batch).decode(errors="replace")
         if code == 3:
             raise OutOfMeshError(code, msg)
         raise MpmError(code, msg)

@@ -179,28 +179,19 @@ int resort(MpmHandle* h, cudaStream_t s) {
 }
 
 int take_snapshot(MpmHandle* h, cudaStream_t s) {
-    std::vector<float**> f = movable_f32(h, h->ps[h->pcur], true);
-    if (h->snap_f.size() != f.size()) return fail(h, MPM_ERR_STATE, "snapshot layout mismatch");
-    for (size_t i = 0; i < f.size(); ++i)
-        CK(h, cudaMemcpyAsync(h->snap_f[i], *f[i], sizeof(float) * h->np, cudaMemcpyDeviceToDevice, s));
-    CK(h, cudaMemcpyAsync(h->snap_cflag, h->cflag, h->ncell, cudaMemcpyDeviceToDevice, s));
-    CK(h, cudaMemcpyAsync(h->snap_nvbx, h->nvbx, sizeof(float) * h->nn, cudaMemcpyDeviceToDevice, s));
-    CK(h, cudaMemcpyAsync(h->snap_nvby, h->nvby, sizeof(float) * h->nn, cudaMemcpyDeviceToDevice, s));
-    return MPM_OK;
+    if (h->snap_f.size() != movable_f32(h, h->ps[h->pcur], true).size())
+        return fail(h, MPM_ERR_STATE, "snapshot layout mismatch");
+    std::vector<CopySeg> v;
+    snapshot_segments(h, true, v);
+    return run_segments(h, h->segbuf, v, s);
 }
 
 int restore_snapshot(MpmHandle* h, int64_t step0, cudaStream_t s) {
     h->step = step0;
-    std::vector<float**> f = movable_f32(h, h->ps[h->pcur], true);
-    for (size_t i = 0; i < f.size(); ++i)
-        CK(h, cudaMemcpyAsync(*f[i], h->snap_f[i], sizeof(float) * h->np, cudaMemcpyDeviceToDevice, s));
-    CK(h, cudaMemcpyAsync(h->cflag, h->snap_cflag, h->ncell, cudaMemcpyDeviceToDevice, s));
-    CK(h, cudaMemcpyAsync(h->nvbx, h->snap_nvbx, sizeof(float) * h->nn, cudaMemcpyDeviceToDevice, s));
-    CK(h, cudaMemcpyAsync(h->nvby, h->snap_nvby, sizeof(float) * h->nn, cudaMemcpyDeviceToDevice, s));
-    Control c{};
-    c.step = (int)step0;
-    *h->h_ctl = c;
-    CK(h, cudaMemcpyAsync(h->ctl, h->h_ctl, sizeof(Control), cudaMemcpyHostToDevice, s));
+    std::vector<CopySeg> v;
+    snapshot_segments(h, false, v);
+    TRY(run_segments(h, h->segbuf, v, s));
+    TRY(clear_status(h, s));
     return sync(h, s);
 }
 
@@ -391,6 +382,25 @@ int copy_passive(MpmHandle* h, int field, float* aos, bool to_aos, cudaStream_t 
     return MPM_OK;
 }
 
+// Roll the block that started at step0 back to its snapshot and replay its B
+// steps one at a time, re-sorting before each step; `st` gets the last status.
+int replay_block(MpmHandle* h, int64_t step0, int B, int& st, cudaStream_t s) {
+    h->rollbacks++;
+    TRY(restore_snapshot(h, step0, s));
+    for (int i = 0; i < B; ++i) {
+        TRY(resort(h, s));
+        TRY(launch_steps(h, 1, s));
+        h->step++;
+        TRY(read_ctl(h, s));
+        TRY(check_status(h, st));
+        if (st & ST_DRIFT_VIOLATION)
+            return fail(h, MPM_ERR_CFL, "a particle crossed more than one cell in one step (step %lld)",
+                        (long long)h->step - 1);
+        TRY(clear_status(h, s));
+    }
+    return MPM_OK;
+}
+
 }  // namespace host
 }  // namespace mpm
 
@@ -572,6 +582,7 @@ int mpm_create(const MpmDesc* d, MpmHandle** out) {
     A(&h->snap_cflag, (size_t)h->ncell);
     A(&h->snap_nvbx, (size_t)h->nn);
     A(&h->snap_nvby, (size_t)h->nn);
+    A(&h->snap_ctl, 1);
     A(&h->ds, 1);
     A(&h->ctl, 1);
     A(&h->d_ptrs, 16);
@@ -641,6 +652,7 @@ int mpm_create(const MpmDesc* d, MpmHandle** out) {
 int mpm_destroy(MpmHandle* h) {
     if (!h) return MPM_OK;
     mpm::adjoint_free(h);
+    segbuf_free(h->segbuf);
     drop_graphs(h);
     if (h->cap) cudaStreamDestroy(h->cap);
     for (void* p : h->allocs) cudaFree(p);
@@ -936,21 +948,7 @@ int mpm_step(MpmHandle* h, int nsteps, void* stream) {
         TRY(read_ctl(h, s));
         int st = 0;
         TRY(check_status(h, st));
-        if (st & ST_DRIFT_VIOLATION) {
-            // replay the block one step at a time, re-sorting before each step
-            h->rollbacks++;
-            TRY(restore_snapshot(h, step0, s));
-            for (int i = 0; i < B; ++i) {
-                TRY(resort(h, s));
-                TRY(launch_steps(h, 1, s));
-                h->step++;
-                TRY(read_ctl(h, s));
-                TRY(check_status(h, st));
-                if (st & ST_DRIFT_VIOLATION)
-                    return fail(h, MPM_ERR_CFL, "a particle crossed more than one cell in one step (step %lld)", (long long)h->step - 1);
-                TRY(clear_status(h, s));
-            }
-        }
+        if (st & ST_DRIFT_VIOLATION) TRY(replay_block(h, step0, B, st, s));
         h->needs_resort = (st & ST_DRIFTED) != 0;
         TRY(clear_status(h, s));
         nsteps -= B;
@@ -1021,6 +1019,16 @@ int mpm_time_phases(MpmHandle* h, int nsteps, float* ms_out, void* stream) {
     h->needs_resort = (st & (ST_DRIFTED | ST_DRIFT_VIOLATION)) != 0;
     TRY(clear_status(h, s));
     return MPM_OK;
+}
+
+int mpm_set_gravity(MpmHandle* h, double gx, double gy) {
+    if (!h) return MPM_ERR_INVALID;
+    h->gen++;
+    h->gx = (float)gx;
+    h->gy = (float)gy;
+    h->hs.gx = h->gx;
+    h->hs.gy = h->gy;
+    return upload_desc(h);
 }
 
 int mpm_set_block_steps(MpmHandle* h, int steps) {

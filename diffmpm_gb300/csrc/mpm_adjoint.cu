@@ -35,16 +35,6 @@ constexpr int NTN = 7;     // tape per node: m vAx vAy vBx vBy aBx aBy
 constexpr int NPS = 5;     // per-particle scratch: r0b r1b r3b c0b c1b
 constexpr int NNS = 8;     // per-node scratch: fbx fby mb vabx vaby qbx qby mbt
 
-struct Checkpoint {
-    int64_t step = 0;
-    bool needs_resort = false;
-    std::vector<float*> f;   // movable_f32(.., false) of the particle set
-    uint8_t* mat = nullptr;
-    int* cstart = nullptr;
-    uint8_t* cflag = nullptr;
-    float *nvbx = nullptr, *nvby = nullptr;
-};
-
 struct Epoch {               // arrays of one sort epoch inside a segment
     int* pid = nullptr;
     uint8_t* mat = nullptr;
@@ -82,18 +72,8 @@ struct AdjointState {
 
 namespace {
 
-void free_checkpoint(MpmHandle* h, Checkpoint& c) {
-    for (float* p : c.f) dfree(h, p);
-    dfree(h, c.mat);
-    dfree(h, c.cstart);
-    dfree(h, c.cflag);
-    dfree(h, c.nvbx);
-    dfree(h, c.nvby);
-    c = Checkpoint{};
-}
-
 void free_buffers(MpmHandle* h, AdjointState* a) {
-    for (auto& c : a->ck) free_checkpoint(h, c);
+    for (auto& c : a->ck) checkpoint_free(h, c);
     a->ck.clear();
     for (float*& p : a->tp) { dfree(h, p); p = nullptr; }
     for (float*& p : a->tn) { dfree(h, p); p = nullptr; }
@@ -137,49 +117,17 @@ void fit(MpmHandle* h, AdjointState* a) {
 int save_checkpoint(MpmHandle* h, AdjointState* a, size_t idx, cudaStream_t s) {
     if (a->ck.size() <= idx) a->ck.resize(idx + 1);
     Checkpoint& c = a->ck[idx];
-    const size_t np = (size_t)h->np;
-    std::vector<float**> f = movable_f32(h, h->ps[h->pcur], false);
-    if (c.f.size() != f.size()) {
-        free_checkpoint(h, c);
-        c.f.assign(f.size(), nullptr);
-        for (float*& p : c.f) TRY(dalloc(h, &p, np));
-        TRY(dalloc(h, &c.mat, np));
-        TRY(dalloc(h, &c.cstart, (size_t)h->ncell + 2));
-        TRY(dalloc(h, &c.cflag, (size_t)h->ncell));
-        TRY(dalloc(h, &c.nvbx, (size_t)h->nn));
-        TRY(dalloc(h, &c.nvby, (size_t)h->nn));
-    }
-    for (size_t i = 0; i < f.size(); ++i)
-        CK(h, cudaMemcpyAsync(c.f[i], *f[i], sizeof(float) * np, cudaMemcpyDeviceToDevice, s));
-    CK(h, cudaMemcpyAsync(c.mat, h->ps[h->pcur].mat, np, cudaMemcpyDeviceToDevice, s));
-    CK(h, cudaMemcpyAsync(c.cstart, h->cstart[h->cs_cur], sizeof(int) * (h->ncell + 2),
-                          cudaMemcpyDeviceToDevice, s));
-    CK(h, cudaMemcpyAsync(c.cflag, h->cflag, h->ncell, cudaMemcpyDeviceToDevice, s));
-    CK(h, cudaMemcpyAsync(c.nvbx, h->nvbx, sizeof(float) * h->nn, cudaMemcpyDeviceToDevice, s));
-    CK(h, cudaMemcpyAsync(c.nvby, h->nvby, sizeof(float) * h->nn, cudaMemcpyDeviceToDevice, s));
-    c.step = h->step;
-    c.needs_resort = h->needs_resort;
-    return MPM_OK;
+    TRY(checkpoint_alloc(h, c));
+    std::vector<CopySeg> v;
+    checkpoint_segments(h, c, true, v);
+    return run_segments(h, h->segbuf, v, s);
 }
 
-int restore_checkpoint(MpmHandle* h, const Checkpoint& c, cudaStream_t s) {
-    h->step = c.step;   // selects the ping-pong parity the data goes to
-    const size_t np = (size_t)h->np;
-    std::vector<float**> f = movable_f32(h, h->ps[h->pcur], false);
-    if (f.size() != c.f.size()) return fail(h, MPM_ERR_STATE, "checkpoint layout mismatch");
-    for (size_t i = 0; i < f.size(); ++i)
-        CK(h, cudaMemcpyAsync(*f[i], c.f[i], sizeof(float) * np, cudaMemcpyDeviceToDevice, s));
-    CK(h, cudaMemcpyAsync(h->ps[h->pcur].mat, c.mat, np, cudaMemcpyDeviceToDevice, s));
-    CK(h, cudaMemcpyAsync(h->cstart[h->cs_cur], c.cstart, sizeof(int) * (h->ncell + 2),
-                          cudaMemcpyDeviceToDevice, s));
-    CK(h, cudaMemcpyAsync(h->cflag, c.cflag, h->ncell, cudaMemcpyDeviceToDevice, s));
-    CK(h, cudaMemcpyAsync(h->nvbx, c.nvbx, sizeof(float) * h->nn, cudaMemcpyDeviceToDevice, s));
-    CK(h, cudaMemcpyAsync(h->nvby, c.nvby, sizeof(float) * h->nn, cudaMemcpyDeviceToDevice, s));
-    Control ctl{};
-    ctl.step = (int)c.step;
-    *h->h_ctl = ctl;
-    CK(h, cudaMemcpyAsync(h->ctl, h->h_ctl, sizeof(Control), cudaMemcpyHostToDevice, s));
-    h->needs_resort = c.needs_resort;
+int restore_checkpoint(MpmHandle* h, Checkpoint& c, cudaStream_t s) {
+    std::vector<CopySeg> v;
+    checkpoint_segments(h, c, false, v);
+    TRY(run_segments(h, h->segbuf, v, s));
+    TRY(clear_status(h, s));
     return sync(h, s);
 }
 

@@ -1,0 +1,338 @@
+// Batches: many independent simulations advanced together, one launch per
+// phase per step for all of them.
+//
+// A batch groups simulation handles of one configuration (scheme, volume
+// set-up, tractions) on one GPU.  Their tiles form one tile list, each tile
+// tagged with its simulation's index; the batched kernels read that
+// simulation's descriptor (the handle's device copy, which a re-sort updates in
+// place) and control block through two pointer tables, so a captured graph of
+// a step block stays valid across re-sorts.  Per block: re-sort the
+// simulations that drifted, snapshot all of them (one segmented copy), run the
+// block graph, gather every status word in one copy; a simulation whose
+// particle drifted two cells is rolled back and replayed alone, step by step.
+// No counterpart in the reference, which runs one simulation per solve.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <map>
+#include <set>
+#include <string>
+#include <vector>
+
+#include "mpm_handle.h"
+
+using namespace mpm;
+using namespace mpm::host;
+
+struct MpmBatch {
+    int device = 0;
+    std::vector<MpmHandle*> sims;
+    StepConfig cfg{};
+    const SimDev** d_sims = nullptr;
+    Control** d_ctls = nullptr;
+    int4* d_tiles = nullptr;
+    int ntiles = 0;
+    Control* d_status = nullptr;
+    Control* h_status = nullptr;   // pinned
+    int block_steps = 100;
+    cudaStream_t cap = nullptr;
+    std::map<int, cudaGraphExec_t> graphs;
+    SegBuf segbuf;
+    std::vector<Checkpoint> tune;  // per-simulation state saved by the autotuner
+    std::string err;
+};
+
+namespace {
+
+thread_local std::string g_batch_create_error;
+
+int bfail(MpmBatch* b, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (b) b->err = buf;
+    else g_batch_create_error = buf;
+    return code;
+}
+
+// A failure reported on simulation i's handle, copied to the batch.
+int from_sim(MpmBatch* b, int i, int code) {
+    return bfail(b, code, "simulation %d: %s", i, b->sims[i]->err.c_str());
+}
+
+#define BCK(b, call)                                                                       \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess)                                                             \
+            return bfail(b, MPM_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_));        \
+    } while (0)
+
+#define BTRY(b, i, x)                                  \
+    do {                                               \
+        int r_ = (x);                                  \
+        if (r_ != MPM_OK) return from_sim(b, i, r_);   \
+    } while (0)
+
+void drop_batch_graphs(MpmBatch* b) {
+    for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
+    b->graphs.clear();
+}
+
+int launch_batch_steps(MpmBatch* b, int n, cudaStream_t s) {
+    for (int i = 0; i < n; ++i) {
+        BCK(b, launch_nodal_kinematics_batch(b->cfg, b->d_sims, b->d_ctls, b->d_tiles, b->ntiles, s));
+        BCK(b, launch_forces_batch(b->cfg, b->d_sims, b->d_ctls, b->d_tiles, b->ntiles, s));
+        BCK(b, launch_particle_kinematics_batch(b->cfg, b->d_sims, b->d_ctls, b->d_tiles, b->ntiles, s));
+    }
+    return MPM_OK;
+}
+
+int run_batch_graph(MpmBatch* b, int n, cudaStream_t s) {
+    auto it = b->graphs.find(n);
+    if (it == b->graphs.end()) {
+        cudaGraph_t g = nullptr;
+        BCK(b, cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal));
+        int r = launch_batch_steps(b, n, b->cap);
+        cudaError_t e = cudaStreamEndCapture(b->cap, &g);
+        if (r != MPM_OK) {
+            if (g) cudaGraphDestroy(g);
+            return r;
+        }
+        BCK(b, e);
+        cudaGraphExec_t ex = nullptr;
+        e = cudaGraphInstantiate(&ex, g, 0);
+        cudaGraphDestroy(g);
+        BCK(b, e);
+        it = b->graphs.emplace(n, ex).first;
+    }
+    BCK(b, cudaGraphLaunch(it->second, s));
+    return MPM_OK;
+}
+
+int check_ready(MpmBatch* b) {
+    for (size_t i = 0; i < b->sims.size(); ++i) {
+        MpmHandle* h = b->sims[i];
+        if (!h->initialized || h->np <= 0)
+            return bfail(b, MPM_ERR_STATE, "simulation %zu is not initialised with particles", i);
+        if (h->has_trac != b->cfg.traction)
+            return bfail(b, MPM_ERR_STATE, "simulation %zu changed its traction set-up", i);
+    }
+    return MPM_OK;
+}
+
+// Gather every simulation's control block into h_status and clear the status words.
+int read_statuses(MpmBatch* b, cudaStream_t s) {
+    const int n = (int)b->sims.size();
+    BCK(b, launch_gather_status(b->d_ctls, n, b->d_status, s));
+    BCK(b, cudaMemcpyAsync(b->h_status, b->d_status, sizeof(Control) * n, cudaMemcpyDeviceToHost, s));
+    BCK(b, cudaStreamSynchronize(s));
+    return MPM_OK;
+}
+
+// One block of B steps for every simulation (see the file comment).
+int batch_block(MpmBatch* b, int B, cudaStream_t s) {
+    const int n = (int)b->sims.size();
+    for (int i = 0; i < n; ++i)
+        if (b->sims[i]->needs_resort) BTRY(b, i, resort(b->sims[i], s));
+    std::vector<CopySeg> v;
+    for (MpmHandle* h : b->sims) snapshot_segments(h, true, v);
+    BTRY(b, 0, run_segments(b->sims[0], b->segbuf, v, s));
+    std::vector<int64_t> step0(n);
+    for (int i = 0; i < n; ++i) step0[i] = b->sims[i]->step;
+    int r = run_batch_graph(b, B, s);
+    if (r != MPM_OK) return r;
+    for (MpmHandle* h : b->sims) {
+        h->step += B;
+        h->gen++;
+    }
+    r = read_statuses(b, s);
+    if (r != MPM_OK) return r;
+    for (int i = 0; i < n; ++i) {
+        MpmHandle* h = b->sims[i];
+        int st = b->h_status[i].status;
+        if (st & ST_OUT_OF_MESH)
+            return bfail(b, MPM_ERR_OUT_OF_MESH, "simulation %d: a particle left the mesh", i);
+        if (st & ST_DRIFT_VIOLATION) BTRY(b, i, replay_block(h, step0[i], B, st, s));
+        h->needs_resort = (st & ST_DRIFTED) != 0;
+    }
+    return MPM_OK;
+}
+
+int batch_steps(MpmBatch* b, int nsteps, cudaStream_t s) {
+    while (nsteps > 0) {
+        const int B = std::min(nsteps, b->block_steps);
+        const int r = batch_block(b, B, s);
+        if (r != MPM_OK) return r;
+        nsteps -= B;
+    }
+    return MPM_OK;
+}
+
+// Save (or restore) the full state of every simulation in b->tune.
+int tune_state(MpmBatch* b, bool save, cudaStream_t s) {
+    const int n = (int)b->sims.size();
+    if ((int)b->tune.size() != n) b->tune.resize(n);
+    std::vector<CopySeg> v;
+    for (int i = 0; i < n; ++i) {
+        if (save) BTRY(b, i, checkpoint_alloc(b->sims[i], b->tune[i]));
+        checkpoint_segments(b->sims[i], b->tune[i], save, v);
+    }
+    BTRY(b, 0, run_segments(b->sims[0], b->segbuf, v, s));
+    BCK(b, cudaStreamSynchronize(s));
+    return MPM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mpm_batch_create(MpmHandle* const* sims, int n, MpmBatch** out) {
+    if (!out || !sims || n < 1) return bfail(nullptr, MPM_ERR_INVALID, "need at least one simulation");
+    *out = nullptr;
+    std::set<MpmHandle*> seen;
+    for (int i = 0; i < n; ++i) {
+        MpmHandle* h = sims[i];
+        if (!h) return bfail(nullptr, MPM_ERR_INVALID, "simulation %d is null", i);
+        if (!seen.insert(h).second) return bfail(nullptr, MPM_ERR_INVALID, "simulation %d appears twice", i);
+        if (!h->initialized || h->np <= 0)
+            return bfail(nullptr, MPM_ERR_STATE, "simulation %d is not initialised with particles", i);
+        if (h->device != sims[0]->device)
+            return bfail(nullptr, MPM_ERR_INVALID, "simulations are on different devices");
+        if (h->usl != sims[0]->usl || h->reinit != sims[0]->reinit || h->has_trac != sims[0]->has_trac)
+            return bfail(nullptr, MPM_ERR_UNSUPPORTED,
+                         "simulation %d: a batch needs one scheme, volume set-up and traction set-up", i);
+    }
+    MpmBatch* b = new MpmBatch();
+    b->device = sims[0]->device;
+    b->sims.assign(sims, sims + n);
+    b->cfg.usl = sims[0]->usl;
+    b->cfg.reinit = sims[0]->reinit;
+    b->cfg.traction = sims[0]->has_trac;
+    std::vector<int4> tiles;
+    std::vector<const SimDev*> ds(n);
+    std::vector<Control*> ctl(n);
+    for (int i = 0; i < n; ++i) {
+        const SimDev& S = sims[i]->hs;
+        for (int ty = 0; ty < S.tiles_y; ++ty)
+            for (int tx = 0; tx < S.tiles_x; ++tx) tiles.push_back(make_int4(i, tx, ty, 0));
+        ds[i] = sims[i]->ds;
+        ctl[i] = sims[i]->ctl;
+    }
+    b->ntiles = (int)tiles.size();
+    auto bail = [&](const char* what, cudaError_t e) {
+        bfail(nullptr, MPM_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+        mpm_batch_destroy(b);
+        return e == cudaErrorMemoryAllocation ? MPM_ERR_NOMEM : MPM_ERR_CUDA;
+    };
+    cudaError_t e;
+    if ((e = cudaMalloc(&b->d_sims, sizeof(SimDev*) * n)) != cudaSuccess) return bail("cudaMalloc", e);
+    if ((e = cudaMalloc(&b->d_ctls, sizeof(Control*) * n)) != cudaSuccess) return bail("cudaMalloc", e);
+    if ((e = cudaMalloc(&b->d_tiles, sizeof(int4) * tiles.size())) != cudaSuccess) return bail("cudaMalloc", e);
+    if ((e = cudaMalloc(&b->d_status, sizeof(Control) * n)) != cudaSuccess) return bail("cudaMalloc", e);
+    if ((e = cudaMallocHost(&b->h_status, sizeof(Control) * n)) != cudaSuccess) return bail("cudaMallocHost", e);
+    if ((e = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking)) != cudaSuccess)
+        return bail("cudaStreamCreate", e);
+    if ((e = cudaMemcpy(b->d_sims, ds.data(), sizeof(SimDev*) * n, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(b->d_ctls, ctl.data(), sizeof(Control*) * n, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(b->d_tiles, tiles.data(), sizeof(int4) * tiles.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return bail("cudaMemcpy", e);
+    *out = b;
+    return MPM_OK;
+}
+
+int mpm_batch_destroy(MpmBatch* b) {
+    if (!b) return MPM_OK;
+    drop_batch_graphs(b);
+    for (size_t i = 0; i < b->tune.size() && i < b->sims.size(); ++i) checkpoint_free(b->sims[i], b->tune[i]);
+    segbuf_free(b->segbuf);
+    if (b->cap) cudaStreamDestroy(b->cap);
+    cudaFree(b->d_sims);
+    cudaFree(b->d_ctls);
+    cudaFree(b->d_tiles);
+    cudaFree(b->d_status);
+    if (b->h_status) cudaFreeHost(b->h_status);
+    delete b;
+    return MPM_OK;
+}
+
+const char* mpm_batch_last_error(const MpmBatch* b) {
+    return b ? b->err.c_str() : g_batch_create_error.c_str();
+}
+
+int mpm_batch_size(const MpmBatch* b, int* n, int* ntiles) {
+    if (!b) return MPM_ERR_INVALID;
+    if (n) *n = (int)b->sims.size();
+    if (ntiles) *ntiles = b->ntiles;
+    return MPM_OK;
+}
+
+int mpm_batch_set_block_steps(MpmBatch* b, int steps) {
+    if (!b || steps < 1) return MPM_ERR_INVALID;
+    b->block_steps = steps;
+    return MPM_OK;
+}
+
+int mpm_batch_step(MpmBatch* b, int nsteps, void* stream) {
+    if (!b) return MPM_ERR_INVALID;
+    if (nsteps < 0) return bfail(b, MPM_ERR_INVALID, "nsteps must be >= 0");
+    int r = check_ready(b);
+    if (r != MPM_OK) return r;
+    cudaStream_t s = S(stream);
+    r = batch_steps(b, nsteps, s);
+    if (r != MPM_OK) return r;
+    BCK(b, cudaStreamSynchronize(s));
+    return MPM_OK;
+}
+
+int mpm_batch_autotune(MpmBatch* b, int trial_steps, int* block_steps, float* ms_per_step,
+                       void* stream) {
+    if (!b || trial_steps < 1) return MPM_ERR_INVALID;
+    int r = check_ready(b);
+    if (r != MPM_OK) return r;
+    cudaStream_t s = S(stream);
+    std::vector<int> cand;
+    for (int c : {10, 25, 50, 100, 200})
+        if (c <= trial_steps) cand.push_back(c);
+    if (cand.empty()) cand.push_back(trial_steps);
+    r = tune_state(b, true, s);
+    if (r != MPM_OK) return r;
+    cudaEvent_t e0, e1;
+    BCK(b, cudaEventCreate(&e0));
+    BCK(b, cudaEventCreate(&e1));
+    int best = cand.back();
+    float best_ms = -1.0f;
+    for (int c : cand) {
+        b->block_steps = c;
+        // first pass captures the block graphs; the second is timed
+        for (int pass = 0; pass < 2 && r == MPM_OK; ++pass) {
+            r = tune_state(b, false, s);
+            if (r != MPM_OK) break;
+            if (cudaEventRecord(e0, s) != cudaSuccess) r = bfail(b, MPM_ERR_CUDA, "event record");
+            if (r == MPM_OK) r = batch_steps(b, trial_steps, s);
+            if (r == MPM_OK && cudaEventRecord(e1, s) != cudaSuccess) r = bfail(b, MPM_ERR_CUDA, "event record");
+            if (r == MPM_OK && cudaEventSynchronize(e1) != cudaSuccess) r = bfail(b, MPM_ERR_CUDA, "event sync");
+        }
+        if (r != MPM_OK) break;
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (best_ms < 0.0f || ms < best_ms) {
+            best_ms = ms;
+            best = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    const int r2 = tune_state(b, false, s);
+    if (r != MPM_OK) return r;
+    if (r2 != MPM_OK) return r2;
+    b->block_steps = best;
+    if (block_steps) *block_steps = best;
+    if (ms_per_step) *ms_per_step = best_ms / (float)trial_steps;
+    return MPM_OK;
+}
+
+}  // extern "C"

@@ -28,6 +28,28 @@ struct PSet {
 
 struct AdjointState;   // checkpoints, tape and adjoint arrays (mpm_adjoint.cu)
 
+// Full copy of the state of one simulation that steps and re-sorts change:
+// the particle arrays (storage order, current ping-pong parity), material ids,
+// cell starts, drift flags, the persistent nodal velocity and the control
+// block.
+struct Checkpoint {
+    int64_t step = 0;
+    bool needs_resort = false;
+    std::vector<float*> f;   // movable_f32(.., false) of the particle set
+    uint8_t* mat = nullptr;
+    int* cstart = nullptr;
+    uint8_t* cflag = nullptr;
+    float *nvbx = nullptr, *nvby = nullptr;
+    Control* ctl = nullptr;
+};
+
+// Device tables of a segmented copy (grown on demand).
+struct SegBuf {
+    CopySeg* segs = nullptr;
+    unsigned* first = nullptr;
+    size_t cap = 0;
+};
+
 }  // namespace mpm
 
 struct MpmHandle {
@@ -70,6 +92,8 @@ struct MpmHandle {
     std::vector<float*> snap_f;
     uint8_t* snap_cflag = nullptr;
     float *snap_nvbx = nullptr, *snap_nvby = nullptr;
+    mpm::Control* snap_ctl = nullptr;
+    mpm::SegBuf segbuf;
     // descriptors
     mpm::SimDev hs{};
     mpm::SimDev* ds = nullptr;
@@ -146,8 +170,24 @@ int clear_status(MpmHandle* h, cudaStream_t s);
 int resort(MpmHandle* h, cudaStream_t s);
 int launch_steps(MpmHandle* h, int n, cudaStream_t s);
 int check_status(MpmHandle* h, int& st);
+int take_snapshot(MpmHandle* h, cudaStream_t s);
+int replay_block(MpmHandle* h, int64_t step0, int B, int& st, cudaStream_t s);
 int to_device(MpmHandle* h, const void* src, size_t bytes, int on_device, cudaStream_t s,
               const void** dsrc);
+
+
+// Whole-state copies as segment lists (mpm_state.cu).  The snapshot of a step
+// block goes to the handle's snap_* arrays; a checkpoint to its own arrays.
+// A restore first sets the step counter (which selects the ping-pong parity
+// the data goes to) and needs_resort from the saved values.
+void snapshot_segments(MpmHandle* h, bool save, std::vector<CopySeg>& out);
+int checkpoint_alloc(MpmHandle* h, Checkpoint& c);
+void checkpoint_free(MpmHandle* h, Checkpoint& c);
+void checkpoint_segments(MpmHandle* h, Checkpoint& c, bool save, std::vector<CopySeg>& out);
+// Copy the segments in one launch on stream s (tables kept in `buf`, which
+// owns its device memory; errors are reported on h).
+int run_segments(MpmHandle* h, SegBuf& buf, const std::vector<CopySeg>& segs, cudaStream_t s);
+void segbuf_free(SegBuf& buf);
 
 }  // namespace host
 

@@ -26,6 +26,16 @@ __device__ __forceinline__ int load_step(const Control* ctl) {
     return *reinterpret_cast<const volatile int*>(&ctl->step);
 }
 
+// Batched launches: the CTA copies the descriptor of its simulation into
+// shared memory (one word per thread) before the tile work starts.
+__device__ __forceinline__ void load_sim(const SimDev* __restrict__ src, SimDev& dst) {
+    static_assert(sizeof(SimDev) % 4 == 0, "descriptor copied in 4-byte words");
+    const int* a = reinterpret_cast<const int*>(src);
+    int* b = reinterpret_cast<int*>(&dst);
+    for (int i = threadIdx.x; i < (int)(sizeof(SimDev) / 4); i += blockDim.x) b[i] = a[i];
+    __syncthreads();
+}
+
 // Visit, in a fixed order, the particles whose current cell is (ci, cj):
 // sort-cells (ci+di, cj+dj) row by row; a neighbour is scanned only when its
 // drift flag is set, and particles of a flagged sort-cell are tested.
@@ -395,9 +405,8 @@ constexpr int K1_DEPTH = 4;
 constexpr int K1_NF = 5;   // x, y, vx, vy, rho (solve_jit) or mass (solve)
 
 template <bool REINIT>
-__global__ void __launch_bounds__(TILE_THREADS, 2)
-k_nodal_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
-                   Control* __restrict__ ctl) {
+__device__ __forceinline__ void nodal_kinematics_tile(const SimDev& S, const int4 T,
+                                                      Control* __restrict__ ctl) {
     constexpr int NQ = 12;
     __shared__ float s_c[NQ][SC_STRIDE];               // [m, px, py] x corner, per cell
     __shared__ float s_slot[TILE_CY][NQ][SLOT_STRIDE]; // per-warp particle contributions
@@ -405,7 +414,6 @@ k_nodal_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__ ti
     __shared__ int s_cs[TILE_CY][33];
     __shared__ float s_V0[TILE_CY][32];
     __shared__ TileGeo G;
-    const int4 T = tiles[blockIdx.x];
     const int parity = load_step(ctl) & 1;
     const int tid = threadIdx.x, lx = tid & (TILE_CX - 1), ly = tid / TILE_CX;
     const int c0x = T.y * TILE_NX - 1, c0y = T.z * TILE_NY - 1;
@@ -487,6 +495,23 @@ k_nodal_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__ ti
     }
 }
 
+template <bool REINIT>
+__global__ void __launch_bounds__(TILE_THREADS, 2)
+k_nodal_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
+                   Control* __restrict__ ctl) {
+    nodal_kinematics_tile<REINIT>(S, tiles[blockIdx.x], ctl);
+}
+
+template <bool REINIT>
+__global__ void __launch_bounds__(TILE_THREADS, 2)
+k_nodal_kinematics_batch(const SimDev* const* __restrict__ sims, Control* const* __restrict__ ctls,
+                         const int4* __restrict__ tiles) {
+    __shared__ SimDev sS;
+    const int4 T = tiles[blockIdx.x];
+    load_sim(sims[T.x], sS);
+    nodal_kinematics_tile<REINIT>(sS, T, ctls[T.x]);
+}
+
 // Nodal update shared by both schemes: concentrated forces (element.py:270-284),
 // a = nan_to_num(f/m), v += a dt, constraints, flush (element.py:305-329).
 // (fx, fy) is the summed internal plus external force of the particles.
@@ -527,9 +552,8 @@ constexpr int NV_H = TILE_CY + 1;
 constexpr int K2_DEPTH = 2;
 
 template <bool USL, bool REINIT, bool TRAC>
-__global__ void __launch_bounds__(TILE_THREADS, 2)
-k_forces(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
-         Control* __restrict__ ctl) {
+__device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
+                                            Control* __restrict__ ctl) {
     constexpr int NQ = 8;
     __shared__ float s_c[NQ][SC_STRIDE];               // [f x, f y] x corner, per cell
     __shared__ float s_slot[TILE_CY][NQ][SLOT_STRIDE];
@@ -538,7 +562,6 @@ k_forces(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
     __shared__ float s_V0[TILE_CY][32], s_size0[TILE_CY][32], s_dvol[TILE_CY][32];
     __shared__ float s_vx[NV_W * NV_H], s_vy[NV_W * NV_H];
     __shared__ TileGeo G;
-    const int4 T = tiles[blockIdx.x];
     const int step = load_step(ctl);
     const int parity = step & 1;
     const float t = step_time(step, S.dt);
@@ -653,6 +676,23 @@ k_forces(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
     }
 }
 
+template <bool USL, bool REINIT, bool TRAC>
+__global__ void __launch_bounds__(TILE_THREADS, 2)
+k_forces(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
+         Control* __restrict__ ctl) {
+    forces_tile<USL, REINIT, TRAC>(S, tiles[blockIdx.x], ctl);
+}
+
+template <bool USL, bool REINIT, bool TRAC>
+__global__ void __launch_bounds__(TILE_THREADS, 2)
+k_forces_batch(const SimDev* const* __restrict__ sims, Control* const* __restrict__ ctls,
+               const int4* __restrict__ tiles) {
+    __shared__ SimDev sS;
+    const int4 T = tiles[blockIdx.x];
+    load_sim(sims[T.x], sS);
+    forces_tile<USL, REINIT, TRAC>(sS, T, ctls[T.x]);
+}
+
 // ---------------------------------------------------------------------------
 // Phase 3: G2P (diffmpm/particle.py:208-247): v_hat = sum N v_i,
 // a_hat = sum N a_i, v_p = v_hat or v_p + a_hat dt, x_p += v_hat dt.  USL adds
@@ -687,9 +727,8 @@ struct G2PStage {
 };
 
 template <bool USL, bool REINIT>
-__global__ void __launch_bounds__(TILE_THREADS, 2)
-k_particle_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
-                      Control* __restrict__ ctl) {
+__device__ __forceinline__ void particle_kinematics_tile(const SimDev& S, const int4 T,
+                                                         Control* __restrict__ ctl) {
     constexpr int NF = G2PStage<USL>::NF, DEPTH = G2PStage<USL>::DEPTH;
     __shared__ float s_vx[G_W * G_H], s_vy[G_W * G_H], s_ax[G_W * G_H], s_ay[G_W * G_H];
     __shared__ float s_stage[TILE_CY][DEPTH][NF][32];
@@ -698,7 +737,6 @@ k_particle_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__
     __shared__ int s_flag[TILE_CY][32];   // drift flag after this step
     __shared__ int s_status;
     __shared__ TileGeo G;
-    const int4 T = tiles[blockIdx.x];
     const int step = load_step(ctl);
     const int parity = step & 1, next = parity ^ 1;
     const int tid = threadIdx.x, lane = tid & 31, w = tid / 32;
@@ -887,12 +925,29 @@ k_particle_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__
         // last CTA to finish advances the step counter (every CTA has read it)
         __threadfence();
         const unsigned prev = atomicAdd(&ctl->done, 1u);
-        if (prev == gridDim.x - 1) {
+        if (prev == (unsigned)(S.tiles_x * S.tiles_y) - 1u) {
             ctl->done = 0u;
             ctl->step = step + 1;
             __threadfence();
         }
     }
+}
+
+template <bool USL, bool REINIT>
+__global__ void __launch_bounds__(TILE_THREADS, 2)
+k_particle_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
+                      Control* __restrict__ ctl) {
+    particle_kinematics_tile<USL, REINIT>(S, tiles[blockIdx.x], ctl);
+}
+
+template <bool USL, bool REINIT>
+__global__ void __launch_bounds__(TILE_THREADS, 2)
+k_particle_kinematics_batch(const SimDev* const* __restrict__ sims, Control* const* __restrict__ ctls,
+                            const int4* __restrict__ tiles) {
+    __shared__ SimDev sS;
+    const int4 T = tiles[blockIdx.x];
+    load_sim(sims[T.x], sS);
+    particle_kinematics_tile<USL, REINIT>(sS, T, ctls[T.x]);
 }
 
 // ---------------------------------------------------------------------------
@@ -963,6 +1018,66 @@ cudaError_t launch_particle_kinematics(const StepConfig& c, const SimDev& S, con
     } else {
         if (c.reinit) particle_kinematics<false, true>(S, tiles, ntiles, ctl, s);
         else particle_kinematics<false, false>(S, tiles, ntiles, ctl, s);
+    }
+    return cudaGetLastError();
+}
+
+// Batched launches: one grid over the tiles of every simulation of a batch.
+template <bool REINIT>
+static void nodal_kinematics_batch(const SimDev* const* sims, Control* const* ctls,
+                                   const int4* tiles, int ntiles, cudaStream_t s) {
+    prefer_shared(k_nodal_kinematics_batch<REINIT>);
+    k_nodal_kinematics_batch<REINIT><<<ntiles, TILE_THREADS, 0, s>>>(sims, ctls, tiles);
+}
+
+cudaError_t launch_nodal_kinematics_batch(const StepConfig& c, const SimDev* const* sims,
+                                          Control* const* ctls, const int4* tiles, int ntiles,
+                                          cudaStream_t s) {
+    if (c.reinit) nodal_kinematics_batch<true>(sims, ctls, tiles, ntiles, s);
+    else nodal_kinematics_batch<false>(sims, ctls, tiles, ntiles, s);
+    return cudaGetLastError();
+}
+
+template <bool USL, bool REINIT, bool TRAC>
+static void forces_batch(const SimDev* const* sims, Control* const* ctls, const int4* tiles,
+                         int ntiles, cudaStream_t s) {
+    prefer_shared(k_forces_batch<USL, REINIT, TRAC>);
+    k_forces_batch<USL, REINIT, TRAC><<<ntiles, TILE_THREADS, 0, s>>>(sims, ctls, tiles);
+}
+
+cudaError_t launch_forces_batch(const StepConfig& c, const SimDev* const* sims,
+                                Control* const* ctls, const int4* tiles, int ntiles,
+                                cudaStream_t s) {
+    const int key = (c.usl ? 4 : 0) | (c.reinit ? 2 : 0) | (c.traction ? 1 : 0);
+    switch (key) {
+        case 0: forces_batch<false, false, false>(sims, ctls, tiles, ntiles, s); break;
+        case 1: forces_batch<false, false, true>(sims, ctls, tiles, ntiles, s); break;
+        case 2: forces_batch<false, true, false>(sims, ctls, tiles, ntiles, s); break;
+        case 3: forces_batch<false, true, true>(sims, ctls, tiles, ntiles, s); break;
+        case 4: forces_batch<true, false, false>(sims, ctls, tiles, ntiles, s); break;
+        case 5: forces_batch<true, false, true>(sims, ctls, tiles, ntiles, s); break;
+        case 6: forces_batch<true, true, false>(sims, ctls, tiles, ntiles, s); break;
+        default: forces_batch<true, true, true>(sims, ctls, tiles, ntiles, s); break;
+    }
+    return cudaGetLastError();
+}
+
+template <bool USL, bool REINIT>
+static void particle_kinematics_batch(const SimDev* const* sims, Control* const* ctls,
+                                      const int4* tiles, int ntiles, cudaStream_t s) {
+    prefer_shared(k_particle_kinematics_batch<USL, REINIT>);
+    k_particle_kinematics_batch<USL, REINIT><<<ntiles, TILE_THREADS, 0, s>>>(sims, ctls, tiles);
+}
+
+cudaError_t launch_particle_kinematics_batch(const StepConfig& c, const SimDev* const* sims,
+                                             Control* const* ctls, const int4* tiles, int ntiles,
+                                             cudaStream_t s) {
+    if (c.usl) {
+        if (c.reinit) particle_kinematics_batch<true, true>(sims, ctls, tiles, ntiles, s);
+        else particle_kinematics_batch<true, false>(sims, ctls, tiles, ntiles, s);
+    } else {
+        if (c.reinit) particle_kinematics_batch<false, true>(sims, ctls, tiles, ntiles, s);
+        else particle_kinematics_batch<false, false>(sims, ctls, tiles, ntiles, s);
     }
     return cudaGetLastError();
 }
@@ -1298,6 +1413,55 @@ cudaError_t launch_deinterleave2(const float* in, int n, float* a, float* b, cud
 cudaError_t launch_node_momentum(const float* m, const float* vx, const float* vy, int n,
                                  float* out, cudaStream_t s) {
     if (n > 0) k_node_momentum<<<(n + 255) / 256, 256, 0, s>>>(m, vx, vy, n, out);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Segmented copy and status gather for batches
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+k_copy_segments(const CopySeg* __restrict__ segs, const unsigned* __restrict__ first, int nseg) {
+    const unsigned b = blockIdx.x;
+    int lo = 0, hi = nseg - 1;
+    #pragma unroll 1
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (first[mid] <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    const CopySeg sg = segs[lo];
+    const unsigned long long off = (unsigned long long)(b - first[lo]) * COPY_CHUNK;
+    if (off >= sg.bytes) return;
+    const unsigned long long end = min(off + COPY_CHUNK, sg.bytes);
+    const char* src = static_cast<const char*>(sg.src);
+    char* dst = static_cast<char*>(sg.dst);
+    const bool vec = ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15) == 0;
+    unsigned long long i = off;
+    if (vec) {
+        const unsigned long long vend = off + ((end - off) & ~15ull);
+        for (unsigned long long k = off + 16ull * threadIdx.x; k < vend; k += 16ull * blockDim.x)
+            *reinterpret_cast<uint4*>(dst + k) = *reinterpret_cast<const uint4*>(src + k);
+        i = vend;
+    }
+    for (unsigned long long k = i + threadIdx.x; k < end; k += blockDim.x) dst[k] = src[k];
+}
+
+cudaError_t launch_copy_segments(const CopySeg* segs, const unsigned* first, int nseg,
+                                 unsigned nblocks, cudaStream_t s) {
+    if (nseg > 0 && nblocks > 0) k_copy_segments<<<nblocks, 256, 0, s>>>(segs, first, nseg);
+    return cudaGetLastError();
+}
+
+__global__ void k_gather_status(Control* const* __restrict__ ctls, int n, Control* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Control* c = ctls[i];
+    out[i] = *c;
+    c->status = 0;
+}
+
+cudaError_t launch_gather_status(Control* const* ctls, int n, Control* out, cudaStream_t s) {
+    if (n > 0) k_gather_status<<<(n + 127) / 128, 128, 0, s>>>(ctls, n, out);
     return cudaGetLastError();
 }
 

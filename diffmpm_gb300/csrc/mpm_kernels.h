@@ -23,6 +23,19 @@ cudaError_t launch_forces(const StepConfig& c, const SimDev& S, const int4* tile
 cudaError_t launch_particle_kinematics(const StepConfig& c, const SimDev& S, const int4* tiles,
                                        int ntiles, Control* ctl, cudaStream_t s);
 
+// The same three phases for a batch of simulations in one launch each: tile
+// t works on simulation tiles[t].x, whose descriptor is sims[tiles[t].x] and
+// whose step counter and status are in ctls[tiles[t].x].
+cudaError_t launch_nodal_kinematics_batch(const StepConfig& c, const SimDev* const* sims,
+                                          Control* const* ctls, const int4* tiles, int ntiles,
+                                          cudaStream_t s);
+cudaError_t launch_forces_batch(const StepConfig& c, const SimDev* const* sims,
+                                Control* const* ctls, const int4* tiles, int ntiles,
+                                cudaStream_t s);
+cudaError_t launch_particle_kinematics_batch(const StepConfig& c, const SimDev* const* sims,
+                                             Control* const* ctls, const int4* tiles, int ntiles,
+                                             cudaStream_t s);
+
 // Re-sort of one simulation's particles by current cell, stable in storage order.
 struct SortScratch {
     int* count;        // ncell + 1 (last bucket: particles outside the mesh)
@@ -72,6 +85,21 @@ cudaError_t launch_interleave2(const float* a, const float* b, int n, float* out
 cudaError_t launch_deinterleave2(const float* in, int n, float* a, float* b, cudaStream_t s);
 cudaError_t launch_node_momentum(const float* m, const float* vx, const float* vy, int n,
                                  float* out, cudaStream_t s);
+
+// Copy of many device-memory segments in one launch (snapshots and checkpoints
+// of whole batches).  Segment i is copied by the CTAs first[i] .. first[i+1]-1,
+// COPY_CHUNK bytes each; first[nseg] is the grid size.
+struct CopySeg {
+    const void* src;
+    void* dst;
+    unsigned long long bytes;
+};
+constexpr unsigned COPY_CHUNK = 8192;
+cudaError_t launch_copy_segments(const CopySeg* segs, const unsigned* first, int nseg,
+                                 unsigned nblocks, cudaStream_t s);
+
+// out[i] = *ctls[i], then ctls[i]->status = 0, for i < n.
+cudaError_t launch_gather_status(Control* const* ctls, int n, Control* out, cudaStream_t s);
 
 // Set the calling thread's message returned by mpm_last_error(NULL).
 void set_thread_error(const std::string& msg);

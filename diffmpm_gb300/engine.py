@@ -239,6 +239,10 @@ class Simulation:
     def set_block_steps(self, n):
         self._ok(self._lib.mpm_set_block_steps(self._h, int(n)))
 
+    def set_gravity(self, gravity):
+        g = np.broadcast_to(np.asarray(gravity, dtype=np.float64).reshape(-1), (2,))
+        self._ok(self._lib.mpm_set_gravity(self._h, float(g[0]), float(g[1])))
+
     def counters(self):
         a, b = C.c_int64(), C.c_int64()
         self._ok(self._lib.mpm_get_counters(self._h, C.byref(a), C.byref(b)))
@@ -280,3 +284,53 @@ class Simulation:
         self._ok(self._lib.mpm_adjoint(self._h, p, pv, optr("youngs_modulus"), optr("loc"),
                                        optr("velocity"), dev, _stream_for(dl_dloc)))
         return out
+
+
+class Batch:
+    """Simulations advanced together, one kernel launch per phase per step for
+    all of them (include/diffmpm_gb300.h, mpm_batch_*).  The members stay
+    ordinary ``Simulation`` objects: set them up and read them as usual."""
+
+    def __init__(self, sims: Sequence[Simulation]):
+        self._lib = _lib.load()
+        self.sims = list(sims)
+        handles = (C.c_void_p * len(self.sims))(*[s._h.value for s in self.sims])
+        self._b = C.c_void_p()
+        rc = self._lib.mpm_batch_create(handles, len(self.sims), C.byref(self._b))
+        if rc != _lib.MPM_OK:
+            self._b = C.c_void_p()
+            _lib.check_batch(rc, None)
+
+    def _ok(self, rc):
+        _lib.check_batch(rc, self._b)
+
+    def close(self):
+        if self._b:
+            self._lib.mpm_batch_destroy(self._b)
+            self._b = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def size(self):
+        """(number of simulations, tiles per phase launch)."""
+        n, t = C.c_int(), C.c_int()
+        self._ok(self._lib.mpm_batch_size(self._b, C.byref(n), C.byref(t)))
+        return n.value, t.value
+
+    def step(self, nsteps=1, stream=None):
+        self._ok(self._lib.mpm_batch_step(self._b, int(nsteps), stream))
+
+    def set_block_steps(self, n):
+        self._ok(self._lib.mpm_batch_set_block_steps(self._b, int(n)))
+
+    def autotune(self, trial_steps=100, stream=None):
+        """Pick the step-block size by timing; the state is left unchanged.
+        Returns (block_steps, ms_per_step)."""
+        blk, ms = C.c_int(), C.c_float()
+        self._ok(self._lib.mpm_batch_autotune(self._b, int(trial_steps), C.byref(blk), C.byref(ms),
+                                              stream))
+        return blk.value, ms.value

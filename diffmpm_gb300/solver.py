@@ -68,9 +68,10 @@ class MPMExplicit:
         return fns
 
     def simulation(self, gravity, reinit=True) -> Simulation:
-        """The GPU simulation for this configuration (cached per gravity/mode)."""
+        """The GPU simulation for this configuration (cached per mode, scheme,
+        velocity update and dt), with ``gravity`` set."""
         g = np.broadcast_to(np.asarray(gravity, dtype=np.float64).reshape(-1), (2,))
-        key = (float(g[0]), float(g[1]), bool(reinit))
+        key = (bool(reinit), self.scheme, bool(self.velocity_update), float(self.dt))
         if key not in self._sims:
             el = self.mesh.elements
             _, mats, _, _ = self._population()
@@ -80,7 +81,12 @@ class MPMExplicit:
                 constraints=el.constraints, functions=self._functions(),
                 nodal_forces=el.concentrated_nodal_forces, materials=mats,
                 ndim=getattr(el, "ndim", 2))
-        return self._sims[key]
+            self._sims[key].gravity = tuple(g)
+        sim = self._sims[key]
+        if sim.gravity != tuple(g):
+            sim.set_gravity(g)
+            sim.gravity = tuple(g)
+        return sim
 
     def _upload(self, sim: Simulation):
         sets, mats, mat_index, offsets = self._population()

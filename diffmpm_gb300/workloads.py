@@ -18,6 +18,17 @@ Inputs are seeded (NumPy PCG64); no dataset is involved.
   per cell in the cells whose centres lie in [0.1, 0.9] x [0, 0.6] (125,664
   particles at n=256), per-particle Young's modulus 1e6 exp(0.5 z), z ~ N(0,1)
   seeded, nu=0.3, rho=1000, gravity, bottom fixed, USF, dt=5e-6, 2000 steps.
+* ``batch_specs`` / ``batch_member``  independent simulations of uneven size
+  (512 at full size): mesh side uniform in {32, ..., 256}, 4 Gauss-point
+  particles per cell in a seeded random rectangle of cells covering 20-60% of
+  the domain, resting on the fixed bottom and kept 5% of the width from the
+  side walls and the top (so that 1000 steps of gravity keep every particle in
+  the mesh), E log-uniform in [1e5, 1e8], nu uniform
+  in [0.2, 0.35], rho=1500, gravity, dt = 0.3 h / v_p with the P-wave
+  velocity of diffmpm/material.py:73-81, USF with velocity_update=True (with
+  the default False the reference's own step goes unstable on the softest
+  members within 1000 steps: in the float32 oracle particle 147 of member 86
+  leaves the mesh at step 963).
 * ``mixed_large``  n x n mesh (n=4096 at full size), an elastic block
   x in [0.125, 0.375] and a Newtonian block x in [0.625, 0.875], both
   y in [0, 0.5], 4 Gauss points per cell, elastic E=5e6, nu=0.3, rho=1800,
@@ -120,6 +131,46 @@ def differentiation(api, n=256, sim_steps=2000, dt=5e-6, seed=101, velocity=None
     solver = api.MPMExplicit(mesh, dt, scheme="usf", velocity_update=False, sim_steps=sim_steps)
     return solver, np.array([0.0, -9.81]), {"workload": "differentiation", "n": n, "np": len(pts),
                                              "seed": seed, "E": E}
+
+
+def batch_specs(nsims=512, seed=5, sides=(32, 256), area=(0.2, 0.6), E=(1e5, 1e8),
+                nu=(0.2, 0.35), rho=1500.0, cfl=0.3):
+    """Seeded parameters of the batch members (plain dicts)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for _ in range(nsims):
+        n = int(rng.integers(sides[0], sides[1] + 1))
+        a = rng.uniform(*area)
+        aspect = np.exp(rng.uniform(np.log(0.5), np.log(2.0)))
+        margin = int(np.ceil(0.05 * n))
+        w = min(0.9, np.sqrt(a * aspect))
+        hgt = min(0.9, a / w)
+        wc = max(1, min(n - 2 * margin, int(round(w * n))))
+        hc = max(1, min(n - margin, int(round(hgt * n))))
+        i0 = int(rng.integers(margin, n - margin - wc + 1))
+        Ek = float(np.exp(rng.uniform(np.log(E[0]), np.log(E[1]))))
+        nuk = float(rng.uniform(*nu))
+        M = Ek * (1 - nuk) / ((1 + nuk) * (1 - 2 * nuk))
+        dt = cfl * (1.0 / n) / np.sqrt(M / rho)
+        out.append({"side": n, "cells": (i0, i0 + wc, 0, hc), "E": Ek, "nu": nuk, "rho": rho,
+                    "dt": float(dt), "np": 4 * wc * hc})
+    return out
+
+
+def batch_member(api, spec, sim_steps=1000, **kw):
+    n = spec["side"]
+    h = 1.0 / n
+    pts = gauss_points(*spec["cells"], h)
+    mat = api.LinearElastic({"density": spec["rho"], "youngs_modulus": spec["E"],
+                             "poisson_ratio": spec["nu"]})
+    bottom = _node_ids(n, n, lambda i, j: j == 0)
+    cons = [(bottom, api.Constraint(0, 0.0)), (bottom, api.Constraint(1, 0.0))]
+    el = _mesh(api, n, h, cons, kw)
+    ps = api.Particles(pts.reshape(-1, 1, 2), mat, np.zeros(len(pts), dtype=np.int32), **kw)
+    mesh = api.Mesh2D({"particles": [ps], "elements": el, "particle_surface_traction": []})
+    solver = api.MPMExplicit(mesh, spec["dt"], scheme="usf", velocity_update=True,
+                             sim_steps=sim_steps)
+    return solver, np.array([0.0, -9.81]), {"workload": "batch_member", "n": n, "np": len(pts)}
 
 
 def mixed_large(api, n=4096, sim_steps=200, seed=7, **kw):

@@ -196,6 +196,10 @@ int mpm_time_phases(MpmHandle* h, int nsteps, float* ms_out, void* stream);
 /* Steps per captured CUDA graph (default 100). */
 int mpm_set_block_steps(MpmHandle* h, int steps);
 
+/* Replace desc.gravity (the `gravity` argument of solve_jit / solve,
+ * diffmpm/solver.py:116,159), so one handle serves solves with any gravity. */
+int mpm_set_gravity(MpmHandle* h, double gx, double gy);
+
 /* Number of particle re-sorts and rolled-back step blocks so far. */
 int mpm_get_counters(const MpmHandle* h, int64_t* resorts, int64_t* rollbacks);
 
@@ -222,6 +226,32 @@ int mpm_record(MpmHandle* h, int nsteps, int checkpoint_steps, void* stream);
  * (step, write, set) in between makes it return MPM_ERR_STATE. */
 int mpm_adjoint(MpmHandle* h, const float* dl_dloc, const float* dl_dvel, float* dl_dE,
                 float* dl_dloc0, float* dl_dvel0, int on_device, void* stream);
+
+/* Batches of independent simulations.  No counterpart in the reference, which
+ * runs one simulation per solve; a batch advances many (of any mesh and
+ * particle counts) with one kernel launch per phase per step for all of
+ * them, captured in CUDA graphs of step blocks.  The handles must be
+ * initialised, on one device, and share the scheme, volume set-up and
+ * traction set-up; each keeps its own state, so mpm_read_field etc. work on
+ * them as usual.  Destroy the batch before its handles. */
+typedef struct MpmBatch MpmBatch;
+
+int mpm_batch_create(MpmHandle* const* sims, int n, MpmBatch** out);
+int mpm_batch_destroy(MpmBatch* b);
+/* Message of the last failure on b (NULL: of the last mpm_batch_create). */
+const char* mpm_batch_last_error(const MpmBatch* b);
+/* Number of simulations and of tiles (CTAs per phase launch). */
+int mpm_batch_size(const MpmBatch* b, int* n, int* ntiles);
+/* Advance every simulation by `nsteps` steps (as mpm_step does for one). */
+int mpm_batch_step(MpmBatch* b, int nsteps, void* stream);
+/* Steps per captured graph (default 100). */
+int mpm_batch_set_block_steps(MpmBatch* b, int steps);
+/* Time `trial_steps` steps with each candidate block size (10, 25, 50, 100,
+ * 200 up to trial_steps) from the current state, keep the fastest, and put
+ * every simulation back in the state it had.  Outputs (may be NULL): the
+ * chosen block size and its device time per step in ms. */
+int mpm_batch_autotune(MpmBatch* b, int trial_steps, int* block_steps, float* ms_per_step,
+                       void* stream);
 
 /* Largest mesh (nx * ny elements) mpm_volume_setup_noalloc accepts. */
 #define MPM_NOALLOC_MAX_ELEMENTS (1 << 20)

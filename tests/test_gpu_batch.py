@@ -1,0 +1,128 @@
+"""Batches of independent simulations (mpm_batch_*) against single runs.
+
+A batch runs the same tile kernels over the tiles of all its simulations, so
+every member must end bit for bit where the same simulation run alone (with
+the same step-block size, hence the same re-sort schedule) ends, and within
+the parity tolerances of the oracle.
+"""
+import numpy as np
+import pytest
+
+import diffmpm_gb300 as D
+from diffmpm_gb300 import workloads
+from oracle import mpm_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("loc", "velocity", "stress", "strain", "density")
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+def small_specs(k=5, seed=3):
+    return workloads.batch_specs(nsims=k, seed=seed, sides=(12, 40))
+
+
+def member_sim(spec, steps):
+    solver, g, info = workloads.batch_member(D, spec, sim_steps=steps)
+    sim = solver.simulation(g, reinit=True)
+    solver._upload(sim)
+    sim.initialize()
+    return solver, sim, g
+
+
+def state(sim):
+    return {k: sim.read(k).copy() for k in FIELDS}
+
+
+def test_batch_equals_single_runs(built):
+    specs = small_specs()
+    steps = 60
+    members = [member_sim(sp, steps) for sp in specs]
+    batch = D.Batch([m[1] for m in members])
+    n, ntiles = batch.size()
+    assert n == len(specs) and ntiles > n
+    batch.set_block_steps(20)
+    batch.step(steps)
+    for sp in specs:
+        _, alone, _ = member_sim(sp, steps)
+        alone.set_block_steps(20)
+        alone.step(steps)
+        ref = state(alone)
+        got = state(members[specs.index(sp)][1])
+        for k in FIELDS:
+            assert np.array_equal(got[k], ref[k]), (sp["side"], k)
+    for _, sim, _ in members:
+        assert sim.step_index == steps
+
+
+def test_batch_member_matches_oracle(built):
+    spec = small_specs(k=1, seed=11)[0]
+    steps = 40
+    solver, sim, g = member_sim(spec, steps)
+    other = member_sim(small_specs(k=2, seed=12)[1], steps)
+    batch = D.Batch([sim, other[1]])
+    batch.step(steps)
+    o, og, _ = workloads.batch_member(O, spec, sim_steps=steps)
+    exp = o.solve_jit(og)
+    assert rel(sim.read("loc"), exp["loc"].reshape(-1, 2)) < 1e-4
+    assert rel(sim.read("velocity"), exp["velocity"].reshape(-1, 2)) < 1e-4
+
+
+def test_autotune_leaves_state_unchanged(built):
+    specs = small_specs(k=4, seed=7)
+    members = [member_sim(sp, 30) for sp in specs]
+    batch = D.Batch([m[1] for m in members])
+    batch.step(5)
+    before = [state(m[1]) for m in members]
+    steps_before = [m[1].step_index for m in members]
+    blk, ms = batch.autotune(trial_steps=30)
+    assert blk in (10, 25) and ms > 0
+    for m, st, sb in zip(members, before, steps_before):
+        assert m[1].step_index == sb
+        now = state(m[1])
+        for k in FIELDS:
+            assert np.array_equal(now[k], st[k]), k
+
+
+def test_batch_rollback_matches_single(built):
+    """A member whose particles drift two cells inside a block is rolled back
+    and replayed alone, exactly as a single run does."""
+    # 0.3 cells per step: within 5 steps particles cross two cell edges
+    specs = small_specs(k=3, seed=9)
+    fast = workloads.plain_small(D, sim_steps=5, dt=2e-3, velocity=(15.0, 0.0))
+    members = [member_sim(sp, 5) for sp in specs]
+    gs, g, _ = fast
+    fsim = gs.simulation(g, reinit=True)
+    gs._upload(fsim)
+    fsim.initialize()
+    batch = D.Batch([members[0][1], fsim, members[1][1], members[2][1]])
+    batch.set_block_steps(5)
+    batch.step(5)
+    assert fsim.counters()["rollbacks"] >= 1
+    alone_solver, ag, _ = workloads.plain_small(D, sim_steps=5, dt=2e-3, velocity=(15.0, 0.0))
+    alone = alone_solver.simulation(ag, reinit=True)
+    alone_solver._upload(alone)
+    alone.initialize()
+    alone.set_block_steps(5)
+    alone.step(5)
+    for k in FIELDS:
+        assert np.array_equal(fsim.read(k), alone.read(k)), k
+
+
+def test_batch_rejects_mixed_configurations(built):
+    a = member_sim(small_specs(k=1)[0], 5)[1]
+    s2, g2, _ = workloads.plain_scaleup(D, n=16, scheme="usl", sim_steps=2)
+    b = s2.simulation(g2, reinit=True)
+    s2._upload(b)
+    b.initialize()
+    with pytest.raises(D.MpmError) as e:
+        D.Batch([a, b])
+    assert e.value.code == 5
+    with pytest.raises(D.MpmError):
+        D.Batch([a, a])
