@@ -96,6 +96,9 @@ SIGNATURES = [
     ("mpm_batch_step", C.c_int, [_VP, C.c_int, _VP]),
     ("mpm_batch_set_block_steps", C.c_int, [_VP, C.c_int]),
     ("mpm_batch_autotune", C.c_int, [_VP, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float), _VP]),
+    ("mpm_batch_record", C.c_int, [_VP, C.c_int, C.c_int, _VP]),
+    ("mpm_batch_adjoint", C.c_int, [_VP, C.POINTER(_VP), C.POINTER(_VP), C.POINTER(_VP),
+                                    C.POINTER(_VP), C.POINTER(_VP), C.c_int, _VP]),
     ("mpm_volume_setup_noalloc", C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_int64,
                                            _VP, _VP, _VP, _VP, _VP, _VP]),
 ]

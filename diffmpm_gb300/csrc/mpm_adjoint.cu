@@ -10,20 +10,30 @@
 // step matches the recorded run), then runs the four reverse passes of
 // mpm_adjoint.h for each step from the last to the first.  The adjoint arrays
 // follow the storage order of the step being reversed; where a re-sort
-// separates two steps they are permuted through the original particle order.
+// separates two steps they are permuted through the original particle order,
+// and after a segment they are left in the order of its checkpoint, which is
+// the order the re-run of the previous segment ends in (the re-run is checked
+// to reproduce the recorded state bit for bit).
 // Memory: one checkpoint per segment (the particle state, cell starts and
 // persistent nodal velocity) and a tape of K steps (9 floats per particle, 7
 // per node and 1 byte per cell per step).
+//
+// mpm_batch_record / mpm_batch_adjoint do the same for every simulation of a
+// batch in lockstep: each re-run step, tape copy and reverse pass is one
+// launch for all simulations (segmented copies with a slot offset, and the
+// reverse passes over a table of per-simulation arguments).
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <vector>
 
 #include "mpm_adjoint.h"
+#include "mpm_batch.h"
 #include "mpm_handle.h"
 
 using namespace mpm;
 using namespace mpm::host;
+
 
 namespace mpm {
 
@@ -59,15 +69,28 @@ struct AdjointState {
     float* tn[NTN] = {};
     std::vector<Epoch> epochs;
     std::vector<int> epoch_of;
+    int nep = 0;               // epochs captured in the current segment
     float* lam[NLAM] = {};
     float* lam_tmp = nullptr;
-    int* lam_pid = nullptr;
     float** d_lam = nullptr;
     float* pscr[NPS] = {};
     float* nscr[NNS] = {};
     int* cnt = nullptr;
     int* mismatch = nullptr;   // device counter of the re-run check
     int* h_mismatch = nullptr; // pinned
+};
+
+// Scratch of a batched adjoint (owned by the batch).
+struct BatchAdjoint {
+    AdjStep* d_bases = nullptr;
+    AdjStep* d_table = nullptr;
+    std::vector<AdjStep> bases;
+    int2* node_blocks = nullptr;
+    int2* part_blocks = nullptr;
+    int n_node_blocks = 0, n_part_blocks = 0;
+    SegBuf tape_p[2], tape_n, misc;
+    int* mismatch = nullptr;
+    int* h_mismatch = nullptr;
 };
 
 namespace {
@@ -91,7 +114,6 @@ void free_buffers(MpmHandle* h, AdjointState* a) {
     for (float*& p : a->pscr) { dfree(h, p); p = nullptr; }
     for (float*& p : a->nscr) { dfree(h, p); p = nullptr; }
     dfree(h, a->lam_tmp);
-    dfree(h, a->lam_pid);
     dfree(h, a->d_lam);
     dfree(h, a->cnt);
     dfree(h, a->mismatch);
@@ -99,7 +121,6 @@ void free_buffers(MpmHandle* h, AdjointState* a) {
     a->mismatch = nullptr;
     a->h_mismatch = nullptr;
     a->lam_tmp = nullptr;
-    a->lam_pid = nullptr;
     a->d_lam = nullptr;
     a->cnt = nullptr;
     a->np_alloc = -1;
@@ -114,13 +135,11 @@ void fit(MpmHandle* h, AdjointState* a) {
     }
 }
 
-int save_checkpoint(MpmHandle* h, AdjointState* a, size_t idx, cudaStream_t s) {
+int save_checkpoint(MpmHandle* h, AdjointState* a, size_t idx, std::vector<CopySeg>& v) {
     if (a->ck.size() <= idx) a->ck.resize(idx + 1);
-    Checkpoint& c = a->ck[idx];
-    TRY(checkpoint_alloc(h, c));
-    std::vector<CopySeg> v;
-    checkpoint_segments(h, c, true, v);
-    return run_segments(h, h->segbuf, v, s);
+    TRY(checkpoint_alloc(h, a->ck[idx]));
+    checkpoint_segments(h, a->ck[idx], true, v);
+    return MPM_OK;
 }
 
 int restore_checkpoint(MpmHandle* h, Checkpoint& c, cudaStream_t s) {
@@ -149,7 +168,6 @@ int ensure_adjoint_buffers(MpmHandle* h, AdjointState* a, int slots, cudaStream_
         for (float*& p : a->pscr) TRY(dalloc(h, &p, np));
         for (float*& p : a->nscr) TRY(dalloc(h, &p, nn));
         TRY(dalloc(h, &a->lam_tmp, np * NLAM));
-        TRY(dalloc(h, &a->lam_pid, np));
         TRY(dalloc(h, &a->d_lam, NLAM));
         TRY(dalloc(h, &a->cnt, (size_t)h->ncell));
         TRY(dalloc(h, &a->mismatch, 1));
@@ -160,83 +178,134 @@ int ensure_adjoint_buffers(MpmHandle* h, AdjointState* a, int slots, cudaStream_
     return MPM_OK;
 }
 
-// Copy the current sort epoch's order-dependent arrays into epoch slot e.
-int capture_epoch(MpmHandle* h, AdjointState* a, size_t e, cudaStream_t s) {
+void add_seg(std::vector<CopySeg>& v, const void* src, void* dst, size_t bytes, size_t step) {
+    CopySeg c;
+    c.src = src;
+    c.dst = dst;
+    c.bytes = bytes;
+    c.dst_step = step;
+    v.push_back(c);
+}
+
+// Segments copying the current sort epoch's order-dependent arrays into epoch slot e.
+int epoch_segments(MpmHandle* h, AdjointState* a, size_t e, std::vector<CopySeg>& v) {
     const size_t np = (size_t)h->np;
     if (a->epochs.size() <= e) {
         Epoch ep;
         TRY(dalloc(h, &ep.pid, np));
         TRY(dalloc(h, &ep.mat, np));
-        if (h->has_E) TRY(dalloc(h, &ep.E, np));
         TRY(dalloc(h, &ep.cstart, (size_t)h->ncell + 2));
         a->epochs.push_back(ep);
     }
     Epoch& ep = a->epochs[e];
     if (h->has_E && !ep.E) TRY(dalloc(h, &ep.E, np));
     const PSet& p = h->ps[h->pcur];
-    CK(h, cudaMemcpyAsync(ep.pid, p.pid, sizeof(int) * np, cudaMemcpyDeviceToDevice, s));
-    CK(h, cudaMemcpyAsync(ep.mat, p.mat, np, cudaMemcpyDeviceToDevice, s));
-    if (h->has_E) CK(h, cudaMemcpyAsync(ep.E, p.E, sizeof(float) * np, cudaMemcpyDeviceToDevice, s));
-    CK(h, cudaMemcpyAsync(ep.cstart, h->cstart[h->cs_cur], sizeof(int) * (h->ncell + 2),
-                          cudaMemcpyDeviceToDevice, s));
+    add_seg(v, p.pid, ep.pid, sizeof(int) * np, 0);
+    add_seg(v, p.mat, ep.mat, np, 0);
+    if (h->has_E) add_seg(v, p.E, ep.E, sizeof(float) * np, 0);
+    add_seg(v, h->cstart[h->cs_cur], ep.cstart, sizeof(int) * ((size_t)h->ncell + 2), 0);
     return MPM_OK;
 }
 
-// Re-run segment `seg` from its checkpoint, filling tape slots 0..len-1.
+int capture_epoch(MpmHandle* h, AdjointState* a, cudaStream_t s) {
+    std::vector<CopySeg> v;
+    TRY(epoch_segments(h, a, (size_t)a->nep, v));
+    a->nep++;
+    return run_segments(h, h->segbuf, v, s);
+}
+
+// Tape copies of a step that starts with ping-pong parity `par`: the particle
+// state and drift flags (before the step) into slot 0 + t * stride.
+void tape_particle_segments(MpmHandle* h, AdjointState* a, int par, std::vector<CopySeg>& v) {
+    const PSet& p = h->ps[h->pcur];
+    const size_t np = (size_t)h->np;
+    const float* src[NTP] = {p.x, p.y, p.vx, p.vy, p.sxx[par], p.syy[par], p.szz[par],
+                             p.sxy[par], p.rho[par]};
+    for (int k = 0; k < NTP; ++k) add_seg(v, src[k], a->tp[k], sizeof(float) * np, sizeof(float) * np);
+    add_seg(v, h->cflag, a->tflag, (size_t)h->ncell, (size_t)h->ncell);
+}
+
+// ... and the nodal results (after the step).
+void tape_node_segments(MpmHandle* h, AdjointState* a, std::vector<CopySeg>& v) {
+    const size_t nn = (size_t)h->nn;
+    const float* src[NTN] = {h->nm, h->nvax, h->nvay, h->nvbx, h->nvby, h->nax, h->nay};
+    for (int k = 0; k < NTN; ++k) add_seg(v, src[k], a->tn[k], sizeof(float) * nn, sizeof(float) * nn);
+}
+
+// Pairs (re-run state, recorded state of the next checkpoint) for the bitwise check.
+void check_segments(MpmHandle* h, AdjointState* a, int seg, std::vector<CopySeg>& v) {
+    const Checkpoint& next = a->ck[seg + 1];
+    std::vector<float**> f = movable_f32(h, h->ps[h->pcur], false);
+    for (size_t i = 0; i < f.size(); ++i) add_seg(v, *f[i], next.f[i], sizeof(float) * h->np, 0);
+}
+
+bool resorts_at(const AdjointState* a, int64_t step) {
+    return std::binary_search(a->resort_steps.begin(), a->resort_steps.end(), step);
+}
+
+// Re-run segment `seg` of one simulation from its checkpoint, filling tape
+// slots 0..len-1, and check that it ends in the next checkpoint's state.
 int recompute_segment(MpmHandle* h, AdjointState* a, int seg, int len, cudaStream_t s) {
     TRY(restore_checkpoint(h, a->ck[seg], s));
-    TRY(clear_status(h, s));
     const int64_t first = a->ck[seg].step;
-    const size_t np = (size_t)h->np, nn = (size_t)h->nn;
     a->epoch_of.assign(len, 0);
-    int nep = 0;
-    TRY(capture_epoch(h, a, nep++, s));
-    for (int t = 0; t < len; ++t) {
-        if (std::binary_search(a->resort_steps.begin(), a->resort_steps.end(), first + t)) {
-            TRY(resort(h, s));
-            TRY(capture_epoch(h, a, nep++, s));
+    a->nep = 0;
+    TRY(capture_epoch(h, a, s));
+    SegBuf& tp = h->segbuf;
+    int tp_par = -1;
+    SegBuf tn;
+    std::vector<CopySeg> vn;
+    tape_node_segments(h, a, vn);
+    TRY(upload_segments(h, tn, vn, s));
+    int r = MPM_OK;
+    for (int t = 0; t < len && r == MPM_OK; ++t) {
+        if (resorts_at(a, first + t)) {
+            r = resort(h, s);
+            if (r == MPM_OK) r = capture_epoch(h, a, s);
+            tp_par = -1;
+            if (r != MPM_OK) break;
         }
-        const PSet& p = h->ps[h->pcur];
         const int par = parity(h);
-        CopyJob jp{};
-        const float* src[NTP] = {p.x, p.y, p.vx, p.vy, p.sxx[par], p.syy[par], p.szz[par],
-                                 p.sxy[par], p.rho[par]};
-        for (int k = 0; k < NTP; ++k) {
-            jp.src[k] = src[k];
-            jp.dst[k] = a->tp[k] + np * t;
+        if (par != tp_par) {
+            std::vector<CopySeg> v;
+            tape_particle_segments(h, a, par, v);
+            r = upload_segments(h, tp, v, s);
+            if (r != MPM_OK) break;
+            tp_par = par;
         }
-        jp.count = NTP;
-        jp.n = (int)np;
-        CK(h, launch_copy_f32(jp, s));
-        CK(h, cudaMemcpyAsync(a->tflag + (size_t)h->ncell * t, h->cflag, h->ncell,
-                              cudaMemcpyDeviceToDevice, s));
-        TRY(launch_steps(h, 1, s));
-        h->step++;
-        CopyJob jn{};
-        const float* nsrc[NTN] = {h->nm, h->nvax, h->nvay, h->nvbx, h->nvby, h->nax, h->nay};
-        for (int k = 0; k < NTN; ++k) {
-            jn.src[k] = nsrc[k];
-            jn.dst[k] = a->tn[k] + nn * t;
+        cudaError_t e = launch_copy_segments(tp.segs, tp.first, tp.nseg, tp.nblocks, t, s);
+        if (e == cudaSuccess) {
+            r = launch_steps(h, 1, s);
+            h->step++;
         }
-        jn.count = NTN;
-        jn.n = (int)nn;
-        CK(h, launch_copy_f32(jn, s));
-        a->epoch_of[t] = nep - 1;
+        if (e == cudaSuccess && r == MPM_OK)
+            e = launch_copy_segments(tn.segs, tn.first, tn.nseg, tn.nblocks, t, s);
+        if (e != cudaSuccess) r = fail(h, MPM_ERR_CUDA, "tape copy: %s", cudaGetErrorString(e));
+        a->epoch_of[t] = a->nep - 1;
     }
-    TRY(read_ctl(h, s));
+    if (r == MPM_OK) r = read_ctl(h, s);
+    segbuf_free(tn);
+    TRY(r);
     int st = 0;
     TRY(check_status(h, st));
     // the re-run must end bit for bit in the recorded state of the next checkpoint
-    const Checkpoint& next = a->ck[seg + 1];
-    std::vector<float**> f = movable_f32(h, h->ps[h->pcur], false);
-    CK(h, cudaMemsetAsync(a->mismatch, 0, sizeof(int), s));
-    for (size_t i = 0; i < f.size(); ++i)
-        CK(h, launch_count_mismatch(*f[i], next.f[i], (int)np, a->mismatch, s));
-    CK(h, cudaMemcpyAsync(a->h_mismatch, a->mismatch, sizeof(int), cudaMemcpyDeviceToHost, s));
-    TRY(sync(h, s));
-    if ((st & ST_DRIFT_VIOLATION) || *a->h_mismatch != 0 || h->step != next.step)
+    std::vector<CopySeg> vc;
+    check_segments(h, a, seg, vc);
+    SegBuf cb;
+    r = upload_segments(h, cb, vc, s);
+    if (r == MPM_OK) {
+        cudaError_t e = cudaMemsetAsync(a->mismatch, 0, sizeof(int), s);
+        if (e == cudaSuccess) e = launch_compare_segments(cb.segs, cb.first, cb.nseg, cb.nblocks, a->mismatch, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(a->h_mismatch, a->mismatch, sizeof(int), cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) r = fail(h, MPM_ERR_CUDA, "re-run check: %s", cudaGetErrorString(e));
+        if (r == MPM_OK) r = sync(h, s);
+    }
+    segbuf_free(cb);
+    TRY(r);
+    if ((st & ST_DRIFT_VIOLATION) || *a->h_mismatch != 0 || h->step != a->ck[seg + 1].step)
         return fail(h, MPM_ERR_STATE,
-                    "re-run of steps %lld..%lld did not reproduce the recorded run (%d values differ)",
+                    "re-run of steps %lld..%lld did not reproduce the recorded run (%d words differ)",
                     (long long)first, (long long)(first + len - 1), *a->h_mismatch);
     return clear_status(h, s);
 }
@@ -250,13 +319,13 @@ int permute(MpmHandle* h, AdjointState* a, const int* from, const int* to, cudaS
     return MPM_OK;
 }
 
-AdjStep step_args(MpmHandle* h, AdjointState* a, int t) {
-    const size_t np = (size_t)h->np, nn = (size_t)h->nn;
-    const Epoch& ep = a->epochs[a->epoch_of[t]];
+// Reverse-pass arguments with the tape at slot 0 and the epoch of slot t.
+AdjStep base_args(MpmHandle* h, AdjointState* a, int epoch) {
+    const Epoch& ep = a->epochs[epoch];
     AdjStep A{};
     A.nx = h->nx;
     A.ny = h->ny;
-    A.np = (int)np;
+    A.np = (int)h->np;
     A.hx = h->hx;
     A.hy = h->hy;
     A.dt = h->dt;
@@ -270,10 +339,10 @@ AdjStep step_args(MpmHandle* h, AdjointState* a, int t) {
     A.mat = ep.mat;
     A.E = h->has_E ? ep.E : nullptr;
     const float** tp[NTP] = {&A.x, &A.y, &A.vx, &A.vy, &A.sxx, &A.syy, &A.szz, &A.sxy, &A.rho};
-    for (int k = 0; k < NTP; ++k) *tp[k] = a->tp[k] + np * t;
-    A.cflag = a->tflag + (size_t)h->ncell * t;
+    for (int k = 0; k < NTP; ++k) *tp[k] = a->tp[k];
+    A.cflag = a->tflag;
     const float** tn[NTN] = {&A.nm, &A.nvax, &A.nvay, &A.nvbx, &A.nvby, &A.nax, &A.nay};
-    for (int k = 0; k < NTN; ++k) *tn[k] = a->tn[k] + nn * t;
+    for (int k = 0; k < NTN; ++k) *tn[k] = a->tn[k];
     float** lam[NLAM] = {&A.lx, &A.ly, &A.lvx, &A.lvy, &A.lsxx, &A.lsyy, &A.lszz, &A.lsxy,
                          &A.lrho, &A.lE};
     for (int k = 0; k < NLAM; ++k) *lam[k] = a->lam[k];
@@ -282,11 +351,19 @@ AdjStep step_args(MpmHandle* h, AdjointState* a, int t) {
     float** ns[NNS] = {&A.fbx, &A.fby, &A.mb, &A.vabx, &A.vaby, &A.qbx, &A.qby, &A.mbt};
     for (int k = 0; k < NNS; ++k) *ns[k] = a->nscr[k];
     A.cnt = a->cnt;
+    A.sp = h->np;
+    A.sn = h->nn;
+    A.sc = h->ncell;
     return A;
 }
 
 int reverse_step(MpmHandle* h, AdjointState* a, int t, cudaStream_t s) {
-    const AdjStep A = step_args(h, a, t);
+    AdjStep A = base_args(h, a, a->epoch_of[t]);
+    const size_t op = (size_t)t * A.sp, on = (size_t)t * A.sn, oc = (size_t)t * A.sc;
+    A.x += op; A.y += op; A.vx += op; A.vy += op;
+    A.sxx += op; A.syy += op; A.szz += op; A.sxy += op; A.rho += op;
+    A.cflag += oc;
+    A.nm += on; A.nvax += on; A.nvay += on; A.nvbx += on; A.nvby += on; A.nax += on; A.nay += on;
     CK(h, launch_rev_nodal_update(A, s));
     CK(h, launch_rev_forces(A, s));
     CK(h, launch_rev_nodal_kinematics(A, s));
@@ -294,28 +371,44 @@ int reverse_step(MpmHandle* h, AdjointState* a, int t, cudaStream_t s) {
     return MPM_OK;
 }
 
-// Particle (n, ncomp) array in original order -> adjoint arrays lam[first..].
-int seed(MpmHandle* h, AdjointState* a, const float* src, int first, int ncomp, int on_device,
-         cudaStream_t s) {
-    const void* d = nullptr;
-    TRY(to_device(h, src, sizeof(float) * ncomp * h->np, on_device, s, &d));
-    CK(h, launch_gather_in(a->d_lam + first, ncomp, a->lam_pid, (int)h->np,
-                           static_cast<const float*>(d), s));
-    return sync(h, s);
+// Zero the adjoint arrays; particle (n, 2) seeds in original order -> lam[0..3]
+// in the storage order `pid`.
+int seed(MpmHandle* h, AdjointState* a, const float* dl_dloc, const float* dl_dvel,
+         const int* pid, int on_device, cudaStream_t s) {
+    for (float* p : a->lam) CK(h, cudaMemsetAsync(p, 0, sizeof(float) * h->np, s));
+    const float* src[2] = {dl_dloc, dl_dvel};
+    for (int k = 0; k < 2; ++k) {
+        if (!src[k]) continue;
+        const void* d = nullptr;
+        TRY(to_device(h, src[k], sizeof(float) * 2 * h->np, on_device, s, &d));
+        CK(h, launch_gather_in(a->d_lam + 2 * k, 2, pid, (int)h->np, static_cast<const float*>(d), s));
+        TRY(sync(h, s));
+    }
+    return MPM_OK;
 }
 
-// Adjoint arrays lam[first..] -> particle (n, ncomp) array in original order.
-int emit(MpmHandle* h, AdjointState* a, float* dst, int first, int ncomp, int on_device,
-         cudaStream_t s) {
+// Adjoint arrays lam[first..] in storage order `pid` -> particle (n, ncomp)
+// array in original order.
+int emit(MpmHandle* h, AdjointState* a, float* dst, int first, int ncomp, const int* pid,
+         int on_device, cudaStream_t s) {
+    if (!dst) return MPM_OK;
     const size_t bytes = sizeof(float) * ncomp * h->np;
     float* d = dst;
     if (!on_device) {
         TRY(ensure_stage(h, bytes));
         d = static_cast<float*>(h->stage);
     }
-    CK(h, launch_scatter_out(a->d_lam + first, ncomp, a->lam_pid, (int)h->np, d, s));
+    CK(h, launch_scatter_out(a->d_lam + first, ncomp, pid, (int)h->np, d, s));
     if (!on_device) CK(h, cudaMemcpyAsync(dst, d, bytes, cudaMemcpyDeviceToHost, s));
     return sync(h, s);
+}
+
+int emit_all(MpmHandle* h, AdjointState* a, float* dl_dE, float* dl_dloc0, float* dl_dvel0,
+             int on_device, cudaStream_t s) {
+    const int* pid = a->epochs[0].pid;   // the order of the first checkpoint
+    TRY(emit(h, a, dl_dE, 9, 1, pid, on_device, s));
+    TRY(emit(h, a, dl_dloc0, 0, 2, pid, on_device, s));
+    return emit(h, a, dl_dvel0, 2, 2, pid, on_device, s);
 }
 
 int check_supported(MpmHandle* h) {
@@ -327,6 +420,43 @@ int check_supported(MpmHandle* h) {
     for (const MatDev& m : h->mats)
         if (m.type == MAT_NEWTONIAN)
             return fail(h, MPM_ERR_UNSUPPORTED, "the adjoint covers LinearElastic and SimpleMaterial");
+    return MPM_OK;
+}
+
+// Start a recording on h: checks, state and bookkeeping.
+int record_begin(MpmHandle* h, int nsteps, int K) {
+    if (!h->initialized) return fail(h, MPM_ERR_STATE, "initialize first");
+    if (nsteps < 1 || K < 1) return fail(h, MPM_ERR_INVALID, "nsteps and checkpoint_steps must be >= 1");
+    if (h->np <= 0) return fail(h, MPM_ERR_STATE, "no particles");
+    TRY(check_supported(h));
+    if (!h->adj) h->adj = new AdjointState();
+    AdjointState* a = h->adj;
+    fit(h, a);
+    a->valid = false;
+    a->resort_steps.clear();
+    a->step0 = h->step;
+    a->K = K;
+    a->nsteps = nsteps;
+    a->nseg = (nsteps + K - 1) / K;
+    a->recording = true;
+    return MPM_OK;
+}
+
+void record_end(MpmHandle* h, bool ok) {
+    AdjointState* a = h->adj;
+    a->recording = false;
+    if (!ok) return;
+    std::sort(a->resort_steps.begin(), a->resort_steps.end());
+    a->resort_steps.erase(std::unique(a->resort_steps.begin(), a->resort_steps.end()),
+                          a->resort_steps.end());
+    a->gen = h->gen;
+    a->valid = true;
+}
+
+int check_recorded(MpmHandle* h) {
+    AdjointState* a = h->adj;
+    if (!a || !a->valid || a->np_alloc != h->np) return fail(h, MPM_ERR_STATE, "call mpm_record first");
+    if (a->gen != h->gen) return fail(h, MPM_ERR_STATE, "the simulation changed since mpm_record");
     return MPM_OK;
 }
 
@@ -343,88 +473,307 @@ void adjoint_free(MpmHandle* h) {
     h->adj = nullptr;
 }
 
+void batch_adjoint_free(MpmBatch* b) {
+    BatchAdjoint* x = b->badj;
+    if (!x) return;
+    cudaFree(x->d_bases);
+    cudaFree(x->d_table);
+    cudaFree(x->node_blocks);
+    cudaFree(x->part_blocks);
+    cudaFree(x->mismatch);
+    if (x->h_mismatch) cudaFreeHost(x->h_mismatch);
+    segbuf_free(x->tape_p[0]);
+    segbuf_free(x->tape_p[1]);
+    segbuf_free(x->tape_n);
+    segbuf_free(x->misc);
+    delete x;
+    b->badj = nullptr;
+}
+
 }  // namespace mpm
+
+using namespace mpm::batch;
+
+namespace {
+
+// Batched re-run of segment `seg` of every simulation (tape slots 0..len-1),
+// with the bitwise check against the next checkpoints.
+int batch_recompute(MpmBatch* b, BatchAdjoint* x, int seg, int len, cudaStream_t s) {
+    const int n = (int)b->sims.size();
+    std::vector<CopySeg> v;
+    for (int i = 0; i < n; ++i) checkpoint_segments(b->sims[i], b->sims[i]->adj->ck[seg], false, v);
+    BTRY(b, 0, run_segments(b->sims[0], x->misc, v, s));
+    int r = read_statuses(b, s);   // (clears the restored status words)
+    if (r != MPM_OK) return r;
+    v.clear();
+    for (int i = 0; i < n; ++i) {
+        AdjointState* a = b->sims[i]->adj;
+        a->epoch_of.assign(len, 0);
+        a->nep = 0;
+        BTRY(b, i, epoch_segments(b->sims[i], a, 0, v));
+        a->nep = 1;
+    }
+    BTRY(b, 0, run_segments(b->sims[0], x->misc, v, s));
+    // tape tables: particle copies for even and odd t (each simulation's own
+    // parity), nodal copies
+    auto build_particle_tables = [&]() -> int {
+        for (int q = 0; q < 2; ++q) {
+            std::vector<CopySeg> w;
+            for (MpmHandle* h : b->sims)
+                tape_particle_segments(h, h->adj, (int)((h->step + q) & 1), w);
+            BTRY(b, 0, upload_segments(b->sims[0], x->tape_p[q], w, s));
+        }
+        return MPM_OK;
+    };
+    // (the parity of slot t is that of the segment's first step plus t)
+    std::vector<int64_t> first(n);
+    for (int i = 0; i < n; ++i) first[i] = b->sims[i]->step;
+    r = build_particle_tables();
+    if (r != MPM_OK) return r;
+    v.clear();
+    for (MpmHandle* h : b->sims) tape_node_segments(h, h->adj, v);
+    BTRY(b, 0, upload_segments(b->sims[0], x->tape_n, v, s));
+    for (int t = 0; t < len; ++t) {
+        bool resorted = false;
+        for (int i = 0; i < n; ++i) {
+            MpmHandle* h = b->sims[i];
+            if (!resorts_at(h->adj, first[i] + t)) continue;
+            BTRY(b, i, resort(h, s));
+            BTRY(b, i, capture_epoch(h, h->adj, s));
+            resorted = true;
+        }
+        if (resorted) {
+            // tables are built for the parity at t = 0: shift the simulations' steps back
+            for (int i = 0; i < n; ++i) b->sims[i]->step -= t;
+            r = build_particle_tables();
+            for (int i = 0; i < n; ++i) b->sims[i]->step += t;
+            if (r != MPM_OK) return r;
+        }
+        const SegBuf& tp = x->tape_p[t & 1];
+        BCK(b, launch_copy_segments(tp.segs, tp.first, tp.nseg, tp.nblocks, t, s));
+        r = launch_batch_steps(b, 1, s);
+        if (r != MPM_OK) return r;
+        for (MpmHandle* h : b->sims) h->step++;
+        BCK(b, launch_copy_segments(x->tape_n.segs, x->tape_n.first, x->tape_n.nseg,
+                                    x->tape_n.nblocks, t, s));
+        for (MpmHandle* h : b->sims) h->adj->epoch_of[t] = h->adj->nep - 1;
+    }
+    r = read_statuses(b, s);
+    if (r != MPM_OK) return r;
+    v.clear();
+    for (int i = 0; i < n; ++i) {
+        const int st = b->h_status[i].status;
+        if (st & (ST_DRIFT_VIOLATION | ST_OUT_OF_MESH))
+            return bfail(b, MPM_ERR_STATE, "simulation %d: re-run of segment %d left the recorded run",
+                         i, seg);
+        if (b->sims[i]->step != b->sims[i]->adj->ck[seg + 1].step)
+            return bfail(b, MPM_ERR_STATE, "simulation %d: step count of the re-run differs", i);
+        check_segments(b->sims[i], b->sims[i]->adj, seg, v);
+    }
+    BTRY(b, 0, upload_segments(b->sims[0], x->misc, v, s));
+    BCK(b, cudaMemsetAsync(x->mismatch, 0, sizeof(int), s));
+    BCK(b, launch_compare_segments(x->misc.segs, x->misc.first, x->misc.nseg, x->misc.nblocks,
+                                   x->mismatch, s));
+    BCK(b, cudaMemcpyAsync(x->h_mismatch, x->mismatch, sizeof(int), cudaMemcpyDeviceToHost, s));
+    BCK(b, cudaStreamSynchronize(s));
+    if (*x->h_mismatch != 0)
+        return bfail(b, MPM_ERR_STATE, "re-run of segment %d did not reproduce the recorded run "
+                     "(%d words differ)", seg, *x->h_mismatch);
+    return MPM_OK;
+}
+
+int ensure_batch_adjoint(MpmBatch* b, cudaStream_t s) {
+    if (!b->badj) b->badj = new BatchAdjoint();
+    BatchAdjoint* x = b->badj;
+    const int n = (int)b->sims.size();
+    if (!x->d_bases) {
+        BCK(b, cudaMalloc(&x->d_bases, sizeof(AdjStep) * n));
+        BCK(b, cudaMalloc(&x->d_table, sizeof(AdjStep) * n));
+        BCK(b, cudaMalloc(&x->mismatch, sizeof(int)));
+        BCK(b, cudaMallocHost(&x->h_mismatch, sizeof(int)));
+    }
+    // block maps (particle counts may have changed since the last call)
+    std::vector<int2> nb, pb;
+    for (int i = 0; i < n; ++i) {
+        const MpmHandle* h = b->sims[i];
+        for (int c = 0; c * ADJ_BLOCK < h->nn; ++c) nb.push_back(make_int2(i, c));
+        for (int c = 0; c * ADJ_BLOCK < h->np; ++c) pb.push_back(make_int2(i, c));
+    }
+    cudaFree(x->node_blocks);
+    cudaFree(x->part_blocks);
+    x->node_blocks = x->part_blocks = nullptr;
+    BCK(b, cudaMalloc(&x->node_blocks, sizeof(int2) * nb.size()));
+    BCK(b, cudaMalloc(&x->part_blocks, sizeof(int2) * pb.size()));
+    BCK(b, cudaMemcpyAsync(x->node_blocks, nb.data(), sizeof(int2) * nb.size(), cudaMemcpyHostToDevice, s));
+    BCK(b, cudaMemcpyAsync(x->part_blocks, pb.data(), sizeof(int2) * pb.size(), cudaMemcpyHostToDevice, s));
+    BCK(b, cudaStreamSynchronize(s));
+    x->n_node_blocks = (int)nb.size();
+    x->n_part_blocks = (int)pb.size();
+    return MPM_OK;
+}
+
+}  // namespace
 
 extern "C" {
 
 int mpm_record(MpmHandle* h, int nsteps, int checkpoint_steps, void* stream) {
     if (!h) return MPM_ERR_INVALID;
-    if (!h->initialized) return fail(h, MPM_ERR_STATE, "initialize first");
-    if (nsteps < 1 || checkpoint_steps < 1)
-        return fail(h, MPM_ERR_INVALID, "nsteps and checkpoint_steps must be >= 1");
-    if (h->np <= 0) return fail(h, MPM_ERR_STATE, "no particles");
-    TRY(check_supported(h));
+    TRY(record_begin(h, nsteps, checkpoint_steps));
     cudaStream_t s = S(stream);
-    if (!h->adj) h->adj = new AdjointState();
     AdjointState* a = h->adj;
-    fit(h, a);
-    a->valid = false;
-    const int nseg = (nsteps + checkpoint_steps - 1) / checkpoint_steps;
-    a->resort_steps.clear();
-    a->step0 = h->step;
-    a->K = checkpoint_steps;
-    a->nsteps = nsteps;
-    a->nseg = nseg;
-    a->recording = true;
     int r = MPM_OK;
-    for (int seg = 0; seg < nseg && r == MPM_OK; ++seg) {
-        r = save_checkpoint(h, a, seg, s);
+    for (int seg = 0; seg < a->nseg && r == MPM_OK; ++seg) {
+        std::vector<CopySeg> v;
+        r = save_checkpoint(h, a, seg, v);
+        if (r == MPM_OK) r = run_segments(h, h->segbuf, v, s);
         const int len = std::min(checkpoint_steps, nsteps - seg * checkpoint_steps);
         if (r == MPM_OK) r = mpm_step(h, len, stream);
     }
-    a->recording = false;
-    TRY(r);
-    TRY(save_checkpoint(h, a, nseg, s));
-    std::sort(a->resort_steps.begin(), a->resort_steps.end());
-    a->resort_steps.erase(std::unique(a->resort_steps.begin(), a->resort_steps.end()),
-                          a->resort_steps.end());
-    TRY(sync(h, s));
-    a->gen = h->gen;
-    a->valid = true;
-    return MPM_OK;
+    if (r == MPM_OK) {
+        std::vector<CopySeg> v;
+        r = save_checkpoint(h, a, a->nseg, v);
+        if (r == MPM_OK) r = run_segments(h, h->segbuf, v, s);
+        if (r == MPM_OK) r = sync(h, s);
+    }
+    record_end(h, r == MPM_OK);
+    return r;
 }
 
 int mpm_adjoint(MpmHandle* h, const float* dl_dloc, const float* dl_dvel, float* dl_dE,
                 float* dl_dloc0, float* dl_dvel0, int on_device, void* stream) {
     if (!h) return MPM_ERR_INVALID;
-    AdjointState* a = h->adj;
-    if (!a || !a->valid || a->np_alloc != h->np)
-        return fail(h, MPM_ERR_STATE, "call mpm_record first");
-    if (a->gen != h->gen)
-        return fail(h, MPM_ERR_STATE, "the simulation changed since mpm_record");
+    TRY(check_recorded(h));
     if (!dl_dloc) return fail(h, MPM_ERR_INVALID, "dl_dloc is null");
+    AdjointState* a = h->adj;
     cudaStream_t s = S(stream);
     const int K = a->K;
     TRY(ensure_adjoint_buffers(h, a, K, s));
-    for (float* p : a->lam) CK(h, cudaMemsetAsync(p, 0, sizeof(float) * h->np, s));
-    CK(h, cudaMemcpyAsync(a->lam_pid, h->ps[h->pcur].pid, sizeof(int) * h->np,
-                          cudaMemcpyDeviceToDevice, s));
-    TRY(seed(h, a, dl_dloc, 0, 2, on_device, s));
-    if (dl_dvel) TRY(seed(h, a, dl_dvel, 2, 2, on_device, s));
-
+    // the seeds are in the order of the recorded end state (the current one)
+    TRY(seed(h, a, dl_dloc, dl_dvel, h->ps[h->pcur].pid, on_device, s));
     int r = MPM_OK;
     for (int seg = a->nseg - 1; seg >= 0 && r == MPM_OK; --seg) {
         const int len = (int)std::min<int64_t>(K, a->nsteps - (int64_t)seg * K);
         r = recompute_segment(h, a, seg, len, s);
-        if (r != MPM_OK) break;
-        r = permute(h, a, a->lam_pid, a->epochs[a->epoch_of[len - 1]].pid, s);
         for (int t = len - 1; t >= 0 && r == MPM_OK; --t) {
             if (t < len - 1 && a->epoch_of[t] != a->epoch_of[t + 1])
                 r = permute(h, a, a->epochs[a->epoch_of[t + 1]].pid, a->epochs[a->epoch_of[t]].pid, s);
             if (r == MPM_OK) r = reverse_step(h, a, t, s);
         }
-        if (r == MPM_OK) {
-            cudaError_t e = cudaMemcpyAsync(a->lam_pid, a->epochs[a->epoch_of[0]].pid,
-                                            sizeof(int) * h->np, cudaMemcpyDeviceToDevice, s);
-            if (e != cudaSuccess) r = fail(h, MPM_ERR_CUDA, "%s", cudaGetErrorString(e));
-        }
+        if (r == MPM_OK && a->epoch_of[0] != 0)
+            r = permute(h, a, a->epochs[a->epoch_of[0]].pid, a->epochs[0].pid, s);
     }
-    if (r == MPM_OK && dl_dE) r = emit(h, a, dl_dE, 9, 1, on_device, s);
-    if (r == MPM_OK && dl_dloc0) r = emit(h, a, dl_dloc0, 0, 2, on_device, s);
-    if (r == MPM_OK && dl_dvel0) r = emit(h, a, dl_dvel0, 2, 2, on_device, s);
+    if (r == MPM_OK) r = emit_all(h, a, dl_dE, dl_dloc0, dl_dvel0, on_device, s);
     // leave the handle at the recorded end state
     const int r2 = restore_checkpoint(h, a->ck[a->nseg], s);
     TRY(r);
+    return r2;
+}
+
+int mpm_batch_record(MpmBatch* b, int nsteps, int checkpoint_steps, void* stream) {
+    if (!b) return MPM_ERR_INVALID;
+    int r = check_ready(b);
+    if (r != MPM_OK) return r;
+    const int n = (int)b->sims.size();
+    for (int i = 0; i < n; ++i) BTRY(b, i, record_begin(b->sims[i], nsteps, checkpoint_steps));
+    cudaStream_t s = S(stream);
+    const int nseg = b->sims[0]->adj->nseg;
+    for (int seg = 0; seg <= nseg && r == MPM_OK; ++seg) {
+        std::vector<CopySeg> v;
+        for (int i = 0; i < n && r == MPM_OK; ++i) {
+            r = save_checkpoint(b->sims[i], b->sims[i]->adj, seg, v);
+            if (r != MPM_OK) r = from_sim(b, i, r);
+        }
+        if (r == MPM_OK && run_segments(b->sims[0], b->segbuf, v, s) != MPM_OK) r = from_sim(b, 0, MPM_ERR_CUDA);
+        if (r == MPM_OK && seg < nseg)
+            r = batch_steps(b, std::min(checkpoint_steps, nsteps - seg * checkpoint_steps), s);
+    }
+    if (r == MPM_OK && cudaStreamSynchronize(s) != cudaSuccess) r = bfail(b, MPM_ERR_CUDA, "synchronise");
+    for (MpmHandle* h : b->sims) record_end(h, r == MPM_OK);
+    return r;
+}
+
+int mpm_batch_adjoint(MpmBatch* b, const float* const* dl_dloc, const float* const* dl_dvel,
+                      float* const* dl_dE, float* const* dl_dloc0, float* const* dl_dvel0,
+                      int on_device, void* stream) {
+    if (!b) return MPM_ERR_INVALID;
+    if (!dl_dloc) return bfail(b, MPM_ERR_INVALID, "dl_dloc is null");
+    const int n = (int)b->sims.size();
+    for (int i = 0; i < n; ++i) {
+        MpmHandle* h = b->sims[i];
+        BTRY(b, i, check_recorded(h));
+        if (h->adj->nsteps != b->sims[0]->adj->nsteps || h->adj->K != b->sims[0]->adj->K)
+            return bfail(b, MPM_ERR_STATE, "simulation %d was recorded apart from the batch", i);
+        if (!dl_dloc[i]) return bfail(b, MPM_ERR_INVALID, "dl_dloc[%d] is null", i);
+    }
+    cudaStream_t s = S(stream);
+    const int K = b->sims[0]->adj->K, nseg = b->sims[0]->adj->nseg;
+    const int64_t nsteps = b->sims[0]->adj->nsteps;
+    int r = ensure_batch_adjoint(b, s);
+    if (r != MPM_OK) return r;
+    BatchAdjoint* x = b->badj;
+    for (int i = 0; i < n; ++i) {
+        MpmHandle* h = b->sims[i];
+        BTRY(b, i, ensure_adjoint_buffers(h, h->adj, K, s));
+        BTRY(b, i, seed(h, h->adj, dl_dloc[i], dl_dvel ? dl_dvel[i] : nullptr, h->ps[h->pcur].pid,
+                        on_device, s));
+    }
+    x->bases.assign(n, AdjStep{});
+    std::vector<int> cur(n, -1);   // epoch whose pointers bases[i] holds
+    for (int seg = nseg - 1; seg >= 0 && r == MPM_OK; --seg) {
+        const int len = (int)std::min<int64_t>(K, nsteps - (int64_t)seg * K);
+        r = batch_recompute(b, x, seg, len, s);
+        if (r != MPM_OK) break;
+        for (int i = 0; i < n; ++i) {
+            AdjointState* a = b->sims[i]->adj;
+            x->bases[i] = base_args(b->sims[i], a, a->epoch_of[len - 1]);
+            cur[i] = a->epoch_of[len - 1];
+        }
+        BCK(b, cudaMemcpyAsync(x->d_bases, x->bases.data(), sizeof(AdjStep) * n, cudaMemcpyHostToDevice, s));
+        for (int t = len - 1; t >= 0 && r == MPM_OK; --t) {
+            for (int i = 0; i < n && r == MPM_OK; ++i) {
+                MpmHandle* h = b->sims[i];
+                AdjointState* a = h->adj;
+                if (a->epoch_of[t] == cur[i]) continue;
+                r = permute(h, a, a->epochs[cur[i]].pid, a->epochs[a->epoch_of[t]].pid, s);
+                if (r != MPM_OK) {
+                    r = from_sim(b, i, r);
+                    break;
+                }
+                cur[i] = a->epoch_of[t];
+                x->bases[i] = base_args(h, a, cur[i]);
+                if (cudaMemcpyAsync(x->d_bases + i, &x->bases[i], sizeof(AdjStep), cudaMemcpyHostToDevice,
+                                    s) != cudaSuccess)
+                    r = bfail(b, MPM_ERR_CUDA, "argument upload");
+            }
+            if (r != MPM_OK) break;
+            BCK(b, launch_adj_table(x->d_bases, n, t, x->d_table, s));
+            BCK(b, launch_rev_batch(x->d_table, x->node_blocks, x->n_node_blocks, x->part_blocks,
+                                    x->n_part_blocks, s));
+        }
+        for (int i = 0; i < n && r == MPM_OK; ++i) {
+            MpmHandle* h = b->sims[i];
+            AdjointState* a = h->adj;
+            if (a->epoch_of[0] != 0) {
+                const int e = permute(h, a, a->epochs[a->epoch_of[0]].pid, a->epochs[0].pid, s);
+                if (e != MPM_OK) r = from_sim(b, i, e);
+            }
+        }
+        // (the host copy of the arguments must outlive the uploads)
+        if (r == MPM_OK && cudaStreamSynchronize(s) != cudaSuccess) r = bfail(b, MPM_ERR_CUDA, "synchronise");
+    }
+    for (int i = 0; i < n && r == MPM_OK; ++i) {
+        MpmHandle* h = b->sims[i];
+        const int e = emit_all(h, h->adj, dl_dE ? dl_dE[i] : nullptr, dl_dloc0 ? dl_dloc0[i] : nullptr,
+                               dl_dvel0 ? dl_dvel0[i] : nullptr, on_device, s);
+        if (e != MPM_OK) r = from_sim(b, i, e);
+    }
+    // leave every simulation at the recorded end state
+    std::vector<CopySeg> v;
+    for (MpmHandle* h : b->sims) checkpoint_segments(h, h->adj->ck[nseg], false, v);
+    int r2 = run_segments(b->sims[0], x->misc, v, s);
+    if (r2 == MPM_OK) r2 = read_statuses(b, s);
+    else r2 = from_sim(b, 0, r2);
+    if (r != MPM_OK) return r;
     return r2;
 }
 

@@ -49,12 +49,23 @@ struct AdjStep {
     float *fbx, *fby, *mb, *vabx, *vaby;
     float *qbx, *qby, *mbt;
     int* cnt;              // particles per cell at the step start (pass 1 -> 2, 4)
+    // tape slot strides (particles, nodes, cells) for batched launches
+    long long sp, sn, sc;
 };
 
 cudaError_t launch_rev_nodal_update(const AdjStep& A, cudaStream_t s);
 cudaError_t launch_rev_forces(const AdjStep& A, cudaStream_t s);
 cudaError_t launch_rev_nodal_kinematics(const AdjStep& A, cudaStream_t s);
 cudaError_t launch_rev_mass_momentum(const AdjStep& A, cudaStream_t s);
+
+// Batches: table[i] = bases[i] with the tape pointers at slot t; then the four
+// passes over every simulation, CTA b working on simulation blocks[b].x,
+// elements blocks[b].y * 256 .. + 255 (nodes for passes 1 and 3, particles
+// for passes 2 and 4).
+constexpr int ADJ_BLOCK = 256;
+cudaError_t launch_adj_table(const AdjStep* bases, int n, int t, AdjStep* table, cudaStream_t s);
+cudaError_t launch_rev_batch(const AdjStep* table, const int2* node_blocks, int n_node_blocks,
+                             const int2* part_blocks, int n_part_blocks, cudaStream_t s);
 
 // *mismatch += number of i < n with a[i] != b[i] bitwise (4-byte words).
 cudaError_t launch_count_mismatch(const void* a, const void* b, int n, int* mismatch,

@@ -77,6 +77,16 @@ __device__ __forceinline__ void particle_cell(const AdjStep& A, float x, float y
     cj = min(max(locate_axis(y, A.hy, A.ny), 0), A.ny - 1);
 }
 
+// Batched launches: the CTA copies its simulation's arguments into shared
+// memory (one word per thread).
+__device__ __forceinline__ void load_step_args(const AdjStep* __restrict__ src, AdjStep& dst) {
+    static_assert(sizeof(AdjStep) % 4 == 0, "arguments copied in 4-byte words");
+    const int* a = reinterpret_cast<const int*>(src);
+    int* b = reinterpret_cast<int*>(&dst);
+    for (int i = threadIdx.x; i < (int)(sizeof(AdjStep) / 4); i += blockDim.x) b[i] = a[i];
+    __syncthreads();
+}
+
 // Adjoint seeds of G2P: (v-hat bar, a-hat bar) of particle q.
 __device__ __forceinline__ void g2p_seeds(const AdjStep& A, int q, float& gx, float& gy,
                                           float& hx, float& hy) {
@@ -98,10 +108,8 @@ __device__ __forceinline__ void g2p_seeds(const AdjStep& A, int q, float& gx, fl
 // Pass 1: transposed G2P and reverse nodal update (element.py:305-329,
 // particle.py:208-247).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(NODE_THREADS)
-k_rev_nodal_update(const __grid_constant__ AdjStep A) {
+__device__ __forceinline__ void rev_nodal_update_at(const AdjStep& A, int n) {
     const int nxn = A.nx + 1;
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= nxn * (A.ny + 1)) return;
     const int I = n % nxn, J = n / nxn;
     float vbx = 0.0f, vby = 0.0f, abx = 0.0f, aby = 0.0f;
@@ -149,13 +157,24 @@ k_rev_nodal_update(const __grid_constant__ AdjStep A) {
     A.vaby[n] = wby;
 }
 
+__global__ void __launch_bounds__(NODE_THREADS)
+k_rev_nodal_update(const __grid_constant__ AdjStep A) {
+    rev_nodal_update_at(A, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+__global__ void __launch_bounds__(NODE_THREADS)
+k_rev_nodal_update_batch(const AdjStep* __restrict__ table, const int2* __restrict__ blocks) {
+    __shared__ AdjStep sA;
+    const int2 bm = blocks[blockIdx.x];
+    load_step_args(table + bm.x, sA);
+    rev_nodal_update_at(sA, bm.y * NODE_THREADS + threadIdx.x);
+}
+
 // ---------------------------------------------------------------------------
 // Pass 2: reverse of the forces (element.py:236-268, 842-901) and of the USF
 // strain / volume / stress update (particle.py:249-327, material.py:113-131).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(PART_THREADS)
-k_rev_forces(const __grid_constant__ AdjStep A) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q) {
     if (q >= A.np) return;
     const float x = A.x[q], y = A.y[q];
     int ci, cj;
@@ -292,14 +311,25 @@ k_rev_forces(const __grid_constant__ AdjStep A) {
     A.c1b[q] = c1b;
 }
 
+__global__ void __launch_bounds__(PART_THREADS)
+k_rev_forces(const __grid_constant__ AdjStep A) {
+    rev_forces_at(A, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+__global__ void __launch_bounds__(PART_THREADS)
+k_rev_forces_batch(const AdjStep* __restrict__ table, const int2* __restrict__ blocks) {
+    __shared__ AdjStep sA;
+    const int2 bm = blocks[blockIdx.x];
+    load_step_args(table + bm.x, sA);
+    rev_forces_at(sA, bm.y * PART_THREADS + threadIdx.x);
+}
+
 // ---------------------------------------------------------------------------
 // Pass 3: transposed strain-rate gather and reverse nodal velocity
 // (element.py:191-202, 331-334; particle.py:281-313).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(NODE_THREADS)
-k_rev_nodal_kinematics(const __grid_constant__ AdjStep A) {
+__device__ __forceinline__ void rev_nodal_kinematics_at(const AdjStep& A, int n) {
     const int nxn = A.nx + 1;
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= nxn * (A.ny + 1)) return;
     const int I = n % nxn, J = n / nxn;
     float vbx = A.vabx[n], vby = A.vaby[n];
@@ -338,13 +368,24 @@ k_rev_nodal_kinematics(const __grid_constant__ AdjStep A) {
     A.mbt[n] = mbt;
 }
 
+__global__ void __launch_bounds__(NODE_THREADS)
+k_rev_nodal_kinematics(const __grid_constant__ AdjStep A) {
+    rev_nodal_kinematics_at(A, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+__global__ void __launch_bounds__(NODE_THREADS)
+k_rev_nodal_kinematics_batch(const AdjStep* __restrict__ table, const int2* __restrict__ blocks) {
+    __shared__ AdjStep sA;
+    const int2 bm = blocks[blockIdx.x];
+    load_step_args(table + bm.x, sA);
+    rev_nodal_kinematics_at(sA, bm.y * NODE_THREADS + threadIdx.x);
+}
+
 // ---------------------------------------------------------------------------
 // Pass 4: reverse of the mass and momentum P2G (element.py:122-189) and of
 // m = V0 rho (particle.py:158-178).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(PART_THREADS)
-k_rev_mass_momentum(const __grid_constant__ AdjStep A) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void rev_mass_momentum_at(const AdjStep& A, int q) {
     if (q >= A.np) return;
     const float x = A.x[q], y = A.y[q];
     int ci, cj;
@@ -381,6 +422,19 @@ k_rev_mass_momentum(const __grid_constant__ AdjStep A) {
     A.ly[q] = yb;
 }
 
+__global__ void __launch_bounds__(PART_THREADS)
+k_rev_mass_momentum(const __grid_constant__ AdjStep A) {
+    rev_mass_momentum_at(A, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+__global__ void __launch_bounds__(PART_THREADS)
+k_rev_mass_momentum_batch(const AdjStep* __restrict__ table, const int2* __restrict__ blocks) {
+    __shared__ AdjStep sA;
+    const int2 bm = blocks[blockIdx.x];
+    load_step_args(table + bm.x, sA);
+    rev_mass_momentum_at(sA, bm.y * PART_THREADS + threadIdx.x);
+}
+
 __global__ void k_copy_f32(const __grid_constant__ CopyJob j) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= j.n) return;
@@ -395,6 +449,20 @@ __global__ void k_count_mismatch(const uint32_t* __restrict__ a, const uint32_t*
     const bool diff = i < n && a[i] != b[i];
     const int c = __syncthreads_count(diff);
     if (threadIdx.x == 0 && c) atomicAdd(mismatch, c);
+}
+
+// table[i] = bases[i] with the tape pointers moved to slot t.
+__global__ void k_adj_table(const AdjStep* __restrict__ bases, int n, int t,
+                            AdjStep* __restrict__ table) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    AdjStep a = bases[i];
+    const size_t op = (size_t)t * a.sp, on = (size_t)t * a.sn, oc = (size_t)t * a.sc;
+    a.x += op; a.y += op; a.vx += op; a.vy += op;
+    a.sxx += op; a.syy += op; a.szz += op; a.sxy += op; a.rho += op;
+    a.cflag += oc;
+    a.nm += on; a.nvax += on; a.nvay += on; a.nvbx += on; a.nvby += on; a.nax += on; a.nay += on;
+    table[i] = a;
 }
 
 inline int blocks_for(int n, int t) { return (n + t - 1) / t; }
@@ -422,6 +490,24 @@ cudaError_t launch_rev_nodal_kinematics(const AdjStep& A, cudaStream_t s) {
 cudaError_t launch_rev_mass_momentum(const AdjStep& A, cudaStream_t s) {
     if (A.np <= 0) return cudaSuccess;
     k_rev_mass_momentum<<<blocks_for(A.np, PART_THREADS), PART_THREADS, 0, s>>>(A);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adj_table(const AdjStep* bases, int n, int t, AdjStep* table, cudaStream_t s) {
+    if (n > 0) k_adj_table<<<blocks_for(n, 128), 128, 0, s>>>(bases, n, t, table);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rev_batch(const AdjStep* table, const int2* node_blocks, int n_node_blocks,
+                             const int2* part_blocks, int n_part_blocks, cudaStream_t s) {
+    if (n_node_blocks > 0)
+        k_rev_nodal_update_batch<<<n_node_blocks, NODE_THREADS, 0, s>>>(table, node_blocks);
+    if (n_part_blocks > 0)
+        k_rev_forces_batch<<<n_part_blocks, PART_THREADS, 0, s>>>(table, part_blocks);
+    if (n_node_blocks > 0)
+        k_rev_nodal_kinematics_batch<<<n_node_blocks, NODE_THREADS, 0, s>>>(table, node_blocks);
+    if (n_part_blocks > 0)
+        k_rev_mass_momentum_batch<<<n_part_blocks, PART_THREADS, 0, s>>>(table, part_blocks);
     return cudaGetLastError();
 }
 

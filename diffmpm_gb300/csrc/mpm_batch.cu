@@ -21,32 +21,17 @@
 #include <string>
 #include <vector>
 
-#include "mpm_handle.h"
+#include "mpm_batch.h"
 
 using namespace mpm;
 using namespace mpm::host;
 
-struct MpmBatch {
-    int device = 0;
-    std::vector<MpmHandle*> sims;
-    StepConfig cfg{};
-    const SimDev** d_sims = nullptr;
-    Control** d_ctls = nullptr;
-    int4* d_tiles = nullptr;
-    int ntiles = 0;
-    Control* d_status = nullptr;
-    Control* h_status = nullptr;   // pinned
-    int block_steps = 100;
-    cudaStream_t cap = nullptr;
-    std::map<int, cudaGraphExec_t> graphs;
-    SegBuf segbuf;
-    std::vector<Checkpoint> tune;  // per-simulation state saved by the autotuner
-    std::string err;
-};
-
 namespace {
-
 thread_local std::string g_batch_create_error;
+}  // namespace
+
+namespace mpm {
+namespace batch {
 
 int bfail(MpmBatch* b, int code, const char* fmt, ...) {
     char buf[512];
@@ -63,19 +48,6 @@ int bfail(MpmBatch* b, int code, const char* fmt, ...) {
 int from_sim(MpmBatch* b, int i, int code) {
     return bfail(b, code, "simulation %d: %s", i, b->sims[i]->err.c_str());
 }
-
-#define BCK(b, call)                                                                       \
-    do {                                                                                   \
-        cudaError_t e_ = (call);                                                           \
-        if (e_ != cudaSuccess)                                                             \
-            return bfail(b, MPM_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_));        \
-    } while (0)
-
-#define BTRY(b, i, x)                                  \
-    do {                                               \
-        int r_ = (x);                                  \
-        if (r_ != MPM_OK) return from_sim(b, i, r_);   \
-    } while (0)
 
 void drop_batch_graphs(MpmBatch* b) {
     for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
@@ -186,7 +158,10 @@ int tune_state(MpmBatch* b, bool save, cudaStream_t s) {
     return MPM_OK;
 }
 
-}  // namespace
+}  // namespace batch
+}  // namespace mpm
+
+using namespace mpm::batch;
 
 extern "C" {
 
@@ -246,6 +221,7 @@ int mpm_batch_create(MpmHandle* const* sims, int n, MpmBatch** out) {
 
 int mpm_batch_destroy(MpmBatch* b) {
     if (!b) return MPM_OK;
+    mpm::batch_adjoint_free(b);
     drop_batch_graphs(b);
     for (size_t i = 0; i < b->tune.size() && i < b->sims.size(); ++i) checkpoint_free(b->sims[i], b->tune[i]);
     segbuf_free(b->segbuf);

@@ -43,11 +43,14 @@ struct Checkpoint {
     Control* ctl = nullptr;
 };
 
-// Device tables of a segmented copy (grown on demand).
+// Device tables of a segmented copy (grown on demand) and the size of the
+// list last uploaded.
 struct SegBuf {
     CopySeg* segs = nullptr;
     unsigned* first = nullptr;
     size_t cap = 0;
+    int nseg = 0;
+    unsigned nblocks = 0;
 };
 
 }  // namespace mpm
@@ -187,6 +190,8 @@ void checkpoint_segments(MpmHandle* h, Checkpoint& c, bool save, std::vector<Cop
 // Copy the segments in one launch on stream s (tables kept in `buf`, which
 // owns its device memory; errors are reported on h).
 int run_segments(MpmHandle* h, SegBuf& buf, const std::vector<CopySeg>& segs, cudaStream_t s);
+// Upload only (launch later, possibly many times, with launch_copy_segments).
+int upload_segments(MpmHandle* h, SegBuf& buf, const std::vector<CopySeg>& segs, cudaStream_t s);
 void segbuf_free(SegBuf& buf);
 
 }  // namespace host

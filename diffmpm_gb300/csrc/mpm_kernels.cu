@@ -1419,9 +1419,8 @@ cudaError_t launch_node_momentum(const float* m, const float* vx, const float* v
 // ---------------------------------------------------------------------------
 // Segmented copy and status gather for batches
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256)
-k_copy_segments(const CopySeg* __restrict__ segs, const unsigned* __restrict__ first, int nseg) {
-    const unsigned b = blockIdx.x;
+// Segment of block b: the last i with first[i] <= b.
+__device__ __forceinline__ int segment_of(const unsigned* __restrict__ first, int nseg, unsigned b) {
     int lo = 0, hi = nseg - 1;
     #pragma unroll 1
     while (lo < hi) {
@@ -1429,26 +1428,69 @@ k_copy_segments(const CopySeg* __restrict__ segs, const unsigned* __restrict__ f
         if (first[mid] <= b) lo = mid;
         else hi = mid - 1;
     }
-    const CopySeg sg = segs[lo];
-    const unsigned long long off = (unsigned long long)(b - first[lo]) * COPY_CHUNK;
+    return lo;
+}
+
+__global__ void __launch_bounds__(256)
+k_copy_segments(const CopySeg* __restrict__ segs, const unsigned* __restrict__ first, int nseg,
+                int t) {
+    const unsigned b = blockIdx.x;
+    const int i = segment_of(first, nseg, b);
+    const CopySeg sg = segs[i];
+    const unsigned long long off = (unsigned long long)(b - first[i]) * COPY_CHUNK;
     if (off >= sg.bytes) return;
     const unsigned long long end = min(off + COPY_CHUNK, sg.bytes);
     const char* src = static_cast<const char*>(sg.src);
-    char* dst = static_cast<char*>(sg.dst);
+    char* dst = static_cast<char*>(sg.dst) + (unsigned long long)t * sg.dst_step;
     const bool vec = ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15) == 0;
-    unsigned long long i = off;
+    unsigned long long k0 = off;
     if (vec) {
         const unsigned long long vend = off + ((end - off) & ~15ull);
         for (unsigned long long k = off + 16ull * threadIdx.x; k < vend; k += 16ull * blockDim.x)
             *reinterpret_cast<uint4*>(dst + k) = *reinterpret_cast<const uint4*>(src + k);
-        i = vend;
+        k0 = vend;
     }
-    for (unsigned long long k = i + threadIdx.x; k < end; k += blockDim.x) dst[k] = src[k];
+    for (unsigned long long k = k0 + threadIdx.x; k < end; k += blockDim.x) dst[k] = src[k];
 }
 
 cudaError_t launch_copy_segments(const CopySeg* segs, const unsigned* first, int nseg,
-                                 unsigned nblocks, cudaStream_t s) {
-    if (nseg > 0 && nblocks > 0) k_copy_segments<<<nblocks, 256, 0, s>>>(segs, first, nseg);
+                                 unsigned nblocks, int t, cudaStream_t s) {
+    if (nseg > 0 && nblocks > 0) k_copy_segments<<<nblocks, 256, 0, s>>>(segs, first, nseg, t);
+    return cudaGetLastError();
+}
+
+__global__ void __launch_bounds__(256)
+k_compare_segments(const CopySeg* __restrict__ segs, const unsigned* __restrict__ first, int nseg,
+                   int* __restrict__ mismatch) {
+    const unsigned b = blockIdx.x;
+    const int i = segment_of(first, nseg, b);
+    const CopySeg sg = segs[i];
+    const unsigned long long off = (unsigned long long)(b - first[i]) * COPY_CHUNK;
+    int diff = 0;
+    if (off < sg.bytes) {
+        const unsigned long long end = min(off + COPY_CHUNK, sg.bytes);
+        const char* a = static_cast<const char*>(sg.src);
+        const char* c = static_cast<const char*>(sg.dst);
+        const bool vec = ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(c)) & 15) == 0;
+        unsigned long long k0 = off;
+        if (vec) {
+            const unsigned long long vend = off + ((end - off) & ~15ull);
+            for (unsigned long long k = off + 16ull * threadIdx.x; k < vend; k += 16ull * blockDim.x) {
+                const uint4 x = *reinterpret_cast<const uint4*>(a + k);
+                const uint4 y = *reinterpret_cast<const uint4*>(c + k);
+                diff += (x.x != y.x) | (x.y != y.y) | (x.z != y.z) | (x.w != y.w);
+            }
+            k0 = vend;
+        }
+        for (unsigned long long k = k0 + threadIdx.x; k < end; k += blockDim.x) diff += a[k] != c[k];
+    }
+    const int total = __syncthreads_count(diff != 0);
+    if (threadIdx.x == 0 && total) atomicAdd(mismatch, total);
+}
+
+cudaError_t launch_compare_segments(const CopySeg* segs, const unsigned* first, int nseg,
+                                    unsigned nblocks, int* mismatch, cudaStream_t s) {
+    if (nseg > 0 && nblocks > 0) k_compare_segments<<<nblocks, 256, 0, s>>>(segs, first, nseg, mismatch);
     return cudaGetLastError();
 }
 

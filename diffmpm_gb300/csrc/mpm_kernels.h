@@ -87,16 +87,21 @@ cudaError_t launch_node_momentum(const float* m, const float* vx, const float* v
                                  float* out, cudaStream_t s);
 
 // Copy of many device-memory segments in one launch (snapshots and checkpoints
-// of whole batches).  Segment i is copied by the CTAs first[i] .. first[i+1]-1,
-// COPY_CHUNK bytes each; first[nseg] is the grid size.
+// of whole batches, the adjoint's tape).  Segment i is copied by the CTAs
+// first[i] .. first[i+1]-1, COPY_CHUNK bytes each; first[nseg] is the grid
+// size.  The destination of a launch with slot t is dst + t * dst_step.
 struct CopySeg {
     const void* src;
     void* dst;
     unsigned long long bytes;
+    unsigned long long dst_step;
 };
 constexpr unsigned COPY_CHUNK = 8192;
 cudaError_t launch_copy_segments(const CopySeg* segs, const unsigned* first, int nseg,
-                                 unsigned nblocks, cudaStream_t s);
+                                 unsigned nblocks, int t, cudaStream_t s);
+// *mismatch += number of differing 16-byte words or tail bytes between src and dst.
+cudaError_t launch_compare_segments(const CopySeg* segs, const unsigned* first, int nseg,
+                                    unsigned nblocks, int* mismatch, cudaStream_t s);
 
 // out[i] = *ctls[i], then ctls[i]->status = 0, for i < n.
 cudaError_t launch_gather_status(Control* const* ctls, int n, Control* out, cudaStream_t s);

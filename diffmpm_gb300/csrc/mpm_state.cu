@@ -18,6 +18,7 @@ void add(std::vector<CopySeg>& out, const void* src, void* dst, size_t bytes, bo
     s.src = save ? src : dst;
     s.dst = save ? dst : const_cast<void*>(src);
     s.bytes = bytes;
+    s.dst_step = 0;
     out.push_back(s);
 }
 
@@ -85,7 +86,9 @@ void segbuf_free(SegBuf& buf) {
     buf = SegBuf{};
 }
 
-int run_segments(MpmHandle* h, SegBuf& buf, const std::vector<CopySeg>& segs, cudaStream_t s) {
+int upload_segments(MpmHandle* h, SegBuf& buf, const std::vector<CopySeg>& segs, cudaStream_t s) {
+    buf.nseg = (int)segs.size();
+    buf.nblocks = 0;
     if (segs.empty()) return MPM_OK;
     std::vector<unsigned> first(segs.size() + 1);
     unsigned long long total = 0;
@@ -102,12 +105,19 @@ int run_segments(MpmHandle* h, SegBuf& buf, const std::vector<CopySeg>& segs, cu
         CK(h, cudaMalloc(&buf.first, sizeof(unsigned) * cap));
         buf.cap = cap;
     }
+    // (copies from pageable memory return once the host tables are staged)
     CK(h, cudaMemcpyAsync(buf.segs, segs.data(), sizeof(CopySeg) * segs.size(),
                           cudaMemcpyHostToDevice, s));
     CK(h, cudaMemcpyAsync(buf.first, first.data(), sizeof(unsigned) * first.size(),
                           cudaMemcpyHostToDevice, s));
-    // (copies from pageable memory return once the host tables are staged)
-    CK(h, launch_copy_segments(buf.segs, buf.first, (int)segs.size(), (unsigned)total, s));
+    buf.nseg = (int)segs.size();
+    buf.nblocks = (unsigned)total;
+    return MPM_OK;
+}
+
+int run_segments(MpmHandle* h, SegBuf& buf, const std::vector<CopySeg>& segs, cudaStream_t s) {
+    TRY(upload_segments(h, buf, segs, s));
+    CK(h, launch_copy_segments(buf.segs, buf.first, buf.nseg, buf.nblocks, 0, s));
     return MPM_OK;
 }
 

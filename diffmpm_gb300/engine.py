@@ -334,3 +334,55 @@ class Batch:
         self._ok(self._lib.mpm_batch_autotune(self._b, int(trial_steps), C.byref(blk), C.byref(ms),
                                               stream))
         return blk.value, ms.value
+
+    def record(self, nsteps, checkpoint_steps=100, stream=None):
+        """``Simulation.record`` for every member at once."""
+        self._ok(self._lib.mpm_batch_record(self._b, int(nsteps), int(checkpoint_steps), stream))
+
+    def adjoint(self, dl_dloc, dl_dvel=None, *, want=("youngs_modulus", "loc", "velocity")):
+        """``Simulation.adjoint`` for every member at once: ``dl_dloc`` (and the
+        optional ``dl_dvel``) are sequences with one (n_i, 2) array per member
+        (all NumPy, or all CUDA tensors); returns one dict per member."""
+        k = len(self.sims)
+        if len(dl_dloc) != k or (dl_dvel is not None and len(dl_dvel) != k):
+            raise ValueError("one seed array per simulation")
+        keep, dev = [], None
+        P = C.c_void_p * k
+
+        def table(arrs, count_of):
+            nonlocal dev
+            t = P()
+            for i, a in enumerate(arrs):
+                p, d, kp = _in_arg(a, np.float32, count_of(i))
+                if dev is None:
+                    dev = d
+                elif d != dev:
+                    raise ValueError("seeds must all be host arrays or all CUDA tensors")
+                keep.append(kp)
+                t[i] = p.value if isinstance(p, C.c_void_p) else p
+            return t
+
+        tl = table(dl_dloc, lambda i: 2 * self.sims[i].n)
+        tv = table(dl_dvel, lambda i: 2 * self.sims[i].n) if dl_dvel is not None else None
+        shapes = {"youngs_modulus": lambda n: (n,), "loc": lambda n: (n, 2), "velocity": lambda n: (n, 2)}
+        outs = [{} for _ in range(k)]
+        tabs = {}
+        for key in ("youngs_modulus", "loc", "velocity"):
+            if key not in want:
+                tabs[key] = None
+                continue
+            t = P()
+            for i, sim in enumerate(self.sims):
+                if dev:
+                    import torch
+                    o = torch.empty(shapes[key](sim.n), dtype=torch.float32, device=dl_dloc[i].device)
+                    t[i] = o.data_ptr()
+                else:
+                    o = np.empty(shapes[key](sim.n), dtype=np.float32)
+                    t[i] = o.ctypes.data
+                outs[i][key] = o
+            tabs[key] = t
+        stream = _stream_for(dl_dloc[0])
+        self._ok(self._lib.mpm_batch_adjoint(self._b, tl, tv, tabs["youngs_modulus"], tabs["loc"],
+                                             tabs["velocity"], dev or 0, stream))
+        return outs

@@ -253,6 +253,15 @@ int mpm_batch_set_block_steps(MpmBatch* b, int steps);
 int mpm_batch_autotune(MpmBatch* b, int trial_steps, int* block_steps, float* ms_per_step,
                        void* stream);
 
+/* mpm_record / mpm_adjoint for every simulation of a batch at once: one
+ * launch per re-run step and per reverse pass for all of them.  The arrays
+ * hold one pointer per simulation (batch order); dl_dvel and the outputs may be
+ * NULL as a whole or per entry. */
+int mpm_batch_record(MpmBatch* b, int nsteps, int checkpoint_steps, void* stream);
+int mpm_batch_adjoint(MpmBatch* b, const float* const* dl_dloc, const float* const* dl_dvel,
+                      float* const* dl_dE, float* const* dl_dloc0, float* const* dl_dvel0,
+                      int on_device, void* stream);
+
 /* Largest mesh (nx * ny elements) mpm_volume_setup_noalloc accepts. */
 #define MPM_NOALLOC_MAX_ELEMENTS (1 << 20)
 
