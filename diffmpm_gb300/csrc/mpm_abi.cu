@@ -383,12 +383,16 @@ int copy_passive(MpmHandle* h, int field, float* aos, bool to_aos, cudaStream_t 
 }
 
 // Roll the block that started at step0 back to its snapshot and replay its B
-// steps one at a time, re-sorting before each step; `st` gets the last status.
+// steps one at a time, re-sorting after every step that left a particle
+// outside its sort-cell; `st` gets the last status.  A particle that leaves
+// the mesh during the replay is an error; so is one that crosses two cells in
+// a single step (the replay starts every step with drift at most one cell).
 int replay_block(MpmHandle* h, int64_t step0, int B, int& st, cudaStream_t s) {
     h->rollbacks++;
     TRY(restore_snapshot(h, step0, s));
+    st = 0;
     for (int i = 0; i < B; ++i) {
-        TRY(resort(h, s));
+        if (st & ST_DRIFTED) TRY(resort(h, s));
         TRY(launch_steps(h, 1, s));
         h->step++;
         TRY(read_ctl(h, s));
@@ -946,9 +950,11 @@ int mpm_step(MpmHandle* h, int nsteps, void* stream) {
         TRY(run_graph(h, B, s));
         h->step += B;
         TRY(read_ctl(h, s));
-        int st = 0;
-        TRY(check_status(h, st));
+        // a two-cell drift corrupts the rest of the block (a particle may even be
+        // thrown out of the mesh by it): roll back before judging anything else
+        int st = h->h_ctl->status;
         if (st & ST_DRIFT_VIOLATION) TRY(replay_block(h, step0, B, st, s));
+        else TRY(check_status(h, st));
         h->needs_resort = (st & ST_DRIFTED) != 0;
         TRY(clear_status(h, s));
         nsteps -= B;

@@ -126,9 +126,10 @@ int batch_block(MpmBatch* b, int B, cudaStream_t s) {
     for (int i = 0; i < n; ++i) {
         MpmHandle* h = b->sims[i];
         int st = b->h_status[i].status;
-        if (st & ST_OUT_OF_MESH)
-            return bfail(b, MPM_ERR_OUT_OF_MESH, "simulation %d: a particle left the mesh", i);
+        // a two-cell drift corrupts the rest of the block: roll back first
         if (st & ST_DRIFT_VIOLATION) BTRY(b, i, replay_block(h, step0[i], B, st, s));
+        else if (st & ST_OUT_OF_MESH)
+            return bfail(b, MPM_ERR_OUT_OF_MESH, "simulation %d: a particle left the mesh", i);
         h->needs_resort = (st & ST_DRIFTED) != 0;
     }
     return MPM_OK;
@@ -223,7 +224,7 @@ int mpm_batch_destroy(MpmBatch* b) {
     if (!b) return MPM_OK;
     mpm::batch_adjoint_free(b);
     drop_batch_graphs(b);
-    for (size_t i = 0; i < b->tune.size() && i < b->sims.size(); ++i) checkpoint_free(b->sims[i], b->tune[i]);
+    // (the autotuner's saved states belong to the handles, which free them)
     segbuf_free(b->segbuf);
     if (b->cap) cudaStreamDestroy(b->cap);
     cudaFree(b->d_sims);

@@ -8,6 +8,7 @@ current stream).  All arithmetic runs in the CUDA library.
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 from typing import Sequence
 
 import numpy as np
@@ -59,6 +60,7 @@ class Simulation:
                  nodal_forces=(), materials=(), ndim=2):
         self._lib = _lib.load()
         self._h = C.c_void_p()
+        self._batches = weakref.WeakSet()   # batches holding this handle
         if scheme not in ("usf", "usl"):
             raise ValueError(f"Please select scheme from ('usf', 'usl'). Found {scheme}")
         nel = np.asarray(nelements, dtype=np.int64).reshape(-1)
@@ -141,6 +143,9 @@ class Simulation:
         _lib.check(rc, self._h)
 
     def close(self):
+        # a batch refers to its members' handles: it goes first
+        for b in list(getattr(self, "_batches", ())):
+            b.close()
         if self._h:
             self._lib.mpm_destroy(self._h)
             self._h = C.c_void_p()
@@ -300,6 +305,8 @@ class Batch:
         if rc != _lib.MPM_OK:
             self._b = C.c_void_p()
             _lib.check_batch(rc, None)
+        for s in self.sims:
+            s._batches.add(self)
 
     def _ok(self, rc):
         _lib.check_batch(rc, self._b)

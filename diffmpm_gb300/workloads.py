@@ -19,16 +19,19 @@ Inputs are seeded (NumPy PCG64); no dataset is involved.
   particles at n=256), per-particle Young's modulus 1e6 exp(0.5 z), z ~ N(0,1)
   seeded, nu=0.3, rho=1000, gravity, bottom fixed, USF, dt=5e-6, 2000 steps.
 * ``batch_specs`` / ``batch_member``  independent simulations of uneven size
-  (512 at full size): mesh side uniform in {32, ..., 256}, 4 Gauss-point
-  particles per cell in a seeded random rectangle of cells covering 20-60% of
-  the domain, resting on the fixed bottom and kept 5% of the width from the
-  side walls and the top (so that 1000 steps of gravity keep every particle in
-  the mesh), E log-uniform in [1e5, 1e8], nu uniform
-  in [0.2, 0.35], rho=1500, gravity, dt = 0.3 h / v_p with the P-wave
-  velocity of diffmpm/material.py:73-81, USF with velocity_update=True (with
-  the default False the reference's own step goes unstable on the softest
-  members within 1000 steps: in the float32 oracle particle 147 of member 86
-  leaves the mesh at step 963).
+  (512 at full size): mesh side uniform in {32, ..., 256} over [0, 0.05 m]^2,
+  4 Gauss-point particles per cell in a seeded random rectangle of cells
+  covering 20-60% of the domain, resting on the fixed bottom and kept 5% of
+  the width from the side walls and the top, E log-uniform in [1e5, 1e8],
+  nu uniform in [0.2, 0.35], rho=1500, gravity, dt = 0.3 h / v_p with the
+  P-wave velocity of diffmpm/material.py:73-81, USF, velocity_update=False.
+  The domain size is not part of the configuration; on [0, 1 m]^2 the softest
+  blocks sag by more than a cell under gravity, their free surfaces leave
+  nodes with vanishing mass, and the reference's step (a = nan_to_num(f/m),
+  diffmpm/element.py:311) blows up within 1000 steps (in the float32 oracle:
+  member 86 leaves the mesh at step 963; member 9 reaches 2991 m/s at step
+  799).  At 0.05 m the sag stays below a tenth of a cell and all 512 members
+  run 1000 steps.  Step cost does not depend on the domain size.
 * ``mixed_large``  n x n mesh (n=4096 at full size), an elastic block
   x in [0.125, 0.375] and a Newtonian block x in [0.625, 0.875], both
   y in [0, 0.5], 4 Gauss points per cell, elastic E=5e6, nu=0.3, rho=1800,
@@ -134,8 +137,9 @@ def differentiation(api, n=256, sim_steps=2000, dt=5e-6, seed=101, velocity=None
 
 
 def batch_specs(nsims=512, seed=5, sides=(32, 256), area=(0.2, 0.6), E=(1e5, 1e8),
-                nu=(0.2, 0.35), rho=1500.0, cfl=0.3):
-    """Seeded parameters of the batch members (plain dicts)."""
+                nu=(0.2, 0.35), rho=1500.0, cfl=0.3, domain=0.05, velocity_update=False):
+    """Seeded parameters of the batch members (plain dicts); the mesh covers
+    [0, domain]^2."""
     rng = np.random.Generator(np.random.PCG64(seed))
     out = []
     for _ in range(nsims):
@@ -151,15 +155,16 @@ def batch_specs(nsims=512, seed=5, sides=(32, 256), area=(0.2, 0.6), E=(1e5, 1e8
         Ek = float(np.exp(rng.uniform(np.log(E[0]), np.log(E[1]))))
         nuk = float(rng.uniform(*nu))
         M = Ek * (1 - nuk) / ((1 + nuk) * (1 - 2 * nuk))
-        dt = cfl * (1.0 / n) / np.sqrt(M / rho)
+        dt = cfl * (domain / n) / np.sqrt(M / rho)
         out.append({"side": n, "cells": (i0, i0 + wc, 0, hc), "E": Ek, "nu": nuk, "rho": rho,
-                    "dt": float(dt), "np": 4 * wc * hc})
+                    "dt": float(dt), "np": 4 * wc * hc, "domain": domain,
+                    "velocity_update": bool(velocity_update)})
     return out
 
 
 def batch_member(api, spec, sim_steps=1000, **kw):
     n = spec["side"]
-    h = 1.0 / n
+    h = spec["domain"] / n
     pts = gauss_points(*spec["cells"], h)
     mat = api.LinearElastic({"density": spec["rho"], "youngs_modulus": spec["E"],
                              "poisson_ratio": spec["nu"]})
@@ -168,8 +173,8 @@ def batch_member(api, spec, sim_steps=1000, **kw):
     el = _mesh(api, n, h, cons, kw)
     ps = api.Particles(pts.reshape(-1, 1, 2), mat, np.zeros(len(pts), dtype=np.int32), **kw)
     mesh = api.Mesh2D({"particles": [ps], "elements": el, "particle_surface_traction": []})
-    solver = api.MPMExplicit(mesh, spec["dt"], scheme="usf", velocity_update=True,
-                             sim_steps=sim_steps)
+    solver = api.MPMExplicit(mesh, spec["dt"], scheme="usf",
+                             velocity_update=spec["velocity_update"], sim_steps=sim_steps)
     return solver, np.array([0.0, -9.81]), {"workload": "batch_member", "n": n, "np": len(pts)}
 
 

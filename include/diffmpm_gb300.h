@@ -233,7 +233,8 @@ int mpm_adjoint(MpmHandle* h, const float* dl_dloc, const float* dl_dvel, float*
  * them, captured in CUDA graphs of step blocks.  The handles must be
  * initialised, on one device, and share the scheme, volume set-up and
  * traction set-up; each keeps its own state, so mpm_read_field etc. work on
- * them as usual.  Destroy the batch before its handles. */
+ * them as usual.  Destroy the batch before its handles (mpm_batch_destroy
+ * does not touch them). */
 typedef struct MpmBatch MpmBatch;
 
 int mpm_batch_create(MpmHandle* const* sims, int n, MpmBatch** out);

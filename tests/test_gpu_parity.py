@@ -248,3 +248,23 @@ def test_out_of_mesh_raises(built):
     sim.write("loc", loc)
     with pytest.raises(D.OutOfMeshError):
         sim.initialize()
+
+
+def test_long_block_drift_is_rolled_back(built):
+    """In a long step block a particle can drift two cells from its sort-cell;
+    the sums of the rest of the block are then wrong and may throw particles
+    out of the mesh.  The block must be rolled back and replayed (not reported
+    as out-of-mesh), and the run must match the oracle (a soft block on a 1 m
+    domain, 100-step blocks, 200 steps)."""
+    spec = workloads.batch_specs(domain=1.0, velocity_update=True)[332]
+    gs, g, _ = workloads.batch_member(D, spec, sim_steps=200)
+    sim = gs.simulation(g)
+    gs._upload(sim)
+    sim.initialize()
+    sim.set_block_steps(100)
+    sim.step(200)
+    assert sim.counters()["rollbacks"] >= 1
+    os_, og, _ = workloads.batch_member(O, spec, sim_steps=200)
+    for i in range(200):
+        os_.step(i, og)
+    assert rel(sim.read("loc"), os_.mesh.particles[0].loc.reshape(-1, 2)) < RUN_TOL
