@@ -1,22 +1,28 @@
-"""Benchmark of the explicit MPM step on GB300.
+"""Benchmark of the explicit MPM step and its adjoint on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload batch|plain] [--nsims 512] [--checkpoint-steps 100]
 
-Workload: the plain 2-D scale-up configuration -- 1024 x 1024 Q4 mesh, 4
-jittered Gauss-point particles per cell over x in [0, 0.5] (2,097,152
-particles), LinearElastic E=1e6 nu=0.25 rho=2000, gravity, roller walls and
-fixed bottom, dt=1e-6, USF (``--scheme usl`` for USL), float32.  A step is one
-explicit MPM step of the whole population.  The state (~190 MB) is larger than
-the 129 MB L2.
+Default workload (``batch``): the batching configuration -- 512 independent
+2-D USF simulations of uneven size (mesh side uniform in {32..256}, 4 Gauss-
+point particles per cell over a seeded random rectangle covering 20-60% of
+the domain, E log-uniform in [1e5, 1e8], nu in [0.2, 0.35], rho 1500,
+gravity, bottom fixed, dt from CFL 0.3; 19.6M particles in total), 1000
+steps, float32.  The headline ``value`` is batched forward + adjoint
+particle-steps/s: one checkpointed batched forward run (mpm_batch_record,
+checkpoints every 100 steps) plus the batched adjoint w.r.t. each
+simulation's E (mpm_batch_adjoint) of L = mean |x_end - x_target|^2, timed
+with CUDA events after one untimed warm-up iteration.  Beside it: the same
+batch forward only, and the plain path -- each simulation advanced alone by
+mpm_step, one after another -- which the spec ratio compares against.
+The plain 2-D scale-up configuration (1024^2 mesh, 2.1M particles, 500 USF
+steps) is measured too and gives the roofline of the plain forces kernel.
 
-Our arm prints one JSON line: device-timed particle-steps/s (``value``), an
-end-to-end number through the public API with host buffers (``e2e``), the
-roofline of the dominant kernel from CUDA-event timing of each phase, clocks
-sampled during the timed region, and a CPU baseline (the NumPy restatement of
-the reference step, one core, on a bounded sample).  ``--impl reference``
-times that CPU restatement alone (the reference itself is JAX, which is not
-installed on these machines).  Under torchrun each rank runs an independent
-replica (weak scaling) and rank 0 prints.
+``--impl reference`` times the CPU restatement of the reference step and its
+autograd gradient (the reference itself is JAX, not installed) on a sample of
+the same simulations with every host core (one process per core).  Under
+torchrun each rank runs an independent replica (weak scaling) and rank 0
+prints.
 """
 from __future__ import annotations
 
@@ -37,18 +43,23 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "particle-steps/s: batched fwd+adjoint vs plain fwd, 1 GB300, rel err ≤1e-5"
 UNIT = "particle-steps/s"
-MESH_N = 1024
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=500)
-    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "plain"])
+    ap.add_argument("--nsims", type=int, default=512)
+    ap.add_argument("--checkpoint-steps", type=int, default=100)
     ap.add_argument("--scheme", default="usf", choices=["usf", "usl"])
-    ap.add_argument("--n", type=int, default=MESH_N)
+    ap.add_argument("--n", type=int, default=1024, help="mesh side of the plain scale-up")
+    ap.add_argument("--plain-steps", type=int, default=500)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain-path", action="store_true",
+                    help="skip timing each simulation alone (the ratio's denominator)")
     ap.add_argument("--phase-steps", type=int, default=20)
     return ap.parse_args()
 
@@ -59,8 +70,7 @@ def dist_setup(args):
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch.distributed as dist
-        backend = "nccl" if args.impl == "ours" else "gloo"
-        dist.init_process_group(backend=backend)
+        dist.init_process_group(backend="nccl" if args.impl == "ours" else "gloo")
     return world, rank, local
 
 
@@ -139,97 +149,123 @@ def phase_bytes(np_, nn, scheme):
             "particle_kinematics": 104 * np_ + 16 * nn}
 
 
-def cpu_baseline(n, scheme, steps=2):
-    """The NumPy float32 restatement on the full workload, `steps` steps, one core."""
-    from oracle import mpm_oracle as O
+# ---------------------------------------------------------------------------
+# CPU arms: the NumPy / torch float32 restatements of the reference step
+# ---------------------------------------------------------------------------
+def _cpu_fwd_adj_member(args):
+    """Forward + autograd backward of `steps` steps of one batch member with
+    the float32 torch restatement; returns (particle-steps, seconds)."""
+    k, steps, seed_specs = args
+    import torch
+    torch.set_num_threads(1)
     from diffmpm_gb300 import workloads
-    s, g, info = workloads.plain_scaleup(O, n=n, scheme=scheme, sim_steps=steps)
+    from oracle import mpm_oracle as O
+    from oracle import mpm_torch as T
+    spec = workloads.batch_specs(**seed_specs)[k]
+    o, g, info = workloads.batch_member(O, spec, sim_steps=steps)
+    sim, st0 = T.from_solver(o, g, dtype=torch.float32)
+    n = info["np"]
     t0 = time.perf_counter()
-    for i in range(steps):
-        s.step(i, g)
-    dt = time.perf_counter() - t0
-    return {"value": info["np"] * steps / dt, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"{steps} of the 500 steps of the full workload ({info['np']} particles), "
-                      f"NumPy float32 restatement of the reference step"}
+    E = torch.tensor(spec["E"], dtype=torch.float32, requires_grad=True)
+    end = sim.run(dict(st0), steps, E=E.expand(n))
+    L = ((end["x"] - st0["x"] - 1e-4) ** 2).sum(1).mean()
+    L.backward()
+    return n * steps, time.perf_counter() - t0
+
+
+def cpu_fwd_adj(members, steps, workers, seed_specs=None):
+    """Particle-steps/s of forward + adjoint on the CPU over `members`."""
+    import multiprocessing as mp
+    jobs = [(k, steps, seed_specs or {}) for k in members]
+    if workers > 1:
+        with mp.get_context("spawn").Pool(workers) as pool:
+            res = pool.map(_cpu_fwd_adj_member, jobs)
+    else:
+        res = [_cpu_fwd_adj_member(j) for j in jobs]
+    # every core busy: the per-core rate (time inside the workers, without
+    # process start-up) times the number of cores
+    ps = sum(r[0] for r in res)
+    busy = sum(r[1] for r in res)
+    wall = busy / max(1, min(workers, len(jobs)))
+    return ps / wall, ps, wall
+
+
+def cpu_sample_members(nsims, limit_particles):
+    """The first batch members whose particle counts add up to `limit_particles`."""
+    from diffmpm_gb300 import workloads
+    specs = workloads.batch_specs(nsims=nsims)
+    out, tot = [], 0
+    for k, sp in enumerate(specs):
+        if tot + sp["np"] > limit_particles and out:
+            break
+        out.append(k)
+        tot += sp["np"]
+    return out, tot
 
 
 def run_reference(args, world, rank):
-    """CPU restatement of the reference step (the reference is JAX, not installed)."""
     if rank != 0:
         return
-    from oracle import mpm_oracle as O
-    from diffmpm_gb300 import workloads
-    rows = max(8, args.n // 8)
-    s, g, info = workloads.plain_scaleup(O, n=args.n, scheme=args.scheme,
-                                         sim_steps=args.steps + args.warmup, rows=rows)
-    for i in range(args.warmup):
-        s.step(i, g)
-    t0 = time.perf_counter()
-    for i in range(args.warmup, args.warmup + args.steps):
-        s.step(i, g)
-    el = time.perf_counter() - t0
-    v = info["np"] * args.steps / el
-    sample = (f"rows [0, {rows}) of the {args.n}x{args.n} workload ({info['np']} particles) per step, "
-              f"NumPy float32 restatement of the reference step (JAX is not installed)")
+    workers = os.cpu_count() or 1
+    steps = 20
+    members, tot = cpu_sample_members(args.nsims, 60000 * workers)
+    for _ in range(max(0, min(args.warmup, 1))):
+        cpu_fwd_adj(members[:workers], 2, workers)
+    v, ps, wall = cpu_fwd_adj(members, steps, workers)
+    sample = (f"{steps} steps of batch members {members[0]}..{members[-1]} ({tot} particles), "
+              f"float32 torch restatement of the reference step, forward + autograd adjoint "
+              f"w.r.t. each simulation's E, one process per core (JAX is not installed)")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * el / args.steps,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * wall / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": f"plain_scaleup_{args.scheme}", "mesh": f"{args.n}x{args.n}",
-                   "particles": info["np"], "sample": sample},
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+        "config": {"workload": "batch_fwd_adjoint", "sims": args.nsims, "sample": sample},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": workers, "kind": "port",
+                         "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
 
 
-def run_ours(args, world, rank, local):
-    import torch
-    torch.cuda.set_device(local)
-    import diffmpm_gb300 as D
-    from diffmpm_gb300 import workloads
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def build_batch(D, workloads, nsims, steps):
+    specs = workloads.batch_specs(nsims=nsims)
+    members = []
+    for sp in specs:
+        solver, g, info = workloads.batch_member(D, sp, sim_steps=steps)
+        sim = solver.simulation(g, reinit=True)
+        solver._upload(sim)
+        sim.initialize()
+        members.append((solver, sim, g))
+    return specs, members
 
+
+def reset_batch(members):
+    for solver, sim, g in members:
+        solver._upload(sim)
+        sim.initialize()
+
+
+def plain_scaleup(args, D, workloads, torch):
+    """The plain 2-D scale-up: device-timed forward, per-phase kernel times and
+    the roofline of the top kernel."""
     solver, g, info = workloads.plain_scaleup(D, n=args.n, scheme=args.scheme,
-                                              sim_steps=args.steps)
-    np_ = info["np"]
-    nn = (args.n + 1) ** 2
+                                              sim_steps=args.plain_steps)
+    np_, nn = info["np"], (args.n + 1) ** 2
     sim = solver.simulation(g, reinit=True)
     solver._upload(sim)
     sim.initialize()
-    sim.set_block_steps(min(100, max(1, args.steps)))
-    stream = torch.cuda.current_stream()
-
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
-
-    # warm-up (captures the step graphs)
+    sim.set_block_steps(100)
     sim.step(max(args.warmup, 3))
     torch.cuda.synchronize()
-    barrier()
-    clocks = ClockSampler(local)
-    clocks.start()
-    time.sleep(0.3)
-    torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    sim.step(args.steps)
-    e1.record(stream)
+    e0.record()
+    sim.step(args.plain_steps)
+    e1.record()
     torch.cuda.synchronize()
-    barrier()
-    clk = clocks.stop()
     ms = e0.elapsed_time(e1)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * np_ * args.steps / (ms / 1000.0)
-    counters = sim.counters()
-
-    # per-phase kernel time: CUDA events recorded between back-to-back launches
-    # of the phase kernels on the launching stream
     tot = sim.time_phases(args.phase_steps)
     avg = {k: v / args.phase_steps for k, v in tot.items()}
     top = max(avg, key=avg.get)
@@ -242,53 +278,200 @@ def run_ours(args, world, rank, local):
         for line in tf.read_text().splitlines():
             if line.startswith("dram bytes per launch:"):
                 traffic = int(line.split(":")[1])
+    out = {
+        "workload": f"plain_scaleup_{args.scheme}", "mesh": f"{args.n}x{args.n}", "particles": np_,
+        "steps": args.plain_steps, "value": np_ * args.plain_steps / (ms / 1000.0),
+        "ms_per_step": ms / args.plain_steps, "phase_ms": avg,
+        "step_roofline_frac": (workloads.particle_steps_bytes(np_, nn) * args.plain_steps
+                               / (ms / 1000.0) / 1e9) / peak,
+    }
+    roof = {"bound": "hbm", "kernel": top, "workload": out["workload"], "achieved": achieved,
+            "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": traffic, "algorithmic_bytes": pb[top]}
+    sim.close()
+    return out, roof
 
-    # end to end through the public API with host buffers: upload, set-up,
-    # K steps, read back loc/velocity/stress/strain (solve_jit's outputs)
-    host = {k: np.ascontiguousarray(v) for k, v in {
-        "loc": solver.mesh.particles[0].loc.reshape(-1, 2),
-        "velocity": solver.mesh.particles[0].velocity.reshape(-1, 2)}.items()}
+
+def run_ours(args, world, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    import diffmpm_gb300 as D
+    from diffmpm_gb300 import workloads
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def ev():
+        return torch.cuda.Event(enable_timing=True)
+
+    K = args.steps
+    specs, members = build_batch(D, workloads, args.nsims, K)
+    sims = [m[1] for m in members]
+    npart = sum(sp["np"] for sp in specs)
+    nnode = sum((sp["side"] + 1) ** 2 for sp in specs)
+    batch = D.Batch(sims)
+    _, ntiles = batch.size()
+    block, _ = batch.autotune(trial_steps=100)
+    ckpt = min(args.checkpoint_steps, K)
+    x0 = [sim.read("loc") for sim in sims]
+    targets = [x + 1e-4 for x in x0]
+
+    def seeds_for():
+        out = []
+        for sim, tgt in zip(sims, targets):
+            x = sim.read("loc")
+            out.append((2.0 / len(x) * (x - tgt)).astype(np.float32))
+        return out
+
+    # warm-up: W forward steps, then one full record + adjoint (allocations,
+    # graph capture), then back to the initial state
+    batch.step(max(args.warmup, 3))
+    reset_batch(members)
+    batch.record(K, ckpt)
+    batch.adjoint(seeds_for(), want=("youngs_modulus",))
+    reset_batch(members)
+    torch.cuda.synchronize()
+    barrier()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    # timed: batched forward + adjoint
+    e0, e1, e2, e3 = ev(), ev(), ev(), ev()
+    e0.record()
+    batch.record(K, ckpt)
+    e1.record()
+    torch.cuda.synchronize()
+    seeds = seeds_for()
+    e2.record()
+    grads = batch.adjoint(seeds, want=("youngs_modulus",))
+    e3.record()
+    torch.cuda.synchronize()
+    rec_ms, adj_ms = e0.elapsed_time(e1), e2.elapsed_time(e3)
+    fa_ms = rec_ms + adj_ms
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([fa_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        fa_ms = float(t.item())
+    dLdE = [float(g["youngs_modulus"].astype(np.float64).sum()) for g in grads]
+    # batched forward only
+    reset_batch(members)
+    torch.cuda.synchronize()
+    e0.record()
+    batch.step(K)
+    e1.record()
+    torch.cuda.synchronize()
+    fwd_ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    counters = {"resorts": sum(s.counters()["resorts"] for s in sims),
+                "rollbacks": sum(s.counters()["rollbacks"] for s in sims)}
+
+    # end to end through the public API with host buffers: upload of the
+    # initial states, record, adjoint with host seeds, gradients back
+    reset_batch(members)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    solver._upload(sim)
-    sim.initialize()
-    sim.step(args.steps)
-    outs = {k: sim.read(k) for k in ("loc", "velocity", "stress", "strain")}
+    reset_batch(members)
+    batch.record(K, ckpt)
+    seeds = seeds_for()
+    grads = batch.adjoint(seeds, want=("youngs_modulus",))
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
-    h2d = np_ * (2 + 2 + 6 + 6 + 1 + 1 + 1) * 4 + nn * 2 * 4
-    d2h = sum(v.nbytes for v in outs.values())
-    del host
+    h2d = npart * (2 + 2 + 6 + 6 + 1 + 1) * 4 + nnode * 2 * 4 + sum(s.nbytes for s in seeds)
+    d2h = npart * 2 * 4 + sum(g["youngs_modulus"].nbytes for g in grads)
+
+    # plain path: each simulation alone, one after another
+    plain_ms = None
+    if not args.no_plain_path:
+        batch.close()
+        reset_batch(members)
+        for sim in sims:
+            sim.set_block_steps(100)
+            sim.step(2)
+        reset_batch(members)
+        torch.cuda.synchronize()
+        e0.record()
+        for sim in sims:
+            sim.step(K)
+        e1.record()
+        torch.cuda.synchronize()
+        plain_ms = e0.elapsed_time(e1)
+    for sim in sims:
+        sim.close()
+    del members, sims
+
+    plain, roof = plain_scaleup(args, D, workloads, torch)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(args.n, args.scheme)
+        workers = os.cpu_count() or 1
+        mem, tot = cpu_sample_members(args.nsims, 30000 * workers)
+        v, ps, wall = cpu_fwd_adj(mem, 10, workers)
+        cpu = {"value": v, "unit": UNIT, "cores": workers, "kind": "port",
+               "sample": f"10 steps of batch members {mem[0]}..{mem[-1]} ({tot} particles), "
+                         f"float32 torch restatement of the reference step, forward + autograd "
+                         f"adjoint, one process per core"}
 
+    ps = npart * K
+    value = world * ps / (fa_ms / 1000.0)
+    # kernels of ours launched in the timed region (record + adjoint)
+    nseg = (K + ckpt - 1) // ckpt
+    launches = (3 * K + 2 * ((K + block - 1) // block) + (nseg + 1)        # record
+                + nseg * 6 + K * (5 + 5)                                  # adjoint re-run + reverse
+                + 9 * counters["resorts"] // 2)
     if rank == 0:
         print(json.dumps({
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic",
-            "config": {"workload": f"plain_scaleup_{args.scheme}", "mesh": f"{args.n}x{args.n}",
-                       "particles": np_, "nodes": nn, "dt": 1e-6,
-                       "l2": "inputs larger than L2 (~190 MB resident state)",
-                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                       "block_steps": min(100, max(1, args.steps))},
-            "e2e": {"value": world * np_ * args.steps / e2e_s, "unit": UNIT,
-                    "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
-                    "what": "upload + set-up + K steps + read of loc/velocity/stress/strain, host arrays"},
-            "gpu_launches": 3 * args.steps + 9 * counters.get("resorts", 0),
-            "phase_ms": avg,
-            "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak,
-                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": traffic, "algorithmic_bytes": pb[top]},
-            "step_roofline_frac": (workloads.particle_steps_bytes(np_, nn) * args.steps
-                                   / (ms / 1000.0) / 1e9) / peak,
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
+            "warmup": args.warmup, "ms_per_step": fa_ms / K, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "batch_fwd_adjoint", "sims": args.nsims, "particles": npart,
+                       "nodes": nnode, "tiles_per_launch": ntiles, "steps": K,
+                       "checkpoint_steps": ckpt, "block_steps": block, "domain_m": 0.05,
+                       "dt": "CFL 0.3 per simulation", "scheme": "usf",
+                       "loss": "mean |x_end - x_target|^2 per simulation, grad w.r.t. its E",
+                       "l2": "inputs larger than L2 (~2 GB of particle state)",
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+            "components": {
+                "batch_fwd_adjoint": value / world,
+                "batch_fwd": ps / (fwd_ms / 1000.0),
+                "plain_fwd": ps / (plain_ms / 1000.0) if plain_ms else None,
+                "ratio_fwd_adjoint_vs_plain_fwd": (plain_ms / fa_ms) if plain_ms else None,
+                "ratio_batch_fwd_vs_plain_fwd": (plain_ms / fwd_ms) if plain_ms else None,
+                "record_ms": rec_ms, "adjoint_ms": adj_ms, "batch_fwd_ms": fwd_ms,
+                "plain_fwd_ms": plain_ms},
+            "dLdE_first_sims": dLdE[:4],
+            "e2e": {"value": world * ps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d / K,
+                    "d2h_bytes_per_step": d2h / K,
+                    "what": "upload of all initial states + batched record + adjoint with host "
+                            "seeds + gradients to host"},
+            "gpu_launches": launches,
+            "roofline": roof,
+            "plain_scaleup": plain,
             "clocks": clk,
             "counters": counters,
             "cpu_baseline": cpu,
         }), flush=True)
+
+
+def run_ours_plain(args, world, rank, local):
+    """``--workload plain``: the plain scale-up alone (a short run for profiling)."""
+    import torch
+    torch.cuda.set_device(local)
+    import diffmpm_gb300 as D
+    from diffmpm_gb300 import workloads
+    args.plain_steps = args.steps
+    plain, roof = plain_scaleup(args, D, workloads, torch)
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": world * plain["value"], "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": plain["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": {"workload": plain["workload"], "mesh": plain["mesh"],
+                                            "particles": plain["particles"]},
+            "roofline": roof, "plain_scaleup": plain}), flush=True)
 
 
 def main():
@@ -296,6 +479,8 @@ def main():
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.workload == "plain":
+        run_ours_plain(args, world, rank, local)
     else:
         run_ours(args, world, rank, local)
     if world > 1:
