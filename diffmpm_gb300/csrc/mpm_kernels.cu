@@ -202,6 +202,23 @@ __device__ __forceinline__ bool tile_drifted(const SimDev& S, int c0x, int c0y) 
     return __syncthreads_or(any) != 0;
 }
 
+// True when a particle is stored in the sort-cells [x0, x1) x [y0, y1)
+// (clamped to the mesh); also a block barrier.  A particle is at most one
+// cell from its sort-cell, so when the cells of a tile and the ring of cells
+// around them store no particle, no particle is in the tile's cells.
+__device__ __forceinline__ bool sort_cells_occupied(const SimDev& S, int x0, int x1, int y0,
+                                                    int y1) {
+    x0 = max(x0, 0);
+    x1 = min(x1, S.nx);
+    y0 = max(y0, 0);
+    y1 = min(y1, S.ny);
+    int any = 0;
+    if (x0 < x1)
+        for (int r = y0 + (int)threadIdx.x; r < y1; r += blockDim.x)
+            any |= S.cstart[r * S.nx + x1] != S.cstart[r * S.nx + x0];
+    return __syncthreads_or(any) != 0;
+}
+
 // Per-warp staging of the chunks of a row: chunk c of [rb, re) holds storage
 // indices rb + 32c + lane; field f of it lands in buf[c % DEPTH][f][lane].
 template <int NF, int DEPTH>
@@ -422,6 +439,18 @@ __device__ __forceinline__ void nodal_kinematics_tile(const SimDev& S, const int
     const bool node_ok = lx < TILE_NX && ly < TILE_NY && c0x + 1 + lx <= S.nx && c0y + 1 + ly <= S.ny;
     const int node = (c0y + 1 + ly) * (S.nx + 1) + c0x + 1 + lx;
     const uint16_t ncons = node_ok ? S.ncons[node] : 0;   // node-phase input, fetched early
+    if (!sort_cells_occupied(S, c0x - 1, c0x + TILE_CX + 1, c0y - 1, c0y + TILE_CY + 1)) {
+        // no particle in the tile: every node is massless and keeps its
+        // velocity (the node phase below with all sums zero)
+        if (node_ok) {
+            float vx = flush(S.nvbx[node]), vy = flush(S.nvby[node]);
+            apply_constraint(S, ncons, vx, vy, nullptr, nullptr);
+            S.nm[node] = 0.0f;
+            S.nvax[node] = vx;
+            S.nvay[node] = vy;
+        }
+        return;
+    }
     #pragma unroll
     for (int k = 0; k < NQ; ++k) s_c[k][tid] = 0.0f;
     load_row_starts(S, c0x, cj, s_cs[ly], lx);
@@ -573,6 +602,11 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
     // node-phase inputs, fetched early
     const float nmass = node_ok ? S.nm[node] : 0.0f;
     const uint16_t ncons = node_ok ? S.ncons[node] : 0;
+    if (!sort_cells_occupied(S, c0x - 1, c0x + TILE_CX + 1, c0y - 1, c0y + TILE_CY + 1)) {
+        // no particle in the tile: the nodal update with zero particle forces
+        if (node_ok) nodal_update(S, node, t, 0.0f, 0.0f, S.nvax[node], S.nvay[node], nmass, ncons);
+        return;
+    }
     #pragma unroll
     for (int k = 0; k < NQ; ++k) s_c[k][tid] = 0.0f;
     load_row_starts(S, c0x, cj, s_cs[ly], lx);
@@ -776,7 +810,9 @@ __device__ __forceinline__ void particle_kinematics_tile(const SimDev& S, const 
     }
     st.prime();
     if (tid == 0) s_status = 0;
-    for (int idx = tid; idx < G_W * G_H; idx += TILE_THREADS) {
+    // a tile whose rows store no particle only clears its drift flags
+    const bool occupied = __syncthreads_or(re > rb) != 0;
+    for (int idx = tid; occupied && idx < G_W * G_H; idx += TILE_THREADS) {
         const int I = c0x + idx % G_W, J = c0y + idx / G_W;
         float vx = 0.0f, vy = 0.0f, ax = 0.0f, ay = 0.0f;
         if (I >= 0 && I <= S.nx && J >= 0 && J <= S.ny) {
@@ -791,7 +827,7 @@ __device__ __forceinline__ void particle_kinematics_tile(const SimDev& S, const 
         s_ax[idx] = ax;
         s_ay[idx] = ay;
     }
-    build_geo(S, c0x, c0y, G);
+    if (occupied) build_geo(S, c0x, c0y, G);
     __syncthreads();
     int status = 0;
     const int* cs = s_cs[w];
