@@ -390,25 +390,33 @@ __device__ __forceinline__ void force_contrib(const SimDev& S, int q, const Forc
     add_traction<TRAC>(S, q, t, V, REINIT ? size0 : (S.psize ? S.psize[q] : 1.0f), N, c, c + 4);
 }
 
-// Fast-path accumulation of one chunk [base, min(base + 32, re)) of row `row`
-// holding cells c_lo .. c_hi of the row: the warp's lanes share the
-// (cell, quantity) pairs, and each pair adds its cell's slots in storage order.
-constexpr int SLOT_STRIDE = 33;
+// Fast path of the two particle-to-grid phases: warp w stages the particles
+// stored in sort-cell row w of the tile (storage range [rb, re)) into shared
+// memory with coalesced cp.async copies, ROW_P particles per pass, and lane l
+// then visits the particles of its own cell (storage range [cb, ce)) in storage
+// order, summing their corner contributions in registers: the same order and
+// the same roundings as the slow path's visit_cell, so both paths give the
+// same bits.
+constexpr int ROW_P = 160;
 
-template <int NQ>
-__device__ __forceinline__ void accumulate_chunk(float (*s_c)[SC_STRIDE],
-                                                 const float (*slot)[SLOT_STRIDE], const int* cs,
-                                                 int base, int end, int c_lo, int c_hi, int lane,
-                                                 int row) {
-    const int npairs = (c_hi - c_lo + 1) * NQ;
+template <int NF, class F>
+__device__ __forceinline__ void row_pass(float (*buf)[ROW_P], const float* const (&src)[NF], int rb,
+                                         int re, int cb, int ce, int lane, F&& f) {
     #pragma unroll 1
-    for (int p = lane; p < npairs; p += 32) {
-        const int cell = c_lo + p / NQ, k = p % NQ;
-        const int lo = max(cs[cell], base), hi = min(cs[cell + 1], end);
-        float acc = s_c[k][row * 32 + cell];
+    for (int p0 = rb; p0 < re; p0 += ROW_P) {
+        const int p1 = min(p0 + ROW_P, re);
+        for (int q = p0 + lane; q < p1; q += 32) {
+            #pragma unroll
+            for (int k = 0; k < NF; ++k)
+                if (src[k]) cp_async4(&buf[k][q - p0], src[k] + q);
+        }
+        cp_async_commit();
+        cp_async_wait<0>();
+        __syncwarp();
+        const int lo = max(cb, p0), hi = min(ce, p1);
         #pragma unroll 1
-        for (int qq = lo; qq < hi; ++qq) acc = fa(acc, slot[k][qq - base]);
-        s_c[k][row * 32 + cell] = acc;
+        for (int q = lo; q < hi; ++q) f(q, q - p0);
+        __syncwarp();
     }
 }
 
@@ -418,7 +426,6 @@ __device__ __forceinline__ void accumulate_chunk(float (*s_c)[SC_STRIDE],
 //   P2G of mass and momentum (element.py:122-189), nodal velocity
 //   (element.py:191-202), velocity constraints (element.py:331-334).
 // ---------------------------------------------------------------------------
-constexpr int K1_DEPTH = 4;
 constexpr int K1_NF = 5;   // x, y, vx, vy, rho (solve_jit) or mass (solve)
 
 template <bool REINIT>
@@ -426,10 +433,8 @@ __device__ __forceinline__ void nodal_kinematics_tile(const SimDev& S, const int
                                                       Control* __restrict__ ctl) {
     constexpr int NQ = 12;
     __shared__ float s_c[NQ][SC_STRIDE];               // [m, px, py] x corner, per cell
-    __shared__ float s_slot[TILE_CY][NQ][SLOT_STRIDE]; // per-warp particle contributions
-    __shared__ float s_stage[TILE_CY][K1_DEPTH][K1_NF][32];
+    __shared__ float s_row[TILE_CY][K1_NF][ROW_P];     // staged particles of each cell row
     __shared__ int s_cs[TILE_CY][33];
-    __shared__ float s_V0[TILE_CY][32];
     __shared__ TileGeo G;
     const int parity = load_step(ctl) & 1;
     const int tid = threadIdx.x, lx = tid & (TILE_CX - 1), ly = tid / TILE_CX;
@@ -459,34 +464,23 @@ __device__ __forceinline__ void nodal_kinematics_tile(const SimDev& S, const int
 
     if (!slow) {
         const int* cs = s_cs[ly];
-        const int rb = cs[0], re = cs[32];
         const int cb = cs[lx], ce = cs[lx + 1];
-        RowStage<K1_NF, K1_DEPTH> st{s_stage[ly], {S.x, S.y, S.vx, S.vy, REINIT ? rho : S.mass},
-                                     rb, re, (re - rb + 31) / 32, lx};
-        st.prime();
-        if (REINIT) s_V0[ly][lx] = ce > cb ? fdv(S.vol_el, (float)(ce - cb)) : 0.0f;
-        const float cy = G.cy[ly + 1], ry = G.ry[ly + 1];   // row geometry (warp-uniform)
-        __syncwarp();
-        #pragma unroll 1
-        for (int c = 0; c < st.nch; ++c) {
-            const float (*b)[32] = st.advance(c);
-            const int base = rb + 32 * c, q = base + lx, end = min(base + 32, re);
-            int l = -1;
-            if (q < re) {
-                l = cell_of(cs, 31, q);
-                const float m = REINIT ? fm(s_V0[ly][l], b[4][lx]) : b[4][lx];
-                float cc[NQ];
-                mass_contrib(b[0][lx], b[1][lx], b[2][lx], b[3][lx], m, G.cx[l + 1], G.rx[l + 1],
-                             cy, ry, cc);
-                #pragma unroll
-                for (int k = 0; k < NQ; ++k) s_slot[ly][k][lx] = cc[k];
-            }
-            const int c_lo = __shfl_sync(0xffffffffu, l, 0);
-            const int c_hi = __shfl_sync(0xffffffffu, l, end - 1 - base);
-            __syncwarp();
-            accumulate_chunk<NQ>(s_c, s_slot[ly], cs, base, end, c_lo, c_hi, lx, ly);
-            __syncwarp();
-        }
+        const CellGeo g = geo_of(G, lx + 1, ly + 1);
+        const float V0 = (REINIT && ce > cb) ? fdv(S.vol_el, (float)(ce - cb)) : 0.0f;
+        float acc[NQ];
+        #pragma unroll
+        for (int k = 0; k < NQ; ++k) acc[k] = 0.0f;
+        const float* const src[K1_NF] = {S.x, S.y, S.vx, S.vy, REINIT ? rho : S.mass};
+        float (*buf)[ROW_P] = s_row[ly];
+        row_pass<K1_NF>(buf, src, cs[0], cs[32], cb, ce, lx, [&](int, int j) {
+            const float m = REINIT ? fm(V0, buf[4][j]) : buf[4][j];
+            float cc[NQ];
+            mass_contrib(buf[0][j], buf[1][j], buf[2][j], buf[3][j], m, g.cx, g.rx, g.cy, g.ry, cc);
+            #pragma unroll
+            for (int k = 0; k < NQ; ++k) acc[k] = fa(acc[k], cc[k]);
+        });
+        #pragma unroll
+        for (int k = 0; k < NQ; ++k) s_c[k][tid] = acc[k];
     } else if (ci >= 0 && ci < S.nx && cj >= 0 && cj < S.ny) {
         const CellGeo g = geo_of(G, lx + 1, ly + 1);
         float V0 = 0.0f;
@@ -525,14 +519,14 @@ __device__ __forceinline__ void nodal_kinematics_tile(const SimDev& S, const int
 }
 
 template <bool REINIT>
-__global__ void __launch_bounds__(TILE_THREADS, 2)
+__global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
 k_nodal_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
                    Control* __restrict__ ctl) {
     nodal_kinematics_tile<REINIT>(S, tiles[blockIdx.x], ctl);
 }
 
 template <bool REINIT>
-__global__ void __launch_bounds__(TILE_THREADS, 2)
+__global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
 k_nodal_kinematics_batch(const SimDev* const* __restrict__ sims, Control* const* __restrict__ ctls,
                          const int4* __restrict__ tiles) {
     __shared__ SimDev sS;
@@ -578,17 +572,17 @@ __device__ __forceinline__ void nodal_update(const SimDev& S, int n, float t, fl
 // ---------------------------------------------------------------------------
 constexpr int NV_W = TILE_CX + 1;   // node tile of the R cells: [c0x, c0x+33) x [c0y, c0y+17)
 constexpr int NV_H = TILE_CY + 1;
-constexpr int K2_DEPTH = 2;
+constexpr int K2_ROW_P = 128;   // particles of a row per pass (two CTAs per SM)
 
 template <bool USL, bool REINIT, bool TRAC>
 __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
                                             Control* __restrict__ ctl) {
     constexpr int NQ = 8;
     __shared__ float s_c[NQ][SC_STRIDE];               // [f x, f y] x corner, per cell
-    __shared__ float s_slot[TILE_CY][NQ][SLOT_STRIDE];
-    __shared__ float s_stage[TILE_CY][K2_DEPTH][FF_N][32];
+    __shared__ float s_slot[TILE_CY][NQ][K2_ROW_P];    // contributions of a row's particles
+    __shared__ unsigned char s_cell[TILE_CY][K2_ROW_P];   // their cell within the row
+    __shared__ float s_cellv[TILE_CY][3][32];          // V0, size0, dvol per cell
     __shared__ int s_cs[TILE_CY][33];
-    __shared__ float s_V0[TILE_CY][32], s_size0[TILE_CY][32], s_dvol[TILE_CY][32];
     __shared__ float s_vx[NV_W * NV_H], s_vy[NV_W * NV_H];
     __shared__ TileGeo G;
     const int step = load_step(ctl);
@@ -635,57 +629,54 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
     };
 
     if (!slow) {
+        // particle per lane for the per-particle work (coalesced global loads
+        // and stores), contributions to row slots, then lane per cell adds
+        // the slots of its cell's particles in storage order
         const int* cs = s_cs[ly];
         const int rb = cs[0], re = cs[32];
         const int cb = cs[lx], ce = cs[lx + 1];
-        RowStage<FF_N, K2_DEPTH> st{s_stage[ly],
-                                    {S.x, S.y, S.sxx[parity], S.syy[parity], S.szz[parity],
-                                     S.sxy[parity], S.rho[parity], REINIT ? nullptr : S.vol[parity]},
-                                    rb, re, (re - rb + 31) / 32, lx};
-        st.prime();
         {
-            // per-cell values, one lane per cell of the row
             float nvx[4], nvy[4], V0, size0, dvol;
             if (!USL) cell_velocities(lx, ly, nvx, nvy);
             force_cell_values<USL, REINIT>(S, ce - cb, geo_of(G, lx + 1, ly + 1), nvx, nvy, V0,
                                            size0, dvol);
-            s_V0[ly][lx] = V0;
-            s_size0[ly][lx] = size0;
-            s_dvol[ly][lx] = dvol;
+            s_cellv[ly][0][lx] = V0;
+            s_cellv[ly][1][lx] = size0;
+            s_cellv[ly][2][lx] = dvol;
         }
         const float cy = G.cy[ly + 1], ry = G.ry[ly + 1];   // row geometry (warp-uniform)
-        __syncwarp();
+        float acc[NQ];
+        #pragma unroll
+        for (int k = 0; k < NQ; ++k) acc[k] = 0.0f;
         #pragma unroll 1
-        for (int c = 0; c < st.nch; ++c) {
-            const float (*b)[32] = st.advance(c);
-            const int base = rb + 32 * c, q = base + lx, end = min(base + 32, re);
-            int l = -1;
-            if (q < re) {
-                l = cell_of(cs, 31, q);
+        for (int p0 = rb; p0 < re; p0 += K2_ROW_P) {
+            const int p1 = min(p0 + K2_ROW_P, re);
+            for (int q = max(cb, p0); q < min(ce, p1); ++q) s_cell[ly][q - p0] = (unsigned char)lx;
+            __syncwarp();
+            #pragma unroll 1
+            for (int q = p0 + lx; q < p1; q += 32) {
+                const int l = s_cell[ly][q - p0];
                 float nvx[4], nvy[4];
                 if (!USL) cell_velocities(l, ly, nvx, nvy);
-                ForceIn in;
-                in.x = b[FF_X][lx];
-                in.y = b[FF_Y][lx];
-                in.sxx = b[FF_SXX][lx];
-                in.syy = b[FF_SYY][lx];
-                in.szz = b[FF_SZZ][lx];
-                in.sxy = b[FF_SXY][lx];
-                in.rho = b[FF_RHO][lx];
-                in.vol = REINIT ? 0.0f : b[FF_VOL][lx];
                 float cc[NQ];
-                force_contrib<USL, REINIT, TRAC>(S, q, in, G.cx[l + 1], G.rx[l + 1], cy, ry,
-                                                 s_V0[ly][l], s_size0[ly][l], nvx, nvy,
-                                                 s_dvol[ly][l], parity, t, l >= 1 && ly >= 1, cc);
+                force_contrib<USL, REINIT, TRAC>(S, q, force_in_global(S, q, parity, REINIT),
+                                                 G.cx[l + 1], G.rx[l + 1], cy, ry,
+                                                 s_cellv[ly][0][l], s_cellv[ly][1][l], nvx, nvy,
+                                                 s_cellv[ly][2][l], parity, t, l >= 1 && ly >= 1,
+                                                 cc);
                 #pragma unroll
-                for (int k = 0; k < NQ; ++k) s_slot[ly][k][lx] = cc[k];
+                for (int k = 0; k < NQ; ++k) s_slot[ly][k][q - p0] = cc[k];
             }
-            const int c_lo = __shfl_sync(0xffffffffu, l, 0);
-            const int c_hi = __shfl_sync(0xffffffffu, l, end - 1 - base);
             __syncwarp();
-            accumulate_chunk<NQ>(s_c, s_slot[ly], cs, base, end, c_lo, c_hi, lx, ly);
+            #pragma unroll 1
+            for (int q = max(cb, p0); q < min(ce, p1); ++q) {
+                #pragma unroll
+                for (int k = 0; k < NQ; ++k) acc[k] = fa(acc[k], s_slot[ly][k][q - p0]);
+            }
             __syncwarp();
         }
+        #pragma unroll
+        for (int k = 0; k < NQ; ++k) s_c[k][tid] = acc[k];
     } else if (ci >= 0 && ci < S.nx && cj >= 0 && cj < S.ny) {
         const CellGeo g = geo_of(G, lx + 1, ly + 1);
         const int cnt = REINIT ? count_cell(S, ci, cj, g) : 0;
@@ -711,14 +702,14 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
 }
 
 template <bool USL, bool REINIT, bool TRAC>
-__global__ void __launch_bounds__(TILE_THREADS, 2)
+__global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
 k_forces(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
          Control* __restrict__ ctl) {
     forces_tile<USL, REINIT, TRAC>(S, tiles[blockIdx.x], ctl);
 }
 
 template <bool USL, bool REINIT, bool TRAC>
-__global__ void __launch_bounds__(TILE_THREADS, 2)
+__global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
 k_forces_batch(const SimDev* const* __restrict__ sims, Control* const* __restrict__ ctls,
                const int4* __restrict__ tiles) {
     __shared__ SimDev sS;
@@ -970,14 +961,14 @@ __device__ __forceinline__ void particle_kinematics_tile(const SimDev& S, const 
 }
 
 template <bool USL, bool REINIT>
-__global__ void __launch_bounds__(TILE_THREADS, 2)
+__global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
 k_particle_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
                       Control* __restrict__ ctl) {
     particle_kinematics_tile<USL, REINIT>(S, tiles[blockIdx.x], ctl);
 }
 
 template <bool USL, bool REINIT>
-__global__ void __launch_bounds__(TILE_THREADS, 2)
+__global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
 k_particle_kinematics_batch(const SimDev* const* __restrict__ sims, Control* const* __restrict__ ctls,
                             const int4* __restrict__ tiles) {
     __shared__ SimDev sS;

@@ -21,6 +21,7 @@ constexpr int TILE_CY = 16;              // cell rows per tile
 constexpr int TILE_NX = TILE_CX - 1;     // nodes owned per tile row
 constexpr int TILE_NY = TILE_CY - 1;     // node rows owned per tile
 constexpr int TILE_THREADS = TILE_CX * TILE_CY;
+constexpr int TILE_MIN_CTAS = 16 / TILE_CY * 2;   // resident CTAs per SM the kernels are built for
 
 enum StatusBits : int {
     ST_OUT_OF_MESH = 1,     // a particle left the mesh
