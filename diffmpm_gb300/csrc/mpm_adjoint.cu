@@ -85,9 +85,8 @@ struct BatchAdjoint {
     AdjStep* d_bases = nullptr;
     AdjStep* d_table = nullptr;
     std::vector<AdjStep> bases;
-    int2* node_blocks = nullptr;
     int2* part_blocks = nullptr;
-    int n_node_blocks = 0, n_part_blocks = 0;
+    int n_part_blocks = 0;
     SegBuf tape_p[2], tape_n, misc;
     int* mismatch = nullptr;
     int* h_mismatch = nullptr;
@@ -364,9 +363,9 @@ int reverse_step(MpmHandle* h, AdjointState* a, int t, cudaStream_t s) {
     A.sxx += op; A.syy += op; A.szz += op; A.sxy += op; A.rho += op;
     A.cflag += oc;
     A.nm += on; A.nvax += on; A.nvay += on; A.nvbx += on; A.nvby += on; A.nax += on; A.nay += on;
-    CK(h, launch_rev_nodal_update(A, s));
+    CK(h, launch_rev_nodal_update(A, h->dtiles, h->ntiles, s));
     CK(h, launch_rev_forces(A, s));
-    CK(h, launch_rev_nodal_kinematics(A, s));
+    CK(h, launch_rev_nodal_kinematics(A, h->dtiles, h->ntiles, s));
     CK(h, launch_rev_mass_momentum(A, s));
     return MPM_OK;
 }
@@ -478,7 +477,6 @@ void batch_adjoint_free(MpmBatch* b) {
     if (!x) return;
     cudaFree(x->d_bases);
     cudaFree(x->d_table);
-    cudaFree(x->node_blocks);
     cudaFree(x->part_blocks);
     cudaFree(x->mismatch);
     if (x->h_mismatch) cudaFreeHost(x->h_mismatch);
@@ -593,21 +591,16 @@ int ensure_batch_adjoint(MpmBatch* b, cudaStream_t s) {
         BCK(b, cudaMallocHost(&x->h_mismatch, sizeof(int)));
     }
     // block maps (particle counts may have changed since the last call)
-    std::vector<int2> nb, pb;
+    std::vector<int2> pb;
     for (int i = 0; i < n; ++i) {
         const MpmHandle* h = b->sims[i];
-        for (int c = 0; c * ADJ_BLOCK < h->nn; ++c) nb.push_back(make_int2(i, c));
         for (int c = 0; c * ADJ_BLOCK < h->np; ++c) pb.push_back(make_int2(i, c));
     }
-    cudaFree(x->node_blocks);
     cudaFree(x->part_blocks);
-    x->node_blocks = x->part_blocks = nullptr;
-    BCK(b, cudaMalloc(&x->node_blocks, sizeof(int2) * nb.size()));
+    x->part_blocks = nullptr;
     BCK(b, cudaMalloc(&x->part_blocks, sizeof(int2) * pb.size()));
-    BCK(b, cudaMemcpyAsync(x->node_blocks, nb.data(), sizeof(int2) * nb.size(), cudaMemcpyHostToDevice, s));
     BCK(b, cudaMemcpyAsync(x->part_blocks, pb.data(), sizeof(int2) * pb.size(), cudaMemcpyHostToDevice, s));
     BCK(b, cudaStreamSynchronize(s));
-    x->n_node_blocks = (int)nb.size();
     x->n_part_blocks = (int)pb.size();
     return MPM_OK;
 }
@@ -747,7 +740,7 @@ int mpm_batch_adjoint(MpmBatch* b, const float* const* dl_dloc, const float* con
             }
             if (r != MPM_OK) break;
             BCK(b, launch_adj_table(x->d_bases, n, t, x->d_table, s));
-            BCK(b, launch_rev_batch(x->d_table, x->node_blocks, x->n_node_blocks, x->part_blocks,
+            BCK(b, launch_rev_batch(x->d_table, b->d_tiles, b->ntiles, x->part_blocks,
                                     x->n_part_blocks, s));
         }
         for (int i = 0; i < n && r == MPM_OK; ++i) {

@@ -53,18 +53,22 @@ struct AdjStep {
     long long sp, sn, sc;
 };
 
-cudaError_t launch_rev_nodal_update(const AdjStep& A, cudaStream_t s);
+// Passes 1 and 3 run over the forward kernels' tile list, passes 2 and 4 over
+// the particles.
+cudaError_t launch_rev_nodal_update(const AdjStep& A, const int4* tiles, int ntiles,
+                                    cudaStream_t s);
 cudaError_t launch_rev_forces(const AdjStep& A, cudaStream_t s);
-cudaError_t launch_rev_nodal_kinematics(const AdjStep& A, cudaStream_t s);
+cudaError_t launch_rev_nodal_kinematics(const AdjStep& A, const int4* tiles, int ntiles,
+                                        cudaStream_t s);
 cudaError_t launch_rev_mass_momentum(const AdjStep& A, cudaStream_t s);
 
 // Batches: table[i] = bases[i] with the tape pointers at slot t; then the four
-// passes over every simulation, CTA b working on simulation blocks[b].x,
-// elements blocks[b].y * 256 .. + 255 (nodes for passes 1 and 3, particles
-// for passes 2 and 4).
+// passes over every simulation: passes 1 and 3 over the batch's tile list
+// (tile t of simulation tiles[t].x), passes 2 and 4 with CTA b on simulation
+// part_blocks[b].x, particles part_blocks[b].y * 256 .. + 255.
 constexpr int ADJ_BLOCK = 256;
 cudaError_t launch_adj_table(const AdjStep* bases, int n, int t, AdjStep* table, cudaStream_t s);
-cudaError_t launch_rev_batch(const AdjStep* table, const int2* node_blocks, int n_node_blocks,
+cudaError_t launch_rev_batch(const AdjStep* table, const int4* tiles, int ntiles,
                              const int2* part_blocks, int n_part_blocks, cudaStream_t s);
 
 // *mismatch += number of i < n with a[i] != b[i] bitwise (4-byte words).

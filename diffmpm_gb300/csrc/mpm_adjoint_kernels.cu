@@ -25,7 +25,6 @@ namespace mpm {
 
 namespace {
 
-constexpr int NODE_THREADS = 256;
 constexpr int PART_THREADS = 256;
 
 // Particles currently in cell (ci, cj) at the step start, in the order of the
@@ -105,47 +104,63 @@ __device__ __forceinline__ void g2p_seeds(const AdjStep& A, int q, float& gx, fl
 }
 
 // ---------------------------------------------------------------------------
-// Pass 1: transposed G2P and reverse nodal update (element.py:305-329,
-// particle.py:208-247).
+// Tiles of the two node passes: the forward kernels' tiles (a CTA of
+// TILE_THREADS threads covers TILE_CX x TILE_CY cells and owns the nodes at
+// the upper-right corners of all but its first column and row), with each
+// thread summing the corner contributions of its cell's particles.  Fast
+// path: the cell rows are staged with coalesced copies (row_pass); slow path
+// (a particle near the tile was outside its sort-cell at the step start): the
+// tape's drift flags and visit_tape_cell.  Tiles with no stored particle in
+// reach only write their nodes (all sums zero).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void rev_nodal_update_at(const AdjStep& A, int n) {
-    const int nxn = A.nx + 1;
-    if (n >= nxn * (A.ny + 1)) return;
-    const int I = n % nxn, J = n / nxn;
-    float vbx = 0.0f, vby = 0.0f, abx = 0.0f, aby = 0.0f;
-    #pragma unroll 1
-    for (int c = 0; c < 4; ++c) {
-        const int ci = I - 1 + (c & 1), cj = J - 1 + (c >> 1);
-        if (ci < 0 || ci >= A.nx || cj < 0 || cj >= A.ny) continue;
-        const int k = corner_of(c);
-        const CellGeo g = cell_geo(ci, cj, A.hx, A.hy);
-        int cnt = 0;
-        visit_tape_cell(A, ci, cj, g, [&](int q) {
-            float N, Gx, Gy;
-            corner_shape(k, natural(A.x[q], g.cx, g.rx), natural(A.y[q], g.cy, g.ry), g.rx, g.ry,
-                         N, Gx, Gy);
-            float gx, gy, hx, hy;
-            g2p_seeds(A, q, gx, gy, hx, hy);
-            vbx = fa(vbx, fm(N, gx));
-            vby = fa(vby, fm(N, gy));
-            abx = fa(abx, fm(N, hx));
-            aby = fa(aby, fm(N, hy));
-            ++cnt;
-        });
-        if (c == 3) A.cnt[cj * A.nx + ci] = cnt;
+__device__ __forceinline__ bool rev_occupied(const AdjStep& A, int x0, int x1, int y0, int y1) {
+    x0 = max(x0, 0);
+    x1 = min(x1, A.nx);
+    y0 = max(y0, 0);
+    y1 = min(y1, A.ny);
+    int any = 0;
+    if (x0 < x1)
+        for (int r = y0 + (int)threadIdx.x; r < y1; r += blockDim.x)
+            any |= A.cstart[r * A.nx + x1] != A.cstart[r * A.nx + x0];
+    return __syncthreads_or(any) != 0;
+}
+
+__device__ __forceinline__ bool rev_drifted(const AdjStep& A, int c0x, int c0y) {
+    int any = 0;
+    for (int idx = threadIdx.x; idx < (TILE_CX + 2) * (TILE_CY + 2); idx += blockDim.x) {
+        const int si = c0x - 1 + idx % (TILE_CX + 2), sj = c0y - 1 + idx / (TILE_CX + 2);
+        if (si >= 0 && si < A.nx && sj >= 0 && sj < A.ny) any |= A.cflag[sj * A.nx + si];
     }
+    return __syncthreads_or(any) != 0;
+}
+
+// Storage starts of the 33 sort-cells c0x .. c0x+32 of row cj (clamped).
+__device__ __forceinline__ void rev_row_starts(const AdjStep& A, int c0x, int cj, int* cs,
+                                               int lane) {
+    if (cj < 0 || cj >= A.ny) {
+        cs[lane] = 0;
+        if (lane == 0) cs[32] = 0;
+        return;
+    }
+    const int base = cj * A.nx;
+    cs[lane] = A.cstart[base + min(max(c0x + lane, 0), A.nx)];
+    if (lane == 0) cs[32] = A.cstart[base + min(max(c0x + 32, 0), A.nx)];
+}
+
+// Reverse nodal update of node n from the G2P adjoint sums (vB-bar, aB-bar):
+// vB = flush(C(vA + a dt)), aB = flush(C0(a)), a = F / M (element.py:305-329).
+__device__ __forceinline__ void rev_node_update(const AdjStep& A, int n, float vbx, float vby,
+                                                float abx, float aby) {
     float fbx = 0.0f, fby = 0.0f, mb = 0.0f, wbx = 0.0f, wby = 0.0f;
     const float M = A.nm[n];
     if (M != 0.0f) {
         const uint16_t code = A.ncons[n];
         const bool cx = (code & 0xff) != 0, cy = (code >> 8) != 0;
         const float vBx = A.nvbx[n], vBy = A.nvby[n], aBx = A.nax[n], aBy = A.nay[n];
-        // vB = flush(C(vA + a dt)), aB = flush(C0(a))
         wbx = (cx || vBx == 0.0f) ? 0.0f : vbx;
         wby = (cy || vBy == 0.0f) ? 0.0f : vby;
         const float ax = fa((cx || aBx == 0.0f) ? 0.0f : abx, fm(wbx, A.dt));
         const float ay = fa((cy || aBy == 0.0f) ? 0.0f : aby, fm(wby, A.dt));
-        // a = F / M
         fbx = fdv(ax, M);
         fby = fdv(ay, M);
         mb = -fdv(fa(fm(ax, aBx), fm(ay, aBy)), M);
@@ -157,17 +172,89 @@ __device__ __forceinline__ void rev_nodal_update_at(const AdjStep& A, int n) {
     A.vaby[n] = wby;
 }
 
-__global__ void __launch_bounds__(NODE_THREADS)
-k_rev_nodal_update(const __grid_constant__ AdjStep A) {
-    rev_nodal_update_at(A, blockIdx.x * blockDim.x + threadIdx.x);
+// ---------------------------------------------------------------------------
+// Pass 1: transposed G2P (v-hat bar = x-bar dt [+ v-bar], a-hat bar = v-bar dt
+// gathered to the nodes with the shape functions), the reverse nodal update
+// and the particle count of every cell (particle.py:208-247, element.py:305-329).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void rev_nodal_update_tile(const AdjStep& A, const int4 T) {
+    constexpr int NQ = 16;   // [v-hat bar x, y, a-hat bar x, y] x corner
+    __shared__ float s_c[NQ][SC_STRIDE];
+    __shared__ float s_row[TILE_CY][6][ROW_P];
+    __shared__ int s_cs[TILE_CY][33];
+    const int tid = threadIdx.x, tx = tid % TILE_CX, ty = tid / TILE_CX;
+    const int c0x = T.y * TILE_NX - 1, c0y = T.z * TILE_NY - 1;
+    const int ci = c0x + tx, cj = c0y + ty;
+    const bool node_ok = tx < TILE_NX && ty < TILE_NY && c0x + 1 + tx <= A.nx && c0y + 1 + ty <= A.ny;
+    const int node = (c0y + 1 + ty) * (A.nx + 1) + c0x + 1 + tx;
+    const bool own_cell = tx >= 1 && ty >= 1 && ci < A.nx && cj < A.ny;
+    float sum[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    if (rev_occupied(A, c0x - 1, c0x + TILE_CX + 1, c0y - 1, c0y + TILE_CY + 1)) {
+        rev_row_starts(A, c0x, cj, s_cs[ty], tx);
+        const bool slow = rev_drifted(A, c0x, c0y);   // (also a block barrier)
+        const bool in_mesh = ci >= 0 && ci < A.nx && cj >= 0 && cj < A.ny;
+        const CellGeo g = cell_geo(ci, cj, A.hx, A.hy);
+        float acc[NQ];
+        #pragma unroll
+        for (int k = 0; k < NQ; ++k) acc[k] = 0.0f;
+        int cnt = 0;
+        auto add = [&](float x, float y, float lxv, float lyv, float lvx, float lvy) {
+            float N[4];
+            shape4(natural(x, g.cx, g.rx), natural(y, g.cy, g.ry), N);
+            float gx = fm(lxv, A.dt), gy = fm(lyv, A.dt), hx = 0.0f, hy = 0.0f;
+            if (A.velocity_update) {
+                gx = fa(gx, lvx);
+                gy = fa(gy, lvy);
+            } else {
+                hx = fm(lvx, A.dt);
+                hy = fm(lvy, A.dt);
+            }
+            #pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                acc[k] = fa(acc[k], fm(N[k], gx));
+                acc[4 + k] = fa(acc[4 + k], fm(N[k], gy));
+                acc[8 + k] = fa(acc[8 + k], fm(N[k], hx));
+                acc[12 + k] = fa(acc[12 + k], fm(N[k], hy));
+            }
+            ++cnt;
+        };
+        if (!slow) {
+            const int* cs = s_cs[ty];
+            const float* const src[6] = {A.x, A.y, A.lx, A.ly, A.lvx, A.lvy};
+            float (*buf)[ROW_P] = s_row[ty];
+            row_pass<6>(buf, src, cs[0], cs[32], cs[tx], cs[tx + 1], tx, [&](int, int j) {
+                add(buf[0][j], buf[1][j], buf[2][j], buf[3][j], buf[4][j], buf[5][j]);
+            });
+        } else if (in_mesh) {
+            visit_tape_cell(A, ci, cj, g, [&](int q) {
+                add(A.x[q], A.y[q], A.lx[q], A.ly[q], A.lvx[q], A.lvy[q]);
+            });
+        }
+        #pragma unroll
+        for (int k = 0; k < NQ; ++k) s_c[k][tid] = acc[k];
+        if (own_cell) A.cnt[cj * A.nx + ci] = cnt;
+        __syncthreads();
+        if (node_ok) {
+            #pragma unroll
+            for (int k = 0; k < 4; ++k) sum[k] = node_sum(s_c + 4 * k, tid);
+        }
+    } else if (own_cell) {
+        A.cnt[cj * A.nx + ci] = 0;
+    }
+    if (node_ok) rev_node_update(A, node, sum[0], sum[1], sum[2], sum[3]);
 }
 
-__global__ void __launch_bounds__(NODE_THREADS)
-k_rev_nodal_update_batch(const AdjStep* __restrict__ table, const int2* __restrict__ blocks) {
+__global__ void __launch_bounds__(TILE_THREADS, 2)
+k_rev_nodal_update(const __grid_constant__ AdjStep A, const int4* __restrict__ tiles) {
+    rev_nodal_update_tile(A, tiles[blockIdx.x]);
+}
+
+__global__ void __launch_bounds__(TILE_THREADS, 2)
+k_rev_nodal_update_batch(const AdjStep* __restrict__ table, const int4* __restrict__ tiles) {
     __shared__ AdjStep sA;
-    const int2 bm = blocks[blockIdx.x];
-    load_step_args(table + bm.x, sA);
-    rev_nodal_update_at(sA, bm.y * NODE_THREADS + threadIdx.x);
+    const int4 T = tiles[blockIdx.x];
+    load_step_args(table + T.x, sA);
+    rev_nodal_update_tile(sA, T);
 }
 
 // ---------------------------------------------------------------------------
@@ -325,38 +412,17 @@ k_rev_forces_batch(const AdjStep* __restrict__ table, const int2* __restrict__ b
 }
 
 // ---------------------------------------------------------------------------
-// Pass 3: transposed strain-rate gather and reverse nodal velocity
-// (element.py:191-202, 331-334; particle.py:281-313).
+// Pass 3: transposed strain-rate gather (vA-bar += sum over particles of
+// G r-bar + Gc c-bar) and the reverse nodal velocity vA = C(flush(P / M)),
+// P = flush(sum N m v) (element.py:191-202, 331-334; particle.py:281-313).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void rev_nodal_kinematics_at(const AdjStep& A, int n) {
-    const int nxn = A.nx + 1;
-    if (n >= nxn * (A.ny + 1)) return;
-    const int I = n % nxn, J = n / nxn;
-    float vbx = A.vabx[n], vby = A.vaby[n];
-    #pragma unroll 1
-    for (int c = 0; c < 4; ++c) {
-        const int ci = I - 1 + (c & 1), cj = J - 1 + (c >> 1);
-        if (ci < 0 || ci >= A.nx || cj < 0 || cj >= A.ny) continue;
-        const int k = corner_of(c);
-        const CellGeo g = cell_geo(ci, cj, A.hx, A.hy);
-        float Nc, Gcx, Gcy;
-        corner_shape(k, 0.0f, 0.0f, g.rx, g.ry, Nc, Gcx, Gcy);
-        visit_tape_cell(A, ci, cj, g, [&](int q) {
-            float N, Gx, Gy;
-            corner_shape(k, natural(A.x[q], g.cx, g.rx), natural(A.y[q], g.cy, g.ry), g.rx, g.ry,
-                         N, Gx, Gy);
-            const float r0b = A.r0b[q], r1b = A.r1b[q], r3b = A.r3b[q];
-            vbx = fa(vbx, fa(fa(fm(Gx, r0b), fm(Gy, r3b)), fm(Gcx, A.c0b[q])));
-            vby = fa(vby, fa(fa(fm(Gy, r1b), fm(Gx, r3b)), fm(Gcy, A.c1b[q])));
-        });
-    }
+__device__ __forceinline__ void rev_node_velocity(const AdjStep& A, int n, float vbx, float vby) {
     float qbx = 0.0f, qby = 0.0f, mbt = A.mb[n];
     const float M = A.nm[n];
     if (M != 0.0f) {
         const uint16_t code = A.ncons[n];
         const bool cx = (code & 0xff) != 0, cy = (code >> 8) != 0;
         const float vAx = A.nvax[n], vAy = A.nvay[n];
-        // vA = C(flush(P / M)), P = flush(sum N m v)
         const float ubx = (cx || vAx == 0.0f) ? 0.0f : vbx;
         const float uby = (cy || vAy == 0.0f) ? 0.0f : vby;
         qbx = fdv(ubx, M);
@@ -368,17 +434,70 @@ __device__ __forceinline__ void rev_nodal_kinematics_at(const AdjStep& A, int n)
     A.mbt[n] = mbt;
 }
 
-__global__ void __launch_bounds__(NODE_THREADS)
-k_rev_nodal_kinematics(const __grid_constant__ AdjStep A) {
-    rev_nodal_kinematics_at(A, blockIdx.x * blockDim.x + threadIdx.x);
+__device__ __forceinline__ void rev_nodal_kinematics_tile(const AdjStep& A, const int4 T) {
+    constexpr int NQ = 8;    // [vA-bar x, y] x corner
+    __shared__ float s_c[NQ][SC_STRIDE];
+    __shared__ float s_row[TILE_CY][7][ROW_P];
+    __shared__ int s_cs[TILE_CY][33];
+    const int tid = threadIdx.x, tx = tid % TILE_CX, ty = tid / TILE_CX;
+    const int c0x = T.y * TILE_NX - 1, c0y = T.z * TILE_NY - 1;
+    const int ci = c0x + tx, cj = c0y + ty;
+    const bool node_ok = tx < TILE_NX && ty < TILE_NY && c0x + 1 + tx <= A.nx && c0y + 1 + ty <= A.ny;
+    const int node = (c0y + 1 + ty) * (A.nx + 1) + c0x + 1 + tx;
+    float sx = 0.0f, sy = 0.0f;
+    if (rev_occupied(A, c0x - 1, c0x + TILE_CX + 1, c0y - 1, c0y + TILE_CY + 1)) {
+        rev_row_starts(A, c0x, cj, s_cs[ty], tx);
+        const bool slow = rev_drifted(A, c0x, c0y);   // (also a block barrier)
+        const bool in_mesh = ci >= 0 && ci < A.nx && cj >= 0 && cj < A.ny;
+        const CellGeo g = cell_geo(ci, cj, A.hx, A.hy);
+        float Gcx[4], Gcy[4];
+        dshape4(0.0f, 0.0f, g.rx, g.ry, Gcx, Gcy);
+        float acc[NQ];
+        #pragma unroll
+        for (int k = 0; k < NQ; ++k) acc[k] = 0.0f;
+        auto add = [&](float x, float y, float r0b, float r1b, float r3b, float c0b, float c1b) {
+            float Gx[4], Gy[4];
+            dshape4(natural(x, g.cx, g.rx), natural(y, g.cy, g.ry), g.rx, g.ry, Gx, Gy);
+            #pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                acc[k] = fa(acc[k], fa(fa(fm(Gx[k], r0b), fm(Gy[k], r3b)), fm(Gcx[k], c0b)));
+                acc[4 + k] = fa(acc[4 + k], fa(fa(fm(Gy[k], r1b), fm(Gx[k], r3b)), fm(Gcy[k], c1b)));
+            }
+        };
+        if (!slow) {
+            const int* cs = s_cs[ty];
+            const float* const src[7] = {A.x, A.y, A.r0b, A.r1b, A.r3b, A.c0b, A.c1b};
+            float (*buf)[ROW_P] = s_row[ty];
+            row_pass<7>(buf, src, cs[0], cs[32], cs[tx], cs[tx + 1], tx, [&](int, int j) {
+                add(buf[0][j], buf[1][j], buf[2][j], buf[3][j], buf[4][j], buf[5][j], buf[6][j]);
+            });
+        } else if (in_mesh) {
+            visit_tape_cell(A, ci, cj, g, [&](int q) {
+                add(A.x[q], A.y[q], A.r0b[q], A.r1b[q], A.r3b[q], A.c0b[q], A.c1b[q]);
+            });
+        }
+        #pragma unroll
+        for (int k = 0; k < NQ; ++k) s_c[k][tid] = acc[k];
+        __syncthreads();
+        if (node_ok) {
+            sx = node_sum(s_c + 0, tid);
+            sy = node_sum(s_c + 4, tid);
+        }
+    }
+    if (node_ok) rev_node_velocity(A, node, fa(A.vabx[node], sx), fa(A.vaby[node], sy));
 }
 
-__global__ void __launch_bounds__(NODE_THREADS)
-k_rev_nodal_kinematics_batch(const AdjStep* __restrict__ table, const int2* __restrict__ blocks) {
+__global__ void __launch_bounds__(TILE_THREADS, 2)
+k_rev_nodal_kinematics(const __grid_constant__ AdjStep A, const int4* __restrict__ tiles) {
+    rev_nodal_kinematics_tile(A, tiles[blockIdx.x]);
+}
+
+__global__ void __launch_bounds__(TILE_THREADS, 2)
+k_rev_nodal_kinematics_batch(const AdjStep* __restrict__ table, const int4* __restrict__ tiles) {
     __shared__ AdjStep sA;
-    const int2 bm = blocks[blockIdx.x];
-    load_step_args(table + bm.x, sA);
-    rev_nodal_kinematics_at(sA, bm.y * NODE_THREADS + threadIdx.x);
+    const int4 T = tiles[blockIdx.x];
+    load_step_args(table + T.x, sA);
+    rev_nodal_kinematics_tile(sA, T);
 }
 
 // ---------------------------------------------------------------------------
@@ -469,9 +588,9 @@ inline int blocks_for(int n, int t) { return (n + t - 1) / t; }
 
 }  // namespace
 
-cudaError_t launch_rev_nodal_update(const AdjStep& A, cudaStream_t s) {
-    const int nn = (A.nx + 1) * (A.ny + 1);
-    k_rev_nodal_update<<<blocks_for(nn, NODE_THREADS), NODE_THREADS, 0, s>>>(A);
+cudaError_t launch_rev_nodal_update(const AdjStep& A, const int4* tiles, int ntiles,
+                                    cudaStream_t s) {
+    if (ntiles > 0) k_rev_nodal_update<<<ntiles, TILE_THREADS, 0, s>>>(A, tiles);
     return cudaGetLastError();
 }
 
@@ -481,9 +600,9 @@ cudaError_t launch_rev_forces(const AdjStep& A, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_rev_nodal_kinematics(const AdjStep& A, cudaStream_t s) {
-    const int nn = (A.nx + 1) * (A.ny + 1);
-    k_rev_nodal_kinematics<<<blocks_for(nn, NODE_THREADS), NODE_THREADS, 0, s>>>(A);
+cudaError_t launch_rev_nodal_kinematics(const AdjStep& A, const int4* tiles, int ntiles,
+                                        cudaStream_t s) {
+    if (ntiles > 0) k_rev_nodal_kinematics<<<ntiles, TILE_THREADS, 0, s>>>(A, tiles);
     return cudaGetLastError();
 }
 
@@ -498,14 +617,12 @@ cudaError_t launch_adj_table(const AdjStep* bases, int n, int t, AdjStep* table,
     return cudaGetLastError();
 }
 
-cudaError_t launch_rev_batch(const AdjStep* table, const int2* node_blocks, int n_node_blocks,
+cudaError_t launch_rev_batch(const AdjStep* table, const int4* tiles, int ntiles,
                              const int2* part_blocks, int n_part_blocks, cudaStream_t s) {
-    if (n_node_blocks > 0)
-        k_rev_nodal_update_batch<<<n_node_blocks, NODE_THREADS, 0, s>>>(table, node_blocks);
+    if (ntiles > 0) k_rev_nodal_update_batch<<<ntiles, TILE_THREADS, 0, s>>>(table, tiles);
     if (n_part_blocks > 0)
         k_rev_forces_batch<<<n_part_blocks, PART_THREADS, 0, s>>>(table, part_blocks);
-    if (n_node_blocks > 0)
-        k_rev_nodal_kinematics_batch<<<n_node_blocks, NODE_THREADS, 0, s>>>(table, node_blocks);
+    if (ntiles > 0) k_rev_nodal_kinematics_batch<<<ntiles, TILE_THREADS, 0, s>>>(table, tiles);
     if (n_part_blocks > 0)
         k_rev_mass_momentum_batch<<<n_part_blocks, PART_THREADS, 0, s>>>(table, part_blocks);
     return cudaGetLastError();

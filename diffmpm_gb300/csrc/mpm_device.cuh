@@ -204,4 +204,49 @@ __device__ __forceinline__ float strain_stress_update(const MatDev& M, float Ep,
     return f;
 }
 
+// ---------------------------------------------------------------------------
+// Tile helpers shared by the forward and reverse kernels: a CTA of
+// TILE_THREADS threads covers TILE_CX x TILE_CY cells, thread tid = cell
+// (tid % TILE_CX, tid / TILE_CX), and owns the node at the upper-right corner
+// of its cell for lx < TILE_NX, ly < TILE_NY.
+// ---------------------------------------------------------------------------
+// Sum of the four cell-corner partials meeting at the node of thread `tid`
+// (node = lower-left corner of cell tid + 33): cell (I-1,J-1) corner 2,
+// cell (I,J-1) corner 3, cell (I-1,J) corner 1, cell (I,J) corner 0.
+constexpr int SC_STRIDE = TILE_THREADS + 1;   // per-quantity row of the cell-corner partials
+
+__device__ __forceinline__ float node_sum(const float (*s)[SC_STRIDE], int tid) {
+    return fa(fa(fa(s[2][tid], s[3][tid + 1]), s[1][tid + TILE_CX]), s[0][tid + TILE_CX + 1]);
+}
+
+// Fast path of the particle-to-grid gathers (forward and reverse): warp w
+// stages the particles stored in sort-cell row w of a tile (storage range [rb, re)) into shared
+// memory with coalesced cp.async copies, ROW_P particles per pass, and lane l
+// then visits the particles of its own cell (storage range [cb, ce)) in storage
+// order, summing their corner contributions in registers: the same order and
+// the same roundings as the slow path's visit_cell, so both paths give the
+// same bits.
+constexpr int ROW_P = 160;
+
+template <int NF, class F>
+__device__ __forceinline__ void row_pass(float (*buf)[ROW_P], const float* const (&src)[NF], int rb,
+                                         int re, int cb, int ce, int lane, F&& f) {
+    #pragma unroll 1
+    for (int p0 = rb; p0 < re; p0 += ROW_P) {
+        const int p1 = min(p0 + ROW_P, re);
+        for (int q = p0 + lane; q < p1; q += 32) {
+            #pragma unroll
+            for (int k = 0; k < NF; ++k)
+                if (src[k]) cp_async4(&buf[k][q - p0], src[k] + q);
+        }
+        cp_async_commit();
+        cp_async_wait<0>();
+        __syncwarp();
+        const int lo = max(cb, p0), hi = min(ce, p1);
+        #pragma unroll 1
+        for (int q = lo; q < hi; ++q) f(q, q - p0);
+        __syncwarp();
+    }
+}
+
 }  // namespace mpm

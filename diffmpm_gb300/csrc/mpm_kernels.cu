@@ -78,15 +78,6 @@ __device__ __forceinline__ void cell_nodes(const SimDev& S, int ci, int cj, int 
     ids[3] = ll + S.nx + 1;
 }
 
-// Sum of the four cell-corner partials meeting at the node of thread `tid`
-// (node = lower-left corner of cell tid + 33): cell (I-1,J-1) corner 2,
-// cell (I,J-1) corner 3, cell (I-1,J) corner 1, cell (I,J) corner 0.
-constexpr int SC_STRIDE = TILE_THREADS + 1;   // per-quantity row of the cell-corner partials
-
-__device__ __forceinline__ float node_sum(const float (*s)[SC_STRIDE], int tid) {
-    return fa(fa(fa(s[2][tid], s[3][tid + 1]), s[1][tid + TILE_CX]), s[0][tid + TILE_CX + 1]);
-}
-
 __device__ __forceinline__ void apply_constraint(const SimDev& S, uint16_t code, float& vx,
                                                  float& vy, float* ax, float* ay) {
     const int c0 = code & 0xff, c1 = code >> 8;
@@ -388,36 +379,6 @@ __device__ __forceinline__ void force_contrib(const SimDev& S, int q, const Forc
         c[4 + k] = fa(fm(nV, fy), fm(N[k], mgy));
     }
     add_traction<TRAC>(S, q, t, V, REINIT ? size0 : (S.psize ? S.psize[q] : 1.0f), N, c, c + 4);
-}
-
-// Fast path of the two particle-to-grid phases: warp w stages the particles
-// stored in sort-cell row w of the tile (storage range [rb, re)) into shared
-// memory with coalesced cp.async copies, ROW_P particles per pass, and lane l
-// then visits the particles of its own cell (storage range [cb, ce)) in storage
-// order, summing their corner contributions in registers: the same order and
-// the same roundings as the slow path's visit_cell, so both paths give the
-// same bits.
-constexpr int ROW_P = 160;
-
-template <int NF, class F>
-__device__ __forceinline__ void row_pass(float (*buf)[ROW_P], const float* const (&src)[NF], int rb,
-                                         int re, int cb, int ce, int lane, F&& f) {
-    #pragma unroll 1
-    for (int p0 = rb; p0 < re; p0 += ROW_P) {
-        const int p1 = min(p0 + ROW_P, re);
-        for (int q = p0 + lane; q < p1; q += 32) {
-            #pragma unroll
-            for (int k = 0; k < NF; ++k)
-                if (src[k]) cp_async4(&buf[k][q - p0], src[k] + q);
-        }
-        cp_async_commit();
-        cp_async_wait<0>();
-        __syncwarp();
-        const int lo = max(cb, p0), hi = min(ce, p1);
-        #pragma unroll 1
-        for (int q = lo; q < hi; ++q) f(q, q - p0);
-        __syncwarp();
-    }
 }
 
 // ---------------------------------------------------------------------------
