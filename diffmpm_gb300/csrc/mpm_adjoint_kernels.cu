@@ -274,58 +274,84 @@ __device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q) {
     dshape4(0.0f, 0.0f, g.rx, g.ry, Gcx, Gcy);
     const int ll = cj * (A.nx + 1) + ci;
     const int ids[4] = {ll, ll + 1, ll + A.nx + 2, ll + A.nx + 1};
-    float vAx[4], vAy[4], vBx[4], vBy[4], aBx[4], aBy[4], fbx[4], fby[4];
-    #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        vAx[k] = A.nvax[ids[k]];
-        vAy[k] = A.nvay[ids[k]];
-        vBx[k] = A.nvbx[ids[k]];
-        vBy[k] = A.nvby[ids[k]];
-        aBx[k] = A.nax[ids[k]];
-        aBy[k] = A.nay[ids[k]];
-        fbx[k] = A.fbx[ids[k]];
-        fby[k] = A.fby[ids[k]];
-    }
     const int cnt = A.cnt[cj * A.nx + ci];
     const float V0 = cnt ? fdv(A.vol_el, (float)cnt) : 0.0f;
     const float rho0 = A.rho[q];
     const float m = fm(V0, rho0);
 
-    // forward recomputation of the stress update
+    // forward recomputation of the strain rates (the left-to-right sums of
+    // strain_rate4) and of the stress update; sAx, sAy: sum of +-vA (signs
+    // + - + - of d Gx_k / d eta and d Gy_k / d xi)
+    float r0 = 0.0f, r1 = 0.0f, r3a = 0.0f, r3b_ = 0.0f, c0 = 0.0f, c1 = 0.0f;
+    float sAx = 0.0f, sAy = 0.0f;
+    #pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float vax = A.nvax[ids[k]], vay = A.nvay[ids[k]];
+        if (k == 0) {
+            r0 = fm(Gx[0], vax);
+            r1 = fm(Gy[0], vay);
+            r3a = fm(Gx[0], vay);
+            r3b_ = fm(Gy[0], vax);
+            c0 = fm(Gcx[0], vax);
+            c1 = fm(Gcy[0], vay);
+            sAx = vax;
+            sAy = vay;
+        } else {
+            r0 = fa(r0, fm(Gx[k], vax));
+            r1 = fa(r1, fm(Gy[k], vay));
+            r3a = fa(r3a, fm(Gx[k], vay));
+            r3b_ = fa(r3b_, fm(Gy[k], vax));
+            c0 = fa(c0, fm(Gcx[k], vax));
+            c1 = fa(c1, fm(Gcy[k], vay));
+            sAx = (k & 1) ? fs(sAx, vax) : fa(sAx, vax);
+            sAy = (k & 1) ? fs(sAy, vay) : fa(sAy, vay);
+        }
+    }
+    r0 = flush(r0);
+    r1 = flush(r1);
+    const float r3 = flush(fa(r3a, r3b_));
+    c0 = flush(c0);
+    c1 = flush(c1);
     PState p{};
     p.sxx = A.sxx[q];
     p.syy = A.syy[q];
     p.szz = A.szz[q];
     p.sxy = A.sxy[q];
     p.rho = rho0;
-    float r0, r1, r3, c0, c1, c3;
-    strain_rate4(Gx, Gy, vAx, vAy, r0, r1, r3);
-    strain_rate4(Gcx, Gcy, vAx, vAy, c0, c1, c3);
     const float dvol = fm(A.dt, fa(c0, c1));
     const MatDev& mat = A.mats[A.mat[q]];
     const float Ep = A.E ? A.E[q] : -1.0f;
     const float f = strain_stress_update(mat, Ep, A.dt, r0, r1, r3, dvol, p);
     const float V = fm(V0, f);
 
-    // G2P (x' = x + dt v-hat, v' from v-hat or a-hat): shape-function adjoints
+    // G2P, external and internal forces: adjoints of the shape functions (as
+    // x-bar, y-bar contributions), of m and V, of the end-of-step stress, and
+    // the signed sums of the gradient adjoints
     float gx, gy, hx, hy;
     g2p_seeds(A, q, gx, gy, hx, hy);
-    float Nb[4], Gxb[4], Gyb[4];
-    float mb = 0.0f, Vb = 0.0f, fsxx = 0.0f, fsyy = 0.0f, fsxy = 0.0f;
+    float xb = A.lx[q], yb = A.ly[q];
+    float mb = 0.0f, Vb = 0.0f, fsxx = 0.0f, fsyy = 0.0f, fsxy = 0.0f, sgx = 0.0f, sgy = 0.0f;
     #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        const float fg = fa(fm(fbx[k], A.gx), fm(fby[k], A.gy));   // F-bar . g
-        Nb[k] = fa(fa(fa(fm(gx, vBx[k]), fm(gy, vBy[k])), fa(fm(hx, aBx[k]), fm(hy, aBy[k]))),
-                   fm(m, fg));
+        const int n = ids[k];
+        const float fbx = A.fbx[n], fby = A.fby[n];
+        const float fg = fa(fm(fbx, A.gx), fm(fby, A.gy));   // F-bar . g
+        const float Nb = fa(fa(fa(fm(gx, A.nvbx[n]), fm(gy, A.nvby[n])),
+                               fa(fm(hx, A.nax[n]), fm(hy, A.nay[n]))),
+                            fm(m, fg));
         mb = fa(mb, fm(N[k], fg));
         const float fx = fa(fm(Gx[k], p.sxx), fm(Gy[k], p.sxy));
         const float fy = fa(fm(Gy[k], p.syy), fm(Gx[k], p.sxy));
-        Vb = fs(Vb, fa(fm(fbx[k], fx), fm(fby[k], fy)));
-        fsxx = fa(fsxx, fm(fbx[k], Gx[k]));
-        fsyy = fa(fsyy, fm(fby[k], Gy[k]));
-        fsxy = fa(fsxy, fa(fm(fbx[k], Gy[k]), fm(fby[k], Gx[k])));
-        Gxb[k] = -fm(V, fa(fm(fbx[k], p.sxx), fm(fby[k], p.sxy)));
-        Gyb[k] = -fm(V, fa(fm(fbx[k], p.sxy), fm(fby[k], p.syy)));
+        Vb = fs(Vb, fa(fm(fbx, fx), fm(fby, fy)));
+        fsxx = fa(fsxx, fm(fbx, Gx[k]));
+        fsyy = fa(fsyy, fm(fby, Gy[k]));
+        fsxy = fa(fsxy, fa(fm(fbx, Gy[k]), fm(fby, Gx[k])));
+        const float gxk = -fm(V, fa(fm(fbx, p.sxx), fm(fby, p.sxy)));
+        const float gyk = -fm(V, fa(fm(fbx, p.sxy), fm(fby, p.syy)));
+        sgx = (k & 1) ? fs(sgx, gxk) : fa(sgx, gxk);
+        sgy = (k & 1) ? fs(sgy, gyk) : fa(sgy, gyk);
+        xb = fa(xb, fm(Nb, Gx[k]));
+        yb = fa(yb, fm(Nb, Gy[k]));
     }
     // stress adjoint at the end of the forces: loss/next-step part + force part
     const float sbxx = fs(A.lsxx[q], fm(V, fsxx));
@@ -366,22 +392,13 @@ __device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q) {
     const float c0b = c0 != 0.0f ? fm(fb, A.dt) : 0.0f;
     const float c1b = c1 != 0.0f ? fm(fb, A.dt) : 0.0f;
 
-    // strain-rate part of the gradient adjoints
-    float xb = A.lx[q], yb = A.ly[q];
-    float gyb = 0.0f, gxb = 0.0f;
-    #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const float gxk = fa(Gxb[k], fa(fm(r0b, vAx[k]), fm(r3b, vAy[k])));
-        const float gyk = fa(Gyb[k], fa(fm(r1b, vAy[k]), fm(r3b, vAx[k])));
-        const float sgn = (k & 1) ? -1.0f : 1.0f;   // d Gx_k / d eta, d Gy_k / d xi: + - + -
-        gxb = fa(gxb, fm(sgn, gxk));
-        gyb = fa(gyb, fm(sgn, gyk));
-        xb = fa(xb, fm(Nb[k], Gx[k]));
-        yb = fa(yb, fm(Nb[k], Gy[k]));
-    }
+    // strain-rate part of the gradient adjoints: Gx_k-bar += r0b vAx_k + r3b
+    // vAy_k, Gy_k-bar += r1b vAy_k + r3b vAx_k; their signed sums move x, y
+    sgx = fa(sgx, fa(fm(r0b, sAx), fm(r3b, sAy)));
+    sgy = fa(sgy, fa(fm(r1b, sAy), fm(r3b, sAx)));
     const float rxy = fm(fm(0.25f, g.rx), g.ry);
-    xb = fa(xb, fm(rxy, gyb));
-    yb = fa(yb, fm(rxy, gxb));
+    xb = fa(xb, fm(rxy, sgy));
+    yb = fa(yb, fm(rxy, sgx));
 
     A.lx[q] = xb;
     A.ly[q] = yb;
@@ -398,12 +415,12 @@ __device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q) {
     A.c1b[q] = c1b;
 }
 
-__global__ void __launch_bounds__(PART_THREADS)
+__global__ void __launch_bounds__(PART_THREADS, 4)
 k_rev_forces(const __grid_constant__ AdjStep A) {
     rev_forces_at(A, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
-__global__ void __launch_bounds__(PART_THREADS)
+__global__ void __launch_bounds__(PART_THREADS, 4)
 k_rev_forces_batch(const AdjStep* __restrict__ table, const int2* __restrict__ blocks) {
     __shared__ AdjStep sA;
     const int2 bm = blocks[blockIdx.x];
