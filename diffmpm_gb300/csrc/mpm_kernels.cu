@@ -544,7 +544,7 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
     __shared__ unsigned char s_cell[TILE_CY][K2_ROW_P];   // their cell within the row
     __shared__ float s_cellv[TILE_CY][3][32];          // V0, size0, dvol per cell
     __shared__ int s_cs[TILE_CY][33];
-    __shared__ float s_vx[NV_W * NV_H], s_vy[NV_W * NV_H];
+    __shared__ float2 s_v[NV_W * NV_H];   // nodal velocity after phase 1 of the tile's nodes
     __shared__ TileGeo G;
     const int step = load_step(ctl);
     const int parity = step & 1;
@@ -574,8 +574,7 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
             vx = S.nvax[n];
             vy = S.nvay[n];
         }
-        s_vx[idx] = vx;
-        s_vy[idx] = vy;
+        s_v[idx] = make_float2(vx, vy);
     }
     const bool slow = tile_drifted(S, c0x, c0y);   // (also a block barrier)
 
@@ -584,8 +583,9 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
         const int id[4] = {a, a + 1, a + NV_W + 1, a + NV_W};
         #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            vx[k] = s_vx[id[k]];
-            vy[k] = s_vy[id[k]];
+            const float2 v = s_v[id[k]];
+            vx[k] = v.x;
+            vy[k] = v.y;
         }
     };
 
@@ -657,7 +657,7 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
     __syncthreads();
     if (node_ok) {
         const int a = (ly + 1) * NV_W + lx + 1;   // node (I, J) in the node tile
-        nodal_update(S, node, t, node_sum(s_c + 0, tid), node_sum(s_c + 4, tid), s_vx[a], s_vy[a],
+        nodal_update(S, node, t, node_sum(s_c + 0, tid), node_sum(s_c + 4, tid), s_v[a].x, s_v[a].y,
                      nmass, ncons);
     }
 }
@@ -691,6 +691,7 @@ k_forces_batch(const SimDev* const* __restrict__ sims, Control* const* __restric
 // ---------------------------------------------------------------------------
 constexpr int G_W = TILE_CX + 2;   // node tile [c0x, c0x+34) x [c0y, c0y+18)
 constexpr int G_H = TILE_CY + 2;
+constexpr int G2P_MAP = 160;        // particles of a row whose sort-cell is looked up in a map
 
 // New cell along one axis for a coordinate that was in table column k (cell
 // c = base + k): same, or a neighbour by one, decided against the tabulated
@@ -716,9 +717,10 @@ template <bool USL, bool REINIT>
 __device__ __forceinline__ void particle_kinematics_tile(const SimDev& S, const int4 T,
                                                          Control* __restrict__ ctl) {
     constexpr int NF = G2PStage<USL>::NF, DEPTH = G2PStage<USL>::DEPTH;
-    __shared__ float s_vx[G_W * G_H], s_vy[G_W * G_H], s_ax[G_W * G_H], s_ay[G_W * G_H];
+    __shared__ float4 s_nd[G_W * G_H];    // nodal (vx, vy, ax, ay) of the tile's nodes
     __shared__ float s_stage[TILE_CY][DEPTH][NF][32];
     __shared__ int s_cs[TILE_CY][33];
+    __shared__ unsigned char s_map[TILE_CY][G2P_MAP];   // sort-cell of the row's first particles
     __shared__ int s_sf[TILE_CY][32];     // drift flag of the sort-cell at the start of the step
     __shared__ int s_flag[TILE_CY][32];   // drift flag after this step
     __shared__ int s_status;
@@ -774,12 +776,14 @@ __device__ __forceinline__ void particle_kinematics_tile(const SimDev& S, const 
             ax = S.nax[n];
             ay = S.nay[n];
         }
-        s_vx[idx] = vx;
-        s_vy[idx] = vy;
-        s_ax[idx] = ax;
-        s_ay[idx] = ay;
+        s_nd[idx] = make_float4(vx, vy, ax, ay);
     }
     if (occupied) build_geo(S, c0x, c0y, G);
+    if (row_ok && lane < TILE_NX) {
+        // storage index rb + j of the row holds a particle of sort-cell s_map[j]
+        const int lo = s_cs[w][lane] - rb, hi = min(s_cs[w][lane + 1] - rb, G2P_MAP);
+        for (int j = lo; j < hi; ++j) s_map[w][j] = (unsigned char)lane;
+    }
     __syncthreads();
     int status = 0;
     const int* cs = s_cs[w];
@@ -788,7 +792,7 @@ __device__ __forceinline__ void particle_kinematics_tile(const SimDev& S, const 
         const float (*b)[32] = st.advance(c);
         const int q = rb + 32 * c + lane;
         if (q >= re) continue;
-        const int l = cell_of(cs, 30, q);   // sort-cell c0x + 1 + l
+        const int l = q - rb < G2P_MAP ? s_map[w][q - rb] : cell_of(cs, 30, q);   // sort-cell c0x + 1 + l
         const int si = c0x + 1 + l;
         const float x = b[GF_X][lane], y = b[GF_Y][lane];
         int ci = si, cj = sj;
@@ -811,10 +815,11 @@ __device__ __forceinline__ void particle_kinematics_tile(const SimDev& S, const 
             const int id[4] = {a, a + 1, a + G_W + 1, a + G_W};
             #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                nvx[k] = s_vx[id[k]];
-                nvy[k] = s_vy[id[k]];
-                nax[k] = s_ax[id[k]];
-                nay[k] = s_ay[id[k]];
+                const float4 v = s_nd[id[k]];
+                nvx[k] = v.x;
+                nvy[k] = v.y;
+                nax[k] = v.z;
+                nay[k] = v.w;
             }
         } else {
             int ids[4];
