@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--no-plain-path", action="store_true",
                     help="skip timing each simulation alone (the ratio's denominator)")
     ap.add_argument("--phase-steps", type=int, default=20)
+    ap.add_argument("--diff-steps", type=int, default=2000,
+                    help="steps of the differentiation workload (0 skips it)")
     return ap.parse_args()
 
 
@@ -292,6 +294,65 @@ def plain_scaleup(args, D, workloads, torch):
     return out, roof
 
 
+def differentiation(args, D, workloads, torch):
+    """The differentiation workload: 256^2 mesh, 125,664 particles with a
+    seeded log-normal E field, 2000 USF steps; loss = mean |x_end - x_target|^2
+    against a forward run from another seeded field; gradient w.r.t. the
+    per-particle E through the checkpointed adjoint (checkpoints every 100)."""
+    K = args.diff_steps
+    ts, tg, _ = workloads.differentiation(D, sim_steps=K, seed=202)
+    tsim = ts.simulation(tg, reinit=True)
+    ts._upload(tsim)
+    tsim.initialize()
+    tsim.step(K)
+    target = tsim.read("loc")
+    tsim.close()
+    solver, g, info = workloads.differentiation(D, sim_steps=K, seed=101)
+    sim = solver.simulation(g, reinit=True)
+    n = info["np"]
+
+    def reset():
+        solver._upload(sim)
+        sim.initialize()
+
+    def seed():
+        x = sim.read("loc")
+        d = x.astype(np.float64) - target
+        return (2.0 / n * d).astype(np.float32), float((d * d).sum(1).mean())
+
+    ckpt = min(args.checkpoint_steps, K)
+    reset()
+    sim.record(K, ckpt)
+    sim.adjoint(seed()[0], want=("youngs_modulus",))
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    reset()
+    torch.cuda.synchronize()
+    e[0].record()
+    sim.record(K, ckpt)
+    e[1].record()
+    torch.cuda.synchronize()
+    sd, loss = seed()
+    e[2].record()
+    gr = sim.adjoint(sd, want=("youngs_modulus",))["youngs_modulus"]
+    e[3].record()
+    torch.cuda.synchronize()
+    rec_ms, adj_ms = e[0].elapsed_time(e[1]), e[2].elapsed_time(e[3])
+    reset()
+    torch.cuda.synchronize()
+    e[0].record()
+    sim.step(K)
+    e[1].record()
+    torch.cuda.synchronize()
+    fwd_ms = e[0].elapsed_time(e[1])
+    sim.close()
+    ps = n * K
+    return {"workload": "differentiation", "mesh": "256x256", "particles": n, "steps": K,
+            "checkpoint_steps": ckpt, "loss": loss,
+            "dLdE_norm": float(np.linalg.norm(gr.astype(np.float64))),
+            "fwd_adjoint": ps / ((rec_ms + adj_ms) / 1000.0), "fwd": ps / (fwd_ms / 1000.0),
+            "record_ms": rec_ms, "adjoint_ms": adj_ms, "fwd_ms": fwd_ms}
+
+
 def run_ours(args, world, rank, local):
     import torch
     torch.cuda.set_device(local)
@@ -404,6 +465,7 @@ def run_ours(args, world, rank, local):
     del members, sims
 
     plain, roof = plain_scaleup(args, D, workloads, torch)
+    diff = differentiation(args, D, workloads, torch) if args.diff_steps > 0 else None
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -450,6 +512,7 @@ def run_ours(args, world, rank, local):
             "gpu_launches": launches,
             "roofline": roof,
             "plain_scaleup": plain,
+            "differentiation": diff,
             "clocks": clk,
             "counters": counters,
             "cpu_baseline": cpu,

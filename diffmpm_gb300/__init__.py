@@ -11,6 +11,7 @@ from .forces import NodalForce, ParticleTraction
 from .functions import Linear, Unit
 from .material import LinearElastic, Newtonian, SimpleMaterial
 from .mesh import Mesh1D, Mesh2D
+from .mpm import MPM
 from .node import Nodes
 from .particle import Particles
 from .solver import MPMExplicit
@@ -19,6 +20,6 @@ from ._lib import MpmError, OutOfMeshError
 __all__ = [
     "Batch", "Constraint", "Linear1D", "Quadrilateral4Node", "Simulation", "NodalForce",
     "ParticleTraction", "Linear", "Unit", "LinearElastic", "Newtonian", "SimpleMaterial",
-    "Mesh1D", "Mesh2D", "Nodes", "Particles", "MPMExplicit", "MpmError", "OutOfMeshError",
+    "Mesh1D", "Mesh2D", "MPM", "Nodes", "Particles", "MPMExplicit", "MpmError", "OutOfMeshError",
 ]
 __version__ = "0.1.0"

@@ -153,9 +153,10 @@ int resort(MpmHandle* h, cudaStream_t s) {
     int* start = h->cstart[h->cs_cur ^ 1];
     CK(h, launch_exclusive_scan(w.count, start, nb, w.block_sums, s));
     CK(h, launch_resort_place(np, start, w, s));
-    CK(h, launch_resort_segsort(nb, start, w, s));
     PSet& src = h->ps[h->pcur];
     PSet& dst = h->ps[h->pcur ^ 1];
+    if (h->ndim == 1) CK(h, launch_line_segsort(nb, start, w.perm, src.pid, s));
+    else CK(h, launch_resort_segsort(nb, start, w, s));
     std::vector<float**> a = movable_f32(h, src, false), b = movable_f32(h, dst, false);
     for (size_t i = 0; i < a.size(); ++i)
         CK(h, launch_gather_u32(reinterpret_cast<const uint32_t*>(*a[i]),
@@ -170,6 +171,7 @@ int resort(MpmHandle* h, cudaStream_t s) {
     h->pcur ^= 1;
     h->cs_cur ^= 1;
     CK(h, cudaMemsetAsync(h->cflag, 0, h->ncell, s));
+    if (h->ndim == 1) CK(h, launch_line_eid(start, h->nx, h->line_eid, s));
     bind_particles(h);
     drop_graphs(h);   // the step graphs hold the descriptor by value
     CK(h, cudaMemcpyAsync(h->ds, &h->hs, sizeof(SimDev), cudaMemcpyHostToDevice, s));
@@ -263,10 +265,12 @@ int alloc_particles(MpmHandle* h, int64_t n) {
                          &p.rho[0], &p.rho[1], &p.vsc[0], &p.vsc[1]};
         for (float** f : f32) TRY(dalloc(h, f, n));
         if (!h->reinit) {
-            TRY(dalloc(h, &p.vol[0], n));
-            TRY(dalloc(h, &p.vol[1], n));
             TRY(dalloc(h, &p.mass, n));
             TRY(dalloc(h, &p.psize, n));
+        }
+        if (!h->reinit || h->ndim == 1) {   // 1-D keeps the updated volume for its forces kernel
+            TRY(dalloc(h, &p.vol[0], n));
+            TRY(dalloc(h, &p.vol[1], n));
         }
         TRY(dalloc(h, &p.mat, n));
         TRY(dalloc(h, &p.pid, n));
@@ -274,6 +278,7 @@ int alloc_particles(MpmHandle* h, int64_t n) {
     TRY(dalloc(h, &h->passive, 5 * n));
     TRY(dalloc(h, &h->sw.key, n));
     TRY(dalloc(h, &h->sw.perm, n));
+    if (h->ndim == 1) TRY(dalloc(h, &h->line_eid, n));
     const size_t nsnap = movable_f32(h, h->ps[0], true).size();
     h->snap_f.assign(nsnap, nullptr);
     for (size_t i = 0; i < nsnap; ++i) TRY(dalloc(h, &h->snap_f[i], n));
@@ -295,6 +300,8 @@ void free_particles(MpmHandle* h) {
     dfree(h, h->sw.key);
     dfree(h, h->sw.perm);
     h->sw.key = h->sw.perm = nullptr;
+    dfree(h, h->line_eid);
+    h->line_eid = nullptr;
     for (float* f : h->snap_f) dfree(h, f);
     h->snap_f.clear();
     h->np = -1;
@@ -344,8 +351,8 @@ std::vector<float*> comps(MpmHandle* h, int field) {
     PSet& p = h->ps[h->pcur];
     const int par = parity(h);
     switch (field) {
-        case MPM_FIELD_LOC: return {p.x, p.y};
-        case MPM_FIELD_VELOCITY: return {p.vx, p.vy};
+        case MPM_FIELD_LOC: return h->ndim == 1 ? std::vector<float*>{p.x} : std::vector<float*>{p.x, p.y};
+        case MPM_FIELD_VELOCITY: return h->ndim == 1 ? std::vector<float*>{p.vx} : std::vector<float*>{p.vx, p.vy};
         case MPM_FIELD_STRESS: return {p.sxx[par], p.syy[par], p.szz[par], p.sxy[par], nullptr, nullptr};
         case MPM_FIELD_STRAIN: return {p.exx, p.eyy, nullptr, p.exy, nullptr, nullptr};
         case MPM_FIELD_DENSITY: return {p.rho[par]};
@@ -423,13 +430,15 @@ const char* mpm_last_error(const MpmHandle* h) {
 int mpm_create(const MpmDesc* d, MpmHandle** out) {
     if (!d || !out) return fail(nullptr, MPM_ERR_INVALID, "null argument");
     *out = nullptr;
-    if (d->ndim != 2)
-        return fail(nullptr, MPM_ERR_UNSUPPORTED, "ndim=%d: this build implements Quadrilateral4Node (ndim=2)", d->ndim);
-    if (d->nelements[0] < 1 || d->nelements[1] < 1)
+    if (d->ndim != 1 && d->ndim != 2)
+        return fail(nullptr, MPM_ERR_UNSUPPORTED, "ndim=%d: Linear1D (1) and Quadrilateral4Node (2) only", d->ndim);
+    const bool line = d->ndim == 1;
+    if (d->nelements[0] < 1 || (!line && d->nelements[1] < 1))
         return fail(nullptr, MPM_ERR_INVALID, "nelements must be positive");
-    const int64_t nn64 = (int64_t)(d->nelements[0] + 1) * (d->nelements[1] + 1);
+    const int64_t nn64 = line ? (int64_t)d->nelements[0] + 1
+                              : (int64_t)(d->nelements[0] + 1) * (d->nelements[1] + 1);
     if (nn64 > (int64_t)1 << 30) return fail(nullptr, MPM_ERR_INVALID, "mesh too large");
-    if (!(d->el_len[0] > 0) || !(d->el_len[1] > 0))
+    if (!(d->el_len[0] > 0) || (!line && !(d->el_len[1] > 0)))
         return fail(nullptr, MPM_ERR_INVALID, "element lengths must be positive");
     if (d->scheme != MPM_USF && d->scheme != MPM_USL)
         return fail(nullptr, MPM_ERR_INVALID, "Please select scheme from ('usf', 'usl'). Found %d", d->scheme);
@@ -438,11 +447,12 @@ int mpm_create(const MpmDesc* d, MpmHandle** out) {
 
     MpmHandle* h = new MpmHandle();
     cudaGetDevice(&h->device);
-    h->ndim = 2;
+    // a 1-D mesh sorts its particles as one row of cells (y = 0, hy = 1)
+    h->ndim = d->ndim;
     h->nx = d->nelements[0];
-    h->ny = d->nelements[1];
+    h->ny = line ? 1 : d->nelements[1];
     h->hx = (float)d->el_len[0];
-    h->hy = (float)d->el_len[1];
+    h->hy = line ? 1.0f : (float)d->el_len[1];
     h->dt = (float)d->dt;
     h->gx = (float)d->gravity[0];
     h->gy = (float)d->gravity[1];
@@ -499,6 +509,7 @@ int mpm_create(const MpmDesc* d, MpmHandle** out) {
         const int n = d->constraint_node[i], dir = d->constraint_dir[i];
         if (n < 0 || n >= h->nn) return failc(MPM_ERR_INVALID, "constraint node id out of range");
         if (dir != 0 && dir != 1) return failc(MPM_ERR_INVALID, "constraint dir must be 0 or 1");
+        if (line && dir != 0) return failc(MPM_ERR_INVALID, "constraint dir must be 0 in 1-D");
         const float v = (float)d->constraint_velocity[i];
         int slot = -1;
         for (size_t k = 0; k < vel.size(); ++k)
@@ -535,8 +546,9 @@ int mpm_create(const MpmDesc* d, MpmHandle** out) {
         for (int i = 0; i < d->n_nodal_forces; ++i) {
             const int n = d->nodal_force_node[i];
             if (n < 0 || n >= h->nn) return failc(MPM_ERR_INVALID, "nodal force node id out of range");
-            if (d->nodal_force_dir[i] != 0 && d->nodal_force_dir[i] != 1)
-                return failc(MPM_ERR_INVALID, "nodal force dir must be 0 or 1");
+            if (d->nodal_force_dir[i] != 0 && d->nodal_force_dir[i] != (line ? 0 : 1))
+                return failc(MPM_ERR_INVALID, line ? "nodal force dir must be 0 in 1-D"
+                                                   : "nodal force dir must be 0 or 1");
             const int f = d->nodal_force_function[i];
             if (f < -1 || f >= d->n_functions) return failc(MPM_ERR_INVALID, "nodal force function out of range");
             cnf_ptr[n + 1]++;
@@ -659,6 +671,8 @@ int mpm_destroy(MpmHandle* h) {
     segbuf_free(h->segbuf);
     drop_graphs(h);
     if (h->cap) cudaStreamDestroy(h->cap);
+    for (cudaEvent_t& e : h->out_ev)
+        if (e) cudaEventDestroy(e);
     for (void* p : h->allocs) cudaFree(p);
     h->allocs.clear();
     if (h->h_ctl) cudaFreeHost(h->h_ctl);
@@ -712,7 +726,7 @@ int mpm_set_particles(MpmHandle* h, int64_t n, const float* loc, const int32_t* 
     }
     CK(h, cudaMemcpy(p.mat, m8.data(), n, cudaMemcpyHostToDevice));
     for (int k = 0; k < 2; ++k) CK(h, cudaMemcpy(p.rho[k], dens.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
-    float* zero[] = {p.vx, p.vy, p.sxx[0], p.sxx[1], p.syy[0], p.syy[1], p.szz[0], p.szz[1],
+    float* zero[] = {p.y, p.vx, p.vy, p.sxx[0], p.sxx[1], p.syy[0], p.syy[1], p.szz[0], p.szz[1],
                      p.sxy[0], p.sxy[1], p.exx, p.eyy, p.exy, p.vsc[0], p.vsc[1]};
     for (float* z : zero) CK(h, cudaMemset(z, 0, sizeof(float) * n));
     CK(h, cudaMemset(h->passive, 0, sizeof(float) * 5 * n));
@@ -769,21 +783,15 @@ int mpm_write_field(MpmHandle* h, int field, const void* src, int on_device, voi
     return sync(h, s);
 }
 
-int mpm_read_field(MpmHandle* h, int field, void* dst, int on_device, void* stream) {
-    if (!h) return MPM_ERR_INVALID;
-    if (h->np < 0) return fail(h, MPM_ERR_STATE, "set particles first");
-    if (h->np == 0) return MPM_OK;
-    if (!dst) return fail(h, MPM_ERR_INVALID, "null destination");
-    cudaStream_t s = S(stream);
+}  // extern "C"
+
+namespace {
+
+// Particle field `field` in original order into the device buffer `d`.
+int gather_field(MpmHandle* h, int field, void* d, cudaStream_t s) {
     const int64_t n = h->np;
     PSet& p = h->ps[h->pcur];
     const int nc = ncomp_of(h, field);
-    const size_t bytes = sizeof(float) * nc * n;
-    void* d = on_device ? dst : nullptr;
-    if (!on_device) {
-        TRY(ensure_stage(h, bytes));
-        d = h->stage;
-    }
     const bool derived = field == MPM_FIELD_ELEMENT_ID || field == MPM_FIELD_MOMENTUM ||
                          ((field == MPM_FIELD_VOLUME || field == MPM_FIELD_MASS) && h->reinit);
     if (derived) {
@@ -793,7 +801,7 @@ int mpm_read_field(MpmHandle* h, int field, void* dst, int on_device, void* stre
         int what = field == MPM_FIELD_ELEMENT_ID ? 0 : field == MPM_FIELD_VOLUME ? 1 : field == MPM_FIELD_MASS ? 2 : 3;
         if (!h->initialized && (what == 1 || what == 2))
             return fail(h, MPM_ERR_STATE, "initialize first");
-        CK(h, launch_derived_out(h->ds, (int)n, parity(h), h->reinit, what, h->ps[h->pcur].pid, d, s));
+        CK(h, launch_derived_out(h->ds, h->ndim, (int)n, parity(h), h->reinit, what, h->ps[h->pcur].pid, d, s));
     } else if (field == MPM_FIELD_MATERIAL_ID) {
         CK(h, launch_scatter_out_u8(p.mat, p.pid, (int)n, static_cast<int32_t*>(d), s));
     } else {
@@ -805,8 +813,93 @@ int mpm_read_field(MpmHandle* h, int field, void* dst, int on_device, void* stre
         if (field == MPM_FIELD_STRESS || field == MPM_FIELD_STRAIN)
             TRY(copy_passive(h, field, static_cast<float*>(d), true, s));
     }
+    return MPM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mpm_read_field(MpmHandle* h, int field, void* dst, int on_device, void* stream) {
+    if (!h) return MPM_ERR_INVALID;
+    if (h->np < 0) return fail(h, MPM_ERR_STATE, "set particles first");
+    if (h->np == 0) return MPM_OK;
+    if (!dst) return fail(h, MPM_ERR_INVALID, "null destination");
+    if (field < 0 || field >= MPM_FIELD_COUNT) return fail(h, MPM_ERR_INVALID, "unknown field %d", field);
+    cudaStream_t s = S(stream);
+    const size_t bytes = sizeof(float) * ncomp_of(h, field) * h->np;
+    void* d = on_device ? dst : nullptr;
+    if (!on_device) {
+        TRY(ensure_stage(h, bytes));
+        d = h->stage;
+    }
+    TRY(gather_field(h, field, d, s));
     if (!on_device) CK(h, cudaMemcpyAsync(dst, d, bytes, cudaMemcpyDeviceToHost, s));
     return sync(h, s);
+}
+
+int mpm_output_enqueue(MpmHandle* h, int nfields, const int* fields, void* host_dst, void* stream,
+                       int64_t* ticket) {
+    if (!h) return MPM_ERR_INVALID;
+    if (h->np < 0) return fail(h, MPM_ERR_STATE, "set particles first");
+    if (nfields < 1 || !fields || !host_dst || !ticket)
+        return fail(h, MPM_ERR_INVALID, "need at least one field, a destination and a ticket");
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, host_dst) != cudaSuccess || at.type != cudaMemoryTypeHost) {
+        cudaGetLastError();
+        return fail(h, MPM_ERR_INVALID, "host_dst must be pinned host memory (mpm_host_alloc)");
+    }
+    cudaStream_t s = S(stream);
+    size_t total = 0;
+    for (int k = 0; k < nfields; ++k) {
+        if (fields[k] < 0 || fields[k] >= MPM_FIELD_COUNT)
+            return fail(h, MPM_ERR_INVALID, "unknown field %d", fields[k]);
+        total += sizeof(float) * ncomp_of(h, fields[k]) * h->np;
+    }
+    if (h->out_stage_bytes < total) {
+        CK(h, cudaStreamSynchronize(s));      // copies from the old buffer are done
+        dfree(h, h->out_stage);
+        h->out_stage = nullptr;
+        h->out_stage_bytes = 0;
+        TRY(dalloc(h, reinterpret_cast<char**>(&h->out_stage), total));
+        h->out_stage_bytes = total;
+    }
+    const int slot = (int)(h->out_tickets % MpmHandle::OUT_SLOTS);
+    if (!h->out_ev[slot]) CK(h, cudaEventCreateWithFlags(&h->out_ev[slot], cudaEventDisableTiming));
+    size_t off = 0;
+    for (int k = 0; k < nfields; ++k) {
+        if (h->np > 0) TRY(gather_field(h, fields[k], static_cast<char*>(h->out_stage) + off, s));
+        off += sizeof(float) * ncomp_of(h, fields[k]) * h->np;
+    }
+    if (total) CK(h, cudaMemcpyAsync(host_dst, h->out_stage, total, cudaMemcpyDeviceToHost, s));
+    CK(h, cudaEventRecord(h->out_ev[slot], s));
+    *ticket = h->out_tickets++;
+    return MPM_OK;
+}
+
+int mpm_output_wait(MpmHandle* h, int64_t ticket) {
+    if (!h) return MPM_ERR_INVALID;
+    if (ticket < 0 || ticket >= h->out_tickets || ticket < h->out_tickets - MpmHandle::OUT_SLOTS)
+        return MPM_ERR_INVALID;
+    cudaEvent_t e = h->out_ev[ticket % MpmHandle::OUT_SLOTS];
+    return cudaEventSynchronize(e) == cudaSuccess ? MPM_OK : MPM_ERR_CUDA;
+}
+
+int mpm_host_alloc(size_t bytes, void** p) {
+    if (!p) return MPM_ERR_INVALID;
+    *p = nullptr;
+    if (bytes == 0) return MPM_OK;
+    if (cudaHostAlloc(p, bytes, cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return MPM_ERR_CUDA;
+    }
+    return MPM_OK;
+}
+
+int mpm_host_free(void* p) {
+    if (!p) return MPM_OK;
+    return cudaFreeHost(p) == cudaSuccess ? MPM_OK : MPM_ERR_CUDA;
 }
 
 int mpm_set_tractions(MpmHandle* h, int n, const int64_t* pid, const int32_t* dir,
@@ -814,6 +907,7 @@ int mpm_set_tractions(MpmHandle* h, int n, const int64_t* pid, const int32_t* di
     if (!h) return MPM_ERR_INVALID;
     h->gen++;
     if (h->np < 0) return fail(h, MPM_ERR_STATE, "set particles first");
+    if (h->ndim == 1 && n > 0) return fail(h, MPM_ERR_UNSUPPORTED, "particle tractions are not available in 1-D");
     const int64_t np = h->np;
     cudaStream_t s = S(stream);
     if (n <= 0) {
@@ -861,7 +955,8 @@ int mpm_set_tractions(MpmHandle* h, int n, const int64_t* pid, const int32_t* di
 int mpm_read_nodal_field(MpmHandle* h, int field, float* dst, int on_device, void* stream) {
     if (!h || !dst) return MPM_ERR_INVALID;
     cudaStream_t s = S(stream);
-    const int nc = field == MPM_NODE_MASS ? 1 : 2;
+    const bool line = h->ndim == 1;
+    const int nc = field == MPM_NODE_MASS || line ? 1 : 2;
     const size_t bytes = sizeof(float) * nc * h->nn;
     float* d = dst;
     if (!on_device) {
@@ -869,9 +964,12 @@ int mpm_read_nodal_field(MpmHandle* h, int field, float* dst, int on_device, voi
         d = static_cast<float*>(h->stage);
     }
     if (field == MPM_NODE_MASS) CK(h, cudaMemcpyAsync(d, h->nm, bytes, cudaMemcpyDeviceToDevice, s));
+    else if (field == MPM_NODE_VELOCITY && line) CK(h, cudaMemcpyAsync(d, h->nvbx, bytes, cudaMemcpyDeviceToDevice, s));
+    else if (field == MPM_NODE_ACCELERATION && line) CK(h, cudaMemcpyAsync(d, h->nax, bytes, cudaMemcpyDeviceToDevice, s));
     else if (field == MPM_NODE_VELOCITY) CK(h, launch_interleave2(h->nvbx, h->nvby, h->nn, d, s));
     else if (field == MPM_NODE_ACCELERATION) CK(h, launch_interleave2(h->nax, h->nay, h->nn, d, s));
-    else if (field == MPM_NODE_MOMENTUM) CK(h, launch_node_momentum(h->nm, h->nvbx, h->nvby, h->nn, d, s));
+    else if (field == MPM_NODE_MOMENTUM)
+        CK(h, launch_node_momentum(h->nm, h->nvbx, line ? nullptr : h->nvby, h->nn, d, s));
     else return fail(h, MPM_ERR_INVALID, "unknown nodal field %d", field);
     if (!on_device) CK(h, cudaMemcpyAsync(dst, d, bytes, cudaMemcpyDeviceToHost, s));
     return sync(h, s);
@@ -881,11 +979,16 @@ int mpm_write_nodal_field(MpmHandle* h, int field, const float* src, int on_devi
     if (!h || !src) return MPM_ERR_INVALID;
     h->gen++;
     cudaStream_t s = S(stream);
-    const int nc = field == MPM_NODE_MASS ? 1 : 2;
+    const bool line = h->ndim == 1;
+    const int nc = field == MPM_NODE_MASS || line ? 1 : 2;
     const void* d = nullptr;
     TRY(to_device(h, src, sizeof(float) * nc * h->nn, on_device, s, &d));
     const float* df = static_cast<const float*>(d);
     if (field == MPM_NODE_MASS) CK(h, cudaMemcpyAsync(h->nm, df, sizeof(float) * h->nn, cudaMemcpyDeviceToDevice, s));
+    else if (field == MPM_NODE_VELOCITY && line)
+        CK(h, cudaMemcpyAsync(h->nvbx, df, sizeof(float) * h->nn, cudaMemcpyDeviceToDevice, s));
+    else if (field == MPM_NODE_ACCELERATION && line)
+        CK(h, cudaMemcpyAsync(h->nax, df, sizeof(float) * h->nn, cudaMemcpyDeviceToDevice, s));
     else if (field == MPM_NODE_VELOCITY) CK(h, launch_deinterleave2(df, h->nn, h->nvbx, h->nvby, s));
     else if (field == MPM_NODE_ACCELERATION) CK(h, launch_deinterleave2(df, h->nn, h->nax, h->nay, s));
     else return fail(h, MPM_ERR_INVALID, "nodal field %d is not writable", field);
@@ -899,7 +1002,10 @@ int mpm_initialize(MpmHandle* h, void* stream) {
     cudaStream_t s = S(stream);
     TRY(clear_status(h, s));
     TRY(resort(h, s));
-    if (!h->reinit && h->np > 0) CK(h, launch_setup_volume(h->ds, (int)h->np, parity(h), s));
+    if (!h->reinit && h->np > 0) {
+        if (h->ndim == 1) TRY(line_setup_volume(h, s));
+        else CK(h, launch_setup_volume(h->ds, (int)h->np, parity(h), s));
+    }
     TRY(read_ctl(h, s));
     int st = 0;
     TRY(check_status(h, st));
@@ -912,6 +1018,7 @@ int mpm_run_phase(MpmHandle* h, int phase, void* stream) {
     h->gen++;
     if (!h->initialized) return fail(h, MPM_ERR_STATE, "initialize first");
     if (phase < 0 || phase > 2) return fail(h, MPM_ERR_INVALID, "phase must be 0, 1 or 2");
+    if (h->ndim == 1) return fail(h, MPM_ERR_UNSUPPORTED, "single phases are not available in 1-D");
     cudaStream_t s = S(stream);
     if (phase == 0 && h->needs_resort) TRY(resort(h, s));
     TRY(launch_phase(h, phase, s));
@@ -942,6 +1049,14 @@ int mpm_step(MpmHandle* h, int nsteps, void* stream) {
         return MPM_OK;
     }
     cudaStream_t s = S(stream);
+    if (h->ndim == 1) {   // Linear1D: re-sorted every step, status checked at the end
+        for (int t = 0; t < nsteps; ++t) TRY(line_step(h, s));
+        TRY(read_ctl(h, s));
+        int st = h->h_ctl->status;
+        TRY(check_status(h, st));
+        TRY(clear_status(h, s));
+        return sync(h, s);
+    }
     while (nsteps > 0) {
         const int B = nsteps < h->block_steps ? nsteps : h->block_steps;
         if (h->needs_resort) TRY(resort(h, s));
@@ -996,6 +1111,7 @@ int mpm_time_phases(MpmHandle* h, int nsteps, float* ms_out, void* stream) {
     if (!h || !ms_out || nsteps < 1) return MPM_ERR_INVALID;
     h->gen++;
     if (!h->initialized) return fail(h, MPM_ERR_STATE, "initialize first");
+    if (h->ndim == 1) return fail(h, MPM_ERR_UNSUPPORTED, "phase timing is not available in 1-D");
     cudaStream_t s = S(stream);
     if (h->needs_resort) TRY(resort(h, s));
     std::vector<cudaEvent_t> ev((size_t)3 * nsteps + 1);

@@ -411,6 +411,7 @@ int emit_all(MpmHandle* h, AdjointState* a, float* dl_dE, float* dl_dloc0, float
 }
 
 int check_supported(MpmHandle* h) {
+    if (h->ndim != 2) return fail(h, MPM_ERR_UNSUPPORTED, "the adjoint implements Quadrilateral4Node meshes");
     if (h->usl) return fail(h, MPM_ERR_UNSUPPORTED, "the adjoint implements the USF scheme");
     if (!h->reinit)
         return fail(h, MPM_ERR_UNSUPPORTED,

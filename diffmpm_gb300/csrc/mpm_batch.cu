@@ -176,6 +176,8 @@ int mpm_batch_create(MpmHandle* const* sims, int n, MpmBatch** out) {
         if (!seen.insert(h).second) return bfail(nullptr, MPM_ERR_INVALID, "simulation %d appears twice", i);
         if (!h->initialized || h->np <= 0)
             return bfail(nullptr, MPM_ERR_STATE, "simulation %d is not initialised with particles", i);
+        if (h->ndim != 2)
+            return bfail(nullptr, MPM_ERR_UNSUPPORTED, "batches hold Quadrilateral4Node simulations");
         if (h->device != sims[0]->device)
             return bfail(nullptr, MPM_ERR_INVALID, "simulations are on different devices");
         if (h->usl != sims[0]->usl || h->reinit != sims[0]->reinit || h->has_trac != sims[0]->has_trac)

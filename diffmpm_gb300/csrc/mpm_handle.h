@@ -109,6 +109,14 @@ struct MpmHandle {
     void* stage = nullptr;
     size_t stage_bytes = 0;
     float** d_ptrs = nullptr;
+    int* line_eid = nullptr;         // 1-D: element of each storage slot this step
+    // asynchronous output (mpm_output_enqueue): its own staging buffer and a
+    // ring of events, one per outstanding copy
+    static constexpr int OUT_SLOTS = 8;
+    void* out_stage = nullptr;
+    size_t out_stage_bytes = 0;
+    cudaEvent_t out_ev[OUT_SLOTS] = {};
+    int64_t out_tickets = 0;
     // graphs
     cudaStream_t cap = nullptr;
     std::map<int, cudaGraphExec_t> graphs;
@@ -175,6 +183,8 @@ int launch_steps(MpmHandle* h, int n, cudaStream_t s);
 int check_status(MpmHandle* h, int& st);
 int take_snapshot(MpmHandle* h, cudaStream_t s);
 int replay_block(MpmHandle* h, int64_t step0, int B, int& st, cudaStream_t s);
+int line_step(MpmHandle* h, cudaStream_t s);            // mpm_line.cu
+int line_setup_volume(MpmHandle* h, cudaStream_t s);
 int to_device(MpmHandle* h, const void* src, size_t bytes, int on_device, cudaStream_t s,
               const void** dsrc);
 

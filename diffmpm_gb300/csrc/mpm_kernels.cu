@@ -1328,8 +1328,8 @@ cudaError_t launch_scatter_out_u8(const uint8_t* src, const int* pid, int np, in
     return cudaGetLastError();
 }
 
-// what: 0 element id (int32), 1 volume, 2 mass, 3 momentum (2 comps)
-__global__ void k_derived_out(const SimDev* __restrict__ sim, int np, int parity, int reinit,
+// what: 0 element id (int32), 1 volume, 2 mass, 3 momentum (ndim comps)
+__global__ void k_derived_out(const SimDev* __restrict__ sim, int ndim, int np, int parity, int reinit,
                               int what, const int* __restrict__ pid, void* __restrict__ out) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     const SimDev& S = *sim;
@@ -1345,7 +1345,9 @@ __global__ void k_derived_out(const SimDev* __restrict__ sim, int np, int parity
             const int c = j * S.nx + i;
             cnt = S.cstart[c + 1] - S.cstart[c];
         }
-        V = cnt ? fdv(S.vol_el, (float)cnt) : 0.0f;
+        // element volume: the 2-D formula, or the element length in 1-D
+        const float vel = ndim == 1 ? fs(node_coord(i + 1, S.hx), node_coord(i, S.hx)) : S.vol_el;
+        V = cnt ? fdv(vel, (float)cnt) : 0.0f;
         m = fm(V, S.rho[parity][q]);
     } else {
         V = S.vol[parity][q];
@@ -1357,16 +1359,18 @@ __global__ void k_derived_out(const SimDev* __restrict__ sim, int np, int parity
         static_cast<float*>(out)[o] = V;
     } else if (what == 2) {
         static_cast<float*>(out)[o] = m;
+    } else if (ndim == 1) {
+        static_cast<float*>(out)[o] = fm(m, S.vx[q]);
     } else {
         static_cast<float*>(out)[2 * (size_t)o] = fm(m, S.vx[q]);
         static_cast<float*>(out)[2 * (size_t)o + 1] = fm(m, S.vy[q]);
     }
 }
 
-cudaError_t launch_derived_out(const SimDev* sim, int np, int parity, bool reinit, int what,
+cudaError_t launch_derived_out(const SimDev* sim, int ndim, int np, int parity, bool reinit, int what,
                                const int* pid, void* out, cudaStream_t s) {
     if (np > 0)
-        k_derived_out<<<(np + 255) / 256, 256, 0, s>>>(sim, np, parity, reinit ? 1 : 0, what, pid, out);
+        k_derived_out<<<(np + 255) / 256, 256, 0, s>>>(sim, ndim, np, parity, reinit ? 1 : 0, what, pid, out);
     return cudaGetLastError();
 }
 
@@ -1389,7 +1393,9 @@ __global__ void k_deinterleave2(const float* __restrict__ in, int n, float* __re
 __global__ void k_node_momentum(const float* __restrict__ m, const float* __restrict__ vx,
                                 const float* __restrict__ vy, int n, float* __restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) {
+    if (i < n && !vy) {
+        out[i] = fm(m[i], vx[i]);   // 1-D
+    } else if (i < n) {
         out[2 * i] = fm(m[i], vx[i]);
         out[2 * i + 1] = fm(m[i], vy[i]);
     }

@@ -77,7 +77,10 @@ cudaError_t launch_scatter_out_u8(const uint8_t* src, const int* pid, int np, in
 
 // Derived per-particle outputs in original order: element id, volume, mass
 // (solve_jit semantics: the volume set-up at the current positions), momentum.
-cudaError_t launch_derived_out(const SimDev* sim, int np, int parity, bool reinit, int what,
+// 1-D (mpm_line.cu): buckets ordered by original index; element per storage slot
+cudaError_t launch_line_segsort(int nbucket, const int* start, int* perm, const int* pid, cudaStream_t s);
+cudaError_t launch_line_eid(const int* cstart, int nx, int* eid, cudaStream_t s);
+cudaError_t launch_derived_out(const SimDev* sim, int ndim, int np, int parity, bool reinit, int what,
                                const int* pid, void* out, cudaStream_t s);
 
 // Interleave / de-interleave nodal vectors.

@@ -57,9 +57,11 @@ class Quadrilateral4Node(_Element):
 
 
 class Linear1D(_Element):
-    """1-D two-node line elements (diffmpm/element.py:343-600).  The GPU path of
-    this build implements Quadrilateral4Node; a solve with Linear1D raises
-    ``MpmError(MPM_ERR_UNSUPPORTED)``."""
+    """1-D two-node line elements (diffmpm/element.py:343-600), nodes at
+    float(i) * el_len.  The GPU step (csrc/mpm_line.cu) takes the element
+    volume as its length and the strain rate as [dN/dx . v, 0, 0, 0, 0, 0],
+    where the reference's own 1-D code does not run as written
+    (element.py:543-546, particle.py:304-305)."""
 
     ndim = 1
 

@@ -45,6 +45,30 @@ def _in_arg(a, dtype, count):
     return _lib.ptr(arr), 0, arr
 
 
+class PinnedBuffer:
+    """Page-locked host memory from the library (mpm_host_alloc), the
+    destination of :meth:`Simulation.output_enqueue`."""
+
+    def __init__(self, nbytes: int):
+        self._lib = _lib.load()
+        p = C.c_void_p()
+        _lib.check(self._lib.mpm_host_alloc(int(nbytes), C.byref(p)))
+        self.ptr, self.nbytes = p, int(nbytes)
+        self.view = (C.c_char * max(self.nbytes, 1)).from_address(p.value) if p.value else bytearray(1)
+
+    def close(self):
+        if self.ptr is not None and self.ptr.value:
+            self.view = None
+            self._lib.mpm_host_free(self.ptr)
+        self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Simulation:
     """One explicit-MPM simulation on the current CUDA device.
 
@@ -67,7 +91,7 @@ class Simulation:
         el = np.broadcast_to(np.asarray(el_len, dtype=np.float64).reshape(-1), (2,))
         self.ndim = ndim
         self.nelements = (int(nel[0]), int(nel[1]) if nel.size > 1 else 1)
-        self.nnodes = (self.nelements[0] + 1) * (self.nelements[1] + 1)
+        self.nnodes = (self.nelements[0] + 1) * ((self.nelements[1] + 1) if ndim == 2 else 1)
         self.functions = [f for f in functions if isinstance(f, Linear)]
         self._fn_index = {id(f): k for k, f in enumerate(self.functions)}
         g = np.broadcast_to(np.asarray(gravity, dtype=np.float64).reshape(-1), (2,))
@@ -190,6 +214,36 @@ class Simulation:
         self._ok(self._lib.mpm_read_field(self._h, _lib.FIELD[field], p, dev, _stream_for(out)))
         return out
 
+    def output_enqueue(self, fields, buffer: "PinnedBuffer", stream=None) -> int:
+        """Enqueue the copy of ``fields`` (names, original order, laid out one
+        after the other as :meth:`read` returns them) into ``buffer`` and
+        return a ticket for :meth:`output_wait`; does not wait."""
+        codes = (C.c_int * len(fields))(*[_lib.FIELD[f] for f in fields])
+        need = sum(4 * self.n * self.ncomp(f) for f in fields)
+        if buffer.nbytes < need:
+            raise ValueError(f"buffer holds {buffer.nbytes} bytes, the fields need {need}")
+        t = C.c_int64()
+        self._ok(self._lib.mpm_output_enqueue(self._h, len(fields), codes, buffer.ptr, stream,
+                                              C.byref(t)))
+        return t.value
+
+    def output_wait(self, ticket: int):
+        """Block until the copy of ``ticket`` is in host memory (callable from
+        another thread while this one steps)."""
+        self._ok(self._lib.mpm_output_wait(self._h, int(ticket)))
+
+    def output_views(self, fields, buffer: "PinnedBuffer"):
+        """NumPy views of ``fields`` inside ``buffer`` (layout of
+        :meth:`output_enqueue`)."""
+        out, off = {}, 0
+        for f in fields:
+            nc = self.ncomp(f)
+            dt = np.int32 if f in _INT_FIELDS else np.float32
+            a = np.frombuffer(buffer.view, dtype=dt, count=self.n * nc, offset=off)
+            out[f] = a.reshape((self.n, nc) if nc > 1 else (self.n,))
+            off += 4 * self.n * nc
+        return out
+
     def set_tractions(self, pids, dirs, values, functions):
         """Particle tractions: entry k adds f_k(t) * values[k] * V / size in
         direction dirs[k] of particle pids[k] (diffmpm/particle.py:329-343)."""
@@ -202,7 +256,7 @@ class Simulation:
                                              _lib.ptr(vals), _lib.ptr(fns), None))
 
     def read_nodal(self, field, out=None):
-        nc = 1 if field == "mass" else 2
+        nc = 1 if field == "mass" else self.ndim
         if out is None:
             out = np.empty((self.nnodes, nc) if nc > 1 else (self.nnodes,), dtype=np.float32)
         dev = 1 if _is_cuda_tensor(out) else 0
@@ -211,7 +265,7 @@ class Simulation:
         return out
 
     def write_nodal(self, field, values):
-        nc = 1 if field == "mass" else 2
+        nc = 1 if field == "mass" else self.ndim
         p, dev, keep = _in_arg(values, np.float32, self.nnodes * nc)
         self._ok(self._lib.mpm_write_nodal_field(self._h, _lib.NODAL_FIELD[field], p, dev, _stream_for(values)))
 

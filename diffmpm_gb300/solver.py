@@ -21,6 +21,7 @@ from collections import defaultdict
 import numpy as np
 
 from .engine import Simulation
+from .writers import AsyncOutput
 from .functions import Linear
 
 _schemes = ("usf", "usl")
@@ -133,24 +134,31 @@ class MPMExplicit:
             p.element_ids = e[sl].copy()
             p.volume = vol[sl].reshape(-1, 1, 1).copy()
             p.mass = mass[sl].reshape(-1, 1, 1).copy()
-            p.size = np.broadcast_to(np.sqrt(p.volume), p.loc.shape).astype(np.float32).copy()
+            size = np.sqrt(p.volume) if ndim == 2 else p.volume
+            p.size = np.broadcast_to(size, p.loc.shape).astype(np.float32).copy()
         self.mesh.elements.volume[:] = self._element_volume()
 
     def _element_volume(self):
         """Element volume by the reference's formula (element.py:903-909), the
-        value the library uses."""
+        value the library uses; in 1-D the element length x_{e+1} - x_e."""
         el = self.mesh.elements
+        if getattr(el, "ndim", 2) == 1:
+            x = el.nodes.loc.reshape(-1)
+            return (x[1:] - x[:-1]).reshape(-1, 1, 1)
         a = c = np.float32(el.el_len[1])
         b = d = np.float32(el.el_len[0])
         p = q = np.sqrt(a * a + b * b)
         t = a * a + c * c - b * b - d * d
         return np.float32(0.25) * np.sqrt(np.float32(4) * p * p * q * q - t * t)
 
-    def _arrays(self, sim: Simulation, squeeze_each=True):
+    def _arrays(self, sim: Simulation, squeeze_each=True, read=None):
+        """The reference's output dict: per field, the sets' arrays stacked
+        (solver.py:190-197, 214-222); ``read`` supplies the fields already
+        read (original order), else they are read from ``sim``."""
         sets, _, _, offsets = self._population()
         out = {}
         for name in self.__particle_props:
-            a = sim.read(name)
+            a = sim.read(name) if read is None else read[name]
             per = []
             for k, p in enumerate(sets):
                 v = a[offsets[k]:offsets[k + 1]]
@@ -167,12 +175,21 @@ class MPMExplicit:
         sim.initialize()
         done = 0
         if self.writer_func is not None:
-            for i in range(0, self.sim_steps, self.out_steps):
-                sim.step(i + 1 - done)
-                done = i + 1
-                self.writer_func((self._arrays(sim), i), None, out_dir=self.out_dir,
-                                 max_steps=self.sim_steps)
-        sim.step(self.sim_steps - done)
+            # the output of step i is copied to pinned host memory behind the
+            # next steps and written by a host thread (writers.AsyncOutput)
+            out = AsyncOutput(sim, self.__particle_props,
+                              lambda read: self._arrays(sim, read=read), self.writer_func,
+                              out_dir=self.out_dir, max_steps=self.sim_steps)
+            try:
+                for i in range(0, self.sim_steps, self.out_steps):
+                    sim.step(i + 1 - done)
+                    done = i + 1
+                    out.submit(i)
+                sim.step(self.sim_steps - done)
+            finally:
+                out.close()
+        else:
+            sim.step(self.sim_steps)
         return {k: v.squeeze() for k, v in self._arrays(sim, squeeze_each=False).items()}
 
     def solve(self, gravity) -> dict:

@@ -26,6 +26,7 @@
 #ifndef DIFFMPM_GB300_H
 #define DIFFMPM_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -113,7 +114,8 @@ typedef enum MpmField {
     MPM_FIELD_MATERIAL_ID = 8,    /* int32 (n) */
     MPM_FIELD_YOUNGS_MODULUS = 9, /* float (n) per-particle E (LinearElastic), write enables it */
     MPM_FIELD_ELEMENT_ID = 10,    /* int32 (n), read only */
-    MPM_FIELD_MOMENTUM = 11       /* float (n, ndim), read only: mass * velocity */
+    MPM_FIELD_MOMENTUM = 11,      /* float (n, ndim), read only: mass * velocity */
+    MPM_FIELD_COUNT = 12
 } MpmField;
 
 /* Nodal fields (mpm_read_nodal_field / mpm_write_nodal_field). */
@@ -158,6 +160,22 @@ int mpm_write_field(MpmHandle* h, int field, const void* src, int on_device, voi
 /* Read one particle field in original particle order.  Replaces the output
  * assembly of MPMExplicit.solve_jit (diffmpm/solver.py:214-222). */
 int mpm_read_field(MpmHandle* h, int field, void* dst, int on_device, void* stream);
+
+/* Asynchronous output: enqueue on `stream` the copy of `nfields` particle
+ * fields (original order, each as mpm_read_field lays it out, one after the
+ * other) into the pinned host buffer `host_dst`, and return at once with a
+ * ticket; mpm_output_wait(ticket) blocks until that copy is in host memory
+ * and may be called from another host thread while this one keeps stepping.
+ * At most 8 copies may be outstanding.  Replaces the host callback that
+ * writes the outputs of solve_jit every out_steps steps
+ * (diffmpm/solver.py:187-210, writers.py:30-54). */
+int mpm_output_enqueue(MpmHandle* h, int nfields, const int* fields, void* host_dst, void* stream,
+                       int64_t* ticket);
+int mpm_output_wait(MpmHandle* h, int64_t ticket);
+
+/* Pinned host memory for mpm_output_enqueue. */
+int mpm_host_alloc(size_t bytes, void** p);
+int mpm_host_free(void* p);
 
 /* Particle tractions (diffmpm/forces.py:26-41, mesh.py:60-77): `n` entries
  * (particle id, dir, traction, function: -1 Unit, k table k).  Replaces any

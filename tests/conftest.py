@@ -41,3 +41,16 @@ def built():
     import __graft_entry__
     __graft_entry__.build()
     return True
+
+
+def pytest_terminal_summary(terminalreporter):
+    """Print the float64 error table collected by test_gpu_fp64_error."""
+    mod = sys.modules.get("test_gpu_fp64_error")
+    rows = getattr(mod, "TABLE", None) if mod else None
+    if not rows:
+        return
+    tr = terminalreporter
+    tr.section("error against float64 (GPU | float32 oracle)")
+    for row in rows:
+        cells = [f"{k} {v[0]:.2e} | {v[1]:.2e}" for k, v in row.items() if k != "config"]
+        tr.write_line(f"{row['config']}: " + "; ".join(cells))

@@ -1,0 +1,30 @@
+"""1-D (Linear1D) cases built with either API -- the oracle or the product."""
+import numpy as np
+
+
+def bar(api, nx=40, ppe=3, scheme="usf", velocity_update=False, sim_steps=50, dt=2e-4,
+        material="linear", gravity=-9.81, seed=4, **kw):
+    """A bar of ``nx`` elements on [0, 1], ``ppe`` particles per element over
+    the middle 80 % of the elements with seeded jitter, node 0 fixed, a
+    sinusoidal initial velocity, gravity along the bar and a concentrated
+    force ramp at the free end."""
+    h = 1.0 / nx
+    rng = np.random.Generator(np.random.PCG64(seed))
+    e0, e1 = int(0.1 * nx), int(0.9 * nx)
+    off = (np.arange(ppe) + 0.5) / ppe
+    x = ((np.arange(e0, e1)[:, None] + off[None, :]) * h).reshape(-1)
+    x = x + rng.uniform(-0.1, 0.1, x.size) * h / ppe
+    if material == "linear":
+        mat = api.LinearElastic({"density": 1000.0, "youngs_modulus": 1e6, "poisson_ratio": 0.3})
+    else:
+        mat = api.SimpleMaterial({"density": 1000.0, "E": 1e6})
+    fn = api.Linear(0, np.array([0.0, sim_steps * dt]), np.array([0.0, 1.0]))
+    cnf = [api.NodalForce(node_ids=np.array([nx]), function=fn, dir=0, force=2.0)]
+    cons = [(np.array([0]), api.Constraint(0, 0.0))]
+    el = api.Linear1D(nx, nx, h, cons, concentrated_nodal_forces=cnf, **kw)
+    ps = api.Particles(x.reshape(-1, 1, 1), mat, np.zeros(x.size, dtype=np.int32), **kw)
+    ps.velocity[:] = (0.05 * np.sin(np.pi * x)).reshape(-1, 1, 1)
+    mesh = api.Mesh1D({"particles": [ps], "elements": el, "particle_surface_traction": []})
+    solver = api.MPMExplicit(mesh, dt, scheme=scheme, velocity_update=velocity_update,
+                             sim_steps=sim_steps)
+    return solver, np.array([gravity])

@@ -49,13 +49,28 @@ def test_create_rejects_bad_scheme_without_gpu(built):
     assert b"scheme" in lib.mpm_last_error(None)
 
 
-def test_create_rejects_linear1d_as_unsupported(built):
+def test_create_validates_dimension(built):
+    """ndim 1 (Linear1D) and 2 only; a 1-D mesh takes direction 0 only."""
     from diffmpm_gb300 import _lib
     lib = _lib.load()
     d = _lib.MpmDesc()
-    d.ndim = 1
+    d.ndim = 3
     h = ctypes.c_void_p()
     assert lib.mpm_create(ctypes.byref(d), ctypes.byref(h)) == 5
+    d.ndim = 1
+    d.nelements[0] = 4
+    d.el_len[0] = 0.25
+    d.scheme = _lib.USF
+    node = (ctypes.c_int32 * 1)(0)
+    direction = (ctypes.c_int32 * 1)(1)
+    vel = (ctypes.c_double * 1)(0.0)
+    d.n_constraints = 1
+    d.constraint_node, d.constraint_dir, d.constraint_velocity = node, direction, vel
+    mats = (_lib.MpmMaterial * 1)()
+    mats[0].type, mats[0].density, mats[0].E = 1, 1.0, 100.0
+    d.n_materials, d.materials = 1, mats
+    assert lib.mpm_create(ctypes.byref(d), ctypes.byref(h)) == 1
+    assert b"dir must be 0 in 1-D" in lib.mpm_last_error(None)
 
 
 def test_library_is_sm103a(built):
