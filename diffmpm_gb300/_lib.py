@@ -80,6 +80,7 @@ SIGNATURES = [
     ("mpm_host_alloc", C.c_int, [C.c_size_t, C.POINTER(_VP)]),
     ("mpm_host_free", C.c_int, [_VP]),
     ("mpm_set_tractions", C.c_int, [_VP, C.c_int, _VP, _VP, _VP, _VP, _VP]),
+    ("mpm_set_particle_velocity_constraints", C.c_int, [_VP, C.c_int, _VP, _VP, _VP, _VP]),
     ("mpm_read_nodal_field", C.c_int, [_VP, C.c_int, _VP, C.c_int, _VP]),
     ("mpm_write_nodal_field", C.c_int, [_VP, C.c_int, _VP, C.c_int, _VP]),
     ("mpm_initialize", C.c_int, [_VP, _VP]),

@@ -88,6 +88,8 @@ void bind_particles(MpmHandle* h) {
     s.E = h->has_E ? p.E : nullptr;
     s.tr_fn = h->has_trac ? p.tr_fn : nullptr;
     s.tr_tau = h->has_trac ? p.tr_tau : nullptr;
+    s.pvc = h->has_pvc ? p.pvc : nullptr;
+    s.pvc_vel = h->d_pvc_vel;
     s.pid = p.pid;
     s.cstart = h->cstart[h->cs_cur];
     s.cflag = h->cflag;
@@ -162,6 +164,7 @@ int resort(MpmHandle* h, cudaStream_t s) {
         CK(h, launch_gather_u32(reinterpret_cast<const uint32_t*>(*a[i]),
                                 reinterpret_cast<uint32_t*>(*b[i]), w.perm, np, s));
     CK(h, launch_gather_u8(src.mat, dst.mat, w.perm, np, s));
+    if (h->has_pvc) CK(h, launch_gather_pair_u8(src.pvc, dst.pvc, w.perm, np, s));
     if (h->has_trac) {
         CK(h, launch_gather_pair_u8(reinterpret_cast<const uint8_t*>(src.tr_fn),
                                     reinterpret_cast<uint8_t*>(dst.tr_fn), w.perm, np, s));
@@ -291,7 +294,7 @@ void free_particles(MpmHandle* h) {
         void* ptrs[] = {p.x, p.y, p.vx, p.vy, p.sxx[0], p.sxx[1], p.syy[0], p.syy[1], p.szz[0],
                         p.szz[1], p.sxy[0], p.sxy[1], p.exx, p.eyy, p.exy, p.rho[0], p.rho[1],
                         p.vsc[0], p.vsc[1], p.vol[0], p.vol[1], p.mass, p.psize, p.E, p.tr_tau,
-                        p.mat, p.tr_fn, p.pid};
+                        p.mat, p.tr_fn, p.pvc, p.pid};
         for (void* q : ptrs) dfree(h, q);
         p = PSet{};
     }
@@ -305,7 +308,7 @@ void free_particles(MpmHandle* h) {
     for (float* f : h->snap_f) dfree(h, f);
     h->snap_f.clear();
     h->np = -1;
-    h->has_trac = h->has_E = false;
+    h->has_trac = h->has_E = h->has_pvc = false;
 }
 
 // Bring device data of `bytes` at `src` into device memory (staging host data).
@@ -696,6 +699,7 @@ int mpm_set_particles(MpmHandle* h, int64_t n, const float* loc, const int32_t* 
     }
     h->has_trac = false;
     h->has_E = false;
+    h->has_pvc = false;
     h->pcur = 0;
     h->cs_cur = 0;
     h->step = 0;
@@ -946,6 +950,54 @@ int mpm_set_tractions(MpmHandle* h, int n, const int64_t* pid, const int32_t* di
     CK(h, launch_gather_pair_u32(reinterpret_cast<const uint32_t*>(st), reinterpret_cast<uint32_t*>(p.tr_tau), p.pid, (int)np, s));
     CK(h, launch_gather_pair_u8(reinterpret_cast<const uint8_t*>(st8), reinterpret_cast<uint8_t*>(p.tr_fn), p.pid, (int)np, s));
     h->has_trac = true;
+    bind_particles(h);
+    drop_graphs(h);
+    CK(h, cudaMemcpyAsync(h->ds, &h->hs, sizeof(SimDev), cudaMemcpyHostToDevice, s));
+    return sync(h, s);
+}
+
+int mpm_set_particle_velocity_constraints(MpmHandle* h, int n, const int64_t* pid, const int32_t* dir,
+                                          const double* velocity, void* stream) {
+    if (!h) return MPM_ERR_INVALID;
+    h->gen++;
+    if (h->np < 0) return fail(h, MPM_ERR_STATE, "set particles first");
+    const int64_t np = h->np;
+    cudaStream_t s = S(stream);
+    TRY(sync(h, s));
+    if (n <= 0 || np == 0) {
+        h->has_pvc = false;
+        bind_particles(h);
+        drop_graphs(h);
+        return upload_desc(h);
+    }
+    if (!pid || !dir || !velocity) return fail(h, MPM_ERR_INVALID, "null constraint list");
+    std::vector<uint8_t> code((size_t)(2 * np), 0);
+    std::vector<float> vel;
+    for (int i = 0; i < n; ++i) {
+        const int64_t q = pid[i];
+        const int d = dir[i];
+        if (q < 0 || q >= np) return fail(h, MPM_ERR_INVALID, "constrained particle id out of range");
+        if (d < 0 || d >= h->ndim) return fail(h, MPM_ERR_INVALID, "constraint dir out of range");
+        const float v = (float)velocity[i];
+        int slot = -1;
+        for (size_t k = 0; k < vel.size(); ++k)
+            if (std::memcmp(&vel[k], &v, sizeof v) == 0) slot = (int)k;
+        if (slot < 0) {
+            if (vel.size() >= 255) return fail(h, MPM_ERR_UNSUPPORTED, "more than 255 distinct particle velocities");
+            vel.push_back(v);
+            slot = (int)vel.size() - 1;
+        }
+        code[2 * q + d] = (uint8_t)(slot + 1);   // later entries win, as for nodes
+    }
+    for (int k = 0; k < 2; ++k)
+        if (!h->ps[k].pvc) TRY(dalloc(h, &h->ps[k].pvc, 2 * np));
+    if (!h->d_pvc_vel) TRY(dalloc(h, &h->d_pvc_vel, 256));
+    CK(h, cudaMemcpy(h->d_pvc_vel, vel.data(), sizeof(float) * vel.size(), cudaMemcpyHostToDevice));
+    PSet& p = h->ps[h->pcur];
+    TRY(ensure_stage(h, 2 * np));
+    CK(h, cudaMemcpyAsync(h->stage, code.data(), 2 * np, cudaMemcpyHostToDevice, s));
+    CK(h, launch_gather_pair_u8(static_cast<const uint8_t*>(h->stage), p.pvc, p.pid, (int)np, s));
+    h->has_pvc = true;
     bind_particles(h);
     drop_graphs(h);
     CK(h, cudaMemcpyAsync(h->ds, &h->hs, sizeof(SimDev), cudaMemcpyHostToDevice, s));

@@ -417,6 +417,8 @@ int check_supported(MpmHandle* h) {
         return fail(h, MPM_ERR_UNSUPPORTED,
                     "the adjoint implements the per-step volume set-up of solve_jit");
     if (h->has_trac) return fail(h, MPM_ERR_UNSUPPORTED, "the adjoint does not cover particle tractions");
+    if (h->has_pvc)
+        return fail(h, MPM_ERR_UNSUPPORTED, "the adjoint does not cover particle velocity constraints");
     for (const MatDev& m : h->mats)
         if (m.type == MAT_NEWTONIAN)
             return fail(h, MPM_ERR_UNSUPPORTED, "the adjoint covers LinearElastic and SimpleMaterial");

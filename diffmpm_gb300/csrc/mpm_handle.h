@@ -23,6 +23,7 @@ struct PSet {
     float *mass = nullptr, *psize = nullptr, *E = nullptr, *tr_tau = nullptr;
     uint8_t* mat = nullptr;
     int8_t* tr_fn = nullptr;
+    uint8_t* pvc = nullptr;     // particle velocity constraint codes (2 per particle)
     int* pid = nullptr;
 };
 
@@ -121,6 +122,8 @@ struct MpmHandle {
     cudaStream_t cap = nullptr;
     std::map<int, cudaGraphExec_t> graphs;
     bool graphs_trac = false;
+    bool has_pvc = false;              // particle velocity constraints set
+    float* d_pvc_vel = nullptr;
     bool initialized = false, needs_resort = false;
     int block_steps = 100;
     int64_t resorts = 0, rollbacks = 0;

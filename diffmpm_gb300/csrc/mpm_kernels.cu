@@ -845,6 +845,11 @@ __device__ __forceinline__ void particle_kinematics_tile(const SimDev& S, const 
             vx = fa(b[GF_VX][lane], fm(dot4(N, nax), dt));
             vy = fa(b[GF_VY][lane], fm(dot4(N, nay), dt));
         }
+        if (S.pvc) {   // particle velocity constraints (an extension; scheme.py:67 leaves a TODO)
+            const uchar2 c = reinterpret_cast<const uchar2*>(S.pvc)[q];
+            if (c.x) vx = S.pvc_vel[c.x - 1];
+            if (c.y) vy = S.pvc_vel[c.y - 1];
+        }
         const float xn = fa(x, fm(vhx, dt)), yn = fa(y, fm(vhy, dt));
         S.x[q] = xn;
         S.y[q] = yn;

@@ -174,7 +174,9 @@ k_line_g2p(const __grid_constant__ SimDev S, const int* __restrict__ eid, Contro
     const float N0 = shape2(0, xi), N1 = shape2(1, xi);
     const float vh = fa(fm(N0, S.nvbx[e]), fm(N1, S.nvbx[e + 1]));
     const float ah = fa(fm(N0, S.nax[e]), fm(N1, S.nax[e + 1]));
-    S.vx[q] = S.velocity_update ? vh : fa(S.vx[q], fm(ah, S.dt));
+    float v = S.velocity_update ? vh : fa(S.vx[q], fm(ah, S.dt));
+    if (S.pvc && S.pvc[2 * q]) v = S.pvc_vel[S.pvc[2 * q] - 1];   // particle velocity constraint
+    S.vx[q] = v;
     const float x = fa(S.x[q], fm(vh, S.dt));
     S.x[q] = x;
     const int ne = locate_axis(x, S.hx, S.nx);

@@ -64,6 +64,8 @@ struct SimDev {
     int8_t *tr_fn;         // [2 per particle] 0 none, 1 Unit, k+2 table k; null if no tractions
     float *tr_tau;         // [2 per particle]
     int *pid;              // storage index -> original particle index
+    const uint8_t *pvc;    // [2 per particle] velocity constraint slot+1 per direction, or null
+    const float *pvc_vel;  // particle velocity constraint table
     // cells
     int *cstart;
     uint8_t *cflag;

@@ -255,6 +255,18 @@ class Simulation:
         self._ok(self._lib.mpm_set_tractions(self._h, int(pids.size), _lib.ptr(pids), _lib.ptr(dirs),
                                              _lib.ptr(vals), _lib.ptr(fns), None))
 
+    def set_particle_velocity_constraints(self, pids, dirs, values):
+        """After every particle velocity update, the velocity of particle
+        pids[k] in direction dirs[k] is set to values[k] (later entries win);
+        an empty list clears them."""
+        pids = np.ascontiguousarray(np.asarray(pids, dtype=np.int64).reshape(-1))
+        dirs = np.ascontiguousarray(np.asarray(dirs, dtype=np.int32).reshape(-1))
+        vals = np.ascontiguousarray(np.asarray(values, dtype=np.float64).reshape(-1))
+        if not (pids.size == dirs.size == vals.size):
+            raise ValueError("pids, dirs and values must have the same length")
+        self._ok(self._lib.mpm_set_particle_velocity_constraints(
+            self._h, int(pids.size), _lib.ptr(pids), _lib.ptr(dirs), _lib.ptr(vals), None))
+
     def read_nodal(self, field, out=None):
         nc = 1 if field == "mass" else self.ndim
         if out is None:

@@ -15,6 +15,7 @@ class _MeshBase:
         self.particles = list(config["particles"])
         self.elements = config["elements"]
         self.particle_tractions = list(config.get("particle_surface_traction", []))
+        self.particle_velocity_constraints = list(config.get("particle_velocity_constraints", []))
 
 
 class Mesh1D(_MeshBase):

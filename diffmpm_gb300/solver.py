@@ -122,6 +122,16 @@ class MPMExplicit:
                 fns.extend([pt.function] * ids.size)
         if pids:
             sim.set_tractions(pids, dirs, vals, fns)
+        pids, dirs, vals = [], [], []
+        for pc in getattr(self.mesh, "particle_velocity_constraints", []):
+            psets = pc.pset if isinstance(pc.pset, (list, tuple, np.ndarray)) else [pc.pset]
+            ids = np.asarray(pc.pids, dtype=np.int64).reshape(-1)
+            for s in psets:
+                pids.extend((offsets[int(s)] + ids).tolist())
+                dirs.extend([int(pc.dir)] * ids.size)
+                vals.extend([float(pc.velocity)] * ids.size)
+        if pids:
+            sim.set_particle_velocity_constraints(pids, dirs, vals)
 
     def _pull_setup(self, sim: Simulation):
         sets, _, _, offsets = self._population()

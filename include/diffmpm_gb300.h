@@ -183,6 +183,14 @@ int mpm_host_free(void* p);
 int mpm_set_tractions(MpmHandle* h, int n, const int64_t* pid, const int32_t* dir,
                       const double* traction, const int32_t* function, void* stream);
 
+/* Particle velocity constraints: after the particle velocity update of every
+ * step, the velocity of particle pid[i] (original order) in direction dir[i]
+ * becomes velocity[i]; later entries win; n = 0 clears the list.  The
+ * reference leaves this step as a TODO (diffmpm/scheme.py:67); this extension
+ * mirrors the nodal Constraint (diffmpm/constraint.py:29-44) on particles. */
+int mpm_set_particle_velocity_constraints(MpmHandle* h, int n, const int64_t* pid, const int32_t* dir,
+                                          const double* velocity, void* stream);
+
 /* Nodal state access (diffmpm/node.py:64-71). */
 int mpm_read_nodal_field(MpmHandle* h, int field, float* dst, int on_device, void* stream);
 int mpm_write_nodal_field(MpmHandle* h, int field, const float* src, int on_device, void* stream);

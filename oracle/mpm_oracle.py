@@ -49,7 +49,7 @@ import numpy as np
 __all__ = [
     "Nodes", "Linear1D", "Quadrilateral4Node", "Particles", "LinearElastic",
     "SimpleMaterial", "Newtonian", "Constraint", "NodalForce", "ParticleTraction",
-    "Unit", "Linear", "Mesh1D", "Mesh2D", "USF", "USL", "MPMExplicit",
+    "ParticleVelocityConstraint", "Unit", "Linear", "Mesh1D", "Mesh2D", "USF", "USL", "MPMExplicit",
     "OutOfMeshError",
 ]
 
@@ -149,6 +149,17 @@ class ParticleTraction(NamedTuple):
     function: object
     dir: int
     traction: float
+
+
+class ParticleVelocityConstraint(NamedTuple):
+    """Velocity ``velocity`` in direction ``dir`` of particles ``pids`` of the
+    particle sets ``pset``, imposed after every particle velocity update (an
+    extension: the reference leaves this as a TODO, scheme.py:67)."""
+
+    pset: object
+    pids: object
+    dir: int
+    velocity: float
 
 
 # ----------------------------------------------------------------------------
@@ -845,6 +856,20 @@ class _MeshBase:
         self.particles = config["particles"]
         self.elements = config["elements"]
         self.particle_tractions = config.get("particle_surface_traction", [])
+        self.particle_velocity_constraints = config.get("particle_velocity_constraints", [])
+
+    def apply_particle_velocity_constraints(self):
+        """v[pids, dir] = velocity for each entry in list order, after the
+        particle velocity update (an extension: the reference leaves this
+        step as a TODO, scheme.py:67); momentum follows the velocity."""
+        dtype = self.elements.dtype
+        for pc in self.particle_velocity_constraints:
+            psets = pc.pset if isinstance(pc.pset, (list, tuple, np.ndarray)) else [pc.pset]
+            for pset_id in psets:
+                p = self.particles[int(pset_id)]
+                ids = np.asarray(pc.pids, dtype=np.int64).reshape(-1)
+                p.velocity[ids, 0, pc.dir] = _c(pc.velocity, dtype)
+                p.momentum = p.mass * p.velocity
 
     def apply_on_elements(self, function, args=()):
         """mesh.py:31-43 -- the element method once per particle set."""
@@ -918,6 +943,7 @@ class _MPMScheme:
         self.mesh.apply_on_elements("update_nodal_acceleration_velocity", args=(self.dt,))
         self.mesh.apply_on_particles("update_position_velocity",
                                      args=(self.dt, self.velocity_update))
+        self.mesh.apply_particle_velocity_constraints()
 
 
 class USF(_MPMScheme):

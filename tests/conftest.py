@@ -52,5 +52,6 @@ def pytest_terminal_summary(terminalreporter):
     tr = terminalreporter
     tr.section("error against float64 (GPU | float32 oracle)")
     for row in rows:
-        cells = [f"{k} {v[0]:.2e} | {v[1]:.2e}" for k, v in row.items() if k != "config"]
+        cells = [f"{k} {v[0]:.2e} | {v[1]:.2e}" + (" abs" if v[2] == "abs" else "")
+                 for k, v in row.items() if k != "config"]
         tr.write_line(f"{row['config']}: " + "; ".join(cells))

@@ -51,7 +51,7 @@ def test_deck_goldens_from_npz(built, tmp_path, monkeypatch, name):
     decks.check_goldens(deck, stress)
     # the same files as the oracle's writer gives, step for step
     ref = {}
-    osv, _ = decks.build(O, deck, writer_func=lambda a, t, **kw: ref.__setitem__(a[1], a[0]))
+    osv, _ = decks.build(O, deck, writer_func=lambda a, i: ref.__setitem__(i, a))
     osv.solve_jit(np.asarray(deck["external_loading"]["gravity"], float))
     for i in list(ref)[:: max(1, len(ref) // 10)]:
         with np.load(folder / npz_name(i, meta["nsteps"])) as f:
