@@ -597,7 +597,7 @@ int ensure_batch_adjoint(MpmBatch* b, cudaStream_t s) {
     std::vector<int2> pb;
     for (int i = 0; i < n; ++i) {
         const MpmHandle* h = b->sims[i];
-        for (int c = 0; c * ADJ_BLOCK < h->np; ++c) pb.push_back(make_int2(i, c));
+        for (int c = 0; c * ADJ_BLOCK * ADJ_ITER < h->np; ++c) pb.push_back(make_int2(i, c));
     }
     cudaFree(x->part_blocks);
     x->part_blocks = nullptr;

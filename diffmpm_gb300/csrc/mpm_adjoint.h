@@ -67,6 +67,9 @@ cudaError_t launch_rev_mass_momentum(const AdjStep& A, cudaStream_t s);
 // (tile t of simulation tiles[t].x), passes 2 and 4 with CTA b on simulation
 // part_blocks[b].x, particles part_blocks[b].y * 256 .. + 255.
 constexpr int ADJ_BLOCK = 256;
+// Particles of one simulation per block of the batched particle passes: the
+// block copies the simulation's arguments once and walks ADJ_ITER chunks.
+constexpr int ADJ_ITER = 4;
 cudaError_t launch_adj_table(const AdjStep* bases, int n, int t, AdjStep* table, cudaStream_t s);
 cudaError_t launch_rev_batch(const AdjStep* table, const int4* tiles, int ntiles,
                              const int2* part_blocks, int n_part_blocks, cudaStream_t s);

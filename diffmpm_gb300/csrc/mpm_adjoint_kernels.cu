@@ -26,6 +26,7 @@ namespace mpm {
 namespace {
 
 constexpr int PART_THREADS = 256;
+static_assert(PART_THREADS == ADJ_BLOCK, "the batched block map counts ADJ_BLOCK particles per chunk");
 
 // Particles currently in cell (ci, cj) at the step start, in the order of the
 // forward gathers: the cell's own sort-cell, and neighbouring sort-cells whose
@@ -425,7 +426,8 @@ k_rev_forces_batch(const AdjStep* __restrict__ table, const int2* __restrict__ b
     __shared__ AdjStep sA;
     const int2 bm = blocks[blockIdx.x];
     load_step_args(table + bm.x, sA);
-    rev_forces_at(sA, bm.y * PART_THREADS + threadIdx.x);
+    #pragma unroll 1
+    for (int k = 0; k < ADJ_ITER; ++k) rev_forces_at(sA, (bm.y * ADJ_ITER + k) * PART_THREADS + threadIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -568,7 +570,9 @@ k_rev_mass_momentum_batch(const AdjStep* __restrict__ table, const int2* __restr
     __shared__ AdjStep sA;
     const int2 bm = blocks[blockIdx.x];
     load_step_args(table + bm.x, sA);
-    rev_mass_momentum_at(sA, bm.y * PART_THREADS + threadIdx.x);
+    #pragma unroll 1
+    for (int k = 0; k < ADJ_ITER; ++k)
+        rev_mass_momentum_at(sA, (bm.y * ADJ_ITER + k) * PART_THREADS + threadIdx.x);
 }
 
 __global__ void k_copy_f32(const __grid_constant__ CopyJob j) {

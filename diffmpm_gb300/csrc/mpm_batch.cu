@@ -55,10 +55,14 @@ void drop_batch_graphs(MpmBatch* b) {
 }
 
 int launch_batch_steps(MpmBatch* b, int n, cudaStream_t s) {
+    // the descriptors change only between step blocks (re-sorts, set-up calls):
+    // one contiguous copy per block lets a CTA fetch its simulation's
+    // descriptor without first loading a pointer to it
+    BCK(b, launch_gather_descs(b->d_sims, (int)b->sims.size(), b->d_descs, s));
     for (int i = 0; i < n; ++i) {
-        BCK(b, launch_nodal_kinematics_batch(b->cfg, b->d_sims, b->d_ctls, b->d_tiles, b->ntiles, s));
-        BCK(b, launch_forces_batch(b->cfg, b->d_sims, b->d_ctls, b->d_tiles, b->ntiles, s));
-        BCK(b, launch_particle_kinematics_batch(b->cfg, b->d_sims, b->d_ctls, b->d_tiles, b->ntiles, s));
+        BCK(b, launch_nodal_kinematics_batch(b->cfg, b->d_descs, b->d_ctls, b->d_tiles, b->ntiles, s));
+        BCK(b, launch_forces_batch(b->cfg, b->d_descs, b->d_ctls, b->d_tiles, b->ntiles, s));
+        BCK(b, launch_particle_kinematics_batch(b->cfg, b->d_descs, b->d_ctls, b->d_tiles, b->ntiles, s));
     }
     return MPM_OK;
 }
@@ -208,6 +212,7 @@ int mpm_batch_create(MpmHandle* const* sims, int n, MpmBatch** out) {
     };
     cudaError_t e;
     if ((e = cudaMalloc(&b->d_sims, sizeof(SimDev*) * n)) != cudaSuccess) return bail("cudaMalloc", e);
+    if ((e = cudaMalloc(&b->d_descs, sizeof(SimDev) * n)) != cudaSuccess) return bail("cudaMalloc", e);
     if ((e = cudaMalloc(&b->d_ctls, sizeof(Control*) * n)) != cudaSuccess) return bail("cudaMalloc", e);
     if ((e = cudaMalloc(&b->d_tiles, sizeof(int4) * tiles.size())) != cudaSuccess) return bail("cudaMalloc", e);
     if ((e = cudaMalloc(&b->d_status, sizeof(Control) * n)) != cudaSuccess) return bail("cudaMalloc", e);
@@ -230,6 +235,7 @@ int mpm_batch_destroy(MpmBatch* b) {
     segbuf_free(b->segbuf);
     if (b->cap) cudaStreamDestroy(b->cap);
     cudaFree(b->d_sims);
+    cudaFree(b->d_descs);
     cudaFree(b->d_ctls);
     cudaFree(b->d_tiles);
     cudaFree(b->d_status);

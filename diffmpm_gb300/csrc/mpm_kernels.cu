@@ -28,6 +28,17 @@ __device__ __forceinline__ int load_step(const Control* ctl) {
 
 // Batched launches: the CTA copies the descriptor of its simulation into
 // shared memory (one word per thread) before the tile work starts.
+__global__ void k_gather_descs(const SimDev* const* __restrict__ sims, int n, SimDev* __restrict__ out) {
+    const int* a = reinterpret_cast<const int*>(sims[blockIdx.x]);
+    int* b = reinterpret_cast<int*>(out + blockIdx.x);
+    for (int i = threadIdx.x; i < (int)(sizeof(SimDev) / 4); i += blockDim.x) b[i] = a[i];
+}
+
+cudaError_t launch_gather_descs(const SimDev* const* sims, int n, SimDev* descs, cudaStream_t s) {
+    if (n > 0) k_gather_descs<<<n, 128, 0, s>>>(sims, n, descs);
+    return cudaGetLastError();
+}
+
 __device__ __forceinline__ void load_sim(const SimDev* __restrict__ src, SimDev& dst) {
     static_assert(sizeof(SimDev) % 4 == 0, "descriptor copied in 4-byte words");
     const int* a = reinterpret_cast<const int*>(src);
@@ -78,15 +89,28 @@ __device__ __forceinline__ void cell_nodes(const SimDev& S, int ci, int cj, int 
     ids[3] = ll + S.nx + 1;
 }
 
+// A descriptor field read at its point of use.  With VD (the descriptor is a
+// shared-memory copy, batched kernels) the read is volatile, so the compiler
+// reloads the field instead of keeping ~20 loop-invariant pointers live in
+// registers (which spilled); a __grid_constant__ descriptor is read from the
+// constant bank either way.
+template <bool VD, class T>
+__device__ __forceinline__ T rd(const T& f) {
+    if constexpr (VD) return *const_cast<const volatile T*>(&f);
+    else return f;
+}
+
+
+template <bool VD = false>
 __device__ __forceinline__ void apply_constraint(const SimDev& S, uint16_t code, float& vx,
                                                  float& vy, float* ax, float* ay) {
     const int c0 = code & 0xff, c1 = code >> 8;
     if (c0) {
-        vx = S.cons_vel[c0 - 1];
+        vx = rd<VD>(S.cons_vel)[c0 - 1];
         if (ax) *ax = 0.0f;
     }
     if (c1) {
-        vy = S.cons_vel[c1 - 1];
+        vy = rd<VD>(S.cons_vel)[c1 - 1];
         if (ay) *ay = 0.0f;
     }
 }
@@ -281,14 +305,14 @@ __device__ __forceinline__ void add_traction(const SimDev& S, int q, float t, fl
 // Per-cell values of phase 2: the volume set-up V0 = V_el / count and
 // size0 = sqrt(V0) (particle.py:169-178), and (USF) dt times the centroid
 // volumetric strain rate from the cell's nodal velocities (particle.py:270-279).
-template <bool USL, bool REINIT>
+template <bool USL, bool REINIT, bool VD = false>
 __device__ __forceinline__ void force_cell_values(const SimDev& S, int cnt, const CellGeo& g,
                                                   const float nvx[4], const float nvy[4],
                                                   float& V0, float& size0, float& dvol) {
     V0 = 0.0f;
     size0 = 1.0f;
     if (REINIT) {
-        if (cnt) V0 = fdv(S.vol_el, (float)cnt);
+        if (cnt) V0 = fdv(rd<VD>(S.vol_el), (float)cnt);
         size0 = sqrtf(V0);
     }
     dvol = 0.0f;
@@ -296,7 +320,7 @@ __device__ __forceinline__ void force_cell_values(const SimDev& S, int cnt, cons
         float Gcx[4], Gcy[4], c0, c1, c3;
         dshape4(0.0f, 0.0f, g.rx, g.ry, Gcx, Gcy);
         strain_rate4(Gcx, Gcy, nvx, nvy, c0, c1, c3);
-        dvol = fm(S.dt, fa(c0, c1));
+        dvol = fm(rd<VD>(S.dt), fa(c0, c1));
     }
 }
 
@@ -307,24 +331,25 @@ struct ForceIn {
 
 enum ForceField { FF_X, FF_Y, FF_SXX, FF_SYY, FF_SZZ, FF_SXY, FF_RHO, FF_VOL, FF_N };
 
+template <bool VD = false>
 __device__ __forceinline__ ForceIn force_in_global(const SimDev& S, int q, int parity,
                                                    bool reinit) {
     ForceIn in;
-    in.x = S.x[q];
-    in.y = S.y[q];
-    in.sxx = S.sxx[parity][q];
-    in.syy = S.syy[parity][q];
-    in.szz = S.szz[parity][q];
-    in.sxy = S.sxy[parity][q];
-    in.rho = S.rho[parity][q];
-    in.vol = reinit ? 0.0f : S.vol[parity][q];
+    in.x = rd<VD>(S.x)[q];
+    in.y = rd<VD>(S.y)[q];
+    in.sxx = rd<VD>(S.sxx[parity])[q];
+    in.syy = rd<VD>(S.syy[parity])[q];
+    in.szz = rd<VD>(S.szz[parity])[q];
+    in.sxy = rd<VD>(S.sxy[parity])[q];
+    in.rho = rd<VD>(S.rho[parity])[q];
+    in.vol = reinit ? 0.0f : rd<VD>(S.vol[parity])[q];
     return in;
 }
 
 // Per-particle work of phase 2: USF strain/volume/stress update (written back
 // when `write`) and the total-force contributions [f x, f y] x 4 corners,
 // internal plus external force (element.py:236-303, 842-901).
-template <bool USL, bool REINIT, bool TRAC>
+template <bool USL, bool REINIT, bool TRAC, bool VD = false>
 __device__ __forceinline__ void force_contrib(const SimDev& S, int q, const ForceIn& in, float cx,
                                               float rx, float cy, float ry, float V0, float size0,
                                               const float nvx[4], const float nvy[4], float dvol,
@@ -333,10 +358,10 @@ __device__ __forceinline__ void force_contrib(const SimDev& S, int q, const Forc
     PState p;
     if (!USL) {
         // state updated but not needed for the forces: loaded early, used late
-        p.exx = S.exx[q];
-        p.eyy = S.eyy[q];
-        p.exy = S.exy[q];
-        p.vsc = S.vsc[parity][q];
+        p.exx = rd<VD>(S.exx)[q];
+        p.eyy = rd<VD>(S.eyy)[q];
+        p.exy = rd<VD>(S.exy)[q];
+        p.vsc = rd<VD>(S.vsc[parity])[q];
     }
     const float xi = natural(in.x, cx, rx);
     const float eta = natural(in.y, cy, ry);
@@ -348,29 +373,30 @@ __device__ __forceinline__ void force_contrib(const SimDev& S, int q, const Forc
     p.szz = in.szz;
     p.sxy = in.sxy;
     p.rho = in.rho;
-    const float mp = REINIT ? fm(V0, p.rho) : S.mass[q];
+    const float mp = REINIT ? fm(V0, p.rho) : rd<VD>(S.mass)[q];
     float V = REINIT ? V0 : in.vol;
     if (!USL) {
         float r0, r1, r3;
         strain_rate4(Gx, Gy, nvx, nvy, r0, r1, r3);
-        const MatDev& M = S.mats[S.mat[q]];
-        const float Ep = S.E ? S.E[q] : -1.0f;
-        V = fm(V, strain_stress_update(M, Ep, S.dt, r0, r1, r3, dvol, p));
+        const MatDev& M = rd<VD>(S.mats)[rd<VD>(S.mat)[q]];
+        const float* E = rd<VD>(S.E);
+        const float Ep = E ? E[q] : -1.0f;
+        V = fm(V, strain_stress_update(M, Ep, rd<VD>(S.dt), r0, r1, r3, dvol, p));
         if (write) {
-            S.sxx[next][q] = p.sxx;
-            S.syy[next][q] = p.syy;
-            S.szz[next][q] = p.szz;
-            S.sxy[next][q] = p.sxy;
-            S.exx[q] = p.exx;
-            S.eyy[q] = p.eyy;
-            S.exy[q] = p.exy;
-            S.rho[next][q] = p.rho;
-            S.vsc[next][q] = p.vsc;
-            if (!REINIT) S.vol[next][q] = V;
+            rd<VD>(S.sxx[next])[q] = p.sxx;
+            rd<VD>(S.syy[next])[q] = p.syy;
+            rd<VD>(S.szz[next])[q] = p.szz;
+            rd<VD>(S.sxy[next])[q] = p.sxy;
+            rd<VD>(S.exx)[q] = p.exx;
+            rd<VD>(S.eyy)[q] = p.eyy;
+            rd<VD>(S.exy)[q] = p.exy;
+            rd<VD>(S.rho[next])[q] = p.rho;
+            rd<VD>(S.vsc[next])[q] = p.vsc;
+            if (!REINIT) rd<VD>(S.vol[next])[q] = V;
         }
     }
     const float nV = -V;
-    const float mgx = fm(mp, S.gx), mgy = fm(mp, S.gy);
+    const float mgx = fm(mp, rd<VD>(S.gx)), mgy = fm(mp, rd<VD>(S.gy));
     #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const float fx = fa(fm(Gx[k], p.sxx), fm(Gy[k], p.sxy));
@@ -488,20 +514,21 @@ k_nodal_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__ ti
 
 template <bool REINIT>
 __global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
-k_nodal_kinematics_batch(const SimDev* const* __restrict__ sims, Control* const* __restrict__ ctls,
+k_nodal_kinematics_batch(const SimDev* __restrict__ descs, Control* const* __restrict__ ctls,
                          const int4* __restrict__ tiles) {
     __shared__ SimDev sS;
     const int4 T = tiles[blockIdx.x];
-    load_sim(sims[T.x], sS);
+    load_sim(descs + T.x, sS);
     nodal_kinematics_tile<REINIT>(sS, T, ctls[T.x]);
 }
 
 // Nodal update shared by both schemes: concentrated forces (element.py:270-284),
 // a = nan_to_num(f/m), v += a dt, constraints, flush (element.py:305-329).
 // (fx, fy) is the summed internal plus external force of the particles.
+template <bool VD = false>
 __device__ __forceinline__ void nodal_update(const SimDev& S, int n, float t, float fx, float fy,
                                              float v0x, float v0y, float mass, uint16_t ncons) {
-    if (S.cnf_ptr) {
+    if (rd<VD>(S.cnf_ptr)) {
         const int b = S.cnf_ptr[n], e = S.cnf_ptr[n + 1];
         #pragma unroll 1
         for (int k = b; k < e; ++k) {
@@ -514,13 +541,14 @@ __device__ __forceinline__ void nodal_update(const SimDev& S, int n, float t, fl
     const float ty = fa(fy, 0.0f);
     float ax = nan_to_num(fdv(tx, mass));
     float ay = nan_to_num(fdv(ty, mass));
-    float vx = fa(v0x, fm(ax, S.dt));
-    float vy = fa(v0y, fm(ay, S.dt));
-    apply_constraint(S, ncons, vx, vy, &ax, &ay);
-    S.nvbx[n] = flush(vx);
-    S.nvby[n] = flush(vy);
-    S.nax[n] = flush(ax);
-    S.nay[n] = flush(ay);
+    const float dt = rd<VD>(S.dt);
+    float vx = fa(v0x, fm(ax, dt));
+    float vy = fa(v0y, fm(ay, dt));
+    apply_constraint<VD>(S, ncons, vx, vy, &ax, &ay);
+    rd<VD>(S.nvbx)[n] = flush(vx);
+    rd<VD>(S.nvby)[n] = flush(vy);
+    rd<VD>(S.nax)[n] = flush(ax);
+    rd<VD>(S.nay)[n] = flush(ay);
 }
 
 // ---------------------------------------------------------------------------
@@ -535,7 +563,7 @@ constexpr int NV_W = TILE_CX + 1;   // node tile of the R cells: [c0x, c0x+33) x
 constexpr int NV_H = TILE_CY + 1;
 constexpr int K2_ROW_P = 128;   // particles of a row per pass (two CTAs per SM)
 
-template <bool USL, bool REINIT, bool TRAC>
+template <bool USL, bool REINIT, bool TRAC, bool VD>
 __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
                                             Control* __restrict__ ctl) {
     constexpr int NQ = 8;
@@ -559,7 +587,7 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
     const uint16_t ncons = node_ok ? S.ncons[node] : 0;
     if (!sort_cells_occupied(S, c0x - 1, c0x + TILE_CX + 1, c0y - 1, c0y + TILE_CY + 1)) {
         // no particle in the tile: the nodal update with zero particle forces
-        if (node_ok) nodal_update(S, node, t, 0.0f, 0.0f, S.nvax[node], S.nvay[node], nmass, ncons);
+        if (node_ok) nodal_update<VD>(S, node, t, 0.0f, 0.0f, S.nvax[node], S.nvay[node], nmass, ncons);
         return;
     }
     #pragma unroll
@@ -599,7 +627,7 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
         {
             float nvx[4], nvy[4], V0, size0, dvol;
             if (!USL) cell_velocities(lx, ly, nvx, nvy);
-            force_cell_values<USL, REINIT>(S, ce - cb, geo_of(G, lx + 1, ly + 1), nvx, nvy, V0,
+            force_cell_values<USL, REINIT, VD>(S, ce - cb, geo_of(G, lx + 1, ly + 1), nvx, nvy, V0,
                                            size0, dvol);
             s_cellv[ly][0][lx] = V0;
             s_cellv[ly][1][lx] = size0;
@@ -620,7 +648,7 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
                 float nvx[4], nvy[4];
                 if (!USL) cell_velocities(l, ly, nvx, nvy);
                 float cc[NQ];
-                force_contrib<USL, REINIT, TRAC>(S, q, force_in_global(S, q, parity, REINIT),
+                force_contrib<USL, REINIT, TRAC, VD>(S, q, force_in_global<VD>(S, q, parity, REINIT),
                                                  G.cx[l + 1], G.rx[l + 1], cy, ry,
                                                  s_cellv[ly][0][l], s_cellv[ly][1][l], nvx, nvy,
                                                  s_cellv[ly][2][l], parity, t, l >= 1 && ly >= 1,
@@ -643,11 +671,11 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
         const int cnt = REINIT ? count_cell(S, ci, cj, g) : 0;
         float nvx[4], nvy[4], V0, size0, dvol;
         if (!USL) cell_velocities(lx, ly, nvx, nvy);
-        force_cell_values<USL, REINIT>(S, cnt, g, nvx, nvy, V0, size0, dvol);
+        force_cell_values<USL, REINIT, VD>(S, cnt, g, nvx, nvy, V0, size0, dvol);
         const bool own = lx >= 1 && ly >= 1;
         visit_cell(S, ci, cj, g, [&](int q) {
             float cc[NQ];
-            force_contrib<USL, REINIT, TRAC>(S, q, force_in_global(S, q, parity, REINIT), g.cx,
+            force_contrib<USL, REINIT, TRAC, VD>(S, q, force_in_global<VD>(S, q, parity, REINIT), g.cx,
                                              g.rx, g.cy, g.ry, V0, size0, nvx, nvy, dvol, parity,
                                              t, own, cc);
             #pragma unroll
@@ -657,7 +685,7 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
     __syncthreads();
     if (node_ok) {
         const int a = (ly + 1) * NV_W + lx + 1;   // node (I, J) in the node tile
-        nodal_update(S, node, t, node_sum(s_c + 0, tid), node_sum(s_c + 4, tid), s_v[a].x, s_v[a].y,
+        nodal_update<VD>(S, node, t, node_sum(s_c + 0, tid), node_sum(s_c + 4, tid), s_v[a].x, s_v[a].y,
                      nmass, ncons);
     }
 }
@@ -666,17 +694,17 @@ template <bool USL, bool REINIT, bool TRAC>
 __global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
 k_forces(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
          Control* __restrict__ ctl) {
-    forces_tile<USL, REINIT, TRAC>(S, tiles[blockIdx.x], ctl);
+    forces_tile<USL, REINIT, TRAC, false>(S, tiles[blockIdx.x], ctl);
 }
 
 template <bool USL, bool REINIT, bool TRAC>
 __global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
-k_forces_batch(const SimDev* const* __restrict__ sims, Control* const* __restrict__ ctls,
+k_forces_batch(const SimDev* __restrict__ descs, Control* const* __restrict__ ctls,
                const int4* __restrict__ tiles) {
     __shared__ SimDev sS;
     const int4 T = tiles[blockIdx.x];
-    load_sim(sims[T.x], sS);
-    forces_tile<USL, REINIT, TRAC>(sS, T, ctls[T.x]);
+    load_sim(descs + T.x, sS);
+    forces_tile<USL, REINIT, TRAC, true>(sS, T, ctls[T.x]);
 }
 
 // ---------------------------------------------------------------------------
@@ -940,11 +968,11 @@ k_particle_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__
 
 template <bool USL, bool REINIT>
 __global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
-k_particle_kinematics_batch(const SimDev* const* __restrict__ sims, Control* const* __restrict__ ctls,
+k_particle_kinematics_batch(const SimDev* __restrict__ descs, Control* const* __restrict__ ctls,
                             const int4* __restrict__ tiles) {
     __shared__ SimDev sS;
     const int4 T = tiles[blockIdx.x];
-    load_sim(sims[T.x], sS);
+    load_sim(descs + T.x, sS);
     particle_kinematics_tile<USL, REINIT>(sS, T, ctls[T.x]);
 }
 
@@ -1022,60 +1050,60 @@ cudaError_t launch_particle_kinematics(const StepConfig& c, const SimDev& S, con
 
 // Batched launches: one grid over the tiles of every simulation of a batch.
 template <bool REINIT>
-static void nodal_kinematics_batch(const SimDev* const* sims, Control* const* ctls,
+static void nodal_kinematics_batch(const SimDev* descs, Control* const* ctls,
                                    const int4* tiles, int ntiles, cudaStream_t s) {
     prefer_shared(k_nodal_kinematics_batch<REINIT>);
-    k_nodal_kinematics_batch<REINIT><<<ntiles, TILE_THREADS, 0, s>>>(sims, ctls, tiles);
+    k_nodal_kinematics_batch<REINIT><<<ntiles, TILE_THREADS, 0, s>>>(descs, ctls, tiles);
 }
 
-cudaError_t launch_nodal_kinematics_batch(const StepConfig& c, const SimDev* const* sims,
+cudaError_t launch_nodal_kinematics_batch(const StepConfig& c, const SimDev* descs,
                                           Control* const* ctls, const int4* tiles, int ntiles,
                                           cudaStream_t s) {
-    if (c.reinit) nodal_kinematics_batch<true>(sims, ctls, tiles, ntiles, s);
-    else nodal_kinematics_batch<false>(sims, ctls, tiles, ntiles, s);
+    if (c.reinit) nodal_kinematics_batch<true>(descs, ctls, tiles, ntiles, s);
+    else nodal_kinematics_batch<false>(descs, ctls, tiles, ntiles, s);
     return cudaGetLastError();
 }
 
 template <bool USL, bool REINIT, bool TRAC>
-static void forces_batch(const SimDev* const* sims, Control* const* ctls, const int4* tiles,
+static void forces_batch(const SimDev* descs, Control* const* ctls, const int4* tiles,
                          int ntiles, cudaStream_t s) {
     prefer_shared(k_forces_batch<USL, REINIT, TRAC>);
-    k_forces_batch<USL, REINIT, TRAC><<<ntiles, TILE_THREADS, 0, s>>>(sims, ctls, tiles);
+    k_forces_batch<USL, REINIT, TRAC><<<ntiles, TILE_THREADS, 0, s>>>(descs, ctls, tiles);
 }
 
-cudaError_t launch_forces_batch(const StepConfig& c, const SimDev* const* sims,
+cudaError_t launch_forces_batch(const StepConfig& c, const SimDev* descs,
                                 Control* const* ctls, const int4* tiles, int ntiles,
                                 cudaStream_t s) {
     const int key = (c.usl ? 4 : 0) | (c.reinit ? 2 : 0) | (c.traction ? 1 : 0);
     switch (key) {
-        case 0: forces_batch<false, false, false>(sims, ctls, tiles, ntiles, s); break;
-        case 1: forces_batch<false, false, true>(sims, ctls, tiles, ntiles, s); break;
-        case 2: forces_batch<false, true, false>(sims, ctls, tiles, ntiles, s); break;
-        case 3: forces_batch<false, true, true>(sims, ctls, tiles, ntiles, s); break;
-        case 4: forces_batch<true, false, false>(sims, ctls, tiles, ntiles, s); break;
-        case 5: forces_batch<true, false, true>(sims, ctls, tiles, ntiles, s); break;
-        case 6: forces_batch<true, true, false>(sims, ctls, tiles, ntiles, s); break;
-        default: forces_batch<true, true, true>(sims, ctls, tiles, ntiles, s); break;
+        case 0: forces_batch<false, false, false>(descs, ctls, tiles, ntiles, s); break;
+        case 1: forces_batch<false, false, true>(descs, ctls, tiles, ntiles, s); break;
+        case 2: forces_batch<false, true, false>(descs, ctls, tiles, ntiles, s); break;
+        case 3: forces_batch<false, true, true>(descs, ctls, tiles, ntiles, s); break;
+        case 4: forces_batch<true, false, false>(descs, ctls, tiles, ntiles, s); break;
+        case 5: forces_batch<true, false, true>(descs, ctls, tiles, ntiles, s); break;
+        case 6: forces_batch<true, true, false>(descs, ctls, tiles, ntiles, s); break;
+        default: forces_batch<true, true, true>(descs, ctls, tiles, ntiles, s); break;
     }
     return cudaGetLastError();
 }
 
 template <bool USL, bool REINIT>
-static void particle_kinematics_batch(const SimDev* const* sims, Control* const* ctls,
+static void particle_kinematics_batch(const SimDev* descs, Control* const* ctls,
                                       const int4* tiles, int ntiles, cudaStream_t s) {
     prefer_shared(k_particle_kinematics_batch<USL, REINIT>);
-    k_particle_kinematics_batch<USL, REINIT><<<ntiles, TILE_THREADS, 0, s>>>(sims, ctls, tiles);
+    k_particle_kinematics_batch<USL, REINIT><<<ntiles, TILE_THREADS, 0, s>>>(descs, ctls, tiles);
 }
 
-cudaError_t launch_particle_kinematics_batch(const StepConfig& c, const SimDev* const* sims,
+cudaError_t launch_particle_kinematics_batch(const StepConfig& c, const SimDev* descs,
                                              Control* const* ctls, const int4* tiles, int ntiles,
                                              cudaStream_t s) {
     if (c.usl) {
-        if (c.reinit) particle_kinematics_batch<true, true>(sims, ctls, tiles, ntiles, s);
-        else particle_kinematics_batch<true, false>(sims, ctls, tiles, ntiles, s);
+        if (c.reinit) particle_kinematics_batch<true, true>(descs, ctls, tiles, ntiles, s);
+        else particle_kinematics_batch<true, false>(descs, ctls, tiles, ntiles, s);
     } else {
-        if (c.reinit) particle_kinematics_batch<false, true>(sims, ctls, tiles, ntiles, s);
-        else particle_kinematics_batch<false, false>(sims, ctls, tiles, ntiles, s);
+        if (c.reinit) particle_kinematics_batch<false, true>(descs, ctls, tiles, ntiles, s);
+        else particle_kinematics_batch<false, false>(descs, ctls, tiles, ntiles, s);
     }
     return cudaGetLastError();
 }

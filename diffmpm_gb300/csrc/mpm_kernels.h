@@ -26,13 +26,15 @@ cudaError_t launch_particle_kinematics(const StepConfig& c, const SimDev& S, con
 // The same three phases for a batch of simulations in one launch each: tile
 // t works on simulation tiles[t].x, whose descriptor is sims[tiles[t].x] and
 // whose step counter and status are in ctls[tiles[t].x].
-cudaError_t launch_nodal_kinematics_batch(const StepConfig& c, const SimDev* const* sims,
+// Copy *sims[i] to descs[i] for i < n.
+cudaError_t launch_gather_descs(const SimDev* const* sims, int n, SimDev* descs, cudaStream_t s);
+cudaError_t launch_nodal_kinematics_batch(const StepConfig& c, const SimDev* descs,
                                           Control* const* ctls, const int4* tiles, int ntiles,
                                           cudaStream_t s);
-cudaError_t launch_forces_batch(const StepConfig& c, const SimDev* const* sims,
+cudaError_t launch_forces_batch(const StepConfig& c, const SimDev* descs,
                                 Control* const* ctls, const int4* tiles, int ntiles,
                                 cudaStream_t s);
-cudaError_t launch_particle_kinematics_batch(const StepConfig& c, const SimDev* const* sims,
+cudaError_t launch_particle_kinematics_batch(const StepConfig& c, const SimDev* descs,
                                              Control* const* ctls, const int4* tiles, int ntiles,
                                              cudaStream_t s);
 
