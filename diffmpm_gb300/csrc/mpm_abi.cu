@@ -208,19 +208,22 @@ StepConfig step_config(const MpmHandle* h) {
     return c;
 }
 
-int launch_phase(MpmHandle* h, int phase, cudaStream_t s) {
+// One phase of step (ctl->step + k); phase 2 ends the step, whose counter the
+// caller advances.
+int launch_phase(MpmHandle* h, int phase, int k, cudaStream_t s) {
     const StepConfig c = step_config(h);
     cudaError_t e = cudaSuccess;
-    if (phase == 0) e = launch_nodal_kinematics(c, h->hs, h->dtiles, h->ntiles, h->ctl, s);
-    else if (phase == 1) e = launch_forces(c, h->hs, h->dtiles, h->ntiles, h->ctl, s);
-    else e = launch_particle_kinematics(c, h->hs, h->dtiles, h->ntiles, h->ctl, s);
+    if (phase == 0) e = launch_nodal_kinematics(c, h->hs, h->dtiles, h->ntiles, h->ctl, k, s);
+    else if (phase == 1) e = launch_forces(c, h->hs, h->dtiles, h->ntiles, h->ctl, k, s);
+    else e = launch_particle_kinematics(c, h->hs, h->dtiles, h->ntiles, h->ctl, k, s);
     CK(h, e);
     return MPM_OK;
 }
 
 int launch_steps(MpmHandle* h, int n, cudaStream_t s) {
     for (int i = 0; i < n; ++i)
-        for (int p = 0; p < 3; ++p) TRY(launch_phase(h, p, s));
+        for (int p = 0; p < 3; ++p) TRY(launch_phase(h, p, i, s));
+    CK(h, launch_advance_step(h->ctl, n, s));
     return MPM_OK;
 }
 
@@ -1073,8 +1076,9 @@ int mpm_run_phase(MpmHandle* h, int phase, void* stream) {
     if (h->ndim == 1) return fail(h, MPM_ERR_UNSUPPORTED, "single phases are not available in 1-D");
     cudaStream_t s = S(stream);
     if (phase == 0 && h->needs_resort) TRY(resort(h, s));
-    TRY(launch_phase(h, phase, s));
+    TRY(launch_phase(h, phase, 0, s));
     if (phase == 2) {
+        CK(h, launch_advance_step(h->ctl, 1, s));
         h->step++;
         TRY(read_ctl(h, s));
         int st = 0;
@@ -1172,7 +1176,8 @@ int mpm_time_phases(MpmHandle* h, int nsteps, float* ms_out, void* stream) {
     CK(h, cudaEventRecord(ev[0], s));
     for (int i = 0; i < nsteps && r == MPM_OK; ++i)
         for (int p = 0; p < 3 && r == MPM_OK; ++p) {
-            r = launch_phase(h, p, s);
+            r = launch_phase(h, p, 0, s);
+            if (r == MPM_OK && p == 2) CK(h, launch_advance_step(h->ctl, 1, s));
             if (r == MPM_OK) CK(h, cudaEventRecord(ev[3 * i + p + 1], s));
         }
     CK(h, cudaStreamSynchronize(s));

@@ -60,10 +60,11 @@ int launch_batch_steps(MpmBatch* b, int n, cudaStream_t s) {
     // descriptor without first loading a pointer to it
     BCK(b, launch_gather_descs(b->d_sims, (int)b->sims.size(), b->d_descs, s));
     for (int i = 0; i < n; ++i) {
-        BCK(b, launch_nodal_kinematics_batch(b->cfg, b->d_descs, b->d_ctls, b->d_tiles, b->ntiles, s));
-        BCK(b, launch_forces_batch(b->cfg, b->d_descs, b->d_ctls, b->d_tiles, b->ntiles, s));
-        BCK(b, launch_particle_kinematics_batch(b->cfg, b->d_descs, b->d_ctls, b->d_tiles, b->ntiles, s));
+        BCK(b, launch_nodal_kinematics_batch(b->cfg, b->d_descs, b->d_ctls, b->d_tiles, b->ntiles, i, s));
+        BCK(b, launch_forces_batch(b->cfg, b->d_descs, b->d_ctls, b->d_tiles, b->ntiles, i, s));
+        BCK(b, launch_particle_kinematics_batch(b->cfg, b->d_descs, b->d_ctls, b->d_tiles, b->ntiles, i, s));
     }
+    BCK(b, launch_advance_steps(b->d_ctls, (int)b->sims.size(), n, s));
     return MPM_OK;
 }
 

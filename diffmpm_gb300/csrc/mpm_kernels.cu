@@ -39,6 +39,28 @@ cudaError_t launch_gather_descs(const SimDev* const* sims, int n, SimDev* descs,
     return cudaGetLastError();
 }
 
+// The step counter advances once per launch sequence, after its last kernel:
+// the step kernels read step = counter + k (k their offset in the sequence).
+__global__ void k_advance_steps(Control* const* __restrict__ ctls, Control* __restrict__ one, int n,
+                                int by) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (one) {
+        if (i == 0) one->step += by;
+    } else if (i < n) {
+        ctls[i]->step += by;
+    }
+}
+
+cudaError_t launch_advance_steps(Control* const* ctls, int n, int by, cudaStream_t s) {
+    if (n > 0 && by != 0) k_advance_steps<<<(n + 127) / 128, 128, 0, s>>>(ctls, nullptr, n, by);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_advance_step(Control* ctl, int by, cudaStream_t s) {
+    if (by != 0) k_advance_steps<<<1, 32, 0, s>>>(nullptr, ctl, 1, by);
+    return cudaGetLastError();
+}
+
 __device__ __forceinline__ void load_sim(const SimDev* __restrict__ src, SimDev& dst) {
     static_assert(sizeof(SimDev) % 4 == 0, "descriptor copied in 4-byte words");
     const int* a = reinterpret_cast<const int*>(src);
@@ -417,13 +439,13 @@ constexpr int K1_NF = 5;   // x, y, vx, vy, rho (solve_jit) or mass (solve)
 
 template <bool REINIT>
 __device__ __forceinline__ void nodal_kinematics_tile(const SimDev& S, const int4 T,
-                                                      Control* __restrict__ ctl) {
+                                                      Control* __restrict__ ctl, int k) {
     constexpr int NQ = 12;
     __shared__ float s_c[NQ][SC_STRIDE];               // [m, px, py] x corner, per cell
     __shared__ float s_row[TILE_CY][K1_NF][ROW_P];     // staged particles of each cell row
     __shared__ int s_cs[TILE_CY][33];
     __shared__ TileGeo G;
-    const int parity = load_step(ctl) & 1;
+    const int parity = (load_step(ctl) + k) & 1;
     const int tid = threadIdx.x, lx = tid & (TILE_CX - 1), ly = tid / TILE_CX;
     const int c0x = T.y * TILE_NX - 1, c0y = T.z * TILE_NY - 1;
     const int ci = c0x + lx, cj = c0y + ly;
@@ -508,18 +530,18 @@ __device__ __forceinline__ void nodal_kinematics_tile(const SimDev& S, const int
 template <bool REINIT>
 __global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
 k_nodal_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
-                   Control* __restrict__ ctl) {
-    nodal_kinematics_tile<REINIT>(S, tiles[blockIdx.x], ctl);
+                   Control* __restrict__ ctl, int k) {
+    nodal_kinematics_tile<REINIT>(S, tiles[blockIdx.x], ctl, k);
 }
 
 template <bool REINIT>
 __global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
 k_nodal_kinematics_batch(const SimDev* __restrict__ descs, Control* const* __restrict__ ctls,
-                         const int4* __restrict__ tiles) {
+                         const int4* __restrict__ tiles, int k) {
     __shared__ SimDev sS;
     const int4 T = tiles[blockIdx.x];
     load_sim(descs + T.x, sS);
-    nodal_kinematics_tile<REINIT>(sS, T, ctls[T.x]);
+    nodal_kinematics_tile<REINIT>(sS, T, ctls[T.x], k);
 }
 
 // Nodal update shared by both schemes: concentrated forces (element.py:270-284),
@@ -565,7 +587,7 @@ constexpr int K2_ROW_P = 128;   // particles of a row per pass (two CTAs per SM)
 
 template <bool USL, bool REINIT, bool TRAC, bool VD>
 __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
-                                            Control* __restrict__ ctl) {
+                                            Control* __restrict__ ctl, int k) {
     constexpr int NQ = 8;
     __shared__ float s_c[NQ][SC_STRIDE];               // [f x, f y] x corner, per cell
     __shared__ float s_slot[TILE_CY][NQ][K2_ROW_P];    // contributions of a row's particles
@@ -574,7 +596,7 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
     __shared__ int s_cs[TILE_CY][33];
     __shared__ float2 s_v[NV_W * NV_H];   // nodal velocity after phase 1 of the tile's nodes
     __shared__ TileGeo G;
-    const int step = load_step(ctl);
+    const int step = load_step(ctl) + k;
     const int parity = step & 1;
     const float t = step_time(step, S.dt);
     const int tid = threadIdx.x, lx = tid & (TILE_CX - 1), ly = tid / TILE_CX;
@@ -693,18 +715,18 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
 template <bool USL, bool REINIT, bool TRAC>
 __global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
 k_forces(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
-         Control* __restrict__ ctl) {
-    forces_tile<USL, REINIT, TRAC, false>(S, tiles[blockIdx.x], ctl);
+         Control* __restrict__ ctl, int k) {
+    forces_tile<USL, REINIT, TRAC, false>(S, tiles[blockIdx.x], ctl, k);
 }
 
 template <bool USL, bool REINIT, bool TRAC>
 __global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
 k_forces_batch(const SimDev* __restrict__ descs, Control* const* __restrict__ ctls,
-               const int4* __restrict__ tiles) {
+               const int4* __restrict__ tiles, int k) {
     __shared__ SimDev sS;
     const int4 T = tiles[blockIdx.x];
     load_sim(descs + T.x, sS);
-    forces_tile<USL, REINIT, TRAC, true>(sS, T, ctls[T.x]);
+    forces_tile<USL, REINIT, TRAC, true>(sS, T, ctls[T.x], k);
 }
 
 // ---------------------------------------------------------------------------
@@ -743,7 +765,7 @@ struct G2PStage {
 
 template <bool USL, bool REINIT>
 __device__ __forceinline__ void particle_kinematics_tile(const SimDev& S, const int4 T,
-                                                         Control* __restrict__ ctl) {
+                                                         Control* __restrict__ ctl, int k) {
     constexpr int NF = G2PStage<USL>::NF, DEPTH = G2PStage<USL>::DEPTH;
     __shared__ float4 s_nd[G_W * G_H];    // nodal (vx, vy, ax, ay) of the tile's nodes
     __shared__ float s_stage[TILE_CY][DEPTH][NF][32];
@@ -753,7 +775,7 @@ __device__ __forceinline__ void particle_kinematics_tile(const SimDev& S, const 
     __shared__ int s_flag[TILE_CY][32];   // drift flag after this step
     __shared__ int s_status;
     __shared__ TileGeo G;
-    const int step = load_step(ctl);
+    const int step = load_step(ctl) + k;
     const int parity = step & 1, next = parity ^ 1;
     const int tid = threadIdx.x, lane = tid & 31, w = tid / 32;
     const int c0x = T.y * TILE_NX - 1, c0y = T.z * TILE_NY - 1;
@@ -946,34 +968,24 @@ __device__ __forceinline__ void particle_kinematics_tile(const SimDev& S, const 
     status = __reduce_or_sync(0xffffffffu, status);
     if (lane == 0 && status) atomicOr(&s_status, status);
     __syncthreads();
-    if (tid == 0) {
-        if (s_status) atomicOr(&ctl->status, s_status);
-        // last CTA to finish advances the step counter (every CTA has read it)
-        __threadfence();
-        const unsigned prev = atomicAdd(&ctl->done, 1u);
-        if (prev == (unsigned)(S.tiles_x * S.tiles_y) - 1u) {
-            ctl->done = 0u;
-            ctl->step = step + 1;
-            __threadfence();
-        }
-    }
+    if (tid == 0 && s_status) atomicOr(&ctl->status, s_status);
 }
 
 template <bool USL, bool REINIT>
 __global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
 k_particle_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
-                      Control* __restrict__ ctl) {
-    particle_kinematics_tile<USL, REINIT>(S, tiles[blockIdx.x], ctl);
+                      Control* __restrict__ ctl, int k) {
+    particle_kinematics_tile<USL, REINIT>(S, tiles[blockIdx.x], ctl, k);
 }
 
 template <bool USL, bool REINIT>
 __global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
 k_particle_kinematics_batch(const SimDev* __restrict__ descs, Control* const* __restrict__ ctls,
-                            const int4* __restrict__ tiles) {
+                            const int4* __restrict__ tiles, int k) {
     __shared__ SimDev sS;
     const int4 T = tiles[blockIdx.x];
     load_sim(descs + T.x, sS);
-    particle_kinematics_tile<USL, REINIT>(sS, T, ctls[T.x]);
+    particle_kinematics_tile<USL, REINIT>(sS, T, ctls[T.x], k);
 }
 
 // ---------------------------------------------------------------------------
@@ -993,57 +1005,57 @@ static void prefer_shared(K kernel) {
 
 template <bool REINIT>
 static void nodal_kinematics(const SimDev& S, const int4* tiles, int ntiles, Control* ctl,
-                             cudaStream_t s) {
+                             int k, cudaStream_t s) {
     prefer_shared(k_nodal_kinematics<REINIT>);
-    k_nodal_kinematics<REINIT><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl);
+    k_nodal_kinematics<REINIT><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl, k);
 }
 
 cudaError_t launch_nodal_kinematics(const StepConfig& c, const SimDev& S, const int4* tiles,
-                                    int ntiles, Control* ctl, cudaStream_t s) {
-    if (c.reinit) nodal_kinematics<true>(S, tiles, ntiles, ctl, s);
-    else nodal_kinematics<false>(S, tiles, ntiles, ctl, s);
+                                    int ntiles, Control* ctl, int k, cudaStream_t s) {
+    if (c.reinit) nodal_kinematics<true>(S, tiles, ntiles, ctl, k, s);
+    else nodal_kinematics<false>(S, tiles, ntiles, ctl, k, s);
     return cudaGetLastError();
 }
 
 template <bool USL, bool REINIT>
 static void forces_trac(bool trac, const SimDev& S, const int4* tiles, int ntiles, Control* ctl,
-                        cudaStream_t s) {
+                        int k, cudaStream_t s) {
     if (trac) {
         prefer_shared(k_forces<USL, REINIT, true>);
-        k_forces<USL, REINIT, true><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl);
+        k_forces<USL, REINIT, true><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl, k);
     } else {
         prefer_shared(k_forces<USL, REINIT, false>);
-        k_forces<USL, REINIT, false><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl);
+        k_forces<USL, REINIT, false><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl, k);
     }
 }
 
 cudaError_t launch_forces(const StepConfig& c, const SimDev& S, const int4* tiles, int ntiles,
-                          Control* ctl, cudaStream_t s) {
+                          Control* ctl, int k, cudaStream_t s) {
     if (c.usl) {
-        if (c.reinit) forces_trac<true, true>(c.traction, S, tiles, ntiles, ctl, s);
-        else forces_trac<true, false>(c.traction, S, tiles, ntiles, ctl, s);
+        if (c.reinit) forces_trac<true, true>(c.traction, S, tiles, ntiles, ctl, k, s);
+        else forces_trac<true, false>(c.traction, S, tiles, ntiles, ctl, k, s);
     } else {
-        if (c.reinit) forces_trac<false, true>(c.traction, S, tiles, ntiles, ctl, s);
-        else forces_trac<false, false>(c.traction, S, tiles, ntiles, ctl, s);
+        if (c.reinit) forces_trac<false, true>(c.traction, S, tiles, ntiles, ctl, k, s);
+        else forces_trac<false, false>(c.traction, S, tiles, ntiles, ctl, k, s);
     }
     return cudaGetLastError();
 }
 
 template <bool USL, bool REINIT>
 static void particle_kinematics(const SimDev& S, const int4* tiles, int ntiles, Control* ctl,
-                                cudaStream_t s) {
+                                int k, cudaStream_t s) {
     prefer_shared(k_particle_kinematics<USL, REINIT>);
-    k_particle_kinematics<USL, REINIT><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl);
+    k_particle_kinematics<USL, REINIT><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl, k);
 }
 
 cudaError_t launch_particle_kinematics(const StepConfig& c, const SimDev& S, const int4* tiles,
-                                       int ntiles, Control* ctl, cudaStream_t s) {
+                                       int ntiles, Control* ctl, int k, cudaStream_t s) {
     if (c.usl) {
-        if (c.reinit) particle_kinematics<true, true>(S, tiles, ntiles, ctl, s);
-        else particle_kinematics<true, false>(S, tiles, ntiles, ctl, s);
+        if (c.reinit) particle_kinematics<true, true>(S, tiles, ntiles, ctl, k, s);
+        else particle_kinematics<true, false>(S, tiles, ntiles, ctl, k, s);
     } else {
-        if (c.reinit) particle_kinematics<false, true>(S, tiles, ntiles, ctl, s);
-        else particle_kinematics<false, false>(S, tiles, ntiles, ctl, s);
+        if (c.reinit) particle_kinematics<false, true>(S, tiles, ntiles, ctl, k, s);
+        else particle_kinematics<false, false>(S, tiles, ntiles, ctl, k, s);
     }
     return cudaGetLastError();
 }
@@ -1051,59 +1063,59 @@ cudaError_t launch_particle_kinematics(const StepConfig& c, const SimDev& S, con
 // Batched launches: one grid over the tiles of every simulation of a batch.
 template <bool REINIT>
 static void nodal_kinematics_batch(const SimDev* descs, Control* const* ctls,
-                                   const int4* tiles, int ntiles, cudaStream_t s) {
+                                   const int4* tiles, int ntiles, int k, cudaStream_t s) {
     prefer_shared(k_nodal_kinematics_batch<REINIT>);
-    k_nodal_kinematics_batch<REINIT><<<ntiles, TILE_THREADS, 0, s>>>(descs, ctls, tiles);
+    k_nodal_kinematics_batch<REINIT><<<ntiles, TILE_THREADS, 0, s>>>(descs, ctls, tiles, k);
 }
 
 cudaError_t launch_nodal_kinematics_batch(const StepConfig& c, const SimDev* descs,
                                           Control* const* ctls, const int4* tiles, int ntiles,
-                                          cudaStream_t s) {
-    if (c.reinit) nodal_kinematics_batch<true>(descs, ctls, tiles, ntiles, s);
-    else nodal_kinematics_batch<false>(descs, ctls, tiles, ntiles, s);
+                                          int k, cudaStream_t s) {
+    if (c.reinit) nodal_kinematics_batch<true>(descs, ctls, tiles, ntiles, k, s);
+    else nodal_kinematics_batch<false>(descs, ctls, tiles, ntiles, k, s);
     return cudaGetLastError();
 }
 
 template <bool USL, bool REINIT, bool TRAC>
 static void forces_batch(const SimDev* descs, Control* const* ctls, const int4* tiles,
-                         int ntiles, cudaStream_t s) {
+                         int ntiles, int k, cudaStream_t s) {
     prefer_shared(k_forces_batch<USL, REINIT, TRAC>);
-    k_forces_batch<USL, REINIT, TRAC><<<ntiles, TILE_THREADS, 0, s>>>(descs, ctls, tiles);
+    k_forces_batch<USL, REINIT, TRAC><<<ntiles, TILE_THREADS, 0, s>>>(descs, ctls, tiles, k);
 }
 
 cudaError_t launch_forces_batch(const StepConfig& c, const SimDev* descs,
                                 Control* const* ctls, const int4* tiles, int ntiles,
-                                cudaStream_t s) {
+                                int k, cudaStream_t s) {
     const int key = (c.usl ? 4 : 0) | (c.reinit ? 2 : 0) | (c.traction ? 1 : 0);
     switch (key) {
-        case 0: forces_batch<false, false, false>(descs, ctls, tiles, ntiles, s); break;
-        case 1: forces_batch<false, false, true>(descs, ctls, tiles, ntiles, s); break;
-        case 2: forces_batch<false, true, false>(descs, ctls, tiles, ntiles, s); break;
-        case 3: forces_batch<false, true, true>(descs, ctls, tiles, ntiles, s); break;
-        case 4: forces_batch<true, false, false>(descs, ctls, tiles, ntiles, s); break;
-        case 5: forces_batch<true, false, true>(descs, ctls, tiles, ntiles, s); break;
-        case 6: forces_batch<true, true, false>(descs, ctls, tiles, ntiles, s); break;
-        default: forces_batch<true, true, true>(descs, ctls, tiles, ntiles, s); break;
+        case 0: forces_batch<false, false, false>(descs, ctls, tiles, ntiles, k, s); break;
+        case 1: forces_batch<false, false, true>(descs, ctls, tiles, ntiles, k, s); break;
+        case 2: forces_batch<false, true, false>(descs, ctls, tiles, ntiles, k, s); break;
+        case 3: forces_batch<false, true, true>(descs, ctls, tiles, ntiles, k, s); break;
+        case 4: forces_batch<true, false, false>(descs, ctls, tiles, ntiles, k, s); break;
+        case 5: forces_batch<true, false, true>(descs, ctls, tiles, ntiles, k, s); break;
+        case 6: forces_batch<true, true, false>(descs, ctls, tiles, ntiles, k, s); break;
+        default: forces_batch<true, true, true>(descs, ctls, tiles, ntiles, k, s); break;
     }
     return cudaGetLastError();
 }
 
 template <bool USL, bool REINIT>
 static void particle_kinematics_batch(const SimDev* descs, Control* const* ctls,
-                                      const int4* tiles, int ntiles, cudaStream_t s) {
+                                      const int4* tiles, int ntiles, int k, cudaStream_t s) {
     prefer_shared(k_particle_kinematics_batch<USL, REINIT>);
-    k_particle_kinematics_batch<USL, REINIT><<<ntiles, TILE_THREADS, 0, s>>>(descs, ctls, tiles);
+    k_particle_kinematics_batch<USL, REINIT><<<ntiles, TILE_THREADS, 0, s>>>(descs, ctls, tiles, k);
 }
 
 cudaError_t launch_particle_kinematics_batch(const StepConfig& c, const SimDev* descs,
                                              Control* const* ctls, const int4* tiles, int ntiles,
-                                             cudaStream_t s) {
+                                             int k, cudaStream_t s) {
     if (c.usl) {
-        if (c.reinit) particle_kinematics_batch<true, true>(descs, ctls, tiles, ntiles, s);
-        else particle_kinematics_batch<true, false>(descs, ctls, tiles, ntiles, s);
+        if (c.reinit) particle_kinematics_batch<true, true>(descs, ctls, tiles, ntiles, k, s);
+        else particle_kinematics_batch<true, false>(descs, ctls, tiles, ntiles, k, s);
     } else {
-        if (c.reinit) particle_kinematics_batch<false, true>(descs, ctls, tiles, ntiles, s);
-        else particle_kinematics_batch<false, false>(descs, ctls, tiles, ntiles, s);
+        if (c.reinit) particle_kinematics_batch<false, true>(descs, ctls, tiles, ntiles, k, s);
+        else particle_kinematics_batch<false, false>(descs, ctls, tiles, ntiles, k, s);
     }
     return cudaGetLastError();
 }

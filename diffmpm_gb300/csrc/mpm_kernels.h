@@ -17,11 +17,15 @@ struct StepConfig {
 // passed by value (a __grid_constant__ kernel parameter), so a captured graph
 // holds the descriptor current at capture time.
 cudaError_t launch_nodal_kinematics(const StepConfig& c, const SimDev& S, const int4* tiles,
-                                    int ntiles, Control* ctl, cudaStream_t s);
+                                    int ntiles, Control* ctl, int k, cudaStream_t s);
 cudaError_t launch_forces(const StepConfig& c, const SimDev& S, const int4* tiles, int ntiles,
-                          Control* ctl, cudaStream_t s);
+                          Control* ctl, int k, cudaStream_t s);
 cudaError_t launch_particle_kinematics(const StepConfig& c, const SimDev& S, const int4* tiles,
-                                       int ntiles, Control* ctl, cudaStream_t s);
+                                       int ntiles, Control* ctl, int k, cudaStream_t s);
+// The kernels above work on step (ctl->step + k); these advance the counter
+// once a sequence of steps has been launched.
+cudaError_t launch_advance_step(Control* ctl, int by, cudaStream_t s);
+cudaError_t launch_advance_steps(Control* const* ctls, int n, int by, cudaStream_t s);
 
 // The same three phases for a batch of simulations in one launch each: tile
 // t works on simulation tiles[t].x, whose descriptor is sims[tiles[t].x] and
@@ -30,13 +34,13 @@ cudaError_t launch_particle_kinematics(const StepConfig& c, const SimDev& S, con
 cudaError_t launch_gather_descs(const SimDev* const* sims, int n, SimDev* descs, cudaStream_t s);
 cudaError_t launch_nodal_kinematics_batch(const StepConfig& c, const SimDev* descs,
                                           Control* const* ctls, const int4* tiles, int ntiles,
-                                          cudaStream_t s);
+                                          int k, cudaStream_t s);
 cudaError_t launch_forces_batch(const StepConfig& c, const SimDev* descs,
                                 Control* const* ctls, const int4* tiles, int ntiles,
-                                cudaStream_t s);
+                                int k, cudaStream_t s);
 cudaError_t launch_particle_kinematics_batch(const StepConfig& c, const SimDev* descs,
                                              Control* const* ctls, const int4* tiles, int ntiles,
-                                             cudaStream_t s);
+                                             int k, cudaStream_t s);
 
 // Re-sort of one simulation's particles by current cell, stable in storage order.
 struct SortScratch {

@@ -91,9 +91,9 @@ struct SimDev {
 
 // Per-batch control block.
 struct Control {
-    int step;              // step counter i (t = i * dt)
+    int step;              // step counter i (t = i * dt) at the start of the launched sequence
     int status;            // StatusBits
-    unsigned int done;     // finished-block counter of the last-block pattern
+    unsigned int done;     // reserved (zero)
     int pad;
 };
 
