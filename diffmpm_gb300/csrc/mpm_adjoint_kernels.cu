@@ -114,38 +114,28 @@ __device__ __forceinline__ void g2p_seeds(const AdjStep& A, int q, float& gx, fl
 // tape's drift flags and visit_tape_cell.  Tiles with no stored particle in
 // reach only write their nodes (all sums zero).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ bool rev_occupied(const AdjStep& A, int x0, int x1, int y0, int y1) {
-    x0 = max(x0, 0);
-    x1 = min(x1, A.nx);
-    y0 = max(y0, 0);
-    y1 = min(y1, A.ny);
-    int any = 0;
+
+// Tile set-up of the reverse node passes with every load issued before any is
+// consumed (one round trip): this thread's storage start of row cj (cs, and
+// cs32 for lane 0), and its shares of two block-wide ORs: a particle is stored
+// in the sort-cells around the tile (occ), one of them has a drift flag (drift).
+__device__ __forceinline__ void rev_tile_loads(const AdjStep& A, int c0x, int c0y, int cj, int lane,
+                                               int& cs, int& cs32, int& occ, int& drift) {
+    cs = cs32 = occ = drift = 0;
+    if (cj >= 0 && cj < A.ny) {
+        const int base = cj * A.nx;
+        cs = A.cstart[base + min(max(c0x + lane, 0), A.nx)];
+        if (lane == 0) cs32 = A.cstart[base + min(max(c0x + 32, 0), A.nx)];
+    }
+    const int x0 = max(c0x - 1, 0), x1 = min(c0x + TILE_CX + 1, A.nx);
+    const int y0 = max(c0y - 1, 0), y1 = min(c0y + TILE_CY + 1, A.ny);
     if (x0 < x1)
         for (int r = y0 + (int)threadIdx.x; r < y1; r += blockDim.x)
-            any |= A.cstart[r * A.nx + x1] != A.cstart[r * A.nx + x0];
-    return __syncthreads_or(any) != 0;
-}
-
-__device__ __forceinline__ bool rev_drifted(const AdjStep& A, int c0x, int c0y) {
-    int any = 0;
+            occ |= A.cstart[r * A.nx + x1] != A.cstart[r * A.nx + x0];
     for (int idx = threadIdx.x; idx < (TILE_CX + 2) * (TILE_CY + 2); idx += blockDim.x) {
         const int si = c0x - 1 + idx % (TILE_CX + 2), sj = c0y - 1 + idx / (TILE_CX + 2);
-        if (si >= 0 && si < A.nx && sj >= 0 && sj < A.ny) any |= A.cflag[sj * A.nx + si];
+        if (si >= 0 && si < A.nx && sj >= 0 && sj < A.ny) drift |= A.cflag[sj * A.nx + si];
     }
-    return __syncthreads_or(any) != 0;
-}
-
-// Storage starts of the 33 sort-cells c0x .. c0x+32 of row cj (clamped).
-__device__ __forceinline__ void rev_row_starts(const AdjStep& A, int c0x, int cj, int* cs,
-                                               int lane) {
-    if (cj < 0 || cj >= A.ny) {
-        cs[lane] = 0;
-        if (lane == 0) cs[32] = 0;
-        return;
-    }
-    const int base = cj * A.nx;
-    cs[lane] = A.cstart[base + min(max(c0x + lane, 0), A.nx)];
-    if (lane == 0) cs[32] = A.cstart[base + min(max(c0x + 32, 0), A.nx)];
 }
 
 // Reverse nodal update of node n from the G2P adjoint sums (vB-bar, aB-bar):
@@ -190,9 +180,12 @@ __device__ __forceinline__ void rev_nodal_update_tile(const AdjStep& A, const in
     const int node = (c0y + 1 + ty) * (A.nx + 1) + c0x + 1 + tx;
     const bool own_cell = tx >= 1 && ty >= 1 && ci < A.nx && cj < A.ny;
     float sum[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-    if (rev_occupied(A, c0x - 1, c0x + TILE_CX + 1, c0y - 1, c0y + TILE_CY + 1)) {
-        rev_row_starts(A, c0x, cj, s_cs[ty], tx);
-        const bool slow = rev_drifted(A, c0x, c0y);   // (also a block barrier)
+    int L_cs, L_cs32, L_occ, L_drift;
+    rev_tile_loads(A, c0x, c0y, cj, tx, L_cs, L_cs32, L_occ, L_drift);
+    s_cs[ty][tx] = L_cs;
+    if (tx == 0) s_cs[ty][32] = L_cs32;
+    if (__syncthreads_or(L_occ)) {
+        const bool slow = __syncthreads_or(L_drift) != 0;
         const bool in_mesh = ci >= 0 && ci < A.nx && cj >= 0 && cj < A.ny;
         const CellGeo g = cell_geo(ci, cj, A.hx, A.hy);
         float acc[NQ];
@@ -464,9 +457,12 @@ __device__ __forceinline__ void rev_nodal_kinematics_tile(const AdjStep& A, cons
     const bool node_ok = tx < TILE_NX && ty < TILE_NY && c0x + 1 + tx <= A.nx && c0y + 1 + ty <= A.ny;
     const int node = (c0y + 1 + ty) * (A.nx + 1) + c0x + 1 + tx;
     float sx = 0.0f, sy = 0.0f;
-    if (rev_occupied(A, c0x - 1, c0x + TILE_CX + 1, c0y - 1, c0y + TILE_CY + 1)) {
-        rev_row_starts(A, c0x, cj, s_cs[ty], tx);
-        const bool slow = rev_drifted(A, c0x, c0y);   // (also a block barrier)
+    int L_cs, L_cs32, L_occ, L_drift;
+    rev_tile_loads(A, c0x, c0y, cj, tx, L_cs, L_cs32, L_occ, L_drift);
+    s_cs[ty][tx] = L_cs;
+    if (tx == 0) s_cs[ty][32] = L_cs32;
+    if (__syncthreads_or(L_occ)) {
+        const bool slow = __syncthreads_or(L_drift) != 0;
         const bool in_mesh = ci >= 0 && ci < A.nx && cj >= 0 && cj < A.ny;
         const CellGeo g = cell_geo(ci, cj, A.hx, A.hy);
         float Gcx[4], Gcy[4];

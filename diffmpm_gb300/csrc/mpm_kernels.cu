@@ -201,20 +201,6 @@ __device__ __forceinline__ CellGeo geo_of(const TileGeo& G, int kc, int kr) {
     return g;
 }
 
-// Load the 33 cell starts of row cj for cells c0x .. c0x+32 (clamped to the
-// mesh so that cells outside it have empty ranges) into cs[0..32].
-__device__ __forceinline__ void load_row_starts(const SimDev& S, int c0x, int cj, int* cs,
-                                                int lane) {
-    if (cj < 0 || cj >= S.ny) {
-        cs[lane] = 0;
-        if (lane == 0) cs[32] = 0;
-        return;
-    }
-    const int base = cj * S.nx;
-    const int col = min(max(c0x + lane, 0), S.nx);
-    cs[lane] = S.cstart[base + col];
-    if (lane == 0) cs[32] = S.cstart[base + min(max(c0x + 32, 0), S.nx)];
-}
 
 // The cell l in [0, last] whose range [cs[l], cs[l+1]) holds storage index q
 // (the last l with cs[l] <= q; q lies in [cs[0], cs[last+1])).
@@ -229,31 +215,36 @@ __device__ __forceinline__ int cell_of(const int* cs, int last, int q) {
     return lo;
 }
 
-// True when any sort-cell around the tile has its drift flag set.
-__device__ __forceinline__ bool tile_drifted(const SimDev& S, int c0x, int c0y) {
-    int any = 0;
+// The tile set-up loads, all issued before any is consumed so that they cost
+// one round trip: the storage starts of the tile's cell row cj (lane l: column
+// c0x + l, lane 0 also column c0x + 32), whether a particle is stored in the
+// sort-cells [c0x-1, c0x+33) x [c0y-1, c0y+17) (a particle is at most one
+// cell from its sort-cell, so when the cells of a tile and the ring of cells
+// around them store no particle, no particle is in the tile's cells), and
+// whether any of them has its drift flag set (the tile then takes the
+// gathering path).
+struct TileLoads {
+    int cs, cs32;     // row starts
+    int occ, drift;   // this thread's share of the two block-wide ORs
+};
+
+__device__ __forceinline__ TileLoads tile_loads(const SimDev& S, int c0x, int c0y, int cj, int lane) {
+    TileLoads L{0, 0, 0, 0};
+    if (cj >= 0 && cj < S.ny) {
+        const int base = cj * S.nx;
+        L.cs = S.cstart[base + min(max(c0x + lane, 0), S.nx)];
+        if (lane == 0) L.cs32 = S.cstart[base + min(max(c0x + 32, 0), S.nx)];
+    }
+    const int x0 = max(c0x - 1, 0), x1 = min(c0x + TILE_CX + 1, S.nx);
+    const int y0 = max(c0y - 1, 0), y1 = min(c0y + TILE_CY + 1, S.ny);
+    if (x0 < x1)
+        for (int r = y0 + (int)threadIdx.x; r < y1; r += TILE_THREADS)
+            L.occ |= S.cstart[r * S.nx + x1] != S.cstart[r * S.nx + x0];
     for (int idx = threadIdx.x; idx < HALO_W * HALO_H; idx += TILE_THREADS) {
         const int si = c0x - 1 + idx % HALO_W, sj = c0y - 1 + idx / HALO_W;
-        if (si >= 0 && si < S.nx && sj >= 0 && sj < S.ny) any |= S.cflag[sj * S.nx + si];
+        if (si >= 0 && si < S.nx && sj >= 0 && sj < S.ny) L.drift |= S.cflag[sj * S.nx + si];
     }
-    return __syncthreads_or(any) != 0;
-}
-
-// True when a particle is stored in the sort-cells [x0, x1) x [y0, y1)
-// (clamped to the mesh); also a block barrier.  A particle is at most one
-// cell from its sort-cell, so when the cells of a tile and the ring of cells
-// around them store no particle, no particle is in the tile's cells.
-__device__ __forceinline__ bool sort_cells_occupied(const SimDev& S, int x0, int x1, int y0,
-                                                    int y1) {
-    x0 = max(x0, 0);
-    x1 = min(x1, S.nx);
-    y0 = max(y0, 0);
-    y1 = min(y1, S.ny);
-    int any = 0;
-    if (x0 < x1)
-        for (int r = y0 + (int)threadIdx.x; r < y1; r += blockDim.x)
-            any |= S.cstart[r * S.nx + x1] != S.cstart[r * S.nx + x0];
-    return __syncthreads_or(any) != 0;
+    return L;
 }
 
 // Per-warp staging of the chunks of a row: chunk c of [rb, re) holds storage
@@ -453,7 +444,13 @@ __device__ __forceinline__ void nodal_kinematics_tile(const SimDev& S, const int
     const bool node_ok = lx < TILE_NX && ly < TILE_NY && c0x + 1 + lx <= S.nx && c0y + 1 + ly <= S.ny;
     const int node = (c0y + 1 + ly) * (S.nx + 1) + c0x + 1 + lx;
     const uint16_t ncons = node_ok ? S.ncons[node] : 0;   // node-phase input, fetched early
-    if (!sort_cells_occupied(S, c0x - 1, c0x + TILE_CX + 1, c0y - 1, c0y + TILE_CY + 1)) {
+    const TileLoads L = tile_loads(S, c0x, c0y, cj, lx);
+    build_geo(S, c0x, c0y, G);
+    #pragma unroll
+    for (int q = 0; q < NQ; ++q) s_c[q][tid] = 0.0f;
+    s_cs[ly][lx] = L.cs;
+    if (lx == 0) s_cs[ly][32] = L.cs32;
+    if (!__syncthreads_or(L.occ)) {
         // no particle in the tile: every node is massless and keeps its
         // velocity (the node phase below with all sums zero)
         if (node_ok) {
@@ -465,11 +462,7 @@ __device__ __forceinline__ void nodal_kinematics_tile(const SimDev& S, const int
         }
         return;
     }
-    #pragma unroll
-    for (int k = 0; k < NQ; ++k) s_c[k][tid] = 0.0f;
-    load_row_starts(S, c0x, cj, s_cs[ly], lx);
-    build_geo(S, c0x, c0y, G);
-    const bool slow = tile_drifted(S, c0x, c0y);   // (also a block barrier)
+    const bool slow = __syncthreads_or(L.drift) != 0;
 
     if (!slow) {
         const int* cs = s_cs[ly];
@@ -607,26 +600,35 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
     // node-phase inputs, fetched early
     const float nmass = node_ok ? S.nm[node] : 0.0f;
     const uint16_t ncons = node_ok ? S.ncons[node] : 0;
-    if (!sort_cells_occupied(S, c0x - 1, c0x + TILE_CX + 1, c0y - 1, c0y + TILE_CY + 1)) {
+    // the node tile (two entries per thread at most) and the tile set-up in
+    // one round trip
+    static_assert(NV_W * NV_H <= 2 * TILE_THREADS, "two node-tile entries per thread");
+    float2 nv[2];
+    #pragma unroll
+    for (int e = 0; e < 2; ++e) {
+        const int idx = tid + e * TILE_THREADS;
+        const int I = c0x + idx % NV_W, J = c0y + idx / NV_W;
+        nv[e] = make_float2(0.0f, 0.0f);
+        if (idx < NV_W * NV_H && I >= 0 && I <= S.nx && J >= 0 && J <= S.ny) {
+            const int n = J * (S.nx + 1) + I;
+            nv[e] = make_float2(S.nvax[n], S.nvay[n]);
+        }
+    }
+    const TileLoads L = tile_loads(S, c0x, c0y, cj, lx);
+    build_geo(S, c0x, c0y, G);
+    #pragma unroll
+    for (int q = 0; q < NQ; ++q) s_c[q][tid] = 0.0f;
+    s_cs[ly][lx] = L.cs;
+    if (lx == 0) s_cs[ly][32] = L.cs32;
+    #pragma unroll
+    for (int e = 0; e < 2; ++e)
+        if (tid + e * TILE_THREADS < NV_W * NV_H) s_v[tid + e * TILE_THREADS] = nv[e];
+    if (!__syncthreads_or(L.occ)) {
         // no particle in the tile: the nodal update with zero particle forces
         if (node_ok) nodal_update<VD>(S, node, t, 0.0f, 0.0f, S.nvax[node], S.nvay[node], nmass, ncons);
         return;
     }
-    #pragma unroll
-    for (int k = 0; k < NQ; ++k) s_c[k][tid] = 0.0f;
-    load_row_starts(S, c0x, cj, s_cs[ly], lx);
-    build_geo(S, c0x, c0y, G);
-    for (int idx = tid; idx < NV_W * NV_H; idx += TILE_THREADS) {
-        const int I = c0x + idx % NV_W, J = c0y + idx / NV_W;
-        float vx = 0.0f, vy = 0.0f;
-        if (I >= 0 && I <= S.nx && J >= 0 && J <= S.ny) {
-            const int n = J * (S.nx + 1) + I;
-            vx = S.nvax[n];
-            vy = S.nvay[n];
-        }
-        s_v[idx] = make_float2(vx, vy);
-    }
-    const bool slow = tile_drifted(S, c0x, c0y);   // (also a block barrier)
+    const bool slow = __syncthreads_or(L.drift) != 0;
 
     auto cell_velocities = [&](int li, int lj, float* vx, float* vy) {
         const int a = lj * NV_W + li;
@@ -816,19 +818,26 @@ __device__ __forceinline__ void particle_kinematics_tile(const SimDev& S, const 
     if (tid == 0) s_status = 0;
     // a tile whose rows store no particle only clears its drift flags
     const bool occupied = __syncthreads_or(re > rb) != 0;
-    for (int idx = tid; occupied && idx < G_W * G_H; idx += TILE_THREADS) {
-        const int I = c0x + idx % G_W, J = c0y + idx / G_W;
-        float vx = 0.0f, vy = 0.0f, ax = 0.0f, ay = 0.0f;
-        if (I >= 0 && I <= S.nx && J >= 0 && J <= S.ny) {
-            const int n = J * (S.nx + 1) + I;
-            vx = S.nvbx[n];
-            vy = S.nvby[n];
-            ax = S.nax[n];
-            ay = S.nay[n];
+    if (occupied) {
+        // the node tile, both entries of a thread in flight together (and in
+        // flight with the rows' first chunks)
+        static_assert(G_W * G_H <= 2 * TILE_THREADS, "two node-tile entries per thread");
+        float4 nd[2];
+        #pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const int idx = tid + e * TILE_THREADS;
+            const int I = c0x + idx % G_W, J = c0y + idx / G_W;
+            nd[e] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (idx < G_W * G_H && I >= 0 && I <= S.nx && J >= 0 && J <= S.ny) {
+                const int n = J * (S.nx + 1) + I;
+                nd[e] = make_float4(S.nvbx[n], S.nvby[n], S.nax[n], S.nay[n]);
+            }
         }
-        s_nd[idx] = make_float4(vx, vy, ax, ay);
+        build_geo(S, c0x, c0y, G);
+        #pragma unroll
+        for (int e = 0; e < 2; ++e)
+            if (tid + e * TILE_THREADS < G_W * G_H) s_nd[tid + e * TILE_THREADS] = nd[e];
     }
-    if (occupied) build_geo(S, c0x, c0y, G);
     if (row_ok && lane < TILE_NX) {
         // storage index rb + j of the row holds a particle of sort-cell s_map[j]
         const int lo = s_cs[w][lane] - rb, hi = min(s_cs[w][lane + 1] - rb, G2P_MAP);
