@@ -255,9 +255,8 @@ k_rev_nodal_update_batch(const AdjStep* __restrict__ table, const int4* __restri
 // Pass 2: reverse of the forces (element.py:236-268, 842-901) and of the USF
 // strain / volume / stress update (particle.py:249-327, material.py:113-131).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q) {
+__device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q, float x, float y) {
     if (q >= A.np) return;
-    const float x = A.x[q], y = A.y[q];
     int ci, cj;
     particle_cell(A, x, y, ci, cj);
     const CellGeo g = cell_geo(ci, cj, A.hx, A.hy);
@@ -411,7 +410,8 @@ __device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q) {
 
 __global__ void __launch_bounds__(PART_THREADS, 4)
 k_rev_forces(const __grid_constant__ AdjStep A) {
-    rev_forces_at(A, blockIdx.x * blockDim.x + threadIdx.x);
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < A.np) rev_forces_at(A, q, A.x[q], A.y[q]);
 }
 
 __global__ void __launch_bounds__(PART_THREADS, 4)
@@ -420,7 +420,10 @@ k_rev_forces_batch(const AdjStep* __restrict__ table, const int2* __restrict__ b
     const int2 bm = blocks[blockIdx.x];
     load_step_args(table + bm.x, sA);
     #pragma unroll 1
-    for (int k = 0; k < ADJ_ITER; ++k) rev_forces_at(sA, (bm.y * ADJ_ITER + k) * PART_THREADS + threadIdx.x);
+    for (int k = 0; k < ADJ_ITER; ++k) {
+        const int q = (bm.y * ADJ_ITER + k) * PART_THREADS + threadIdx.x;
+        if (q < sA.np) rev_forces_at(sA, q, sA.x[q], sA.y[q]);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -519,9 +522,8 @@ k_rev_nodal_kinematics_batch(const AdjStep* __restrict__ table, const int4* __re
 // Pass 4: reverse of the mass and momentum P2G (element.py:122-189) and of
 // m = V0 rho (particle.py:158-178).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void rev_mass_momentum_at(const AdjStep& A, int q) {
+__device__ __forceinline__ void rev_mass_momentum_at(const AdjStep& A, int q, float x, float y) {
     if (q >= A.np) return;
-    const float x = A.x[q], y = A.y[q];
     int ci, cj;
     particle_cell(A, x, y, ci, cj);
     const CellGeo g = cell_geo(ci, cj, A.hx, A.hy);
@@ -558,7 +560,8 @@ __device__ __forceinline__ void rev_mass_momentum_at(const AdjStep& A, int q) {
 
 __global__ void __launch_bounds__(PART_THREADS)
 k_rev_mass_momentum(const __grid_constant__ AdjStep A) {
-    rev_mass_momentum_at(A, blockIdx.x * blockDim.x + threadIdx.x);
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < A.np) rev_mass_momentum_at(A, q, A.x[q], A.y[q]);
 }
 
 __global__ void __launch_bounds__(PART_THREADS)
@@ -566,9 +569,17 @@ k_rev_mass_momentum_batch(const AdjStep* __restrict__ table, const int2* __restr
     __shared__ AdjStep sA;
     const int2 bm = blocks[blockIdx.x];
     load_step_args(table + bm.x, sA);
-    #pragma unroll 1
+    // the positions of all the block's chunks in flight at once
+    float x[ADJ_ITER], y[ADJ_ITER];
+    #pragma unroll
+    for (int k = 0; k < ADJ_ITER; ++k) {
+        const int q = (bm.y * ADJ_ITER + k) * PART_THREADS + threadIdx.x;
+        x[k] = q < sA.np ? sA.x[q] : 0.0f;
+        y[k] = q < sA.np ? sA.y[q] : 0.0f;
+    }
+    #pragma unroll
     for (int k = 0; k < ADJ_ITER; ++k)
-        rev_mass_momentum_at(sA, (bm.y * ADJ_ITER + k) * PART_THREADS + threadIdx.x);
+        rev_mass_momentum_at(sA, (bm.y * ADJ_ITER + k) * PART_THREADS + threadIdx.x, x[k], y[k]);
 }
 
 __global__ void k_copy_f32(const __grid_constant__ CopyJob j) {
