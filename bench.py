@@ -66,6 +66,18 @@ def parse():
     return ap.parse_args()
 
 
+def max_over_ranks(value, world, device="cpu"):
+    """The largest of every rank's ``value`` (the job's time is its slowest
+    rank's); ``value`` itself when there is one rank."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -411,12 +423,7 @@ def run_ours(args, world, rank, local):
     e3.record()
     torch.cuda.synchronize()
     rec_ms, adj_ms = e0.elapsed_time(e1), e2.elapsed_time(e3)
-    fa_ms = rec_ms + adj_ms
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([fa_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        fa_ms = float(t.item())
+    fa_ms = max_over_ranks(rec_ms + adj_ms, world, device="cuda")
     dLdE = [float(g["youngs_modulus"].astype(np.float64).sum()) for g in grads]
     # batched forward only
     reset_batch(members)

@@ -102,3 +102,15 @@ def test_missing_material_property_raises_key_error():
     import diffmpm_gb300 as D
     with pytest.raises(KeyError):
         D.LinearElastic({"density": 1, "youngs_modulus": 1})
+
+
+def test_create_rejects_meshes_beyond_the_node_index_range(built):
+    from diffmpm_gb300 import _lib
+    lib = _lib.load()
+    d = _lib.MpmDesc()
+    d.ndim = 2
+    d.nelements[0] = d.nelements[1] = 40000     # 1.6e9 nodes > 2^30
+    d.el_len[0] = d.el_len[1] = 1.0
+    h = ctypes.c_void_p()
+    assert lib.mpm_create(ctypes.byref(d), ctypes.byref(h)) == 1
+    assert b"too large" in lib.mpm_last_error(None)
