@@ -488,8 +488,15 @@ def run_ours(args, world, rank, local):
     value = world * ps / (fa_ms / 1000.0)
     # kernels of ours launched in the timed region (record + adjoint)
     nseg = (K + ckpt - 1) // ckpt
-    launches = (3 * K + 2 * ((K + block - 1) // block) + (nseg + 1)        # record
-                + nseg * 6 + K * (5 + 5)                                  # adjoint re-run + reverse
+    # record: 3 step kernels per step; per block a descriptor copy, a counter
+    # advance, a snapshot copy and a status gather; a checkpoint copy per
+    # segment.  adjoint: per step the 3 step kernels, a descriptor copy, a
+    # counter advance, 2 tape copies, the argument table and 4 reverse passes;
+    # per segment a restore, a check and the block-map set-up.  re-sorts: 9
+    # kernels each (counted over the record and the forward alone: halved).
+    nblk = (K + block - 1) // block
+    launches = (3 * K + 4 * nblk + (nseg + 1)
+                + K * (3 + 2 + 2 + 1 + 4) + nseg * 6
                 + 9 * counters["resorts"] // 2)
     if rank == 0:
         print(json.dumps({
