@@ -56,13 +56,13 @@ void drop_batch_graphs(MpmBatch* b) {
 
 int launch_batch_steps(MpmBatch* b, int n, cudaStream_t s) {
     // the descriptors change only between step blocks (re-sorts, set-up calls):
-    // one contiguous copy per block lets a CTA fetch its simulation's
-    // descriptor without first loading a pointer to it
-    BCK(b, launch_gather_descs(b->d_sims, (int)b->sims.size(), b->d_descs, s));
+    // one copy per tile and block lets a CTA fetch its tile, descriptor and
+    // control pointer in one read
+    BCK(b, launch_gather_tiles(b->d_sims, b->d_ctls, b->d_tiles, b->ntiles, b->d_tdescs, s));
     for (int i = 0; i < n; ++i) {
-        BCK(b, launch_nodal_kinematics_batch(b->cfg, b->d_descs, b->d_ctls, b->d_tiles, b->ntiles, i, s));
-        BCK(b, launch_forces_batch(b->cfg, b->d_descs, b->d_ctls, b->d_tiles, b->ntiles, i, s));
-        BCK(b, launch_particle_kinematics_batch(b->cfg, b->d_descs, b->d_ctls, b->d_tiles, b->ntiles, i, s));
+        BCK(b, launch_nodal_kinematics_batch(b->cfg, b->d_tdescs, b->ntiles, i, s));
+        BCK(b, launch_forces_batch(b->cfg, b->d_tdescs, b->ntiles, i, s));
+        BCK(b, launch_particle_kinematics_batch(b->cfg, b->d_tdescs, b->ntiles, i, s));
     }
     BCK(b, launch_advance_steps(b->d_ctls, (int)b->sims.size(), n, s));
     return MPM_OK;
@@ -213,7 +213,8 @@ int mpm_batch_create(MpmHandle* const* sims, int n, MpmBatch** out) {
     };
     cudaError_t e;
     if ((e = cudaMalloc(&b->d_sims, sizeof(SimDev*) * n)) != cudaSuccess) return bail("cudaMalloc", e);
-    if ((e = cudaMalloc(&b->d_descs, sizeof(SimDev) * n)) != cudaSuccess) return bail("cudaMalloc", e);
+    if ((e = cudaMalloc(&b->d_tdescs, sizeof(TileDesc) * tiles.size())) != cudaSuccess)
+        return bail("cudaMalloc", e);
     if ((e = cudaMalloc(&b->d_ctls, sizeof(Control*) * n)) != cudaSuccess) return bail("cudaMalloc", e);
     if ((e = cudaMalloc(&b->d_tiles, sizeof(int4) * tiles.size())) != cudaSuccess) return bail("cudaMalloc", e);
     if ((e = cudaMalloc(&b->d_status, sizeof(Control) * n)) != cudaSuccess) return bail("cudaMalloc", e);
@@ -236,7 +237,7 @@ int mpm_batch_destroy(MpmBatch* b) {
     segbuf_free(b->segbuf);
     if (b->cap) cudaStreamDestroy(b->cap);
     cudaFree(b->d_sims);
-    cudaFree(b->d_descs);
+    cudaFree(b->d_tdescs);
     cudaFree(b->d_ctls);
     cudaFree(b->d_tiles);
     cudaFree(b->d_status);

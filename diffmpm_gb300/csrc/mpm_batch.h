@@ -16,7 +16,7 @@ struct MpmBatch {
     std::vector<MpmHandle*> sims;
     mpm::StepConfig cfg{};
     const mpm::SimDev** d_sims = nullptr;
-    mpm::SimDev* d_descs = nullptr;     // contiguous copies of the descriptors, refreshed per block
+    mpm::TileDesc* d_tdescs = nullptr;  // per-tile descriptor copies, refreshed per block
     mpm::Control** d_ctls = nullptr;
     int4* d_tiles = nullptr;
     int ntiles = 0;

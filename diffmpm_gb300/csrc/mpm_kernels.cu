@@ -26,17 +26,38 @@ __device__ __forceinline__ int load_step(const Control* ctl) {
     return *reinterpret_cast<const volatile int*>(&ctl->step);
 }
 
-// Batched launches: the CTA copies the descriptor of its simulation into
-// shared memory (one word per thread) before the tile work starts.
-__global__ void k_gather_descs(const SimDev* const* __restrict__ sims, int n, SimDev* __restrict__ out) {
-    const int* a = reinterpret_cast<const int*>(sims[blockIdx.x]);
-    int* b = reinterpret_cast<int*>(out + blockIdx.x);
-    for (int i = threadIdx.x; i < (int)(sizeof(SimDev) / 4); i += blockDim.x) b[i] = a[i];
+// Batched launches: per step block, every tile gets a record with its
+// simulation's descriptor and control pointer (one warp per record).
+__global__ void k_gather_tiles(const SimDev* const* __restrict__ sims, Control* const* __restrict__ ctls,
+                               const int4* __restrict__ tiles, int ntiles, TileDesc* __restrict__ out) {
+    const int t = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32, lane = threadIdx.x & 31;
+    if (t >= ntiles) return;
+    const int4 T = tiles[t];
+    TileDesc& d = out[t];
+    if (lane == 0) {
+        d.T = T;
+        d.ctl = ctls[T.x];
+        d.pad = 0;
+    }
+    const int* a = reinterpret_cast<const int*>(sims[T.x]);
+    int* b = reinterpret_cast<int*>(&d.S);
+    for (int i = lane; i < (int)(sizeof(SimDev) / 4); i += 32) b[i] = a[i];
 }
 
-cudaError_t launch_gather_descs(const SimDev* const* sims, int n, SimDev* descs, cudaStream_t s) {
-    if (n > 0) k_gather_descs<<<n, 128, 0, s>>>(sims, n, descs);
+cudaError_t launch_gather_tiles(const SimDev* const* sims, Control* const* ctls, const int4* tiles,
+                                int ntiles, TileDesc* out, cudaStream_t s) {
+    if (ntiles > 0) k_gather_tiles<<<(ntiles + 7) / 8, 256, 0, s>>>(sims, ctls, tiles, ntiles, out);
     return cudaGetLastError();
+}
+
+// A batched CTA copies its tile record (tile, control pointer, descriptor)
+// into shared memory, one word per thread.
+__device__ __forceinline__ void load_tile(const TileDesc* __restrict__ src, TileDesc& dst) {
+    static_assert(sizeof(TileDesc) % 4 == 0, "tile record copied in 4-byte words");
+    const int* a = reinterpret_cast<const int*>(src);
+    int* b = reinterpret_cast<int*>(&dst);
+    for (int i = threadIdx.x; i < (int)(sizeof(TileDesc) / 4); i += blockDim.x) b[i] = a[i];
+    __syncthreads();
 }
 
 // The step counter advances once per launch sequence, after its last kernel:
@@ -61,13 +82,6 @@ cudaError_t launch_advance_step(Control* ctl, int by, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-__device__ __forceinline__ void load_sim(const SimDev* __restrict__ src, SimDev& dst) {
-    static_assert(sizeof(SimDev) % 4 == 0, "descriptor copied in 4-byte words");
-    const int* a = reinterpret_cast<const int*>(src);
-    int* b = reinterpret_cast<int*>(&dst);
-    for (int i = threadIdx.x; i < (int)(sizeof(SimDev) / 4); i += blockDim.x) b[i] = a[i];
-    __syncthreads();
-}
 
 // Visit, in a fixed order, the particles whose current cell is (ci, cj):
 // sort-cells (ci+di, cj+dj) row by row; a neighbour is scanned only when its
@@ -529,12 +543,10 @@ k_nodal_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__ ti
 
 template <bool REINIT>
 __global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
-k_nodal_kinematics_batch(const SimDev* __restrict__ descs, Control* const* __restrict__ ctls,
-                         const int4* __restrict__ tiles, int k) {
-    __shared__ SimDev sS;
-    const int4 T = tiles[blockIdx.x];
-    load_sim(descs + T.x, sS);
-    nodal_kinematics_tile<REINIT>(sS, T, ctls[T.x], k);
+k_nodal_kinematics_batch(const TileDesc* __restrict__ td, int k) {
+    __shared__ TileDesc sT;
+    load_tile(td + blockIdx.x, sT);
+    nodal_kinematics_tile<REINIT>(sT.S, sT.T, sT.ctl, k);
 }
 
 // Nodal update shared by both schemes: concentrated forces (element.py:270-284),
@@ -723,12 +735,10 @@ k_forces(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
 
 template <bool USL, bool REINIT, bool TRAC>
 __global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
-k_forces_batch(const SimDev* __restrict__ descs, Control* const* __restrict__ ctls,
-               const int4* __restrict__ tiles, int k) {
-    __shared__ SimDev sS;
-    const int4 T = tiles[blockIdx.x];
-    load_sim(descs + T.x, sS);
-    forces_tile<USL, REINIT, TRAC, true>(sS, T, ctls[T.x], k);
+k_forces_batch(const TileDesc* __restrict__ td, int k) {
+    __shared__ TileDesc sT;
+    load_tile(td + blockIdx.x, sT);
+    forces_tile<USL, REINIT, TRAC, true>(sT.S, sT.T, sT.ctl, k);
 }
 
 // ---------------------------------------------------------------------------
@@ -989,12 +999,10 @@ k_particle_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__
 
 template <bool USL, bool REINIT>
 __global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
-k_particle_kinematics_batch(const SimDev* __restrict__ descs, Control* const* __restrict__ ctls,
-                            const int4* __restrict__ tiles, int k) {
-    __shared__ SimDev sS;
-    const int4 T = tiles[blockIdx.x];
-    load_sim(descs + T.x, sS);
-    particle_kinematics_tile<USL, REINIT>(sS, T, ctls[T.x], k);
+k_particle_kinematics_batch(const TileDesc* __restrict__ td, int k) {
+    __shared__ TileDesc sT;
+    load_tile(td + blockIdx.x, sT);
+    particle_kinematics_tile<USL, REINIT>(sT.S, sT.T, sT.ctl, k);
 }
 
 // ---------------------------------------------------------------------------
@@ -1071,60 +1079,54 @@ cudaError_t launch_particle_kinematics(const StepConfig& c, const SimDev& S, con
 
 // Batched launches: one grid over the tiles of every simulation of a batch.
 template <bool REINIT>
-static void nodal_kinematics_batch(const SimDev* descs, Control* const* ctls,
-                                   const int4* tiles, int ntiles, int k, cudaStream_t s) {
+static void nodal_kinematics_batch(const TileDesc* td, int ntiles, int k, cudaStream_t s) {
     prefer_shared(k_nodal_kinematics_batch<REINIT>);
-    k_nodal_kinematics_batch<REINIT><<<ntiles, TILE_THREADS, 0, s>>>(descs, ctls, tiles, k);
+    k_nodal_kinematics_batch<REINIT><<<ntiles, TILE_THREADS, 0, s>>>(td, k);
 }
 
-cudaError_t launch_nodal_kinematics_batch(const StepConfig& c, const SimDev* descs,
-                                          Control* const* ctls, const int4* tiles, int ntiles,
+cudaError_t launch_nodal_kinematics_batch(const StepConfig& c, const TileDesc* td, int ntiles,
                                           int k, cudaStream_t s) {
-    if (c.reinit) nodal_kinematics_batch<true>(descs, ctls, tiles, ntiles, k, s);
-    else nodal_kinematics_batch<false>(descs, ctls, tiles, ntiles, k, s);
+    if (c.reinit) nodal_kinematics_batch<true>(td, ntiles, k, s);
+    else nodal_kinematics_batch<false>(td, ntiles, k, s);
     return cudaGetLastError();
 }
 
 template <bool USL, bool REINIT, bool TRAC>
-static void forces_batch(const SimDev* descs, Control* const* ctls, const int4* tiles,
-                         int ntiles, int k, cudaStream_t s) {
+static void forces_batch(const TileDesc* td, int ntiles, int k, cudaStream_t s) {
     prefer_shared(k_forces_batch<USL, REINIT, TRAC>);
-    k_forces_batch<USL, REINIT, TRAC><<<ntiles, TILE_THREADS, 0, s>>>(descs, ctls, tiles, k);
+    k_forces_batch<USL, REINIT, TRAC><<<ntiles, TILE_THREADS, 0, s>>>(td, k);
 }
 
-cudaError_t launch_forces_batch(const StepConfig& c, const SimDev* descs,
-                                Control* const* ctls, const int4* tiles, int ntiles,
-                                int k, cudaStream_t s) {
+cudaError_t launch_forces_batch(const StepConfig& c, const TileDesc* td, int ntiles, int k,
+                                cudaStream_t s) {
     const int key = (c.usl ? 4 : 0) | (c.reinit ? 2 : 0) | (c.traction ? 1 : 0);
     switch (key) {
-        case 0: forces_batch<false, false, false>(descs, ctls, tiles, ntiles, k, s); break;
-        case 1: forces_batch<false, false, true>(descs, ctls, tiles, ntiles, k, s); break;
-        case 2: forces_batch<false, true, false>(descs, ctls, tiles, ntiles, k, s); break;
-        case 3: forces_batch<false, true, true>(descs, ctls, tiles, ntiles, k, s); break;
-        case 4: forces_batch<true, false, false>(descs, ctls, tiles, ntiles, k, s); break;
-        case 5: forces_batch<true, false, true>(descs, ctls, tiles, ntiles, k, s); break;
-        case 6: forces_batch<true, true, false>(descs, ctls, tiles, ntiles, k, s); break;
-        default: forces_batch<true, true, true>(descs, ctls, tiles, ntiles, k, s); break;
+        case 0: forces_batch<false, false, false>(td, ntiles, k, s); break;
+        case 1: forces_batch<false, false, true>(td, ntiles, k, s); break;
+        case 2: forces_batch<false, true, false>(td, ntiles, k, s); break;
+        case 3: forces_batch<false, true, true>(td, ntiles, k, s); break;
+        case 4: forces_batch<true, false, false>(td, ntiles, k, s); break;
+        case 5: forces_batch<true, false, true>(td, ntiles, k, s); break;
+        case 6: forces_batch<true, true, false>(td, ntiles, k, s); break;
+        default: forces_batch<true, true, true>(td, ntiles, k, s); break;
     }
     return cudaGetLastError();
 }
 
 template <bool USL, bool REINIT>
-static void particle_kinematics_batch(const SimDev* descs, Control* const* ctls,
-                                      const int4* tiles, int ntiles, int k, cudaStream_t s) {
+static void particle_kinematics_batch(const TileDesc* td, int ntiles, int k, cudaStream_t s) {
     prefer_shared(k_particle_kinematics_batch<USL, REINIT>);
-    k_particle_kinematics_batch<USL, REINIT><<<ntiles, TILE_THREADS, 0, s>>>(descs, ctls, tiles, k);
+    k_particle_kinematics_batch<USL, REINIT><<<ntiles, TILE_THREADS, 0, s>>>(td, k);
 }
 
-cudaError_t launch_particle_kinematics_batch(const StepConfig& c, const SimDev* descs,
-                                             Control* const* ctls, const int4* tiles, int ntiles,
+cudaError_t launch_particle_kinematics_batch(const StepConfig& c, const TileDesc* td, int ntiles,
                                              int k, cudaStream_t s) {
     if (c.usl) {
-        if (c.reinit) particle_kinematics_batch<true, true>(descs, ctls, tiles, ntiles, k, s);
-        else particle_kinematics_batch<true, false>(descs, ctls, tiles, ntiles, k, s);
+        if (c.reinit) particle_kinematics_batch<true, true>(td, ntiles, k, s);
+        else particle_kinematics_batch<true, false>(td, ntiles, k, s);
     } else {
-        if (c.reinit) particle_kinematics_batch<false, true>(descs, ctls, tiles, ntiles, k, s);
-        else particle_kinematics_batch<false, false>(descs, ctls, tiles, ntiles, k, s);
+        if (c.reinit) particle_kinematics_batch<false, true>(td, ntiles, k, s);
+        else particle_kinematics_batch<false, false>(td, ntiles, k, s);
     }
     return cudaGetLastError();
 }

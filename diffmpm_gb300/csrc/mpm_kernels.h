@@ -30,16 +30,14 @@ cudaError_t launch_advance_steps(Control* const* ctls, int n, int by, cudaStream
 // The same three phases for a batch of simulations in one launch each: tile
 // t works on simulation tiles[t].x, whose descriptor is sims[tiles[t].x] and
 // whose step counter and status are in ctls[tiles[t].x].
-// Copy *sims[i] to descs[i] for i < n.
-cudaError_t launch_gather_descs(const SimDev* const* sims, int n, SimDev* descs, cudaStream_t s);
-cudaError_t launch_nodal_kinematics_batch(const StepConfig& c, const SimDev* descs,
-                                          Control* const* ctls, const int4* tiles, int ntiles,
+// out[t] = {tiles[t], ctls[tiles[t].x], *sims[tiles[t].x]} for t < ntiles.
+cudaError_t launch_gather_tiles(const SimDev* const* sims, Control* const* ctls, const int4* tiles,
+                                int ntiles, TileDesc* out, cudaStream_t s);
+cudaError_t launch_nodal_kinematics_batch(const StepConfig& c, const TileDesc* td, int ntiles,
                                           int k, cudaStream_t s);
-cudaError_t launch_forces_batch(const StepConfig& c, const SimDev* descs,
-                                Control* const* ctls, const int4* tiles, int ntiles,
-                                int k, cudaStream_t s);
-cudaError_t launch_particle_kinematics_batch(const StepConfig& c, const SimDev* descs,
-                                             Control* const* ctls, const int4* tiles, int ntiles,
+cudaError_t launch_forces_batch(const StepConfig& c, const TileDesc* td, int ntiles, int k,
+                                cudaStream_t s);
+cudaError_t launch_particle_kinematics_batch(const StepConfig& c, const TileDesc* td, int ntiles,
                                              int k, cudaStream_t s);
 
 // Re-sort of one simulation's particles by current cell, stable in storage order.

@@ -89,6 +89,18 @@ struct SimDev {
     const MatDev *mats;
 };
 
+struct Control;
+
+// One tile of a batched launch together with its simulation's descriptor and
+// control block, so that a CTA fetches everything it needs to start in one
+// contiguous read (refreshed before every step block).
+struct alignas(16) TileDesc {
+    int4 T;                // (simulation, tile x, tile y, 0)
+    Control* ctl;
+    long long pad;
+    SimDev S;
+};
+
 // Per-batch control block.
 struct Control {
     int step;              // step counter i (t = i * dt) at the start of the launched sequence
