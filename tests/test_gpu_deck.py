@@ -128,3 +128,33 @@ def test_output_enqueue_rejects_pageable_memory(built):
     with pytest.raises(D.MpmError):
         sim.output_enqueue(("loc",), Pageable)
     sim.close()
+
+
+def test_one_dimensional_deck_end_to_end(built, tmp_path, monkeypatch):
+    """The reference's 1-D example deck form (examples/input_1d.toml: node_ids
+    constraints, no entity sets, SimpleMaterial, one element) runs through
+    MPM on the GPU and matches the oracle bit for bit."""
+    (tmp_path / "p.json").write_text("[[[0.5]]]")
+    (tmp_path / "d.toml").write_text(
+        '[meta]\ntitle = "bar"\ntype = "MPMExplicit"\ndimension = 1\nscheme = "usf"\n'
+        'dt = 0.01\nnsteps = 200\nvelocity_update = true\n'
+        '[output]\nformat = "npz"\nfolder = "results/"\nstep_frequency = 50\n'
+        '[mesh]\ntype = "generator"\nnelements = 1\nelement_length = 1.0\n'
+        'particle_element_ids = [0]\nelement = "Linear1D"\n'
+        '[[mesh.constraints]]\nnode_ids = [0]\ndir = 0\nvelocity = 0.0\n'
+        '[[materials]]\nid = 0\ndensity = 1\npoisson_ratio = 1\nE = 100\ntype = "SimpleMaterial"\n'
+        '[[particles]]\nfile = "p.json"\nmaterial_id = 0\ninit_velocity = 0.1\n'
+        '[external_loading]\ngravity = 0\n')
+    monkeypatch.chdir(tmp_path)
+    got = D.MPM("d.toml").solve()
+    assert sorted(p.name for p in (tmp_path / "results" / "bar").iterdir()) == \
+        [npz_name(i, 200) for i in range(0, 200, 50)]
+    mat = O.SimpleMaterial({"E": 100, "density": 1})
+    el = O.Linear1D(1, 1, 1.0, [(np.array([0]), O.Constraint(0, 0.0))])
+    ps = O.Particles(np.array([0.5]).reshape(1, 1, 1), mat, np.zeros(1, dtype=np.int32))
+    ps.velocity[:] = 0.1
+    mesh = O.Mesh1D({"particles": [ps], "elements": el, "particle_surface_traction": []})
+    ref = O.MPMExplicit(mesh, 0.01, scheme="usf", velocity_update=True, sim_steps=200).solve_jit(
+        np.array([0.0]))
+    for k in ("loc", "velocity", "stress", "strain"):
+        assert np.array_equal(np.asarray(got[k]).reshape(-1), np.asarray(ref[k]).reshape(-1)), k
