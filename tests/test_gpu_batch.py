@@ -126,3 +126,60 @@ def test_batch_rejects_mixed_configurations(built):
     assert e.value.code == 5
     with pytest.raises(D.MpmError):
         D.Batch([a, a])
+
+
+@pytest.mark.parametrize("scheme", ["usf", "usl"])
+@pytest.mark.parametrize("reinit", [True, False])
+def test_batch_variants_equal_single_runs(built, scheme, reinit):
+    """Every batched kernel variant (scheme x volume set-up) gives each member
+    the bits of its single run."""
+    specs = small_specs(k=3, seed=21)
+    steps = 30
+
+    def make(sp):
+        solver, g, _ = workloads.batch_member(D, sp, sim_steps=steps)
+        solver.scheme = scheme
+        sim = solver.simulation(g, reinit=reinit)
+        solver._upload(sim)
+        sim.initialize()
+        sim.set_block_steps(10)
+        return sim
+
+    members = [make(sp) for sp in specs]
+    batch = D.Batch(members)
+    batch.set_block_steps(10)
+    batch.step(steps)
+    for sp, sim in zip(specs, members):
+        alone = make(sp)
+        alone.step(steps)
+        for k in FIELDS:
+            assert np.array_equal(sim.read(k), alone.read(k)), (sp["side"], k)
+    batch.close()
+
+
+def test_batch_with_tractions_equals_single_runs(built):
+    """The traction variant of the batched forces kernel, on the particle
+    traction benchmark deck (two copies with different Young's moduli)."""
+    import decks
+    deck = decks.load_deck("uniaxial_particle_traction")
+    steps = 200
+
+    def make(E):
+        d = dict(deck, materials=[dict(deck["materials"][0], youngs_modulus=E)])
+        solver, g = decks.build(D, d, sim_steps=steps)
+        sim = solver.simulation(g, reinit=True)
+        solver._upload(sim)
+        sim.initialize()
+        sim.set_block_steps(25)
+        return sim
+
+    members = [make(1e6), make(2e6)]
+    batch = D.Batch(members)
+    batch.set_block_steps(25)
+    batch.step(steps)
+    for E, sim in zip((1e6, 2e6), members):
+        alone = make(E)
+        alone.step(steps)
+        for k in FIELDS:
+            assert np.array_equal(sim.read(k), alone.read(k)), (E, k)
+    batch.close()
