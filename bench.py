@@ -437,17 +437,52 @@ def run_ours(args, world, rank, local):
     counters = {"resorts": sum(s.counters()["resorts"] for s in sims),
                 "rollbacks": sum(s.counters()["rollbacks"] for s in sims)}
 
-    # end to end through the public API with host buffers: upload of the
-    # initial states, record, adjoint with host seeds, gradients back
-    reset_batch(members)
+    # end to end through the public API with host buffers: the initial states
+    # of every member from pinned host memory (whole-batch writes and a
+    # restart), record, positions back, adjoint with host seeds, gradients back
+    def pinned(a):
+        t = torch.empty(a.size, dtype=torch.float32, pin_memory=True).numpy()
+        t[:] = a.reshape(-1)
+        return t
+
+    init = {}
+    for name in ("loc", "velocity", "stress", "strain", "density", "volumetric_strain_centroid"):
+        parts = []
+        for solver, sim, g in members:
+            p = solver.mesh.particles[0]
+            v = {"loc": p.loc, "velocity": p.velocity, "stress": p.stress, "strain": p.strain,
+                 "density": p.density,
+                 "volumetric_strain_centroid": p.volumetric_strain_centroid}[name]
+            parts.append(np.asarray(v, np.float32).reshape(-1))
+        init[name] = pinned(np.concatenate(parts))
+    node_v0 = pinned(np.concatenate([np.asarray(solver.mesh.elements.nodes.velocity, np.float32)
+                                     .reshape(-1) for solver, sim, g in members]))
+    target_flat = np.concatenate([t.reshape(-1) for t in targets]).astype(np.float32)
+    scale = np.concatenate([np.full(2 * len(t), 2.0 / len(t), np.float32) for t in targets])
+    loc_out = pinned(np.zeros(target_flat.size, np.float32))
+
+    def e2e_upload():
+        for name, arr in init.items():
+            batch.write(name, arr)
+        batch.write_nodal("velocity", node_v0)
+        batch.restart()
+
+    e2e_upload()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    reset_batch(members)
+    e2e_upload()
+    t1 = time.perf_counter()
     batch.record(K, ckpt)
-    seeds = seeds_for()
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    xs = batch.read("loc", out=loc_out)
+    seeds = batch.split("loc", scale * (xs - target_flat))
+    t3 = time.perf_counter()
     grads = batch.adjoint(seeds, want=("youngs_modulus",))
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
+    e2e_parts = {"upload_s": t1 - t0, "record_s": t2 - t1, "seeds_s": t3 - t2,
+                 "adjoint_s": e2e_s - (t3 - t0)}
     h2d = npart * (2 + 2 + 6 + 6 + 1 + 1) * 4 + nnode * 2 * 4 + sum(s.nbytes for s in seeds)
     d2h = npart * 2 * 4 + sum(g["youngs_modulus"].nbytes for g in grads)
 
@@ -521,8 +556,9 @@ def run_ours(args, world, rank, local):
             "dLdE_first_sims": dLdE[:4],
             "e2e": {"value": world * ps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d / K,
                     "d2h_bytes_per_step": d2h / K,
-                    "what": "upload of all initial states + batched record + adjoint with host "
-                            "seeds + gradients to host"},
+                    "what": "whole-batch upload of all initial states from pinned host memory + "
+                            "restart + batched record + positions to host + adjoint with host "
+                            "seeds + gradients to host", "parts": e2e_parts},
             "gpu_launches": launches,
             "roofline": roof,
             "plain_scaleup": plain,

@@ -99,6 +99,10 @@ SIGNATURES = [
     ("mpm_batch_last_error", C.c_char_p, [_VP]),
     ("mpm_batch_size", C.c_int, [_VP, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     ("mpm_batch_step", C.c_int, [_VP, C.c_int, _VP]),
+    ("mpm_batch_write_field", C.c_int, [_VP, C.c_int, _VP, C.c_int, _VP]),
+    ("mpm_batch_read_field", C.c_int, [_VP, C.c_int, _VP, C.c_int, _VP]),
+    ("mpm_batch_write_nodal_field", C.c_int, [_VP, C.c_int, _VP, C.c_int, _VP]),
+    ("mpm_batch_restart", C.c_int, [_VP, _VP]),
     ("mpm_batch_set_block_steps", C.c_int, [_VP, C.c_int]),
     ("mpm_batch_autotune", C.c_int, [_VP, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float), _VP]),
     ("mpm_batch_record", C.c_int, [_VP, C.c_int, C.c_int, _VP]),

@@ -782,17 +782,50 @@ int mpm_write_field(MpmHandle* h, int field, const void* src, int on_device, voi
     const int nc = (int)c.size();
     const void* d = nullptr;
     TRY(to_device(h, src, sizeof(float) * nc * n, on_device, s, &d));
-    TRY(set_ptr_table(h, c, s));
-    CK(h, launch_gather_in(h->d_ptrs, nc, p.pid, (int)n, static_cast<const float*>(d), s));
-    if (field == MPM_FIELD_STRESS || field == MPM_FIELD_STRAIN)
-        TRY(copy_passive(h, field, const_cast<float*>(static_cast<const float*>(d)), false, s));
-    if (field == MPM_FIELD_LOC && h->initialized) h->needs_resort = true;
+    TRY(write_float_field(h, field, static_cast<const float*>(d), s));
     return sync(h, s);
 }
 
 }  // extern "C"
 
-namespace {
+namespace mpm {
+namespace host {
+
+// Before the step counter changes to `step`: when its parity changes, swap the
+// ping-pong pairs so that the current data stays addressed by the new parity
+// (graphs, which hold the descriptor by value, are dropped).
+int keep_parity_data(MpmHandle* h, int64_t step) {
+    if ((step & 1) == (h->step & 1) || h->np <= 0) return MPM_OK;
+    for (int k = 0; k < 2; ++k) {
+        PSet& p = h->ps[k];
+        std::swap(p.sxx[0], p.sxx[1]);
+        std::swap(p.syy[0], p.syy[1]);
+        std::swap(p.szz[0], p.szz[1]);
+        std::swap(p.sxy[0], p.sxy[1]);
+        std::swap(p.rho[0], p.rho[1]);
+        std::swap(p.vsc[0], p.vsc[1]);
+        std::swap(p.vol[0], p.vol[1]);
+    }
+    bind_particles(h);
+    drop_graphs(h);
+    return upload_desc(h);
+}
+
+// A float particle field (original order) from device memory `d` into the
+// current particle set, on stream s without waiting.
+int write_float_field(MpmHandle* h, int field, const float* d, cudaStream_t s) {
+    std::vector<float*> c = comps(h, field);
+    if (c.empty()) return fail(h, MPM_ERR_INVALID, "field %d is not writable", field);
+    const int nc = (int)c.size();
+    PSet& p = h->ps[h->pcur];
+    TRY(set_ptr_table(h, c, s));
+    CK(h, launch_gather_in(h->d_ptrs, nc, p.pid, (int)h->np, d, s));
+    if (field == MPM_FIELD_STRESS || field == MPM_FIELD_STRAIN)
+        TRY(copy_passive(h, field, const_cast<float*>(d), false, s));
+    if (field == MPM_FIELD_LOC && h->initialized) h->needs_resort = true;
+    return MPM_OK;
+}
+
 
 // Particle field `field` in original order into the device buffer `d`.
 int gather_field(MpmHandle* h, int field, void* d, cudaStream_t s) {
@@ -823,7 +856,8 @@ int gather_field(MpmHandle* h, int field, void* d, cudaStream_t s) {
     return MPM_OK;
 }
 
-}  // namespace
+}  // namespace host
+}  // namespace mpm
 
 extern "C" {
 
@@ -1142,21 +1176,7 @@ int mpm_get_step(const MpmHandle* h, int64_t* step) {
 int mpm_set_step(MpmHandle* h, int64_t step) {
     if (!h || step < 0 || step > 0x7fffffff) return MPM_ERR_INVALID;
     h->gen++;
-    if ((step & 1) != (h->step & 1) && h->np > 0) {
-        // keep the current ping-pong data addressed by the new parity
-        for (int k = 0; k < 2; ++k) {
-            PSet& p = h->ps[k];
-            std::swap(p.sxx[0], p.sxx[1]);
-            std::swap(p.syy[0], p.syy[1]);
-            std::swap(p.szz[0], p.szz[1]);
-            std::swap(p.sxy[0], p.sxy[1]);
-            std::swap(p.rho[0], p.rho[1]);
-            std::swap(p.vsc[0], p.vsc[1]);
-            std::swap(p.vol[0], p.vol[1]);
-        }
-        bind_particles(h);
-        TRY(upload_desc(h));
-    }
+    TRY(keep_parity_data(h, step));
     h->step = step;
     h->h_ctl->step = (int)step;
     CK(h, cudaMemcpy(&h->ctl->step, &h->h_ctl->step, sizeof(int), cudaMemcpyHostToDevice));

@@ -238,6 +238,7 @@ int mpm_batch_destroy(MpmBatch* b) {
     if (b->cap) cudaStreamDestroy(b->cap);
     cudaFree(b->d_sims);
     cudaFree(b->d_tdescs);
+    cudaFree(b->d_stage);
     cudaFree(b->d_ctls);
     cudaFree(b->d_tiles);
     cudaFree(b->d_status);
@@ -254,6 +255,127 @@ int mpm_batch_size(const MpmBatch* b, int* n, int* ntiles) {
     if (!b) return MPM_ERR_INVALID;
     if (n) *n = (int)b->sims.size();
     if (ntiles) *ntiles = b->ntiles;
+    return MPM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Whole-batch state transfers: one host copy for every member, per-member
+// gathers into storage order on the stream, one wait at the end.
+// ---------------------------------------------------------------------------
+static int batch_stage(MpmBatch* b, size_t bytes) {
+    if (b->stage_bytes >= bytes) return MPM_OK;
+    cudaFree(b->d_stage);
+    b->d_stage = nullptr;
+    b->stage_bytes = 0;
+    BCK(b, cudaMalloc(&b->d_stage, bytes));
+    b->stage_bytes = bytes;
+    return MPM_OK;
+}
+
+static bool batch_writable(int field) {
+    return field == MPM_FIELD_LOC || field == MPM_FIELD_VELOCITY || field == MPM_FIELD_STRESS ||
+           field == MPM_FIELD_STRAIN || field == MPM_FIELD_DENSITY || field == MPM_FIELD_VSC;
+}
+
+int mpm_batch_write_field(MpmBatch* b, int field, const void* src, int on_device, void* stream) {
+    if (!b || !src) return MPM_ERR_INVALID;
+    if (!batch_writable(field))
+        return bfail(b, MPM_ERR_INVALID, "field %d cannot be written for a whole batch", field);
+    cudaStream_t s = S(stream);
+    size_t total = 0;
+    for (MpmHandle* h : b->sims) total += sizeof(float) * ncomp_of(h, field) * h->np;
+    const char* d = static_cast<const char*>(src);
+    if (!on_device) {
+        int r = batch_stage(b, total);
+        if (r != MPM_OK) return r;
+        BCK(b, cudaMemcpyAsync(b->d_stage, src, total, cudaMemcpyHostToDevice, s));
+        d = static_cast<const char*>(b->d_stage);
+    }
+    size_t off = 0;
+    for (int i = 0; i < (int)b->sims.size(); ++i) {
+        MpmHandle* h = b->sims[i];
+        h->gen++;
+        BTRY(b, i, write_float_field(h, field, reinterpret_cast<const float*>(d + off), s));
+        off += sizeof(float) * ncomp_of(h, field) * h->np;
+    }
+    BCK(b, cudaStreamSynchronize(s));
+    return MPM_OK;
+}
+
+int mpm_batch_read_field(MpmBatch* b, int field, void* dst, int on_device, void* stream) {
+    if (!b || !dst) return MPM_ERR_INVALID;
+    if (field < 0 || field >= MPM_FIELD_COUNT) return bfail(b, MPM_ERR_INVALID, "unknown field %d", field);
+    cudaStream_t s = S(stream);
+    size_t total = 0;
+    for (MpmHandle* h : b->sims) total += sizeof(float) * ncomp_of(h, field) * h->np;
+    char* d = static_cast<char*>(dst);
+    if (!on_device) {
+        int r = batch_stage(b, total);
+        if (r != MPM_OK) return r;
+        d = static_cast<char*>(b->d_stage);
+    }
+    size_t off = 0;
+    for (int i = 0; i < (int)b->sims.size(); ++i) {
+        MpmHandle* h = b->sims[i];
+        BTRY(b, i, gather_field(h, field, d + off, s));
+        off += sizeof(float) * ncomp_of(h, field) * h->np;
+    }
+    if (!on_device) BCK(b, cudaMemcpyAsync(dst, b->d_stage, total, cudaMemcpyDeviceToHost, s));
+    BCK(b, cudaStreamSynchronize(s));
+    return MPM_OK;
+}
+
+int mpm_batch_write_nodal_field(MpmBatch* b, int field, const float* src, int on_device, void* stream) {
+    if (!b || !src) return MPM_ERR_INVALID;
+    if (field != MPM_NODE_MASS && field != MPM_NODE_VELOCITY && field != MPM_NODE_ACCELERATION)
+        return bfail(b, MPM_ERR_INVALID, "nodal field %d is not writable", field);
+    cudaStream_t s = S(stream);
+    const int nc = field == MPM_NODE_MASS ? 1 : 2;
+    size_t total = 0;
+    for (MpmHandle* h : b->sims) total += sizeof(float) * nc * h->nn;
+    const char* d = reinterpret_cast<const char*>(src);
+    if (!on_device) {
+        int r = batch_stage(b, total);
+        if (r != MPM_OK) return r;
+        BCK(b, cudaMemcpyAsync(b->d_stage, src, total, cudaMemcpyHostToDevice, s));
+        d = static_cast<const char*>(b->d_stage);
+    }
+    size_t off = 0;
+    for (MpmHandle* h : b->sims) {
+        h->gen++;
+        const float* df = reinterpret_cast<const float*>(d + off);
+        if (field == MPM_NODE_MASS)
+            BCK(b, cudaMemcpyAsync(h->nm, df, sizeof(float) * h->nn, cudaMemcpyDeviceToDevice, s));
+        else if (field == MPM_NODE_VELOCITY) BCK(b, launch_deinterleave2(df, h->nn, h->nvbx, h->nvby, s));
+        else BCK(b, launch_deinterleave2(df, h->nn, h->nax, h->nay, s));
+        off += sizeof(float) * nc * h->nn;
+    }
+    BCK(b, cudaStreamSynchronize(s));
+    return MPM_OK;
+}
+
+int mpm_batch_restart(MpmBatch* b, void* stream) {
+    if (!b) return MPM_ERR_INVALID;
+    cudaStream_t s = S(stream);
+    const int n = (int)b->sims.size();
+    for (int i = 0; i < n; ++i) {
+        MpmHandle* h = b->sims[i];
+        h->gen++;
+        BTRY(b, i, keep_parity_data(h, 0));
+        h->step = 0;
+        BCK(b, cudaMemsetAsync(h->ctl, 0, sizeof(Control), s));
+        BTRY(b, i, resort(h, s));
+        if (!h->reinit) BCK(b, launch_setup_volume(h->ds, (int)h->np, parity(h), s));
+        h->initialized = true;
+    }
+    int r = read_statuses(b, s);
+    if (r != MPM_OK) return r;
+    for (int i = 0; i < n; ++i) {
+        MpmHandle* h = b->sims[i];
+        *h->h_ctl = b->h_status[i];
+        int st = b->h_status[i].status;
+        if (check_status(h, st) != MPM_OK) return from_sim(b, i, MPM_ERR_OUT_OF_MESH);
+    }
     return MPM_OK;
 }
 

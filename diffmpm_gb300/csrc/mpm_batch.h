@@ -17,6 +17,8 @@ struct MpmBatch {
     mpm::StepConfig cfg{};
     const mpm::SimDev** d_sims = nullptr;
     mpm::TileDesc* d_tdescs = nullptr;  // per-tile descriptor copies, refreshed per block
+    void* d_stage = nullptr;            // staging of whole-batch field transfers
+    size_t stage_bytes = 0;
     mpm::Control** d_ctls = nullptr;
     int4* d_tiles = nullptr;
     int ntiles = 0;

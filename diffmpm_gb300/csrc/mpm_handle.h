@@ -190,6 +190,12 @@ int line_step(MpmHandle* h, cudaStream_t s);            // mpm_line.cu
 int line_setup_volume(MpmHandle* h, cudaStream_t s);
 int to_device(MpmHandle* h, const void* src, size_t bytes, int on_device, cudaStream_t s,
               const void** dsrc);
+int ncomp_of(const MpmHandle* h, int field);
+// Particle field I/O on stream s without waiting (mpm_abi.cu): a float field
+// from device memory (original order), and any readable field to device memory.
+int write_float_field(MpmHandle* h, int field, const float* d, cudaStream_t s);
+int keep_parity_data(MpmHandle* h, int64_t step);
+int gather_field(MpmHandle* h, int field, void* d, cudaStream_t s);
 
 
 // Whole-state copies as segment lists (mpm_state.cu).  The snapshot of a step

@@ -397,6 +397,60 @@ class Batch:
     def step(self, nsteps=1, stream=None):
         self._ok(self._lib.mpm_batch_step(self._b, int(nsteps), stream))
 
+    # ------------------------------------------------------------------
+    # whole-batch state transfers (one host copy for all members)
+    def _counts(self, field):
+        return [s.n * s.ncomp(field) for s in self.sims]
+
+    def write(self, field, values):
+        """Write ``field`` of every member: one array holding the members'
+        fields one after the other (member order, original particle order),
+        or a sequence of per-member arrays; host memory or a CUDA tensor."""
+        total = sum(self._counts(field))
+        if isinstance(values, (list, tuple)):
+            values = np.concatenate([np.asarray(v, np.float32).reshape(-1) for v in values])
+        p, dev, keep = _in_arg(values, np.float32, total)
+        self._ok(self._lib.mpm_batch_write_field(self._b, _lib.FIELD[field], p, dev,
+                                                 _stream_for(values)))
+
+    def read(self, field, out=None):
+        """``field`` of every member as one array (member order); ``out`` may
+        be a preallocated host array or CUDA tensor of that size.  Returns it
+        with per-member views in ``split(...)`` order."""
+        counts = self._counts(field)
+        if out is None:
+            out = np.empty(sum(counts), dtype=np.float32)
+        dev = 1 if _is_cuda_tensor(out) else 0
+        p = C.c_void_p(out.data_ptr()) if dev else _lib.ptr(out)
+        self._ok(self._lib.mpm_batch_read_field(self._b, _lib.FIELD[field], p, dev, _stream_for(out)))
+        return out
+
+    def split(self, field, flat):
+        """Per-member arrays (n_i, ncomp) or (n_i,) of a whole-batch ``flat``."""
+        out, off = [], 0
+        for s, c in zip(self.sims, self._counts(field)):
+            nc = s.ncomp(field)
+            v = flat[off:off + c]
+            out.append(v.reshape((s.n, nc) if nc > 1 else (s.n,)))
+            off += c
+        return out
+
+    def write_nodal(self, field, values):
+        """Nodal ``field`` ("mass", "velocity", "acceleration") of every member,
+        one array in member order or a sequence of per-member arrays."""
+        nc = 1 if field == "mass" else 2
+        total = sum(s.nnodes * nc for s in self.sims)
+        if isinstance(values, (list, tuple)):
+            values = np.concatenate([np.asarray(v, np.float32).reshape(-1) for v in values])
+        p, dev, keep = _in_arg(values, np.float32, total)
+        self._ok(self._lib.mpm_batch_write_nodal_field(self._b, _lib.NODAL_FIELD[field], p, dev,
+                                                       _stream_for(values)))
+
+    def restart(self, stream=None):
+        """Step counters to 0 and every member re-initialised (re-sort, volume
+        set-up) from the state written since; one wait for all members."""
+        self._ok(self._lib.mpm_batch_restart(self._b, stream))
+
     def set_block_steps(self, n):
         self._ok(self._lib.mpm_batch_set_block_steps(self._b, int(n)))
 

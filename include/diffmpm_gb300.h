@@ -269,6 +269,21 @@ int mpm_batch_destroy(MpmBatch* b);
 const char* mpm_batch_last_error(const MpmBatch* b);
 /* Number of simulations and of tiles (CTAs per phase launch). */
 int mpm_batch_size(const MpmBatch* b, int* n, int* ntiles);
+/* Whole-batch state transfers (a restart of every member from new initial
+ * states without per-member round trips).  `src` / `dst` hold the members'
+ * fields one after the other (member order; within a member the layout of
+ * mpm_write_field / mpm_read_field / mpm_write_nodal_field); host memory is
+ * copied in one transfer.  Writable particle fields: loc, velocity, stress,
+ * strain, density, volumetric strain.  mpm_batch_restart sets every member's
+ * step to 0 and re-runs its initialisation (re-sort, solve-semantics volume
+ * set-up).  Replace per-simulation Particles / Nodes assignments and the
+ * MPMExplicit constructor (diffmpm/particle.py:16-91, node.py:64-71,
+ * solver.py:81-85) for all members at once. */
+int mpm_batch_write_field(MpmBatch* b, int field, const void* src, int on_device, void* stream);
+int mpm_batch_read_field(MpmBatch* b, int field, void* dst, int on_device, void* stream);
+int mpm_batch_write_nodal_field(MpmBatch* b, int field, const float* src, int on_device, void* stream);
+int mpm_batch_restart(MpmBatch* b, void* stream);
+
 /* Advance every simulation by `nsteps` steps (as mpm_step does for one). */
 int mpm_batch_step(MpmBatch* b, int nsteps, void* stream);
 /* Steps per captured graph (default 100). */

@@ -183,3 +183,40 @@ def test_batch_with_tractions_equals_single_runs(built):
         for k in FIELDS:
             assert np.array_equal(sim.read(k), alone.read(k)), (E, k)
     batch.close()
+
+
+def test_batch_state_transfers_and_restart(built):
+    """Whole-batch writes read back bit for bit, and a restart from the
+    written initial states runs like freshly uploaded simulations."""
+    specs = small_specs(k=3, seed=31)
+    steps = 40
+    members = [member_sim(sp, steps) for sp in specs]
+    sims = [m[1] for m in members]
+    batch = D.Batch(sims)
+    batch.set_block_steps(10)
+    batch.step(15)
+    # write the members' initial states back (one array per field)
+    init = {}
+    for k, attr in (("loc", "loc"), ("velocity", "velocity"), ("stress", "stress"),
+                    ("strain", "strain"), ("density", "density"),
+                    ("volumetric_strain_centroid", "volumetric_strain_centroid")):
+        init[k] = np.concatenate([np.asarray(getattr(m[0].mesh.particles[0], attr), np.float32)
+                                  .reshape(-1) for m in members])
+        batch.write(k, init[k])
+        assert np.array_equal(batch.read(k), init[k]), k
+    per = batch.split("loc", batch.read("loc"))
+    for p, (solver, sim, g) in zip(per, members):
+        assert np.array_equal(p, sim.read("loc"))
+    batch.write_nodal("velocity", [np.zeros((s.nnodes, 2), np.float32) for s in sims])
+    batch.restart()
+    assert all(s.step_index == 0 for s in sims)
+    batch.step(steps)
+    for sp, sim in zip(specs, sims):
+        _, alone, _ = member_sim(sp, steps)
+        alone.set_block_steps(10)
+        alone.step(steps)
+        for k in ("loc", "velocity", "stress"):
+            assert rel(sim.read(k), alone.read(k)) <= 1e-6, (sp["side"], k)
+    with pytest.raises(D.MpmError):
+        batch.write("material_id", np.zeros(sum(s.n for s in sims), np.float32))
+    batch.close()
