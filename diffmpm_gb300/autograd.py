@@ -35,17 +35,18 @@ class ExplicitRun(torch.autograd.Function):
         dev = E.device if E.is_cuda else None
         put = (lambda t: _dev_f32(t, dev)) if dev is not None else (
             lambda t: t.detach().cpu().numpy().astype(np.float32))
+        d = sim.ndim
         sim.write("youngs_modulus", put(E))
         if loc is not None:
-            sim.write("loc", put(loc.reshape(-1, 2)))
+            sim.write("loc", put(loc.reshape(-1, d)))
         if velocity is not None:
-            sim.write("velocity", put(velocity.reshape(-1, 2)))
+            sim.write("velocity", put(velocity.reshape(-1, d)))
         sim.initialize()
         sim.record(nsteps, checkpoint_steps)
         n = sim.n
         if dev is not None:
-            x = torch.empty((n, 2), dtype=torch.float32, device=dev)
-            v = torch.empty((n, 2), dtype=torch.float32, device=dev)
+            x = torch.empty((n, d), dtype=torch.float32, device=dev)
+            v = torch.empty((n, d), dtype=torch.float32, device=dev)
             sim.read("loc", out=x)
             sim.read("velocity", out=v)
         else:
@@ -64,12 +65,13 @@ class ExplicitRun(torch.autograd.Function):
     @staticmethod
     def backward(ctx, gx, gv):
         dev = ctx.dev
+        shape = (ctx.sim.n, ctx.sim.ndim)
         if dev is not None:
-            seed_x = (torch.zeros((ctx.sim.n, 2), dtype=torch.float32, device=dev) if gx is None
+            seed_x = (torch.zeros(shape, dtype=torch.float32, device=dev) if gx is None
                       else _dev_f32(gx, dev))
             seed_v = None if gv is None else _dev_f32(gv, dev)
         else:
-            seed_x = (np.zeros((ctx.sim.n, 2), np.float32) if gx is None
+            seed_x = (np.zeros(shape, np.float32) if gx is None
                       else gx.detach().cpu().numpy().astype(np.float32))
             seed_v = None if gv is None else gv.detach().cpu().numpy().astype(np.float32)
         out = ctx.sim.adjoint(seed_x, seed_v, want=ctx.want)

@@ -674,6 +674,7 @@ int mpm_create(const MpmDesc* d, MpmHandle** out) {
 int mpm_destroy(MpmHandle* h) {
     if (!h) return MPM_OK;
     mpm::adjoint_free(h);
+    mpm::line_adjoint_free(h);
     segbuf_free(h->segbuf);
     drop_graphs(h);
     if (h->cap) cudaStreamDestroy(h->cap);

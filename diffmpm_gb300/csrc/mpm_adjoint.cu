@@ -614,6 +614,7 @@ extern "C" {
 
 int mpm_record(MpmHandle* h, int nsteps, int checkpoint_steps, void* stream) {
     if (!h) return MPM_ERR_INVALID;
+    if (h->ndim == 1) return line_record(h, nsteps, S(stream));   // full tape, no checkpoints
     TRY(record_begin(h, nsteps, checkpoint_steps));
     cudaStream_t s = S(stream);
     AdjointState* a = h->adj;
@@ -638,6 +639,8 @@ int mpm_record(MpmHandle* h, int nsteps, int checkpoint_steps, void* stream) {
 int mpm_adjoint(MpmHandle* h, const float* dl_dloc, const float* dl_dvel, float* dl_dE,
                 float* dl_dloc0, float* dl_dvel0, int on_device, void* stream) {
     if (!h) return MPM_ERR_INVALID;
+    if (h->ndim == 1)
+        return line_adjoint(h, dl_dloc, dl_dvel, dl_dE, dl_dloc0, dl_dvel0, on_device, S(stream));
     TRY(check_recorded(h));
     if (!dl_dloc) return fail(h, MPM_ERR_INVALID, "dl_dloc is null");
     AdjointState* a = h->adj;

@@ -369,9 +369,10 @@ __device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q, float x, 
                    fm(mat.c2, fa(fa(fm(d1, sbxx), fm(d0, sbyy)), fm(fa(d0, d1), sbzz)))),
                 fm(mat.c3, fm(d3, sbxy)));
     } else if (mat.type == MAT_SIMPLE) {
-        d0b = fm(mat.E, sbxx);
-        d1b = fm(mat.E, sbyy);
-        d3b = fm(mat.E, sbxy);
+        const float E = Ep >= 0.0f ? Ep : mat.E;
+        d0b = fm(E, sbxx);
+        d1b = fm(E, sbyy);
+        d3b = fm(E, sbxy);
         Eb = fa(fa(fm(d0, sbxx), fm(d1, sbyy)), fm(d3, sbxy));
     }
     const float r0b = r0 != 0.0f ? fm(d0b, A.dt) : 0.0f;

@@ -188,9 +188,10 @@ __device__ __forceinline__ float strain_stress_update(const MatDev& M, float Ep,
         p.szz = fa(p.szz, fa(fm(a2, d0), fm(a2, d1)));
         p.sxy = fa(p.sxy, fm(G, d3));
     } else if (M.type == MAT_SIMPLE) {
-        p.sxx = fa(p.sxx, fm(d0, M.E));
-        p.syy = fa(p.syy, fm(d1, M.E));
-        p.sxy = fa(p.sxy, fm(d3, M.E));
+        const float E = Ep >= 0.0f ? Ep : M.E;   // a per-particle E replaces the material's
+        p.sxx = fa(p.sxx, fm(d0, E));
+        p.syy = fa(p.syy, fm(d1, E));
+        p.sxy = fa(p.sxy, fm(d3, E));
     } else {
         // Newtonian (build definition): total stress from the strain rate and
         // the centroid volumetric strain, p = -K * vsc.

@@ -28,6 +28,7 @@ struct PSet {
 };
 
 struct AdjointState;   // checkpoints, tape and adjoint arrays (mpm_adjoint.cu)
+struct LineAdjoint;    // the 1-D step's full tape and adjoint arrays (mpm_line_adjoint.cu)
 
 // Full copy of the state of one simulation that steps and re-sorts change:
 // the particle arrays (storage order, current ping-pong parity), material ids,
@@ -129,6 +130,7 @@ struct MpmHandle {
     int64_t resorts = 0, rollbacks = 0;
     // differentiation (null until mpm_record); gen counts state changes
     mpm::AdjointState* adj = nullptr;
+    mpm::LineAdjoint* line_adj = nullptr;   // 1-D recording (mpm_line_adjoint.cu)
     uint64_t gen = 0;
     std::vector<void*> allocs;
     std::string err;
@@ -186,7 +188,17 @@ int launch_steps(MpmHandle* h, int n, cudaStream_t s);
 int check_status(MpmHandle* h, int& st);
 int take_snapshot(MpmHandle* h, cudaStream_t s);
 int replay_block(MpmHandle* h, int64_t step0, int B, int& st, cudaStream_t s);
-int line_step(MpmHandle* h, cudaStream_t s);            // mpm_line.cu
+// Where a recorded 1-D step copies its start state (x, v, sxx, syy, szz, sxy,
+// rho in storage order, the storage -> original map and the element starts)
+// and its nodal results (mass, velocity after kinematics, velocity and
+// acceleration after the update).
+struct LineTapeSlot {
+    float* p[7];
+    int* pid;
+    int* cs;
+    float* n[4];
+};
+int line_step(MpmHandle* h, cudaStream_t s, const LineTapeSlot* tape = nullptr);   // mpm_line.cu
 int line_setup_volume(MpmHandle* h, cudaStream_t s);
 int to_device(MpmHandle* h, const void* src, size_t bytes, int on_device, cudaStream_t s,
               const void** dsrc);
@@ -218,6 +230,10 @@ void segbuf_free(SegBuf& buf);
 // Adjoint bookkeeping (mpm_adjoint.cu): release the adjoint state of a handle;
 // note a re-sort at the current step while mpm_record runs.
 void adjoint_free(MpmHandle* h);
+void line_adjoint_free(MpmHandle* h);
+int line_record(MpmHandle* h, int nsteps, cudaStream_t s);
+int line_adjoint(MpmHandle* h, const float* dl_dloc, const float* dl_dvel, float* dl_dE,
+                 float* dl_dloc0, float* dl_dvel0, int on_device, cudaStream_t s);
 void adjoint_note_resort(MpmHandle* h);
 
 }  // namespace mpm

@@ -248,11 +248,18 @@ int line_setup_volume(MpmHandle* h, cudaStream_t s) {
 
 // One step: re-sort by element, nodal kinematics, (USF) stress update, forces
 // and nodal update, G2P, (USL) stress update.
-int line_step(MpmHandle* h, cudaStream_t s) {
+int line_step(MpmHandle* h, cudaStream_t s, const LineTapeSlot* tape) {
     TRY(resort(h, s));
     const SimDev& S = h->hs;
     const int par = parity(h), nb = blocks(h->nx + 1), pb = blocks((int)h->np);
     const int step = (int)h->step;
+    const size_t fb = sizeof(float) * (size_t)h->np, nbytes = sizeof(float) * (size_t)h->nn;
+    if (tape) {
+        const float* src[7] = {S.x, S.vx, S.sxx[par], S.syy[par], S.szz[par], S.sxy[par], S.rho[par]};
+        for (int k = 0; k < 7; ++k) CK(h, cudaMemcpyAsync(tape->p[k], src[k], fb, cudaMemcpyDeviceToDevice, s));
+        CK(h, cudaMemcpyAsync(tape->pid, S.pid, sizeof(int) * (size_t)h->np, cudaMemcpyDeviceToDevice, s));
+        CK(h, cudaMemcpyAsync(tape->cs, S.cstart, sizeof(int) * (size_t)(h->nx + 2), cudaMemcpyDeviceToDevice, s));
+    }
     if (h->reinit) k_line_nodal_kinematics<true><<<nb, LINE_THREADS, 0, s>>>(S, par);
     else k_line_nodal_kinematics<false><<<nb, LINE_THREADS, 0, s>>>(S, par);
     if (!h->usl) {
@@ -268,6 +275,10 @@ int line_step(MpmHandle* h, cudaStream_t s) {
         else k_line_stress<false><<<pb, LINE_THREADS, 0, s>>>(S, h->line_eid, h->nvbx, par);
     }
     CK(h, cudaGetLastError());
+    if (tape) {
+        const float* src[4] = {h->nm, h->nvax, h->nvbx, h->nax};
+        for (int k = 0; k < 4; ++k) CK(h, cudaMemcpyAsync(tape->n[k], src[k], nbytes, cudaMemcpyDeviceToDevice, s));
+    }
     h->step++;
     h->needs_resort = true;
     return MPM_OK;

@@ -326,19 +326,19 @@ class Simulation:
         self._ok(self._lib.mpm_record(self._h, int(nsteps), int(checkpoint_steps), stream))
 
     def adjoint(self, dl_dloc, dl_dvel=None, *, want=("youngs_modulus", "loc", "velocity")):
-        """Reverse of the last :meth:`record` for seeds dL/dx_end (n, 2) and
-        dL/dv_end (n, 2, optional), original particle order.  Returns a dict
+        """Reverse of the last :meth:`record` for seeds dL/dx_end (n, ndim) and
+        dL/dv_end (n, ndim, optional), original particle order.  Returns a dict
         with the requested gradients at the recorded start: "youngs_modulus"
-        (n,), "loc" (n, 2), "velocity" (n, 2).  Seeds and outputs are NumPy
-        arrays, or CUDA tensors (then the outputs are CUDA tensors too)."""
-        n = self.n
-        p, dev, keep = _in_arg(dl_dloc, np.float32, n * 2)
+        (n,), "loc" (n, ndim), "velocity" (n, ndim).  Seeds and outputs are
+        NumPy arrays, or CUDA tensors (then the outputs are CUDA tensors too)."""
+        n, d = self.n, self.ndim
+        p, dev, keep = _in_arg(dl_dloc, np.float32, n * d)
         pv, keepv = None, None
         if dl_dvel is not None:
-            pv, vdev, keepv = _in_arg(dl_dvel, np.float32, n * 2)
+            pv, vdev, keepv = _in_arg(dl_dvel, np.float32, n * d)
             if vdev != dev:
                 raise ValueError("seeds must both be host arrays or both CUDA tensors")
-        shapes = {"youngs_modulus": (n,), "loc": (n, 2), "velocity": (n, 2)}
+        shapes = {"youngs_modulus": (n,), "loc": (n, d), "velocity": (n, d)}
         out = {}
         for k in want:
             if dev:

@@ -3,8 +3,9 @@
 Host-side arrays in the reference's shapes and initial values
 (particle.py:53-71).  A solve uploads them to the GPU.  Two build extensions:
 ``material`` may be a list of materials with per-particle ``material_ids`` (one
-population mixing materials), and ``youngs_modulus`` gives LinearElastic
-particles their own Young's modulus.
+population mixing materials), and ``youngs_modulus`` gives particles their
+own Young's modulus (replacing LinearElastic ``youngs_modulus`` or
+SimpleMaterial ``E``).
 """
 from __future__ import annotations
 

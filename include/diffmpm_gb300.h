@@ -71,7 +71,7 @@ typedef enum MpmScheme { MPM_USF = 0, MPM_USL = 1 } MpmScheme;
  * Constraint (diffmpm/constraint.py:7-20), NodalForce (diffmpm/forces.py:9-18),
  * Linear/Unit (diffmpm/functions.py:16-49) and the material classes. */
 typedef struct MpmDesc {
-    int ndim;                      /* 2 = Quadrilateral4Node (1 reserved for Linear1D) */
+    int ndim;                      /* 2 = Quadrilateral4Node, 1 = Linear1D */
     int nelements[2];              /* nx, ny */
     double el_len[2];              /* hx, hy (converted to float32 like jnp.asarray) */
     int scheme;                    /* MpmScheme */
@@ -231,21 +231,24 @@ int mpm_get_counters(const MpmHandle* h, int64_t* resorts, int64_t* rollbacks);
 
 /* Differentiation.  The reference differentiates solve_jit with jax.grad
  * (examples/optim_1d.py:33-41,55 takes jax.value_and_grad of a loss of the
- * final positions); these two calls are the hand-written reverse of the same
- * steps, for the USF scheme with the per-step volume set-up
- * (reinit_each_step = 1), LinearElastic or SimpleMaterial, without particle
- * tractions (other configurations return MPM_ERR_UNSUPPORTED).
+ * final velocities); these two calls are the hand-written reverse of the same
+ * steps, with the per-step volume set-up (reinit_each_step = 1), LinearElastic
+ * or SimpleMaterial, without particle tractions or particle velocity
+ * constraints: the USF scheme on Quadrilateral4Node meshes, USF or USL on
+ * Linear1D meshes (other configurations return MPM_ERR_UNSUPPORTED).
  *
  * mpm_record advances `nsteps` steps like mpm_step and keeps a checkpoint of
- * the full state every `checkpoint_steps` steps (and at the end). */
+ * the full state every `checkpoint_steps` steps (and at the end); on a
+ * Linear1D mesh it keeps every step's start state instead (checkpoint_steps
+ * is not used). */
 int mpm_record(MpmHandle* h, int nsteps, int checkpoint_steps, void* stream);
 
 /* Gradient of a loss L(x_end, v_end) through the steps of the last
- * mpm_record, given dL/dx_end (n, 2) and dL/dv_end (n, 2; NULL = zero) in
+ * mpm_record, given dL/dx_end (n, ndim) and dL/dv_end (n, ndim; NULL = zero) in
  * original particle order.  Writes, in original particle order, any of
  * dL/dE (n; per-particle Young's modulus, or the material's modulus counted
  * per particle: the sum over a material's particles is dL/dE of that
- * material), dL/dx_0 (n, 2) and dL/dv_0 (n, 2) at the recorded start; NULL
+ * material), dL/dx_0 (n, ndim) and dL/dv_0 (n, ndim) at the recorded start; NULL
  * outputs are skipped.  Each segment between checkpoints is re-run to rebuild
  * its per-step tape.  The handle is left at the recorded end state, so the
  * call may be repeated with other seeds; any call that changes the state

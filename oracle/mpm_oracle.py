@@ -662,9 +662,10 @@ class Particles:
 
     ``material`` may be one material (the reference) or a list of materials
     with per-particle ``material_ids`` (a build extension: one population that
-    mixes materials).  ``youngs_modulus`` optionally gives a per-particle E for
-    LinearElastic particles (a build extension used by the differentiation
-    workload).
+    mixes materials).  ``youngs_modulus`` optionally gives a per-particle E
+    that replaces the material's (LinearElastic ``youngs_modulus``,
+    SimpleMaterial ``E``; a build extension used by the differentiation
+    workloads).
     """
 
     def __init__(self, loc, material, element_ids, initialized=None, data=None,
@@ -796,6 +797,10 @@ class Particles:
             elif isinstance(mat, LinearElastic) and self.youngs_modulus is not None:
                 self.stress[sel] = self.stress[sel] + _le_field_stress(
                     mat, self.youngs_modulus[sel], self.dstrain[sel])
+            elif isinstance(mat, SimpleMaterial) and self.youngs_modulus is not None:
+                # build extension: the per-particle E replaces the material's E
+                E = self.youngs_modulus[sel].astype(self.dstrain.dtype)
+                self.stress[sel] = self.stress[sel] + self.dstrain[sel] * E[:, None, None]
             else:
                 self.stress[sel] = self.stress[sel] + mat.compute_stress(self.dstrain[sel])
 

@@ -3,7 +3,7 @@ import numpy as np
 
 
 def bar(api, nx=40, ppe=3, scheme="usf", velocity_update=False, sim_steps=50, dt=2e-4,
-        material="linear", gravity=-9.81, seed=4, **kw):
+        material="linear", gravity=-9.81, seed=4, E=None, **kw):
     """A bar of ``nx`` elements on [0, 1], ``ppe`` particles per element over
     the middle 80 % of the elements with seeded jitter, node 0 fixed, a
     sinusoidal initial velocity, gravity along the bar and a concentrated
@@ -22,9 +22,27 @@ def bar(api, nx=40, ppe=3, scheme="usf", velocity_update=False, sim_steps=50, dt
     cnf = [api.NodalForce(node_ids=np.array([nx]), function=fn, dir=0, force=2.0)]
     cons = [(np.array([0]), api.Constraint(0, 0.0))]
     el = api.Linear1D(nx, nx, h, cons, concentrated_nodal_forces=cnf, **kw)
-    ps = api.Particles(x.reshape(-1, 1, 1), mat, np.zeros(x.size, dtype=np.int32), **kw)
+    ps = api.Particles(x.reshape(-1, 1, 1), mat, np.zeros(x.size, dtype=np.int32),
+                       youngs_modulus=E, **kw)
     ps.velocity[:] = (0.05 * np.sin(np.pi * x)).reshape(-1, 1, 1)
     mesh = api.Mesh1D({"particles": [ps], "elements": el, "particle_surface_traction": []})
     solver = api.MPMExplicit(mesh, dt, scheme=scheme, velocity_update=velocity_update,
                              sim_steps=sim_steps)
     return solver, np.array([gravity])
+
+
+def point(api, E=100.0, scheme="usl", dt=0.01, sim_steps=1000, v0=0.1, **kw):
+    """The reference's 1-D optimisation example (examples/optim_1d.py:14-26):
+    one element of length 1 with node 0 fixed, one SimpleMaterial particle
+    (density 1) at 0.5 moving at ``v0``, no gravity.  ``E`` is the material's
+    modulus (a number) or a per-particle array."""
+    Em = float(np.ravel(E)[0])
+    mat = api.SimpleMaterial({"E": Em, "density": 1.0})
+    cons = [(np.array([0]), api.Constraint(0, 0.0))]
+    el = api.Linear1D(1, 1, 1.0, cons, **kw)
+    Ep = None if np.ndim(E) == 0 else np.asarray(E, np.float64)
+    ps = api.Particles(np.array([0.5]).reshape(1, 1, 1), mat, np.array([0]), youngs_modulus=Ep, **kw)
+    ps.velocity[:] = v0
+    mesh = api.Mesh1D({"particles": [ps], "elements": el, "particle_surface_traction": []})
+    solver = api.MPMExplicit(mesh, dt, scheme=scheme, sim_steps=sim_steps)
+    return solver, np.array([0.0])

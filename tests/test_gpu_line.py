@@ -80,8 +80,29 @@ def test_line_unsupported_parts(built):
     gs._upload(sim)
     sim.initialize()
     with pytest.raises(D.MpmError):
-        sim.record(3, 1)
-    with pytest.raises(D.MpmError):
         D.Batch([sim])
     with pytest.raises(D.MpmError):
         sim.run_phase("nodal_kinematics")
+
+
+def test_line_adjoint_refusals(built):
+    """The 1-D adjoint covers solve_jit semantics without particle velocity
+    constraints, and needs a recording that is still current."""
+    gs, g = L.bar(D, sim_steps=3)
+    sim = gs.simulation(g, reinit=False)
+    gs._upload(sim)
+    sim.initialize()
+    with pytest.raises(D.MpmError):
+        sim.record(3)
+    sim.close()
+    sim = gs.simulation(g, reinit=True)
+    gs._upload(sim)
+    sim.initialize()
+    seed = np.ones((sim.n, 1), np.float32)
+    with pytest.raises(D.MpmError):
+        sim.adjoint(seed)            # nothing recorded
+    sim.record(3)
+    sim.step(1)                      # the recorded run is overwritten
+    with pytest.raises(D.MpmError):
+        sim.adjoint(seed)
+    sim.close()
