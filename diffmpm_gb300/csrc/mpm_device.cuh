@@ -229,12 +229,12 @@ __device__ __forceinline__ float node_sum(const float (*s)[SC_STRIDE], int tid) 
 // same bits.
 constexpr int ROW_P = 160;
 
-template <int NF, class F>
-__device__ __forceinline__ void row_pass(float (*buf)[ROW_P], const float* const (&src)[NF], int rb,
+template <int NF, int P = ROW_P, class F>
+__device__ __forceinline__ void row_pass(float (*buf)[P], const float* const (&src)[NF], int rb,
                                          int re, int cb, int ce, int lane, F&& f) {
     #pragma unroll 1
-    for (int p0 = rb; p0 < re; p0 += ROW_P) {
-        const int p1 = min(p0 + ROW_P, re);
+    for (int p0 = rb; p0 < re; p0 += P) {
+        const int p1 = min(p0 + P, re);
         for (int q = p0 + lane; q < p1; q += 32) {
             #pragma unroll
             for (int k = 0; k < NF; ++k)

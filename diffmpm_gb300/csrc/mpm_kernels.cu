@@ -441,13 +441,14 @@ __device__ __forceinline__ void force_contrib(const SimDev& S, int q, const Forc
 //   (element.py:191-202), velocity constraints (element.py:331-334).
 // ---------------------------------------------------------------------------
 constexpr int K1_NF = 5;   // x, y, vx, vy, rho (solve_jit) or mass (solve)
+constexpr int K1_ROW_P = 128;   // particles of a row per pass (three CTAs per SM)
 
 template <bool REINIT>
 __device__ __forceinline__ void nodal_kinematics_tile(const SimDev& S, const int4 T,
                                                       Control* __restrict__ ctl, int k) {
     constexpr int NQ = 12;
     __shared__ float s_c[NQ][SC_STRIDE];               // [m, px, py] x corner, per cell
-    __shared__ float s_row[TILE_CY][K1_NF][ROW_P];     // staged particles of each cell row
+    __shared__ float s_row[TILE_CY][K1_NF][K1_ROW_P];  // staged particles of each cell row
     __shared__ int s_cs[TILE_CY][33];
     __shared__ TileGeo G;
     const int parity = (load_step(ctl) + k) & 1;
@@ -487,8 +488,8 @@ __device__ __forceinline__ void nodal_kinematics_tile(const SimDev& S, const int
         #pragma unroll
         for (int k = 0; k < NQ; ++k) acc[k] = 0.0f;
         const float* const src[K1_NF] = {S.x, S.y, S.vx, S.vy, REINIT ? rho : S.mass};
-        float (*buf)[ROW_P] = s_row[ly];
-        row_pass<K1_NF>(buf, src, cs[0], cs[32], cb, ce, lx, [&](int, int j) {
+        float (*buf)[K1_ROW_P] = s_row[ly];
+        row_pass<K1_NF, K1_ROW_P>(buf, src, cs[0], cs[32], cb, ce, lx, [&](int, int j) {
             const float m = REINIT ? fm(V0, buf[4][j]) : buf[4][j];
             float cc[NQ];
             mass_contrib(buf[0][j], buf[1][j], buf[2][j], buf[3][j], m, g.cx, g.rx, g.cy, g.ry, cc);
@@ -535,14 +536,14 @@ __device__ __forceinline__ void nodal_kinematics_tile(const SimDev& S, const int
 }
 
 template <bool REINIT>
-__global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
+__global__ void __launch_bounds__(TILE_THREADS, TILE_CTAS_LIGHT)
 k_nodal_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
                    Control* __restrict__ ctl, int k) {
     nodal_kinematics_tile<REINIT>(S, tiles[blockIdx.x], ctl, k);
 }
 
 template <bool REINIT>
-__global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
+__global__ void __launch_bounds__(TILE_THREADS, TILE_CTAS_LIGHT)
 k_nodal_kinematics_batch(const TileDesc* __restrict__ td, int k) {
     __shared__ TileDesc sT;
     load_tile(td + blockIdx.x, sT);
@@ -991,14 +992,14 @@ __device__ __forceinline__ void particle_kinematics_tile(const SimDev& S, const 
 }
 
 template <bool USL, bool REINIT>
-__global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
+__global__ void __launch_bounds__(TILE_THREADS, USL ? TILE_MIN_CTAS : TILE_CTAS_LIGHT)
 k_particle_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
                       Control* __restrict__ ctl, int k) {
     particle_kinematics_tile<USL, REINIT>(S, tiles[blockIdx.x], ctl, k);
 }
 
 template <bool USL, bool REINIT>
-__global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
+__global__ void __launch_bounds__(TILE_THREADS, USL ? TILE_MIN_CTAS : TILE_CTAS_LIGHT)
 k_particle_kinematics_batch(const TileDesc* __restrict__ td, int k) {
     __shared__ TileDesc sT;
     load_tile(td + blockIdx.x, sT);
@@ -1009,7 +1010,7 @@ k_particle_kinematics_batch(const TileDesc* __restrict__ td, int k) {
 // Launchers
 // ---------------------------------------------------------------------------
 // The step kernels use 50-110 KB of shared memory per CTA and are sized for two
-// CTAs per SM: ask for the largest shared-memory carveout once per kernel.
+// or three CTAs per SM: ask for the largest shared-memory carveout once per kernel.
 template <class K>
 static void prefer_shared(K kernel) {
     static bool done = false;

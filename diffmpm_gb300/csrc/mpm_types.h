@@ -22,6 +22,9 @@ constexpr int TILE_NX = TILE_CX - 1;     // nodes owned per tile row
 constexpr int TILE_NY = TILE_CY - 1;     // node rows owned per tile
 constexpr int TILE_THREADS = TILE_CX * TILE_CY;
 constexpr int TILE_MIN_CTAS = 16 / TILE_CY * 2;   // resident CTAs per SM the kernels are built for
+// The nodal kinematics and USF G2P kernels fit 40 registers a thread and
+// < 75 KB of shared memory, so three of their CTAs are resident per SM.
+constexpr int TILE_CTAS_LIGHT = 3 * TILE_MIN_CTAS / 2;
 
 enum StatusBits : int {
     ST_OUT_OF_MESH = 1,     // a particle left the mesh
