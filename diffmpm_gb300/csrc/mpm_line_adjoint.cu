@@ -349,6 +349,7 @@ int line_record(MpmHandle* h, int nsteps, cudaStream_t s) {
     using namespace host;
     if (!h->initialized) return fail(h, MPM_ERR_STATE, "initialize first");
     if (nsteps < 1) return fail(h, MPM_ERR_INVALID, "nsteps must be >= 1");
+    if (h->np <= 0) return fail(h, MPM_ERR_STATE, "no particles");
     TRY(line_check(h));
     line_adjoint_free(h);
     LineAdjoint* a = new LineAdjoint();
