@@ -3,11 +3,11 @@ import numpy as np
 
 
 def bar(api, nx=40, ppe=3, scheme="usf", velocity_update=False, sim_steps=50, dt=2e-4,
-        material="linear", gravity=-9.81, seed=4, E=None, **kw):
+        material="linear", gravity=-9.81, seed=4, E=None, vshift=0.0, **kw):
     """A bar of ``nx`` elements on [0, 1], ``ppe`` particles per element over
     the middle 80 % of the elements with seeded jitter, node 0 fixed, a
-    sinusoidal initial velocity, gravity along the bar and a concentrated
-    force ramp at the free end."""
+    sinusoidal initial velocity (plus a uniform ``vshift``), gravity along the
+    bar and a concentrated force ramp at the free end."""
     h = 1.0 / nx
     rng = np.random.Generator(np.random.PCG64(seed))
     e0, e1 = int(0.1 * nx), int(0.9 * nx)
@@ -24,7 +24,7 @@ def bar(api, nx=40, ppe=3, scheme="usf", velocity_update=False, sim_steps=50, dt
     el = api.Linear1D(nx, nx, h, cons, concentrated_nodal_forces=cnf, **kw)
     ps = api.Particles(x.reshape(-1, 1, 1), mat, np.zeros(x.size, dtype=np.int32),
                        youngs_modulus=E, **kw)
-    ps.velocity[:] = (0.05 * np.sin(np.pi * x)).reshape(-1, 1, 1)
+    ps.velocity[:] = (vshift + 0.05 * np.sin(np.pi * x)).reshape(-1, 1, 1)
     mesh = api.Mesh1D({"particles": [ps], "elements": el, "particle_surface_traction": []})
     solver = api.MPMExplicit(mesh, dt, scheme=scheme, velocity_update=velocity_update,
                              sim_steps=sim_steps)

@@ -34,9 +34,12 @@ def oracle_end(case, steps, E, x0=None, v0=None):
     return p.loc.reshape(-1).copy(), p.velocity.reshape(-1).copy()
 
 
+# vshift=8: every particle crosses into the next element during the 40 steps,
+# so the reversed steps follow changing element populations (per-step re-sorts)
 CASES = [dict(scheme="usf"), dict(scheme="usl"), dict(scheme="usf", material="simple"),
          dict(scheme="usl", material="simple", nx=12, ppe=1),
-         dict(scheme="usf", velocity_update=True)]
+         dict(scheme="usf", velocity_update=True),
+         dict(scheme="usf", vshift=8.0), dict(scheme="usl", vshift=8.0)]
 
 
 @pytest.mark.parametrize("case", CASES, ids=lambda c: "-".join(f"{k}={v}" for k, v in c.items()))
