@@ -363,10 +363,7 @@ int reverse_step(MpmHandle* h, AdjointState* a, int t, cudaStream_t s) {
     A.sxx += op; A.syy += op; A.szz += op; A.sxy += op; A.rho += op;
     A.cflag += oc;
     A.nm += on; A.nvax += on; A.nvay += on; A.nvbx += on; A.nvby += on; A.nax += on; A.nay += on;
-    CK(h, launch_rev_nodal_update(A, h->dtiles, h->ntiles, s));
-    CK(h, launch_rev_forces(A, s));
-    CK(h, launch_rev_nodal_kinematics(A, h->dtiles, h->ntiles, s));
-    CK(h, launch_rev_mass_momentum(A, s));
+    CK(h, launch_rev_step(A, h->usl, h->dtiles, h->ntiles, s));
     return MPM_OK;
 }
 
@@ -412,7 +409,6 @@ int emit_all(MpmHandle* h, AdjointState* a, float* dl_dE, float* dl_dloc0, float
 
 int check_supported(MpmHandle* h) {
     if (h->ndim != 2) return fail(h, MPM_ERR_UNSUPPORTED, "the adjoint implements Quadrilateral4Node meshes");
-    if (h->usl) return fail(h, MPM_ERR_UNSUPPORTED, "the adjoint implements the USF scheme");
     if (!h->reinit)
         return fail(h, MPM_ERR_UNSUPPORTED,
                     "the adjoint implements the per-step volume set-up of solve_jit");
@@ -746,7 +742,7 @@ int mpm_batch_adjoint(MpmBatch* b, const float* const* dl_dloc, const float* con
             }
             if (r != MPM_OK) break;
             BCK(b, launch_adj_table(x->d_bases, n, t, x->d_table, s));
-            BCK(b, launch_rev_batch(x->d_table, b->d_tiles, b->ntiles, x->part_blocks,
+            BCK(b, launch_rev_batch(x->d_table, b->cfg.usl, b->d_tiles, b->ntiles, x->part_blocks,
                                     x->n_part_blocks, s));
         }
         for (int i = 0; i < n && r == MPM_OK; ++i) {

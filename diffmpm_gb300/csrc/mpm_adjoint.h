@@ -1,7 +1,8 @@
-// Reverse (adjoint) passes of the explicit MPM step, USF with the per-step
-// volume set-up of solve_jit (diffmpm/solver.py:81-85, 100-111, 179-213).
+// Reverse (adjoint) passes of the explicit MPM step, USF or USL, with the
+// per-step volume set-up of solve_jit (diffmpm/solver.py:81-85, 100-111,
+// 179-213).
 //
-// The reverse of one step runs four launches over the step's tape (the
+// The reverse of one USF step runs four launches over the step's tape (the
 // particle state at the step start and the nodal values the forward step
 // produced), in the reverse order of the forward phases:
 //   1. node pass      transposed G2P (v-hat, a-hat adjoints gathered to the
@@ -12,6 +13,11 @@
 //   3. node pass      transposed strain-rate gather (nodal-velocity adjoint)
 //                     and the reverse nodal velocity p/m with constraints
 //   4. particle pass  reverse of the mass and momentum P2G
+// A USL step (stress update after G2P, from the updated nodal velocities)
+// runs two more first: U, a particle pass reversing that stress update, and
+// G, the node pass gathering its strain-rate adjoints into the nodal
+// velocity adjoint that pass 1 adds; then passes 1-4 with the forces of pass
+// 2 on the start-of-step stress and no gather in pass 3.
 // Every node sum is formed in a fixed order (the four cells around the node,
 // particles of a cell in storage order), so the adjoint is deterministic.
 #pragma once
@@ -42,10 +48,12 @@ struct AdjStep {
     // adjoint of the particle state (in: end of step; out: start of step) and
     // the accumulated dL/dE per particle
     float *lx, *ly, *lvx, *lvy, *lsxx, *lsyy, *lszz, *lsxy, *lrho, *lE;
-    // per-particle adjoints of the strain rates and centroid rates (pass 2 -> 3)
+    // per-particle adjoints of the strain rates and centroid rates (USF:
+    // pass 2 -> 3; USL: pass U -> G and 2)
     float *r0b, *r1b, *r3b, *c0b, *c1b;
     // nodal adjoints: force, mass and phase-1 velocity from the nodal update
-    // (pass 1 -> 2, 3), momentum and total mass (pass 3 -> 4)
+    // (pass 1 -> 2, 3; USL pass G leaves its vB-bar in vabx, vaby for pass 1),
+    // momentum and total mass (pass 3 -> 4)
     float *fbx, *fby, *mb, *vabx, *vaby;
     float *qbx, *qby, *mbt;
     int* cnt;              // particles per cell at the step start (pass 1 -> 2, 4)
@@ -53,16 +61,12 @@ struct AdjStep {
     long long sp, sn, sc;
 };
 
-// Passes 1 and 3 run over the forward kernels' tile list, passes 2 and 4 over
-// the particles.
-cudaError_t launch_rev_nodal_update(const AdjStep& A, const int4* tiles, int ntiles,
-                                    cudaStream_t s);
-cudaError_t launch_rev_forces(const AdjStep& A, cudaStream_t s);
-cudaError_t launch_rev_nodal_kinematics(const AdjStep& A, const int4* tiles, int ntiles,
-                                        cudaStream_t s);
-cudaError_t launch_rev_mass_momentum(const AdjStep& A, cudaStream_t s);
+// The passes of one reverse step: node passes over the forward kernels' tile
+// list, particle passes over the particles.
+cudaError_t launch_rev_step(const AdjStep& A, bool usl, const int4* tiles, int ntiles,
+                            cudaStream_t s);
 
-// Batches: table[i] = bases[i] with the tape pointers at slot t; then the four
+// Batches: table[i] = bases[i] with the tape pointers at slot t; then the
 // passes over every simulation: passes 1 and 3 over the batch's tile list
 // (tile t of simulation tiles[t].x), passes 2 and 4 with CTA b on simulation
 // part_blocks[b].x, particles part_blocks[b].y * 256 .. + 255.
@@ -71,7 +75,7 @@ constexpr int ADJ_BLOCK = 256;
 // block copies the simulation's arguments once and walks ADJ_ITER chunks.
 constexpr int ADJ_ITER = 4;
 cudaError_t launch_adj_table(const AdjStep* bases, int n, int t, AdjStep* table, cudaStream_t s);
-cudaError_t launch_rev_batch(const AdjStep* table, const int4* tiles, int ntiles,
+cudaError_t launch_rev_batch(const AdjStep* table, bool usl, const int4* tiles, int ntiles,
                              const int2* part_blocks, int n_part_blocks, cudaStream_t s);
 
 // *mismatch += number of i < n with a[i] != b[i] bitwise (4-byte words).

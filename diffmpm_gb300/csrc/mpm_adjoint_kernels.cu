@@ -1,7 +1,9 @@
-// Reverse passes of the explicit MPM step (USF, per-step volume set-up).
+// Reverse passes of the explicit MPM step (USF or USL, per-step volume set-up).
 //
-// Notation of the forward step, particle p in cell c with corners k = 0..3
-// (diffmpm/element.py, particle.py; the step order of diffmpm/scheme.py:22-67):
+// Notation of the forward USF step, particle p in cell c with corners k = 0..3
+// (diffmpm/element.py, particle.py; the step order of diffmpm/scheme.py:22-67;
+// USL, scheme.py:112-133, uses sig and V0 in F and updates sig, rho after G2P
+// with r = flush(G^T vB), c = flush(Gc^T vB) at the start-of-step positions):
 //   m    = V0 rho,           V0 = V_el / count(c)            (solver.py:81-85)
 //   M_n  = sum N m,  P_n = flush(sum N m v),  vA = C(flush(P / M))
 //   r    = flush(G^T vA) (xx, yy, xy),  c = flush(Gc^T vA),  dvol = dt (c0 + c1)
@@ -140,8 +142,14 @@ __device__ __forceinline__ void rev_tile_loads(const AdjStep& A, int c0x, int c0
 
 // Reverse nodal update of node n from the G2P adjoint sums (vB-bar, aB-bar):
 // vB = flush(C(vA + a dt)), aB = flush(C0(a)), a = F / M (element.py:305-329).
+// USL adds the vB-bar of its stress update, gathered by pass G into vabx, vaby.
+template <bool USL>
 __device__ __forceinline__ void rev_node_update(const AdjStep& A, int n, float vbx, float vby,
                                                 float abx, float aby) {
+    if (USL) {
+        vbx = fa(vbx, A.vabx[n]);
+        vby = fa(vby, A.vaby[n]);
+    }
     float fbx = 0.0f, fby = 0.0f, mb = 0.0f, wbx = 0.0f, wby = 0.0f;
     const float M = A.nm[n];
     if (M != 0.0f) {
@@ -168,6 +176,7 @@ __device__ __forceinline__ void rev_node_update(const AdjStep& A, int n, float v
 // gathered to the nodes with the shape functions), the reverse nodal update
 // and the particle count of every cell (particle.py:208-247, element.py:305-329).
 // ---------------------------------------------------------------------------
+template <bool USL>
 __device__ __forceinline__ void rev_nodal_update_tile(const AdjStep& A, const int4 T) {
     constexpr int NQ = 16;   // [v-hat bar x, y, a-hat bar x, y] x corner
     __shared__ float s_c[NQ][SC_STRIDE];
@@ -235,126 +244,72 @@ __device__ __forceinline__ void rev_nodal_update_tile(const AdjStep& A, const in
     } else if (own_cell) {
         A.cnt[cj * A.nx + ci] = 0;
     }
-    if (node_ok) rev_node_update(A, node, sum[0], sum[1], sum[2], sum[3]);
+    if (node_ok) rev_node_update<USL>(A, node, sum[0], sum[1], sum[2], sum[3]);
 }
 
+template <bool USL>
 __global__ void __launch_bounds__(TILE_THREADS, 2)
 k_rev_nodal_update(const __grid_constant__ AdjStep A, const int4* __restrict__ tiles) {
-    rev_nodal_update_tile(A, tiles[blockIdx.x]);
+    rev_nodal_update_tile<USL>(A, tiles[blockIdx.x]);
 }
 
+template <bool USL>
 __global__ void __launch_bounds__(TILE_THREADS, 2)
 k_rev_nodal_update_batch(const AdjStep* __restrict__ table, const int4* __restrict__ tiles) {
     __shared__ AdjStep sA;
     const int4 T = tiles[blockIdx.x];
     load_step_args(table + T.x, sA);
-    rev_nodal_update_tile(sA, T);
+    rev_nodal_update_tile<USL>(sA, T);
 }
 
-// ---------------------------------------------------------------------------
-// Pass 2: reverse of the forces (element.py:236-268, 842-901) and of the USF
-// strain / volume / stress update (particle.py:249-327, material.py:113-131).
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q, float x, float y) {
-    if (q >= A.np) return;
-    int ci, cj;
-    particle_cell(A, x, y, ci, cj);
-    const CellGeo g = cell_geo(ci, cj, A.hx, A.hy);
-    const float xi = natural(x, g.cx, g.rx), eta = natural(y, g.cy, g.ry);
-    float N[4], Gx[4], Gy[4], Gcx[4], Gcy[4];
-    shape4(xi, eta, N);
-    dshape4(xi, eta, g.rx, g.ry, Gx, Gy);
-    dshape4(0.0f, 0.0f, g.rx, g.ry, Gcx, Gcy);
-    const int ll = cj * (A.nx + 1) + ci;
-    const int ids[4] = {ll, ll + 1, ll + A.nx + 2, ll + A.nx + 1};
-    const int cnt = A.cnt[cj * A.nx + ci];
-    const float V0 = cnt ? fdv(A.vol_el, (float)cnt) : 0.0f;
-    const float rho0 = A.rho[q];
-    const float m = fm(V0, rho0);
-
-    // forward recomputation of the strain rates (the left-to-right sums of
-    // strain_rate4) and of the stress update; sAx, sAy: sum of +-vA (signs
-    // + - + - of d Gx_k / d eta and d Gy_k / d xi)
-    float r0 = 0.0f, r1 = 0.0f, r3a = 0.0f, r3b_ = 0.0f, c0 = 0.0f, c1 = 0.0f;
-    float sAx = 0.0f, sAy = 0.0f;
+// Strain rates (xx, yy, xy) and centroid rates of a particle from the nodal
+// velocities (nvx, nvy) of its cell's corners, the left-to-right sums of
+// strain_rate4 with its flushes; sx, sy: signed sums + - + - of the corner
+// velocities (d Gx_k / d eta and d Gy_k / d xi carry these signs).
+__device__ __forceinline__ void rates_at(const int ids[4], const float Gx[4], const float Gy[4],
+                                         const float Gcx[4], const float Gcy[4],
+                                         const float* __restrict__ nvx, const float* __restrict__ nvy,
+                                         float& r0, float& r1, float& r3, float& c0, float& c1,
+                                         float& sx, float& sy) {
+    float r3a = 0.0f, r3b_ = 0.0f;
     #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        const float vax = A.nvax[ids[k]], vay = A.nvay[ids[k]];
+        const float vx = nvx[ids[k]], vy = nvy[ids[k]];
         if (k == 0) {
-            r0 = fm(Gx[0], vax);
-            r1 = fm(Gy[0], vay);
-            r3a = fm(Gx[0], vay);
-            r3b_ = fm(Gy[0], vax);
-            c0 = fm(Gcx[0], vax);
-            c1 = fm(Gcy[0], vay);
-            sAx = vax;
-            sAy = vay;
+            r0 = fm(Gx[0], vx);
+            r1 = fm(Gy[0], vy);
+            r3a = fm(Gx[0], vy);
+            r3b_ = fm(Gy[0], vx);
+            c0 = fm(Gcx[0], vx);
+            c1 = fm(Gcy[0], vy);
+            sx = vx;
+            sy = vy;
         } else {
-            r0 = fa(r0, fm(Gx[k], vax));
-            r1 = fa(r1, fm(Gy[k], vay));
-            r3a = fa(r3a, fm(Gx[k], vay));
-            r3b_ = fa(r3b_, fm(Gy[k], vax));
-            c0 = fa(c0, fm(Gcx[k], vax));
-            c1 = fa(c1, fm(Gcy[k], vay));
-            sAx = (k & 1) ? fs(sAx, vax) : fa(sAx, vax);
-            sAy = (k & 1) ? fs(sAy, vay) : fa(sAy, vay);
+            r0 = fa(r0, fm(Gx[k], vx));
+            r1 = fa(r1, fm(Gy[k], vy));
+            r3a = fa(r3a, fm(Gx[k], vy));
+            r3b_ = fa(r3b_, fm(Gy[k], vx));
+            c0 = fa(c0, fm(Gcx[k], vx));
+            c1 = fa(c1, fm(Gcy[k], vy));
+            sx = (k & 1) ? fs(sx, vx) : fa(sx, vx);
+            sy = (k & 1) ? fs(sy, vy) : fa(sy, vy);
         }
     }
     r0 = flush(r0);
     r1 = flush(r1);
-    const float r3 = flush(fa(r3a, r3b_));
+    r3 = flush(fa(r3a, r3b_));
     c0 = flush(c0);
     c1 = flush(c1);
-    PState p{};
-    p.sxx = A.sxx[q];
-    p.syy = A.syy[q];
-    p.szz = A.szz[q];
-    p.sxy = A.sxy[q];
-    p.rho = rho0;
-    const float dvol = fm(A.dt, fa(c0, c1));
-    const MatDev& mat = A.mats[A.mat[q]];
-    const float Ep = A.E ? A.E[q] : -1.0f;
-    const float f = strain_stress_update(mat, Ep, A.dt, r0, r1, r3, dvol, p);
-    const float V = fm(V0, f);
+}
 
-    // G2P, external and internal forces: adjoints of the shape functions (as
-    // x-bar, y-bar contributions), of m and V, of the end-of-step stress, and
-    // the signed sums of the gradient adjoints
-    float gx, gy, hx, hy;
-    g2p_seeds(A, q, gx, gy, hx, hy);
-    float xb = A.lx[q], yb = A.ly[q];
-    float mb = 0.0f, Vb = 0.0f, fsxx = 0.0f, fsyy = 0.0f, fsxy = 0.0f, sgx = 0.0f, sgy = 0.0f;
-    #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const int n = ids[k];
-        const float fbx = A.fbx[n], fby = A.fby[n];
-        const float fg = fa(fm(fbx, A.gx), fm(fby, A.gy));   // F-bar . g
-        const float Nb = fa(fa(fa(fm(gx, A.nvbx[n]), fm(gy, A.nvby[n])),
-                               fa(fm(hx, A.nax[n]), fm(hy, A.nay[n]))),
-                            fm(m, fg));
-        mb = fa(mb, fm(N[k], fg));
-        const float fx = fa(fm(Gx[k], p.sxx), fm(Gy[k], p.sxy));
-        const float fy = fa(fm(Gy[k], p.syy), fm(Gx[k], p.sxy));
-        Vb = fs(Vb, fa(fm(fbx, fx), fm(fby, fy)));
-        fsxx = fa(fsxx, fm(fbx, Gx[k]));
-        fsyy = fa(fsyy, fm(fby, Gy[k]));
-        fsxy = fa(fsxy, fa(fm(fbx, Gy[k]), fm(fby, Gx[k])));
-        const float gxk = -fm(V, fa(fm(fbx, p.sxx), fm(fby, p.sxy)));
-        const float gyk = -fm(V, fa(fm(fbx, p.sxy), fm(fby, p.syy)));
-        sgx = (k & 1) ? fs(sgx, gxk) : fa(sgx, gxk);
-        sgy = (k & 1) ? fs(sgy, gyk) : fa(sgy, gyk);
-        xb = fa(xb, fm(Nb, Gx[k]));
-        yb = fa(yb, fm(Nb, Gy[k]));
-    }
-    // stress adjoint at the end of the forces: loss/next-step part + force part
-    const float sbxx = fs(A.lsxx[q], fm(V, fsxx));
-    const float sbyy = fs(A.lsyy[q], fm(V, fsyy));
-    const float sbzz = A.lszz[q];
-    const float sbxy = fs(A.lsxy[q], fm(V, fsxy));
-
-    // reverse of sig' = sig + D r dt
-    const float d0 = fm(r0, A.dt), d1 = fm(r1, A.dt), d3 = fm(r3, A.dt);
-    float d0b = 0.0f, d1b = 0.0f, d3b = 0.0f, Eb = 0.0f;
+// Reverse of sig' = sig + D(E) r dt for the stress adjoint sb: the strain-rate
+// adjoints (zero where the forward flushed the rate) and dL/dE.
+__device__ __forceinline__ void stress_reverse(const MatDev& mat, float Ep, float dt, float r0, float r1,
+                                               float r3, float sbxx, float sbyy, float sbzz, float sbxy,
+                                               float& r0b, float& r1b, float& r3b, float& Eb) {
+    const float d0 = fm(r0, dt), d1 = fm(r1, dt), d3 = fm(r3, dt);
+    float d0b = 0.0f, d1b = 0.0f, d3b = 0.0f;
+    Eb = 0.0f;
     if (mat.type == MAT_LINEAR_ELASTIC) {
         float a1 = mat.a1, a2 = mat.a2, G = mat.G;
         if (Ep >= 0.0f) {
@@ -375,19 +330,177 @@ __device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q, float x, 
         d3b = fm(E, sbxy);
         Eb = fa(fa(fm(d0, sbxx), fm(d1, sbyy)), fm(d3, sbxy));
     }
-    const float r0b = r0 != 0.0f ? fm(d0b, A.dt) : 0.0f;
-    const float r1b = r1 != 0.0f ? fm(d1b, A.dt) : 0.0f;
-    const float r3b = r3 != 0.0f ? fm(d3b, A.dt) : 0.0f;
+    r0b = r0 != 0.0f ? fm(d0b, dt) : 0.0f;
+    r1b = r1 != 0.0f ? fm(d1b, dt) : 0.0f;
+    r3b = r3 != 0.0f ? fm(d3b, dt) : 0.0f;
+}
 
-    // reverse of V = V0 (1 + dvol), rho' = rho / (1 + dvol), m = V0 rho
+// ---------------------------------------------------------------------------
+// USL pass U (before pass 1): reverse of the strain / density / stress update
+// that USL runs after G2P from the updated nodal velocities vB, at the
+// positions of the step start (scheme.py:127-133, particle.py:249-327).  The
+// stress adjoint passes through unchanged; the strain-rate and centroid-rate
+// adjoints go to pass G (their transposed gather) and to pass 2 (their
+// position terms); the density adjoint becomes that of the step start.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void rev_stress_usl_at(const AdjStep& A, int q, float x, float y) {
+    if (q >= A.np) return;
+    int ci, cj;
+    particle_cell(A, x, y, ci, cj);
+    const CellGeo g = cell_geo(ci, cj, A.hx, A.hy);
+    float Gx[4], Gy[4], Gcx[4], Gcy[4];
+    dshape4(natural(x, g.cx, g.rx), natural(y, g.cy, g.ry), g.rx, g.ry, Gx, Gy);
+    dshape4(0.0f, 0.0f, g.rx, g.ry, Gcx, Gcy);
+    const int ll = cj * (A.nx + 1) + ci;
+    const int ids[4] = {ll, ll + 1, ll + A.nx + 2, ll + A.nx + 1};
+    float r0, r1, r3, c0, c1, sx, sy;
+    rates_at(ids, Gx, Gy, Gcx, Gcy, A.nvbx, A.nvby, r0, r1, r3, c0, c1, sx, sy);
+    const float dvol = fm(A.dt, fa(c0, c1));
+    const float f = fa(1.0f, dvol);
+    const float rho1 = fdv(A.rho[q], f);
+    const MatDev& mat = A.mats[A.mat[q]];
+    const float Ep = A.E ? A.E[q] : -1.0f;
+    float r0b, r1b, r3b, Eb;
+    stress_reverse(mat, Ep, A.dt, r0, r1, r3, A.lsxx[q], A.lsyy[q], A.lszz[q], A.lsxy[q], r0b, r1b,
+                   r3b, Eb);
     const float lrho = A.lrho[q];
-    const float fb = fs(fm(Vb, V0), fdv(fm(lrho, p.rho), f));
-    const float rhob = fa(fdv(lrho, f), fm(V0, mb));
-    const float c0b = c0 != 0.0f ? fm(fb, A.dt) : 0.0f;
-    const float c1b = c1 != 0.0f ? fm(fb, A.dt) : 0.0f;
+    const float fb = -fdv(fm(lrho, rho1), f);
+    A.r0b[q] = r0b;
+    A.r1b[q] = r1b;
+    A.r3b[q] = r3b;
+    A.c0b[q] = c0 != 0.0f ? fm(fb, A.dt) : 0.0f;
+    A.c1b[q] = c1 != 0.0f ? fm(fb, A.dt) : 0.0f;
+    A.lrho[q] = fdv(lrho, f);
+    A.lE[q] = fa(A.lE[q], Eb);
+}
 
-    // strain-rate part of the gradient adjoints: Gx_k-bar += r0b vAx_k + r3b
-    // vAy_k, Gy_k-bar += r1b vAy_k + r3b vAx_k; their signed sums move x, y
+__global__ void __launch_bounds__(PART_THREADS)
+k_rev_stress_usl(const __grid_constant__ AdjStep A) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < A.np) rev_stress_usl_at(A, q, A.x[q], A.y[q]);
+}
+
+__global__ void __launch_bounds__(PART_THREADS)
+k_rev_stress_usl_batch(const AdjStep* __restrict__ table, const int2* __restrict__ blocks) {
+    __shared__ AdjStep sA;
+    const int2 bm = blocks[blockIdx.x];
+    load_step_args(table + bm.x, sA);
+    #pragma unroll 1
+    for (int k = 0; k < ADJ_ITER; ++k) {
+        const int q = (bm.y * ADJ_ITER + k) * PART_THREADS + threadIdx.x;
+        if (q < sA.np) rev_stress_usl_at(sA, q, sA.x[q], sA.y[q]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Pass 2: reverse of the forces (element.py:236-268, 842-901) and, for USF,
+// of the strain / volume / stress update before them (particle.py:249-327,
+// material.py:113-131).  USL forces use the start-of-step stress and the
+// reset volume V0; the strain-rate adjoints of its later stress update come
+// from pass U and only add their position terms here.
+// ---------------------------------------------------------------------------
+template <bool USL>
+__device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q, float x, float y) {
+    if (q >= A.np) return;
+    int ci, cj;
+    particle_cell(A, x, y, ci, cj);
+    const CellGeo g = cell_geo(ci, cj, A.hx, A.hy);
+    const float xi = natural(x, g.cx, g.rx), eta = natural(y, g.cy, g.ry);
+    float N[4], Gx[4], Gy[4];
+    shape4(xi, eta, N);
+    dshape4(xi, eta, g.rx, g.ry, Gx, Gy);
+    const int ll = cj * (A.nx + 1) + ci;
+    const int ids[4] = {ll, ll + 1, ll + A.nx + 2, ll + A.nx + 1};
+    const int cnt = A.cnt[cj * A.nx + ci];
+    const float V0 = cnt ? fdv(A.vol_el, (float)cnt) : 0.0f;
+    const float rho0 = A.rho[q];
+    const float m = fm(V0, rho0);
+
+    // the stress and volume of the forces: USF recomputes the strain rates
+    // from vA and the stress update; sAx, sAy: signed sums of the corner
+    // velocities the strain rates used (vA for USF, vB for USL)
+    float r0 = 0.0f, r1 = 0.0f, r3 = 0.0f, c0 = 0.0f, c1 = 0.0f, sAx = 0.0f, sAy = 0.0f;
+    PState p{};
+    p.sxx = A.sxx[q];
+    p.syy = A.syy[q];
+    p.szz = A.szz[q];
+    p.sxy = A.sxy[q];
+    p.rho = rho0;
+    float f = 1.0f, V = V0;
+    const MatDev& mat = A.mats[A.mat[q]];
+    const float Ep = A.E ? A.E[q] : -1.0f;
+    if (!USL) {
+        float Gcx[4], Gcy[4];
+        dshape4(0.0f, 0.0f, g.rx, g.ry, Gcx, Gcy);
+        rates_at(ids, Gx, Gy, Gcx, Gcy, A.nvax, A.nvay, r0, r1, r3, c0, c1, sAx, sAy);
+        const float dvol = fm(A.dt, fa(c0, c1));
+        f = strain_stress_update(mat, Ep, A.dt, r0, r1, r3, dvol, p);
+        V = fm(V0, f);
+    }
+
+    // G2P, external and internal forces: adjoints of the shape functions (as
+    // x-bar, y-bar contributions), of m and V, of the stress the forces used,
+    // and the signed sums of the gradient adjoints
+    float gx, gy, hx, hy;
+    g2p_seeds(A, q, gx, gy, hx, hy);
+    float xb = A.lx[q], yb = A.ly[q];
+    float mb = 0.0f, Vb = 0.0f, fsxx = 0.0f, fsyy = 0.0f, fsxy = 0.0f, sgx = 0.0f, sgy = 0.0f;
+    #pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int n = ids[k];
+        const float fbx = A.fbx[n], fby = A.fby[n];
+        const float vBx = A.nvbx[n], vBy = A.nvby[n];
+        const float fg = fa(fm(fbx, A.gx), fm(fby, A.gy));   // F-bar . g
+        const float Nb = fa(fa(fa(fm(gx, vBx), fm(gy, vBy)),
+                               fa(fm(hx, A.nax[n]), fm(hy, A.nay[n]))),
+                            fm(m, fg));
+        if (USL) {
+            sAx = k == 0 ? vBx : (k & 1) ? fs(sAx, vBx) : fa(sAx, vBx);
+            sAy = k == 0 ? vBy : (k & 1) ? fs(sAy, vBy) : fa(sAy, vBy);
+        }
+        mb = fa(mb, fm(N[k], fg));
+        const float fx = fa(fm(Gx[k], p.sxx), fm(Gy[k], p.sxy));
+        const float fy = fa(fm(Gy[k], p.syy), fm(Gx[k], p.sxy));
+        if (!USL) Vb = fs(Vb, fa(fm(fbx, fx), fm(fby, fy)));
+        fsxx = fa(fsxx, fm(fbx, Gx[k]));
+        fsyy = fa(fsyy, fm(fby, Gy[k]));
+        fsxy = fa(fsxy, fa(fm(fbx, Gy[k]), fm(fby, Gx[k])));
+        const float gxk = -fm(V, fa(fm(fbx, p.sxx), fm(fby, p.sxy)));
+        const float gyk = -fm(V, fa(fm(fbx, p.sxy), fm(fby, p.syy)));
+        sgx = (k & 1) ? fs(sgx, gxk) : fa(sgx, gxk);
+        sgy = (k & 1) ? fs(sgy, gyk) : fa(sgy, gyk);
+        xb = fa(xb, fm(Nb, Gx[k]));
+        yb = fa(yb, fm(Nb, Gy[k]));
+    }
+    // stress adjoint: loss/next-step part (through pass U for USL) + force part
+    const float sbxx = fs(A.lsxx[q], fm(V, fsxx));
+    const float sbyy = fs(A.lsyy[q], fm(V, fsyy));
+    const float sbzz = A.lszz[q];
+    const float sbxy = fs(A.lsxy[q], fm(V, fsxy));
+
+    float r0b, r1b, r3b, rhob;
+    if (USL) {
+        r0b = A.r0b[q];
+        r1b = A.r1b[q];
+        r3b = A.r3b[q];
+        rhob = fa(A.lrho[q], fm(V0, mb));
+    } else {
+        float Eb;
+        stress_reverse(mat, Ep, A.dt, r0, r1, r3, sbxx, sbyy, sbzz, sbxy, r0b, r1b, r3b, Eb);
+        // reverse of V = V0 (1 + dvol), rho' = rho / (1 + dvol), m = V0 rho
+        const float lrho = A.lrho[q];
+        const float fb = fs(fm(Vb, V0), fdv(fm(lrho, p.rho), f));
+        rhob = fa(fdv(lrho, f), fm(V0, mb));
+        A.lE[q] = fa(A.lE[q], Eb);
+        A.r0b[q] = r0b;
+        A.r1b[q] = r1b;
+        A.r3b[q] = r3b;
+        A.c0b[q] = c0 != 0.0f ? fm(fb, A.dt) : 0.0f;
+        A.c1b[q] = c1 != 0.0f ? fm(fb, A.dt) : 0.0f;
+    }
+
+    // strain-rate part of the gradient adjoints: Gx_k-bar += r0b v_x,k + r3b
+    // v_y,k, Gy_k-bar += r1b v_y,k + r3b v_x,k; their signed sums move x, y
     sgx = fa(sgx, fa(fm(r0b, sAx), fm(r3b, sAy)));
     sgy = fa(sgy, fa(fm(r1b, sAy), fm(r3b, sAx)));
     const float rxy = fm(fm(0.25f, g.rx), g.ry);
@@ -401,20 +514,16 @@ __device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q, float x, 
     A.lszz[q] = sbzz;
     A.lsxy[q] = sbxy;
     A.lrho[q] = rhob;
-    A.lE[q] = fa(A.lE[q], Eb);
-    A.r0b[q] = r0b;
-    A.r1b[q] = r1b;
-    A.r3b[q] = r3b;
-    A.c0b[q] = c0b;
-    A.c1b[q] = c1b;
 }
 
+template <bool USL>
 __global__ void __launch_bounds__(PART_THREADS, 4)
 k_rev_forces(const __grid_constant__ AdjStep A) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q < A.np) rev_forces_at(A, q, A.x[q], A.y[q]);
+    if (q < A.np) rev_forces_at<USL>(A, q, A.x[q], A.y[q]);
 }
 
+template <bool USL>
 __global__ void __launch_bounds__(PART_THREADS, 4)
 k_rev_forces_batch(const AdjStep* __restrict__ table, const int2* __restrict__ blocks) {
     __shared__ AdjStep sA;
@@ -423,7 +532,7 @@ k_rev_forces_batch(const AdjStep* __restrict__ table, const int2* __restrict__ b
     #pragma unroll 1
     for (int k = 0; k < ADJ_ITER; ++k) {
         const int q = (bm.y * ADJ_ITER + k) * PART_THREADS + threadIdx.x;
-        if (q < sA.np) rev_forces_at(sA, q, sA.x[q], sA.y[q]);
+        if (q < sA.np) rev_forces_at<USL>(sA, q, sA.x[q], sA.y[q]);
     }
 }
 
@@ -431,7 +540,10 @@ k_rev_forces_batch(const AdjStep* __restrict__ table, const int2* __restrict__ b
 // Pass 3: transposed strain-rate gather (vA-bar += sum over particles of
 // G r-bar + Gc c-bar) and the reverse nodal velocity vA = C(flush(P / M)),
 // P = flush(sum N m v) (element.py:191-202, 331-334; particle.py:281-313).
+// The same tile kernel is USL's pass G (the gather alone, of the pass-U
+// adjoints, into vabx, vaby); USL's pass 3 has no gather.
 // ---------------------------------------------------------------------------
+enum RevKinMode { RK_USF, RK_GATHER, RK_NODES };
 __device__ __forceinline__ void rev_node_velocity(const AdjStep& A, int n, float vbx, float vby) {
     float qbx = 0.0f, qby = 0.0f, mbt = A.mb[n];
     const float M = A.nm[n];
@@ -450,6 +562,7 @@ __device__ __forceinline__ void rev_node_velocity(const AdjStep& A, int n, float
     A.mbt[n] = mbt;
 }
 
+template <int MODE>
 __device__ __forceinline__ void rev_nodal_kinematics_tile(const AdjStep& A, const int4 T) {
     constexpr int NQ = 8;    // [vA-bar x, y] x corner
     __shared__ float s_c[NQ][SC_STRIDE];
@@ -503,20 +616,40 @@ __device__ __forceinline__ void rev_nodal_kinematics_tile(const AdjStep& A, cons
             sy = node_sum(s_c + 4, tid);
         }
     }
-    if (node_ok) rev_node_velocity(A, node, fa(A.vabx[node], sx), fa(A.vaby[node], sy));
+    if (!node_ok) return;
+    if (MODE == RK_GATHER) {
+        A.vabx[node] = sx;
+        A.vaby[node] = sy;
+    } else {
+        rev_node_velocity(A, node, fa(A.vabx[node], sx), fa(A.vaby[node], sy));
+    }
 }
 
+// USL pass 3: the reverse nodal velocity of the tile's nodes from vA-bar alone.
+__device__ __forceinline__ void rev_node_velocity_tile(const AdjStep& A, const int4 T) {
+    const int tid = threadIdx.x, tx = tid % TILE_CX, ty = tid / TILE_CX;
+    const int c0x = T.y * TILE_NX - 1, c0y = T.z * TILE_NY - 1;
+    if (tx < TILE_NX && ty < TILE_NY && c0x + 1 + tx <= A.nx && c0y + 1 + ty <= A.ny) {
+        const int node = (c0y + 1 + ty) * (A.nx + 1) + c0x + 1 + tx;
+        rev_node_velocity(A, node, A.vabx[node], A.vaby[node]);
+    }
+}
+
+template <int MODE>
 __global__ void __launch_bounds__(TILE_THREADS, 2)
 k_rev_nodal_kinematics(const __grid_constant__ AdjStep A, const int4* __restrict__ tiles) {
-    rev_nodal_kinematics_tile(A, tiles[blockIdx.x]);
+    if (MODE == RK_NODES) rev_node_velocity_tile(A, tiles[blockIdx.x]);
+    else rev_nodal_kinematics_tile<MODE>(A, tiles[blockIdx.x]);
 }
 
+template <int MODE>
 __global__ void __launch_bounds__(TILE_THREADS, 2)
 k_rev_nodal_kinematics_batch(const AdjStep* __restrict__ table, const int4* __restrict__ tiles) {
     __shared__ AdjStep sA;
     const int4 T = tiles[blockIdx.x];
     load_step_args(table + T.x, sA);
-    rev_nodal_kinematics_tile(sA, T);
+    if (MODE == RK_NODES) rev_node_velocity_tile(sA, T);
+    else rev_nodal_kinematics_tile<MODE>(sA, T);
 }
 
 // ---------------------------------------------------------------------------
@@ -617,27 +750,21 @@ inline int blocks_for(int n, int t) { return (n + t - 1) / t; }
 
 }  // namespace
 
-cudaError_t launch_rev_nodal_update(const AdjStep& A, const int4* tiles, int ntiles,
-                                    cudaStream_t s) {
-    if (ntiles > 0) k_rev_nodal_update<<<ntiles, TILE_THREADS, 0, s>>>(A, tiles);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_rev_forces(const AdjStep& A, cudaStream_t s) {
-    if (A.np <= 0) return cudaSuccess;
-    k_rev_forces<<<blocks_for(A.np, PART_THREADS), PART_THREADS, 0, s>>>(A);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_rev_nodal_kinematics(const AdjStep& A, const int4* tiles, int ntiles,
-                                        cudaStream_t s) {
-    if (ntiles > 0) k_rev_nodal_kinematics<<<ntiles, TILE_THREADS, 0, s>>>(A, tiles);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_rev_mass_momentum(const AdjStep& A, cudaStream_t s) {
-    if (A.np <= 0) return cudaSuccess;
-    k_rev_mass_momentum<<<blocks_for(A.np, PART_THREADS), PART_THREADS, 0, s>>>(A);
+cudaError_t launch_rev_step(const AdjStep& A, bool usl, const int4* tiles, int ntiles,
+                            cudaStream_t s) {
+    const int pb = A.np > 0 ? blocks_for(A.np, PART_THREADS) : 0;
+    if (usl) {
+        if (pb) k_rev_stress_usl<<<pb, PART_THREADS, 0, s>>>(A);
+        if (ntiles > 0) k_rev_nodal_kinematics<RK_GATHER><<<ntiles, TILE_THREADS, 0, s>>>(A, tiles);
+        if (ntiles > 0) k_rev_nodal_update<true><<<ntiles, TILE_THREADS, 0, s>>>(A, tiles);
+        if (pb) k_rev_forces<true><<<pb, PART_THREADS, 0, s>>>(A);
+        if (ntiles > 0) k_rev_nodal_kinematics<RK_NODES><<<ntiles, TILE_THREADS, 0, s>>>(A, tiles);
+    } else {
+        if (ntiles > 0) k_rev_nodal_update<false><<<ntiles, TILE_THREADS, 0, s>>>(A, tiles);
+        if (pb) k_rev_forces<false><<<pb, PART_THREADS, 0, s>>>(A);
+        if (ntiles > 0) k_rev_nodal_kinematics<RK_USF><<<ntiles, TILE_THREADS, 0, s>>>(A, tiles);
+    }
+    if (pb) k_rev_mass_momentum<<<pb, PART_THREADS, 0, s>>>(A);
     return cudaGetLastError();
 }
 
@@ -646,14 +773,21 @@ cudaError_t launch_adj_table(const AdjStep* bases, int n, int t, AdjStep* table,
     return cudaGetLastError();
 }
 
-cudaError_t launch_rev_batch(const AdjStep* table, const int4* tiles, int ntiles,
+cudaError_t launch_rev_batch(const AdjStep* table, bool usl, const int4* tiles, int ntiles,
                              const int2* part_blocks, int n_part_blocks, cudaStream_t s) {
-    if (ntiles > 0) k_rev_nodal_update_batch<<<ntiles, TILE_THREADS, 0, s>>>(table, tiles);
-    if (n_part_blocks > 0)
-        k_rev_forces_batch<<<n_part_blocks, PART_THREADS, 0, s>>>(table, part_blocks);
-    if (ntiles > 0) k_rev_nodal_kinematics_batch<<<ntiles, TILE_THREADS, 0, s>>>(table, tiles);
-    if (n_part_blocks > 0)
-        k_rev_mass_momentum_batch<<<n_part_blocks, PART_THREADS, 0, s>>>(table, part_blocks);
+    const int nt = ntiles, npb = n_part_blocks;
+    if (usl) {
+        if (npb > 0) k_rev_stress_usl_batch<<<npb, PART_THREADS, 0, s>>>(table, part_blocks);
+        if (nt > 0) k_rev_nodal_kinematics_batch<RK_GATHER><<<nt, TILE_THREADS, 0, s>>>(table, tiles);
+        if (nt > 0) k_rev_nodal_update_batch<true><<<nt, TILE_THREADS, 0, s>>>(table, tiles);
+        if (npb > 0) k_rev_forces_batch<true><<<npb, PART_THREADS, 0, s>>>(table, part_blocks);
+        if (nt > 0) k_rev_nodal_kinematics_batch<RK_NODES><<<nt, TILE_THREADS, 0, s>>>(table, tiles);
+    } else {
+        if (nt > 0) k_rev_nodal_update_batch<false><<<nt, TILE_THREADS, 0, s>>>(table, tiles);
+        if (npb > 0) k_rev_forces_batch<false><<<npb, PART_THREADS, 0, s>>>(table, part_blocks);
+        if (nt > 0) k_rev_nodal_kinematics_batch<RK_USF><<<nt, TILE_THREADS, 0, s>>>(table, tiles);
+    }
+    if (npb > 0) k_rev_mass_momentum_batch<<<npb, PART_THREADS, 0, s>>>(table, part_blocks);
     return cudaGetLastError();
 }
 

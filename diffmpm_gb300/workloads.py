@@ -111,10 +111,12 @@ def youngs_field(npart, seed, median=1e6, sigma_log=0.5):
     return median * np.exp(sigma_log * rng.normal(size=npart))
 
 
-def differentiation(api, n=256, sim_steps=2000, dt=5e-6, seed=101, velocity=None, E=None, **kw):
+def differentiation(api, n=256, sim_steps=2000, dt=5e-6, seed=101, velocity=None, E=None,
+                    scheme="usf", **kw):
     """``E`` overrides the seeded field; ``velocity`` sets the initial particle
     velocity (used by small test variants to make particles change cell): a
-    2-vector for all particles, or a function of the (n, 2) positions."""
+    2-vector for all particles, or a function of the (n, 2) positions;
+    ``scheme`` (USF in the configuration) lets tests differentiate USL."""
     h = 1.0 / n
     i0 = int(np.ceil(0.1 * n - 0.5))
     i1 = int(np.floor(0.9 * n - 0.5)) + 1
@@ -131,7 +133,7 @@ def differentiation(api, n=256, sim_steps=2000, dt=5e-6, seed=101, velocity=None
         v = velocity(pts) if callable(velocity) else velocity
         ps.velocity[:] = np.broadcast_to(np.asarray(v, dtype=np.float64), pts.shape).reshape(-1, 1, 2)
     mesh = api.Mesh2D({"particles": [ps], "elements": el, "particle_surface_traction": []})
-    solver = api.MPMExplicit(mesh, dt, scheme="usf", velocity_update=False, sim_steps=sim_steps)
+    solver = api.MPMExplicit(mesh, dt, scheme=scheme, velocity_update=False, sim_steps=sim_steps)
     return solver, np.array([0.0, -9.81]), {"workload": "differentiation", "n": n, "np": len(pts),
                                              "seed": seed, "E": E}
 

@@ -7,8 +7,13 @@ check that this restatement equals torch autograd of ``oracle.mpm_torch``, so
 the derivation the CUDA kernels implement is pinned without a GPU; the GPU
 tests then compare the kernels with autograd directly.
 
-Scope as the CUDA adjoint: USF, per-step volume set-up, LinearElastic with a
-per-particle E, gravity, velocity constraints.
+Scope as the CUDA adjoint: USF or USL, per-step volume set-up, LinearElastic
+with a per-particle E, gravity, velocity constraints.  USL reverses in six
+passes (the order of the CUDA launches): U, the stress update after G2P
+(strain-rate adjoints from the updated nodal velocities vB); G, their
+transposed gather to the nodes; then passes 1-4 as for USF, with the forces
+of pass 2 on the start-of-step stress and volume and no strain-rate gather in
+pass 3.
 """
 from __future__ import annotations
 
@@ -36,7 +41,8 @@ class Restated:
         self.vol_el = float(tsim.vol_el)
         self.nn = tsim.nn
         self.vu = bool(tsim.velocity_update)
-        assert tsim.scheme == "usf" and len(tsim.materials) == 1
+        assert tsim.scheme in ("usf", "usl") and len(tsim.materials) == 1
+        self.usl = tsim.scheme == "usl"
         self.c1, self.c2, self.c3 = le_coefficients(float(tsim.materials[0].properties["poisson_ratio"]))
 
     def geometry(self, x):
@@ -58,6 +64,45 @@ class Restated:
         e = j * self.nx + i
         return dict(e=e, ids=ids, N=N, Gx=Gx, Gy=Gy, Gcx=Gcx, Gcy=Gcy, rx=rx, ry=ry)
 
+    def rates(self, G, nv):
+        """Strain rates (xx, yy, xy) and centroid rates of nodal velocities nv."""
+        ids = G["ids"]
+        vx, vy = nv[ids, 0], nv[ids, 1]
+        r0 = flush((G["Gx"] * vx).sum(1))
+        r1 = flush((G["Gy"] * vy).sum(1))
+        r3 = flush((G["Gx"] * vy).sum(1) + (G["Gy"] * vx).sum(1))
+        c0 = flush((G["Gcx"] * vx).sum(1))
+        c1 = flush((G["Gcy"] * vy).sum(1))
+        return r0, r1, r3, c0, c1
+
+    def stress(self, s, E, r0, r1, r3):
+        dt = self.dt
+        d0, d1, d3 = r0 * dt, r1 * dt, r3 * dt
+        a1, a2, Gm = E * self.c1, E * self.c2, E * self.c3
+        return s + np.stack([a1 * d0 + a2 * d1, a2 * d0 + a1 * d1, a2 * d0 + a2 * d1, Gm * d3], 1)
+
+    def stress_reverse(self, sb, E, r0, r1, r3):
+        """D^T sb dt (masked where a rate was flushed) and dL/dE."""
+        dt = self.dt
+        d0, d1, d3 = r0 * dt, r1 * dt, r3 * dt
+        a1, a2, Gm = E * self.c1, E * self.c2, E * self.c3
+        d0b = a1 * sb[:, 0] + a2 * sb[:, 1] + a2 * sb[:, 2]
+        d1b = a2 * sb[:, 0] + a1 * sb[:, 1] + a2 * sb[:, 2]
+        d3b = Gm * sb[:, 3]
+        Eb = (self.c1 * (d0 * sb[:, 0] + d1 * sb[:, 1])
+              + self.c2 * (d1 * sb[:, 0] + d0 * sb[:, 1] + (d0 + d1) * sb[:, 2])
+              + self.c3 * d3 * sb[:, 3])
+        r0b = np.where(r0 != 0, d0b * dt, 0.0)
+        r1b = np.where(r1 != 0, d1b * dt, 0.0)
+        r3b = np.where(r3 != 0, d3b * dt, 0.0)
+        return r0b, r1b, r3b, Eb
+
+    def rate_gather(self, G, r0b, r1b, r3b, c0b, c1b):
+        """Transposed strain-rate gather: nodal-velocity adjoint."""
+        Gx, Gy, Gcx, Gcy = G["Gx"], G["Gy"], G["Gcx"], G["Gcy"]
+        return self.scatter(G["ids"], np.stack([Gx * r0b[:, None] + Gy * r3b[:, None] + Gcx * c0b[:, None],
+                                                Gy * r1b[:, None] + Gx * r3b[:, None] + Gcy * c1b[:, None]], 2))
+
     def scatter(self, ids, vals):
         out = np.zeros((self.nn,) + vals.shape[2:])
         np.add.at(out, ids.reshape(-1), vals.reshape((-1,) + vals.shape[2:]))
@@ -78,19 +123,14 @@ class Restated:
         safe = np.where(M == 0, 1.0, M)
         vA = np.where((M == 0)[:, None], nvo, P / safe[:, None])
         vA = np.where(self.cmask, self.cval, flush(vA))
-        vx, vy = vA[ids, 0], vA[ids, 1]
-        r0 = flush((Gx * vx).sum(1))
-        r1 = flush((Gy * vy).sum(1))
-        r3 = flush((Gx * vy).sum(1) + (Gy * vx).sum(1))
-        c0 = flush((G["Gcx"] * vx).sum(1))
-        c1 = flush((G["Gcy"] * vy).sum(1))
-        dvol = self.dt * (c0 + c1)
-        d0, d1, d3 = r0 * self.dt, r1 * self.dt, r3 * self.dt
-        a1, a2, Gm = E * self.c1, E * self.c2, E * self.c3
-        s2 = s + np.stack([a1 * d0 + a2 * d1, a2 * d0 + a1 * d1, a2 * d0 + a2 * d1, Gm * d3], 1)
-        f = 1 + dvol
-        V = V0 * f
-        rho2 = rho / f
+        if self.usl:   # forces on the start-of-step stress and volume
+            s2, V, rho2 = s, V0, rho
+        else:
+            r0, r1, r3, c0, c1 = self.rates(G, vA)
+            f = 1 + self.dt * (c0 + c1)
+            s2 = self.stress(s, E, r0, r1, r3)
+            V = V0 * f
+            rho2 = rho / f
         fx = Gx * s2[:, 0:1] + Gy * s2[:, 3:4]
         fy = Gy * s2[:, 1:2] + Gx * s2[:, 3:4]
         F = self.scatter(ids, np.stack([-V[:, None] * fx, -V[:, None] * fy], 2))
@@ -103,6 +143,11 @@ class Restated:
         ahat = (N[:, :, None] * aB[ids]).sum(1)
         v2 = vhat if self.vu else v + ahat * self.dt
         x2 = x + vhat * self.dt
+        if self.usl:   # stress update from vB at the start-of-step positions
+            r0, r1, r3, c0, c1 = self.rates(G, vB)
+            f = 1 + self.dt * (c0 + c1)
+            s2 = self.stress(s, E, r0, r1, r3)
+            rho2 = rho / f
         tape = dict(x=x, v=v, sig=s, rho=rho, M=M, vA=vA, vB=vB, aB=aB)
         return dict(x=x2, v=v2, sig=s2, rho=rho2, nv=vB), tape
 
@@ -114,35 +159,43 @@ class Restated:
         x, v, s, rho = tape["x"], tape["v"], tape["sig"], tape["rho"]
         M, vA, vB, aB = tape["M"], tape["vA"], tape["vB"], tape["aB"]
         G = self.geometry(x)
-        ids, N, Gx, Gy, Gcx, Gcy = G["ids"], G["N"], G["Gx"], G["Gy"], G["Gcx"], G["Gcy"]
+        ids, N, Gx, Gy = G["ids"], G["N"], G["Gx"], G["Gy"]
         live = (M != 0)[:, None]
         safe = np.where(M == 0, 1.0, M)
+        cnt = np.bincount(G["e"], minlength=self.nx * self.ny).astype(float)
+        V0 = self.vol_el / cnt[G["e"]]
+        m = V0 * rho
+        sb = lam["sig"].copy()
+        vBb = np.zeros((self.nn, 2))
+        if self.usl:
+            # pass U: the stress update after G2P; the stress adjoint passes
+            # through to the start of the step
+            r0, r1, r3, c0, c1 = self.rates(G, vB)
+            f = 1 + dt * (c0 + c1)
+            r0b, r1b, r3b, Eb = self.stress_reverse(sb, E, r0, r1, r3)
+            fb = -lam["rho"] * (rho / f) / f
+            rhob = lam["rho"] / f
+            c0b = np.where(c0 != 0, fb * dt, 0.0)
+            c1b = np.where(c1 != 0, fb * dt, 0.0)
+            # pass G: its transposed strain-rate gather (vB adjoint)
+            vBb = self.rate_gather(G, r0b, r1b, r3b, c0b, c1b)
+            s2, V, nvr = s, V0, vB
         # pass 1: transposed G2P, reverse nodal update
         gh = lam["x"] * dt + (lam["v"] if self.vu else 0.0)
         hh = np.zeros_like(gh) if self.vu else lam["v"] * dt
-        vBb = self.scatter(ids, N[:, :, None] * gh[:, None, :])
+        vBb = vBb + self.scatter(ids, N[:, :, None] * gh[:, None, :])
         aBb = self.scatter(ids, N[:, :, None] * hh[:, None, :])
         wb = np.where(self.cmask | (vB == 0), 0.0, vBb) * live
         ab = (np.where(self.cmask | (aB == 0), 0.0, aBb) + wb * dt) * live
         Fb = ab / safe[:, None]
         Mb = -(ab * aB).sum(1) / safe
-        # pass 2: forces and stress update
-        cnt = np.bincount(G["e"], minlength=self.nx * self.ny).astype(float)
-        V0 = self.vol_el / cnt[G["e"]]
-        m = V0 * rho
-        vx, vy = vA[ids, 0], vA[ids, 1]
-        r0 = flush((Gx * vx).sum(1))
-        r1 = flush((Gy * vy).sum(1))
-        r3 = flush((Gx * vy).sum(1) + (Gy * vx).sum(1))
-        c0 = flush((Gcx * vx).sum(1))
-        c1 = flush((Gcy * vy).sum(1))
-        dvol = dt * (c0 + c1)
-        d0, d1, d3 = r0 * dt, r1 * dt, r3 * dt
-        a1, a2, Gm = E * self.c1, E * self.c2, E * self.c3
-        s2 = s + np.stack([a1 * d0 + a2 * d1, a2 * d0 + a1 * d1, a2 * d0 + a2 * d1, Gm * d3], 1)
-        f = 1 + dvol
-        V = V0 * f
-        rho2 = rho / f
+        # pass 2: forces (and the USF stress update)
+        if not self.usl:
+            r0, r1, r3, c0, c1 = self.rates(G, vA)
+            f = 1 + dt * (c0 + c1)
+            s2 = self.stress(s, E, r0, r1, r3)
+            V = V0 * f
+            nvr = vA
         fbx, fby = Fb[ids, 0], Fb[ids, 1]
         fg = fbx * self.g[0] + fby * self.g[1]
         Nb = (gh[:, None, 0] * vB[ids, 0] + gh[:, None, 1] * vB[ids, 1]
@@ -151,25 +204,20 @@ class Restated:
         fx = Gx * s2[:, 0:1] + Gy * s2[:, 3:4]
         fy = Gy * s2[:, 1:2] + Gx * s2[:, 3:4]
         Vb = -(fbx * fx + fby * fy).sum(1)
-        sb = lam["sig"].copy()
         sb[:, 0] -= V * (fbx * Gx).sum(1)
         sb[:, 1] -= V * (fby * Gy).sum(1)
         sb[:, 3] -= V * (fbx * Gy + fby * Gx).sum(1)
         Gxb = -V[:, None] * (fbx * s2[:, 0:1] + fby * s2[:, 3:4])
         Gyb = -V[:, None] * (fbx * s2[:, 3:4] + fby * s2[:, 1:2])
-        d0b = a1 * sb[:, 0] + a2 * sb[:, 1] + a2 * sb[:, 2]
-        d1b = a2 * sb[:, 0] + a1 * sb[:, 1] + a2 * sb[:, 2]
-        d3b = Gm * sb[:, 3]
-        Eb = (self.c1 * (d0 * sb[:, 0] + d1 * sb[:, 1])
-              + self.c2 * (d1 * sb[:, 0] + d0 * sb[:, 1] + (d0 + d1) * sb[:, 2])
-              + self.c3 * d3 * sb[:, 3])
-        r0b = np.where(r0 != 0, d0b * dt, 0.0)
-        r1b = np.where(r1 != 0, d1b * dt, 0.0)
-        r3b = np.where(r3 != 0, d3b * dt, 0.0)
-        fb = Vb * V0 - lam["rho"] * rho2 / f
-        rhob = lam["rho"] / f + V0 * mb
-        c0b = np.where(c0 != 0, fb * dt, 0.0)
-        c1b = np.where(c1 != 0, fb * dt, 0.0)
+        if self.usl:
+            rhob = rhob + V0 * mb
+        else:
+            r0b, r1b, r3b, Eb = self.stress_reverse(sb, E, r0, r1, r3)
+            fb = Vb * V0 - lam["rho"] * (rho / f) / f
+            rhob = lam["rho"] / f + V0 * mb
+            c0b = np.where(c0 != 0, fb * dt, 0.0)
+            c1b = np.where(c1 != 0, fb * dt, 0.0)
+        vx, vy = nvr[ids, 0], nvr[ids, 1]
         Gxb = Gxb + r0b[:, None] * vx + r3b[:, None] * vy
         Gyb = Gyb + r1b[:, None] * vy + r3b[:, None] * vx
         sgn = np.array([1.0, -1.0, 1.0, -1.0])
@@ -177,9 +225,8 @@ class Restated:
         xb = lam["x"].copy()
         xb[:, 0] += (Nb * Gx).sum(1) + rxy * (Gyb * sgn).sum(1)
         xb[:, 1] += (Nb * Gy).sum(1) + rxy * (Gxb * sgn).sum(1)
-        # pass 3: transposed strain-rate gather, reverse nodal velocity
-        vAb = wb + self.scatter(ids, np.stack([Gx * r0b[:, None] + Gy * r3b[:, None] + Gcx * c0b[:, None],
-                                               Gy * r1b[:, None] + Gx * r3b[:, None] + Gcy * c1b[:, None]], 2))
+        # pass 3: (USF) transposed strain-rate gather, reverse nodal velocity
+        vAb = wb if self.usl else wb + self.rate_gather(G, r0b, r1b, r3b, c0b, c1b)
         ub = np.where(self.cmask | (vA == 0), 0.0, vAb) * live
         Qb = ub / safe[:, None]
         Mbt = Mb - (ub * vA).sum(1) / safe

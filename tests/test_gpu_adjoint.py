@@ -47,8 +47,17 @@ def sheared(p):
 CASE = dict(n=16, sim_steps=24, dt=1e-3, velocity=sheared)
 
 
-def gpu_sim(vu=False, block=None, **kw):
+def case_args(kw):
+    """CASE with overrides; USL steps at dt 2.5e-4 (at 1e-3 a free-surface
+    node's mass falls towards zero within the steps and USL blows up)."""
     args = dict(CASE, **kw)
+    if args.get("scheme") == "usl" and "dt" not in kw:
+        args["dt"] = 2.5e-4
+    return args
+
+
+def gpu_sim(vu=False, block=None, **kw):
+    args = case_args(kw)
     gs, g, info = workloads.differentiation(D, **args)
     gs.velocity_update = vu
     sim = gs.simulation(g, reinit=True)
@@ -67,7 +76,7 @@ def seeds(n, seed=5):
 def autograd_ref(vu, W, U, dtype=torch.float32, **kw):
     """Gradients of L = <W, x_end> + <U, v_end> by autograd of the oracle in
     ``dtype`` (float32: the same discrete program as the GPU)."""
-    args = dict(CASE, **kw)
+    args = case_args(kw)
     npd = np.float32 if dtype == torch.float32 else np.float64
     o, g, info = workloads.differentiation(O, dtype=npd, **args)
     o.velocity_update = vu
@@ -83,15 +92,16 @@ def autograd_ref(vu, W, U, dtype=torch.float32, **kw):
             "x_end": end["x"].detach().numpy()}
 
 
+@pytest.mark.parametrize("scheme", ["usf", "usl"])
 @pytest.mark.parametrize("vu", [False, True])
-def test_adjoint_matches_autograd(built, vu):
-    gs, sim, g, info = gpu_sim(vu)
+def test_adjoint_matches_autograd(built, vu, scheme):
+    gs, sim, g, info = gpu_sim(vu, scheme=scheme)
     W, U = seeds(info["np"])
     sim.record(CASE["sim_steps"], 10)
     x_end = sim.read("loc")
     got = sim.adjoint(W, U)
-    ref = autograd_ref(vu, W, U)
-    ref64 = autograd_ref(vu, W, U, dtype=torch.float64)
+    ref = autograd_ref(vu, W, U, scheme=scheme)
+    ref64 = autograd_ref(vu, W, U, dtype=torch.float64, scheme=scheme)
     fwd = rel(x_end, ref64["x_end"])
     assert fwd < 1e-5
     for k in ("youngs_modulus", "loc", "velocity"):
@@ -120,16 +130,18 @@ def test_adjoint_checkpoint_interval_and_repeat(built):
             assert rel(o[k], outs[0][k]) < 1e-5, k
 
 
-def test_adjoint_across_resorts(built):
+@pytest.mark.parametrize("scheme", ["usf", "usl"])
+def test_adjoint_across_resorts(built, scheme):
     """Short step blocks re-sort the particles between blocks; the recorded
     re-sorts are replayed and the adjoint arrays permuted across them."""
-    gs, sim, g, info = gpu_sim(block=3)
+    steps = CASE["sim_steps"] if scheme == "usf" else 96   # USL: 4x the steps at dt / 4
+    gs, sim, g, info = gpu_sim(block=3, scheme=scheme, sim_steps=steps)
     W, U = seeds(info["np"])
     before = sim.counters()["resorts"]
-    sim.record(CASE["sim_steps"], 10)
+    sim.record(steps, 10)
     assert sim.counters()["resorts"] > before + 1
     a = sim.adjoint(W, U)
-    ref = autograd_ref(False, W, U)
+    ref = autograd_ref(False, W, U, scheme=scheme, sim_steps=steps)
     for k in a:
         assert rel(a[k], ref[k]) < GRAD_TOL, k
 
@@ -151,11 +163,12 @@ def test_autograd_function(built):
     assert np.array_equal(v0.grad.cpu().numpy(), direct["velocity"])
 
 
-def test_adjoint_directional_derivative_vs_finite_differences(built):
+@pytest.mark.parametrize("scheme", ["usf", "usl"])
+def test_adjoint_directional_derivative_vs_finite_differences(built, scheme):
     """<dL/dE, u> from the GPU against a central difference of the float64
     oracle, L = mean |x_end - x_target|^2 (the differentiation workload's loss)
     on a 32 x 32 mesh for 40 steps."""
-    kw = dict(n=32, sim_steps=40, dt=2e-4, velocity=(0.5, 0.0))
+    kw = dict(n=32, sim_steps=40, dt=2e-4, velocity=(0.5, 0.0), scheme=scheme)
     gs, sim, g, info = gpu_sim(**kw)
     n = info["np"]
     rng = np.random.Generator(np.random.PCG64(21))
@@ -181,8 +194,8 @@ def test_adjoint_directional_derivative_vs_finite_differences(built):
 
 
 def test_adjoint_rejects_unsupported(built):
-    gs, g, info = workloads.plain_scaleup(D, n=16, scheme="usl", sim_steps=2)
-    sim = gs.simulation(g, reinit=True)
+    gs, g, info = workloads.plain_scaleup(D, n=16, sim_steps=2)
+    sim = gs.simulation(g, reinit=False)     # solve semantics: not differentiated
     gs._upload(sim)
     sim.initialize()
     with pytest.raises(D.MpmError) as e:
