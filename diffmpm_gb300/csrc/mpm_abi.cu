@@ -64,6 +64,7 @@ float element_volume(float hx, float hy) {
 void drop_graphs(MpmHandle* h) {
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
     h->graphs.clear();
+    h->graph_gen++;
 }
 
 int upload_desc(MpmHandle* h) {

@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <map>
 #include <vector>
 
 #include "mpm_adjoint.h"
@@ -78,6 +79,14 @@ struct AdjointState {
     int* cnt = nullptr;
     int* mismatch = nullptr;   // device counter of the re-run check
     int* h_mismatch = nullptr; // pinned
+    // CUDA graphs of whole segments without a re-sort: the re-run with its
+    // tape copies (keyed by 2 * length + start parity) and the reverse steps
+    // (keyed by length).  They hold the step descriptor and every buffer
+    // pointer by value, so they are dropped when the handle's step graphs are
+    // (g_gen != graph_gen) and whenever a buffer here is (re)allocated.
+    std::map<int, cudaGraphExec_t> g_rerun, g_rev;
+    SegBuf g_tp[2], g_tn;      // tape copy tables of the re-run graphs
+    uint64_t g_gen = ~0ull;
 };
 
 // Scratch of a batched adjoint (owned by the batch).
@@ -94,7 +103,18 @@ struct BatchAdjoint {
 
 namespace {
 
+void drop_adj_graphs(AdjointState* a) {
+    for (auto& kv : a->g_rerun) cudaGraphExecDestroy(kv.second);
+    for (auto& kv : a->g_rev) cudaGraphExecDestroy(kv.second);
+    a->g_rerun.clear();
+    a->g_rev.clear();
+    for (SegBuf& b : a->g_tp) segbuf_free(b);
+    segbuf_free(a->g_tn);
+    a->g_gen = ~0ull;
+}
+
 void free_buffers(MpmHandle* h, AdjointState* a) {
+    drop_adj_graphs(a);
     for (auto& c : a->ck) checkpoint_free(h, c);
     a->ck.clear();
     for (float*& p : a->tp) { dfree(h, p); p = nullptr; }
@@ -152,6 +172,7 @@ int restore_checkpoint(MpmHandle* h, Checkpoint& c, cudaStream_t s) {
 int ensure_adjoint_buffers(MpmHandle* h, AdjointState* a, int slots, cudaStream_t s) {
     const size_t np = (size_t)h->np, nn = (size_t)h->nn;
     if (a->tape_slots < slots) {
+        drop_adj_graphs(a);
         for (float*& p : a->tp) { dfree(h, p); p = nullptr; }
         for (float*& p : a->tn) { dfree(h, p); p = nullptr; }
         dfree(h, a->tflag);
@@ -163,6 +184,7 @@ int ensure_adjoint_buffers(MpmHandle* h, AdjointState* a, int slots, cudaStream_
         a->tape_slots = slots;
     }
     if (!a->lam[0]) {
+        drop_adj_graphs(a);
         for (float*& p : a->lam) TRY(dalloc(h, &p, np));
         for (float*& p : a->pscr) TRY(dalloc(h, &p, np));
         for (float*& p : a->nscr) TRY(dalloc(h, &p, nn));
@@ -190,6 +212,7 @@ void add_seg(std::vector<CopySeg>& v, const void* src, void* dst, size_t bytes, 
 int epoch_segments(MpmHandle* h, AdjointState* a, size_t e, std::vector<CopySeg>& v) {
     const size_t np = (size_t)h->np;
     if (a->epochs.size() <= e) {
+        drop_adj_graphs(a);
         Epoch ep;
         TRY(dalloc(h, &ep.pid, np));
         TRY(dalloc(h, &ep.mat, np));
@@ -197,7 +220,10 @@ int epoch_segments(MpmHandle* h, AdjointState* a, size_t e, std::vector<CopySeg>
         a->epochs.push_back(ep);
     }
     Epoch& ep = a->epochs[e];
-    if (h->has_E && !ep.E) TRY(dalloc(h, &ep.E, np));
+    if (h->has_E && !ep.E) {
+        drop_adj_graphs(a);
+        TRY(dalloc(h, &ep.E, np));
+    }
     const PSet& p = h->ps[h->pcur];
     add_seg(v, p.pid, ep.pid, sizeof(int) * np, 0);
     add_seg(v, p.mat, ep.mat, np, 0);
@@ -242,6 +268,68 @@ bool resorts_at(const AdjointState* a, int64_t step) {
     return std::binary_search(a->resort_steps.begin(), a->resort_steps.end(), step);
 }
 
+// Tape copy tables of the segment graphs, for the handle's current
+// descriptors (the previous graphs are dropped when those changed).
+int prepare_adj_graphs(MpmHandle* h, AdjointState* a, cudaStream_t s) {
+    if (a->g_gen == h->graph_gen) return MPM_OK;
+    drop_adj_graphs(a);
+    for (int par = 0; par < 2; ++par) {
+        std::vector<CopySeg> v;
+        tape_particle_segments(h, a, par, v);
+        TRY(upload_segments(h, a->g_tp[par], v, s));
+    }
+    std::vector<CopySeg> vn;
+    tape_node_segments(h, a, vn);
+    TRY(upload_segments(h, a->g_tn, vn, s));
+    a->g_gen = h->graph_gen;
+    return MPM_OK;
+}
+
+// Capture the launches that `body` issues on the handle's capture stream
+// into an executable graph stored at map[key] (if absent), then launch it.
+template <class F>
+int run_cached_graph(MpmHandle* h, std::map<int, cudaGraphExec_t>& map, int key, cudaStream_t s,
+                     F&& body) {
+    auto it = map.find(key);
+    if (it == map.end()) {
+        cudaGraph_t g = nullptr;
+        CK(h, cudaStreamBeginCapture(h->cap, cudaStreamCaptureModeThreadLocal));
+        const int r = body(h->cap);
+        const cudaError_t e = cudaStreamEndCapture(h->cap, &g);
+        if (r != MPM_OK || e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            if (r != MPM_OK) return r;
+            CK(h, e);
+        }
+        cudaGraphExec_t ex = nullptr;
+        const cudaError_t ei = cudaGraphInstantiate(&ex, g, 0);
+        cudaGraphDestroy(g);
+        CK(h, ei);
+        it = map.emplace(key, ex).first;
+    }
+    CK(h, cudaGraphLaunch(it->second, s));
+    return MPM_OK;
+}
+
+// Re-run of a segment of `len` steps without a re-sort as one graph: per
+// step the tape copy of the start state, the step's kernels and the tape copy
+// of the nodal results.
+int rerun_graph(MpmHandle* h, AdjointState* a, int len, cudaStream_t s) {
+    TRY(prepare_adj_graphs(h, a, s));
+    const int par0 = parity(h);
+    TRY(run_cached_graph(h, a->g_rerun, 2 * len + par0, s, [&](cudaStream_t c) -> int {
+        for (int t = 0; t < len; ++t) {
+            const SegBuf& tp = a->g_tp[(par0 + t) & 1];
+            CK(h, launch_copy_segments(tp.segs, tp.first, tp.nseg, tp.nblocks, t, c));
+            TRY(launch_steps(h, 1, c));
+            CK(h, launch_copy_segments(a->g_tn.segs, a->g_tn.first, a->g_tn.nseg, a->g_tn.nblocks, t, c));
+        }
+        return MPM_OK;
+    }));
+    h->step += len;
+    return MPM_OK;
+}
+
 // Re-run segment `seg` of one simulation from its checkpoint, filling tape
 // slots 0..len-1, and check that it ends in the next checkpoint's state.
 int recompute_segment(MpmHandle* h, AdjointState* a, int seg, int len, cudaStream_t s) {
@@ -250,14 +338,16 @@ int recompute_segment(MpmHandle* h, AdjointState* a, int seg, int len, cudaStrea
     a->epoch_of.assign(len, 0);
     a->nep = 0;
     TRY(capture_epoch(h, a, s));
+    bool resorts = false;
+    for (int t = 0; t < len; ++t) resorts = resorts || resorts_at(a, first + t);
     SegBuf& tp = h->segbuf;
     int tp_par = -1;
     SegBuf tn;
     std::vector<CopySeg> vn;
     tape_node_segments(h, a, vn);
-    TRY(upload_segments(h, tn, vn, s));
-    int r = MPM_OK;
-    for (int t = 0; t < len && r == MPM_OK; ++t) {
+    if (resorts) TRY(upload_segments(h, tn, vn, s));
+    int r = resorts ? MPM_OK : rerun_graph(h, a, len, s);
+    for (int t = 0; t < len && r == MPM_OK && resorts; ++t) {
         if (resorts_at(a, first + t)) {
             r = resort(h, s);
             if (r == MPM_OK) r = capture_epoch(h, a, s);
@@ -365,6 +455,15 @@ int reverse_step(MpmHandle* h, AdjointState* a, int t, cudaStream_t s) {
     A.nm += on; A.nvax += on; A.nvay += on; A.nvbx += on; A.nvby += on; A.nax += on; A.nay += on;
     CK(h, launch_rev_step(A, h->usl, h->dtiles, h->ntiles, s));
     return MPM_OK;
+}
+
+// The reverse steps of a segment of `len` steps in one sort epoch as one graph.
+int reverse_graph(MpmHandle* h, AdjointState* a, int len, cudaStream_t s) {
+    TRY(prepare_adj_graphs(h, a, s));
+    return run_cached_graph(h, a->g_rev, len, s, [&](cudaStream_t c) -> int {
+        for (int t = len - 1; t >= 0; --t) TRY(reverse_step(h, a, t, c));
+        return MPM_OK;
+    });
 }
 
 // Zero the adjoint arrays; particle (n, 2) seeds in original order -> lam[0..3]
@@ -649,6 +748,10 @@ int mpm_adjoint(MpmHandle* h, const float* dl_dloc, const float* dl_dvel, float*
     for (int seg = a->nseg - 1; seg >= 0 && r == MPM_OK; --seg) {
         const int len = (int)std::min<int64_t>(K, a->nsteps - (int64_t)seg * K);
         r = recompute_segment(h, a, seg, len, s);
+        if (r == MPM_OK && a->nep == 1) {   // one sort epoch: the segment's reverse steps as a graph
+            r = reverse_graph(h, a, len, s);
+            continue;
+        }
         for (int t = len - 1; t >= 0 && r == MPM_OK; --t) {
             if (t < len - 1 && a->epoch_of[t] != a->epoch_of[t + 1])
                 r = permute(h, a, a->epochs[a->epoch_of[t + 1]].pid, a->epochs[a->epoch_of[t]].pid, s);

@@ -123,6 +123,7 @@ struct MpmHandle {
     cudaStream_t cap = nullptr;
     std::map<int, cudaGraphExec_t> graphs;
     bool graphs_trac = false;
+    uint64_t graph_gen = 0;            // bumped whenever the step graphs are dropped
     bool has_pvc = false;              // particle velocity constraints set
     float* d_pvc_vel = nullptr;
     bool initialized = false, needs_resort = false;
