@@ -51,6 +51,8 @@ struct Epoch {               // arrays of one sort epoch inside a segment
     uint8_t* mat = nullptr;
     float* E = nullptr;
     int* cstart = nullptr;
+    int8_t* tr_fn = nullptr;   // particle tractions (2 per particle), when present
+    float* tr_tau = nullptr;
 };
 
 }  // namespace
@@ -71,6 +73,7 @@ struct AdjointState {
     std::vector<Epoch> epochs;
     std::vector<int> epoch_of;
     int nep = 0;               // epochs captured in the current segment
+    int64_t seg_first = 0;     // first step of the segment being reversed
     float* lam[NLAM] = {};
     float* lam_tmp = nullptr;
     float** d_lam = nullptr;
@@ -127,6 +130,8 @@ void free_buffers(MpmHandle* h, AdjointState* a) {
         dfree(h, e.mat);
         dfree(h, e.E);
         dfree(h, e.cstart);
+        dfree(h, e.tr_fn);
+        dfree(h, e.tr_tau);
     }
     a->epochs.clear();
     for (float*& p : a->lam) { dfree(h, p); p = nullptr; }
@@ -224,10 +229,19 @@ int epoch_segments(MpmHandle* h, AdjointState* a, size_t e, std::vector<CopySeg>
         drop_adj_graphs(a);
         TRY(dalloc(h, &ep.E, np));
     }
+    if (h->has_trac && !ep.tr_fn) {
+        drop_adj_graphs(a);
+        TRY(dalloc(h, &ep.tr_fn, 2 * np));
+        TRY(dalloc(h, &ep.tr_tau, 2 * np));
+    }
     const PSet& p = h->ps[h->pcur];
     add_seg(v, p.pid, ep.pid, sizeof(int) * np, 0);
     add_seg(v, p.mat, ep.mat, np, 0);
     if (h->has_E) add_seg(v, p.E, ep.E, sizeof(float) * np, 0);
+    if (h->has_trac) {
+        add_seg(v, p.tr_fn, ep.tr_fn, 2 * np, 0);
+        add_seg(v, p.tr_tau, ep.tr_tau, sizeof(float) * 2 * np, 0);
+    }
     add_seg(v, h->cstart[h->cs_cur], ep.cstart, sizeof(int) * ((size_t)h->ncell + 2), 0);
     return MPM_OK;
 }
@@ -335,6 +349,7 @@ int rerun_graph(MpmHandle* h, AdjointState* a, int len, cudaStream_t s) {
 int recompute_segment(MpmHandle* h, AdjointState* a, int seg, int len, cudaStream_t s) {
     TRY(restore_checkpoint(h, a->ck[seg], s));
     const int64_t first = a->ck[seg].step;
+    a->seg_first = first;
     a->epoch_of.assign(len, 0);
     a->nep = 0;
     TRY(capture_epoch(h, a, s));
@@ -427,6 +442,12 @@ AdjStep base_args(MpmHandle* h, AdjointState* a, int epoch) {
     A.cstart = ep.cstart;
     A.mat = ep.mat;
     A.E = h->has_E ? ep.E : nullptr;
+    A.tr_fn = h->has_trac ? ep.tr_fn : nullptr;
+    A.tr_tau = h->has_trac ? ep.tr_tau : nullptr;
+    A.fn_off = h->d_fn_off;
+    A.fn_x = h->d_fn_x;
+    A.fn_y = h->d_fn_y;
+    A.step = (int)a->seg_first;
     const float** tp[NTP] = {&A.x, &A.y, &A.vx, &A.vy, &A.sxx, &A.syy, &A.szz, &A.sxy, &A.rho};
     for (int k = 0; k < NTP; ++k) *tp[k] = a->tp[k];
     A.cflag = a->tflag;
@@ -453,7 +474,8 @@ int reverse_step(MpmHandle* h, AdjointState* a, int t, cudaStream_t s) {
     A.sxx += op; A.syy += op; A.szz += op; A.sxy += op; A.rho += op;
     A.cflag += oc;
     A.nm += on; A.nvax += on; A.nvay += on; A.nvbx += on; A.nvby += on; A.nax += on; A.nay += on;
-    CK(h, launch_rev_step(A, h->usl, h->dtiles, h->ntiles, s));
+    A.step += t;
+    CK(h, launch_rev_step(A, h->usl, h->has_trac, h->dtiles, h->ntiles, s));
     return MPM_OK;
 }
 
@@ -511,7 +533,6 @@ int check_supported(MpmHandle* h) {
     if (!h->reinit)
         return fail(h, MPM_ERR_UNSUPPORTED,
                     "the adjoint implements the per-step volume set-up of solve_jit");
-    if (h->has_trac) return fail(h, MPM_ERR_UNSUPPORTED, "the adjoint does not cover particle tractions");
     if (h->has_pvc)
         return fail(h, MPM_ERR_UNSUPPORTED, "the adjoint does not cover particle velocity constraints");
     for (const MatDev& m : h->mats)
@@ -623,7 +644,10 @@ int batch_recompute(MpmBatch* b, BatchAdjoint* x, int seg, int len, cudaStream_t
     };
     // (the parity of slot t is that of the segment's first step plus t)
     std::vector<int64_t> first(n);
-    for (int i = 0; i < n; ++i) first[i] = b->sims[i]->step;
+    for (int i = 0; i < n; ++i) {
+        first[i] = b->sims[i]->step;
+        b->sims[i]->adj->seg_first = first[i];
+    }
     r = build_particle_tables();
     if (r != MPM_OK) return r;
     v.clear();
@@ -748,7 +772,9 @@ int mpm_adjoint(MpmHandle* h, const float* dl_dloc, const float* dl_dvel, float*
     for (int seg = a->nseg - 1; seg >= 0 && r == MPM_OK; --seg) {
         const int len = (int)std::min<int64_t>(K, a->nsteps - (int64_t)seg * K);
         r = recompute_segment(h, a, seg, len, s);
-        if (r == MPM_OK && a->nep == 1) {   // one sort epoch: the segment's reverse steps as a graph
+        // one sort epoch: the segment's reverse steps as a graph (tractions
+        // need the step number, which the graph would hold by value)
+        if (r == MPM_OK && a->nep == 1 && !h->has_trac) {
             r = reverse_graph(h, a, len, s);
             continue;
         }
@@ -845,7 +871,7 @@ int mpm_batch_adjoint(MpmBatch* b, const float* const* dl_dloc, const float* con
             }
             if (r != MPM_OK) break;
             BCK(b, launch_adj_table(x->d_bases, n, t, x->d_table, s));
-            BCK(b, launch_rev_batch(x->d_table, b->cfg.usl, b->d_tiles, b->ntiles, x->part_blocks,
+            BCK(b, launch_rev_batch(x->d_table, b->cfg.usl, b->cfg.traction, b->d_tiles, b->ntiles, x->part_blocks,
                                     x->n_part_blocks, s));
         }
         for (int i = 0; i < n && r == MPM_OK; ++i) {

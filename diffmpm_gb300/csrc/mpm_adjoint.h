@@ -57,13 +57,21 @@ struct AdjStep {
     float *fbx, *fby, *mb, *vabx, *vaby;
     float *qbx, *qby, *mbt;
     int* cnt;              // particles per cell at the step start (pass 1 -> 2, 4)
+    // particle tractions (tr_fn null when the run has none): function code and
+    // traction per particle and direction in the epoch's storage order, the
+    // function tables, and the step number of the step being reversed
+    const int8_t* tr_fn;
+    const float* tr_tau;
+    const int* fn_off;
+    const float *fn_x, *fn_y;
+    int step;
     // tape slot strides (particles, nodes, cells) for batched launches
     long long sp, sn, sc;
 };
 
 // The passes of one reverse step: node passes over the forward kernels' tile
 // list, particle passes over the particles.
-cudaError_t launch_rev_step(const AdjStep& A, bool usl, const int4* tiles, int ntiles,
+cudaError_t launch_rev_step(const AdjStep& A, bool usl, bool trac, const int4* tiles, int ntiles,
                             cudaStream_t s);
 
 // Batches: table[i] = bases[i] with the tape pointers at slot t; then the
@@ -75,7 +83,7 @@ constexpr int ADJ_BLOCK = 256;
 // block copies the simulation's arguments once and walks ADJ_ITER chunks.
 constexpr int ADJ_ITER = 4;
 cudaError_t launch_adj_table(const AdjStep* bases, int n, int t, AdjStep* table, cudaStream_t s);
-cudaError_t launch_rev_batch(const AdjStep* table, bool usl, const int4* tiles, int ntiles,
+cudaError_t launch_rev_batch(const AdjStep* table, bool usl, bool trac, const int4* tiles, int ntiles,
                              const int2* part_blocks, int n_part_blocks, cudaStream_t s);
 
 // *mismatch += number of i < n with a[i] != b[i] bitwise (4-byte words).

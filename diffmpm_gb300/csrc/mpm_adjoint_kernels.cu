@@ -399,7 +399,7 @@ k_rev_stress_usl_batch(const AdjStep* __restrict__ table, const int2* __restrict
 // reset volume V0; the strain-rate adjoints of its later stress update come
 // from pass U and only add their position terms here.
 // ---------------------------------------------------------------------------
-template <bool USL>
+template <bool USL, bool TRAC>
 __device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q, float x, float y) {
     if (q >= A.np) return;
     int ci, cj;
@@ -438,6 +438,28 @@ __device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q, float x, 
         V = fm(V0, f);
     }
 
+    // particle tractions t_d = f(t) tau_d V / size0 (mesh.py:60-77,
+    // particle.py:329-343, element.py:286-303): t_d and d t_d / dV
+    float trx = 0.0f, try_ = 0.0f, tqx = 0.0f, tqy = 0.0f;
+    if (TRAC && A.tr_fn) {
+        const float tt = step_time(A.step, A.dt);
+        const float size0 = sqrtf(V0);
+        #pragma unroll
+        for (int d = 0; d < 2; ++d) {
+            const int code = A.tr_fn[2 * q + d];
+            if (!code) continue;
+            const float tv = fm(fn_value(A, code, tt), A.tr_tau[2 * q + d]);
+            const float tr = fdv(fm(tv, V), size0), tq = fdv(tv, size0);
+            if (d == 0) {
+                trx = tr;
+                tqx = tq;
+            } else {
+                try_ = tr;
+                tqy = tq;
+            }
+        }
+    }
+
     // G2P, external and internal forces: adjoints of the shape functions (as
     // x-bar, y-bar contributions), of m and V, of the stress the forces used,
     // and the signed sums of the gradient adjoints
@@ -451,9 +473,12 @@ __device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q, float x, 
         const float fbx = A.fbx[n], fby = A.fby[n];
         const float vBx = A.nvbx[n], vBy = A.nvby[n];
         const float fg = fa(fm(fbx, A.gx), fm(fby, A.gy));   // F-bar . g
-        const float Nb = fa(fa(fa(fm(gx, vBx), fm(gy, vBy)),
-                               fa(fm(hx, A.nax[n]), fm(hy, A.nay[n]))),
-                            fm(m, fg));
+        float Nb = fa(fa(fa(fm(gx, vBx), fm(gy, vBy)), fa(fm(hx, A.nax[n]), fm(hy, A.nay[n]))),
+                      fm(m, fg));
+        if (TRAC) {
+            Nb = fa(Nb, fa(fm(fbx, trx), fm(fby, try_)));   // F-bar . traction
+            if (!USL) Vb = fa(Vb, fm(N[k], fa(fm(fbx, tqx), fm(fby, tqy))));
+        }
         if (USL) {
             sAx = k == 0 ? vBx : (k & 1) ? fs(sAx, vBx) : fa(sAx, vBx);
             sAy = k == 0 ? vBy : (k & 1) ? fs(sAy, vBy) : fa(sAy, vBy);
@@ -516,14 +541,14 @@ __device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q, float x, 
     A.lrho[q] = rhob;
 }
 
-template <bool USL>
+template <bool USL, bool TRAC>
 __global__ void __launch_bounds__(PART_THREADS, 4)
 k_rev_forces(const __grid_constant__ AdjStep A) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q < A.np) rev_forces_at<USL>(A, q, A.x[q], A.y[q]);
+    if (q < A.np) rev_forces_at<USL, TRAC>(A, q, A.x[q], A.y[q]);
 }
 
-template <bool USL>
+template <bool USL, bool TRAC>
 __global__ void __launch_bounds__(PART_THREADS, 4)
 k_rev_forces_batch(const AdjStep* __restrict__ table, const int2* __restrict__ blocks) {
     __shared__ AdjStep sA;
@@ -532,7 +557,7 @@ k_rev_forces_batch(const AdjStep* __restrict__ table, const int2* __restrict__ b
     #pragma unroll 1
     for (int k = 0; k < ADJ_ITER; ++k) {
         const int q = (bm.y * ADJ_ITER + k) * PART_THREADS + threadIdx.x;
-        if (q < sA.np) rev_forces_at<USL>(sA, q, sA.x[q], sA.y[q]);
+        if (q < sA.np) rev_forces_at<USL, TRAC>(sA, q, sA.x[q], sA.y[q]);
     }
 }
 
@@ -743,6 +768,7 @@ __global__ void k_adj_table(const AdjStep* __restrict__ bases, int n, int t,
     a.sxx += op; a.syy += op; a.szz += op; a.sxy += op; a.rho += op;
     a.cflag += oc;
     a.nm += on; a.nvax += on; a.nvay += on; a.nvbx += on; a.nvby += on; a.nax += on; a.nay += on;
+    a.step += t;
     table[i] = a;
 }
 
@@ -750,18 +776,31 @@ inline int blocks_for(int n, int t) { return (n + t - 1) / t; }
 
 }  // namespace
 
-cudaError_t launch_rev_step(const AdjStep& A, bool usl, const int4* tiles, int ntiles,
+namespace {
+template <bool USL>
+void rev_forces(const AdjStep& A, bool trac, int pb, cudaStream_t s) {
+    if (trac) k_rev_forces<USL, true><<<pb, PART_THREADS, 0, s>>>(A);
+    else k_rev_forces<USL, false><<<pb, PART_THREADS, 0, s>>>(A);
+}
+template <bool USL>
+void rev_forces_batch(const AdjStep* table, bool trac, const int2* pbk, int npb, cudaStream_t s) {
+    if (trac) k_rev_forces_batch<USL, true><<<npb, PART_THREADS, 0, s>>>(table, pbk);
+    else k_rev_forces_batch<USL, false><<<npb, PART_THREADS, 0, s>>>(table, pbk);
+}
+}  // namespace
+
+cudaError_t launch_rev_step(const AdjStep& A, bool usl, bool trac, const int4* tiles, int ntiles,
                             cudaStream_t s) {
     const int pb = A.np > 0 ? blocks_for(A.np, PART_THREADS) : 0;
     if (usl) {
         if (pb) k_rev_stress_usl<<<pb, PART_THREADS, 0, s>>>(A);
         if (ntiles > 0) k_rev_nodal_kinematics<RK_GATHER><<<ntiles, TILE_THREADS, 0, s>>>(A, tiles);
         if (ntiles > 0) k_rev_nodal_update<true><<<ntiles, TILE_THREADS, 0, s>>>(A, tiles);
-        if (pb) k_rev_forces<true><<<pb, PART_THREADS, 0, s>>>(A);
+        if (pb) rev_forces<true>(A, trac, pb, s);
         if (ntiles > 0) k_rev_nodal_kinematics<RK_NODES><<<ntiles, TILE_THREADS, 0, s>>>(A, tiles);
     } else {
         if (ntiles > 0) k_rev_nodal_update<false><<<ntiles, TILE_THREADS, 0, s>>>(A, tiles);
-        if (pb) k_rev_forces<false><<<pb, PART_THREADS, 0, s>>>(A);
+        if (pb) rev_forces<false>(A, trac, pb, s);
         if (ntiles > 0) k_rev_nodal_kinematics<RK_USF><<<ntiles, TILE_THREADS, 0, s>>>(A, tiles);
     }
     if (pb) k_rev_mass_momentum<<<pb, PART_THREADS, 0, s>>>(A);
@@ -773,18 +812,18 @@ cudaError_t launch_adj_table(const AdjStep* bases, int n, int t, AdjStep* table,
     return cudaGetLastError();
 }
 
-cudaError_t launch_rev_batch(const AdjStep* table, bool usl, const int4* tiles, int ntiles,
+cudaError_t launch_rev_batch(const AdjStep* table, bool usl, bool trac, const int4* tiles, int ntiles,
                              const int2* part_blocks, int n_part_blocks, cudaStream_t s) {
     const int nt = ntiles, npb = n_part_blocks;
     if (usl) {
         if (npb > 0) k_rev_stress_usl_batch<<<npb, PART_THREADS, 0, s>>>(table, part_blocks);
         if (nt > 0) k_rev_nodal_kinematics_batch<RK_GATHER><<<nt, TILE_THREADS, 0, s>>>(table, tiles);
         if (nt > 0) k_rev_nodal_update_batch<true><<<nt, TILE_THREADS, 0, s>>>(table, tiles);
-        if (npb > 0) k_rev_forces_batch<true><<<npb, PART_THREADS, 0, s>>>(table, part_blocks);
+        if (npb > 0) rev_forces_batch<true>(table, trac, part_blocks, npb, s);
         if (nt > 0) k_rev_nodal_kinematics_batch<RK_NODES><<<nt, TILE_THREADS, 0, s>>>(table, tiles);
     } else {
         if (nt > 0) k_rev_nodal_update_batch<false><<<nt, TILE_THREADS, 0, s>>>(table, tiles);
-        if (npb > 0) k_rev_forces_batch<false><<<npb, PART_THREADS, 0, s>>>(table, part_blocks);
+        if (npb > 0) rev_forces_batch<false>(table, trac, part_blocks, npb, s);
         if (nt > 0) k_rev_nodal_kinematics_batch<RK_USF><<<nt, TILE_THREADS, 0, s>>>(table, tiles);
     }
     if (npb > 0) k_rev_mass_momentum_batch<<<npb, PART_THREADS, 0, s>>>(table, part_blocks);

@@ -135,7 +135,8 @@ __device__ __forceinline__ void strain_rate4(const float Gx[4], const float Gy[4
 
 // Piecewise-linear time function (diffmpm/functions.py:40-41, jnp.interp);
 // code 1 = Unit (functions.py:24-25), k + 2 = table k.
-__device__ __forceinline__ float fn_value(const SimDev& S, int code, float t) {
+template <class Tables>   // SimDev, or any struct with the same fn_off, fn_x, fn_y
+__device__ __forceinline__ float fn_value(const Tables& S, int code, float t) {
     if (code <= 1) return 1.0f;
     const int k = code - 2;
     const int b = S.fn_off[k], n = S.fn_off[k + 1] - b;

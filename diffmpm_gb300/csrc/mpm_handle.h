@@ -32,13 +32,15 @@ struct LineAdjoint;    // the 1-D step's full tape and adjoint arrays (mpm_line_
 
 // Full copy of the state of one simulation that steps and re-sorts change:
 // the particle arrays (storage order, current ping-pong parity), material ids,
-// cell starts, drift flags, the persistent nodal velocity and the control
-// block.
+// traction codes, cell starts, drift flags, the persistent nodal velocity and
+// the control block.
 struct Checkpoint {
     int64_t step = 0;
     bool needs_resort = false;
     std::vector<float*> f;   // movable_f32(.., false) of the particle set
     uint8_t* mat = nullptr;
+    int8_t* tr_fn = nullptr;    // particle tractions (2 per particle), when present
+    float* tr_tau = nullptr;
     int* cstart = nullptr;
     uint8_t* cflag = nullptr;
     float *nvbx = nullptr, *nvby = nullptr;

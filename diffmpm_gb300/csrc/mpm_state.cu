@@ -37,11 +37,15 @@ void snapshot_segments(MpmHandle* h, bool save, std::vector<CopySeg>& out) {
 int checkpoint_alloc(MpmHandle* h, Checkpoint& c) {
     const size_t np = (size_t)h->np;
     const size_t nf = movable_f32(h, h->ps[h->pcur], false).size();
-    if (c.f.size() == nf && c.ctl) return MPM_OK;
+    if (c.f.size() == nf && c.ctl && (!h->has_trac || c.tr_fn)) return MPM_OK;
     checkpoint_free(h, c);
     c.f.assign(nf, nullptr);
     for (float*& p : c.f) TRY(dalloc(h, &p, np));
     TRY(dalloc(h, &c.mat, np));
+    if (h->has_trac) {
+        TRY(dalloc(h, &c.tr_fn, 2 * np));
+        TRY(dalloc(h, &c.tr_tau, 2 * np));
+    }
     TRY(dalloc(h, &c.cstart, (size_t)h->ncell + 2));
     TRY(dalloc(h, &c.cflag, (size_t)h->ncell));
     TRY(dalloc(h, &c.nvbx, (size_t)h->nn));
@@ -53,6 +57,8 @@ int checkpoint_alloc(MpmHandle* h, Checkpoint& c) {
 void checkpoint_free(MpmHandle* h, Checkpoint& c) {
     for (float* p : c.f) dfree(h, p);
     dfree(h, c.mat);
+    dfree(h, c.tr_fn);
+    dfree(h, c.tr_tau);
     dfree(h, c.cstart);
     dfree(h, c.cflag);
     dfree(h, c.nvbx);
@@ -73,6 +79,10 @@ void checkpoint_segments(MpmHandle* h, Checkpoint& c, bool save, std::vector<Cop
     const size_t np = (size_t)h->np;
     for (size_t i = 0; i < f.size(); ++i) add(out, *f[i], c.f[i], sizeof(float) * np, save);
     add(out, h->ps[h->pcur].mat, c.mat, np, save);
+    if (h->has_trac && c.tr_fn) {   // they move with the particles at a re-sort
+        add(out, h->ps[h->pcur].tr_fn, c.tr_fn, 2 * np, save);
+        add(out, h->ps[h->pcur].tr_tau, c.tr_tau, sizeof(float) * 2 * np, save);
+    }
     add(out, h->cstart[h->cs_cur], c.cstart, sizeof(int) * ((size_t)h->ncell + 2), save);
     add(out, h->cflag, c.cflag, (size_t)h->ncell, save);
     add(out, h->nvbx, c.nvbx, sizeof(float) * h->nn, save);

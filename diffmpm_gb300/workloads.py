@@ -112,11 +112,13 @@ def youngs_field(npart, seed, median=1e6, sigma_log=0.5):
 
 
 def differentiation(api, n=256, sim_steps=2000, dt=5e-6, seed=101, velocity=None, E=None,
-                    scheme="usf", **kw):
+                    scheme="usf", traction=None, **kw):
     """``E`` overrides the seeded field; ``velocity`` sets the initial particle
     velocity (used by small test variants to make particles change cell): a
     2-vector for all particles, or a function of the (n, 2) positions;
-    ``scheme`` (USF in the configuration) lets tests differentiate USL."""
+    ``scheme`` (USF in the configuration) lets tests differentiate USL;
+    ``traction`` = (dir, value) puts a particle traction on the top layer of
+    particles, ramped linearly from 0 to ``value`` over the run (tests)."""
     h = 1.0 / n
     i0 = int(np.ceil(0.1 * n - 0.5))
     i1 = int(np.floor(0.9 * n - 0.5)) + 1
@@ -132,7 +134,12 @@ def differentiation(api, n=256, sim_steps=2000, dt=5e-6, seed=101, velocity=None
     if velocity is not None:
         v = velocity(pts) if callable(velocity) else velocity
         ps.velocity[:] = np.broadcast_to(np.asarray(v, dtype=np.float64), pts.shape).reshape(-1, 1, 2)
-    mesh = api.Mesh2D({"particles": [ps], "elements": el, "particle_surface_traction": []})
+    tractions = []
+    if traction is not None:
+        top = np.nonzero(pts[:, 1] > pts[:, 1].max() - 0.5 * h)[0]
+        ramp = api.Linear(0, np.array([0.0, sim_steps * dt]), np.array([0.0, 1.0]))
+        tractions = [api.ParticleTraction(0, top, ramp, int(traction[0]), float(traction[1]))]
+    mesh = api.Mesh2D({"particles": [ps], "elements": el, "particle_surface_traction": tractions})
     solver = api.MPMExplicit(mesh, dt, scheme=scheme, velocity_update=False, sim_steps=sim_steps)
     return solver, np.array([0.0, -9.81]), {"workload": "differentiation", "n": n, "np": len(pts),
                                              "seed": seed, "E": E}

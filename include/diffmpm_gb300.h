@@ -233,9 +233,10 @@ int mpm_get_counters(const MpmHandle* h, int64_t* resorts, int64_t* rollbacks);
  * (examples/optim_1d.py:33-41,55 takes jax.value_and_grad of a loss of the
  * final velocities); these two calls are the hand-written reverse of the same
  * steps, with the per-step volume set-up (reinit_each_step = 1), LinearElastic
- * or SimpleMaterial, USF or USL, without particle tractions or particle
- * velocity constraints, on Quadrilateral4Node and Linear1D meshes (other
- * configurations return MPM_ERR_UNSUPPORTED).
+ * or SimpleMaterial, USF or USL, with or without particle tractions
+ * (Quadrilateral4Node), without particle velocity constraints, on
+ * Quadrilateral4Node and Linear1D meshes (other configurations return
+ * MPM_ERR_UNSUPPORTED).
  *
  * mpm_record advances `nsteps` steps like mpm_step and keeps a checkpoint of
  * the full state every `checkpoint_steps` steps (and at the end); on a
