@@ -507,6 +507,11 @@ def run_ours(args, world, rank, local):
     del members, sims
 
     plain, roof = plain_scaleup(args, D, workloads, torch)
+    # the scale-up configuration is run with both schemes; the USL line adds
+    # its own top-kernel roofline for reference
+    plain_usl, roof_usl = plain_scaleup(argparse.Namespace(**dict(vars(args), scheme="usl")), D,
+                                        workloads, torch)
+    plain_usl["roofline"] = roof_usl
     diff = differentiation(args, D, workloads, torch) if args.diff_steps > 0 else None
 
     cpu = None
@@ -562,6 +567,7 @@ def run_ours(args, world, rank, local):
             "gpu_launches": launches,
             "roofline": roof,
             "plain_scaleup": plain,
+            "plain_scaleup_usl": plain_usl,
             "differentiation": diff,
             "clocks": clk,
             "counters": counters,
