@@ -53,6 +53,7 @@ struct Epoch {               // arrays of one sort epoch inside a segment
     int* cstart = nullptr;
     int8_t* tr_fn = nullptr;   // particle tractions (2 per particle), when present
     float* tr_tau = nullptr;
+    uint8_t* pvc = nullptr;    // velocity constraint codes (2 per particle), when present
 };
 
 }  // namespace
@@ -132,6 +133,7 @@ void free_buffers(MpmHandle* h, AdjointState* a) {
         dfree(h, e.cstart);
         dfree(h, e.tr_fn);
         dfree(h, e.tr_tau);
+        dfree(h, e.pvc);
     }
     a->epochs.clear();
     for (float*& p : a->lam) { dfree(h, p); p = nullptr; }
@@ -234,6 +236,10 @@ int epoch_segments(MpmHandle* h, AdjointState* a, size_t e, std::vector<CopySeg>
         TRY(dalloc(h, &ep.tr_fn, 2 * np));
         TRY(dalloc(h, &ep.tr_tau, 2 * np));
     }
+    if (h->has_pvc && !ep.pvc) {
+        drop_adj_graphs(a);
+        TRY(dalloc(h, &ep.pvc, 2 * np));
+    }
     const PSet& p = h->ps[h->pcur];
     add_seg(v, p.pid, ep.pid, sizeof(int) * np, 0);
     add_seg(v, p.mat, ep.mat, np, 0);
@@ -242,6 +248,7 @@ int epoch_segments(MpmHandle* h, AdjointState* a, size_t e, std::vector<CopySeg>
         add_seg(v, p.tr_fn, ep.tr_fn, 2 * np, 0);
         add_seg(v, p.tr_tau, ep.tr_tau, sizeof(float) * 2 * np, 0);
     }
+    if (h->has_pvc) add_seg(v, p.pvc, ep.pvc, 2 * np, 0);
     add_seg(v, h->cstart[h->cs_cur], ep.cstart, sizeof(int) * ((size_t)h->ncell + 2), 0);
     return MPM_OK;
 }
@@ -444,6 +451,7 @@ AdjStep base_args(MpmHandle* h, AdjointState* a, int epoch) {
     A.E = h->has_E ? ep.E : nullptr;
     A.tr_fn = h->has_trac ? ep.tr_fn : nullptr;
     A.tr_tau = h->has_trac ? ep.tr_tau : nullptr;
+    A.pvc = h->has_pvc ? ep.pvc : nullptr;
     A.fn_off = h->d_fn_off;
     A.fn_x = h->d_fn_x;
     A.fn_y = h->d_fn_y;
@@ -533,8 +541,6 @@ int check_supported(MpmHandle* h) {
     if (!h->reinit)
         return fail(h, MPM_ERR_UNSUPPORTED,
                     "the adjoint implements the per-step volume set-up of solve_jit");
-    if (h->has_pvc)
-        return fail(h, MPM_ERR_UNSUPPORTED, "the adjoint does not cover particle velocity constraints");
     for (const MatDev& m : h->mats)
         if (m.type == MAT_NEWTONIAN)
             return fail(h, MPM_ERR_UNSUPPORTED, "the adjoint covers LinearElastic and SimpleMaterial");
@@ -843,6 +849,8 @@ int mpm_batch_adjoint(MpmBatch* b, const float* const* dl_dloc, const float* con
     }
     x->bases.assign(n, AdjStep{});
     std::vector<int> cur(n, -1);   // epoch whose pointers bases[i] holds
+    bool any_pvc = false;
+    for (MpmHandle* h : b->sims) any_pvc = any_pvc || h->has_pvc;
     for (int seg = nseg - 1; seg >= 0 && r == MPM_OK; --seg) {
         const int len = (int)std::min<int64_t>(K, nsteps - (int64_t)seg * K);
         r = batch_recompute(b, x, seg, len, s);
@@ -871,8 +879,8 @@ int mpm_batch_adjoint(MpmBatch* b, const float* const* dl_dloc, const float* con
             }
             if (r != MPM_OK) break;
             BCK(b, launch_adj_table(x->d_bases, n, t, x->d_table, s));
-            BCK(b, launch_rev_batch(x->d_table, b->cfg.usl, b->cfg.traction, b->d_tiles, b->ntiles, x->part_blocks,
-                                    x->n_part_blocks, s));
+            BCK(b, launch_rev_batch(x->d_table, b->cfg.usl, b->cfg.traction, any_pvc, b->d_tiles,
+                                    b->ntiles, x->part_blocks, x->n_part_blocks, s));
         }
         for (int i = 0; i < n && r == MPM_OK; ++i) {
             MpmHandle* h = b->sims[i];

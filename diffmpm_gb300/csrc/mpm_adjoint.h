@@ -62,6 +62,10 @@ struct AdjStep {
     // function tables, and the step number of the step being reversed
     const int8_t* tr_fn;
     const float* tr_tau;
+    // particle velocity constraint codes (2 per particle, epoch storage
+    // order; null when the run has none): a constrained velocity component
+    // is set after G2P and passes no adjoint
+    const uint8_t* pvc;
     const int* fn_off;
     const float *fn_x, *fn_y;
     int step;
@@ -83,8 +87,9 @@ constexpr int ADJ_BLOCK = 256;
 // block copies the simulation's arguments once and walks ADJ_ITER chunks.
 constexpr int ADJ_ITER = 4;
 cudaError_t launch_adj_table(const AdjStep* bases, int n, int t, AdjStep* table, cudaStream_t s);
-cudaError_t launch_rev_batch(const AdjStep* table, bool usl, bool trac, const int4* tiles, int ntiles,
-                             const int2* part_blocks, int n_part_blocks, cudaStream_t s);
+// `pvc`: some simulation of the batch has particle velocity constraints.
+cudaError_t launch_rev_batch(const AdjStep* table, bool usl, bool trac, bool pvc, const int4* tiles,
+                             int ntiles, const int2* part_blocks, int n_part_blocks, cudaStream_t s);
 
 // *mismatch += number of i < n with a[i] != b[i] bitwise (4-byte words).
 cudaError_t launch_count_mismatch(const void* a, const void* b, int n, int* mismatch,

@@ -336,6 +336,31 @@ __device__ __forceinline__ void stress_reverse(const MatDev& mat, float Ep, floa
 }
 
 // ---------------------------------------------------------------------------
+// Particle velocity constraints (applied after the G2P velocity update, an
+// extension): a constrained component of the end-of-step velocity is a
+// constant, so its adjoint is cleared before the reverse passes.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void rev_pvc_at(const AdjStep& A, int q) {
+    if (q >= A.np || !A.pvc) return;
+    const uchar2 c = reinterpret_cast<const uchar2*>(A.pvc)[q];
+    if (c.x) A.lvx[q] = 0.0f;
+    if (c.y) A.lvy[q] = 0.0f;
+}
+
+__global__ void __launch_bounds__(PART_THREADS) k_rev_pvc(const __grid_constant__ AdjStep A) {
+    rev_pvc_at(A, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+__global__ void __launch_bounds__(PART_THREADS)
+k_rev_pvc_batch(const AdjStep* __restrict__ table, const int2* __restrict__ blocks) {
+    __shared__ AdjStep sA;
+    const int2 bm = blocks[blockIdx.x];
+    load_step_args(table + bm.x, sA);
+    #pragma unroll 1
+    for (int k = 0; k < ADJ_ITER; ++k) rev_pvc_at(sA, (bm.y * ADJ_ITER + k) * PART_THREADS + threadIdx.x);
+}
+
+// ---------------------------------------------------------------------------
 // USL pass U (before pass 1): reverse of the strain / density / stress update
 // that USL runs after G2P from the updated nodal velocities vB, at the
 // positions of the step start (scheme.py:127-133, particle.py:249-327).  The
@@ -792,6 +817,7 @@ void rev_forces_batch(const AdjStep* table, bool trac, const int2* pbk, int npb,
 cudaError_t launch_rev_step(const AdjStep& A, bool usl, bool trac, const int4* tiles, int ntiles,
                             cudaStream_t s) {
     const int pb = A.np > 0 ? blocks_for(A.np, PART_THREADS) : 0;
+    if (A.pvc && pb) k_rev_pvc<<<pb, PART_THREADS, 0, s>>>(A);
     if (usl) {
         if (pb) k_rev_stress_usl<<<pb, PART_THREADS, 0, s>>>(A);
         if (ntiles > 0) k_rev_nodal_kinematics<RK_GATHER><<<ntiles, TILE_THREADS, 0, s>>>(A, tiles);
@@ -812,9 +838,10 @@ cudaError_t launch_adj_table(const AdjStep* bases, int n, int t, AdjStep* table,
     return cudaGetLastError();
 }
 
-cudaError_t launch_rev_batch(const AdjStep* table, bool usl, bool trac, const int4* tiles, int ntiles,
-                             const int2* part_blocks, int n_part_blocks, cudaStream_t s) {
+cudaError_t launch_rev_batch(const AdjStep* table, bool usl, bool trac, bool pvc, const int4* tiles,
+                             int ntiles, const int2* part_blocks, int n_part_blocks, cudaStream_t s) {
     const int nt = ntiles, npb = n_part_blocks;
+    if (pvc && npb > 0) k_rev_pvc_batch<<<npb, PART_THREADS, 0, s>>>(table, part_blocks);
     if (usl) {
         if (npb > 0) k_rev_stress_usl_batch<<<npb, PART_THREADS, 0, s>>>(table, part_blocks);
         if (nt > 0) k_rev_nodal_kinematics_batch<RK_GATHER><<<nt, TILE_THREADS, 0, s>>>(table, tiles);

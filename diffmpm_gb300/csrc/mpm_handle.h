@@ -32,8 +32,8 @@ struct LineAdjoint;    // the 1-D step's full tape and adjoint arrays (mpm_line_
 
 // Full copy of the state of one simulation that steps and re-sorts change:
 // the particle arrays (storage order, current ping-pong parity), material ids,
-// traction codes, cell starts, drift flags, the persistent nodal velocity and
-// the control block.
+// traction and velocity-constraint codes, cell starts, drift flags, the
+// persistent nodal velocity and the control block.
 struct Checkpoint {
     int64_t step = 0;
     bool needs_resort = false;
@@ -41,6 +41,7 @@ struct Checkpoint {
     uint8_t* mat = nullptr;
     int8_t* tr_fn = nullptr;    // particle tractions (2 per particle), when present
     float* tr_tau = nullptr;
+    uint8_t* pvc = nullptr;     // particle velocity constraint codes (2 per particle), when present
     int* cstart = nullptr;
     uint8_t* cflag = nullptr;
     float *nvbx = nullptr, *nvby = nullptr;

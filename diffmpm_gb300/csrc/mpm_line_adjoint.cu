@@ -49,6 +49,7 @@ struct LineAdjoint {
     int* cs = nullptr;         // [T][nx + 2]
     float* N = nullptr;        // [T][LN_N][nn]
     uint8_t* mat0 = nullptr;   // material ids, original order
+    uint8_t* pvc0 = nullptr;   // velocity constraint codes, original order (or null)
     float* E0 = nullptr;       // per-particle Young's modulus, original order (or null)
     int* eid = nullptr;        // element of each storage slot of the step being reversed
     float* L = nullptr;        // [LA_N][np]
@@ -72,6 +73,7 @@ struct LineStep {
     const float* M; const float* vA; const float* vB; const float* a;
     const uint16_t* ncons;
     const MatDev* mats; const uint8_t* mat0; const float* E0;
+    const uint8_t* pvc0;
     float* L[LA_N];
     float* sc[LS_N];
     float* ns[LNS_N];
@@ -176,7 +178,8 @@ __global__ void k_lrev1(const __grid_constant__ LineStep A) {
     const Elem g = elem_of(A, e);
     float N0, N1, d0, d1;
     shapes(g, A.x[q], N0, N1, d0, d1);
-    const float lx = A.L[LA_X][o], lv = A.L[LA_V][o];
+    // a constrained end velocity (particle velocity constraint) is a constant
+    const float lx = A.L[LA_X][o], lv = (A.pvc0 && A.pvc0[o]) ? 0.0f : A.L[LA_V][o];
     const float gh = fa(fm(lx, A.dt), A.velocity_update ? lv : 0.0f);
     const float hh = A.velocity_update ? 0.0f : fm(lv, A.dt);
     A.sc[LS_G][q] = gh;
@@ -296,11 +299,12 @@ __global__ void k_lrev5(const __grid_constant__ LineStep A) {
     A.L[LA_RHO][o] = fa(A.L[LA_RHO][o], fm(g.V0, mb));
 }
 
-// Material ids from storage to original order.
+// Material ids (or every `stride`-th byte of a per-particle code array) from
+// storage to original order.
 __global__ void k_lmat0(const uint8_t* __restrict__ mat, const int* __restrict__ pid, int np,
-                        uint8_t* __restrict__ out) {
+                        int stride, uint8_t* __restrict__ out) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q < np) out[pid[q]] = mat[q];
+    if (q < np) out[pid[q]] = mat[(size_t)q * stride];
 }
 
 __global__ void k_lfill(float* __restrict__ p, int64_t n, float v) {
@@ -327,8 +331,6 @@ int line_alloc(MpmHandle* h, LineAdjoint* a, T** p, size_t n) {
 int line_check(MpmHandle* h) {
     if (!h->reinit)
         return fail(h, MPM_ERR_UNSUPPORTED, "the 1-D adjoint implements the per-step volume set-up of solve_jit");
-    if (h->has_pvc)
-        return fail(h, MPM_ERR_UNSUPPORTED, "the adjoint does not cover particle velocity constraints");
     for (const MatDev& m : h->mats)
         if (m.type == MAT_NEWTONIAN)
             return fail(h, MPM_ERR_UNSUPPORTED, "the adjoint covers LinearElastic and SimpleMaterial");
@@ -372,7 +374,11 @@ int line_record(MpmHandle* h, int nsteps, cudaStream_t s) {
     TRY(line_alloc(h, a, &a->sc, (size_t)LS_N * np));
     TRY(line_alloc(h, a, &a->ns, (size_t)LNS_N * nn));
     const PSet& p = h->ps[h->pcur];
-    if (np > 0) k_lmat0<<<lblocks((int64_t)np), LA_THREADS, 0, s>>>(p.mat, p.pid, (int)np, a->mat0);
+    if (np > 0) k_lmat0<<<lblocks((int64_t)np), LA_THREADS, 0, s>>>(p.mat, p.pid, (int)np, 1, a->mat0);
+    if (h->has_pvc) {
+        TRY(line_alloc(h, a, &a->pvc0, np));
+        if (np > 0) k_lmat0<<<lblocks((int64_t)np), LA_THREADS, 0, s>>>(p.pvc, p.pid, (int)np, 2, a->pvc0);
+    }
     CK(h, cudaGetLastError());
     if (h->has_E) {
         TRY(line_alloc(h, a, &a->E0, np));
@@ -425,6 +431,7 @@ int line_adjoint(MpmHandle* h, const float* dl_dloc, const float* dl_dvel, float
     A.mats = h->d_mats;
     A.mat0 = a->mat0;
     A.E0 = a->E0;
+    A.pvc0 = a->pvc0;
     for (int k = 0; k < LA_N; ++k) A.L[k] = L + (size_t)k * np;
     for (int k = 0; k < LS_N; ++k) A.sc[k] = a->sc + (size_t)k * np;
     for (int k = 0; k < LNS_N; ++k) A.ns[k] = a->ns + (size_t)k * a->nn;

@@ -37,7 +37,7 @@ void snapshot_segments(MpmHandle* h, bool save, std::vector<CopySeg>& out) {
 int checkpoint_alloc(MpmHandle* h, Checkpoint& c) {
     const size_t np = (size_t)h->np;
     const size_t nf = movable_f32(h, h->ps[h->pcur], false).size();
-    if (c.f.size() == nf && c.ctl && (!h->has_trac || c.tr_fn)) return MPM_OK;
+    if (c.f.size() == nf && c.ctl && (!h->has_trac || c.tr_fn) && (!h->has_pvc || c.pvc)) return MPM_OK;
     checkpoint_free(h, c);
     c.f.assign(nf, nullptr);
     for (float*& p : c.f) TRY(dalloc(h, &p, np));
@@ -46,6 +46,7 @@ int checkpoint_alloc(MpmHandle* h, Checkpoint& c) {
         TRY(dalloc(h, &c.tr_fn, 2 * np));
         TRY(dalloc(h, &c.tr_tau, 2 * np));
     }
+    if (h->has_pvc) TRY(dalloc(h, &c.pvc, 2 * np));
     TRY(dalloc(h, &c.cstart, (size_t)h->ncell + 2));
     TRY(dalloc(h, &c.cflag, (size_t)h->ncell));
     TRY(dalloc(h, &c.nvbx, (size_t)h->nn));
@@ -59,6 +60,7 @@ void checkpoint_free(MpmHandle* h, Checkpoint& c) {
     dfree(h, c.mat);
     dfree(h, c.tr_fn);
     dfree(h, c.tr_tau);
+    dfree(h, c.pvc);
     dfree(h, c.cstart);
     dfree(h, c.cflag);
     dfree(h, c.nvbx);
@@ -83,6 +85,7 @@ void checkpoint_segments(MpmHandle* h, Checkpoint& c, bool save, std::vector<Cop
         add(out, h->ps[h->pcur].tr_fn, c.tr_fn, 2 * np, save);
         add(out, h->ps[h->pcur].tr_tau, c.tr_tau, sizeof(float) * 2 * np, save);
     }
+    if (h->has_pvc && c.pvc) add(out, h->ps[h->pcur].pvc, c.pvc, 2 * np, save);
     add(out, h->cstart[h->cs_cur], c.cstart, sizeof(int) * ((size_t)h->ncell + 2), save);
     add(out, h->cflag, c.cflag, (size_t)h->ncell, save);
     add(out, h->nvbx, c.nvbx, sizeof(float) * h->nn, save);

@@ -234,7 +234,7 @@ int mpm_get_counters(const MpmHandle* h, int64_t* resorts, int64_t* rollbacks);
  * final velocities); these two calls are the hand-written reverse of the same
  * steps, with the per-step volume set-up (reinit_each_step = 1), LinearElastic
  * or SimpleMaterial, USF or USL, with or without particle tractions
- * (Quadrilateral4Node), without particle velocity constraints, on
+ * (Quadrilateral4Node) and particle velocity constraints, on
  * Quadrilateral4Node and Linear1D meshes (other configurations return
  * MPM_ERR_UNSUPPORTED).
  *

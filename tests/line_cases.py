@@ -3,11 +3,12 @@ import numpy as np
 
 
 def bar(api, nx=40, ppe=3, scheme="usf", velocity_update=False, sim_steps=50, dt=2e-4,
-        material="linear", gravity=-9.81, seed=4, E=None, vshift=0.0, **kw):
+        material="linear", gravity=-9.81, seed=4, E=None, vshift=0.0, pvc=False, **kw):
     """A bar of ``nx`` elements on [0, 1], ``ppe`` particles per element over
     the middle 80 % of the elements with seeded jitter, node 0 fixed, a
     sinusoidal initial velocity (plus a uniform ``vshift``), gravity along the
-    bar and a concentrated force ramp at the free end."""
+    bar and a concentrated force ramp at the free end; ``pvc`` holds every
+    4th particle's velocity with a particle velocity constraint."""
     h = 1.0 / nx
     rng = np.random.Generator(np.random.PCG64(seed))
     e0, e1 = int(0.1 * nx), int(0.9 * nx)
@@ -28,6 +29,9 @@ def bar(api, nx=40, ppe=3, scheme="usf", velocity_update=False, sim_steps=50, dt
     mesh = api.Mesh1D({"particles": [ps], "elements": el, "particle_surface_traction": []})
     solver = api.MPMExplicit(mesh, dt, scheme=scheme, velocity_update=velocity_update,
                              sim_steps=sim_steps)
+    if pvc:   # every 4th particle held at 0.02 m/s
+        mesh.particle_velocity_constraints = [
+            api.ParticleVelocityConstraint(pset=0, pids=np.arange(0, x.size, 4), dir=0, velocity=0.02)]
     return solver, np.array([gravity])
 
 

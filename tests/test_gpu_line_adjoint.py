@@ -39,7 +39,8 @@ def oracle_end(case, steps, E, x0=None, v0=None):
 CASES = [dict(scheme="usf"), dict(scheme="usl"), dict(scheme="usf", material="simple"),
          dict(scheme="usl", material="simple", nx=12, ppe=1),
          dict(scheme="usf", velocity_update=True),
-         dict(scheme="usf", vshift=8.0), dict(scheme="usl", vshift=8.0)]
+         dict(scheme="usf", vshift=8.0), dict(scheme="usl", vshift=8.0),
+         dict(scheme="usf", pvc=True), dict(scheme="usl", pvc=True, vshift=8.0)]
 
 
 @pytest.mark.parametrize("case", CASES, ids=lambda c: "-".join(f"{k}={v}" for k, v in c.items()))
