@@ -333,8 +333,8 @@ int run_cached_graph(MpmHandle* h, std::map<int, cudaGraphExec_t>& map, int key,
 }
 
 // Re-run of a segment of `len` steps without a re-sort as one graph: per
-// step the tape copy of the start state, the step's kernels and the tape copy
-// of the nodal results.
+// step the tape copy of the start state, the step's kernels (at step offset
+// t) and the tape copy of the nodal results; the step counter advances once.
 int rerun_graph(MpmHandle* h, AdjointState* a, int len, cudaStream_t s) {
     TRY(prepare_adj_graphs(h, a, s));
     const int par0 = parity(h);
@@ -342,9 +342,10 @@ int rerun_graph(MpmHandle* h, AdjointState* a, int len, cudaStream_t s) {
         for (int t = 0; t < len; ++t) {
             const SegBuf& tp = a->g_tp[(par0 + t) & 1];
             CK(h, launch_copy_segments(tp.segs, tp.first, tp.nseg, tp.nblocks, t, c));
-            TRY(launch_steps(h, 1, c));
+            for (int p = 0; p < 3; ++p) TRY(launch_phase(h, p, t, c));
             CK(h, launch_copy_segments(a->g_tn.segs, a->g_tn.first, a->g_tn.nseg, a->g_tn.nblocks, t, c));
         }
+        CK(h, launch_advance_step(h->ctl, len, c));
         return MPM_OK;
     }));
     h->step += len;

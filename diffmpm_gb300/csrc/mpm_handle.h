@@ -189,6 +189,8 @@ int read_ctl(MpmHandle* h, cudaStream_t s);
 int clear_status(MpmHandle* h, cudaStream_t s);
 int resort(MpmHandle* h, cudaStream_t s);
 int launch_steps(MpmHandle* h, int n, cudaStream_t s);
+// Phase `phase` (0 nodal kinematics, 1 forces, 2 G2P) of step ctl->step + k.
+int launch_phase(MpmHandle* h, int phase, int k, cudaStream_t s);
 int check_status(MpmHandle* h, int& st);
 int take_snapshot(MpmHandle* h, cudaStream_t s);
 int replay_block(MpmHandle* h, int64_t step0, int B, int& st, cudaStream_t s);
