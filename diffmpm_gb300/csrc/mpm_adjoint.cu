@@ -40,7 +40,7 @@ namespace mpm {
 
 namespace {
 
-constexpr int NLAM = 10;   // adjoint arrays: x y vx vy sxx syy szz sxy rho E
+constexpr int NLAM = 11;   // adjoint arrays: x y vx vy sxx syy szz sxy rho E vol
 constexpr int NTP = 9;     // tape per particle: x y vx vy sxx syy szz sxy rho
 constexpr int NTN = 7;     // tape per node: m vAx vAy vBx vBy aBx aBy
 constexpr int NPS = 5;     // per-particle scratch: r0b r1b r3b c0b c1b
@@ -54,6 +54,8 @@ struct Epoch {               // arrays of one sort epoch inside a segment
     int8_t* tr_fn = nullptr;   // particle tractions (2 per particle), when present
     float* tr_tau = nullptr;
     uint8_t* pvc = nullptr;    // velocity constraint codes (2 per particle), when present
+    float* mass = nullptr;     // solve semantics: the constant mass and size
+    float* psize = nullptr;
 };
 
 }  // namespace
@@ -69,6 +71,7 @@ struct AdjointState {
     int64_t np_alloc = -1;
     int tape_slots = 0;
     float* tp[NTP] = {};
+    float* tvol = nullptr;     // volume at each step start (solve semantics only)
     uint8_t* tflag = nullptr;
     float* tn[NTN] = {};
     std::vector<Epoch> epochs;
@@ -123,6 +126,8 @@ void free_buffers(MpmHandle* h, AdjointState* a) {
     a->ck.clear();
     for (float*& p : a->tp) { dfree(h, p); p = nullptr; }
     for (float*& p : a->tn) { dfree(h, p); p = nullptr; }
+    dfree(h, a->tvol);
+    a->tvol = nullptr;
     dfree(h, a->tflag);
     a->tflag = nullptr;
     a->tape_slots = 0;
@@ -134,6 +139,8 @@ void free_buffers(MpmHandle* h, AdjointState* a) {
         dfree(h, e.tr_fn);
         dfree(h, e.tr_tau);
         dfree(h, e.pvc);
+        dfree(h, e.mass);
+        dfree(h, e.psize);
     }
     a->epochs.clear();
     for (float*& p : a->lam) { dfree(h, p); p = nullptr; }
@@ -178,14 +185,17 @@ int restore_checkpoint(MpmHandle* h, Checkpoint& c, cudaStream_t s) {
 
 int ensure_adjoint_buffers(MpmHandle* h, AdjointState* a, int slots, cudaStream_t s) {
     const size_t np = (size_t)h->np, nn = (size_t)h->nn;
-    if (a->tape_slots < slots) {
+    if (a->tape_slots < slots || (!h->reinit && !a->tvol)) {
         drop_adj_graphs(a);
         for (float*& p : a->tp) { dfree(h, p); p = nullptr; }
+        dfree(h, a->tvol);
+        a->tvol = nullptr;
         for (float*& p : a->tn) { dfree(h, p); p = nullptr; }
         dfree(h, a->tflag);
         a->tflag = nullptr;
         a->tape_slots = 0;
         for (float*& p : a->tp) TRY(dalloc(h, &p, np * slots));
+        if (!h->reinit) TRY(dalloc(h, &a->tvol, np * slots));
         for (float*& p : a->tn) TRY(dalloc(h, &p, nn * slots));
         TRY(dalloc(h, &a->tflag, (size_t)h->ncell * slots));
         a->tape_slots = slots;
@@ -240,6 +250,11 @@ int epoch_segments(MpmHandle* h, AdjointState* a, size_t e, std::vector<CopySeg>
         drop_adj_graphs(a);
         TRY(dalloc(h, &ep.pvc, 2 * np));
     }
+    if (!h->reinit && !ep.mass) {
+        drop_adj_graphs(a);
+        TRY(dalloc(h, &ep.mass, np));
+        TRY(dalloc(h, &ep.psize, np));
+    }
     const PSet& p = h->ps[h->pcur];
     add_seg(v, p.pid, ep.pid, sizeof(int) * np, 0);
     add_seg(v, p.mat, ep.mat, np, 0);
@@ -249,6 +264,10 @@ int epoch_segments(MpmHandle* h, AdjointState* a, size_t e, std::vector<CopySeg>
         add_seg(v, p.tr_tau, ep.tr_tau, sizeof(float) * 2 * np, 0);
     }
     if (h->has_pvc) add_seg(v, p.pvc, ep.pvc, 2 * np, 0);
+    if (!h->reinit) {
+        add_seg(v, p.mass, ep.mass, sizeof(float) * np, 0);
+        add_seg(v, p.psize, ep.psize, sizeof(float) * np, 0);
+    }
     add_seg(v, h->cstart[h->cs_cur], ep.cstart, sizeof(int) * ((size_t)h->ncell + 2), 0);
     return MPM_OK;
 }
@@ -268,6 +287,7 @@ void tape_particle_segments(MpmHandle* h, AdjointState* a, int par, std::vector<
     const float* src[NTP] = {p.x, p.y, p.vx, p.vy, p.sxx[par], p.syy[par], p.szz[par],
                              p.sxy[par], p.rho[par]};
     for (int k = 0; k < NTP; ++k) add_seg(v, src[k], a->tp[k], sizeof(float) * np, sizeof(float) * np);
+    if (!h->reinit) add_seg(v, p.vol[par], a->tvol, sizeof(float) * np, sizeof(float) * np);
     add_seg(v, h->cflag, a->tflag, (size_t)h->ncell, (size_t)h->ncell);
 }
 
@@ -453,6 +473,10 @@ AdjStep base_args(MpmHandle* h, AdjointState* a, int epoch) {
     A.tr_fn = h->has_trac ? ep.tr_fn : nullptr;
     A.tr_tau = h->has_trac ? ep.tr_tau : nullptr;
     A.pvc = h->has_pvc ? ep.pvc : nullptr;
+    A.reinit = h->reinit ? 1 : 0;
+    A.vol = h->reinit ? nullptr : a->tvol;
+    A.mass = h->reinit ? nullptr : ep.mass;
+    A.psize = h->reinit ? nullptr : ep.psize;
     A.fn_off = h->d_fn_off;
     A.fn_x = h->d_fn_x;
     A.fn_y = h->d_fn_y;
@@ -463,7 +487,7 @@ AdjStep base_args(MpmHandle* h, AdjointState* a, int epoch) {
     const float** tn[NTN] = {&A.nm, &A.nvax, &A.nvay, &A.nvbx, &A.nvby, &A.nax, &A.nay};
     for (int k = 0; k < NTN; ++k) *tn[k] = a->tn[k];
     float** lam[NLAM] = {&A.lx, &A.ly, &A.lvx, &A.lvy, &A.lsxx, &A.lsyy, &A.lszz, &A.lsxy,
-                         &A.lrho, &A.lE};
+                         &A.lrho, &A.lE, &A.lvol};
     for (int k = 0; k < NLAM; ++k) *lam[k] = a->lam[k];
     float** ps[NPS] = {&A.r0b, &A.r1b, &A.r3b, &A.c0b, &A.c1b};
     for (int k = 0; k < NPS; ++k) *ps[k] = a->pscr[k];
@@ -481,6 +505,7 @@ int reverse_step(MpmHandle* h, AdjointState* a, int t, cudaStream_t s) {
     const size_t op = (size_t)t * A.sp, on = (size_t)t * A.sn, oc = (size_t)t * A.sc;
     A.x += op; A.y += op; A.vx += op; A.vy += op;
     A.sxx += op; A.syy += op; A.szz += op; A.sxy += op; A.rho += op;
+    if (A.vol) A.vol += op;
     A.cflag += oc;
     A.nm += on; A.nvax += on; A.nvay += on; A.nvbx += on; A.nvby += on; A.nax += on; A.nay += on;
     A.step += t;
@@ -539,9 +564,6 @@ int emit_all(MpmHandle* h, AdjointState* a, float* dl_dE, float* dl_dloc0, float
 
 int check_supported(MpmHandle* h) {
     if (h->ndim != 2) return fail(h, MPM_ERR_UNSUPPORTED, "the adjoint implements Quadrilateral4Node meshes");
-    if (!h->reinit)
-        return fail(h, MPM_ERR_UNSUPPORTED,
-                    "the adjoint implements the per-step volume set-up of solve_jit");
     for (const MatDev& m : h->mats)
         if (m.type == MAT_NEWTONIAN)
             return fail(h, MPM_ERR_UNSUPPORTED, "the adjoint covers LinearElastic and SimpleMaterial");
@@ -880,8 +902,8 @@ int mpm_batch_adjoint(MpmBatch* b, const float* const* dl_dloc, const float* con
             }
             if (r != MPM_OK) break;
             BCK(b, launch_adj_table(x->d_bases, n, t, x->d_table, s));
-            BCK(b, launch_rev_batch(x->d_table, b->cfg.usl, b->cfg.traction, any_pvc, b->d_tiles,
-                                    b->ntiles, x->part_blocks, x->n_part_blocks, s));
+            BCK(b, launch_rev_batch(x->d_table, b->cfg.usl, b->cfg.traction, any_pvc, b->cfg.reinit,
+                                    b->d_tiles, b->ntiles, x->part_blocks, x->n_part_blocks, s));
         }
         for (int i = 0; i < n && r == MPM_OK; ++i) {
             MpmHandle* h = b->sims[i];

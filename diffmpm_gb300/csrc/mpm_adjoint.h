@@ -66,6 +66,12 @@ struct AdjStep {
     // order; null when the run has none): a constrained velocity component
     // is set after G2P and passes no adjoint
     const uint8_t* pvc;
+    // solve semantics (reinit 0: no per-step volume set-up): the volume at the
+    // step start (tape), the constant mass and size (epoch order) and the
+    // volume adjoint (in: end of step; out: start of step)
+    int reinit;
+    const float *vol, *mass, *psize;
+    float* lvol;
     const int* fn_off;
     const float *fn_x, *fn_y;
     int step;
@@ -88,8 +94,9 @@ constexpr int ADJ_BLOCK = 256;
 constexpr int ADJ_ITER = 4;
 cudaError_t launch_adj_table(const AdjStep* bases, int n, int t, AdjStep* table, cudaStream_t s);
 // `pvc`: some simulation of the batch has particle velocity constraints.
-cudaError_t launch_rev_batch(const AdjStep* table, bool usl, bool trac, bool pvc, const int4* tiles,
-                             int ntiles, const int2* part_blocks, int n_part_blocks, cudaStream_t s);
+cudaError_t launch_rev_batch(const AdjStep* table, bool usl, bool trac, bool pvc, bool reinit,
+                             const int4* tiles, int ntiles, const int2* part_blocks, int n_part_blocks,
+                             cudaStream_t s);
 
 // *mismatch += number of i < n with a[i] != b[i] bitwise (4-byte words).
 cudaError_t launch_count_mismatch(const void* a, const void* b, int n, int* mismatch,

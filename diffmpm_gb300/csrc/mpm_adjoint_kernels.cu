@@ -368,6 +368,7 @@ k_rev_pvc_batch(const AdjStep* __restrict__ table, const int2* __restrict__ bloc
 // adjoints go to pass G (their transposed gather) and to pass 2 (their
 // position terms); the density adjoint becomes that of the step start.
 // ---------------------------------------------------------------------------
+template <bool REINIT>
 __device__ __forceinline__ void rev_stress_usl_at(const AdjStep& A, int q, float x, float y) {
     if (q >= A.np) return;
     int ci, cj;
@@ -389,7 +390,12 @@ __device__ __forceinline__ void rev_stress_usl_at(const AdjStep& A, int q, float
     stress_reverse(mat, Ep, A.dt, r0, r1, r3, A.lsxx[q], A.lsyy[q], A.lszz[q], A.lsxy[q], r0b, r1b,
                    r3b, Eb);
     const float lrho = A.lrho[q];
-    const float fb = -fdv(fm(lrho, rho1), f);
+    float fb = -fdv(fm(lrho, rho1), f);
+    if (!REINIT) {   // solve semantics: V' = V f carries the volume to the next step
+        const float lv = A.lvol[q];
+        fb = fa(fb, fm(lv, A.vol[q]));
+        A.lvol[q] = fm(lv, f);
+    }
     A.r0b[q] = r0b;
     A.r1b[q] = r1b;
     A.r3b[q] = r3b;
@@ -399,12 +405,14 @@ __device__ __forceinline__ void rev_stress_usl_at(const AdjStep& A, int q, float
     A.lE[q] = fa(A.lE[q], Eb);
 }
 
+template <bool REINIT>
 __global__ void __launch_bounds__(PART_THREADS)
 k_rev_stress_usl(const __grid_constant__ AdjStep A) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q < A.np) rev_stress_usl_at(A, q, A.x[q], A.y[q]);
+    if (q < A.np) rev_stress_usl_at<REINIT>(A, q, A.x[q], A.y[q]);
 }
 
+template <bool REINIT>
 __global__ void __launch_bounds__(PART_THREADS)
 k_rev_stress_usl_batch(const AdjStep* __restrict__ table, const int2* __restrict__ blocks) {
     __shared__ AdjStep sA;
@@ -413,7 +421,7 @@ k_rev_stress_usl_batch(const AdjStep* __restrict__ table, const int2* __restrict
     #pragma unroll 1
     for (int k = 0; k < ADJ_ITER; ++k) {
         const int q = (bm.y * ADJ_ITER + k) * PART_THREADS + threadIdx.x;
-        if (q < sA.np) rev_stress_usl_at(sA, q, sA.x[q], sA.y[q]);
+        if (q < sA.np) rev_stress_usl_at<REINIT>(sA, q, sA.x[q], sA.y[q]);
     }
 }
 
@@ -424,7 +432,7 @@ k_rev_stress_usl_batch(const AdjStep* __restrict__ table, const int2* __restrict
 // reset volume V0; the strain-rate adjoints of its later stress update come
 // from pass U and only add their position terms here.
 // ---------------------------------------------------------------------------
-template <bool USL, bool TRAC>
+template <bool USL, bool TRAC, bool REINIT>
 __device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q, float x, float y) {
     if (q >= A.np) return;
     int ci, cj;
@@ -436,10 +444,17 @@ __device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q, float x, 
     dshape4(xi, eta, g.rx, g.ry, Gx, Gy);
     const int ll = cj * (A.nx + 1) + ci;
     const int ids[4] = {ll, ll + 1, ll + A.nx + 2, ll + A.nx + 1};
-    const int cnt = A.cnt[cj * A.nx + ci];
-    const float V0 = cnt ? fdv(A.vol_el, (float)cnt) : 0.0f;
+    // V0: the volume at the step start (the per-step set-up V_el / count, or
+    // under solve semantics the carried volume); m: the particle mass
+    float V0;
+    if (REINIT) {
+        const int cnt = A.cnt[cj * A.nx + ci];
+        V0 = cnt ? fdv(A.vol_el, (float)cnt) : 0.0f;
+    } else {
+        V0 = A.vol[q];
+    }
     const float rho0 = A.rho[q];
-    const float m = fm(V0, rho0);
+    const float m = REINIT ? fm(V0, rho0) : A.mass[q];
 
     // the stress and volume of the forces: USF recomputes the strain rates
     // from vA and the stress update; sAx, sAy: signed sums of the corner
@@ -468,7 +483,7 @@ __device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q, float x, 
     float trx = 0.0f, try_ = 0.0f, tqx = 0.0f, tqy = 0.0f;
     if (TRAC && A.tr_fn) {
         const float tt = step_time(A.step, A.dt);
-        const float size0 = sqrtf(V0);
+        const float size0 = REINIT ? sqrtf(V0) : A.psize[q];
         #pragma unroll
         for (int d = 0; d < 2; ++d) {
             const int code = A.tr_fn[2 * q + d];
@@ -502,7 +517,7 @@ __device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q, float x, 
                       fm(m, fg));
         if (TRAC) {
             Nb = fa(Nb, fa(fm(fbx, trx), fm(fby, try_)));   // F-bar . traction
-            if (!USL) Vb = fa(Vb, fm(N[k], fa(fm(fbx, tqx), fm(fby, tqy))));
+            if (!USL || !REINIT) Vb = fa(Vb, fm(N[k], fa(fm(fbx, tqx), fm(fby, tqy))));
         }
         if (USL) {
             sAx = k == 0 ? vBx : (k & 1) ? fs(sAx, vBx) : fa(sAx, vBx);
@@ -511,7 +526,7 @@ __device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q, float x, 
         mb = fa(mb, fm(N[k], fg));
         const float fx = fa(fm(Gx[k], p.sxx), fm(Gy[k], p.sxy));
         const float fy = fa(fm(Gy[k], p.syy), fm(Gx[k], p.sxy));
-        if (!USL) Vb = fs(Vb, fa(fm(fbx, fx), fm(fby, fy)));
+        if (!USL || !REINIT) Vb = fs(Vb, fa(fm(fbx, fx), fm(fby, fy)));
         fsxx = fa(fsxx, fm(fbx, Gx[k]));
         fsyy = fa(fsyy, fm(fby, Gy[k]));
         fsxy = fa(fsxy, fa(fm(fbx, Gy[k]), fm(fby, Gx[k])));
@@ -533,14 +548,18 @@ __device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q, float x, 
         r0b = A.r0b[q];
         r1b = A.r1b[q];
         r3b = A.r3b[q];
-        rhob = fa(A.lrho[q], fm(V0, mb));
+        rhob = REINIT ? fa(A.lrho[q], fm(V0, mb)) : A.lrho[q];
+        if (!REINIT) A.lvol[q] = fa(A.lvol[q], Vb);   // the forces used the start volume
     } else {
         float Eb;
         stress_reverse(mat, Ep, A.dt, r0, r1, r3, sbxx, sbyy, sbzz, sbxy, r0b, r1b, r3b, Eb);
         // reverse of V = V0 (1 + dvol), rho' = rho / (1 + dvol), m = V0 rho
+        // (solve semantics: m is constant and V also carries to the next step)
         const float lrho = A.lrho[q];
-        const float fb = fs(fm(Vb, V0), fdv(fm(lrho, p.rho), f));
-        rhob = fa(fdv(lrho, f), fm(V0, mb));
+        const float Vt = REINIT ? Vb : fa(Vb, A.lvol[q]);
+        const float fb = fs(fm(Vt, V0), fdv(fm(lrho, p.rho), f));
+        rhob = REINIT ? fa(fdv(lrho, f), fm(V0, mb)) : fdv(lrho, f);
+        if (!REINIT) A.lvol[q] = fm(Vt, f);
         A.lE[q] = fa(A.lE[q], Eb);
         A.r0b[q] = r0b;
         A.r1b[q] = r1b;
@@ -566,14 +585,14 @@ __device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q, float x, 
     A.lrho[q] = rhob;
 }
 
-template <bool USL, bool TRAC>
+template <bool USL, bool TRAC, bool REINIT>
 __global__ void __launch_bounds__(PART_THREADS, 4)
 k_rev_forces(const __grid_constant__ AdjStep A) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q < A.np) rev_forces_at<USL, TRAC>(A, q, A.x[q], A.y[q]);
+    if (q < A.np) rev_forces_at<USL, TRAC, REINIT>(A, q, A.x[q], A.y[q]);
 }
 
-template <bool USL, bool TRAC>
+template <bool USL, bool TRAC, bool REINIT>
 __global__ void __launch_bounds__(PART_THREADS, 4)
 k_rev_forces_batch(const AdjStep* __restrict__ table, const int2* __restrict__ blocks) {
     __shared__ AdjStep sA;
@@ -582,7 +601,7 @@ k_rev_forces_batch(const AdjStep* __restrict__ table, const int2* __restrict__ b
     #pragma unroll 1
     for (int k = 0; k < ADJ_ITER; ++k) {
         const int q = (bm.y * ADJ_ITER + k) * PART_THREADS + threadIdx.x;
-        if (q < sA.np) rev_forces_at<USL, TRAC>(sA, q, sA.x[q], sA.y[q]);
+        if (q < sA.np) rev_forces_at<USL, TRAC, REINIT>(sA, q, sA.x[q], sA.y[q]);
     }
 }
 
@@ -706,6 +725,7 @@ k_rev_nodal_kinematics_batch(const AdjStep* __restrict__ table, const int4* __re
 // Pass 4: reverse of the mass and momentum P2G (element.py:122-189) and of
 // m = V0 rho (particle.py:158-178).
 // ---------------------------------------------------------------------------
+template <bool REINIT>
 __device__ __forceinline__ void rev_mass_momentum_at(const AdjStep& A, int q, float x, float y) {
     if (q >= A.np) return;
     int ci, cj;
@@ -717,9 +737,14 @@ __device__ __forceinline__ void rev_mass_momentum_at(const AdjStep& A, int q, fl
     dshape4(xi, eta, g.rx, g.ry, Gx, Gy);
     const int ll = cj * (A.nx + 1) + ci;
     const int ids[4] = {ll, ll + 1, ll + A.nx + 2, ll + A.nx + 1};
-    const int cnt = A.cnt[cj * A.nx + ci];
-    const float V0 = cnt ? fdv(A.vol_el, (float)cnt) : 0.0f;
-    const float m = fm(V0, A.rho[q]);
+    float V0 = 0.0f, m;
+    if (REINIT) {
+        const int cnt = A.cnt[cj * A.nx + ci];
+        V0 = cnt ? fdv(A.vol_el, (float)cnt) : 0.0f;
+        m = fm(V0, A.rho[q]);
+    } else {
+        m = A.mass[q];   // solve semantics: constant mass
+    }
     const float vx = A.vx[q], vy = A.vy[q];
     float mb = 0.0f, sqx = 0.0f, sqy = 0.0f, xb = A.lx[q], yb = A.ly[q];
     #pragma unroll
@@ -737,17 +762,19 @@ __device__ __forceinline__ void rev_mass_momentum_at(const AdjStep& A, int q, fl
     const float lvy = A.velocity_update ? 0.0f : A.lvy[q];
     A.lvx[q] = fa(lvx, fm(m, sqx));
     A.lvy[q] = fa(lvy, fm(m, sqy));
-    A.lrho[q] = fa(A.lrho[q], fm(V0, mb));
+    if (REINIT) A.lrho[q] = fa(A.lrho[q], fm(V0, mb));
     A.lx[q] = xb;
     A.ly[q] = yb;
 }
 
+template <bool REINIT>
 __global__ void __launch_bounds__(PART_THREADS)
 k_rev_mass_momentum(const __grid_constant__ AdjStep A) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q < A.np) rev_mass_momentum_at(A, q, A.x[q], A.y[q]);
+    if (q < A.np) rev_mass_momentum_at<REINIT>(A, q, A.x[q], A.y[q]);
 }
 
+template <bool REINIT>
 __global__ void __launch_bounds__(PART_THREADS)
 k_rev_mass_momentum_batch(const AdjStep* __restrict__ table, const int2* __restrict__ blocks) {
     __shared__ AdjStep sA;
@@ -763,7 +790,7 @@ k_rev_mass_momentum_batch(const AdjStep* __restrict__ table, const int2* __restr
     }
     #pragma unroll
     for (int k = 0; k < ADJ_ITER; ++k)
-        rev_mass_momentum_at(sA, (bm.y * ADJ_ITER + k) * PART_THREADS + threadIdx.x, x[k], y[k]);
+        rev_mass_momentum_at<REINIT>(sA, (bm.y * ADJ_ITER + k) * PART_THREADS + threadIdx.x, x[k], y[k]);
 }
 
 __global__ void k_copy_f32(const __grid_constant__ CopyJob j) {
@@ -791,6 +818,7 @@ __global__ void k_adj_table(const AdjStep* __restrict__ bases, int n, int t,
     const size_t op = (size_t)t * a.sp, on = (size_t)t * a.sn, oc = (size_t)t * a.sc;
     a.x += op; a.y += op; a.vx += op; a.vy += op;
     a.sxx += op; a.syy += op; a.szz += op; a.sxy += op; a.rho += op;
+    if (a.vol) a.vol += op;
     a.cflag += oc;
     a.nm += on; a.nvax += on; a.nvay += on; a.nvbx += on; a.nvby += on; a.nax += on; a.nay += on;
     a.step += t;
@@ -802,34 +830,67 @@ inline int blocks_for(int n, int t) { return (n + t - 1) / t; }
 }  // namespace
 
 namespace {
-template <bool USL>
-void rev_forces(const AdjStep& A, bool trac, int pb, cudaStream_t s) {
-    if (trac) k_rev_forces<USL, true><<<pb, PART_THREADS, 0, s>>>(A);
-    else k_rev_forces<USL, false><<<pb, PART_THREADS, 0, s>>>(A);
+
+// The particle passes of one reverse step for a configuration: `Single`
+// launches take the step arguments, batched ones the table and block map.
+template <bool USL, bool TRAC, bool REINIT>
+void rev_particles(const AdjStep& A, int pb, bool first, cudaStream_t s) {
+    if (first) {
+        if (USL) k_rev_stress_usl<REINIT><<<pb, PART_THREADS, 0, s>>>(A);
+    } else {
+        k_rev_forces<USL, TRAC, REINIT><<<pb, PART_THREADS, 0, s>>>(A);
+    }
 }
-template <bool USL>
-void rev_forces_batch(const AdjStep* table, bool trac, const int2* pbk, int npb, cudaStream_t s) {
-    if (trac) k_rev_forces_batch<USL, true><<<npb, PART_THREADS, 0, s>>>(table, pbk);
-    else k_rev_forces_batch<USL, false><<<npb, PART_THREADS, 0, s>>>(table, pbk);
+template <bool USL, bool TRAC, bool REINIT>
+void rev_particles_batch(const AdjStep* table, const int2* pbk, int npb, bool first, cudaStream_t s) {
+    if (first) {
+        if (USL) k_rev_stress_usl_batch<REINIT><<<npb, PART_THREADS, 0, s>>>(table, pbk);
+    } else {
+        k_rev_forces_batch<USL, TRAC, REINIT><<<npb, PART_THREADS, 0, s>>>(table, pbk);
+    }
+}
+// first: pass U (USL only); else pass 2
+void rev_part(const AdjStep& A, bool usl, bool trac, bool reinit, int pb, bool first, cudaStream_t s) {
+    if (usl) {
+        if (trac) reinit ? rev_particles<true, true, true>(A, pb, first, s) : rev_particles<true, true, false>(A, pb, first, s);
+        else reinit ? rev_particles<true, false, true>(A, pb, first, s) : rev_particles<true, false, false>(A, pb, first, s);
+    } else {
+        if (trac) reinit ? rev_particles<false, true, true>(A, pb, first, s) : rev_particles<false, true, false>(A, pb, first, s);
+        else reinit ? rev_particles<false, false, true>(A, pb, first, s) : rev_particles<false, false, false>(A, pb, first, s);
+    }
+}
+void rev_part_batch(const AdjStep* t, bool usl, bool trac, bool reinit, const int2* pbk, int npb, bool first,
+                    cudaStream_t s) {
+    if (usl) {
+        if (trac) reinit ? rev_particles_batch<true, true, true>(t, pbk, npb, first, s) : rev_particles_batch<true, true, false>(t, pbk, npb, first, s);
+        else reinit ? rev_particles_batch<true, false, true>(t, pbk, npb, first, s) : rev_particles_batch<true, false, false>(t, pbk, npb, first, s);
+    } else {
+        if (trac) reinit ? rev_particles_batch<false, true, true>(t, pbk, npb, first, s) : rev_particles_batch<false, true, false>(t, pbk, npb, first, s);
+        else reinit ? rev_particles_batch<false, false, true>(t, pbk, npb, first, s) : rev_particles_batch<false, false, false>(t, pbk, npb, first, s);
+    }
 }
 }  // namespace
 
 cudaError_t launch_rev_step(const AdjStep& A, bool usl, bool trac, const int4* tiles, int ntiles,
                             cudaStream_t s) {
     const int pb = A.np > 0 ? blocks_for(A.np, PART_THREADS) : 0;
+    const bool reinit = A.reinit != 0;
     if (A.pvc && pb) k_rev_pvc<<<pb, PART_THREADS, 0, s>>>(A);
     if (usl) {
-        if (pb) k_rev_stress_usl<<<pb, PART_THREADS, 0, s>>>(A);
+        if (pb) rev_part(A, usl, trac, reinit, pb, true, s);
         if (ntiles > 0) k_rev_nodal_kinematics<RK_GATHER><<<ntiles, TILE_THREADS, 0, s>>>(A, tiles);
         if (ntiles > 0) k_rev_nodal_update<true><<<ntiles, TILE_THREADS, 0, s>>>(A, tiles);
-        if (pb) rev_forces<true>(A, trac, pb, s);
+        if (pb) rev_part(A, usl, trac, reinit, pb, false, s);
         if (ntiles > 0) k_rev_nodal_kinematics<RK_NODES><<<ntiles, TILE_THREADS, 0, s>>>(A, tiles);
     } else {
         if (ntiles > 0) k_rev_nodal_update<false><<<ntiles, TILE_THREADS, 0, s>>>(A, tiles);
-        if (pb) rev_forces<false>(A, trac, pb, s);
+        if (pb) rev_part(A, usl, trac, reinit, pb, false, s);
         if (ntiles > 0) k_rev_nodal_kinematics<RK_USF><<<ntiles, TILE_THREADS, 0, s>>>(A, tiles);
     }
-    if (pb) k_rev_mass_momentum<<<pb, PART_THREADS, 0, s>>>(A);
+    if (pb) {
+        if (reinit) k_rev_mass_momentum<true><<<pb, PART_THREADS, 0, s>>>(A);
+        else k_rev_mass_momentum<false><<<pb, PART_THREADS, 0, s>>>(A);
+    }
     return cudaGetLastError();
 }
 
@@ -838,22 +899,26 @@ cudaError_t launch_adj_table(const AdjStep* bases, int n, int t, AdjStep* table,
     return cudaGetLastError();
 }
 
-cudaError_t launch_rev_batch(const AdjStep* table, bool usl, bool trac, bool pvc, const int4* tiles,
-                             int ntiles, const int2* part_blocks, int n_part_blocks, cudaStream_t s) {
+cudaError_t launch_rev_batch(const AdjStep* table, bool usl, bool trac, bool pvc, bool reinit,
+                             const int4* tiles, int ntiles, const int2* part_blocks, int n_part_blocks,
+                             cudaStream_t s) {
     const int nt = ntiles, npb = n_part_blocks;
     if (pvc && npb > 0) k_rev_pvc_batch<<<npb, PART_THREADS, 0, s>>>(table, part_blocks);
     if (usl) {
-        if (npb > 0) k_rev_stress_usl_batch<<<npb, PART_THREADS, 0, s>>>(table, part_blocks);
+        if (npb > 0) rev_part_batch(table, usl, trac, reinit, part_blocks, npb, true, s);
         if (nt > 0) k_rev_nodal_kinematics_batch<RK_GATHER><<<nt, TILE_THREADS, 0, s>>>(table, tiles);
         if (nt > 0) k_rev_nodal_update_batch<true><<<nt, TILE_THREADS, 0, s>>>(table, tiles);
-        if (npb > 0) rev_forces_batch<true>(table, trac, part_blocks, npb, s);
+        if (npb > 0) rev_part_batch(table, usl, trac, reinit, part_blocks, npb, false, s);
         if (nt > 0) k_rev_nodal_kinematics_batch<RK_NODES><<<nt, TILE_THREADS, 0, s>>>(table, tiles);
     } else {
         if (nt > 0) k_rev_nodal_update_batch<false><<<nt, TILE_THREADS, 0, s>>>(table, tiles);
-        if (npb > 0) rev_forces_batch<false>(table, trac, part_blocks, npb, s);
+        if (npb > 0) rev_part_batch(table, usl, trac, reinit, part_blocks, npb, false, s);
         if (nt > 0) k_rev_nodal_kinematics_batch<RK_USF><<<nt, TILE_THREADS, 0, s>>>(table, tiles);
     }
-    if (npb > 0) k_rev_mass_momentum_batch<<<npb, PART_THREADS, 0, s>>>(table, part_blocks);
+    if (npb > 0) {
+        if (reinit) k_rev_mass_momentum_batch<true><<<npb, PART_THREADS, 0, s>>>(table, part_blocks);
+        else k_rev_mass_momentum_batch<false><<<npb, PART_THREADS, 0, s>>>(table, part_blocks);
+    }
     return cudaGetLastError();
 }
 

@@ -288,9 +288,50 @@ def test_adjoint_with_particle_velocity_constraints(built, scheme):
         assert abs(gd - fd) <= tol * max(abs(fd), 1e-12), (name, gd, fd)
 
 
+@pytest.mark.parametrize("scheme", ["usf", "usl"])
+def test_adjoint_solve_semantics(built, scheme):
+    """solve semantics (no per-step volume set-up: constant mass, the volume
+    carried from step to step): directional derivatives in E, x_0 and v_0
+    against central differences of the float64 oracle stepped the same way."""
+    dt = 1e-3 if scheme == "usf" else 2.5e-4
+    kw = dict(n=16, sim_steps=24, dt=dt, velocity=sheared, scheme=scheme)
+    gs, g, info = workloads.differentiation(D, **kw)
+    sim = gs.simulation(g, reinit=False)
+    gs._upload(sim)
+    sim.initialize()
+    n = info["np"]
+    W, U = seeds(n, 31)
+    sim.record(kw["sim_steps"], 10)
+    got = sim.adjoint(W, U)
+    sim.close()
+    E0 = info["E"]
+    rng = np.random.Generator(np.random.PCG64(37))
+
+    def loss(E=None, dx=None, dv=None):
+        o, og, _ = workloads.differentiation(O, dtype=np.float64, E=E0 if E is None else E, **kw)
+        p = o.mesh.particles[0]
+        if dx is not None:
+            p.loc[:] = p.loc + dx.reshape(-1, 1, 2)
+        if dv is not None:
+            p.velocity[:] = p.velocity + dv.reshape(-1, 1, 2)
+        for i in range(kw["sim_steps"]):
+            o.step(i, og, reinit=False)
+        return float((p.loc.reshape(-1, 2) * W).sum() + (p.velocity.reshape(-1, 2) * U).sum())
+
+    for name, h, perturb, grad in (
+            ("youngs_modulus", 1e-4, lambda u, s_: dict(E=E0 * (1 + s_ * u)), lambda u: (got["youngs_modulus"] * E0 * u).sum()),
+            ("loc", 1e-7, lambda u, s_: dict(dx=s_ * u), lambda u: (got["loc"].reshape(-1) * u).sum()),
+            ("velocity", 1e-6, lambda u, s_: dict(dv=s_ * u), lambda u: (got["velocity"].reshape(-1) * u).sum())):
+        u = rng.normal(size=n if name == "youngs_modulus" else 2 * n)
+        fd = (loss(**perturb(u, h)) - loss(**perturb(u, -h))) / (2 * h)
+        gd = float(grad(u))
+        tol = 2e-3 if name == "youngs_modulus" else 5e-3
+        assert abs(gd - fd) <= tol * max(abs(fd), 1e-12), (name, gd, fd)
+
+
 def test_adjoint_rejects_unsupported(built):
-    gs, g, info = workloads.plain_scaleup(D, n=16, sim_steps=2)
-    sim = gs.simulation(g, reinit=False)     # solve semantics: not differentiated
+    gs, g, info = workloads.mixed_large(D, n=16, sim_steps=2)
+    sim = gs.simulation(g, reinit=True)     # Newtonian: not differentiated
     gs._upload(sim)
     sim.initialize()
     with pytest.raises(D.MpmError) as e:
