@@ -40,7 +40,7 @@ namespace mpm {
 
 namespace {
 
-constexpr int NLAM = 11;   // adjoint arrays: x y vx vy sxx syy szz sxy rho E vol
+constexpr int NLAM = 12;   // adjoint arrays: x y vx vy sxx syy szz sxy rho E vol vsc
 constexpr int NTP = 9;     // tape per particle: x y vx vy sxx syy szz sxy rho
 constexpr int NTN = 7;     // tape per node: m vAx vAy vBx vBy aBx aBy
 constexpr int NPS = 5;     // per-particle scratch: r0b r1b r3b c0b c1b
@@ -72,6 +72,7 @@ struct AdjointState {
     int tape_slots = 0;
     float* tp[NTP] = {};
     float* tvol = nullptr;     // volume at each step start (solve semantics only)
+    float* tvsc = nullptr;     // centroid volumetric strain at each step start (Newtonian only)
     uint8_t* tflag = nullptr;
     float* tn[NTN] = {};
     std::vector<Epoch> epochs;
@@ -128,6 +129,8 @@ void free_buffers(MpmHandle* h, AdjointState* a) {
     for (float*& p : a->tn) { dfree(h, p); p = nullptr; }
     dfree(h, a->tvol);
     a->tvol = nullptr;
+    dfree(h, a->tvsc);
+    a->tvsc = nullptr;
     dfree(h, a->tflag);
     a->tflag = nullptr;
     a->tape_slots = 0;
@@ -185,17 +188,22 @@ int restore_checkpoint(MpmHandle* h, Checkpoint& c, cudaStream_t s) {
 
 int ensure_adjoint_buffers(MpmHandle* h, AdjointState* a, int slots, cudaStream_t s) {
     const size_t np = (size_t)h->np, nn = (size_t)h->nn;
-    if (a->tape_slots < slots || (!h->reinit && !a->tvol)) {
+    bool newtonian = false;
+    for (const MatDev& m : h->mats) newtonian = newtonian || m.type == MAT_NEWTONIAN;
+    if (a->tape_slots < slots || (!h->reinit && !a->tvol) || (newtonian && !a->tvsc)) {
         drop_adj_graphs(a);
         for (float*& p : a->tp) { dfree(h, p); p = nullptr; }
         dfree(h, a->tvol);
         a->tvol = nullptr;
+        dfree(h, a->tvsc);
+        a->tvsc = nullptr;
         for (float*& p : a->tn) { dfree(h, p); p = nullptr; }
         dfree(h, a->tflag);
         a->tflag = nullptr;
         a->tape_slots = 0;
         for (float*& p : a->tp) TRY(dalloc(h, &p, np * slots));
         if (!h->reinit) TRY(dalloc(h, &a->tvol, np * slots));
+        if (newtonian) TRY(dalloc(h, &a->tvsc, np * slots));
         for (float*& p : a->tn) TRY(dalloc(h, &p, nn * slots));
         TRY(dalloc(h, &a->tflag, (size_t)h->ncell * slots));
         a->tape_slots = slots;
@@ -288,6 +296,7 @@ void tape_particle_segments(MpmHandle* h, AdjointState* a, int par, std::vector<
                              p.sxy[par], p.rho[par]};
     for (int k = 0; k < NTP; ++k) add_seg(v, src[k], a->tp[k], sizeof(float) * np, sizeof(float) * np);
     if (!h->reinit) add_seg(v, p.vol[par], a->tvol, sizeof(float) * np, sizeof(float) * np);
+    if (a->tvsc) add_seg(v, p.vsc[par], a->tvsc, sizeof(float) * np, sizeof(float) * np);
     add_seg(v, h->cflag, a->tflag, (size_t)h->ncell, (size_t)h->ncell);
 }
 
@@ -477,6 +486,7 @@ AdjStep base_args(MpmHandle* h, AdjointState* a, int epoch) {
     A.vol = h->reinit ? nullptr : a->tvol;
     A.mass = h->reinit ? nullptr : ep.mass;
     A.psize = h->reinit ? nullptr : ep.psize;
+    A.vsc = a->tvsc;
     A.fn_off = h->d_fn_off;
     A.fn_x = h->d_fn_x;
     A.fn_y = h->d_fn_y;
@@ -487,7 +497,7 @@ AdjStep base_args(MpmHandle* h, AdjointState* a, int epoch) {
     const float** tn[NTN] = {&A.nm, &A.nvax, &A.nvay, &A.nvbx, &A.nvby, &A.nax, &A.nay};
     for (int k = 0; k < NTN; ++k) *tn[k] = a->tn[k];
     float** lam[NLAM] = {&A.lx, &A.ly, &A.lvx, &A.lvy, &A.lsxx, &A.lsyy, &A.lszz, &A.lsxy,
-                         &A.lrho, &A.lE, &A.lvol};
+                         &A.lrho, &A.lE, &A.lvol, &A.lvsc};
     for (int k = 0; k < NLAM; ++k) *lam[k] = a->lam[k];
     float** ps[NPS] = {&A.r0b, &A.r1b, &A.r3b, &A.c0b, &A.c1b};
     for (int k = 0; k < NPS; ++k) *ps[k] = a->pscr[k];
@@ -506,6 +516,7 @@ int reverse_step(MpmHandle* h, AdjointState* a, int t, cudaStream_t s) {
     A.x += op; A.y += op; A.vx += op; A.vy += op;
     A.sxx += op; A.syy += op; A.szz += op; A.sxy += op; A.rho += op;
     if (A.vol) A.vol += op;
+    if (A.vsc) A.vsc += op;
     A.cflag += oc;
     A.nm += on; A.nvax += on; A.nvay += on; A.nvbx += on; A.nvby += on; A.nax += on; A.nay += on;
     A.step += t;
@@ -564,9 +575,6 @@ int emit_all(MpmHandle* h, AdjointState* a, float* dl_dE, float* dl_dloc0, float
 
 int check_supported(MpmHandle* h) {
     if (h->ndim != 2) return fail(h, MPM_ERR_UNSUPPORTED, "the adjoint implements Quadrilateral4Node meshes");
-    for (const MatDev& m : h->mats)
-        if (m.type == MAT_NEWTONIAN)
-            return fail(h, MPM_ERR_UNSUPPORTED, "the adjoint covers LinearElastic and SimpleMaterial");
     return MPM_OK;
 }
 
@@ -872,8 +880,11 @@ int mpm_batch_adjoint(MpmBatch* b, const float* const* dl_dloc, const float* con
     }
     x->bases.assign(n, AdjStep{});
     std::vector<int> cur(n, -1);   // epoch whose pointers bases[i] holds
-    bool any_pvc = false;
-    for (MpmHandle* h : b->sims) any_pvc = any_pvc || h->has_pvc;
+    bool any_pvc = false, any_newt = false;
+    for (MpmHandle* h : b->sims) {
+        any_pvc = any_pvc || h->has_pvc;
+        any_newt = any_newt || h->adj->tvsc != nullptr;
+    }
     for (int seg = nseg - 1; seg >= 0 && r == MPM_OK; --seg) {
         const int len = (int)std::min<int64_t>(K, nsteps - (int64_t)seg * K);
         r = batch_recompute(b, x, seg, len, s);
@@ -903,7 +914,7 @@ int mpm_batch_adjoint(MpmBatch* b, const float* const* dl_dloc, const float* con
             if (r != MPM_OK) break;
             BCK(b, launch_adj_table(x->d_bases, n, t, x->d_table, s));
             BCK(b, launch_rev_batch(x->d_table, b->cfg.usl, b->cfg.traction, any_pvc, b->cfg.reinit,
-                                    b->d_tiles, b->ntiles, x->part_blocks, x->n_part_blocks, s));
+                                    any_newt, b->d_tiles, b->ntiles, x->part_blocks, x->n_part_blocks, s));
         }
         for (int i = 0; i < n && r == MPM_OK; ++i) {
             MpmHandle* h = b->sims[i];

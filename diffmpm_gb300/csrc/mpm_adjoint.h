@@ -72,6 +72,10 @@ struct AdjStep {
     int reinit;
     const float *vol, *mass, *psize;
     float* lvol;
+    // centroid volumetric strain at the step start (tape; null unless a
+    // material reads it: Newtonian) and its adjoint
+    const float* vsc;
+    float* lvsc;
     const int* fn_off;
     const float *fn_x, *fn_y;
     int step;
@@ -94,7 +98,8 @@ constexpr int ADJ_BLOCK = 256;
 constexpr int ADJ_ITER = 4;
 cudaError_t launch_adj_table(const AdjStep* bases, int n, int t, AdjStep* table, cudaStream_t s);
 // `pvc`: some simulation of the batch has particle velocity constraints.
-cudaError_t launch_rev_batch(const AdjStep* table, bool usl, bool trac, bool pvc, bool reinit,
+// `newt`: some simulation of the batch has Newtonian particles.
+cudaError_t launch_rev_batch(const AdjStep* table, bool usl, bool trac, bool pvc, bool reinit, bool newt,
                              const int4* tiles, int ntiles, const int2* part_blocks, int n_part_blocks,
                              cudaStream_t s);
 

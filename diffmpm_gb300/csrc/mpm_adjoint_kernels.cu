@@ -302,14 +302,35 @@ __device__ __forceinline__ void rates_at(const int ids[4], const float Gx[4], co
     c1 = flush(c1);
 }
 
-// Reverse of sig' = sig + D(E) r dt for the stress adjoint sb: the strain-rate
-// adjoints (zero where the forward flushed the rate) and dL/dE.
+// Reverse of the stress update for the stress adjoint sb: the strain-rate
+// adjoints (zero where the forward flushed the rate), dL/dE, the adjoint of
+// the updated centroid volumetric strain (vscb) and whether the update is a
+// total stress (the start-of-step stress then passes no adjoint).
+//   LinearElastic, SimpleMaterial: sig' = sig + D(E) r dt;
+//   Newtonian (the build's definition): sig' = K vsc' I + 2 mu dev(r) with
+//   r_zz = 0, s_xy = mu r_xy (material.py has no Newtonian).
+template <bool NEWT>   // NEWT: the run has Newtonian particles
 __device__ __forceinline__ void stress_reverse(const MatDev& mat, float Ep, float dt, float r0, float r1,
                                                float r3, float sbxx, float sbyy, float sbzz, float sbxy,
-                                               float& r0b, float& r1b, float& r3b, float& Eb) {
+                                               float& r0b, float& r1b, float& r3b, float& Eb,
+                                               float& vscb, bool& total) {
     const float d0 = fm(r0, dt), d1 = fm(r1, dt), d3 = fm(r3, dt);
     float d0b = 0.0f, d1b = 0.0f, d3b = 0.0f;
     Eb = 0.0f;
+    vscb = 0.0f;
+    total = false;
+    if (NEWT && mat.type == MAT_NEWTONIAN) {
+        const float tr = fa(fa(sbxx, sbyy), sbzz);
+        const float t3b = -fm(mat.twomu, tr);              // t3 = (r0 + r1) / 3
+        vscb = fm(mat.K, tr);                              // kv = K vsc'
+        const float r0n = fa(fm(mat.twomu, sbxx), fdv(t3b, 3.0f));
+        const float r1n = fa(fm(mat.twomu, sbyy), fdv(t3b, 3.0f));
+        r0b = r0 != 0.0f ? r0n : 0.0f;
+        r1b = r1 != 0.0f ? r1n : 0.0f;
+        r3b = r3 != 0.0f ? fm(mat.mu, sbxy) : 0.0f;
+        total = true;
+        return;
+    }
     if (mat.type == MAT_LINEAR_ELASTIC) {
         float a1 = mat.a1, a2 = mat.a2, G = mat.G;
         if (Ep >= 0.0f) {
@@ -368,7 +389,7 @@ k_rev_pvc_batch(const AdjStep* __restrict__ table, const int2* __restrict__ bloc
 // adjoints go to pass G (their transposed gather) and to pass 2 (their
 // position terms); the density adjoint becomes that of the step start.
 // ---------------------------------------------------------------------------
-template <bool REINIT>
+template <bool REINIT, bool NEWT>
 __device__ __forceinline__ void rev_stress_usl_at(const AdjStep& A, int q, float x, float y) {
     if (q >= A.np) return;
     int ci, cj;
@@ -386,11 +407,23 @@ __device__ __forceinline__ void rev_stress_usl_at(const AdjStep& A, int q, float
     const float rho1 = fdv(A.rho[q], f);
     const MatDev& mat = A.mats[A.mat[q]];
     const float Ep = A.E ? A.E[q] : -1.0f;
-    float r0b, r1b, r3b, Eb;
-    stress_reverse(mat, Ep, A.dt, r0, r1, r3, A.lsxx[q], A.lsyy[q], A.lszz[q], A.lsxy[q], r0b, r1b,
-                   r3b, Eb);
+    float r0b, r1b, r3b, Eb, vscb;
+    bool total;
+    stress_reverse<NEWT>(mat, Ep, A.dt, r0, r1, r3, A.lsxx[q], A.lsyy[q], A.lszz[q], A.lsxy[q], r0b,
+                         r1b, r3b, Eb, vscb, total);
+    if (total) {   // the start-of-step stress passes no adjoint (pass 2 adds the forces')
+        A.lsxx[q] = 0.0f;
+        A.lsyy[q] = 0.0f;
+        A.lszz[q] = 0.0f;
+        A.lsxy[q] = 0.0f;
+    }
     const float lrho = A.lrho[q];
     float fb = -fdv(fm(lrho, rho1), f);
+    if (NEWT) {   // vsc' = vsc + dvol (only Newtonian stress reads vsc; else its adjoint is 0)
+        const float lvsc = fa(A.lvsc[q], vscb);
+        A.lvsc[q] = lvsc;
+        fb = fa(fb, lvsc);
+    }
     if (!REINIT) {   // solve semantics: V' = V f carries the volume to the next step
         const float lv = A.lvol[q];
         fb = fa(fb, fm(lv, A.vol[q]));
@@ -405,14 +438,14 @@ __device__ __forceinline__ void rev_stress_usl_at(const AdjStep& A, int q, float
     A.lE[q] = fa(A.lE[q], Eb);
 }
 
-template <bool REINIT>
+template <bool REINIT, bool NEWT>
 __global__ void __launch_bounds__(PART_THREADS)
 k_rev_stress_usl(const __grid_constant__ AdjStep A) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q < A.np) rev_stress_usl_at<REINIT>(A, q, A.x[q], A.y[q]);
+    if (q < A.np) rev_stress_usl_at<REINIT, NEWT>(A, q, A.x[q], A.y[q]);
 }
 
-template <bool REINIT>
+template <bool REINIT, bool NEWT>
 __global__ void __launch_bounds__(PART_THREADS)
 k_rev_stress_usl_batch(const AdjStep* __restrict__ table, const int2* __restrict__ blocks) {
     __shared__ AdjStep sA;
@@ -421,7 +454,7 @@ k_rev_stress_usl_batch(const AdjStep* __restrict__ table, const int2* __restrict
     #pragma unroll 1
     for (int k = 0; k < ADJ_ITER; ++k) {
         const int q = (bm.y * ADJ_ITER + k) * PART_THREADS + threadIdx.x;
-        if (q < sA.np) rev_stress_usl_at<REINIT>(sA, q, sA.x[q], sA.y[q]);
+        if (q < sA.np) rev_stress_usl_at<REINIT, NEWT>(sA, q, sA.x[q], sA.y[q]);
     }
 }
 
@@ -432,7 +465,7 @@ k_rev_stress_usl_batch(const AdjStep* __restrict__ table, const int2* __restrict
 // reset volume V0; the strain-rate adjoints of its later stress update come
 // from pass U and only add their position terms here.
 // ---------------------------------------------------------------------------
-template <bool USL, bool TRAC, bool REINIT>
+template <bool USL, bool TRAC, bool REINIT, bool NEWT>
 __device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q, float x, float y) {
     if (q >= A.np) return;
     int ci, cj;
@@ -466,6 +499,7 @@ __device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q, float x, 
     p.szz = A.szz[q];
     p.sxy = A.sxy[q];
     p.rho = rho0;
+    p.vsc = NEWT ? A.vsc[q] : 0.0f;   // taped when a material uses it (Newtonian)
     float f = 1.0f, V = V0;
     const MatDev& mat = A.mats[A.mat[q]];
     const float Ep = A.E ? A.E[q] : -1.0f;
@@ -538,10 +572,10 @@ __device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q, float x, 
         yb = fa(yb, fm(Nb, Gy[k]));
     }
     // stress adjoint: loss/next-step part (through pass U for USL) + force part
-    const float sbxx = fs(A.lsxx[q], fm(V, fsxx));
-    const float sbyy = fs(A.lsyy[q], fm(V, fsyy));
-    const float sbzz = A.lszz[q];
-    const float sbxy = fs(A.lsxy[q], fm(V, fsxy));
+    float sbxx = fs(A.lsxx[q], fm(V, fsxx));
+    float sbyy = fs(A.lsyy[q], fm(V, fsyy));
+    float sbzz = A.lszz[q];
+    float sbxy = fs(A.lsxy[q], fm(V, fsxy));
 
     float r0b, r1b, r3b, rhob;
     if (USL) {
@@ -551,13 +585,22 @@ __device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q, float x, 
         rhob = REINIT ? fa(A.lrho[q], fm(V0, mb)) : A.lrho[q];
         if (!REINIT) A.lvol[q] = fa(A.lvol[q], Vb);   // the forces used the start volume
     } else {
-        float Eb;
-        stress_reverse(mat, Ep, A.dt, r0, r1, r3, sbxx, sbyy, sbzz, sbxy, r0b, r1b, r3b, Eb);
-        // reverse of V = V0 (1 + dvol), rho' = rho / (1 + dvol), m = V0 rho
-        // (solve semantics: m is constant and V also carries to the next step)
+        float Eb, vscb;
+        bool total;
+        stress_reverse<NEWT>(mat, Ep, A.dt, r0, r1, r3, sbxx, sbyy, sbzz, sbxy, r0b, r1b, r3b, Eb, vscb,
+                             total);
+        if (total) sbxx = sbyy = sbzz = sbxy = 0.0f;   // total stress: no adjoint to the start
+        // reverse of V = V0 (1 + dvol), rho' = rho / (1 + dvol), m = V0 rho,
+        // vsc' = vsc + dvol (solve semantics: m is constant and V also
+        // carries to the next step)
         const float lrho = A.lrho[q];
         const float Vt = REINIT ? Vb : fa(Vb, A.lvol[q]);
-        const float fb = fs(fm(Vt, V0), fdv(fm(lrho, p.rho), f));
+        float fb = fs(fm(Vt, V0), fdv(fm(lrho, p.rho), f));
+        if (NEWT) {   // only Newtonian stress reads vsc; otherwise its adjoint is 0
+            const float lvsc = fa(A.lvsc[q], vscb);
+            A.lvsc[q] = lvsc;
+            fb = fa(fb, lvsc);
+        }
         rhob = REINIT ? fa(fdv(lrho, f), fm(V0, mb)) : fdv(lrho, f);
         if (!REINIT) A.lvol[q] = fm(Vt, f);
         A.lE[q] = fa(A.lE[q], Eb);
@@ -585,14 +628,14 @@ __device__ __forceinline__ void rev_forces_at(const AdjStep& A, int q, float x, 
     A.lrho[q] = rhob;
 }
 
-template <bool USL, bool TRAC, bool REINIT>
+template <bool USL, bool TRAC, bool REINIT, bool NEWT>
 __global__ void __launch_bounds__(PART_THREADS, 4)
 k_rev_forces(const __grid_constant__ AdjStep A) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q < A.np) rev_forces_at<USL, TRAC, REINIT>(A, q, A.x[q], A.y[q]);
+    if (q < A.np) rev_forces_at<USL, TRAC, REINIT, NEWT>(A, q, A.x[q], A.y[q]);
 }
 
-template <bool USL, bool TRAC, bool REINIT>
+template <bool USL, bool TRAC, bool REINIT, bool NEWT>
 __global__ void __launch_bounds__(PART_THREADS, 4)
 k_rev_forces_batch(const AdjStep* __restrict__ table, const int2* __restrict__ blocks) {
     __shared__ AdjStep sA;
@@ -601,7 +644,7 @@ k_rev_forces_batch(const AdjStep* __restrict__ table, const int2* __restrict__ b
     #pragma unroll 1
     for (int k = 0; k < ADJ_ITER; ++k) {
         const int q = (bm.y * ADJ_ITER + k) * PART_THREADS + threadIdx.x;
-        if (q < sA.np) rev_forces_at<USL, TRAC, REINIT>(sA, q, sA.x[q], sA.y[q]);
+        if (q < sA.np) rev_forces_at<USL, TRAC, REINIT, NEWT>(sA, q, sA.x[q], sA.y[q]);
     }
 }
 
@@ -819,6 +862,7 @@ __global__ void k_adj_table(const AdjStep* __restrict__ bases, int n, int t,
     a.x += op; a.y += op; a.vx += op; a.vy += op;
     a.sxx += op; a.syy += op; a.szz += op; a.sxy += op; a.rho += op;
     if (a.vol) a.vol += op;
+    if (a.vsc) a.vsc += op;
     a.cflag += oc;
     a.nm += on; a.nvax += on; a.nvay += on; a.nvbx += on; a.nvby += on; a.nax += on; a.nay += on;
     a.step += t;
@@ -831,43 +875,46 @@ inline int blocks_for(int n, int t) { return (n + t - 1) / t; }
 
 namespace {
 
-// The particle passes of one reverse step for a configuration: `Single`
-// launches take the step arguments, batched ones the table and block map.
-template <bool USL, bool TRAC, bool REINIT>
-void rev_particles(const AdjStep& A, int pb, bool first, cudaStream_t s) {
-    if (first) {
-        if (USL) k_rev_stress_usl<REINIT><<<pb, PART_THREADS, 0, s>>>(A);
+// The particle passes of one reverse step for a configuration: pass U (USL,
+// `first`) or pass 2, single-simulation and batched launches.
+template <bool USL, bool TRAC, bool REINIT, bool NEWT>
+void rev_particles(const AdjStep& A, const AdjStep* table, const int2* pbk, int nb, bool first,
+                   cudaStream_t s) {
+    if (table) {
+        if (first) {
+            if (USL) k_rev_stress_usl_batch<REINIT, NEWT><<<nb, PART_THREADS, 0, s>>>(table, pbk);
+        } else {
+            k_rev_forces_batch<USL, TRAC, REINIT, NEWT><<<nb, PART_THREADS, 0, s>>>(table, pbk);
+        }
     } else {
-        k_rev_forces<USL, TRAC, REINIT><<<pb, PART_THREADS, 0, s>>>(A);
+        if (first) {
+            if (USL) k_rev_stress_usl<REINIT, NEWT><<<nb, PART_THREADS, 0, s>>>(A);
+        } else {
+            k_rev_forces<USL, TRAC, REINIT, NEWT><<<nb, PART_THREADS, 0, s>>>(A);
+        }
     }
 }
-template <bool USL, bool TRAC, bool REINIT>
-void rev_particles_batch(const AdjStep* table, const int2* pbk, int npb, bool first, cudaStream_t s) {
-    if (first) {
-        if (USL) k_rev_stress_usl_batch<REINIT><<<npb, PART_THREADS, 0, s>>>(table, pbk);
-    } else {
-        k_rev_forces_batch<USL, TRAC, REINIT><<<npb, PART_THREADS, 0, s>>>(table, pbk);
-    }
+
+using RevParticlesFn = void (*)(const AdjStep&, const AdjStep*, const int2*, int, bool, cudaStream_t);
+#define MPM_REV(u, t, r) rev_particles<u, t, r, false>, rev_particles<u, t, r, true>
+constexpr RevParticlesFn kRevParticles[16] = {
+    MPM_REV(false, false, false), MPM_REV(false, false, true), MPM_REV(false, true, false),
+    MPM_REV(false, true, true),   MPM_REV(true, false, false), MPM_REV(true, false, true),
+    MPM_REV(true, true, false),   MPM_REV(true, true, true)};
+#undef MPM_REV
+
+struct RevConfig {
+    bool usl, trac, reinit, newt;
+    RevParticlesFn fn() const { return kRevParticles[usl * 8 + trac * 4 + reinit * 2 + newt]; }
+};
+
+void rev_part(const AdjStep& A, const RevConfig& c, int pb, bool first, cudaStream_t s) {
+    c.fn()(A, nullptr, nullptr, pb, first, s);
 }
-// first: pass U (USL only); else pass 2
-void rev_part(const AdjStep& A, bool usl, bool trac, bool reinit, int pb, bool first, cudaStream_t s) {
-    if (usl) {
-        if (trac) reinit ? rev_particles<true, true, true>(A, pb, first, s) : rev_particles<true, true, false>(A, pb, first, s);
-        else reinit ? rev_particles<true, false, true>(A, pb, first, s) : rev_particles<true, false, false>(A, pb, first, s);
-    } else {
-        if (trac) reinit ? rev_particles<false, true, true>(A, pb, first, s) : rev_particles<false, true, false>(A, pb, first, s);
-        else reinit ? rev_particles<false, false, true>(A, pb, first, s) : rev_particles<false, false, false>(A, pb, first, s);
-    }
-}
-void rev_part_batch(const AdjStep* t, bool usl, bool trac, bool reinit, const int2* pbk, int npb, bool first,
+void rev_part_batch(const AdjStep* t, const RevConfig& c, const int2* pbk, int npb, bool first,
                     cudaStream_t s) {
-    if (usl) {
-        if (trac) reinit ? rev_particles_batch<true, true, true>(t, pbk, npb, first, s) : rev_particles_batch<true, true, false>(t, pbk, npb, first, s);
-        else reinit ? rev_particles_batch<true, false, true>(t, pbk, npb, first, s) : rev_particles_batch<true, false, false>(t, pbk, npb, first, s);
-    } else {
-        if (trac) reinit ? rev_particles_batch<false, true, true>(t, pbk, npb, first, s) : rev_particles_batch<false, true, false>(t, pbk, npb, first, s);
-        else reinit ? rev_particles_batch<false, false, true>(t, pbk, npb, first, s) : rev_particles_batch<false, false, false>(t, pbk, npb, first, s);
-    }
+    static const AdjStep unused{};   // the batched launches read the device table `t`
+    c.fn()(unused, t, pbk, npb, first, s);
 }
 }  // namespace
 
@@ -875,16 +922,17 @@ cudaError_t launch_rev_step(const AdjStep& A, bool usl, bool trac, const int4* t
                             cudaStream_t s) {
     const int pb = A.np > 0 ? blocks_for(A.np, PART_THREADS) : 0;
     const bool reinit = A.reinit != 0;
+    const RevConfig rc{usl, trac, reinit, A.vsc != nullptr};
     if (A.pvc && pb) k_rev_pvc<<<pb, PART_THREADS, 0, s>>>(A);
     if (usl) {
-        if (pb) rev_part(A, usl, trac, reinit, pb, true, s);
+        if (pb) rev_part(A, rc, pb, true, s);
         if (ntiles > 0) k_rev_nodal_kinematics<RK_GATHER><<<ntiles, TILE_THREADS, 0, s>>>(A, tiles);
         if (ntiles > 0) k_rev_nodal_update<true><<<ntiles, TILE_THREADS, 0, s>>>(A, tiles);
-        if (pb) rev_part(A, usl, trac, reinit, pb, false, s);
+        if (pb) rev_part(A, rc, pb, false, s);
         if (ntiles > 0) k_rev_nodal_kinematics<RK_NODES><<<ntiles, TILE_THREADS, 0, s>>>(A, tiles);
     } else {
         if (ntiles > 0) k_rev_nodal_update<false><<<ntiles, TILE_THREADS, 0, s>>>(A, tiles);
-        if (pb) rev_part(A, usl, trac, reinit, pb, false, s);
+        if (pb) rev_part(A, rc, pb, false, s);
         if (ntiles > 0) k_rev_nodal_kinematics<RK_USF><<<ntiles, TILE_THREADS, 0, s>>>(A, tiles);
     }
     if (pb) {
@@ -899,20 +947,21 @@ cudaError_t launch_adj_table(const AdjStep* bases, int n, int t, AdjStep* table,
     return cudaGetLastError();
 }
 
-cudaError_t launch_rev_batch(const AdjStep* table, bool usl, bool trac, bool pvc, bool reinit,
+cudaError_t launch_rev_batch(const AdjStep* table, bool usl, bool trac, bool pvc, bool reinit, bool newt,
                              const int4* tiles, int ntiles, const int2* part_blocks, int n_part_blocks,
                              cudaStream_t s) {
     const int nt = ntiles, npb = n_part_blocks;
+    const RevConfig rc{usl, trac, reinit, newt};
     if (pvc && npb > 0) k_rev_pvc_batch<<<npb, PART_THREADS, 0, s>>>(table, part_blocks);
     if (usl) {
-        if (npb > 0) rev_part_batch(table, usl, trac, reinit, part_blocks, npb, true, s);
+        if (npb > 0) rev_part_batch(table, rc, part_blocks, npb, true, s);
         if (nt > 0) k_rev_nodal_kinematics_batch<RK_GATHER><<<nt, TILE_THREADS, 0, s>>>(table, tiles);
         if (nt > 0) k_rev_nodal_update_batch<true><<<nt, TILE_THREADS, 0, s>>>(table, tiles);
-        if (npb > 0) rev_part_batch(table, usl, trac, reinit, part_blocks, npb, false, s);
+        if (npb > 0) rev_part_batch(table, rc, part_blocks, npb, false, s);
         if (nt > 0) k_rev_nodal_kinematics_batch<RK_NODES><<<nt, TILE_THREADS, 0, s>>>(table, tiles);
     } else {
         if (nt > 0) k_rev_nodal_update_batch<false><<<nt, TILE_THREADS, 0, s>>>(table, tiles);
-        if (npb > 0) rev_part_batch(table, usl, trac, reinit, part_blocks, npb, false, s);
+        if (npb > 0) rev_part_batch(table, rc, part_blocks, npb, false, s);
         if (nt > 0) k_rev_nodal_kinematics_batch<RK_USF><<<nt, TILE_THREADS, 0, s>>>(table, tiles);
     }
     if (npb > 0) {

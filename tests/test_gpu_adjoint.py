@@ -329,14 +329,9 @@ def test_adjoint_solve_semantics(built, scheme):
         assert abs(gd - fd) <= tol * max(abs(fd), 1e-12), (name, gd, fd)
 
 
-def test_adjoint_rejects_unsupported(built):
-    gs, g, info = workloads.mixed_large(D, n=16, sim_steps=2)
-    sim = gs.simulation(g, reinit=True)     # Newtonian: not differentiated
-    gs._upload(sim)
-    sim.initialize()
-    with pytest.raises(D.MpmError) as e:
-        sim.record(2, 1)
-    assert e.value.code == 5
+def test_adjoint_needs_a_current_recording(built):
+    """(Every 2-D configuration is differentiable; the 1-D refusals are in
+    test_gpu_line.py.)  The adjoint needs a recording that is still current."""
     gs, sim, g, info = gpu_sim()
     with pytest.raises(D.MpmError) as e:
         sim.adjoint(np.zeros((info["np"], 2), np.float32))
@@ -346,3 +341,65 @@ def test_adjoint_rejects_unsupported(built):
     with pytest.raises(D.MpmError) as e:
         sim.adjoint(np.zeros((info["np"], 2), np.float32))
     assert e.value.code == 6
+
+
+def mixed_newtonian(api, scheme, dtype=np.float32, E=None):
+    """16 x 16 mesh, Gauss-point particles over [0.1, 0.9] x [0, 0.6]: LinearElastic
+    (per-particle E) left of x = 0.5, Newtonian right of it, sheared initial
+    velocity, bottom fixed, gravity; USF at dt 1e-3 or USL at dt 2.5e-4, 24 steps."""
+    n, h = 16, 1.0 / 16
+    pts = workloads.gauss_points(2, 14, 0, 10, h)
+    mid = (pts[:, 0] >= 0.5).astype(np.int32)
+    mats = [api.LinearElastic({"density": 1000, "youngs_modulus": 1e6, "poisson_ratio": 0.3}),
+            api.Newtonian({"density": 1000, "bulk_modulus": 5e5, "dynamic_viscosity": 50.0})]
+    E0 = workloads.youngs_field(len(pts), 41) if E is None else E
+    bottom = workloads._node_ids(n, n, lambda i, j: j == 0)
+    cons = [(bottom, api.Constraint(0, 0.0)), (bottom, api.Constraint(1, 0.0))]
+    dk = {} if dtype == np.float32 else {"dtype": dtype}   # (the oracle's float64 runs)
+    el = api.Quadrilateral4Node((n, n), n * n, (h, h), cons, **dk)
+    ps = api.Particles(pts.reshape(-1, 1, 2), mats, np.zeros(len(pts), dtype=np.int32),
+                       material_ids=mid, youngs_modulus=E0, **dk)
+    ps.velocity[:] = sheared(pts).reshape(-1, 1, 2)
+    mesh = api.Mesh2D({"particles": [ps], "elements": el, "particle_surface_traction": []})
+    dt = 1e-3 if scheme == "usf" else 2.5e-4
+    solver = api.MPMExplicit(mesh, dt, scheme=scheme, sim_steps=24)
+    return solver, np.array([0.0, -9.81]), E0
+
+
+@pytest.mark.parametrize("scheme", ["usf", "usl"])
+def test_adjoint_newtonian_mixed(built, scheme):
+    """Elastic and Newtonian particles in one population (the Newtonian stress
+    is total: it reads the accumulated centroid volumetric strain, which the
+    adjoint then carries): directional derivatives in E, x_0 and v_0 against
+    central differences of the float64 oracle."""
+    gs, g, E0 = mixed_newtonian(D, scheme)
+    sim = gs.simulation(g, reinit=True)
+    gs._upload(sim)
+    sim.initialize()
+    n = len(E0)
+    W, U = seeds(n, 43)
+    sim.record(24, 10)
+    got = sim.adjoint(W, U)
+    sim.close()
+    rng = np.random.Generator(np.random.PCG64(47))
+
+    def loss(E=None, dx=None, dv=None):
+        o, og, _ = mixed_newtonian(O, scheme, dtype=np.float64, E=E0 if E is None else E)
+        p = o.mesh.particles[0]
+        if dx is not None:
+            p.loc[:] = p.loc + dx.reshape(-1, 1, 2)
+        if dv is not None:
+            p.velocity[:] = p.velocity + dv.reshape(-1, 1, 2)
+        for i in range(24):
+            o.step(i, og, reinit=True)
+        return float((p.loc.reshape(-1, 2) * W).sum() + (p.velocity.reshape(-1, 2) * U).sum())
+
+    for name, h, perturb, grad in (
+            ("youngs_modulus", 1e-4, lambda u, s_: dict(E=E0 * (1 + s_ * u)), lambda u: (got["youngs_modulus"] * E0 * u).sum()),
+            ("loc", 1e-7, lambda u, s_: dict(dx=s_ * u), lambda u: (got["loc"].reshape(-1) * u).sum()),
+            ("velocity", 1e-6, lambda u, s_: dict(dv=s_ * u), lambda u: (got["velocity"].reshape(-1) * u).sum())):
+        u = rng.normal(size=n if name == "youngs_modulus" else 2 * n)
+        fd = (loss(**perturb(u, h)) - loss(**perturb(u, -h))) / (2 * h)
+        gd = float(grad(u))
+        tol = 2e-3 if name == "youngs_modulus" else 5e-3
+        assert abs(gd - fd) <= tol * max(abs(fd), 1e-12), (name, gd, fd)
