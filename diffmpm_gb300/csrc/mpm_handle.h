@@ -195,11 +195,11 @@ int check_status(MpmHandle* h, int& st);
 int take_snapshot(MpmHandle* h, cudaStream_t s);
 int replay_block(MpmHandle* h, int64_t step0, int B, int& st, cudaStream_t s);
 // Where a recorded 1-D step copies its start state (x, v, sxx, syy, szz, sxy,
-// rho in storage order, the storage -> original map and the element starts)
-// and its nodal results (mass, velocity after kinematics, velocity and
-// acceleration after the update).
+// rho, volume, centroid volumetric strain in storage order, the storage ->
+// original map and the element starts) and its nodal results (mass, velocity
+// after kinematics, velocity and acceleration after the update).
 struct LineTapeSlot {
-    float* p[7];
+    float* p[9];
     int* pid;
     int* cs;
     float* n[4];

@@ -255,8 +255,9 @@ int line_step(MpmHandle* h, cudaStream_t s, const LineTapeSlot* tape) {
     const int step = (int)h->step;
     const size_t fb = sizeof(float) * (size_t)h->np, nbytes = sizeof(float) * (size_t)h->nn;
     if (tape) {
-        const float* src[7] = {S.x, S.vx, S.sxx[par], S.syy[par], S.szz[par], S.sxy[par], S.rho[par]};
-        for (int k = 0; k < 7; ++k) CK(h, cudaMemcpyAsync(tape->p[k], src[k], fb, cudaMemcpyDeviceToDevice, s));
+        const float* src[9] = {S.x, S.vx, S.sxx[par], S.syy[par], S.szz[par], S.sxy[par], S.rho[par],
+                               S.vol[par], S.vsc[par]};
+        for (int k = 0; k < 9; ++k) CK(h, cudaMemcpyAsync(tape->p[k], src[k], fb, cudaMemcpyDeviceToDevice, s));
         CK(h, cudaMemcpyAsync(tape->pid, S.pid, sizeof(int) * (size_t)h->np, cudaMemcpyDeviceToDevice, s));
         CK(h, cudaMemcpyAsync(tape->cs, S.cstart, sizeof(int) * (size_t)(h->nx + 2), cudaMemcpyDeviceToDevice, s));
     }

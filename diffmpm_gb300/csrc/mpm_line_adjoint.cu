@@ -30,10 +30,11 @@
 
 namespace mpm {
 
-enum { LP_X, LP_V, LP_SXX, LP_SYY, LP_SZZ, LP_SXY, LP_RHO, LP_N };   // particle tape fields
+enum { LP_X, LP_V, LP_SXX, LP_SYY, LP_SZZ, LP_SXY, LP_RHO, LP_VOL, LP_VSC, LP_N };   // particle tape
 enum { LN_M, LN_VA, LN_VB, LN_A, LN_N };                            // nodal tape fields
 // particle adjoints (original order)
-enum { LA_X, LA_V, LA_SXX, LA_SYY, LA_SZZ, LA_SXY, LA_RHO, LA_VSC, LA_EXX, LA_EYY, LA_EXY, LA_E, LA_N };
+enum { LA_X, LA_V, LA_SXX, LA_SYY, LA_SZZ, LA_SXY, LA_RHO, LA_VSC, LA_EXX, LA_EYY, LA_EXY, LA_E, LA_VOL,
+       LA_N };
 // per-step particle scratch (storage order) and nodal scratch
 enum { LS_G, LS_H, LS_R, LS_M, LS_X, LS_V, LS_N };
 enum { LNS_F, LNS_M, LNS_VA, LNS_P, LNS_N };
@@ -50,6 +51,7 @@ struct LineAdjoint {
     float* N = nullptr;        // [T][LN_N][nn]
     uint8_t* mat0 = nullptr;   // material ids, original order
     uint8_t* pvc0 = nullptr;   // velocity constraint codes, original order (or null)
+    float* mass0 = nullptr;    // solve semantics: the constant particle mass, original order
     float* E0 = nullptr;       // per-particle Young's modulus, original order (or null)
     int* eid = nullptr;        // element of each storage slot of the step being reversed
     float* L = nullptr;        // [LA_N][np]
@@ -65,15 +67,16 @@ inline int lblocks(int64_t n) { return (int)((n + LA_THREADS - 1) / LA_THREADS);
 
 // Arguments of one reversed step.
 struct LineStep {
-    int np, nx, usl, velocity_update;
+    int np, nx, usl, velocity_update, reinit;
     float hx, dt, gx;
     const float* x; const float* v; const float* sxx; const float* syy; const float* szz;
-    const float* sxy; const float* rho;
+    const float* sxy; const float* rho; const float* vol; const float* vsc;
     const int* pid; const int* cs; const int* eid;
     const float* M; const float* vA; const float* vB; const float* a;
     const uint16_t* ncons;
     const MatDev* mats; const uint8_t* mat0; const float* E0;
     const uint8_t* pvc0;
+    const float* mass0;
     float* L[LA_N];
     float* sc[LS_N];
     float* ns[LNS_N];
@@ -117,20 +120,24 @@ __device__ __forceinline__ void for_node(const LineStep& A, int i, F&& f) {
 }
 
 // Reverse of the strain / volume / density / stress update driven by the
-// nodal velocities nv (particle.py:249-327, material.py:113-131) at slot q:
-// given the adjoints of the updated stress (sb, by component; xx may carry
-// the forces' share), density, centroid strain and strain, and of the
-// updated volume Vb (USF forces), returns r-bar (zero when the rate was
-// flushed), adds dL/dE and writes the start-of-step adjoints.
-__device__ __forceinline__ float rev_stress(const LineStep& A, int q, int o, int e, const Elem& g,
+// nodal velocities nv (particle.py:249-327, material.py:113-131 and the
+// build's Newtonian total stress) at slot q: given the adjoints of the updated
+// stress (sb, by component; xx may carry the forces' share), density,
+// centroid strain and strain, of the updated volume used by the USF forces
+// (Vb) and, under solve semantics, carried to the next step (L[LA_VOL]),
+// returns r-bar (zero when the rate was flushed), adds dL/dE and writes the
+// start-of-step adjoints.  V0 is the volume the update starts from.
+__device__ __forceinline__ float rev_stress(const LineStep& A, int q, int o, int e, float V0,
                                             const float* nv, const float sb[4], float Vb) {
+    const Elem g = elem_of(A, e);
     const float d0n = fm(-0.5f, g.r), d1n = fm(0.5f, g.r);
     const float raw = fa(fm(d0n, nv[e]), fm(d1n, nv[e + 1]));
     const float r = flush(raw);
     const float dvol = fm(A.dt, r), f = fa(1.0f, dvol), d0 = fm(r, A.dt);
     const MatDev M = A.mats[A.mat0[o]];
     const float Ep = A.E0 ? A.E0[o] : -1.0f;
-    float rb = 0.0f, Eb = 0.0f;
+    float rb = 0.0f, Eb = 0.0f, vscb = 0.0f;
+    bool total = false;
     if (M.type == MAT_LINEAR_ELASTIC) {
         float a1 = M.a1, a2 = M.a2;
         if (Ep >= 0.0f) {
@@ -139,25 +146,40 @@ __device__ __forceinline__ float rev_stress(const LineStep& A, int q, int o, int
         }
         rb = fm(A.dt, fa(fa(fm(a1, sb[0]), fm(a2, sb[1])), fm(a2, sb[2])));
         Eb = fm(d0, fa(fa(fm(M.c1, sb[0]), fm(M.c2, sb[1])), fm(M.c2, sb[2])));
-    } else {   // SimpleMaterial: sigma += E * deps (only the xx strain moves in 1-D)
+    } else if (M.type == MAT_SIMPLE) {   // sigma += E * deps (only the xx strain moves in 1-D)
         rb = fm(A.dt, fm(Ep >= 0.0f ? Ep : M.E, sb[0]));
         Eb = fm(d0, sb[0]);
+    } else {   // Newtonian: sigma = K vsc' I + 2 mu dev(r), r = (r, 0, 0)
+        const float tr = fa(fa(sb[0], sb[1]), sb[2]);
+        rb = fa(fm(M.twomu, sb[0]), fdv(-fm(M.twomu, tr), 3.0f));
+        vscb = fm(M.K, tr);
+        total = true;
     }
     const float rho0 = A.rho[q];
     const float rhob1 = A.L[LA_RHO][o];
     // rho' = rho / f, V = V0 f, vsc' = vsc + dvol, exx' = exx + r dt
-    float fb = fm(g.V0, Vb);
+    const float Vt = A.reinit ? Vb : fa(Vb, A.L[LA_VOL][o]);
+    float fb = fm(V0, Vt);
     fb = fs(fb, fdv(fm(rhob1, fdv(rho0, f)), f));
-    const float dvolb = fa(fb, A.L[LA_VSC][o]);
+    const float vscb1 = fa(A.L[LA_VSC][o], vscb);
+    const float dvolb = fa(fb, vscb1);
     rb = fa(rb, fm(A.dt, fa(dvolb, A.L[LA_EXX][o])));
     if (r == 0.0f) rb = 0.0f;
     A.L[LA_RHO][o] = fdv(rhob1, f);
-    A.L[LA_SXX][o] = sb[0];
-    A.L[LA_SYY][o] = sb[1];
-    A.L[LA_SZZ][o] = sb[2];
-    A.L[LA_SXY][o] = sb[3];
+    A.L[LA_VSC][o] = vscb1;
+    if (!A.reinit) A.L[LA_VOL][o] = fm(Vt, f);
+    A.L[LA_SXX][o] = total ? 0.0f : sb[0];
+    A.L[LA_SYY][o] = total ? 0.0f : sb[1];
+    A.L[LA_SZZ][o] = total ? 0.0f : sb[2];
+    A.L[LA_SXY][o] = total ? 0.0f : sb[3];
     A.L[LA_E][o] = fa(A.L[LA_E][o], Eb);
     return rb;
+}
+
+// The volume a step's stress update starts from: the per-step set-up
+// (element length / count) or, under solve semantics, the carried volume.
+__device__ __forceinline__ float start_volume(const LineStep& A, int q, int e) {
+    return A.reinit ? elem_of(A, e).V0 : A.vol[q];
 }
 
 // pass 0 (USL): the stress update after G2P used the updated velocities
@@ -165,9 +187,8 @@ __global__ void k_lrev0(const __grid_constant__ LineStep A) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= A.np) return;
     const int o = A.pid[q], e = A.eid[q];
-    const Elem g = elem_of(A, e);
     const float sb[4] = {A.L[LA_SXX][o], A.L[LA_SYY][o], A.L[LA_SZZ][o], A.L[LA_SXY][o]};
-    A.sc[LS_R][q] = rev_stress(A, q, o, e, g, A.vB, sb, 0.0f);
+    A.sc[LS_R][q] = rev_stress(A, q, o, e, start_volume(A, q, e), A.vB, sb, 0.0f);
 }
 
 // pass 1: G2P (particle.py:208-247)
@@ -231,27 +252,29 @@ __global__ void k_lrev3(const __grid_constant__ LineStep A) {
     shapes(g, A.x[q], N0, N1, d0, d1);
     const float F0 = A.ns[LNS_F][e], F1 = A.ns[LNS_F][e + 1];
     const float SF = fa(fm(N0, F0), fm(N1, F1)), SD = fa(fm(d0, F0), fm(d1, F1));
-    const float m = fm(g.V0, A.rho[q]);
+    const float V0 = start_volume(A, q, e);
+    const float m = A.reinit ? fm(g.V0, A.rho[q]) : A.mass0[o];
     float xb = fa(A.sc[LS_X][q], fm(fm(m, A.gx), SD));
     float mb = fm(A.gx, SF);
     // the stress and volume the forces used (USF: after this step's update)
-    float sxx = A.sxx[q], V = g.V0;
+    float sxx = A.sxx[q], V = V0;
     if (!USL) {
         const float r = flush(fa(fm(fm(-0.5f, g.r), A.vA[e]), fm(fm(0.5f, g.r), A.vA[e + 1])));
-        PState ps{A.sxx[q], A.syy[q], A.szz[q], A.sxy[q], 0.0f, 0.0f, 0.0f, A.rho[q], 0.0f};
+        PState ps{A.sxx[q], A.syy[q], A.szz[q], A.sxy[q], 0.0f, 0.0f, 0.0f, A.rho[q], A.vsc[q]};
         const float f = strain_stress_update(A.mats[A.mat0[o]], A.E0 ? A.E0[o] : -1.0f, A.dt, r,
                                              0.0f, 0.0f, fm(A.dt, r), ps);
         sxx = ps.sxx;
-        V = fm(g.V0, f);
+        V = fm(V0, f);
     }
     const float sxxb = fm(-V, SD);   // d F_i / d sxx = -V dN_i
     const float Vb = fm(-sxx, SD);
     if (USL) {
         A.L[LA_SXX][o] = fa(A.L[LA_SXX][o], sxxb);
+        if (!A.reinit) A.L[LA_VOL][o] = fa(A.L[LA_VOL][o], Vb);   // the start volume
         A.sc[LS_R][q] = 0.0f;
     } else {
         const float sb[4] = {fa(A.L[LA_SXX][o], sxxb), A.L[LA_SYY][o], A.L[LA_SZZ][o], A.L[LA_SXY][o]};
-        A.sc[LS_R][q] = rev_stress(A, q, o, e, g, A.vA, sb, Vb);
+        A.sc[LS_R][q] = rev_stress(A, q, o, e, V0, A.vA, sb, Vb);
     }
     A.sc[LS_X][q] = xb;
     A.sc[LS_M][q] = mb;
@@ -290,13 +313,20 @@ __global__ void k_lrev5(const __grid_constant__ LineStep A) {
     shapes(g, A.x[q], N0, N1, d0, d1);
     const float M0 = A.ns[LNS_M][e], M1 = A.ns[LNS_M][e + 1];
     const float P0 = A.ns[LNS_P][e], P1 = A.ns[LNS_P][e + 1];
-    const float m = fm(g.V0, A.rho[q]), v = A.v[q];
+    const float m = A.reinit ? fm(g.V0, A.rho[q]) : A.mass0[o], v = A.v[q];
     const float SM = fa(fm(N0, M0), fm(N1, M1)), SP = fa(fm(N0, P0), fm(N1, P1));
     const float DM = fa(fm(d0, M0), fm(d1, M1)), DP = fa(fm(d0, P0), fm(d1, P1));
     const float mb = fa(A.sc[LS_M][q], fa(SM, fm(v, SP)));
     A.L[LA_X][o] = fa(A.sc[LS_X][q], fa(fm(m, DM), fm(fm(m, v), DP)));
     A.L[LA_V][o] = fa(A.sc[LS_V][q], fm(m, SP));
-    A.L[LA_RHO][o] = fa(A.L[LA_RHO][o], fm(g.V0, mb));
+    if (A.reinit) A.L[LA_RHO][o] = fa(A.L[LA_RHO][o], fm(g.V0, mb));   // m = V0 rho
+}
+
+// A float per particle from storage to original order.
+__global__ void k_lscatter(const float* __restrict__ src, const int* __restrict__ pid, int np,
+                           float* __restrict__ out) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < np) out[pid[q]] = src[q];
 }
 
 // Material ids (or every `stride`-th byte of a per-particle code array) from
@@ -328,14 +358,7 @@ int line_alloc(MpmHandle* h, LineAdjoint* a, T** p, size_t n) {
     return MPM_OK;
 }
 
-int line_check(MpmHandle* h) {
-    if (!h->reinit)
-        return fail(h, MPM_ERR_UNSUPPORTED, "the 1-D adjoint implements the per-step volume set-up of solve_jit");
-    for (const MatDev& m : h->mats)
-        if (m.type == MAT_NEWTONIAN)
-            return fail(h, MPM_ERR_UNSUPPORTED, "the adjoint covers LinearElastic and SimpleMaterial");
-    return MPM_OK;
-}
+
 
 }  // namespace
 }  // namespace host
@@ -352,7 +375,6 @@ int line_record(MpmHandle* h, int nsteps, cudaStream_t s) {
     if (!h->initialized) return fail(h, MPM_ERR_STATE, "initialize first");
     if (nsteps < 1) return fail(h, MPM_ERR_INVALID, "nsteps must be >= 1");
     if (h->np <= 0) return fail(h, MPM_ERR_STATE, "no particles");
-    TRY(line_check(h));
     line_adjoint_free(h);
     LineAdjoint* a = new LineAdjoint();
     h->line_adj = a;
@@ -375,6 +397,10 @@ int line_record(MpmHandle* h, int nsteps, cudaStream_t s) {
     TRY(line_alloc(h, a, &a->ns, (size_t)LNS_N * nn));
     const PSet& p = h->ps[h->pcur];
     if (np > 0) k_lmat0<<<lblocks((int64_t)np), LA_THREADS, 0, s>>>(p.mat, p.pid, (int)np, 1, a->mat0);
+    if (!h->reinit) {   // solve semantics: the constant mass
+        TRY(line_alloc(h, a, &a->mass0, np));
+        if (np > 0) k_lscatter<<<lblocks((int64_t)np), LA_THREADS, 0, s>>>(p.mass, p.pid, (int)np, a->mass0);
+    }
     if (h->has_pvc) {
         TRY(line_alloc(h, a, &a->pvc0, np));
         if (np > 0) k_lmat0<<<lblocks((int64_t)np), LA_THREADS, 0, s>>>(p.pvc, p.pid, (int)np, 2, a->pvc0);
@@ -423,6 +449,8 @@ int line_adjoint(MpmHandle* h, const float* dl_dloc, const float* dl_dvel, float
     A.nx = a->nx;
     A.usl = h->usl ? 1 : 0;
     A.velocity_update = h->velocity_update;
+    A.reinit = h->reinit ? 1 : 0;
+    A.mass0 = a->mass0;
     A.hx = h->hx;
     A.dt = h->dt;
     A.gx = h->gx;
@@ -441,6 +469,7 @@ int line_adjoint(MpmHandle* h, const float* dl_dloc, const float* dl_dvel, float
         A.x = P + LP_X * np; A.v = P + LP_V * np;
         A.sxx = P + LP_SXX * np; A.syy = P + LP_SYY * np; A.szz = P + LP_SZZ * np;
         A.sxy = P + LP_SXY * np; A.rho = P + LP_RHO * np;
+        A.vol = P + LP_VOL * np; A.vsc = P + LP_VSC * np;
         A.pid = a->pid + (size_t)t * np;
         A.cs = a->cs + (size_t)t * (a->nx + 2);
         const float* N = a->N + (size_t)t * LN_N * a->nn;

@@ -232,12 +232,10 @@ int mpm_get_counters(const MpmHandle* h, int64_t* resorts, int64_t* rollbacks);
 /* Differentiation.  The reference differentiates solve_jit with jax.grad
  * (examples/optim_1d.py:33-41,55 takes jax.value_and_grad of a loss of the
  * final velocities); these two calls are the hand-written reverse of the same
- * steps: every configuration of a Quadrilateral4Node mesh (LinearElastic,
- * SimpleMaterial and Newtonian particles, USF or USL, with or without the
- * per-step volume set-up, particle tractions and particle velocity
- * constraints), and Linear1D meshes with the per-step volume set-up and
- * LinearElastic or SimpleMaterial particles (other 1-D configurations return
- * MPM_ERR_UNSUPPORTED).
+ * steps, for every configuration the forward runs: Quadrilateral4Node and
+ * Linear1D meshes, LinearElastic, SimpleMaterial and Newtonian particles, USF
+ * or USL, with or without the per-step volume set-up, particle tractions and
+ * particle velocity constraints.
  *
  * mpm_record advances `nsteps` steps like mpm_step and keeps a checkpoint of
  * the full state every `checkpoint_steps` steps (and at the end); on a

@@ -17,6 +17,8 @@ def bar(api, nx=40, ppe=3, scheme="usf", velocity_update=False, sim_steps=50, dt
     x = x + rng.uniform(-0.1, 0.1, x.size) * h / ppe
     if material == "linear":
         mat = api.LinearElastic({"density": 1000.0, "youngs_modulus": 1e6, "poisson_ratio": 0.3})
+    elif material == "newtonian":
+        mat = api.Newtonian({"density": 1000.0, "bulk_modulus": 1e6, "dynamic_viscosity": 20.0})
     else:
         mat = api.SimpleMaterial({"density": 1000.0, "E": 1e6})
     fn = api.Linear(0, np.array([0.0, sim_steps * dt]), np.array([0.0, 1.0]))

@@ -6,8 +6,10 @@ differentiated along seeded directions of the per-particle Young's modulus,
 the initial positions and the initial velocities: the GPU's
 dL/dE . dE (and likewise for x0, v0) must match (L(+) - L(-)) / 2 eps of two
 float64 oracle runs within 1e-3 (relative to |FD|, or to a tenth of the summed
-|terms| where a random direction cancels).  The last case is the reference's
-own optimisation example (examples/optim_1d.py): one SimpleMaterial particle,
+|terms| where a random direction cancels).  Besides the solve_jit cases,
+solve semantics (``reinit=False``: constant mass, carried volume) and the
+build's Newtonian material are checked the same way.  The last case is the
+reference's own optimisation example (examples/optim_1d.py): one SimpleMaterial particle,
 USL, 1000 steps, the gradient of |v_end - v_target| in E."""
 import numpy as np
 import pytest
@@ -23,6 +25,8 @@ TOL = 1e-3
 
 
 def oracle_end(case, steps, E, x0=None, v0=None):
+    case = dict(case)
+    reinit = case.pop("reinit", True)
     solver, g = L.bar(O, dtype=np.float64, E=E, sim_steps=steps, **case)
     p = solver.mesh.particles[0]
     if x0 is not None:
@@ -30,7 +34,7 @@ def oracle_end(case, steps, E, x0=None, v0=None):
     if v0 is not None:
         p.velocity[:] = np.asarray(v0, np.float64).reshape(-1, 1, 1)
     for i in range(steps):
-        solver.step(i, g, reinit=True)
+        solver.step(i, g, reinit=reinit)
     return p.loc.reshape(-1).copy(), p.velocity.reshape(-1).copy()
 
 
@@ -40,14 +44,18 @@ CASES = [dict(scheme="usf"), dict(scheme="usl"), dict(scheme="usf", material="si
          dict(scheme="usl", material="simple", nx=12, ppe=1),
          dict(scheme="usf", velocity_update=True),
          dict(scheme="usf", vshift=8.0), dict(scheme="usl", vshift=8.0),
-         dict(scheme="usf", pvc=True), dict(scheme="usl", pvc=True, vshift=8.0)]
+         dict(scheme="usf", pvc=True), dict(scheme="usl", pvc=True, vshift=8.0),
+         dict(scheme="usf", reinit=False), dict(scheme="usl", reinit=False, vshift=8.0),
+         dict(scheme="usf", material="newtonian"), dict(scheme="usl", material="newtonian", reinit=False)]
 
 
 @pytest.mark.parametrize("case", CASES, ids=lambda c: "-".join(f"{k}={v}" for k, v in c.items()))
 def test_line_adjoint_matches_central_differences(built, case):
     case = dict(dict(nx=20, ppe=2), **case)
+    reinit = case.get("reinit", True)
+    bar_case = {k: v for k, v in case.items() if k != "reinit"}
     steps = 40
-    gs0, g = L.bar(O, sim_steps=steps, **case)
+    gs0, g = L.bar(O, sim_steps=steps, **bar_case)
     p0 = gs0.mesh.particles[0]
     n = len(p0.loc)
     x0 = p0.loc.reshape(-1).astype(np.float64)
@@ -56,8 +64,8 @@ def test_line_adjoint_matches_central_differences(built, case):
     E = 1e6 * np.exp(rng.uniform(-0.3, 0.3, n))
     w = rng.standard_normal(n)
     u = rng.standard_normal(n)
-    gs, g = L.bar(D, sim_steps=steps, E=E.astype(np.float32), **case)
-    sim = gs.simulation(g, reinit=True)
+    gs, g = L.bar(D, sim_steps=steps, E=E.astype(np.float32), **bar_case)
+    sim = gs.simulation(g, reinit=reinit)
     gs._upload(sim)
     sim.initialize()
     sim.record(steps)
