@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--no-plain-path", action="store_true",
                     help="skip timing each simulation alone (the ratio's denominator)")
     ap.add_argument("--phase-steps", type=int, default=20)
+    ap.add_argument("--mixed-steps", type=int, default=200,
+                    help="steps of the 4096^2 elastic + Newtonian workload (0 skips it)")
     ap.add_argument("--diff-steps", type=int, default=2000,
                     help="steps of the differentiation workload (0 skips it)")
     return ap.parse_args()
@@ -306,6 +308,36 @@ def plain_scaleup(args, D, workloads, torch):
     return out, roof
 
 
+def mixed_large(args, D, workloads, torch):
+    """The large mixed-material workload: 4096^2 mesh, 16,777,216 particles in
+    a LinearElastic and a Newtonian block, USL, dt 2e-7; device-timed steps
+    in graphs of 100 and per-phase kernel times."""
+    K = args.mixed_steps
+    solver, g, info = workloads.mixed_large(D, sim_steps=K)
+    np_, nn = info["np"], (info["n"] + 1) ** 2
+    sim = solver.simulation(g, reinit=True)
+    solver._upload(sim)
+    sim.initialize()
+    sim.set_block_steps(100)
+    sim.step(max(args.warmup, 3))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    sim.step(K)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    tot = sim.time_phases(args.phase_steps)
+    peak, _ = measured_peak()
+    out = {"workload": "mixed_large_usl", "mesh": f"{info['n']}x{info['n']}", "particles": np_,
+           "steps": K, "value": np_ * K / (ms / 1000.0), "ms_per_step": ms / K,
+           "phase_ms": {k: v / args.phase_steps for k, v in tot.items()},
+           "step_roofline_frac": (workloads.particle_steps_bytes(np_, nn) * K
+                                  / (ms / 1000.0) / 1e9) / peak}
+    sim.close()
+    return out
+
+
 def differentiation(args, D, workloads, torch):
     """The differentiation workload: 256^2 mesh, 125,664 particles with a
     seeded log-normal E field, 2000 USF steps; loss = mean |x_end - x_target|^2
@@ -512,6 +544,7 @@ def run_ours(args, world, rank, local):
     plain_usl, roof_usl = plain_scaleup(argparse.Namespace(**dict(vars(args), scheme="usl")), D,
                                         workloads, torch)
     plain_usl["roofline"] = roof_usl
+    mixed = mixed_large(args, D, workloads, torch) if args.mixed_steps > 0 else None
     diff = differentiation(args, D, workloads, torch) if args.diff_steps > 0 else None
 
     cpu = None
@@ -568,6 +601,7 @@ def run_ours(args, world, rank, local):
             "roofline": roof,
             "plain_scaleup": plain,
             "plain_scaleup_usl": plain_usl,
+            "mixed_large": mixed,
             "differentiation": diff,
             "clocks": clk,
             "counters": counters,

@@ -1,7 +1,9 @@
 """Properties checked at the benchmark configurations' full sizes, where the
 oracle is too slow: bitwise reproducibility of the 1024^2 scale-up, a batch
-of one equal to the simulation run alone, and the adjoint of the 256^2
-differentiation run (2000 steps, checkpoints every 100) linear in its seed."""
+of one equal to the simulation run alone, the 4096^2 elastic + Newtonian run
+reproducible and unchanged by where its step blocks split, and the adjoint of
+the 256^2 differentiation run (2000 steps, checkpoints every 100) linear in
+its seed."""
 import numpy as np
 import pytest
 
@@ -42,6 +44,38 @@ def test_scaleup_full_size_reproducible_and_batch_of_one(built):
     for k in FIELDS:
         assert np.array_equal(sim.read(k), first[k]), ("batch", k)
     b.close()
+    sim.close()
+
+
+def test_mixed_large_full_size_reproducible_and_split_blocks_agree(built):
+    """4096^2 mesh, 16,777,216 particles in a LinearElastic and a Newtonian
+    block, USL, 200 steps of 2e-7 s: two runs agree bitwise, a run advanced as
+    120 + 80 steps in blocks of 40 equals one advanced as 200 in blocks of 100,
+    and every particle stays finite and inside the mesh."""
+    steps = 200
+    solver, g, info = workloads.mixed_large(D, sim_steps=steps)
+    assert info["np"] == 16777216
+    sim = solver.simulation(g, reinit=True)
+    fields = ("loc", "velocity", "stress", "density")
+
+    def run(block, parts):
+        solver._upload(sim)
+        sim.initialize()
+        sim.set_block_steps(block)
+        for k in parts:
+            sim.step(k)
+        return {k: sim.read(k).copy() for k in fields}
+
+    first = run(100, (steps,))
+    for k in fields:
+        assert np.isfinite(first[k]).all(), k
+    loc = first["loc"].reshape(-1, 2)
+    assert loc.min() >= 0.0 and loc.max() < 1.0
+    again = run(100, (steps,))
+    split = run(40, (120, 80))
+    for k in fields:
+        assert np.array_equal(again[k], first[k]), k
+        assert np.array_equal(split[k], first[k]), ("split", k)
     sim.close()
 
 
