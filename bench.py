@@ -14,9 +14,12 @@ checkpoints every 100 steps) plus the batched adjoint w.r.t. each
 simulation's E (mpm_batch_adjoint) of L = mean |x_end - x_target|^2, timed
 with CUDA events after one untimed warm-up iteration.  Beside it: the same
 batch forward only, and the plain path -- each simulation advanced alone by
-mpm_step, one after another -- which the spec ratio compares against.
-The plain 2-D scale-up configuration (1024^2 mesh, 2.1M particles, 500 USF
-steps) is measured too and gives the roofline of the plain forces kernel.
+mpm_step, one after another -- the denominator of the batched / plain
+ratios in ``components``.  The plain 2-D scale-up (1024^2 mesh, 2.1M
+particles, 500 steps, USF and USL) is measured too and gives the roofline of
+the plain top kernel; the 4096^2 elastic + Newtonian run (16.8M particles,
+200 USL steps) and the 256^2 differentiation run (2000 steps) are timed
+beside them.
 
 ``--impl reference`` times the CPU restatement of the reference step and its
 autograd gradient (the reference itself is JAX, not installed) on a sample of

@@ -1,4 +1,4 @@
-// Batch of simulation handles (mpm_batch.cu) and the driver helpers the
+// Batch of simulation handles (mpm_batch.cu) and the host helpers the
 // batched adjoint (mpm_adjoint.cu) shares with the batched step.
 #pragma once
 #include <map>

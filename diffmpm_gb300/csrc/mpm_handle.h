@@ -1,4 +1,4 @@
-// Host-side state of one simulation handle and the driver helpers shared by
+// Host-side state of one simulation handle and the host helpers shared by
 // the forward step (mpm_abi.cu) and the adjoint (mpm_adjoint.cu).
 #pragma once
 #include <cuda_runtime.h>
