@@ -180,6 +180,8 @@ def _cpu_fwd_adj_member(args):
     from diffmpm_gb300 import workloads
     from oracle import mpm_oracle as O
     from oracle import mpm_torch as T
+    if steps == 0:                       # pool warm-up: imports only
+        return 0, 0.0
     spec = workloads.batch_specs(**seed_specs)[k]
     o, g, info = workloads.batch_member(O, spec, sim_steps=steps)
     sim, st0 = T.from_solver(o, g, dtype=torch.float32)
@@ -193,19 +195,26 @@ def _cpu_fwd_adj_member(args):
 
 
 def cpu_fwd_adj(members, steps, workers, seed_specs=None):
-    """Particle-steps/s of forward + adjoint on the CPU over `members`."""
+    """Particle-steps/s of forward + adjoint on the CPU over `members`, timed
+    by the wall clock around the whole pool's work (after a warm-up task on
+    every worker, so that process start-up and imports are outside it).
+    Members go largest first to keep the workers evenly loaded."""
     import multiprocessing as mp
-    jobs = [(k, steps, seed_specs or {}) for k in members]
+    from diffmpm_gb300 import workloads
+    specs = workloads.batch_specs(**(seed_specs or {}))
+    order = sorted(members, key=lambda k: -specs[k]["np"])
+    jobs = [(k, steps, seed_specs or {}) for k in order]
     if workers > 1:
         with mp.get_context("spawn").Pool(workers) as pool:
-            res = pool.map(_cpu_fwd_adj_member, jobs)
+            pool.map(_cpu_fwd_adj_member, [(0, 0, {})] * workers, chunksize=1)
+            t0 = time.perf_counter()
+            res = pool.map(_cpu_fwd_adj_member, jobs, chunksize=1)
+            wall = time.perf_counter() - t0
     else:
+        t0 = time.perf_counter()
         res = [_cpu_fwd_adj_member(j) for j in jobs]
-    # every core busy: the per-core rate (time inside the workers, without
-    # process start-up) times the number of cores
+        wall = time.perf_counter() - t0
     ps = sum(r[0] for r in res)
-    busy = sum(r[1] for r in res)
-    wall = busy / max(1, min(workers, len(jobs)))
     return ps / wall, ps, wall
 
 
@@ -222,24 +231,42 @@ def cpu_sample_members(nsims, limit_particles):
     return out, tot
 
 
+# The CPU sample shared by the `cpu_baseline` leg of the GPU arm and by the
+# reference arm: the first batch members holding about 40,000 particles per
+# host core, forward + adjoint, one process per core.
+CPU_PARTICLES_PER_CORE = 40000
+
+
+def cpu_sample(nsims, workers):
+    members, tot = cpu_sample_members(nsims, CPU_PARTICLES_PER_CORE * workers)
+    return members, tot
+
+
+def cpu_sample_text(members, tot, steps):
+    return (f"{steps} steps of batch members {members[0]}..{members[-1]} ({tot} particles), "
+            f"float32 torch restatement of the reference step, forward + autograd adjoint "
+            f"w.r.t. each simulation's E, one process per core, wall-clock time of the pool "
+            f"(JAX is not installed)")
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
     workers = os.cpu_count() or 1
-    steps = 20
-    members, tot = cpu_sample_members(args.nsims, 60000 * workers)
+    steps = args.steps
+    members, tot = cpu_sample(args.nsims, workers)
     for _ in range(max(0, min(args.warmup, 1))):
         cpu_fwd_adj(members[:workers], 2, workers)
     v, ps, wall = cpu_fwd_adj(members, steps, workers)
-    sample = (f"{steps} steps of batch members {members[0]}..{members[-1]} ({tot} particles), "
-              f"float32 torch restatement of the reference step, forward + autograd adjoint "
-              f"w.r.t. each simulation's E, one process per core (JAX is not installed)")
+    sample = cpu_sample_text(members, tot, steps)
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * wall / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": "batch_fwd_adjoint", "sims": args.nsims, "sample": sample},
+        "config": {"workload": "batch_fwd_adjoint", "sims": args.nsims, "steps": steps,
+                   "sample_members": [members[0], members[-1]], "sample_particles": tot,
+                   "sample": sample},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": workers, "kind": "port",
                          "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -553,12 +580,11 @@ def run_ours(args, world, rank, local):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         workers = os.cpu_count() or 1
-        mem, tot = cpu_sample_members(args.nsims, 30000 * workers)
-        v, ps, wall = cpu_fwd_adj(mem, 10, workers)
+        mem, tot = cpu_sample(args.nsims, workers)
+        csteps = min(K, 20)
+        v, ps, wall = cpu_fwd_adj(mem, csteps, workers)
         cpu = {"value": v, "unit": UNIT, "cores": workers, "kind": "port",
-               "sample": f"10 steps of batch members {mem[0]}..{mem[-1]} ({tot} particles), "
-                         f"float32 torch restatement of the reference step, forward + autograd "
-                         f"adjoint, one process per core"}
+               "sample": cpu_sample_text(mem, tot, csteps)}
 
     ps = npart * K
     value = world * ps / (fa_ms / 1000.0)

@@ -75,7 +75,7 @@ SIGNATURES = [
     ("mpm_set_particles", C.c_int, [_VP, C.c_int64, _VP, _VP, C.c_int, _VP]),
     ("mpm_write_field", C.c_int, [_VP, C.c_int, _VP, C.c_int, _VP]),
     ("mpm_read_field", C.c_int, [_VP, C.c_int, _VP, C.c_int, _VP]),
-    ("mpm_output_enqueue", C.c_int, [_VP, C.c_int, _VP, _VP, _VP, C.POINTER(C.c_int64)]),
+    ("mpm_output_enqueue", C.c_int, [_VP, C.c_int, _VP, _VP, C.c_size_t, _VP, C.POINTER(C.c_int64)]),
     ("mpm_output_wait", C.c_int, [_VP, C.c_int64]),
     ("mpm_host_alloc", C.c_int, [C.c_size_t, C.POINTER(_VP)]),
     ("mpm_host_free", C.c_int, [_VP]),

@@ -13,9 +13,14 @@ velocities; ``torch.autograd.grad`` / ``.backward()`` through them calls the
 adjoint.  Gradients flow to ``E`` and, when given, to the initial positions
 ``loc`` and velocities ``velocity``.  Arithmetic is float32, as the forward.
 
-One handle per (gravity) configuration is reused by every call on the same
-``mpm``: run the backward of one call before the forward of the next (the
-adjoint raises ``MpmError`` if the recorded run was overwritten).
+Every forward records into a simulation of its own, leased from ``mpm``'s
+pool (``MPMExplicit.lease_simulation``) and returned to it when the autograd
+graph that holds the forward is freed, so forwards and backwards may
+interleave freely: two forwards before their backwards, two losses on one
+graph, or a forward-only evaluation inside a training step.  A loop that runs
+forward then backward cycles through a pool of two simulations (the previous
+iteration's graph is freed only once the next forward has returned), keeping
+their allocations and captured step graphs.
 """
 from __future__ import annotations
 
@@ -30,7 +35,8 @@ def _dev_f32(t, device):
 class ExplicitRun(torch.autograd.Function):
     @staticmethod
     def forward(ctx, E, loc, velocity, mpm, gravity, nsteps, checkpoint_steps):
-        sim = mpm.simulation(gravity, reinit=True)
+        lease = mpm.lease_simulation(gravity, reinit=True)
+        sim = lease.sim
         mpm._upload(sim)
         dev = E.device if E.is_cuda else None
         put = (lambda t: _dev_f32(t, dev)) if dev is not None else (
@@ -52,6 +58,7 @@ class ExplicitRun(torch.autograd.Function):
         else:
             x = torch.from_numpy(sim.read("loc"))
             v = torch.from_numpy(sim.read("velocity"))
+        ctx.lease = lease
         ctx.sim = sim
         ctx.dev = dev
         ctx.want = ("youngs_modulus",) + (("loc",) if loc is not None else ()) + (

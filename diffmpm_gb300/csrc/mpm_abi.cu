@@ -881,8 +881,8 @@ int mpm_read_field(MpmHandle* h, int field, void* dst, int on_device, void* stre
     return sync(h, s);
 }
 
-int mpm_output_enqueue(MpmHandle* h, int nfields, const int* fields, void* host_dst, void* stream,
-                       int64_t* ticket) {
+int mpm_output_enqueue(MpmHandle* h, int nfields, const int* fields, void* host_dst,
+                       size_t host_dst_bytes, void* stream, int64_t* ticket) {
     if (!h) return MPM_ERR_INVALID;
     if (h->np < 0) return fail(h, MPM_ERR_STATE, "set particles first");
     if (nfields < 1 || !fields || !host_dst || !ticket)
@@ -899,6 +899,9 @@ int mpm_output_enqueue(MpmHandle* h, int nfields, const int* fields, void* host_
             return fail(h, MPM_ERR_INVALID, "unknown field %d", fields[k]);
         total += sizeof(float) * ncomp_of(h, fields[k]) * h->np;
     }
+    if (host_dst_bytes < total)
+        return fail(h, MPM_ERR_INVALID, "host_dst holds %zu bytes, the fields need %zu", host_dst_bytes,
+                    total);
     if (h->out_stage_bytes < total) {
         CK(h, cudaStreamSynchronize(s));      // copies from the old buffer are done
         dfree(h, h->out_stage);

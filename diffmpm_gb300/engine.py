@@ -45,6 +45,27 @@ def _in_arg(a, dtype, count):
     return _lib.ptr(arr), 0, arr
 
 
+def _out_arg(out, dtype, count):
+    """(pointer, on_device) for a caller-provided destination of ``count``
+    elements: a C-contiguous, writeable NumPy array or a contiguous CUDA
+    tensor of exactly that dtype and size (the library writes
+    ``count * 4`` bytes there, so anything else is refused)."""
+    if _is_cuda_tensor(out):
+        import torch
+        want = torch.float32 if dtype == np.float32 else torch.int32
+        if out.dtype != want or not out.is_contiguous() or out.numel() != count:
+            raise ValueError(f"out must be a contiguous {want} tensor of {count} elements, "
+                             f"found {out.dtype} with {out.numel()} elements")
+        return C.c_void_p(out.data_ptr()), 1
+    if not isinstance(out, np.ndarray):
+        raise ValueError("out must be a NumPy array or a CUDA tensor")
+    if out.dtype != np.dtype(dtype) or not out.flags.c_contiguous or not out.flags.writeable \
+            or out.size != count:
+        raise ValueError(f"out must be a writeable C-contiguous {np.dtype(dtype).name} array of "
+                         f"{count} elements, found {out.dtype.name} with {out.size} elements")
+    return _lib.ptr(out), 0
+
+
 class PinnedBuffer:
     """Page-locked host memory from the library (mpm_host_alloc), the
     destination of :meth:`Simulation.output_enqueue`."""
@@ -207,10 +228,7 @@ class Simulation:
         dtype = np.int32 if field in _INT_FIELDS else np.float32
         if out is None:
             out = np.empty((self.n, nc) if nc > 1 else (self.n,), dtype=dtype)
-        if _is_cuda_tensor(out):
-            p, dev = C.c_void_p(out.data_ptr()), 1
-        else:
-            p, dev = _lib.ptr(out), 0
+        p, dev = _out_arg(out, dtype, self.n * nc)
         self._ok(self._lib.mpm_read_field(self._h, _lib.FIELD[field], p, dev, _stream_for(out)))
         return out
 
@@ -223,8 +241,8 @@ class Simulation:
         if buffer.nbytes < need:
             raise ValueError(f"buffer holds {buffer.nbytes} bytes, the fields need {need}")
         t = C.c_int64()
-        self._ok(self._lib.mpm_output_enqueue(self._h, len(fields), codes, buffer.ptr, stream,
-                                              C.byref(t)))
+        self._ok(self._lib.mpm_output_enqueue(self._h, len(fields), codes, buffer.ptr,
+                                              int(buffer.nbytes), stream, C.byref(t)))
         return t.value
 
     def output_wait(self, ticket: int):
@@ -271,8 +289,7 @@ class Simulation:
         nc = 1 if field == "mass" else self.ndim
         if out is None:
             out = np.empty((self.nnodes, nc) if nc > 1 else (self.nnodes,), dtype=np.float32)
-        dev = 1 if _is_cuda_tensor(out) else 0
-        p = C.c_void_p(out.data_ptr()) if dev else _lib.ptr(out)
+        p, dev = _out_arg(out, np.float32, self.nnodes * nc)
         self._ok(self._lib.mpm_read_nodal_field(self._h, _lib.NODAL_FIELD[field], p, dev, _stream_for(out)))
         return out
 
@@ -418,10 +435,10 @@ class Batch:
         be a preallocated host array or CUDA tensor of that size.  Returns it
         with per-member views in ``split(...)`` order."""
         counts = self._counts(field)
+        dtype = np.int32 if field in _INT_FIELDS else np.float32
         if out is None:
-            out = np.empty(sum(counts), dtype=np.float32)
-        dev = 1 if _is_cuda_tensor(out) else 0
-        p = C.c_void_p(out.data_ptr()) if dev else _lib.ptr(out)
+            out = np.empty(sum(counts), dtype=dtype)
+        p, dev = _out_arg(out, dtype, sum(counts))
         self._ok(self._lib.mpm_batch_read_field(self._b, _lib.FIELD[field], p, dev, _stream_for(out)))
         return out
 

@@ -27,6 +27,25 @@ from .functions import Linear
 _schemes = ("usf", "usl")
 
 
+class SimulationLease:
+    """Holds one pooled simulation (``MPMExplicit.lease_simulation``) and puts
+    it back into its pool when released or garbage-collected."""
+
+    def __init__(self, sim, pool):
+        self.sim, self._pool = sim, pool
+
+    def release(self):
+        if self.sim is not None:
+            self._pool.append(self.sim)
+            self.sim = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
 class MPMExplicit:
     __particle_props = ("loc", "velocity", "stress", "strain")
 
@@ -43,6 +62,7 @@ class MPMExplicit:
         self.out_dir = out_dir
         self.writer_func = writer_func
         self._sims = {}
+        self._idle = {}      # leased simulations returned to the pool, per key
         # the constructor's volume set-up (solver.py:81-85), run on the GPU
         sim = self.simulation(np.zeros(2), reinit=True)
         self._upload(sim)
@@ -74,20 +94,39 @@ class MPMExplicit:
         g = np.broadcast_to(np.asarray(gravity, dtype=np.float64).reshape(-1), (2,))
         key = (bool(reinit), self.scheme, bool(self.velocity_update), float(self.dt))
         if key not in self._sims:
-            el = self.mesh.elements
-            _, mats, _, _ = self._population()
-            self._sims[key] = Simulation(
-                el.nelements, el.el_len, self.dt, scheme=self.scheme,
-                velocity_update=self.velocity_update, reinit_each_step=reinit, gravity=g,
-                constraints=el.constraints, functions=self._functions(),
-                nodal_forces=el.concentrated_nodal_forces, materials=mats,
-                ndim=getattr(el, "ndim", 2))
-            self._sims[key].gravity = tuple(g)
-        sim = self._sims[key]
+            self._sims[key] = self._new_simulation(reinit, g)
+        return self._with_gravity(self._sims[key], g)
+
+    def _new_simulation(self, reinit, g) -> Simulation:
+        el = self.mesh.elements
+        _, mats, _, _ = self._population()
+        sim = Simulation(
+            el.nelements, el.el_len, self.dt, scheme=self.scheme,
+            velocity_update=self.velocity_update, reinit_each_step=reinit, gravity=g,
+            constraints=el.constraints, functions=self._functions(),
+            nodal_forces=el.concentrated_nodal_forces, materials=mats,
+            ndim=getattr(el, "ndim", 2))
+        sim.gravity = tuple(g)
+        return sim
+
+    @staticmethod
+    def _with_gravity(sim, g):
         if sim.gravity != tuple(g):
             sim.set_gravity(g)
             sim.gravity = tuple(g)
         return sim
+
+    def lease_simulation(self, gravity, reinit=True) -> "SimulationLease":
+        """A simulation of this configuration that no other lease holds: an
+        idle one from this solver's pool, or a new one.  It goes back to the
+        pool when the lease is released or garbage-collected, so that every
+        recorded run (``record``) stays intact until its holder lets go --
+        the autograd function takes one lease per forward."""
+        g = np.broadcast_to(np.asarray(gravity, dtype=np.float64).reshape(-1), (2,))
+        key = (bool(reinit), self.scheme, bool(self.velocity_update), float(self.dt))
+        pool = self._idle.setdefault(key, [])
+        sim = pool.pop() if pool else self._new_simulation(reinit, g)
+        return SimulationLease(self._with_gravity(sim, g), pool)
 
     def _upload(self, sim: Simulation):
         sets, mats, mat_index, offsets = self._population()

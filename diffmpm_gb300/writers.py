@@ -19,18 +19,17 @@ class EmptyWriter:
 
 
 class NPZWriter:
-    """Writes ``particles_<step>.npz`` with the step zero-padded to
-    ``int(log10(max_steps)) + 1`` digits (diffmpm/writers.py:30-54)."""
+    """Writes ``particles_<step>.npz`` into ``out_dir``, the step number
+    zero-padded to as many digits as ``max_steps`` has (the file names of
+    diffmpm/writers.py:30-54, which the reference's benchmark readers open)."""
 
     def write(self, args, transforms=None, **kwargs):
         arrays, step = args
-        max_digits = int(np.log10(kwargs["max_steps"])) + 1
-        req_zeros = max_digits - 1 if step == 0 else max_digits - (int(np.log10(step)) + 1)
-        fileno = f"{'0' * req_zeros}{step}"
-        filepath = Path(kwargs["out_dir"]).joinpath(f"particles_{fileno}.npz")
-        filepath.parent.mkdir(parents=True, exist_ok=True)
-        np.savez(filepath, **arrays)
-        logger.info(f"Saved particle data for step {step} at {filepath}")
+        width = len(str(int(kwargs["max_steps"])))
+        target = Path(kwargs["out_dir"]) / f"particles_{int(step):0{width}d}.npz"
+        target.parent.mkdir(parents=True, exist_ok=True)
+        np.savez(target, **arrays)
+        logger.info("step %d written to %s", step, target)
 
 
 class AsyncOutput:

@@ -163,14 +163,16 @@ int mpm_read_field(MpmHandle* h, int field, void* dst, int on_device, void* stre
 
 /* Asynchronous output: enqueue on `stream` the copy of `nfields` particle
  * fields (original order, each as mpm_read_field lays it out, one after the
- * other) into the pinned host buffer `host_dst`, and return at once with a
- * ticket; mpm_output_wait(ticket) blocks until that copy is in host memory
- * and may be called from another host thread while this one keeps stepping.
- * At most 8 copies may be outstanding.  Replaces the host callback that
- * writes the outputs of solve_jit every out_steps steps
- * (diffmpm/solver.py:187-210, writers.py:30-54). */
-int mpm_output_enqueue(MpmHandle* h, int nfields, const int* fields, void* host_dst, void* stream,
-                       int64_t* ticket);
+ * other) into the pinned host buffer `host_dst` of `host_dst_bytes` bytes,
+ * and return at once with a ticket; mpm_output_wait(ticket) blocks until that
+ * copy is in host memory and may be called from another host thread while
+ * this one keeps stepping.  The copy needs 4 * np * (sum of the fields'
+ * component counts) bytes; a smaller `host_dst_bytes` returns MPM_ERR_INVALID
+ * before anything is enqueued.  At most 8 copies may be outstanding.
+ * Replaces the host callback that writes the outputs of solve_jit every
+ * out_steps steps (diffmpm/solver.py:187-210, writers.py:30-54). */
+int mpm_output_enqueue(MpmHandle* h, int nfields, const int* fields, void* host_dst,
+                       size_t host_dst_bytes, void* stream, int64_t* ticket);
 int mpm_output_wait(MpmHandle* h, int64_t ticket);
 
 /* Pinned host memory for mpm_output_enqueue. */
@@ -317,14 +319,19 @@ int mpm_batch_adjoint(MpmBatch* b, const float* const* dl_dloc, const float* con
  * for callers that cannot call cudaMalloc -- a JAX/XLA FFI handler, whose
  * buffers come from XLA's allocator, or an application whose framework owns the
  * device memory pool.  All pointers are device memory: loc (n, 2), density (n)
- * in; element_id (n; -1 outside the mesh), volume (n), mass (n) out.
+ * in; element_id (n), volume (n), mass (n) out.  One difference from the
+ * allocating set-up: a particle outside the mesh (including one exactly on
+ * its top or right edge) gets element id -1 and zero volume and mass, where
+ * mpm_initialize refuses the whole population with MPM_ERR_OUT_OF_MESH.
  * The per-element counters live in a fixed 4 MiB device array, so the mesh may
  * have at most MPM_NOALLOC_MAX_ELEMENTS elements (larger meshes return
  * MPM_ERR_INVALID).  That array stays resident on every GPU that loads the
  * library.  The first call on a device (with that device current) looks up
- * the array's address; make that first call before any stream capture.  All
- * calls share the array, so calls that overlap on the GPU race; order them.
- * Errors are reported through mpm_last_error(NULL). */
+ * the array's address and keeps it for the life of the process; make that
+ * first call before any stream capture, and do not call this entry point
+ * again on a device after cudaDeviceReset (the kept address would be stale).
+ * All calls share the array, so calls that overlap on the GPU race; order
+ * them.  Errors are reported through mpm_last_error(NULL). */
 int mpm_volume_setup_noalloc(int nx, int ny, double hx, double hy, int64_t n, const float* loc,
                              const float* density, int32_t* element_id, float* volume,
                              float* mass, void* stream);

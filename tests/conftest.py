@@ -44,7 +44,16 @@ def built():
 
 
 def pytest_terminal_summary(terminalreporter):
-    """Print the float64 error table collected by test_gpu_fp64_error."""
+    """Print the parity checks that passed through the zero-field fallback
+    (test_gpu_parity.FALLBACKS) and the float64 error table collected by
+    test_gpu_fp64_error."""
+    par = sys.modules.get("test_gpu_parity")
+    used = getattr(par, "FALLBACKS", None) if par else None
+    if used:
+        tr = terminalreporter
+        tr.section("parity checks passed through the zero-field fallback")
+        for name, e, how in used:
+            tr.write_line(f"{name}: {e:.2e} against the float32 oracle; {how}")
     mod = sys.modules.get("test_gpu_fp64_error")
     rows = getattr(mod, "TABLE", None) if mod else None
     if not rows:

@@ -2,7 +2,7 @@
 
 Run once where the reference is mounted:
 
-    python tests/golden/make_fixtures.py /root/reference
+    python tests/golden/make_fixtures.py <reference checkout>
 
 For each end-to-end benchmark in ``benchmarks/2d/<name>/`` of diffmpm it reads
 the TOML input deck, the entity-set JSON and the particle JSON, and the golden
@@ -83,7 +83,9 @@ def build(ref: Path, name: str) -> dict:
 
 
 def main(argv):
-    ref = Path(argv[1] if len(argv) > 1 else "/root/reference")
+    if len(argv) != 2:
+        raise SystemExit(f"usage: {argv[0]} <path of the diffmpm reference checkout>")
+    ref = Path(argv[1])
     out = Path(__file__).resolve().parent
     for name in BENCHMARKS:
         fx = build(ref, name)

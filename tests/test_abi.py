@@ -114,3 +114,35 @@ def test_create_rejects_meshes_beyond_the_node_index_range(built):
     h = ctypes.c_void_p()
     assert lib.mpm_create(ctypes.byref(d), ctypes.byref(h)) == 1
     assert b"too large" in lib.mpm_last_error(None)
+
+
+def test_read_destinations_are_checked_before_the_library_writes():
+    """A read into a caller's ``out`` must be refused when the library would
+    write past it or scramble it: too few elements, a wrong dtype, a
+    non-contiguous or read-only array (checked on the host, no GPU)."""
+    import numpy as np
+    from diffmpm_gb300.engine import _out_arg
+    good = np.empty((10, 2), np.float32)
+    p, dev = _out_arg(good, np.float32, 20)
+    assert dev == 0 and p.value == good.ctypes.data
+    with pytest.raises(ValueError, match="20 elements"):
+        _out_arg(np.empty(10, np.float32), np.float32, 20)          # undersized
+    with pytest.raises(ValueError, match="float32"):
+        _out_arg(np.empty((10, 2), np.float64), np.float32, 20)     # float64
+    with pytest.raises(ValueError):
+        _out_arg(np.empty((10, 4), np.float32)[:, :2], np.float32, 20)   # strided view
+    ro = np.empty(20, np.float32)
+    ro.flags.writeable = False
+    with pytest.raises(ValueError):
+        _out_arg(ro, np.float32, 20)
+    with pytest.raises(ValueError, match="int32"):
+        _out_arg(np.empty(20, np.float32), np.int32, 20)            # integer field
+    with pytest.raises(ValueError):
+        _out_arg([0.0] * 20, np.float32, 20)                        # not an array
+
+
+def test_output_enqueue_takes_the_destination_size():
+    """mpm_output_enqueue is told how large the pinned destination is."""
+    text = HEADER.read_text()
+    decl = re.search(r"int mpm_output_enqueue\(([^)]*)\)", text, re.S).group(1)
+    assert "size_t host_dst_bytes" in decl

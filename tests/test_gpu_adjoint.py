@@ -146,6 +146,16 @@ def test_adjoint_across_resorts(built, scheme):
         assert rel(a[k], ref[k]) < GRAD_TOL, k
 
 
+def _direct_adjoint(gs, g, E, W, U, steps, ckpt=8):
+    """record + adjoint through the Simulation API (no autograd)."""
+    sim = gs.simulation(g, reinit=True)
+    gs._upload(sim)
+    sim.write("youngs_modulus", np.asarray(E, np.float32))
+    sim.initialize()
+    sim.record(steps, ckpt)
+    return sim.adjoint(W, U)
+
+
 def test_autograd_function(built):
     from diffmpm_gb300.autograd import explicit_run
     gs, g, info = workloads.differentiation(D, **CASE)
@@ -157,10 +167,39 @@ def test_autograd_function(built):
     x, v = explicit_run(gs, g, E, velocity=v0, checkpoint_steps=8)
     L = (x * torch.tensor(W, device=dev)).sum() + (v * torch.tensor(U, device=dev)).sum()
     L.backward()
-    sim = gs.simulation(g, reinit=True)
-    direct = sim.adjoint(W, U)
+    direct = _direct_adjoint(gs, g, info["E"], W, U, CASE["sim_steps"])
     assert np.array_equal(E.grad.cpu().numpy(), direct["youngs_modulus"])
     assert np.array_equal(v0.grad.cpu().numpy(), direct["velocity"])
+
+
+def test_autograd_function_is_reentrant(built):
+    """Two forwards with different E before either backward, then the two
+    backwards in reverse order, then a forward-only evaluation between a
+    forward and its backward: every gradient equals the one of the same run
+    differentiated alone (each forward records into its own simulation)."""
+    from diffmpm_gb300.autograd import explicit_run
+    gs, g, info = workloads.differentiation(D, **CASE)
+    n = info["np"]
+    W, U = seeds(n, 9)
+    dev = torch.device("cuda:0")
+    Es = [info["E"], info["E"] * (1.0 + 0.3 * np.sin(np.arange(n)))]
+    want = [_direct_adjoint(gs, g, Ek, W, U, CASE["sim_steps"]) for Ek in Es]
+    tW, tU = torch.tensor(W, device=dev), torch.tensor(U, device=dev)
+    leaves = [torch.tensor(Ek, dtype=torch.float32, device=dev, requires_grad=True) for Ek in Es]
+    losses = []
+    for E in leaves:
+        x, v = explicit_run(gs, g, E, checkpoint_steps=8)
+        losses.append((x * tW).sum() + (v * tU).sum())
+    for k in (1, 0):
+        losses[k].backward()
+        assert np.array_equal(leaves[k].grad.cpu().numpy(), want[k]["youngs_modulus"]), k
+    E = torch.tensor(Es[0], dtype=torch.float32, device=dev, requires_grad=True)
+    x, v = explicit_run(gs, g, E, checkpoint_steps=8)
+    L = (x * tW).sum() + (v * tU).sum()
+    with torch.no_grad():
+        explicit_run(gs, g, torch.tensor(Es[1], dtype=torch.float32, device=dev), checkpoint_steps=8)
+    L.backward()
+    assert np.array_equal(E.grad.cpu().numpy(), want[0]["youngs_modulus"])
 
 
 @pytest.mark.parametrize("scheme", ["usf", "usl"])

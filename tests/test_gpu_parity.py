@@ -8,9 +8,11 @@ at the reference's own decimals.
 A field whose exact value is zero (the stress of a block in free fall) holds
 only float32 round-off in both implementations, and the two round-offs differ
 because the nodal sums are accumulated in different orders.  For such a field
-the check is against the float64 oracle instead: the GPU must be as close to
-float64 as the float32 restatement of the reference is (within 3x), which is
-the "error vs FP64" criterion.
+(stress, strain and the centroid volumetric strain only) the check may pass
+against the float64 oracle instead: the GPU must be as close to float64 as the
+float32 restatement of the reference is (within 3x), which is the "error vs
+FP64" criterion.  Every field that passes that way is listed at the end of the
+run; any other field must meet the tolerance itself.
 """
 import numpy as np
 import pytest
@@ -64,19 +66,30 @@ def start_pair(builder, reinit=True, **kw):
 FLOOR = {"stress": 1e-3, "strain": 1e-9, "volumetric_strain_centroid": 1e-9}
 
 
+# Every check that passed through the round-off floor or the float64
+# criterion instead of the plain tolerance: (check, rel. error against the
+# float32 oracle, how it passed); printed at the end of the run.
+FALLBACKS = []
+
+
 def close(name, gpu, f32, f64, tol, field=None):
-    """``gpu`` matches the float32 oracle within ``tol``, or differs from it by
-    less than the round-off floor, or is as close to float64 as the float32
-    oracle is (within 3x)."""
+    """``gpu`` matches the float32 oracle within ``tol``.  Only for the fields
+    of ``FLOOR``, whose exact value can be zero, a miss may instead pass by
+    differing from the float32 oracle by less than the round-off floor, or by
+    being as close to float64 as the float32 oracle is (within 3x); each such
+    pass is recorded in ``FALLBACKS``."""
     e = rel(gpu, f32)
     if e <= tol:
         return e
     floor = FLOOR.get(field)
+    assert floor is not None, (name, e, f"misses {tol:g} on a field that is not zero-valued")
     diff = np.linalg.norm(np.asarray(gpu, np.float64) - np.asarray(f32, np.float64))
-    if floor is not None and diff <= floor * np.sqrt(np.size(gpu)):
+    if diff <= floor * np.sqrt(np.size(gpu)):
+        FALLBACKS.append((name, e, f"within the round-off floor {floor:g}"))
         return e
     e_gpu, e_ref = rel(gpu, f64), rel(f32, f64)
     assert e_gpu <= max(3.0 * e_ref, tol), (name, e, e_gpu, e_ref)
+    FALLBACKS.append((name, e, f"float64 criterion: GPU {e_gpu:.2e} vs float32 oracle {e_ref:.2e}"))
     return e
 
 

@@ -126,3 +126,20 @@ def test_mpm_rejects_bad_output_and_solver(tmp_path):
     path = _edit(tmp_path / "b", 'type = "MPMExplicit"', 'type = "MPMImplicit"')
     with pytest.raises(ValueError, match="solver"):
         D.MPM(path)
+
+
+def test_npz_writer_file_names(tmp_path):
+    """particles_<step>.npz with the step zero-padded to the digits of
+    max_steps (the names the reference's benchmark readers open)."""
+    import numpy as np
+    from diffmpm_gb300.writers import NPZWriter
+    w = NPZWriter()
+    a = {"loc": np.zeros((2, 2), np.float32)}
+    for step, max_steps, name in [(0, 1000, "particles_0000.npz"), (5, 1000, "particles_0005.npz"),
+                                  (10, 1000, "particles_0010.npz"), (999, 1000, "particles_0999.npz"),
+                                  (0, 10, "particles_00.npz"), (7, 999, "particles_007.npz"),
+                                  (12345, 100, "particles_12345.npz")]:
+        w.write((a, step), None, out_dir=tmp_path / str(max_steps), max_steps=max_steps)
+        f = tmp_path / str(max_steps) / name
+        assert f.exists(), name
+        np.testing.assert_array_equal(np.load(f)["loc"], a["loc"])
