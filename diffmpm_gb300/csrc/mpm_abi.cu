@@ -206,6 +206,7 @@ StepConfig step_config(const MpmHandle* h) {
     c.usl = h->usl;
     c.reinit = h->reinit;
     c.traction = h->has_trac;
+    c.tile_counter = h->tile_counter;
     return c;
 }
 
@@ -608,6 +609,7 @@ int mpm_create(const MpmDesc* d, MpmHandle** out) {
     A(&h->snap_ctl, 1);
     A(&h->ds, 1);
     A(&h->ctl, 1);
+    A(&h->tile_counter, 2);
     A(&h->d_ptrs, 16);
 #undef A
     cudaError_t e = cudaMallocHost(&h->h_ctl, sizeof(Control));
@@ -639,6 +641,7 @@ int mpm_create(const MpmDesc* d, MpmHandle** out) {
     if (cudaMemset(h->cflag, 0, h->ncell) != cudaSuccess) r = MPM_ERR_CUDA;
     Control c{};
     up(h->ctl, &c, sizeof c);
+    if (cudaMemset(h->tile_counter, 0, 2 * sizeof(int)) != cudaSuccess) r = MPM_ERR_CUDA;
     if (r != MPM_OK) return failc(r, "initialisation of the nodal state failed");
 
     // tiles

@@ -17,6 +17,7 @@
 // two cells away sets ST_DRIFT_VIOLATION and the host rolls the block back.
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <cstdlib>
 #include "mpm_device.cuh"
 #include "mpm_kernels.h"
 
@@ -542,6 +543,216 @@ k_nodal_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__ ti
     nodal_kinematics_tile<REINIT>(S, tiles[blockIdx.x], ctl, k);
 }
 
+// ---------------------------------------------------------------------------
+// Persistent nodal kinematics: a grid of resident CTAs, each looping over
+// tiles, with the global round trips of the next tiles in flight while the
+// current tile is summed.  Iteration i of a CTA works on tile t_i and
+//   * issues the row staging of t_{i+1} (its cell-row starts arrived during
+//     iteration i-1) into the other half of a double buffer,
+//   * issues the tile set-up loads of t_{i+2} (row starts, occupancy and
+//     drift flags of the sort-cells around it) into registers,
+//   * fetches the index t_{i+3} (one atomic per tile on the launch's tile
+//     counter),
+// then waits only for the staging of t_i.  The first two tiles of a CTA are
+// blockIdx.x and blockIdx.x + gridDim.x; later ones come from the counter in
+// launch order, so CTAs that meet cheap (empty) tiles take more tiles.  The
+// last CTA to finish resets the counter for the next launch.  Every tile is
+// summed exactly as nodal_kinematics_tile sums it (same per-particle function,
+// same order), so results are bitwise those of the one-tile-per-CTA kernel.
+// ---------------------------------------------------------------------------
+struct TileCounter {
+    int next;       // tiles handed out beyond the first 2 * gridDim.x
+    int finished;   // CTAs done
+};
+
+__device__ __forceinline__ int tile_fetch(TileCounter* c, int ntiles) {
+    const int t = 2 * (int)gridDim.x + atomicAdd(&c->next, 1);
+    return t < ntiles ? t : ntiles;
+}
+
+__device__ __forceinline__ void tile_counter_release(TileCounter* c) {
+    __syncthreads();
+    if (threadIdx.x == 0 && atomicAdd(&c->finished, 1) == (int)gridDim.x - 1) {
+        atomicExch(&c->next, 0);
+        atomicExch(&c->finished, 0);
+    }
+}
+
+// Row staging of one tile row for the persistent kernel: the first pass
+// (K1_ROW_P particles) of storage range [rb, re) into buf, one commit group.
+template <bool REINIT>
+__device__ __forceinline__ void nk_stage_row(const SimDev& S, int parity, float (*buf)[K1_ROW_P],
+                                             int rb, int re, int lane) {
+    const float* src[K1_NF] = {S.x, S.y, S.vx, S.vy, REINIT ? S.rho[parity] : S.mass};
+    const int p1 = min(re, rb + K1_ROW_P);
+    for (int q = rb + lane; q < p1; q += 32) {
+        #pragma unroll
+        for (int f = 0; f < K1_NF; ++f) cp_async4(&buf[f][q - rb], src[f] + q);
+    }
+    cp_async_commit();
+}
+
+template <bool REINIT>
+__global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
+k_nodal_kinematics_persistent(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
+                              int ntiles, Control* __restrict__ ctl, int k,
+                              TileCounter* __restrict__ counter) {
+    constexpr int NQ = 12;
+    __shared__ float s_c[NQ][SC_STRIDE];                  // [m, px, py] x corner, per cell
+    __shared__ float s_row[2][TILE_CY][K1_NF][K1_ROW_P];  // staged rows, double buffered
+    __shared__ int s_cs[TILE_CY][33];                     // row starts of the current tile
+    __shared__ TileGeo G;
+    __shared__ int s_fetch[2];
+    const int parity = (load_step(ctl) + k) & 1;
+    const int tid = threadIdx.x, lx = tid & (TILE_CX - 1), ly = tid / TILE_CX;
+
+    // tile t: origin and this thread's set-up loads
+    auto origin = [&](int t, int& c0x, int& c0y) {
+        const int4 T = tiles[t];
+        c0x = T.y * TILE_NX - 1;
+        c0y = T.z * TILE_NY - 1;
+    };
+    auto setup = [&](int t) {
+        TileLoads L{0, 0, 0, 0};
+        if (t < ntiles) {
+            int c0x, c0y;
+            origin(t, c0x, c0y);
+            L = tile_loads(S, c0x, c0y, c0y + ly, lx);
+        }
+        return L;
+    };
+    auto stage = [&](int t, const TileLoads& L, int buf) {
+        // this warp's row of tile t: [start of column c0x, start of column c0x + 32)
+        const int rb = __shfl_sync(0xffffffffu, L.cs, 0), re = __shfl_sync(0xffffffffu, L.cs32, 0);
+        if (t < ntiles) nk_stage_row<REINIT>(S, parity, s_row[buf][ly], rb, re, lx);
+        else cp_async_commit();
+    };
+
+    int t0 = blockIdx.x, t1 = blockIdx.x + gridDim.x;
+    t0 = t0 < ntiles ? t0 : ntiles;
+    t1 = t1 < ntiles ? t1 : ntiles;
+    if (tid == 0) s_fetch[0] = t1 < ntiles ? tile_fetch(counter, ntiles) : ntiles;
+    TileLoads Lc = setup(t0);          // tile t_i
+    stage(t0, Lc, 0);
+    TileLoads Ln = setup(t1);          // tile t_{i+1}
+    __syncthreads();
+    int t2 = s_fetch[0];
+    int cur = t0, nxt = t1, nnx = t2;
+    #pragma unroll 1
+    for (int i = 0; cur < ntiles; ++i) {
+        const int b = i & 1;
+        // block-wide flags of tile t_i (loads issued two iterations ago)
+        const bool occupied = __syncthreads_or(Lc.occ) != 0;
+        const bool slow = __syncthreads_or(Lc.drift) != 0;
+        // keep the next tiles' loads in flight while t_i is summed
+        stage(nxt, Ln, b ^ 1);
+        const TileLoads Lnn = setup(nnx);
+        if (tid == 0) s_fetch[(i + 1) & 1] = nnx < ntiles ? tile_fetch(counter, ntiles) : ntiles;
+
+        int c0x, c0y;
+        origin(cur, c0x, c0y);
+        const int ci = c0x + lx, cj = c0y + ly;
+        const bool node_ok = lx < TILE_NX && ly < TILE_NY && c0x + 1 + lx <= S.nx && c0y + 1 + ly <= S.ny;
+        const int node = (c0y + 1 + ly) * (S.nx + 1) + c0x + 1 + lx;
+        const uint16_t ncons = node_ok ? S.ncons[node] : 0;
+        if (!occupied) {
+            if (node_ok) {
+                float vx = flush(S.nvbx[node]), vy = flush(S.nvby[node]);
+                apply_constraint(S, ncons, vx, vy, nullptr, nullptr);
+                S.nm[node] = 0.0f;
+                S.nvax[node] = vx;
+                S.nvay[node] = vy;
+            }
+        } else {
+            const float* __restrict__ rho = S.rho[parity];
+            build_geo(S, c0x, c0y, G);
+            #pragma unroll
+            for (int q = 0; q < NQ; ++q) s_c[q][tid] = 0.0f;
+            s_cs[ly][lx] = Lc.cs;
+            if (lx == 0) s_cs[ly][32] = Lc.cs32;
+            __syncthreads();
+            if (!slow) {
+                const int* cs = s_cs[ly];
+                const int cb = cs[lx], ce = cs[lx + 1], rb = cs[0], re = cs[32];
+                const CellGeo g = geo_of(G, lx + 1, ly + 1);
+                const float V0 = (REINIT && ce > cb) ? fdv(S.vol_el, (float)(ce - cb)) : 0.0f;
+                float acc[NQ];
+                #pragma unroll
+                for (int q = 0; q < NQ; ++q) acc[q] = 0.0f;
+                float (*buf)[K1_ROW_P] = s_row[b][ly];
+                cp_async_wait<1>();        // the staging of t_i (t_{i+1}'s may stay in flight)
+                __syncwarp();
+                auto add = [&](int j) {
+                    const float m = REINIT ? fm(V0, buf[4][j]) : buf[4][j];
+                    float cc[NQ];
+                    mass_contrib(buf[0][j], buf[1][j], buf[2][j], buf[3][j], m, g.cx, g.rx, g.cy, g.ry,
+                                 cc);
+                    #pragma unroll
+                    for (int q = 0; q < NQ; ++q) acc[q] = fa(acc[q], cc[q]);
+                };
+                {
+                    const int p1 = min(rb + K1_ROW_P, re);
+                    const int lo = max(cb, rb), hi = min(ce, p1);
+                    #pragma unroll 1
+                    for (int q = lo; q < hi; ++q) add(q - rb);
+                }
+                if (re - rb > K1_ROW_P) {
+                    // a crowded row: its further passes are staged here, in order
+                    const float* const src[K1_NF] = {S.x, S.y, S.vx, S.vy, REINIT ? rho : S.mass};
+                    __syncwarp();
+                    row_pass<K1_NF, K1_ROW_P>(buf, src, rb + K1_ROW_P, re, cb, ce, lx,
+                                              [&](int, int j) { add(j); });
+                }
+                #pragma unroll
+                for (int q = 0; q < NQ; ++q) s_c[q][tid] = acc[q];
+            } else if (ci >= 0 && ci < S.nx && cj >= 0 && cj < S.ny) {
+                const CellGeo g = geo_of(G, lx + 1, ly + 1);
+                float V0 = 0.0f;
+                if (REINIT) {
+                    const int cnt = count_cell(S, ci, cj, g);
+                    if (cnt) V0 = fdv(S.vol_el, (float)cnt);
+                }
+                visit_cell(S, ci, cj, g, [&](int q) {
+                    const float m = REINIT ? fm(V0, rho[q]) : S.mass[q];
+                    float cc[NQ];
+                    mass_contrib(S.x[q], S.y[q], S.vx[q], S.vy[q], m, g.cx, g.rx, g.cy, g.ry, cc);
+                    #pragma unroll
+                    for (int q2 = 0; q2 < NQ; ++q2) s_c[q2][tid] = fa(s_c[q2][tid], cc[q2]);
+                });
+            }
+            __syncthreads();
+            if (node_ok) {
+                const float mass = node_sum(s_c + 0, tid);
+                const float pxn = flush(node_sum(s_c + 4, tid));
+                const float pyn = flush(node_sum(s_c + 8, tid));
+                float vx, vy;
+                if (mass == 0.0f) {
+                    vx = S.nvbx[node];
+                    vy = S.nvby[node];
+                } else {
+                    vx = fdv(pxn, mass);
+                    vy = fdv(pyn, mass);
+                }
+                vx = flush(vx);
+                vy = flush(vy);
+                apply_constraint(S, ncons, vx, vy, nullptr, nullptr);
+                S.nm[node] = mass;
+                S.nvax[node] = vx;
+                S.nvay[node] = vy;
+            }
+        }
+        // rotate the pipeline: t_{i+1} -> t_i, t_{i+2} -> t_{i+1}
+        __syncthreads();   // s_fetch visible; s_c, s_cs, G free for the next tile
+        cur = nxt;
+        nxt = nnx;
+        nnx = s_fetch[(i + 1) & 1];
+        Lc = Ln;
+        Ln = Lnn;
+    }
+    cp_async_wait<0>();
+    tile_counter_release(counter);
+}
+
 template <bool REINIT>
 __global__ void __launch_bounds__(TILE_THREADS, TILE_CTAS_LIGHT)
 k_nodal_kinematics_batch(const TileDesc* __restrict__ td, int k) {
@@ -1021,17 +1232,48 @@ static void prefer_shared(K kernel) {
     }
 }
 
+// Resident CTAs of a persistent kernel on the current device (once per kernel).
+template <class K>
+static int resident_ctas(K kernel) {
+    static int n = 0;
+    if (!n) {
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, TILE_THREADS, 0);
+        n = sms * (per > 0 ? per : 1);
+    }
+    return n;
+}
+
+static bool legacy_tiles() {
+    static int v = -1;
+    if (v < 0) {
+        const char* e = getenv("MPM_LEGACY_TILES");
+        v = (e && e[0] == '1') ? 1 : 0;
+    }
+    return v == 1;
+}
+
 template <bool REINIT>
 static void nodal_kinematics(const SimDev& S, const int4* tiles, int ntiles, Control* ctl,
-                             int k, cudaStream_t s) {
-    prefer_shared(k_nodal_kinematics<REINIT>);
-    k_nodal_kinematics<REINIT><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl, k);
+                             int k, TileCounter* counter, cudaStream_t s) {
+    if (legacy_tiles() || !counter) {
+        prefer_shared(k_nodal_kinematics<REINIT>);
+        k_nodal_kinematics<REINIT><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl, k);
+        return;
+    }
+    prefer_shared(k_nodal_kinematics_persistent<REINIT>);
+    const int grid = min(ntiles, resident_ctas(k_nodal_kinematics_persistent<REINIT>));
+    k_nodal_kinematics_persistent<REINIT><<<grid, TILE_THREADS, 0, s>>>(S, tiles, ntiles, ctl, k,
+                                                                         counter);
 }
 
 cudaError_t launch_nodal_kinematics(const StepConfig& c, const SimDev& S, const int4* tiles,
                                     int ntiles, Control* ctl, int k, cudaStream_t s) {
-    if (c.reinit) nodal_kinematics<true>(S, tiles, ntiles, ctl, k, s);
-    else nodal_kinematics<false>(S, tiles, ntiles, ctl, k, s);
+    TileCounter* counter = reinterpret_cast<TileCounter*>(c.tile_counter);
+    if (c.reinit) nodal_kinematics<true>(S, tiles, ntiles, ctl, k, counter, s);
+    else nodal_kinematics<false>(S, tiles, ntiles, ctl, k, counter, s);
     return cudaGetLastError();
 }
 

@@ -12,8 +12,14 @@ if str(TESTS) not in sys.path:
     sys.path.insert(0, str(TESTS))
 
 
+def pytest_addoption(parser):
+    parser.addoption("--run-long", action="store_true", default=False,
+                     help="also run the tests marked long (full-length runs against the oracle)")
+
+
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+    config.addinivalue_line("markers", "long: a full-length run against the oracle (--run-long)")
 
 
 def _have_gpu() -> bool:
@@ -28,6 +34,11 @@ def _have_gpu() -> bool:
 
 
 def pytest_collection_modifyitems(config, items):
+    if not config.getoption("--run-long"):
+        skip_long = pytest.mark.skip(reason="long run: pass --run-long")
+        for it in items:
+            if it.get_closest_marker("long"):
+                it.add_marker(skip_long)
     gpu_items = [it for it in items if it.get_closest_marker("gpu")]
     if gpu_items and not _have_gpu():
         skip = pytest.mark.skip(reason="no CUDA GPU on this machine")
