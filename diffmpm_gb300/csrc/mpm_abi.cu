@@ -206,7 +206,6 @@ StepConfig step_config(const MpmHandle* h) {
     c.usl = h->usl;
     c.reinit = h->reinit;
     c.traction = h->has_trac;
-    c.tile_counter = h->tile_counter;
     return c;
 }
 
@@ -266,19 +265,23 @@ int check_status(MpmHandle* h, int& st) {
 }
 
 int alloc_particles(MpmHandle* h, int64_t n) {
+    // the step kernels stage particle rows in 16-byte pieces, which may read
+    // up to 3 slots past the last particle: the float arrays hold a multiple
+    // of 4 slots
+    const int64_t n4 = (n + 3) & ~int64_t(3);
     for (int k = 0; k < 2; ++k) {
         PSet& p = h->ps[k];
         float** f32[] = {&p.x, &p.y, &p.vx, &p.vy, &p.sxx[0], &p.sxx[1], &p.syy[0], &p.syy[1],
                          &p.szz[0], &p.szz[1], &p.sxy[0], &p.sxy[1], &p.exx, &p.eyy, &p.exy,
                          &p.rho[0], &p.rho[1], &p.vsc[0], &p.vsc[1]};
-        for (float** f : f32) TRY(dalloc(h, f, n));
+        for (float** f : f32) TRY(dalloc(h, f, n4));
         if (!h->reinit) {
-            TRY(dalloc(h, &p.mass, n));
-            TRY(dalloc(h, &p.psize, n));
+            TRY(dalloc(h, &p.mass, n4));
+            TRY(dalloc(h, &p.psize, n4));
         }
         if (!h->reinit || h->ndim == 1) {   // 1-D keeps the updated volume for its forces kernel
-            TRY(dalloc(h, &p.vol[0], n));
-            TRY(dalloc(h, &p.vol[1], n));
+            TRY(dalloc(h, &p.vol[0], n4));
+            TRY(dalloc(h, &p.vol[1], n4));
         }
         TRY(dalloc(h, &p.mat, n));
         TRY(dalloc(h, &p.pid, n));
@@ -609,7 +612,6 @@ int mpm_create(const MpmDesc* d, MpmHandle** out) {
     A(&h->snap_ctl, 1);
     A(&h->ds, 1);
     A(&h->ctl, 1);
-    A(&h->tile_counter, 2);
     A(&h->d_ptrs, 16);
 #undef A
     cudaError_t e = cudaMallocHost(&h->h_ctl, sizeof(Control));
@@ -641,7 +643,6 @@ int mpm_create(const MpmDesc* d, MpmHandle** out) {
     if (cudaMemset(h->cflag, 0, h->ncell) != cudaSuccess) r = MPM_ERR_CUDA;
     Control c{};
     up(h->ctl, &c, sizeof c);
-    if (cudaMemset(h->tile_counter, 0, 2 * sizeof(int)) != cudaSuccess) r = MPM_ERR_CUDA;
     if (r != MPM_OK) return failc(r, "initialisation of the nodal state failed");
 
     // tiles

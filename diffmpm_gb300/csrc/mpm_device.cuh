@@ -51,6 +51,12 @@ __device__ __forceinline__ void cp_async4(void* smem_dst, const void* gmem_src) 
     const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(gmem_src) : "memory");
 }
+// 16-byte global -> shared copy through L2 only (cp.async.cg); both
+// addresses 16-byte aligned.
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
+    const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem_src) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() {
     asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
@@ -270,6 +276,36 @@ __device__ __forceinline__ void row_pass(float (*buf)[P], const float* const (&s
             #pragma unroll
             for (int k = 0; k < NF; ++k)
                 if (src[k]) cp_async4(&buf[k][q - p0], src[k] + q);
+        }
+        cp_async_commit();
+        cp_async_wait<0>();
+        __syncwarp();
+        const int lo = max(cb, p0), hi = min(ce, p1);
+        #pragma unroll 1
+        for (int q = lo; q < hi; ++q) f(q, q - p0);
+        __syncwarp();
+    }
+}
+
+// row_pass with 16-byte copies: pass k stages storage slots
+// [rb4 + kP, rb4 + (k+1)P) (rb4 = rb rounded down to a multiple of 4, P a
+// multiple of 4) of every field with one cp.async.cg per 16-byte piece, and
+// f(q, j) finds slot q at buf[.][j], j = q - (rb4 + kP).  Every source array
+// must start on a 16-byte boundary and hold a multiple of 4 slots (the last
+// piece may read up to 3 slots past re).  Same visiting order as row_pass.
+template <int NF, int P, class F>
+__device__ __forceinline__ void row_pass16(float (*buf)[P], const float* const (&src)[NF], int rb,
+                                           int re, int cb, int ce, int lane, F&& f) {
+    static_assert(P % 4 == 0, "passes start on 16-byte boundaries");
+    #pragma unroll 1
+    for (int p0 = rb & ~3; p0 < re; p0 += P) {
+        const int p1 = min(p0 + P, re);
+        #pragma unroll
+        for (int k = 0; k < NF; ++k) {
+            if (!src[k]) continue;
+            #pragma unroll
+            for (int o = 4 * lane; o < P; o += 128)
+                if (p0 + o < p1) cp_async16(&buf[k][o], src[k] + p0 + o);
         }
         cp_async_commit();
         cp_async_wait<0>();

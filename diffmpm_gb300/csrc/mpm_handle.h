@@ -107,7 +107,6 @@ struct MpmHandle {
     mpm::SimDev* ds = nullptr;
     mpm::Control* ctl = nullptr;
     mpm::Control* h_ctl = nullptr;   // pinned mirror
-    int* tile_counter = nullptr;     // tile queue of the persistent step kernels (2 ints, zero between launches)
     int4* dtiles = nullptr;
     int ntiles = 0;
     int64_t step = 0;

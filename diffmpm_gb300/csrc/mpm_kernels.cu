@@ -178,41 +178,34 @@ constexpr int GEO_C = TILE_CX + 3;    // geometry table columns k <-> cell c0x -
 constexpr int GEO_R = TILE_CY + 3;    // geometry table rows    k <-> cell c0y - 1 + k
 
 // Per-tile cell geometry: bounds, centre and 2/width of columns and rows, formed
-// exactly as cell_geo forms them.
+// exactly as cell_geo forms them, one 16-byte entry per column and per row.
 struct TileGeo {
-    float x0[GEO_C], x1[GEO_C], cx[GEO_C], rx[GEO_C];
-    float y0[GEO_R], y1[GEO_R], cy[GEO_R], ry[GEO_R];
+    float4 col[GEO_C];   // (x0, x1, cx, rx) of cell column c0x - 1 + k
+    float4 row[GEO_R];   // (y0, y1, cy, ry) of cell row    c0y - 1 + k
 };
+
+__device__ __forceinline__ float4 axis_geo(int i, float h) {
+    const float a = node_coord(i, h), b = node_coord(i + 1, h);
+    return make_float4(a, b, fm(fa(a, b), 0.5f), fdv(2.0f, fs(b, a)));
+}
 
 __device__ __forceinline__ void build_geo(const SimDev& S, int c0x, int c0y, TileGeo& G) {
     const int t = threadIdx.x;
-    if (t < GEO_C) {
-        const int i = c0x - 1 + t;
-        const float a = node_coord(i, S.hx), b = node_coord(i + 1, S.hx);
-        G.x0[t] = a;
-        G.x1[t] = b;
-        G.cx[t] = fm(fa(a, b), 0.5f);
-        G.rx[t] = fdv(2.0f, fs(b, a));
-    } else if (t >= 64 && t < 64 + GEO_R) {
-        const int k = t - 64, j = c0y - 1 + k;
-        const float a = node_coord(j, S.hy), b = node_coord(j + 1, S.hy);
-        G.y0[k] = a;
-        G.y1[k] = b;
-        G.cy[k] = fm(fa(a, b), 0.5f);
-        G.ry[k] = fdv(2.0f, fs(b, a));
-    }
+    if (t < GEO_C) G.col[t] = axis_geo(c0x - 1 + t, S.hx);
+    else if (t >= 64 && t < 64 + GEO_R) G.row[t - 64] = axis_geo(c0y - 1 + (t - 64), S.hy);
 }
 
 __device__ __forceinline__ CellGeo geo_of(const TileGeo& G, int kc, int kr) {
+    const float4 c = G.col[kc], r = G.row[kr];
     CellGeo g;
-    g.x0 = G.x0[kc];
-    g.x1 = G.x1[kc];
-    g.cx = G.cx[kc];
-    g.rx = G.rx[kc];
-    g.y0 = G.y0[kr];
-    g.y1 = G.y1[kr];
-    g.cy = G.cy[kr];
-    g.ry = G.ry[kr];
+    g.x0 = c.x;
+    g.x1 = c.y;
+    g.cx = c.z;
+    g.rx = c.w;
+    g.y0 = r.x;
+    g.y1 = r.y;
+    g.cy = r.z;
+    g.ry = r.w;
     return g;
 }
 
@@ -442,14 +435,16 @@ __device__ __forceinline__ void force_contrib(const SimDev& S, int q, const Forc
 //   (element.py:191-202), velocity constraints (element.py:331-334).
 // ---------------------------------------------------------------------------
 constexpr int K1_NF = 5;   // x, y, vx, vy, rho (solve_jit) or mass (solve)
-constexpr int K1_ROW_P = 128;   // particles of a row per pass (three CTAs per SM)
+// storage slots of a row per pass: a row of 4 particles in each of 32 cells,
+// starting anywhere in a 16-byte piece, fits one pass (three CTAs per SM)
+constexpr int K1_ROW_P = 132;
 
 template <bool REINIT>
 __device__ __forceinline__ void nodal_kinematics_tile(const SimDev& S, const int4 T,
                                                       Control* __restrict__ ctl, int k) {
     constexpr int NQ = 12;
     __shared__ float s_c[NQ][SC_STRIDE];               // [m, px, py] x corner, per cell
-    __shared__ float s_row[TILE_CY][K1_NF][K1_ROW_P];  // staged particles of each cell row
+    __shared__ __align__(16) float s_row[TILE_CY][K1_NF][K1_ROW_P];  // staged particles of each cell row
     __shared__ int s_cs[TILE_CY][33];
     __shared__ TileGeo G;
     const int parity = (load_step(ctl) + k) & 1;
@@ -461,11 +456,6 @@ __device__ __forceinline__ void nodal_kinematics_tile(const SimDev& S, const int
     const int node = (c0y + 1 + ly) * (S.nx + 1) + c0x + 1 + lx;
     const uint16_t ncons = node_ok ? S.ncons[node] : 0;   // node-phase input, fetched early
     const TileLoads L = tile_loads(S, c0x, c0y, cj, lx);
-    build_geo(S, c0x, c0y, G);
-    #pragma unroll
-    for (int q = 0; q < NQ; ++q) s_c[q][tid] = 0.0f;
-    s_cs[ly][lx] = L.cs;
-    if (lx == 0) s_cs[ly][32] = L.cs32;
     if (!__syncthreads_or(L.occ)) {
         // no particle in the tile: every node is massless and keeps its
         // velocity (the node phase below with all sums zero)
@@ -478,6 +468,11 @@ __device__ __forceinline__ void nodal_kinematics_tile(const SimDev& S, const int
         }
         return;
     }
+    build_geo(S, c0x, c0y, G);
+    #pragma unroll
+    for (int q = 0; q < NQ; ++q) s_c[q][tid] = 0.0f;
+    s_cs[ly][lx] = L.cs;
+    if (lx == 0) s_cs[ly][32] = L.cs32;
     const bool slow = __syncthreads_or(L.drift) != 0;
 
     if (!slow) {
@@ -490,7 +485,7 @@ __device__ __forceinline__ void nodal_kinematics_tile(const SimDev& S, const int
         for (int k = 0; k < NQ; ++k) acc[k] = 0.0f;
         const float* const src[K1_NF] = {S.x, S.y, S.vx, S.vy, REINIT ? rho : S.mass};
         float (*buf)[K1_ROW_P] = s_row[ly];
-        row_pass<K1_NF, K1_ROW_P>(buf, src, cs[0], cs[32], cb, ce, lx, [&](int, int j) {
+        row_pass16<K1_NF, K1_ROW_P>(buf, src, cs[0], cs[32], cb, ce, lx, [&](int, int j) {
             const float m = REINIT ? fm(V0, buf[4][j]) : buf[4][j];
             float cc[NQ];
             mass_contrib(buf[0][j], buf[1][j], buf[2][j], buf[3][j], m, g.cx, g.rx, g.cy, g.ry, cc);
@@ -536,221 +531,11 @@ __device__ __forceinline__ void nodal_kinematics_tile(const SimDev& S, const int
     }
 }
 
-template <bool REINIT>
-__global__ void __launch_bounds__(TILE_THREADS, TILE_CTAS_LIGHT)
+template <bool REINIT, int MINB = TILE_CTAS_LIGHT>
+__global__ void __launch_bounds__(TILE_THREADS, MINB)
 k_nodal_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
                    Control* __restrict__ ctl, int k) {
     nodal_kinematics_tile<REINIT>(S, tiles[blockIdx.x], ctl, k);
-}
-
-// ---------------------------------------------------------------------------
-// Persistent nodal kinematics: a grid of resident CTAs, each looping over
-// tiles, with the global round trips of the next tiles in flight while the
-// current tile is summed.  Iteration i of a CTA works on tile t_i and
-//   * issues the row staging of t_{i+1} (its cell-row starts arrived during
-//     iteration i-1) into the other half of a double buffer,
-//   * issues the tile set-up loads of t_{i+2} (row starts, occupancy and
-//     drift flags of the sort-cells around it) into registers,
-//   * fetches the index t_{i+3} (one atomic per tile on the launch's tile
-//     counter),
-// then waits only for the staging of t_i.  The first two tiles of a CTA are
-// blockIdx.x and blockIdx.x + gridDim.x; later ones come from the counter in
-// launch order, so CTAs that meet cheap (empty) tiles take more tiles.  The
-// last CTA to finish resets the counter for the next launch.  Every tile is
-// summed exactly as nodal_kinematics_tile sums it (same per-particle function,
-// same order), so results are bitwise those of the one-tile-per-CTA kernel.
-// ---------------------------------------------------------------------------
-struct TileCounter {
-    int next;       // tiles handed out beyond the first 2 * gridDim.x
-    int finished;   // CTAs done
-};
-
-__device__ __forceinline__ int tile_fetch(TileCounter* c, int ntiles) {
-    const int t = 2 * (int)gridDim.x + atomicAdd(&c->next, 1);
-    return t < ntiles ? t : ntiles;
-}
-
-__device__ __forceinline__ void tile_counter_release(TileCounter* c) {
-    __syncthreads();
-    if (threadIdx.x == 0 && atomicAdd(&c->finished, 1) == (int)gridDim.x - 1) {
-        atomicExch(&c->next, 0);
-        atomicExch(&c->finished, 0);
-    }
-}
-
-// Row staging of one tile row for the persistent kernel: the first pass
-// (K1_ROW_P particles) of storage range [rb, re) into buf, one commit group.
-template <bool REINIT>
-__device__ __forceinline__ void nk_stage_row(const SimDev& S, int parity, float (*buf)[K1_ROW_P],
-                                             int rb, int re, int lane) {
-    const float* src[K1_NF] = {S.x, S.y, S.vx, S.vy, REINIT ? S.rho[parity] : S.mass};
-    const int p1 = min(re, rb + K1_ROW_P);
-    for (int q = rb + lane; q < p1; q += 32) {
-        #pragma unroll
-        for (int f = 0; f < K1_NF; ++f) cp_async4(&buf[f][q - rb], src[f] + q);
-    }
-    cp_async_commit();
-}
-
-template <bool REINIT>
-__global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
-k_nodal_kinematics_persistent(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
-                              int ntiles, Control* __restrict__ ctl, int k,
-                              TileCounter* __restrict__ counter) {
-    constexpr int NQ = 12;
-    __shared__ float s_c[NQ][SC_STRIDE];                  // [m, px, py] x corner, per cell
-    __shared__ float s_row[2][TILE_CY][K1_NF][K1_ROW_P];  // staged rows, double buffered
-    __shared__ int s_cs[TILE_CY][33];                     // row starts of the current tile
-    __shared__ TileGeo G;
-    __shared__ int s_fetch[2];
-    const int parity = (load_step(ctl) + k) & 1;
-    const int tid = threadIdx.x, lx = tid & (TILE_CX - 1), ly = tid / TILE_CX;
-
-    // tile t: origin and this thread's set-up loads
-    auto origin = [&](int t, int& c0x, int& c0y) {
-        const int4 T = tiles[t];
-        c0x = T.y * TILE_NX - 1;
-        c0y = T.z * TILE_NY - 1;
-    };
-    auto setup = [&](int t) {
-        TileLoads L{0, 0, 0, 0};
-        if (t < ntiles) {
-            int c0x, c0y;
-            origin(t, c0x, c0y);
-            L = tile_loads(S, c0x, c0y, c0y + ly, lx);
-        }
-        return L;
-    };
-    auto stage = [&](int t, const TileLoads& L, int buf) {
-        // this warp's row of tile t: [start of column c0x, start of column c0x + 32)
-        const int rb = __shfl_sync(0xffffffffu, L.cs, 0), re = __shfl_sync(0xffffffffu, L.cs32, 0);
-        if (t < ntiles) nk_stage_row<REINIT>(S, parity, s_row[buf][ly], rb, re, lx);
-        else cp_async_commit();
-    };
-
-    int t0 = blockIdx.x, t1 = blockIdx.x + gridDim.x;
-    t0 = t0 < ntiles ? t0 : ntiles;
-    t1 = t1 < ntiles ? t1 : ntiles;
-    if (tid == 0) s_fetch[0] = t1 < ntiles ? tile_fetch(counter, ntiles) : ntiles;
-    TileLoads Lc = setup(t0);          // tile t_i
-    stage(t0, Lc, 0);
-    TileLoads Ln = setup(t1);          // tile t_{i+1}
-    __syncthreads();
-    int t2 = s_fetch[0];
-    int cur = t0, nxt = t1, nnx = t2;
-    #pragma unroll 1
-    for (int i = 0; cur < ntiles; ++i) {
-        const int b = i & 1;
-        // block-wide flags of tile t_i (loads issued two iterations ago)
-        const bool occupied = __syncthreads_or(Lc.occ) != 0;
-        const bool slow = __syncthreads_or(Lc.drift) != 0;
-        // keep the next tiles' loads in flight while t_i is summed
-        stage(nxt, Ln, b ^ 1);
-        const TileLoads Lnn = setup(nnx);
-        if (tid == 0) s_fetch[(i + 1) & 1] = nnx < ntiles ? tile_fetch(counter, ntiles) : ntiles;
-
-        int c0x, c0y;
-        origin(cur, c0x, c0y);
-        const int ci = c0x + lx, cj = c0y + ly;
-        const bool node_ok = lx < TILE_NX && ly < TILE_NY && c0x + 1 + lx <= S.nx && c0y + 1 + ly <= S.ny;
-        const int node = (c0y + 1 + ly) * (S.nx + 1) + c0x + 1 + lx;
-        const uint16_t ncons = node_ok ? S.ncons[node] : 0;
-        if (!occupied) {
-            if (node_ok) {
-                float vx = flush(S.nvbx[node]), vy = flush(S.nvby[node]);
-                apply_constraint(S, ncons, vx, vy, nullptr, nullptr);
-                S.nm[node] = 0.0f;
-                S.nvax[node] = vx;
-                S.nvay[node] = vy;
-            }
-        } else {
-            const float* __restrict__ rho = S.rho[parity];
-            build_geo(S, c0x, c0y, G);
-            #pragma unroll
-            for (int q = 0; q < NQ; ++q) s_c[q][tid] = 0.0f;
-            s_cs[ly][lx] = Lc.cs;
-            if (lx == 0) s_cs[ly][32] = Lc.cs32;
-            __syncthreads();
-            if (!slow) {
-                const int* cs = s_cs[ly];
-                const int cb = cs[lx], ce = cs[lx + 1], rb = cs[0], re = cs[32];
-                const CellGeo g = geo_of(G, lx + 1, ly + 1);
-                const float V0 = (REINIT && ce > cb) ? fdv(S.vol_el, (float)(ce - cb)) : 0.0f;
-                float acc[NQ];
-                #pragma unroll
-                for (int q = 0; q < NQ; ++q) acc[q] = 0.0f;
-                float (*buf)[K1_ROW_P] = s_row[b][ly];
-                cp_async_wait<1>();        // the staging of t_i (t_{i+1}'s may stay in flight)
-                __syncwarp();
-                auto add = [&](int j) {
-                    const float m = REINIT ? fm(V0, buf[4][j]) : buf[4][j];
-                    float cc[NQ];
-                    mass_contrib(buf[0][j], buf[1][j], buf[2][j], buf[3][j], m, g.cx, g.rx, g.cy, g.ry,
-                                 cc);
-                    #pragma unroll
-                    for (int q = 0; q < NQ; ++q) acc[q] = fa(acc[q], cc[q]);
-                };
-                {
-                    const int p1 = min(rb + K1_ROW_P, re);
-                    const int lo = max(cb, rb), hi = min(ce, p1);
-                    #pragma unroll 1
-                    for (int q = lo; q < hi; ++q) add(q - rb);
-                }
-                if (re - rb > K1_ROW_P) {
-                    // a crowded row: its further passes are staged here, in order
-                    const float* const src[K1_NF] = {S.x, S.y, S.vx, S.vy, REINIT ? rho : S.mass};
-                    __syncwarp();
-                    row_pass<K1_NF, K1_ROW_P>(buf, src, rb + K1_ROW_P, re, cb, ce, lx,
-                                              [&](int, int j) { add(j); });
-                }
-                #pragma unroll
-                for (int q = 0; q < NQ; ++q) s_c[q][tid] = acc[q];
-            } else if (ci >= 0 && ci < S.nx && cj >= 0 && cj < S.ny) {
-                const CellGeo g = geo_of(G, lx + 1, ly + 1);
-                float V0 = 0.0f;
-                if (REINIT) {
-                    const int cnt = count_cell(S, ci, cj, g);
-                    if (cnt) V0 = fdv(S.vol_el, (float)cnt);
-                }
-                visit_cell(S, ci, cj, g, [&](int q) {
-                    const float m = REINIT ? fm(V0, rho[q]) : S.mass[q];
-                    float cc[NQ];
-                    mass_contrib(S.x[q], S.y[q], S.vx[q], S.vy[q], m, g.cx, g.rx, g.cy, g.ry, cc);
-                    #pragma unroll
-                    for (int q2 = 0; q2 < NQ; ++q2) s_c[q2][tid] = fa(s_c[q2][tid], cc[q2]);
-                });
-            }
-            __syncthreads();
-            if (node_ok) {
-                const float mass = node_sum(s_c + 0, tid);
-                const float pxn = flush(node_sum(s_c + 4, tid));
-                const float pyn = flush(node_sum(s_c + 8, tid));
-                float vx, vy;
-                if (mass == 0.0f) {
-                    vx = S.nvbx[node];
-                    vy = S.nvby[node];
-                } else {
-                    vx = fdv(pxn, mass);
-                    vy = fdv(pyn, mass);
-                }
-                vx = flush(vx);
-                vy = flush(vy);
-                apply_constraint(S, ncons, vx, vy, nullptr, nullptr);
-                S.nm[node] = mass;
-                S.nvax[node] = vx;
-                S.nvay[node] = vy;
-            }
-        }
-        // rotate the pipeline: t_{i+1} -> t_i, t_{i+2} -> t_{i+1}
-        __syncthreads();   // s_fetch visible; s_c, s_cs, G free for the next tile
-        cur = nxt;
-        nxt = nnx;
-        nnx = s_fetch[(i + 1) & 1];
-        Lc = Ln;
-        Ln = Lnn;
-    }
-    cp_async_wait<0>();
-    tile_counter_release(counter);
 }
 
 template <bool REINIT>
@@ -839,6 +624,11 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
         }
     }
     const TileLoads L = tile_loads(S, c0x, c0y, cj, lx);
+    if (!__syncthreads_or(L.occ)) {
+        // no particle in the tile: the nodal update with zero particle forces
+        if (node_ok) nodal_update<VD>(S, node, t, 0.0f, 0.0f, S.nvax[node], S.nvay[node], nmass, ncons);
+        return;
+    }
     build_geo(S, c0x, c0y, G);
     #pragma unroll
     for (int q = 0; q < NQ; ++q) s_c[q][tid] = 0.0f;
@@ -847,11 +637,6 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
     #pragma unroll
     for (int e = 0; e < 2; ++e)
         if (tid + e * TILE_THREADS < NV_W * NV_H) s_v[tid + e * TILE_THREADS] = nv[e];
-    if (!__syncthreads_or(L.occ)) {
-        // no particle in the tile: the nodal update with zero particle forces
-        if (node_ok) nodal_update<VD>(S, node, t, 0.0f, 0.0f, S.nvax[node], S.nvay[node], nmass, ncons);
-        return;
-    }
     const bool slow = __syncthreads_or(L.drift) != 0;
 
     auto cell_velocities = [&](int li, int lj, float* vx, float* vy) {
@@ -881,7 +666,7 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
             s_cellv[ly][1][lx] = size0;
             s_cellv[ly][2][lx] = dvol;
         }
-        const float cy = G.cy[ly + 1], ry = G.ry[ly + 1];   // row geometry (warp-uniform)
+        const float cy = G.row[ly + 1].z, ry = G.row[ly + 1].w;   // row geometry (warp-uniform)
         float acc[NQ];
         #pragma unroll
         for (int k = 0; k < NQ; ++k) acc[k] = 0.0f;
@@ -897,7 +682,7 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
                 if (!USL) cell_velocities(l, ly, nvx, nvy);
                 float cc[NQ];
                 force_contrib<USL, REINIT, TRAC, VD>(S, q, force_in_global<VD>(S, q, parity, REINIT),
-                                                 G.cx[l + 1], G.rx[l + 1], cy, ry,
+                                                 G.col[l + 1].z, G.col[l + 1].w, cy, ry,
                                                  s_cellv[ly][0][l], s_cellv[ly][1][l], nvx, nvy,
                                                  s_cellv[ly][2][l], parity, t, l >= 1 && ly >= 1,
                                                  cc);
@@ -970,11 +755,12 @@ constexpr int G2P_MAP = 160;        // particles of a row whose sort-cell is loo
 // New cell along one axis for a coordinate that was in table column k (cell
 // c = base + k): same, or a neighbour by one, decided against the tabulated
 // bounds; otherwise a full locate.
-__device__ __forceinline__ int moved_axis(float x, const float* lo, const float* hi, int k,
-                                          int nk, int c, float h, int n) {
-    if (x >= lo[k] && x < hi[k]) return c;
-    if (x >= hi[k] && k + 1 < nk && x < hi[k + 1]) return c + 1;
-    if (x < lo[k] && k >= 1 && x >= lo[k - 1]) return c - 1;
+__device__ __forceinline__ int moved_axis(float x, const float4* tab, int k, int nk, int c, float h,
+                                          int n) {
+    const float lo = tab[k].x, hi = tab[k].y;
+    if (x >= lo && x < hi) return c;
+    if (x >= hi && k + 1 < nk && x < tab[k + 1].y) return c + 1;
+    if (x < lo && k >= 1 && x >= tab[k - 1].x) return c - 1;
     return locate_axis(x, h, n);
 }
 
@@ -987,15 +773,143 @@ struct G2PStage {
     static constexpr int DEPTH = USL ? 2 : 4;
 };
 
+// Per-warp staging of a row's particles in chunks of 32 storage slots that
+// start on 16-byte boundaries: chunk c holds slots rb4 + 32c + [0, 32) with
+// rb4 = rb rounded down to a multiple of 4, copied as 16-byte cp.async pieces
+// (8 per field; NF = 4 fields is one piece per lane).  Pieces wholly past the
+// row end re are skipped; the last piece may read up to 3 slots past re,
+// which the particle arrays' padding (a multiple of 4 slots) covers.  Slot q
+// of chunk c lands in buf[c % DEPTH][f][q - rb4 - 32c].
+template <int NF, int DEPTH>
+struct RowStage16 {
+    static constexpr int NP = (NF * 8 + 31) / 32;   // pieces per lane per chunk
+    float* buf;                 // [DEPTH][NF][32]
+    const float* lp[NP];        // this lane's source array for its piece j (null: none)
+    int doff[NP];               // and its offset in a chunk's [NF][32] block
+    int lo, rb4, re, nch;
+
+    // src: the NF source arrays (null entries are not staged)
+    __device__ __forceinline__ RowStage16(float* b, const float* const* src, int rb, int re_, int lane)
+        : buf(b), lo((lane & 7) * 4), rb4(rb & ~3), re(re_), nch(re_ > rb ? (re_ - (rb & ~3) + 31) / 32 : 0) {
+        #pragma unroll
+        for (int j = 0; j < NP; ++j) {
+            const int p = 32 * j + lane, f = p >> 3;
+            // select the field without indexing src by a runtime value
+            const float* ptr = nullptr;
+            #pragma unroll
+            for (int g = 4 * j; g < 4 * j + 4 && g < NF; ++g)
+                if (f == g) ptr = src[g];
+            lp[j] = p < NF * 8 ? ptr : nullptr;
+            doff[j] = f * 32 + lo;
+        }
+    }
+    __device__ __forceinline__ void issue(int c) {
+        if (c < nch) {
+            const int base = rb4 + 32 * c + lo;
+            float* dst = buf + (c % DEPTH) * (NF * 32);
+            #pragma unroll
+            for (int j = 0; j < NP; ++j)
+                if (lp[j] && base < re) cp_async16(dst + doff[j], lp[j] + base);
+        }
+        cp_async_commit();
+    }
+    __device__ __forceinline__ void prime() {
+        #pragma unroll
+        for (int c = 0; c < DEPTH - 1; ++c) issue(c);
+    }
+    // Issue chunk c + DEPTH - 1 and wait until chunk c has landed (visible to
+    // the whole warp).
+    __device__ __forceinline__ const float (*advance(int c))[32] {
+        issue(c + DEPTH - 1);
+        cp_async_wait<DEPTH - 1>();
+        __syncwarp();
+        return reinterpret_cast<const float (*)[32]>(buf + (c % DEPTH) * (NF * 32));
+    }
+};
+
+// G2P of one particle (storage slot q, staged inputs b[.][lane]) in cell
+// (ci, cj) with geometry g and corner nodal values nd[4] = (vx, vy, ax, ay):
+// velocity and position update (particle.py:208-247) and, under USL, the
+// strain/volume/stress update (scheme.py:127-133).  Writes the particle and
+// returns the new position.
+template <bool USL, bool REINIT>
+__device__ __forceinline__ float2 g2p_particle(const SimDev& S, int q, const float (*b)[32], int lane,
+                                               const CellGeo& g, const float4 nd[4], int next) {
+    const float dt = S.dt;
+    const float x = b[GF_X][lane], y = b[GF_Y][lane];
+    const float xi = natural(x, g.cx, g.rx);
+    const float eta = natural(y, g.cy, g.ry);
+    float N[4], nvx[4], nvy[4], nax[4], nay[4];
+    shape4(xi, eta, N);
+    #pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        nvx[k] = nd[k].x;
+        nvy[k] = nd[k].y;
+        nax[k] = nd[k].z;
+        nay[k] = nd[k].w;
+    }
+    const float vhx = dot4(N, nvx), vhy = dot4(N, nvy);
+    float vx, vy;
+    if (S.velocity_update) {
+        vx = vhx;
+        vy = vhy;
+    } else {
+        vx = fa(b[GF_VX][lane], fm(dot4(N, nax), dt));
+        vy = fa(b[GF_VY][lane], fm(dot4(N, nay), dt));
+    }
+    if (S.pvc) {   // particle velocity constraints (an extension; scheme.py:67 leaves a TODO)
+        const uchar2 c = reinterpret_cast<const uchar2*>(S.pvc)[q];
+        if (c.x) vx = S.pvc_vel[c.x - 1];
+        if (c.y) vy = S.pvc_vel[c.y - 1];
+    }
+    const float xn = fa(x, fm(vhx, dt)), yn = fa(y, fm(vhy, dt));
+    S.x[q] = xn;
+    S.y[q] = yn;
+    S.vx[q] = vx;
+    S.vy[q] = vy;
+    if constexpr (USL) {
+        float Gcx[4], Gcy[4], c0, c1, c3;
+        dshape4(0.0f, 0.0f, g.rx, g.ry, Gcx, Gcy);
+        strain_rate4(Gcx, Gcy, nvx, nvy, c0, c1, c3);
+        const float dvol = fm(dt, fa(c0, c1));
+        float Gx[4], Gy[4], r0, r1, r3;
+        dshape4(xi, eta, g.rx, g.ry, Gx, Gy);
+        strain_rate4(Gx, Gy, nvx, nvy, r0, r1, r3);
+        PState p;
+        p.sxx = b[GF_SXX][lane];
+        p.syy = b[GF_SYY][lane];
+        p.szz = b[GF_SZZ][lane];
+        p.sxy = b[GF_SXY][lane];
+        p.exx = b[GF_EXX][lane];
+        p.eyy = b[GF_EYY][lane];
+        p.exy = b[GF_EXY][lane];
+        p.rho = b[GF_RHO][lane];
+        p.vsc = b[GF_VSC][lane];
+        const MatDev& M = S.mats[S.mat[q]];
+        const float Ep = S.E ? S.E[q] : -1.0f;
+        const float f = strain_stress_update(M, Ep, dt, r0, r1, r3, dvol, p);
+        S.sxx[next][q] = p.sxx;
+        S.syy[next][q] = p.syy;
+        S.szz[next][q] = p.szz;
+        S.sxy[next][q] = p.sxy;
+        S.exx[q] = p.exx;
+        S.eyy[q] = p.eyy;
+        S.exy[q] = p.exy;
+        S.rho[next][q] = p.rho;
+        S.vsc[next][q] = p.vsc;
+        if (!REINIT) S.vol[next][q] = fm(b[GF_VOL][lane], f);
+    }
+    return make_float2(xn, yn);
+}
+
 template <bool USL, bool REINIT>
 __device__ __forceinline__ void particle_kinematics_tile(const SimDev& S, const int4 T,
                                                          Control* __restrict__ ctl, int k) {
     constexpr int NF = G2PStage<USL>::NF, DEPTH = G2PStage<USL>::DEPTH;
     __shared__ float4 s_nd[G_W * G_H];    // nodal (vx, vy, ax, ay) of the tile's nodes
-    __shared__ float s_stage[TILE_CY][DEPTH][NF][32];
+    __shared__ __align__(16) float s_stage[TILE_CY][DEPTH][NF][32];
     __shared__ int s_cs[TILE_CY][33];
     __shared__ unsigned char s_map[TILE_CY][G2P_MAP];   // sort-cell of the row's first particles
-    __shared__ int s_sf[TILE_CY][32];     // drift flag of the sort-cell at the start of the step
     __shared__ int s_flag[TILE_CY][32];   // drift flag after this step
     __shared__ int s_status;
     __shared__ TileGeo G;
@@ -1003,15 +917,15 @@ __device__ __forceinline__ void particle_kinematics_tile(const SimDev& S, const 
     const int parity = step & 1, next = parity ^ 1;
     const int tid = threadIdx.x, lane = tid & 31, w = tid / 32;
     const int c0x = T.y * TILE_NX - 1, c0y = T.z * TILE_NY - 1;
-    const float dt = S.dt;
     // row w + 1 of the tile: owned sort-cells c0x+1 .. c0x+31 -> starts cs[0..31]
     const int sj = c0y + 1 + w;
     const bool row_ok = w < TILE_NY && sj < S.ny;
     int rb = 0, re = 0;
+    unsigned sfmask = 0;   // bit l: sort-cell c0x + 1 + l had a drifted particle at the step start
     if (row_ok) {
         const int col = min(c0x + 1 + lane, S.nx);
         s_cs[w][lane] = S.cstart[sj * S.nx + col];
-        s_sf[w][lane] = col < S.nx ? S.cflag[sj * S.nx + col] : 0;
+        sfmask = __ballot_sync(0xffffffffu, col < S.nx && S.cflag[sj * S.nx + col] != 0);
     }
     s_flag[w][lane] = 0;
     __syncwarp();
@@ -1019,28 +933,29 @@ __device__ __forceinline__ void particle_kinematics_tile(const SimDev& S, const 
         rb = s_cs[w][0];
         re = s_cs[w][31];
     }
-    RowStage<NF, DEPTH> st{s_stage[w], {}, rb, re, (re - rb + 31) / 32, lane};
-    st.src[GF_X] = S.x;
-    st.src[GF_Y] = S.y;
-    st.src[GF_VX] = S.vx;
-    st.src[GF_VY] = S.vy;
+    const float* src[NF] = {S.x, S.y, S.vx, S.vy};
     if constexpr (USL) {
-        st.src[GF_SXX] = S.sxx[parity];
-        st.src[GF_SYY] = S.syy[parity];
-        st.src[GF_SZZ] = S.szz[parity];
-        st.src[GF_SXY] = S.sxy[parity];
-        st.src[GF_EXX] = S.exx;
-        st.src[GF_EYY] = S.eyy;
-        st.src[GF_EXY] = S.exy;
-        st.src[GF_RHO] = S.rho[parity];
-        st.src[GF_VSC] = S.vsc[parity];
-        st.src[GF_VOL] = REINIT ? nullptr : S.vol[parity];
+        src[GF_SXX] = S.sxx[parity];
+        src[GF_SYY] = S.syy[parity];
+        src[GF_SZZ] = S.szz[parity];
+        src[GF_SXY] = S.sxy[parity];
+        src[GF_EXX] = S.exx;
+        src[GF_EYY] = S.eyy;
+        src[GF_EXY] = S.exy;
+        src[GF_RHO] = S.rho[parity];
+        src[GF_VSC] = S.vsc[parity];
+        src[GF_VOL] = REINIT ? nullptr : S.vol[parity];
     }
+    RowStage16<NF, DEPTH> st(&s_stage[w][0][0][0], src, rb, re, lane);
+    const int rb4 = st.rb4;
     st.prime();
+    if (!__syncthreads_or(re > rb)) {
+        // no particle stored in the tile's sort-cells: their drift flags clear
+        if (row_ok && lane < TILE_NX && c0x + 1 + lane < S.nx) S.cflag[sj * S.nx + c0x + 1 + lane] = 0;
+        return;
+    }
     if (tid == 0) s_status = 0;
-    // a tile whose rows store no particle only clears its drift flags
-    const bool occupied = __syncthreads_or(re > rb) != 0;
-    if (occupied) {
+    {
         // the node tile, both entries of a thread in flight together (and in
         // flight with the rows' first chunks)
         static_assert(G_W * G_H <= 2 * TILE_THREADS, "two node-tile entries per thread");
@@ -1068,113 +983,76 @@ __device__ __forceinline__ void particle_kinematics_tile(const SimDev& S, const 
     __syncthreads();
     int status = 0;
     const int* cs = s_cs[w];
+    // this row's geometry (a particle still in its sort-cell is in row sj)
+    const float4 rg = G.row[w + 2];
+    const float4* nrow = s_nd + (w + 1) * G_W + 1;   // node (c0x + 1, sj) of the node tile
     #pragma unroll 1
     for (int c = 0; c < st.nch; ++c) {
         const float (*b)[32] = st.advance(c);
-        const int q = rb + 32 * c + lane;
-        if (q >= re) continue;
+        const int q = rb4 + 32 * c + lane;
+        if (q < rb || q >= re) continue;
         const int l = q - rb < G2P_MAP ? s_map[w][q - rb] : cell_of(cs, 30, q);   // sort-cell c0x + 1 + l
+        if (!((sfmask >> l) & 1u)) {
+            // fast path: the particle is in its sort-cell (c0x + 1 + l, sj)
+            const float4 cg = G.col[l + 2];
+            CellGeo g;
+            g.x0 = cg.x;
+            g.x1 = cg.y;
+            g.cx = cg.z;
+            g.rx = cg.w;
+            g.y0 = rg.x;
+            g.y1 = rg.y;
+            g.cy = rg.z;
+            g.ry = rg.w;
+            const float4* a = nrow + l;
+            const float4 nd[4] = {a[0], a[1], a[G_W + 1], a[G_W]};
+            const float2 pn = g2p_particle<USL, REINIT>(S, q, b, lane, g, nd, next);
+            if (!(pn.x >= g.x0 && pn.x < g.x1 && pn.y >= g.y0 && pn.y < g.y1)) {
+                const int si = c0x + 1 + l;
+                const int ni = moved_axis(pn.x, G.col, l + 2, GEO_C, si, S.hx, S.nx);
+                const int nj = moved_axis(pn.y, G.row, w + 2, GEO_R, sj, S.hy, S.ny);
+                s_flag[w][l] = 1;
+                if (ni < 0 || ni >= S.nx || nj < 0 || nj >= S.ny) status |= ST_OUT_OF_MESH;
+                else if (max(abs(ni - si), abs(nj - sj)) > 1) status |= ST_DRIFT_VIOLATION;
+            }
+            continue;
+        }
+        // the sort-cell holds drifted particles: locate this one
         const int si = c0x + 1 + l;
         const float x = b[GF_X][lane], y = b[GF_Y][lane];
-        int ci = si, cj = sj;
-        if (s_sf[w][l]) {
-            ci = locate_axis(x, S.hx, S.nx);
-            cj = locate_axis(y, S.hy, S.ny);
-            if (ci < 0 || ci >= S.nx || cj < 0 || cj >= S.ny) {
-                status |= ST_OUT_OF_MESH;
-                s_flag[w][l] = 1;
-                continue;
-            }
+        const int ci = locate_axis(x, S.hx, S.nx);
+        const int cj = locate_axis(y, S.hy, S.ny);
+        if (ci < 0 || ci >= S.nx || cj < 0 || cj >= S.ny) {
+            status |= ST_OUT_OF_MESH;
+            s_flag[w][l] = 1;
+            continue;
         }
         const int kc = ci - c0x + 1, kr = cj - c0y + 1;   // geometry table indices
         const bool in_tile = kc >= 0 && kc < GEO_C && kr >= 0 && kr < GEO_R;
         const CellGeo g = in_tile ? geo_of(G, kc, kr) : cell_geo(ci, cj, S.hx, S.hy);
-        float nvx[4], nvy[4], nax[4], nay[4];
+        float4 nd[4];
         const int li = ci - c0x, lj = cj - c0y;
         if (li >= 0 && li + 1 < G_W && lj >= 0 && lj + 1 < G_H) {
             const int a = lj * G_W + li;
-            const int id[4] = {a, a + 1, a + G_W + 1, a + G_W};
-            #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const float4 v = s_nd[id[k]];
-                nvx[k] = v.x;
-                nvy[k] = v.y;
-                nax[k] = v.z;
-                nay[k] = v.w;
-            }
+            nd[0] = s_nd[a];
+            nd[1] = s_nd[a + 1];
+            nd[2] = s_nd[a + G_W + 1];
+            nd[3] = s_nd[a + G_W];
         } else {
             int ids[4];
             cell_nodes(S, ci, cj, ids);
             #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                nvx[k] = S.nvbx[ids[k]];
-                nvy[k] = S.nvby[ids[k]];
-                nax[k] = S.nax[ids[k]];
-                nay[k] = S.nay[ids[k]];
-            }
+            for (int kk = 0; kk < 4; ++kk)
+                nd[kk] = make_float4(S.nvbx[ids[kk]], S.nvby[ids[kk]], S.nax[ids[kk]], S.nay[ids[kk]]);
         }
-        const float xi = natural(x, g.cx, g.rx);
-        const float eta = natural(y, g.cy, g.ry);
-        float N[4];
-        shape4(xi, eta, N);
-        const float vhx = dot4(N, nvx), vhy = dot4(N, nvy);
-        float vx, vy;
-        if (S.velocity_update) {
-            vx = vhx;
-            vy = vhy;
-        } else {
-            vx = fa(b[GF_VX][lane], fm(dot4(N, nax), dt));
-            vy = fa(b[GF_VY][lane], fm(dot4(N, nay), dt));
-        }
-        if (S.pvc) {   // particle velocity constraints (an extension; scheme.py:67 leaves a TODO)
-            const uchar2 c = reinterpret_cast<const uchar2*>(S.pvc)[q];
-            if (c.x) vx = S.pvc_vel[c.x - 1];
-            if (c.y) vy = S.pvc_vel[c.y - 1];
-        }
-        const float xn = fa(x, fm(vhx, dt)), yn = fa(y, fm(vhy, dt));
-        S.x[q] = xn;
-        S.y[q] = yn;
-        S.vx[q] = vx;
-        S.vy[q] = vy;
-        if constexpr (USL) {
-            float Gcx[4], Gcy[4], c0, c1, c3;
-            dshape4(0.0f, 0.0f, g.rx, g.ry, Gcx, Gcy);
-            strain_rate4(Gcx, Gcy, nvx, nvy, c0, c1, c3);
-            const float dvol = fm(dt, fa(c0, c1));
-            float Gx[4], Gy[4], r0, r1, r3;
-            dshape4(xi, eta, g.rx, g.ry, Gx, Gy);
-            strain_rate4(Gx, Gy, nvx, nvy, r0, r1, r3);
-            PState p;
-            p.sxx = b[GF_SXX][lane];
-            p.syy = b[GF_SYY][lane];
-            p.szz = b[GF_SZZ][lane];
-            p.sxy = b[GF_SXY][lane];
-            p.exx = b[GF_EXX][lane];
-            p.eyy = b[GF_EYY][lane];
-            p.exy = b[GF_EXY][lane];
-            p.rho = b[GF_RHO][lane];
-            p.vsc = b[GF_VSC][lane];
-            const MatDev& M = S.mats[S.mat[q]];
-            const float Ep = S.E ? S.E[q] : -1.0f;
-            const float f = strain_stress_update(M, Ep, dt, r0, r1, r3, dvol, p);
-            S.sxx[next][q] = p.sxx;
-            S.syy[next][q] = p.syy;
-            S.szz[next][q] = p.szz;
-            S.sxy[next][q] = p.sxy;
-            S.exx[q] = p.exx;
-            S.eyy[q] = p.eyy;
-            S.exy[q] = p.exy;
-            S.rho[next][q] = p.rho;
-            S.vsc[next][q] = p.vsc;
-            if (!REINIT) S.vol[next][q] = fm(b[GF_VOL][lane], f);
-        }
+        const float2 pn = g2p_particle<USL, REINIT>(S, q, b, lane, g, nd, next);
         int ni, nj;
         if (in_tile) {
-            ni = moved_axis(xn, G.x0, G.x1, kc, GEO_C, ci, S.hx, S.nx);
-            nj = moved_axis(yn, G.y0, G.y1, kr, GEO_R, cj, S.hy, S.ny);
+            ni = moved_axis(pn.x, G.col, kc, GEO_C, ci, S.hx, S.nx);
+            nj = moved_axis(pn.y, G.row, kr, GEO_R, cj, S.hy, S.ny);
         } else {
-            ni = locate_axis(xn, S.hx, S.nx);
-            nj = locate_axis(yn, S.hy, S.ny);
+            ni = locate_axis(pn.x, S.hx, S.nx);
+            nj = locate_axis(pn.y, S.hy, S.ny);
         }
         if (ni < 0 || ni >= S.nx || nj < 0 || nj >= S.ny) {
             status |= ST_OUT_OF_MESH;
@@ -1202,8 +1080,8 @@ __device__ __forceinline__ void particle_kinematics_tile(const SimDev& S, const 
     if (tid == 0 && s_status) atomicOr(&ctl->status, s_status);
 }
 
-template <bool USL, bool REINIT>
-__global__ void __launch_bounds__(TILE_THREADS, USL ? TILE_MIN_CTAS : TILE_CTAS_LIGHT)
+template <bool USL, bool REINIT, int MINB = (USL ? TILE_MIN_CTAS : TILE_CTAS_LIGHT)>
+__global__ void __launch_bounds__(TILE_THREADS, MINB)
 k_particle_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
                       Control* __restrict__ ctl, int k) {
     particle_kinematics_tile<USL, REINIT>(S, tiles[blockIdx.x], ctl, k);
@@ -1232,48 +1110,31 @@ static void prefer_shared(K kernel) {
     }
 }
 
-// Resident CTAs of a persistent kernel on the current device (once per kernel).
-template <class K>
-static int resident_ctas(K kernel) {
-    static int n = 0;
-    if (!n) {
-        int dev = 0, sms = 0, per = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, TILE_THREADS, 0);
-        n = sms * (per > 0 ? per : 1);
-    }
-    return n;
-}
-
-static bool legacy_tiles() {
+static int light_ctas() {
     static int v = -1;
     if (v < 0) {
-        const char* e = getenv("MPM_LEGACY_TILES");
-        v = (e && e[0] == '1') ? 1 : 0;
+        const char* e = getenv("MPM_LIGHT_CTAS");
+        v = (e && e[0] == '2') ? 2 : 3;
     }
-    return v == 1;
+    return v;
 }
 
 template <bool REINIT>
 static void nodal_kinematics(const SimDev& S, const int4* tiles, int ntiles, Control* ctl,
-                             int k, TileCounter* counter, cudaStream_t s) {
-    if (legacy_tiles() || !counter) {
-        prefer_shared(k_nodal_kinematics<REINIT>);
-        k_nodal_kinematics<REINIT><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl, k);
+                             int k, cudaStream_t s) {
+    if (light_ctas() == 2) {
+        prefer_shared(k_nodal_kinematics<REINIT, 2>);
+        k_nodal_kinematics<REINIT, 2><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl, k);
         return;
     }
-    prefer_shared(k_nodal_kinematics_persistent<REINIT>);
-    const int grid = min(ntiles, resident_ctas(k_nodal_kinematics_persistent<REINIT>));
-    k_nodal_kinematics_persistent<REINIT><<<grid, TILE_THREADS, 0, s>>>(S, tiles, ntiles, ctl, k,
-                                                                         counter);
+    prefer_shared(k_nodal_kinematics<REINIT>);
+    k_nodal_kinematics<REINIT><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl, k);
 }
 
 cudaError_t launch_nodal_kinematics(const StepConfig& c, const SimDev& S, const int4* tiles,
                                     int ntiles, Control* ctl, int k, cudaStream_t s) {
-    TileCounter* counter = reinterpret_cast<TileCounter*>(c.tile_counter);
-    if (c.reinit) nodal_kinematics<true>(S, tiles, ntiles, ctl, k, counter, s);
-    else nodal_kinematics<false>(S, tiles, ntiles, ctl, k, counter, s);
+    if (c.reinit) nodal_kinematics<true>(S, tiles, ntiles, ctl, k, s);
+    else nodal_kinematics<false>(S, tiles, ntiles, ctl, k, s);
     return cudaGetLastError();
 }
 
@@ -1304,6 +1165,11 @@ cudaError_t launch_forces(const StepConfig& c, const SimDev& S, const int4* tile
 template <bool USL, bool REINIT>
 static void particle_kinematics(const SimDev& S, const int4* tiles, int ntiles, Control* ctl,
                                 int k, cudaStream_t s) {
+    if (!USL && light_ctas() == 2) {
+        prefer_shared(k_particle_kinematics<USL, REINIT, 2>);
+        k_particle_kinematics<USL, REINIT, 2><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl, k);
+        return;
+    }
     prefer_shared(k_particle_kinematics<USL, REINIT>);
     k_particle_kinematics<USL, REINIT><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl, k);
 }

@@ -11,7 +11,6 @@ struct StepConfig {
     bool usl;          // scheme: USL (else USF)
     bool reinit;       // solve_jit semantics: volume/mass reset each step
     bool traction;     // particle tractions present
-    int* tile_counter = nullptr;   // 2 zeroed ints: the persistent kernels' tile queue
 };
 
 // One explicit step = three launches over the tile list.  The descriptor is
