@@ -448,7 +448,8 @@ def run_ours(args, world, rank, local):
     nnode = sum((sp["side"] + 1) ** 2 for sp in specs)
     batch = D.Batch(sims)
     _, ntiles = batch.size()
-    block, _ = batch.autotune(trial_steps=100)
+    tuning = batch.autotune(trial_steps=100)
+    block = tuning["block_steps"]
     ckpt = min(args.checkpoint_steps, K)
     x0 = [sim.read("loc") for sim in sims]
     targets = [x + 1e-4 for x in x0]
@@ -607,7 +608,10 @@ def run_ours(args, world, rank, local):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "batch_fwd_adjoint", "sims": args.nsims, "particles": npart,
                        "nodes": nnode, "tiles_per_launch": ntiles, "steps": K,
-                       "checkpoint_steps": ckpt, "block_steps": block, "domain_m": 0.05,
+                       "checkpoint_steps": ckpt, "block_steps": block,
+                       "tuning": {k: tuning[k] for k in ("block_steps", "resort_every", "nk_ctas",
+                                                         "g2p_ctas", "ms_per_step", "from_cache")},
+                       "domain_m": 0.05,
                        "dt": "CFL 0.3 per simulation", "scheme": "usf",
                        "loss": "mean |x_end - x_target|^2 per simulation, grad w.r.t. its E",
                        "l2": "inputs larger than L2 (~2 GB of particle state)",

@@ -65,6 +65,11 @@ class MpmDesc(C.Structure):
     ]
 
 
+class MpmTuning(C.Structure):
+    _fields_ = [("block_steps", C.c_int32), ("resort_every", C.c_int32), ("nk_ctas", C.c_int32),
+                ("g2p_ctas", C.c_int32), ("ms_per_step", C.c_float)]
+
+
 # (name, restype, argtypes) of every exported entry point
 _VP = C.c_void_p
 SIGNATURES = [
@@ -90,6 +95,8 @@ SIGNATURES = [
     ("mpm_run_phase", C.c_int, [_VP, C.c_int, _VP]),
     ("mpm_time_phases", C.c_int, [_VP, C.c_int, _VP, _VP]),
     ("mpm_set_block_steps", C.c_int, [_VP, C.c_int]),
+    ("mpm_set_kernel_variant", C.c_int, [_VP, C.c_int, C.c_int]),
+    ("mpm_device_name", C.c_int, [C.c_int, C.c_char_p, C.c_int]),
     ("mpm_get_counters", C.c_int, [_VP, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     ("mpm_set_gravity", C.c_int, [_VP, C.c_double, C.c_double]),
     ("mpm_record", C.c_int, [_VP, C.c_int, C.c_int, _VP]),
@@ -104,7 +111,9 @@ SIGNATURES = [
     ("mpm_batch_write_nodal_field", C.c_int, [_VP, C.c_int, _VP, C.c_int, _VP]),
     ("mpm_batch_restart", C.c_int, [_VP, _VP]),
     ("mpm_batch_set_block_steps", C.c_int, [_VP, C.c_int]),
-    ("mpm_batch_autotune", C.c_int, [_VP, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float), _VP]),
+    ("mpm_batch_autotune", C.c_int, [_VP, C.c_int, C.POINTER(MpmTuning), _VP]),
+    ("mpm_batch_set_tuning", C.c_int, [_VP, C.POINTER(MpmTuning)]),
+    ("mpm_batch_get_tuning", C.c_int, [_VP, C.POINTER(MpmTuning)]),
     ("mpm_batch_record", C.c_int, [_VP, C.c_int, C.c_int, _VP]),
     ("mpm_batch_adjoint", C.c_int, [_VP, C.POINTER(_VP), C.POINTER(_VP), C.POINTER(_VP),
                                     C.POINTER(_VP), C.POINTER(_VP), C.c_int, _VP]),

@@ -206,6 +206,8 @@ StepConfig step_config(const MpmHandle* h) {
     c.usl = h->usl;
     c.reinit = h->reinit;
     c.traction = h->has_trac;
+    c.nk_ctas = h->nk_ctas;
+    c.g2p_ctas = h->g2p_ctas;
     return c;
 }
 
@@ -1242,6 +1244,32 @@ int mpm_set_gravity(MpmHandle* h, double gx, double gy) {
 int mpm_set_block_steps(MpmHandle* h, int steps) {
     if (!h || steps < 1) return MPM_ERR_INVALID;
     h->block_steps = steps;
+    return MPM_OK;
+}
+
+int mpm_device_name(int device, char* name, int len) {
+    if (!name || len < 1) return MPM_ERR_INVALID;
+    cudaDeviceProp prop{};
+    const cudaError_t e = cudaGetDeviceProperties(&prop, device);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        name[0] = 0;
+        return MPM_ERR_CUDA;
+    }
+    snprintf(name, (size_t)len, "%s (sm_%d%d, %d SMs)", prop.name, prop.major, prop.minor,
+             prop.multiProcessorCount);
+    return MPM_OK;
+}
+
+int mpm_set_kernel_variant(MpmHandle* h, int nk_ctas, int g2p_ctas) {
+    if (!h) return MPM_ERR_INVALID;
+    if ((nk_ctas != 2 && nk_ctas != 3) || (g2p_ctas != 2 && g2p_ctas != 3))
+        return fail(h, MPM_ERR_INVALID, "kernel builds exist for 2 or 3 CTAs per SM");
+    if (nk_ctas != h->nk_ctas || g2p_ctas != h->g2p_ctas) {
+        h->nk_ctas = nk_ctas;
+        h->g2p_ctas = g2p_ctas;
+        drop_graphs(h);   // the captured graphs hold the other builds
+    }
     return MPM_OK;
 }
 

@@ -113,8 +113,18 @@ int read_statuses(MpmBatch* b, cudaStream_t s) {
 // One block of B steps for every simulation (see the file comment).
 int batch_block(MpmBatch* b, int B, cudaStream_t s) {
     const int n = (int)b->sims.size();
-    for (int i = 0; i < n; ++i)
-        if (b->sims[i]->needs_resort) BTRY(b, i, resort(b->sims[i], s));
+    if ((int)b->since_resort.size() != n) b->since_resort.assign(n, 0);
+    for (int i = 0; i < n; ++i) {
+        // a drifted simulation keeps its sort for resort_every - 1 more blocks
+        // (its drifted cells take the gathering path); a two-cell drift
+        // rolls the block back and replays it with re-sorts either way
+        if (!b->sims[i]->needs_resort) {
+            b->since_resort[i] = 0;
+        } else if (++b->since_resort[i] >= b->resort_every) {
+            BTRY(b, i, resort(b->sims[i], s));
+            b->since_resort[i] = 0;
+        }
+    }
     std::vector<CopySeg> v;
     for (MpmHandle* h : b->sims) snapshot_segments(h, true, v);
     BTRY(b, 0, run_segments(b->sims[0], b->segbuf, v, s));
@@ -397,50 +407,111 @@ int mpm_batch_step(MpmBatch* b, int nsteps, void* stream) {
     return MPM_OK;
 }
 
-int mpm_batch_autotune(MpmBatch* b, int trial_steps, int* block_steps, float* ms_per_step,
-                       void* stream) {
+int mpm_batch_set_tuning(MpmBatch* b, const MpmTuning* t) {
+    if (!b || !t) return MPM_ERR_INVALID;
+    if (t->block_steps < 1 || t->resort_every < 1 || (t->nk_ctas != 2 && t->nk_ctas != 3) ||
+        (t->g2p_ctas != 2 && t->g2p_ctas != 3))
+        return bfail(b, MPM_ERR_INVALID, "tuning out of range (block_steps >= 1, resort_every >= 1, "
+                                         "2 or 3 CTAs per SM)");
+    if (t->nk_ctas != b->cfg.nk_ctas || t->g2p_ctas != b->cfg.g2p_ctas) {
+        b->cfg.nk_ctas = t->nk_ctas;
+        b->cfg.g2p_ctas = t->g2p_ctas;
+        drop_batch_graphs(b);   // the captured graphs hold the other builds
+    }
+    b->block_steps = t->block_steps;
+    b->resort_every = t->resort_every;
+    // the members' own steps and adjoints use the same builds
+    for (MpmHandle* h : b->sims) {
+        const int r = mpm_set_kernel_variant(h, t->nk_ctas, t->g2p_ctas);
+        if (r != MPM_OK) return r;
+    }
+    return MPM_OK;
+}
+
+int mpm_batch_get_tuning(const MpmBatch* b, MpmTuning* t) {
+    if (!b || !t) return MPM_ERR_INVALID;
+    t->block_steps = b->block_steps;
+    t->resort_every = b->resort_every;
+    t->nk_ctas = b->cfg.nk_ctas;
+    t->g2p_ctas = b->cfg.g2p_ctas;
+    t->ms_per_step = 0.0f;
+    return MPM_OK;
+}
+
+namespace {
+
+// Time trial_steps steps of the batch from the saved state with tuning t
+// (the first pass captures the block graphs, the second is timed).
+int time_tuning(MpmBatch* b, const MpmTuning& t, int trial_steps, cudaEvent_t e0, cudaEvent_t e1,
+                cudaStream_t s, float* ms) {
+    int r = mpm_batch_set_tuning(b, &t);
+    for (int pass = 0; pass < 2 && r == MPM_OK; ++pass) {
+        r = tune_state(b, false, s);
+        if (r != MPM_OK) break;
+        b->since_resort.assign(b->sims.size(), 0);
+        if (cudaEventRecord(e0, s) != cudaSuccess) r = bfail(b, MPM_ERR_CUDA, "event record");
+        if (r == MPM_OK) r = batch_steps(b, trial_steps, s);
+        if (r == MPM_OK && cudaEventRecord(e1, s) != cudaSuccess) r = bfail(b, MPM_ERR_CUDA, "event record");
+        if (r == MPM_OK && cudaEventSynchronize(e1) != cudaSuccess) r = bfail(b, MPM_ERR_CUDA, "event sync");
+    }
+    if (r == MPM_OK) cudaEventElapsedTime(ms, e0, e1);
+    return r;
+}
+
+}  // namespace
+
+int mpm_batch_autotune(MpmBatch* b, int trial_steps, MpmTuning* best_out, void* stream) {
     if (!b || trial_steps < 1) return MPM_ERR_INVALID;
     int r = check_ready(b);
     if (r != MPM_OK) return r;
     cudaStream_t s = S(stream);
-    std::vector<int> cand;
-    for (int c : {10, 25, 50, 100, 200})
-        if (c <= trial_steps) cand.push_back(c);
-    if (cand.empty()) cand.push_back(trial_steps);
     r = tune_state(b, true, s);
     if (r != MPM_OK) return r;
     cudaEvent_t e0, e1;
     BCK(b, cudaEventCreate(&e0));
     BCK(b, cudaEventCreate(&e1));
-    int best = cand.back();
+    // coordinate descent from the current tuning: kernel builds, then the
+    // graph block length, then the re-sort cadence
+    MpmTuning best;
+    mpm_batch_get_tuning(b, &best);
     float best_ms = -1.0f;
-    for (int c : cand) {
-        b->block_steps = c;
-        // first pass captures the block graphs; the second is timed
-        for (int pass = 0; pass < 2 && r == MPM_OK; ++pass) {
-            r = tune_state(b, false, s);
-            if (r != MPM_OK) break;
-            if (cudaEventRecord(e0, s) != cudaSuccess) r = bfail(b, MPM_ERR_CUDA, "event record");
-            if (r == MPM_OK) r = batch_steps(b, trial_steps, s);
-            if (r == MPM_OK && cudaEventRecord(e1, s) != cudaSuccess) r = bfail(b, MPM_ERR_CUDA, "event record");
-            if (r == MPM_OK && cudaEventSynchronize(e1) != cudaSuccess) r = bfail(b, MPM_ERR_CUDA, "event sync");
-        }
-        if (r != MPM_OK) break;
+    auto trial = [&](const MpmTuning& t) {
         float ms = 0.0f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        if (best_ms < 0.0f || ms < best_ms) {
+        if (r == MPM_OK) r = time_tuning(b, t, trial_steps, e0, e1, s, &ms);
+        if (r == MPM_OK && (best_ms < 0.0f || ms < best_ms)) {
             best_ms = ms;
-            best = c;
+            best = t;
         }
+    };
+    trial(best);
+    for (int nk : {3, 2})
+        for (int g2p : {3, 2}) {
+            MpmTuning t = best;
+            t.nk_ctas = nk;
+            t.g2p_ctas = g2p;
+            if (t.nk_ctas != best.nk_ctas || t.g2p_ctas != best.g2p_ctas) trial(t);
+        }
+    const int base_block = best.block_steps;
+    for (int c : {10, 25, 50, 100, 200}) {
+        MpmTuning t = best;
+        t.block_steps = c < trial_steps ? c : trial_steps;
+        if (t.block_steps != base_block) trial(t);
+    }
+    for (int e : {2, 4}) {
+        MpmTuning t = best;
+        t.resort_every = e;
+        if (t.block_steps * e <= trial_steps) trial(t);
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    const int r2 = tune_state(b, false, s);
+    const int r2 = r == MPM_OK ? mpm_batch_set_tuning(b, &best) : MPM_OK;
+    const int r3 = tune_state(b, false, s);
     if (r != MPM_OK) return r;
     if (r2 != MPM_OK) return r2;
-    b->block_steps = best;
-    if (block_steps) *block_steps = best;
-    if (ms_per_step) *ms_per_step = best_ms / (float)trial_steps;
+    if (r3 != MPM_OK) return r3;
+    b->since_resort.assign(b->sims.size(), 0);
+    best.ms_per_step = best_ms / (float)trial_steps;
+    if (best_out) *best_out = best;
     return MPM_OK;
 }
 

@@ -25,6 +25,8 @@ struct MpmBatch {
     mpm::Control* d_status = nullptr;
     mpm::Control* h_status = nullptr;   // pinned
     int block_steps = 100;
+    int resort_every = 1;               // re-sort a drifted simulation every this many blocks
+    std::vector<int> since_resort;      // blocks each simulation has run since it drifted
     cudaStream_t cap = nullptr;
     std::map<int, cudaGraphExec_t> graphs;
     mpm::SegBuf segbuf;

@@ -17,7 +17,6 @@
 // two cells away sets ST_DRIFT_VIOLATION and the host rolls the block back.
 #include <cuda_runtime.h>
 #include <cstdint>
-#include <cstdlib>
 #include "mpm_device.cuh"
 #include "mpm_kernels.h"
 
@@ -538,8 +537,8 @@ k_nodal_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__ ti
     nodal_kinematics_tile<REINIT>(S, tiles[blockIdx.x], ctl, k);
 }
 
-template <bool REINIT>
-__global__ void __launch_bounds__(TILE_THREADS, TILE_CTAS_LIGHT)
+template <bool REINIT, int MINB = TILE_CTAS_LIGHT>
+__global__ void __launch_bounds__(TILE_THREADS, MINB)
 k_nodal_kinematics_batch(const TileDesc* __restrict__ td, int k) {
     __shared__ TileDesc sT;
     load_tile(td + blockIdx.x, sT);
@@ -1087,8 +1086,8 @@ k_particle_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__
     particle_kinematics_tile<USL, REINIT>(S, tiles[blockIdx.x], ctl, k);
 }
 
-template <bool USL, bool REINIT>
-__global__ void __launch_bounds__(TILE_THREADS, USL ? TILE_MIN_CTAS : TILE_CTAS_LIGHT)
+template <bool USL, bool REINIT, int MINB = (USL ? TILE_MIN_CTAS : TILE_CTAS_LIGHT)>
+__global__ void __launch_bounds__(TILE_THREADS, MINB)
 k_particle_kinematics_batch(const TileDesc* __restrict__ td, int k) {
     __shared__ TileDesc sT;
     load_tile(td + blockIdx.x, sT);
@@ -1110,19 +1109,13 @@ static void prefer_shared(K kernel) {
     }
 }
 
-static int light_ctas() {
-    static int v = -1;
-    if (v < 0) {
-        const char* e = getenv("MPM_LIGHT_CTAS");
-        v = (e && e[0] == '2') ? 2 : 3;
-    }
-    return v;
-}
-
+// The nodal kinematics and USF G2P kernels come in two builds: 40 registers
+// and three CTAs per SM, or up to 64 registers and two (StepConfig.nk_ctas,
+// g2p_ctas; chosen by the autotuner).
 template <bool REINIT>
 static void nodal_kinematics(const SimDev& S, const int4* tiles, int ntiles, Control* ctl,
-                             int k, cudaStream_t s) {
-    if (light_ctas() == 2) {
+                             int k, int ctas, cudaStream_t s) {
+    if (ctas == 2) {
         prefer_shared(k_nodal_kinematics<REINIT, 2>);
         k_nodal_kinematics<REINIT, 2><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl, k);
         return;
@@ -1133,8 +1126,8 @@ static void nodal_kinematics(const SimDev& S, const int4* tiles, int ntiles, Con
 
 cudaError_t launch_nodal_kinematics(const StepConfig& c, const SimDev& S, const int4* tiles,
                                     int ntiles, Control* ctl, int k, cudaStream_t s) {
-    if (c.reinit) nodal_kinematics<true>(S, tiles, ntiles, ctl, k, s);
-    else nodal_kinematics<false>(S, tiles, ntiles, ctl, k, s);
+    if (c.reinit) nodal_kinematics<true>(S, tiles, ntiles, ctl, k, c.nk_ctas, s);
+    else nodal_kinematics<false>(S, tiles, ntiles, ctl, k, c.nk_ctas, s);
     return cudaGetLastError();
 }
 
@@ -1164,8 +1157,8 @@ cudaError_t launch_forces(const StepConfig& c, const SimDev& S, const int4* tile
 
 template <bool USL, bool REINIT>
 static void particle_kinematics(const SimDev& S, const int4* tiles, int ntiles, Control* ctl,
-                                int k, cudaStream_t s) {
-    if (!USL && light_ctas() == 2) {
+                                int k, int ctas, cudaStream_t s) {
+    if (!USL && ctas == 2) {
         prefer_shared(k_particle_kinematics<USL, REINIT, 2>);
         k_particle_kinematics<USL, REINIT, 2><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl, k);
         return;
@@ -1177,26 +1170,31 @@ static void particle_kinematics(const SimDev& S, const int4* tiles, int ntiles, 
 cudaError_t launch_particle_kinematics(const StepConfig& c, const SimDev& S, const int4* tiles,
                                        int ntiles, Control* ctl, int k, cudaStream_t s) {
     if (c.usl) {
-        if (c.reinit) particle_kinematics<true, true>(S, tiles, ntiles, ctl, k, s);
-        else particle_kinematics<true, false>(S, tiles, ntiles, ctl, k, s);
+        if (c.reinit) particle_kinematics<true, true>(S, tiles, ntiles, ctl, k, c.g2p_ctas, s);
+        else particle_kinematics<true, false>(S, tiles, ntiles, ctl, k, c.g2p_ctas, s);
     } else {
-        if (c.reinit) particle_kinematics<false, true>(S, tiles, ntiles, ctl, k, s);
-        else particle_kinematics<false, false>(S, tiles, ntiles, ctl, k, s);
+        if (c.reinit) particle_kinematics<false, true>(S, tiles, ntiles, ctl, k, c.g2p_ctas, s);
+        else particle_kinematics<false, false>(S, tiles, ntiles, ctl, k, c.g2p_ctas, s);
     }
     return cudaGetLastError();
 }
 
 // Batched launches: one grid over the tiles of every simulation of a batch.
 template <bool REINIT>
-static void nodal_kinematics_batch(const TileDesc* td, int ntiles, int k, cudaStream_t s) {
+static void nodal_kinematics_batch(const TileDesc* td, int ntiles, int k, int ctas, cudaStream_t s) {
+    if (ctas == 2) {
+        prefer_shared(k_nodal_kinematics_batch<REINIT, 2>);
+        k_nodal_kinematics_batch<REINIT, 2><<<ntiles, TILE_THREADS, 0, s>>>(td, k);
+        return;
+    }
     prefer_shared(k_nodal_kinematics_batch<REINIT>);
     k_nodal_kinematics_batch<REINIT><<<ntiles, TILE_THREADS, 0, s>>>(td, k);
 }
 
 cudaError_t launch_nodal_kinematics_batch(const StepConfig& c, const TileDesc* td, int ntiles,
                                           int k, cudaStream_t s) {
-    if (c.reinit) nodal_kinematics_batch<true>(td, ntiles, k, s);
-    else nodal_kinematics_batch<false>(td, ntiles, k, s);
+    if (c.reinit) nodal_kinematics_batch<true>(td, ntiles, k, c.nk_ctas, s);
+    else nodal_kinematics_batch<false>(td, ntiles, k, c.nk_ctas, s);
     return cudaGetLastError();
 }
 
@@ -1223,7 +1221,12 @@ cudaError_t launch_forces_batch(const StepConfig& c, const TileDesc* td, int nti
 }
 
 template <bool USL, bool REINIT>
-static void particle_kinematics_batch(const TileDesc* td, int ntiles, int k, cudaStream_t s) {
+static void particle_kinematics_batch(const TileDesc* td, int ntiles, int k, int ctas, cudaStream_t s) {
+    if (!USL && ctas == 2) {
+        prefer_shared(k_particle_kinematics_batch<USL, REINIT, 2>);
+        k_particle_kinematics_batch<USL, REINIT, 2><<<ntiles, TILE_THREADS, 0, s>>>(td, k);
+        return;
+    }
     prefer_shared(k_particle_kinematics_batch<USL, REINIT>);
     k_particle_kinematics_batch<USL, REINIT><<<ntiles, TILE_THREADS, 0, s>>>(td, k);
 }
@@ -1231,11 +1234,11 @@ static void particle_kinematics_batch(const TileDesc* td, int ntiles, int k, cud
 cudaError_t launch_particle_kinematics_batch(const StepConfig& c, const TileDesc* td, int ntiles,
                                              int k, cudaStream_t s) {
     if (c.usl) {
-        if (c.reinit) particle_kinematics_batch<true, true>(td, ntiles, k, s);
-        else particle_kinematics_batch<true, false>(td, ntiles, k, s);
+        if (c.reinit) particle_kinematics_batch<true, true>(td, ntiles, k, c.g2p_ctas, s);
+        else particle_kinematics_batch<true, false>(td, ntiles, k, c.g2p_ctas, s);
     } else {
-        if (c.reinit) particle_kinematics_batch<false, true>(td, ntiles, k, s);
-        else particle_kinematics_batch<false, false>(td, ntiles, k, s);
+        if (c.reinit) particle_kinematics_batch<false, true>(td, ntiles, k, c.g2p_ctas, s);
+        else particle_kinematics_batch<false, false>(td, ntiles, k, c.g2p_ctas, s);
     }
     return cudaGetLastError();
 }

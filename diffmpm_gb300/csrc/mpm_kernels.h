@@ -11,6 +11,10 @@ struct StepConfig {
     bool usl;          // scheme: USL (else USF)
     bool reinit;       // solve_jit semantics: volume/mass reset each step
     bool traction;     // particle tractions present
+    // resident CTAs per SM the nodal kinematics and USF G2P kernels are
+    // built for: 3 (40 registers a thread) or 2 (up to 64)
+    int nk_ctas = 3;
+    int g2p_ctas = 2;
 };
 
 // One explicit step = three launches over the tile list.  The descriptor is

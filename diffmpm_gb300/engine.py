@@ -8,7 +8,10 @@ current stream).  All arithmetic runs in the CUDA library.
 from __future__ import annotations
 
 import ctypes as C
+import json
+import os
 import weakref
+from pathlib import Path
 from typing import Sequence
 
 import numpy as np
@@ -64,6 +67,48 @@ def _out_arg(out, dtype, count):
         raise ValueError(f"out must be a writeable C-contiguous {np.dtype(dtype).name} array of "
                          f"{count} elements, found {out.dtype.name} with {out.size} elements")
     return _lib.ptr(out), 0
+
+
+_TUNING_KEYS = ("block_steps", "resort_every", "nk_ctas", "g2p_ctas", "ms_per_step")
+
+
+def device_name(device=None) -> str:
+    """The CUDA device's name, compute capability and SM count (the current
+    device by default)."""
+    lib = _lib.load()
+    if device is None:
+        try:
+            import torch
+            device = torch.cuda.current_device() if torch.cuda.is_available() else 0
+        except ImportError:
+            device = 0
+    buf = C.create_string_buffer(256)
+    _lib.check(lib.mpm_device_name(int(device), buf, len(buf)))
+    return buf.value.decode()
+
+
+def tuning_cache_path() -> Path:
+    """The tuning cache: $DIFFMPM_GB300_TUNING_CACHE, else
+    ~/.cache/diffmpm_gb300/tuning.json."""
+    env = os.environ.get("DIFFMPM_GB300_TUNING_CACHE")
+    return Path(env) if env else Path.home() / ".cache" / "diffmpm_gb300" / "tuning.json"
+
+
+def _read_tuning_cache(path: Path) -> dict:
+    try:
+        return json.loads(Path(path).read_text())
+    except (OSError, ValueError):
+        return {}
+
+
+def _write_tuning_cache(path: Path, key: str, value: dict):
+    path = Path(path)
+    path.parent.mkdir(parents=True, exist_ok=True)
+    data = _read_tuning_cache(path)
+    data[key] = value
+    tmp = path.with_name(path.name + f".{os.getpid()}.tmp")
+    tmp.write_text(json.dumps(data, indent=1, sort_keys=True))
+    os.replace(tmp, path)
 
 
 class PinnedBuffer:
@@ -175,6 +220,21 @@ class Simulation:
             self._h = C.c_void_p()
             _lib.check(rc, None)
         self.n = -1
+        self._config = {"ndim": ndim, "nelements": list(self.nelements),
+                        "el_len": [float(el[0]), float(el[1])], "dt": float(dt), "scheme": scheme,
+                        "velocity_update": bool(velocity_update),
+                        "reinit_each_step": bool(reinit_each_step), "materials": len(materials),
+                        "constraints": len(cn), "nodal_forces": len(fnode)}
+
+    def config(self) -> dict:
+        """The configuration that decides this simulation's step cost (mesh,
+        time step, scheme, particle count), for tuning-cache keys."""
+        return dict(self._config, particles=int(self.n))
+
+    def set_kernel_variant(self, nk_ctas=3, g2p_ctas=2):
+        """Kernel builds of the step (mpm_set_kernel_variant): the same results,
+        built for 2 or 3 resident CTAs per SM."""
+        self._ok(self._lib.mpm_set_kernel_variant(self._h, int(nk_ctas), int(g2p_ctas)))
 
     # ------------------------------------------------------------------
     def function_code(self, fn) -> int:
@@ -471,13 +531,48 @@ class Batch:
     def set_block_steps(self, n):
         self._ok(self._lib.mpm_batch_set_block_steps(self._b, int(n)))
 
-    def autotune(self, trial_steps=100, stream=None):
-        """Pick the step-block size by timing; the state is left unchanged.
-        Returns (block_steps, ms_per_step)."""
-        blk, ms = C.c_int(), C.c_float()
-        self._ok(self._lib.mpm_batch_autotune(self._b, int(trial_steps), C.byref(blk), C.byref(ms),
-                                              stream))
-        return blk.value, ms.value
+    def tuning(self) -> dict:
+        """The batch's current tuning (see :meth:`autotune`)."""
+        t = _lib.MpmTuning()
+        self._ok(self._lib.mpm_batch_get_tuning(self._b, C.byref(t)))
+        return {k: getattr(t, k) for k in _TUNING_KEYS}
+
+    def set_tuning(self, block_steps, resort_every=1, nk_ctas=3, g2p_ctas=2):
+        t = _lib.MpmTuning(int(block_steps), int(resort_every), int(nk_ctas), int(g2p_ctas), 0.0)
+        self._ok(self._lib.mpm_batch_set_tuning(self._b, C.byref(t)))
+
+    def config_key(self, trial_steps) -> str:
+        """Key of this batch's configuration in the tuning cache: the GPU's
+        name and a hash of every member's mesh, time step, scheme and
+        particle count, and of the trial length."""
+        import hashlib
+        import json
+        desc = [s.config() for s in self.sims]
+        h = hashlib.sha256(json.dumps({"members": desc, "trial_steps": int(trial_steps)},
+                                      sort_keys=True).encode()).hexdigest()[:20]
+        return f"{device_name()}|{h}"
+
+    def autotune(self, trial_steps=100, cache=True, stream=None) -> dict:
+        """Choose the batch's tuning by timing ``trial_steps`` steps per
+        candidate from the current state (mpm_batch_autotune: kernel builds,
+        step-block length, re-sort cadence) and leave the state unchanged.
+        With ``cache`` (True: ``tuning_cache_path()``, or a path) the choice
+        is stored in a JSON file under :meth:`config_key` and read back,
+        without timing, by the next autotune of the same configuration on the
+        same kind of GPU.  Returns the tuning with "from_cache" and "key"."""
+        path = tuning_cache_path() if cache is True else (Path(cache) if cache else None)
+        key = self.config_key(trial_steps)
+        if path is not None:
+            hit = _read_tuning_cache(path).get(key)
+            if hit is not None:
+                self.set_tuning(**{k: hit[k] for k in _TUNING_KEYS if k != "ms_per_step"})
+                return dict(hit, from_cache=True, key=key)
+        t = _lib.MpmTuning()
+        self._ok(self._lib.mpm_batch_autotune(self._b, int(trial_steps), C.byref(t), stream))
+        out = {k: getattr(t, k) for k in _TUNING_KEYS}
+        if path is not None:
+            _write_tuning_cache(path, key, out)
+        return dict(out, from_cache=False, key=key)
 
     def record(self, nsteps, checkpoint_steps=100, stream=None):
         """``Simulation.record`` for every member at once."""

@@ -223,6 +223,16 @@ int mpm_time_phases(MpmHandle* h, int nsteps, float* ms_out, void* stream);
 
 /* Steps per captured CUDA graph (default 100). */
 int mpm_set_block_steps(MpmHandle* h, int steps);
+/* Kernel builds of the step: the nodal-kinematics and USF G2P kernels for
+ * nk_ctas / g2p_ctas resident CTAs per SM (2 or 3).  Results are the same
+ * bits either way; only the speed differs (mpm_batch_autotune chooses them
+ * for a batch). */
+int mpm_set_kernel_variant(MpmHandle* h, int nk_ctas, int g2p_ctas);
+
+/* Name of CUDA device `device` with its compute capability and SM count
+ * (NUL-terminated, truncated to len bytes), the GPU part of the key under
+ * which tuning results are cached.  No counterpart in the reference. */
+int mpm_device_name(int device, char* name, int len);
 
 /* Replace desc.gravity (the `gravity` argument of solve_jit / solve,
  * diffmpm/solver.py:116,159), so one handle serves solves with any gravity. */
@@ -293,12 +303,40 @@ int mpm_batch_restart(MpmBatch* b, void* stream);
 int mpm_batch_step(MpmBatch* b, int nsteps, void* stream);
 /* Steps per captured graph (default 100). */
 int mpm_batch_set_block_steps(MpmBatch* b, int steps);
-/* Time `trial_steps` steps with each candidate block size (10, 25, 50, 100,
- * 200 up to trial_steps) from the current state, keep the fastest, and put
- * every simulation back in the state it had.  Outputs (may be NULL): the
- * chosen block size and its device time per step in ms. */
-int mpm_batch_autotune(MpmBatch* b, int trial_steps, int* block_steps, float* ms_per_step,
-                       void* stream);
+/* Tuning of a batch's step loop (no counterpart in the reference, which
+ * runs one simulation per solve_jit):
+ *   block_steps   steps per captured CUDA graph (a step block);
+ *   resort_every  a simulation whose particles left their sort-cells is
+ *                 re-sorted at the start of every resort_every-th block (in
+ *                 between its drifted cells take the gathering path; a
+ *                 particle two cells from its sort-cell rolls the block back
+ *                 either way), so particles are re-sorted every
+ *                 block_steps * resort_every steps at most;
+ *   nk_ctas       CTAs per SM the nodal-kinematics kernel is built for (3:
+ *                 40 registers a thread, or 2);
+ *   g2p_ctas      the same for the USF G2P kernel;
+ *   ms_per_step   (output of mpm_batch_autotune) device time per step.
+ * The builds and the re-sort cadence change no result beyond the last bits
+ * of the re-sort schedule's summation order. */
+typedef struct MpmTuning {
+    int32_t block_steps;
+    int32_t resort_every;
+    int32_t nk_ctas;
+    int32_t g2p_ctas;
+    float ms_per_step;
+} MpmTuning;
+
+/* Time `trial_steps` steps of the batch from its current state for
+ * candidate tunings -- coordinate descent over the kernel builds
+ * ({2, 3} x {2, 3} CTAs per SM), the block length (10, 25, 50, 100, 200,
+ * capped at trial_steps) and the re-sort cadence (1, 2, 4 blocks) --, apply
+ * the fastest, put every simulation back in the state it had, and return the
+ * choice in *best (may be NULL). */
+int mpm_batch_autotune(MpmBatch* b, int trial_steps, MpmTuning* best, void* stream);
+/* Apply a tuning (for example one read back from a cache of earlier
+ * mpm_batch_autotune results), or read the current one. */
+int mpm_batch_set_tuning(MpmBatch* b, const MpmTuning* tuning);
+int mpm_batch_get_tuning(const MpmBatch* b, MpmTuning* tuning);
 
 /* mpm_record / mpm_adjoint for every simulation of a batch at once: one
  * launch per re-run step and per reverse pass for all of them.  The arrays
