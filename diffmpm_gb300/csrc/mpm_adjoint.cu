@@ -708,7 +708,9 @@ int batch_recompute(MpmBatch* b, BatchAdjoint* x, int seg, int len, cudaStream_t
         }
         const SegBuf& tp = x->tape_p[t & 1];
         BCK(b, launch_copy_segments(tp.segs, tp.first, tp.nseg, tp.nblocks, t, s));
-        r = launch_batch_steps(b, 1, s);
+        // the tile records hold the sort: refreshed at the segment start and
+        // after a re-sort only
+        r = launch_batch_steps(b, 1, s, t == 0 || resorted);
         if (r != MPM_OK) return r;
         for (MpmHandle* h : b->sims) h->step++;
         BCK(b, launch_copy_segments(x->tape_n.segs, x->tape_n.first, x->tape_n.nseg,

@@ -54,11 +54,12 @@ void drop_batch_graphs(MpmBatch* b) {
     b->graphs.clear();
 }
 
-int launch_batch_steps(MpmBatch* b, int n, cudaStream_t s) {
-    // the descriptors change only between step blocks (re-sorts, set-up calls):
-    // one copy per tile and block lets a CTA fetch its tile, descriptor and
-    // control pointer in one read
-    BCK(b, launch_gather_tiles(b->d_sims, b->d_ctls, b->d_tiles, b->ntiles, b->d_tdescs, s));
+int launch_batch_steps(MpmBatch* b, int n, cudaStream_t s, bool gather) {
+    // the descriptors and row starts change only between step blocks
+    // (re-sorts, set-up calls): one record per tile and block lets a CTA fetch
+    // its tile, descriptor, control pointer and row starts in one read
+    if (gather)
+        BCK(b, launch_gather_tiles(b->d_sims, b->d_ctls, b->d_tiles, b->ntiles, b->d_tdescs, s));
     for (int i = 0; i < n; ++i) {
         BCK(b, launch_nodal_kinematics_batch(b->cfg, b->d_tdescs, b->ntiles, i, s));
         BCK(b, launch_forces_batch(b->cfg, b->d_tdescs, b->ntiles, i, s));

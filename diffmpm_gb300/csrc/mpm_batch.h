@@ -42,8 +42,10 @@ int bfail(MpmBatch* b, int code, const char* fmt, ...);
 // A failure reported on simulation i's handle, copied to the batch.
 int from_sim(MpmBatch* b, int i, int code);
 int check_ready(MpmBatch* b);
-// n steps of every simulation as 3n batched launches (no status handling).
-int launch_batch_steps(MpmBatch* b, int n, cudaStream_t s);
+// n steps of every simulation as 3n batched launches (no status handling),
+// after refreshing the tile records when `gather` (needed whenever a
+// descriptor or a sort changed since the last refresh).
+int launch_batch_steps(MpmBatch* b, int n, cudaStream_t s, bool gather = true);
 // Gather every control block into b->h_status and clear the status words.
 int read_statuses(MpmBatch* b, cudaStream_t s);
 // Advance every simulation by nsteps steps in blocks (re-sorts, snapshots,

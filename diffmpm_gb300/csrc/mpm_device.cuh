@@ -137,17 +137,22 @@ __device__ __forceinline__ void shape4(float xi, float eta, float N[4]) {
 
 // dN/dx, dN/dy: natural gradient (diffmpm/element.py:781-788) times the
 // inverse Jacobian diag(rx, ry) of the axis-aligned element (element.py:814-817).
+// Rounding to nearest is symmetric in sign, so (-0.25 c) rx is exactly
+// -((0.25 c) rx): each pair of opposite entries costs one product, and the
+// products 0.25 a, 0.25 b are those of shape4.
 __device__ __forceinline__ void dshape4(float xi, float eta, float rx, float ry,
                                         float Gx[4], float Gy[4]) {
     const float a = fs(1.0f, xi), b = fa(1.0f, xi), c = fs(1.0f, eta), d = fa(1.0f, eta);
-    Gx[0] = fm(fm(-0.25f, c), rx);
-    Gx[1] = fm(fm(0.25f, c), rx);
-    Gx[2] = fm(fm(0.25f, d), rx);
-    Gx[3] = fm(fm(-0.25f, d), rx);
-    Gy[0] = fm(fm(-0.25f, a), ry);
-    Gy[1] = fm(fm(-0.25f, b), ry);
-    Gy[2] = fm(fm(0.25f, b), ry);
-    Gy[3] = fm(fm(0.25f, a), ry);
+    const float gc = fm(fm(0.25f, c), rx), gd = fm(fm(0.25f, d), rx);
+    const float ga = fm(fm(0.25f, a), ry), gb = fm(fm(0.25f, b), ry);
+    Gx[0] = -gc;
+    Gx[1] = gc;
+    Gx[2] = gd;
+    Gx[3] = -gd;
+    Gy[0] = -ga;
+    Gy[1] = -gb;
+    Gy[2] = gb;
+    Gy[3] = ga;
 }
 
 // sum_k A[k] * B[k], left to right.

@@ -27,7 +27,8 @@ __device__ __forceinline__ int load_step(const Control* ctl) {
 }
 
 // Batched launches: per step block, every tile gets a record with its
-// simulation's descriptor and control pointer (one warp per record).
+// simulation's descriptor and control pointer, the storage starts of its
+// cell rows and its occupancy (one warp per record).
 __global__ void k_gather_tiles(const SimDev* const* __restrict__ sims, Control* const* __restrict__ ctls,
                                const int4* __restrict__ tiles, int ntiles, TileDesc* __restrict__ out) {
     const int t = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32, lane = threadIdx.x & 31;
@@ -39,9 +40,30 @@ __global__ void k_gather_tiles(const SimDev* const* __restrict__ sims, Control* 
         d.ctl = ctls[T.x];
         d.pad = 0;
     }
-    const int* a = reinterpret_cast<const int*>(sims[T.x]);
+    const SimDev* sd = sims[T.x];
+    const int* a = reinterpret_cast<const int*>(sd);
     int* b = reinterpret_cast<int*>(&d.S);
     for (int i = lane; i < (int)(sizeof(SimDev) / 4); i += 32) b[i] = a[i];
+    const int nx = sd->nx, ny = sd->ny;
+    const int* __restrict__ cstart = sd->cstart;
+    const int c0x = T.y * TILE_NX - 1, c0y = T.z * TILE_NY - 1;
+    #pragma unroll 1
+    for (int r = 0; r < TILE_CY; ++r) {
+        const int cj = c0y + r;
+        const bool in = cj >= 0 && cj < ny;
+        d.cs[r][lane] = in ? cstart[cj * nx + min(max(c0x + lane, 0), nx)] : 0;
+        if (lane == 0) d.cs[r][32] = in ? cstart[cj * nx + min(max(c0x + 32, 0), nx)] : 0;
+    }
+    int occ = 0;
+    const int x0 = max(c0x - 1, 0), x1 = min(c0x + TILE_CX + 1, nx);
+    const int y0 = max(c0y - 1, 0), y1 = min(c0y + TILE_CY + 1, ny);
+    if (x0 < x1)
+        for (int r = y0 + lane; r < y1; r += 32) occ |= cstart[r * nx + x1] != cstart[r * nx + x0];
+    occ = __any_sync(0xffffffffu, occ);
+    if (lane == 0) {
+        d.occ = occ;
+        d.pad2[0] = d.pad2[1] = d.pad2[2] = 0;
+    }
 }
 
 cudaError_t launch_gather_tiles(const SimDev* const* sims, Control* const* ctls, const int4* tiles,
@@ -50,13 +72,12 @@ cudaError_t launch_gather_tiles(const SimDev* const* sims, Control* const* ctls,
     return cudaGetLastError();
 }
 
-// A batched CTA copies its tile record (tile, control pointer, descriptor)
-// into shared memory, one word per thread.
+// A batched CTA copies its tile record (tile, control pointer, descriptor,
+// row starts) into shared memory, 16 bytes per thread.
 __device__ __forceinline__ void load_tile(const TileDesc* __restrict__ src, TileDesc& dst) {
-    static_assert(sizeof(TileDesc) % 4 == 0, "tile record copied in 4-byte words");
-    const int* a = reinterpret_cast<const int*>(src);
-    int* b = reinterpret_cast<int*>(&dst);
-    for (int i = threadIdx.x; i < (int)(sizeof(TileDesc) / 4); i += blockDim.x) b[i] = a[i];
+    const int4* a = reinterpret_cast<const int4*>(src);
+    int4* b = reinterpret_cast<int4*>(&dst);
+    for (int i = threadIdx.x; i < (int)(sizeof(TileDesc) / 16); i += blockDim.x) b[i] = a[i];
     __syncthreads();
 }
 
@@ -235,6 +256,28 @@ struct TileLoads {
     int occ, drift;   // this thread's share of the two block-wide ORs
 };
 
+// The drift-flag share of tile_loads.
+__device__ __forceinline__ int tile_drift(const SimDev& S, int c0x, int c0y) {
+    int drift = 0;
+    for (int idx = threadIdx.x; idx < HALO_W * HALO_H; idx += TILE_THREADS) {
+        const int si = c0x - 1 + idx % HALO_W, sj = c0y - 1 + idx / HALO_W;
+        if (si >= 0 && si < S.nx && sj >= 0 && sj < S.ny) drift |= S.cflag[sj * S.nx + si];
+    }
+    return drift;
+}
+
+// tile_loads for a batched tile: the row starts and the occupancy come from
+// its record (rec, in shared memory); only the drift flags are loaded.
+__device__ __forceinline__ TileLoads record_loads(const SimDev& S, const TileDesc& rec, int c0x, int c0y,
+                                                  int r, int lane) {
+    TileLoads L;
+    L.cs = rec.cs[r][lane];
+    L.cs32 = lane == 0 ? rec.cs[r][32] : 0;
+    L.occ = rec.occ;
+    L.drift = tile_drift(S, c0x, c0y);
+    return L;
+}
+
 __device__ __forceinline__ TileLoads tile_loads(const SimDev& S, int c0x, int c0y, int cj, int lane) {
     TileLoads L{0, 0, 0, 0};
     if (cj >= 0 && cj < S.ny) {
@@ -325,7 +368,7 @@ __device__ __forceinline__ void add_traction(const SimDev& S, int q, float t, fl
 // Per-cell values of phase 2: the volume set-up V0 = V_el / count and
 // size0 = sqrt(V0) (particle.py:169-178), and (USF) dt times the centroid
 // volumetric strain rate from the cell's nodal velocities (particle.py:270-279).
-template <bool USL, bool REINIT, bool VD = false>
+template <bool USL, bool REINIT, bool VD = false, bool TRAC = true>
 __device__ __forceinline__ void force_cell_values(const SimDev& S, int cnt, const CellGeo& g,
                                                   const float nvx[4], const float nvy[4],
                                                   float& V0, float& size0, float& dvol) {
@@ -333,7 +376,7 @@ __device__ __forceinline__ void force_cell_values(const SimDev& S, int cnt, cons
     size0 = 1.0f;
     if (REINIT) {
         if (cnt) V0 = fdv(rd<VD>(S.vol_el), (float)cnt);
-        size0 = sqrtf(V0);
+        if (TRAC) size0 = sqrtf(V0);   // only particle tractions use the size
     }
     dvol = 0.0f;
     if (!USL) {
@@ -438,9 +481,10 @@ constexpr int K1_NF = 5;   // x, y, vx, vy, rho (solve_jit) or mass (solve)
 // starting anywhere in a 16-byte piece, fits one pass (three CTAs per SM)
 constexpr int K1_ROW_P = 132;
 
-template <bool REINIT>
+template <bool REINIT, bool REC = false>
 __device__ __forceinline__ void nodal_kinematics_tile(const SimDev& S, const int4 T,
-                                                      Control* __restrict__ ctl, int k) {
+                                                      Control* __restrict__ ctl, int k,
+                                                      const TileDesc* rec = nullptr) {
     constexpr int NQ = 12;
     __shared__ float s_c[NQ][SC_STRIDE];               // [m, px, py] x corner, per cell
     __shared__ __align__(16) float s_row[TILE_CY][K1_NF][K1_ROW_P];  // staged particles of each cell row
@@ -454,7 +498,7 @@ __device__ __forceinline__ void nodal_kinematics_tile(const SimDev& S, const int
     const bool node_ok = lx < TILE_NX && ly < TILE_NY && c0x + 1 + lx <= S.nx && c0y + 1 + ly <= S.ny;
     const int node = (c0y + 1 + ly) * (S.nx + 1) + c0x + 1 + lx;
     const uint16_t ncons = node_ok ? S.ncons[node] : 0;   // node-phase input, fetched early
-    const TileLoads L = tile_loads(S, c0x, c0y, cj, lx);
+    const TileLoads L = REC ? record_loads(S, *rec, c0x, c0y, ly, lx) : tile_loads(S, c0x, c0y, cj, lx);
     if (!__syncthreads_or(L.occ)) {
         // no particle in the tile: every node is massless and keeps its
         // velocity (the node phase below with all sums zero)
@@ -542,7 +586,7 @@ __global__ void __launch_bounds__(TILE_THREADS, MINB)
 k_nodal_kinematics_batch(const TileDesc* __restrict__ td, int k) {
     __shared__ TileDesc sT;
     load_tile(td + blockIdx.x, sT);
-    nodal_kinematics_tile<REINIT>(sT.S, sT.T, sT.ctl, k);
+    nodal_kinematics_tile<REINIT, true>(sT.S, sT.T, sT.ctl, k, &sT);
 }
 
 // Nodal update shared by both schemes: concentrated forces (element.py:270-284),
@@ -588,7 +632,8 @@ constexpr int K2_ROW_P = 128;   // particles of a row per pass (two CTAs per SM)
 
 template <bool USL, bool REINIT, bool TRAC, bool VD>
 __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
-                                            Control* __restrict__ ctl, int k) {
+                                            Control* __restrict__ ctl, int k,
+                                            const TileDesc* rec = nullptr) {
     constexpr int NQ = 8;
     __shared__ float s_c[NQ][SC_STRIDE];               // [f x, f y] x corner, per cell
     __shared__ float s_slot[TILE_CY][NQ][K2_ROW_P];    // contributions of a row's particles
@@ -622,7 +667,7 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
             nv[e] = make_float2(S.nvax[n], S.nvay[n]);
         }
     }
-    const TileLoads L = tile_loads(S, c0x, c0y, cj, lx);
+    const TileLoads L = VD ? record_loads(S, *rec, c0x, c0y, ly, lx) : tile_loads(S, c0x, c0y, cj, lx);
     if (!__syncthreads_or(L.occ)) {
         // no particle in the tile: the nodal update with zero particle forces
         if (node_ok) nodal_update<VD>(S, node, t, 0.0f, 0.0f, S.nvax[node], S.nvay[node], nmass, ncons);
@@ -659,7 +704,7 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
         {
             float nvx[4], nvy[4], V0, size0, dvol;
             if (!USL) cell_velocities(lx, ly, nvx, nvy);
-            force_cell_values<USL, REINIT, VD>(S, ce - cb, geo_of(G, lx + 1, ly + 1), nvx, nvy, V0,
+            force_cell_values<USL, REINIT, VD, TRAC>(S, ce - cb, geo_of(G, lx + 1, ly + 1), nvx, nvy, V0,
                                            size0, dvol);
             s_cellv[ly][0][lx] = V0;
             s_cellv[ly][1][lx] = size0;
@@ -703,7 +748,7 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
         const int cnt = REINIT ? count_cell(S, ci, cj, g) : 0;
         float nvx[4], nvy[4], V0, size0, dvol;
         if (!USL) cell_velocities(lx, ly, nvx, nvy);
-        force_cell_values<USL, REINIT, VD>(S, cnt, g, nvx, nvy, V0, size0, dvol);
+        force_cell_values<USL, REINIT, VD, TRAC>(S, cnt, g, nvx, nvy, V0, size0, dvol);
         const bool own = lx >= 1 && ly >= 1;
         visit_cell(S, ci, cj, g, [&](int q) {
             float cc[NQ];
@@ -734,7 +779,7 @@ __global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
 k_forces_batch(const TileDesc* __restrict__ td, int k) {
     __shared__ TileDesc sT;
     load_tile(td + blockIdx.x, sT);
-    forces_tile<USL, REINIT, TRAC, true>(sT.S, sT.T, sT.ctl, k);
+    forces_tile<USL, REINIT, TRAC, true>(sT.S, sT.T, sT.ctl, k, &sT);
 }
 
 // ---------------------------------------------------------------------------
@@ -901,9 +946,10 @@ __device__ __forceinline__ float2 g2p_particle(const SimDev& S, int q, const flo
     return make_float2(xn, yn);
 }
 
-template <bool USL, bool REINIT>
+template <bool USL, bool REINIT, bool REC = false>
 __device__ __forceinline__ void particle_kinematics_tile(const SimDev& S, const int4 T,
-                                                         Control* __restrict__ ctl, int k) {
+                                                         Control* __restrict__ ctl, int k,
+                                                         const TileDesc* rec = nullptr) {
     constexpr int NF = G2PStage<USL>::NF, DEPTH = G2PStage<USL>::DEPTH;
     __shared__ float4 s_nd[G_W * G_H];    // nodal (vx, vy, ax, ay) of the tile's nodes
     __shared__ __align__(16) float s_stage[TILE_CY][DEPTH][NF][32];
@@ -922,8 +968,10 @@ __device__ __forceinline__ void particle_kinematics_tile(const SimDev& S, const 
     int rb = 0, re = 0;
     unsigned sfmask = 0;   // bit l: sort-cell c0x + 1 + l had a drifted particle at the step start
     if (row_ok) {
+        // (a batched tile's row starts come with its record: row w + 1,
+        // column lane + 1 of the record's table)
         const int col = min(c0x + 1 + lane, S.nx);
-        s_cs[w][lane] = S.cstart[sj * S.nx + col];
+        s_cs[w][lane] = REC ? rec->cs[w + 1][lane + 1] : S.cstart[sj * S.nx + col];
         sfmask = __ballot_sync(0xffffffffu, col < S.nx && S.cflag[sj * S.nx + col] != 0);
     }
     s_flag[w][lane] = 0;
@@ -1091,7 +1139,7 @@ __global__ void __launch_bounds__(TILE_THREADS, MINB)
 k_particle_kinematics_batch(const TileDesc* __restrict__ td, int k) {
     __shared__ TileDesc sT;
     load_tile(td + blockIdx.x, sT);
-    particle_kinematics_tile<USL, REINIT>(sT.S, sT.T, sT.ctl, k);
+    particle_kinematics_tile<USL, REINIT, true>(sT.S, sT.T, sT.ctl, k, &sT);
 }
 
 // ---------------------------------------------------------------------------

@@ -96,13 +96,22 @@ struct Control;
 
 // One tile of a batched launch together with its simulation's descriptor and
 // control block, so that a CTA fetches everything it needs to start in one
-// contiguous read (refreshed before every step block).
+// contiguous read (refreshed before every step block).  The storage starts
+// of the tile's cell rows and whether any particle is stored around the tile
+// change only at a re-sort, which happens between step blocks, so they are
+// part of the record too: a batched CTA then issues its particle loads right
+// after the record arrives, as a single-simulation CTA does after its own
+// set-up loads.
 struct alignas(16) TileDesc {
     int4 T;                // (simulation, tile x, tile y, 0)
     Control* ctl;
     long long pad;
     SimDev S;
+    int occ;               // a particle is stored in sort-cells [c0x-1, c0x+33) x [c0y-1, c0y+17)
+    int pad2[3];
+    int cs[TILE_CY][33];   // storage start of cell (c0x + l, c0y + r), l clamped to [0, nx]; 0 off the mesh
 };
+static_assert(sizeof(TileDesc) % 16 == 0, "tile records are copied in 16-byte pieces");
 
 // Per-batch control block.
 struct Control {
