@@ -610,7 +610,8 @@ def run_ours(args, world, rank, local):
                        "nodes": nnode, "tiles_per_launch": ntiles, "steps": K,
                        "checkpoint_steps": ckpt, "block_steps": block,
                        "tuning": {k: tuning[k] for k in ("block_steps", "resort_every", "nk_ctas",
-                                                         "g2p_ctas", "ms_per_step", "from_cache")},
+                                                         "g2p_ctas", "forces_lpc", "ms_per_step",
+                                                         "from_cache")},
                        "domain_m": 0.05,
                        "dt": "CFL 0.3 per simulation", "scheme": "usf",
                        "loss": "mean |x_end - x_target|^2 per simulation, grad w.r.t. its E",

@@ -67,7 +67,7 @@ class MpmDesc(C.Structure):
 
 class MpmTuning(C.Structure):
     _fields_ = [("block_steps", C.c_int32), ("resort_every", C.c_int32), ("nk_ctas", C.c_int32),
-                ("g2p_ctas", C.c_int32), ("ms_per_step", C.c_float)]
+                ("g2p_ctas", C.c_int32), ("forces_lpc", C.c_int32), ("ms_per_step", C.c_float)]
 
 
 # (name, restype, argtypes) of every exported entry point
@@ -95,7 +95,7 @@ SIGNATURES = [
     ("mpm_run_phase", C.c_int, [_VP, C.c_int, _VP]),
     ("mpm_time_phases", C.c_int, [_VP, C.c_int, _VP, _VP]),
     ("mpm_set_block_steps", C.c_int, [_VP, C.c_int]),
-    ("mpm_set_kernel_variant", C.c_int, [_VP, C.c_int, C.c_int]),
+    ("mpm_set_kernel_variant", C.c_int, [_VP, C.c_int, C.c_int, C.c_int]),
     ("mpm_device_name", C.c_int, [C.c_int, C.c_char_p, C.c_int]),
     ("mpm_get_counters", C.c_int, [_VP, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     ("mpm_set_gravity", C.c_int, [_VP, C.c_double, C.c_double]),

@@ -208,6 +208,7 @@ StepConfig step_config(const MpmHandle* h) {
     c.traction = h->has_trac;
     c.nk_ctas = h->nk_ctas;
     c.g2p_ctas = h->g2p_ctas;
+    c.forces_lpc = h->forces_lpc;
     return c;
 }
 
@@ -470,6 +471,10 @@ int mpm_create(const MpmDesc* d, MpmHandle** out) {
     h->gx = (float)d->gravity[0];
     h->gy = (float)d->gravity[1];
     h->usl = d->scheme == MPM_USL;
+    // the forces kernel's lane-per-cell path is the faster one when it carries
+    // no stress update (USL: 1024^2 scale-up 51 -> 38 us), the row path when
+    // it does (USF: 68 vs 82 us)
+    h->forces_lpc = h->usl ? 1 : 0;
     h->reinit = d->reinit_each_step != 0;
     h->velocity_update = d->velocity_update ? 1 : 0;
     h->vol_el = element_volume(h->hx, h->hy);
@@ -1261,13 +1266,15 @@ int mpm_device_name(int device, char* name, int len) {
     return MPM_OK;
 }
 
-int mpm_set_kernel_variant(MpmHandle* h, int nk_ctas, int g2p_ctas) {
+int mpm_set_kernel_variant(MpmHandle* h, int nk_ctas, int g2p_ctas, int forces_lpc) {
     if (!h) return MPM_ERR_INVALID;
     if ((nk_ctas != 2 && nk_ctas != 3) || (g2p_ctas != 2 && g2p_ctas != 3))
         return fail(h, MPM_ERR_INVALID, "kernel builds exist for 2 or 3 CTAs per SM");
-    if (nk_ctas != h->nk_ctas || g2p_ctas != h->g2p_ctas) {
+    if (forces_lpc != 0 && forces_lpc != 1) return fail(h, MPM_ERR_INVALID, "forces_lpc is 0 or 1");
+    if (nk_ctas != h->nk_ctas || g2p_ctas != h->g2p_ctas || forces_lpc != h->forces_lpc) {
         h->nk_ctas = nk_ctas;
         h->g2p_ctas = g2p_ctas;
+        h->forces_lpc = forces_lpc;
         drop_graphs(h);   // the captured graphs hold the other builds
     }
     return MPM_OK;

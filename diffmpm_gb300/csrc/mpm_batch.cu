@@ -206,6 +206,9 @@ int mpm_batch_create(MpmHandle* const* sims, int n, MpmBatch** out) {
     b->cfg.usl = sims[0]->usl;
     b->cfg.reinit = sims[0]->reinit;
     b->cfg.traction = sims[0]->has_trac;
+    b->cfg.nk_ctas = sims[0]->nk_ctas;
+    b->cfg.g2p_ctas = sims[0]->g2p_ctas;
+    b->cfg.forces_lpc = sims[0]->forces_lpc;
     std::vector<int4> tiles;
     std::vector<const SimDev*> ds(n);
     std::vector<Control*> ctl(n);
@@ -411,19 +414,21 @@ int mpm_batch_step(MpmBatch* b, int nsteps, void* stream) {
 int mpm_batch_set_tuning(MpmBatch* b, const MpmTuning* t) {
     if (!b || !t) return MPM_ERR_INVALID;
     if (t->block_steps < 1 || t->resort_every < 1 || (t->nk_ctas != 2 && t->nk_ctas != 3) ||
-        (t->g2p_ctas != 2 && t->g2p_ctas != 3))
+        (t->g2p_ctas != 2 && t->g2p_ctas != 3) || (t->forces_lpc != 0 && t->forces_lpc != 1))
         return bfail(b, MPM_ERR_INVALID, "tuning out of range (block_steps >= 1, resort_every >= 1, "
-                                         "2 or 3 CTAs per SM)");
-    if (t->nk_ctas != b->cfg.nk_ctas || t->g2p_ctas != b->cfg.g2p_ctas) {
+                                         "2 or 3 CTAs per SM, forces_lpc 0 or 1)");
+    if (t->nk_ctas != b->cfg.nk_ctas || t->g2p_ctas != b->cfg.g2p_ctas ||
+        t->forces_lpc != b->cfg.forces_lpc) {
         b->cfg.nk_ctas = t->nk_ctas;
         b->cfg.g2p_ctas = t->g2p_ctas;
+        b->cfg.forces_lpc = t->forces_lpc;
         drop_batch_graphs(b);   // the captured graphs hold the other builds
     }
     b->block_steps = t->block_steps;
     b->resort_every = t->resort_every;
     // the members' own steps and adjoints use the same builds
     for (MpmHandle* h : b->sims) {
-        const int r = mpm_set_kernel_variant(h, t->nk_ctas, t->g2p_ctas);
+        const int r = mpm_set_kernel_variant(h, t->nk_ctas, t->g2p_ctas, t->forces_lpc);
         if (r != MPM_OK) return r;
     }
     return MPM_OK;
@@ -435,6 +440,7 @@ int mpm_batch_get_tuning(const MpmBatch* b, MpmTuning* t) {
     t->resort_every = b->resort_every;
     t->nk_ctas = b->cfg.nk_ctas;
     t->g2p_ctas = b->cfg.g2p_ctas;
+    t->forces_lpc = b->cfg.forces_lpc;
     t->ms_per_step = 0.0f;
     return MPM_OK;
 }
@@ -492,6 +498,11 @@ int mpm_batch_autotune(MpmBatch* b, int trial_steps, MpmTuning* best_out, void* 
             t.g2p_ctas = g2p;
             if (t.nk_ctas != best.nk_ctas || t.g2p_ctas != best.g2p_ctas) trial(t);
         }
+    {
+        MpmTuning t = best;
+        t.forces_lpc = 1 - best.forces_lpc;
+        trial(t);
+    }
     const int base_block = best.block_steps;
     for (int c : {10, 25, 50, 100, 200}) {
         MpmTuning t = best;

@@ -132,6 +132,7 @@ struct MpmHandle {
     bool initialized = false, needs_resort = false;
     int block_steps = 100;
     int nk_ctas = 3, g2p_ctas = 2;     // kernel builds (StepConfig), set by mpm_set_kernel_variant
+    int forces_lpc = 0;
     int64_t resorts = 0, rollbacks = 0;
     // differentiation (null until mpm_record); gen counts state changes
     mpm::AdjointState* adj = nullptr;

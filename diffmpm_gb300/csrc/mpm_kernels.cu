@@ -17,6 +17,7 @@
 // two cells away sets ST_DRIFT_VIOLATION and the host rolls the block back.
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <type_traits>
 #include "mpm_device.cuh"
 #include "mpm_kernels.h"
 
@@ -630,15 +631,28 @@ constexpr int NV_W = TILE_CX + 1;   // node tile of the R cells: [c0x, c0x+33) x
 constexpr int NV_H = TILE_CY + 1;
 constexpr int K2_ROW_P = 128;   // particles of a row per pass (two CTAs per SM)
 
-template <bool USL, bool REINIT, bool TRAC, bool VD>
+// Row-pass buffers of the particle-per-lane forces path.
+template <int NQ>
+struct ForceRows {
+    float slot[TILE_CY][NQ][K2_ROW_P];    // contributions of a row's particles
+    unsigned char cell[TILE_CY][K2_ROW_P];   // their cell within the row
+    float cellv[TILE_CY][3][32];          // V0, size0, dvol per cell
+};
+struct NoForceRows {};
+
+// LPC (lane per cell): every lane works through its own cell's particles in
+// storage order, with the cell's nodal velocities and values in registers,
+// adding each contribution as it is formed -- the order of the
+// particle-per-lane path's slot sums, so both give the same bits.  Without
+// LPC, a warp's lanes take consecutive particles of the row (coalesced
+// loads and stores) and the contributions go through shared-memory slots.
+template <bool USL, bool REINIT, bool TRAC, bool VD, bool LPC = false>
 __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
                                             Control* __restrict__ ctl, int k,
                                             const TileDesc* rec = nullptr) {
     constexpr int NQ = 8;
     __shared__ float s_c[NQ][SC_STRIDE];               // [f x, f y] x corner, per cell
-    __shared__ float s_slot[TILE_CY][NQ][K2_ROW_P];    // contributions of a row's particles
-    __shared__ unsigned char s_cell[TILE_CY][K2_ROW_P];   // their cell within the row
-    __shared__ float s_cellv[TILE_CY][3][32];          // V0, size0, dvol per cell
+    __shared__ std::conditional_t<LPC, NoForceRows, ForceRows<NQ>> s_rows;
     __shared__ int s_cs[TILE_CY][33];
     __shared__ float2 s_v[NV_W * NV_H];   // nodal velocity after phase 1 of the tile's nodes
     __shared__ TileGeo G;
@@ -695,9 +709,36 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
     };
 
     if (!slow) {
+      if constexpr (LPC) {
+        if (ci >= 0 && ci < S.nx && cj >= 0 && cj < S.ny) {
+            const int cb = s_cs[ly][lx], ce = s_cs[ly][lx + 1];
+            const CellGeo g = geo_of(G, lx + 1, ly + 1);
+            float nvx[4], nvy[4], V0, size0, dvol;
+            if (!USL) cell_velocities(lx, ly, nvx, nvy);
+            force_cell_values<USL, REINIT, VD, TRAC>(S, ce - cb, g, nvx, nvy, V0, size0, dvol);
+            const bool own = lx >= 1 && ly >= 1;
+            float acc[NQ];
+            #pragma unroll
+            for (int q = 0; q < NQ; ++q) acc[q] = 0.0f;
+            #pragma unroll 1
+            for (int q = cb; q < ce; ++q) {
+                float cc[NQ];
+                force_contrib<USL, REINIT, TRAC, VD>(S, q, force_in_global<VD>(S, q, parity, REINIT), g.cx,
+                                                     g.rx, g.cy, g.ry, V0, size0, nvx, nvy, dvol, parity,
+                                                     t, own, cc);
+                #pragma unroll
+                for (int kk = 0; kk < NQ; ++kk) acc[kk] = fa(acc[kk], cc[kk]);
+            }
+            #pragma unroll
+            for (int q = 0; q < NQ; ++q) s_c[q][tid] = acc[q];
+        }
+      } else {
         // particle per lane for the per-particle work (coalesced global loads
         // and stores), contributions to row slots, then lane per cell adds
         // the slots of its cell's particles in storage order
+        auto& s_slot = s_rows.slot;
+        auto& s_cell = s_rows.cell;
+        auto& s_cellv = s_rows.cellv;
         const int* cs = s_cs[ly];
         const int rb = cs[0], re = cs[32];
         const int cb = cs[lx], ce = cs[lx + 1];
@@ -743,6 +784,7 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
         }
         #pragma unroll
         for (int k = 0; k < NQ; ++k) s_c[k][tid] = acc[k];
+      }
     } else if (ci >= 0 && ci < S.nx && cj >= 0 && cj < S.ny) {
         const CellGeo g = geo_of(G, lx + 1, ly + 1);
         const int cnt = REINIT ? count_cell(S, ci, cj, g) : 0;
@@ -767,19 +809,19 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
     }
 }
 
-template <bool USL, bool REINIT, bool TRAC>
+template <bool USL, bool REINIT, bool TRAC, bool LPC = false>
 __global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
 k_forces(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
          Control* __restrict__ ctl, int k) {
-    forces_tile<USL, REINIT, TRAC, false>(S, tiles[blockIdx.x], ctl, k);
+    forces_tile<USL, REINIT, TRAC, false, LPC>(S, tiles[blockIdx.x], ctl, k);
 }
 
-template <bool USL, bool REINIT, bool TRAC>
+template <bool USL, bool REINIT, bool TRAC, bool LPC = false>
 __global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
 k_forces_batch(const TileDesc* __restrict__ td, int k) {
     __shared__ TileDesc sT;
     load_tile(td + blockIdx.x, sT);
-    forces_tile<USL, REINIT, TRAC, true>(sT.S, sT.T, sT.ctl, k, &sT);
+    forces_tile<USL, REINIT, TRAC, true, LPC>(sT.S, sT.T, sT.ctl, k, &sT);
 }
 
 // ---------------------------------------------------------------------------
@@ -1179,26 +1221,34 @@ cudaError_t launch_nodal_kinematics(const StepConfig& c, const SimDev& S, const 
     return cudaGetLastError();
 }
 
-template <bool USL, bool REINIT>
-static void forces_trac(bool trac, const SimDev& S, const int4* tiles, int ntiles, Control* ctl,
-                        int k, cudaStream_t s) {
-    if (trac) {
-        prefer_shared(k_forces<USL, REINIT, true>);
-        k_forces<USL, REINIT, true><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl, k);
+template <bool USL, bool REINIT, bool TRAC>
+static void forces_one(bool lpc, const SimDev& S, const int4* tiles, int ntiles, Control* ctl, int k,
+                       cudaStream_t s) {
+    if (lpc) {
+        prefer_shared(k_forces<USL, REINIT, TRAC, true>);
+        k_forces<USL, REINIT, TRAC, true><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl, k);
     } else {
-        prefer_shared(k_forces<USL, REINIT, false>);
-        k_forces<USL, REINIT, false><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl, k);
+        prefer_shared(k_forces<USL, REINIT, TRAC>);
+        k_forces<USL, REINIT, TRAC><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl, k);
     }
+}
+
+template <bool USL, bool REINIT>
+static void forces_trac(bool trac, bool lpc, const SimDev& S, const int4* tiles, int ntiles,
+                        Control* ctl, int k, cudaStream_t s) {
+    if (trac) forces_one<USL, REINIT, true>(lpc, S, tiles, ntiles, ctl, k, s);
+    else forces_one<USL, REINIT, false>(lpc, S, tiles, ntiles, ctl, k, s);
 }
 
 cudaError_t launch_forces(const StepConfig& c, const SimDev& S, const int4* tiles, int ntiles,
                           Control* ctl, int k, cudaStream_t s) {
+    const bool lpc = c.forces_lpc != 0;
     if (c.usl) {
-        if (c.reinit) forces_trac<true, true>(c.traction, S, tiles, ntiles, ctl, k, s);
-        else forces_trac<true, false>(c.traction, S, tiles, ntiles, ctl, k, s);
+        if (c.reinit) forces_trac<true, true>(c.traction, lpc, S, tiles, ntiles, ctl, k, s);
+        else forces_trac<true, false>(c.traction, lpc, S, tiles, ntiles, ctl, k, s);
     } else {
-        if (c.reinit) forces_trac<false, true>(c.traction, S, tiles, ntiles, ctl, k, s);
-        else forces_trac<false, false>(c.traction, S, tiles, ntiles, ctl, k, s);
+        if (c.reinit) forces_trac<false, true>(c.traction, lpc, S, tiles, ntiles, ctl, k, s);
+        else forces_trac<false, false>(c.traction, lpc, S, tiles, ntiles, ctl, k, s);
     }
     return cudaGetLastError();
 }
@@ -1247,23 +1297,29 @@ cudaError_t launch_nodal_kinematics_batch(const StepConfig& c, const TileDesc* t
 }
 
 template <bool USL, bool REINIT, bool TRAC>
-static void forces_batch(const TileDesc* td, int ntiles, int k, cudaStream_t s) {
-    prefer_shared(k_forces_batch<USL, REINIT, TRAC>);
-    k_forces_batch<USL, REINIT, TRAC><<<ntiles, TILE_THREADS, 0, s>>>(td, k);
+static void forces_batch(bool lpc, const TileDesc* td, int ntiles, int k, cudaStream_t s) {
+    if (lpc) {
+        prefer_shared(k_forces_batch<USL, REINIT, TRAC, true>);
+        k_forces_batch<USL, REINIT, TRAC, true><<<ntiles, TILE_THREADS, 0, s>>>(td, k);
+    } else {
+        prefer_shared(k_forces_batch<USL, REINIT, TRAC>);
+        k_forces_batch<USL, REINIT, TRAC><<<ntiles, TILE_THREADS, 0, s>>>(td, k);
+    }
 }
 
 cudaError_t launch_forces_batch(const StepConfig& c, const TileDesc* td, int ntiles, int k,
                                 cudaStream_t s) {
     const int key = (c.usl ? 4 : 0) | (c.reinit ? 2 : 0) | (c.traction ? 1 : 0);
+    const bool lpc = c.forces_lpc != 0;
     switch (key) {
-        case 0: forces_batch<false, false, false>(td, ntiles, k, s); break;
-        case 1: forces_batch<false, false, true>(td, ntiles, k, s); break;
-        case 2: forces_batch<false, true, false>(td, ntiles, k, s); break;
-        case 3: forces_batch<false, true, true>(td, ntiles, k, s); break;
-        case 4: forces_batch<true, false, false>(td, ntiles, k, s); break;
-        case 5: forces_batch<true, false, true>(td, ntiles, k, s); break;
-        case 6: forces_batch<true, true, false>(td, ntiles, k, s); break;
-        default: forces_batch<true, true, true>(td, ntiles, k, s); break;
+        case 0: forces_batch<false, false, false>(lpc, td, ntiles, k, s); break;
+        case 1: forces_batch<false, false, true>(lpc, td, ntiles, k, s); break;
+        case 2: forces_batch<false, true, false>(lpc, td, ntiles, k, s); break;
+        case 3: forces_batch<false, true, true>(lpc, td, ntiles, k, s); break;
+        case 4: forces_batch<true, false, false>(lpc, td, ntiles, k, s); break;
+        case 5: forces_batch<true, false, true>(lpc, td, ntiles, k, s); break;
+        case 6: forces_batch<true, true, false>(lpc, td, ntiles, k, s); break;
+        default: forces_batch<true, true, true>(lpc, td, ntiles, k, s); break;
     }
     return cudaGetLastError();
 }

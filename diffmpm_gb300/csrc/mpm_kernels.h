@@ -15,6 +15,9 @@ struct StepConfig {
     // built for: 3 (40 registers a thread) or 2 (up to 64)
     int nk_ctas = 3;
     int g2p_ctas = 2;
+    // forces kernel: particle per lane with shared-memory slots (0) or lane
+    // per cell (1); the same bits either way
+    int forces_lpc = 0;
 };
 
 // One explicit step = three launches over the tile list.  The descriptor is

@@ -69,7 +69,7 @@ def _out_arg(out, dtype, count):
     return _lib.ptr(out), 0
 
 
-_TUNING_KEYS = ("block_steps", "resort_every", "nk_ctas", "g2p_ctas", "ms_per_step")
+_TUNING_KEYS = ("block_steps", "resort_every", "nk_ctas", "g2p_ctas", "forces_lpc", "ms_per_step")
 
 
 def device_name(device=None) -> str:
@@ -231,10 +231,11 @@ class Simulation:
         time step, scheme, particle count), for tuning-cache keys."""
         return dict(self._config, particles=int(self.n))
 
-    def set_kernel_variant(self, nk_ctas=3, g2p_ctas=2):
+    def set_kernel_variant(self, nk_ctas=3, g2p_ctas=2, forces_lpc=0):
         """Kernel builds of the step (mpm_set_kernel_variant): the same results,
-        built for 2 or 3 resident CTAs per SM."""
-        self._ok(self._lib.mpm_set_kernel_variant(self._h, int(nk_ctas), int(g2p_ctas)))
+        built for 2 or 3 resident CTAs per SM, and either forces path."""
+        self._ok(self._lib.mpm_set_kernel_variant(self._h, int(nk_ctas), int(g2p_ctas),
+                                                  int(forces_lpc)))
 
     # ------------------------------------------------------------------
     def function_code(self, fn) -> int:
@@ -537,8 +538,9 @@ class Batch:
         self._ok(self._lib.mpm_batch_get_tuning(self._b, C.byref(t)))
         return {k: getattr(t, k) for k in _TUNING_KEYS}
 
-    def set_tuning(self, block_steps, resort_every=1, nk_ctas=3, g2p_ctas=2):
-        t = _lib.MpmTuning(int(block_steps), int(resort_every), int(nk_ctas), int(g2p_ctas), 0.0)
+    def set_tuning(self, block_steps, resort_every=1, nk_ctas=3, g2p_ctas=2, forces_lpc=0):
+        t = _lib.MpmTuning(int(block_steps), int(resort_every), int(nk_ctas), int(g2p_ctas),
+                           int(forces_lpc), 0.0)
         self._ok(self._lib.mpm_batch_set_tuning(self._b, C.byref(t)))
 
     def config_key(self, trial_steps) -> str:
@@ -564,7 +566,7 @@ class Batch:
         key = self.config_key(trial_steps)
         if path is not None:
             hit = _read_tuning_cache(path).get(key)
-            if hit is not None:
+            if hit is not None and all(k in hit for k in _TUNING_KEYS):
                 self.set_tuning(**{k: hit[k] for k in _TUNING_KEYS if k != "ms_per_step"})
                 return dict(hit, from_cache=True, key=key)
         t = _lib.MpmTuning()

@@ -224,10 +224,10 @@ int mpm_time_phases(MpmHandle* h, int nsteps, float* ms_out, void* stream);
 /* Steps per captured CUDA graph (default 100). */
 int mpm_set_block_steps(MpmHandle* h, int steps);
 /* Kernel builds of the step: the nodal-kinematics and USF G2P kernels for
- * nk_ctas / g2p_ctas resident CTAs per SM (2 or 3).  Results are the same
- * bits either way; only the speed differs (mpm_batch_autotune chooses them
- * for a batch). */
-int mpm_set_kernel_variant(MpmHandle* h, int nk_ctas, int g2p_ctas);
+ * nk_ctas / g2p_ctas resident CTAs per SM (2 or 3), and the forces kernel's
+ * fast path (forces_lpc, see MpmTuning).  Results are the same bits either
+ * way; only the speed differs (mpm_batch_autotune chooses them for a batch). */
+int mpm_set_kernel_variant(MpmHandle* h, int nk_ctas, int g2p_ctas, int forces_lpc);
 
 /* Name of CUDA device `device` with its compute capability and SM count
  * (NUL-terminated, truncated to len bytes), the GPU part of the key under
@@ -315,6 +315,10 @@ int mpm_batch_set_block_steps(MpmBatch* b, int steps);
  *   nk_ctas       CTAs per SM the nodal-kinematics kernel is built for (3:
  *                 40 registers a thread, or 2);
  *   g2p_ctas      the same for the USF G2P kernel;
+ *   forces_lpc    the forces kernel's fast path: 0, a warp's lanes take
+ *                 consecutive particles of a cell row and add their
+ *                 contributions through shared memory; 1, each lane works
+ *                 through the particles of its own cell;
  *   ms_per_step   (output of mpm_batch_autotune) device time per step.
  * The builds and the re-sort cadence change no result beyond the last bits
  * of the re-sort schedule's summation order. */
@@ -323,12 +327,13 @@ typedef struct MpmTuning {
     int32_t resort_every;
     int32_t nk_ctas;
     int32_t g2p_ctas;
+    int32_t forces_lpc;
     float ms_per_step;
 } MpmTuning;
 
 /* Time `trial_steps` steps of the batch from its current state for
  * candidate tunings -- coordinate descent over the kernel builds
- * ({2, 3} x {2, 3} CTAs per SM), the block length (10, 25, 50, 100, 200,
+ * ({2, 3} x {2, 3} CTAs per SM, either forces path), the block length (10, 25, 50, 100, 200,
  * capped at trial_steps) and the re-sort cadence (1, 2, 4 blocks) --, apply
  * the fastest, put every simulation back in the state it had, and return the
  * choice in *best (may be NULL). */

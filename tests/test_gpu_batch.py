@@ -240,7 +240,7 @@ def test_autotune_result_is_cached_and_read_back(built, tmp_path):
     b = D.Batch([member_sim(sp, 30)[1] for sp in specs])
     t2 = b.autotune(trial_steps=20, cache=cache)
     assert t2["from_cache"] and t2["key"] == t1["key"]
-    for k in ("block_steps", "resort_every", "nk_ctas", "g2p_ctas"):
+    for k in ("block_steps", "resort_every", "nk_ctas", "g2p_ctas", "forces_lpc"):
         assert t2[k] == t1[k] and b.tuning()[k] == t1[k], k
     c = D.Batch([member_sim(sp, 30)[1] for sp in small_specs(k=2, seed=12)])
     t3 = c.autotune(trial_steps=20, cache=cache)
@@ -253,16 +253,16 @@ def test_kernel_builds_and_resort_cadence_keep_results(built):
     stays within the parity tolerance of the oracle."""
     spec = small_specs(k=1, seed=13)[0]
     ref = None
-    for nk, g2p in ((3, 3), (2, 2), (3, 2), (2, 3)):
+    for nk, g2p, lpc in ((3, 3, 0), (2, 2, 1), (3, 2, 1), (2, 3, 0)):
         _, sim, _ = member_sim(spec, 40)
         b = D.Batch([sim])
-        b.set_tuning(block_steps=10, resort_every=1, nk_ctas=nk, g2p_ctas=g2p)
+        b.set_tuning(block_steps=10, resort_every=1, nk_ctas=nk, g2p_ctas=g2p, forces_lpc=lpc)
         b.step(40)
         got = state(sim)
         if ref is None:
             ref = got
         for k in FIELDS:
-            assert np.array_equal(got[k], ref[k]), (nk, g2p, k)
+            assert np.array_equal(got[k], ref[k]), (nk, g2p, lpc, k)
     _, sim, _ = member_sim(spec, 40)
     b = D.Batch([sim])
     b.set_tuning(block_steps=10, resort_every=2)
@@ -271,3 +271,27 @@ def test_kernel_builds_and_resort_cadence_keep_results(built):
     exp = o.solve_jit(og)
     assert rel(sim.read("loc"), exp["loc"].reshape(-1, 2)) < 1e-4
     assert rel(sim.read("velocity"), exp["velocity"].reshape(-1, 2)) < 1e-4
+
+
+@pytest.mark.parametrize("builder,kw", [
+    (workloads.plain_scaleup, dict(n=64, scheme="usf")),
+    (workloads.plain_scaleup, dict(n=64, scheme="usl")),
+    (workloads.mixed_large, dict(n=48)),
+])
+def test_forces_paths_give_the_same_bits(built, builder, kw):
+    """The forces kernel's two fast paths (particle per lane with slots, lane
+    per cell) add every cell's contributions in the same order: a single
+    simulation ends bit for bit in the same state with either."""
+    out = []
+    for lpc in (0, 1):
+        s, g, _ = builder(D, sim_steps=30, **kw)
+        sim = s.simulation(g, reinit=True)
+        s._upload(sim)
+        sim.initialize()
+        sim.set_kernel_variant(3, 2, lpc)
+        sim.set_block_steps(10)
+        sim.step(30)
+        out.append(state(sim))
+        sim.close()
+    for k in FIELDS:
+        assert np.array_equal(out[0][k], out[1][k]), k
