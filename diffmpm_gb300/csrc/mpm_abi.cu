@@ -212,19 +212,33 @@ StepConfig step_config(const MpmHandle* h) {
     return c;
 }
 
-// One phase of step (ctl->step + k); phase 2 ends the step, whose counter the
-// caller advances.
+// Split the tiles into active and empty ones for the current sort (see
+// launch_classify_tiles); every launched sequence of steps starts with it.
+int classify_tiles(MpmHandle* h, cudaStream_t s) {
+    CK(h, launch_classify_tiles(h->hs, h->dtiles, h->ntiles, h->d_tile_flags, h->d_active, h->d_empty, s));
+    return MPM_OK;
+}
+
+// One phase of step (ctl->step + k) over the active tiles (the empty tiles'
+// nodes are updated with the nodal kinematics); phase 2 ends the step, whose
+// counter the caller advances.
 int launch_phase(MpmHandle* h, int phase, int k, cudaStream_t s) {
     const StepConfig c = step_config(h);
     cudaError_t e = cudaSuccess;
-    if (phase == 0) e = launch_nodal_kinematics(c, h->hs, h->dtiles, h->ntiles, h->ctl, k, s);
-    else if (phase == 1) e = launch_forces(c, h->hs, h->dtiles, h->ntiles, h->ctl, k, s);
-    else e = launch_particle_kinematics(c, h->hs, h->dtiles, h->ntiles, h->ctl, k, s);
+    if (phase == 0) {
+        CK(h, launch_empty_nodes(h->hs, h->d_empty, h->ntiles, h->ctl, k, s));
+        e = launch_nodal_kinematics(c, h->hs, h->d_active, h->ntiles, h->ctl, k, s);
+    } else if (phase == 1) {
+        e = launch_forces(c, h->hs, h->d_active, h->ntiles, h->ctl, k, s);
+    } else {
+        e = launch_particle_kinematics(c, h->hs, h->d_active, h->ntiles, h->ctl, k, s);
+    }
     CK(h, e);
     return MPM_OK;
 }
 
 int launch_steps(MpmHandle* h, int n, cudaStream_t s) {
+    TRY(classify_tiles(h, s));
     for (int i = 0; i < n; ++i)
         for (int p = 0; p < 3; ++p) TRY(launch_phase(h, p, i, s));
     CK(h, launch_advance_step(h->ctl, n, s));
@@ -663,6 +677,17 @@ int mpm_create(const MpmDesc* d, MpmHandle** out) {
         return bail(MPM_ERR_NOMEM);
     }
     up(h->dtiles, tiles.data(), sizeof(int4) * tiles.size());
+    if (dalloc(h, &h->d_active, tiles.size()) != MPM_OK || dalloc(h, &h->d_empty, tiles.size()) != MPM_OK ||
+        dalloc(h, &h->d_tile_flags, tiles.size()) != MPM_OK) {
+        g_create_error = h->err;
+        return bail(MPM_ERR_NOMEM);
+    }
+    {
+        // until the first classification: every tile active, none empty
+        std::vector<int4> none(tiles.size(), make_int4(-1, 0, 0, 0));
+        up(h->d_active, tiles.data(), sizeof(int4) * tiles.size());
+        up(h->d_empty, none.data(), sizeof(int4) * tiles.size());
+    }
     if (r != MPM_OK) return failc(r, "tile upload failed");
 
     SimDev& s = h->hs;
@@ -1126,6 +1151,7 @@ int mpm_run_phase(MpmHandle* h, int phase, void* stream) {
     if (h->ndim == 1) return fail(h, MPM_ERR_UNSUPPORTED, "single phases are not available in 1-D");
     cudaStream_t s = S(stream);
     if (phase == 0 && h->needs_resort) TRY(resort(h, s));
+    if (phase == 0) TRY(classify_tiles(h, s));
     TRY(launch_phase(h, phase, 0, s));
     if (phase == 2) {
         CK(h, launch_advance_step(h->ctl, 1, s));
@@ -1206,6 +1232,7 @@ int mpm_time_phases(MpmHandle* h, int nsteps, float* ms_out, void* stream) {
     if (h->ndim == 1) return fail(h, MPM_ERR_UNSUPPORTED, "phase timing is not available in 1-D");
     cudaStream_t s = S(stream);
     if (h->needs_resort) TRY(resort(h, s));
+    TRY(classify_tiles(h, s));
     std::vector<cudaEvent_t> ev((size_t)3 * nsteps + 1);
     for (auto& e : ev) CK(h, cudaEventCreate(&e));
     int r = MPM_OK;

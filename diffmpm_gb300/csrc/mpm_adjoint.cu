@@ -368,6 +368,7 @@ int rerun_graph(MpmHandle* h, AdjointState* a, int len, cudaStream_t s) {
     TRY(prepare_adj_graphs(h, a, s));
     const int par0 = parity(h);
     TRY(run_cached_graph(h, a->g_rerun, 2 * len + par0, s, [&](cudaStream_t c) -> int {
+        TRY(classify_tiles(h, c));   // the restored checkpoint's sort
         for (int t = 0; t < len; ++t) {
             const SegBuf& tp = a->g_tp[(par0 + t) & 1];
             CK(h, launch_copy_segments(tp.segs, tp.first, tp.nseg, tp.nblocks, t, c));

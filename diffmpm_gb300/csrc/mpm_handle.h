@@ -109,6 +109,12 @@ struct MpmHandle {
     mpm::Control* h_ctl = nullptr;   // pinned mirror
     int4* dtiles = nullptr;
     int ntiles = 0;
+    // the tiles split by launch_classify_tiles (active: the step kernels'
+    // grid; empty: node updates only), refreshed at the start of every
+    // launched sequence
+    int4* d_active = nullptr;
+    int4* d_empty = nullptr;
+    int* d_tile_flags = nullptr;
     int64_t step = 0;
     // staging and pointer tables
     void* stage = nullptr;
@@ -193,6 +199,8 @@ int resort(MpmHandle* h, cudaStream_t s);
 int launch_steps(MpmHandle* h, int n, cudaStream_t s);
 // Phase `phase` (0 nodal kinematics, 1 forces, 2 G2P) of step ctl->step + k.
 int launch_phase(MpmHandle* h, int phase, int k, cudaStream_t s);
+// Active / empty tile lists for the current sort (before a sequence of launch_phase).
+int classify_tiles(MpmHandle* h, cudaStream_t s);
 int check_status(MpmHandle* h, int& st);
 int take_snapshot(MpmHandle* h, cudaStream_t s);
 int replay_block(MpmHandle* h, int64_t step0, int B, int& st, cudaStream_t s);

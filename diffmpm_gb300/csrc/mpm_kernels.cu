@@ -275,7 +275,7 @@ __device__ __forceinline__ TileLoads record_loads(const SimDev& S, const TileDes
     L.cs = rec.cs[r][lane];
     L.cs32 = lane == 0 ? rec.cs[r][32] : 0;
     L.occ = rec.occ;
-    L.drift = tile_drift(S, c0x, c0y);
+    L.drift = rec.occ ? tile_drift(S, c0x, c0y) : 0;   // an empty tile needs no drift flags
     return L;
 }
 
@@ -579,7 +579,9 @@ template <bool REINIT, int MINB = TILE_CTAS_LIGHT>
 __global__ void __launch_bounds__(TILE_THREADS, MINB)
 k_nodal_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
                    Control* __restrict__ ctl, int k) {
-    nodal_kinematics_tile<REINIT>(S, tiles[blockIdx.x], ctl, k);
+    const int4 T = tiles[blockIdx.x];
+    if (T.x < 0) return;   // past the active tiles
+    nodal_kinematics_tile<REINIT>(S, T, ctl, k);
 }
 
 template <bool REINIT, int MINB = TILE_CTAS_LIGHT>
@@ -813,7 +815,9 @@ template <bool USL, bool REINIT, bool TRAC, bool LPC = false>
 __global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
 k_forces(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
          Control* __restrict__ ctl, int k) {
-    forces_tile<USL, REINIT, TRAC, false, LPC>(S, tiles[blockIdx.x], ctl, k);
+    const int4 T = tiles[blockIdx.x];
+    if (T.x < 0) return;
+    forces_tile<USL, REINIT, TRAC, false, LPC>(S, T, ctl, k);
 }
 
 template <bool USL, bool REINIT, bool TRAC, bool LPC = false>
@@ -1173,7 +1177,9 @@ template <bool USL, bool REINIT, int MINB = (USL ? TILE_MIN_CTAS : TILE_CTAS_LIG
 __global__ void __launch_bounds__(TILE_THREADS, MINB)
 k_particle_kinematics(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
                       Control* __restrict__ ctl, int k) {
-    particle_kinematics_tile<USL, REINIT>(S, tiles[blockIdx.x], ctl, k);
+    const int4 T = tiles[blockIdx.x];
+    if (T.x < 0) return;
+    particle_kinematics_tile<USL, REINIT>(S, T, ctl, k);
 }
 
 template <bool USL, bool REINIT, int MINB = (USL ? TILE_MIN_CTAS : TILE_CTAS_LIGHT)>
@@ -1181,6 +1187,10 @@ __global__ void __launch_bounds__(TILE_THREADS, MINB)
 k_particle_kinematics_batch(const TileDesc* __restrict__ td, int k) {
     __shared__ TileDesc sT;
     load_tile(td + blockIdx.x, sT);
+    // no particle stored in the tile's sort-cells or around them: nothing
+    // moves, and the sort-cells' drift flags are already clear (a flag is set
+    // only for a sort-cell that stores a particle, and a re-sort clears all)
+    if (!sT.occ) return;
     particle_kinematics_tile<USL, REINIT, true>(sT.S, sT.T, sT.ctl, k, &sT);
 }
 
@@ -1403,6 +1413,99 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int* total) {
     if (total) *total = warp_sums[(blockDim.x >> 5) - 1];
     __syncthreads();
     return base + x - v;
+}
+
+// ---------------------------------------------------------------------------
+// Tile classification.  A tile whose cells and the ring of sort-cells around
+// them store no particle receives none during a step block (a particle is at
+// most one cell from its sort-cell, and the sort changes only between
+// blocks), so its step is a node update only.  At the start of every launched
+// sequence the tiles are split into an active list (the step kernels' grid;
+// the rest of the grid returns at once) and an empty list (k_empty_nodes),
+// each in tile order and padded to ntiles entries with (-1, 0, 0, 0).
+// ---------------------------------------------------------------------------
+__global__ void k_tile_flags(const __grid_constant__ SimDev S, const int4* __restrict__ tiles, int ntiles,
+                             int* __restrict__ flags) {
+    const int t = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32, lane = threadIdx.x & 31;
+    if (t >= ntiles) return;
+    const int4 T = tiles[t];
+    const int c0x = T.y * TILE_NX - 1, c0y = T.z * TILE_NY - 1;
+    const int x0 = max(c0x - 1, 0), x1 = min(c0x + TILE_CX + 1, S.nx);
+    const int y0 = max(c0y - 1, 0), y1 = min(c0y + TILE_CY + 1, S.ny);
+    int occ = 0;
+    if (x0 < x1)
+        for (int r = y0 + lane; r < y1; r += 32) occ |= S.cstart[r * S.nx + x1] != S.cstart[r * S.nx + x0];
+    occ = __any_sync(0xffffffffu, occ);
+    if (lane == 0) flags[t] = occ;
+}
+
+__global__ void __launch_bounds__(1024)
+k_compact_tiles(const int* __restrict__ flags, const int4* __restrict__ tiles, int ntiles,
+                int4* __restrict__ active, int4* __restrict__ empty) {
+    __shared__ int base[2];
+    if (threadIdx.x == 0) base[0] = base[1] = 0;
+    __syncthreads();
+    for (int c = 0; c < ntiles; c += 1024) {
+        const int t = c + (int)threadIdx.x;
+        const int f = t < ntiles ? (flags[t] != 0) : 0;
+        const int g = t < ntiles ? 1 - f : 0;
+        int tot_a, tot_e;
+        const int pa = block_exclusive_scan(f, &tot_a);
+        const int pe = block_exclusive_scan(g, &tot_e);
+        if (t < ntiles) {
+            if (f) active[base[0] + pa] = tiles[t];
+            else empty[base[1] + pe] = tiles[t];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            base[0] += tot_a;
+            base[1] += tot_e;
+        }
+        __syncthreads();
+    }
+    const int4 none = make_int4(-1, 0, 0, 0);
+    for (int i = base[0] + (int)threadIdx.x; i < ntiles; i += 1024) active[i] = none;
+    for (int i = base[1] + (int)threadIdx.x; i < ntiles; i += 1024) empty[i] = none;
+}
+
+cudaError_t launch_classify_tiles(const SimDev& S, const int4* tiles, int ntiles, int* flags, int4* active,
+                                  int4* empty, cudaStream_t s) {
+    if (ntiles > 0) {
+        k_tile_flags<<<(ntiles + 7) / 8, 256, 0, s>>>(S, tiles, ntiles, flags);
+        k_compact_tiles<<<1, 1024, 0, s>>>(flags, tiles, ntiles, active, empty);
+    }
+    return cudaGetLastError();
+}
+
+// The step of the nodes of an empty tile: the nodal kinematics of a massless
+// node (nodal_kinematics_tile's empty path) and the nodal update with no
+// particle force (forces_tile's empty path), in one pass.  It runs before
+// the step's nodal-kinematics launch: no other tile reads these nodes' values
+// until the forces kernel (their velocity after nodal kinematics) and G2P
+// (their updated velocity and acceleration).
+__global__ void __launch_bounds__(TILE_THREADS)
+k_empty_nodes(const __grid_constant__ SimDev S, const int4* __restrict__ empty, Control* __restrict__ ctl,
+              int k) {
+    const int4 T = empty[blockIdx.x];
+    if (T.x < 0) return;
+    const int tid = threadIdx.x, lx = tid & (TILE_CX - 1), ly = tid / TILE_CX;
+    const int c0x = T.y * TILE_NX - 1, c0y = T.z * TILE_NY - 1;
+    if (!(lx < TILE_NX && ly < TILE_NY && c0x + 1 + lx <= S.nx && c0y + 1 + ly <= S.ny)) return;
+    const int node = (c0y + 1 + ly) * (S.nx + 1) + c0x + 1 + lx;
+    const uint16_t ncons = S.ncons[node];
+    float vx = flush(S.nvbx[node]), vy = flush(S.nvby[node]);
+    apply_constraint(S, ncons, vx, vy, nullptr, nullptr);
+    S.nm[node] = 0.0f;
+    S.nvax[node] = vx;
+    S.nvay[node] = vy;
+    const int step = load_step(ctl) + k;
+    nodal_update(S, node, step_time(step, S.dt), 0.0f, 0.0f, vx, vy, 0.0f, ncons);
+}
+
+cudaError_t launch_empty_nodes(const SimDev& S, const int4* empty, int ntiles, Control* ctl, int k,
+                               cudaStream_t s) {
+    if (ntiles > 0) k_empty_nodes<<<ntiles, TILE_THREADS, 0, s>>>(S, empty, ctl, k);
+    return cudaGetLastError();
 }
 
 __global__ void k_scan_blocks(const int* __restrict__ in, int* __restrict__ out, int n,

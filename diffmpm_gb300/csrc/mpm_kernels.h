@@ -29,6 +29,15 @@ cudaError_t launch_forces(const StepConfig& c, const SimDev& S, const int4* tile
                           Control* ctl, int k, cudaStream_t s);
 cudaError_t launch_particle_kinematics(const StepConfig& c, const SimDev& S, const int4* tiles,
                                        int ntiles, Control* ctl, int k, cudaStream_t s);
+// Split the tile list into active tiles (cells or their ring store a
+// particle; the step kernels' grid) and empty ones (node updates only,
+// k_empty_nodes), both padded to ntiles entries with (-1, 0, 0, 0); flags is
+// ntiles ints of scratch.  Valid until the sort changes.
+cudaError_t launch_classify_tiles(const SimDev& S, const int4* tiles, int ntiles, int* flags, int4* active,
+                                  int4* empty, cudaStream_t s);
+// The step's node updates of the empty tiles (before the nodal kinematics).
+cudaError_t launch_empty_nodes(const SimDev& S, const int4* empty, int ntiles, Control* ctl, int k,
+                               cudaStream_t s);
 // The kernels above work on step (ctl->step + k); these advance the counter
 // once a sequence of steps has been launched.
 cudaError_t launch_advance_step(Control* ctl, int by, cudaStream_t s);
