@@ -215,8 +215,18 @@ StepConfig step_config(const MpmHandle* h) {
 // Split the tiles into active and empty ones for the current sort (see
 // launch_classify_tiles); every launched sequence of steps starts with it.
 int classify_tiles(MpmHandle* h, cudaStream_t s) {
-    CK(h, launch_classify_tiles(h->hs, h->dtiles, h->ntiles, h->d_tile_flags, h->d_active, h->d_empty, s));
+    CK(h, launch_classify_tiles(h->hs, h->dtiles, h->ntiles, h->d_tile_flags, h->d_active, h->d_empty,
+                                h->d_tile_counts, s));
+    CK(h, cudaMemcpyAsync(h->h_tile_counts, h->d_tile_counts, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(h, cudaStreamSynchronize(s));
+    h->nact = h->h_tile_counts[0];
+    h->nemp = h->h_tile_counts[1];
     return MPM_OK;
+}
+
+// Graph-cache key of a step sequence: its length and the grids it launches.
+int64_t seq_key(const MpmHandle* h, int n) {
+    return (int64_t)n | ((int64_t)h->nact << 24) | ((int64_t)h->nemp << 44);
 }
 
 // One phase of step (ctl->step + k) over the active tiles (the empty tiles'
@@ -226,19 +236,18 @@ int launch_phase(MpmHandle* h, int phase, int k, cudaStream_t s) {
     const StepConfig c = step_config(h);
     cudaError_t e = cudaSuccess;
     if (phase == 0) {
-        CK(h, launch_empty_nodes(h->hs, h->d_empty, h->ntiles, h->ctl, k, s));
-        e = launch_nodal_kinematics(c, h->hs, h->d_active, h->ntiles, h->ctl, k, s);
+        CK(h, launch_empty_nodes(h->hs, h->d_empty, h->nemp, h->ctl, k, s));
+        e = launch_nodal_kinematics(c, h->hs, h->d_active, h->nact, h->ctl, k, s);
     } else if (phase == 1) {
-        e = launch_forces(c, h->hs, h->d_active, h->ntiles, h->ctl, k, s);
+        e = launch_forces(c, h->hs, h->d_active, h->nact, h->ctl, k, s);
     } else {
-        e = launch_particle_kinematics(c, h->hs, h->d_active, h->ntiles, h->ctl, k, s);
+        e = launch_particle_kinematics(c, h->hs, h->d_active, h->nact, h->ctl, k, s);
     }
     CK(h, e);
     return MPM_OK;
 }
 
 int launch_steps(MpmHandle* h, int n, cudaStream_t s) {
-    TRY(classify_tiles(h, s));
     for (int i = 0; i < n; ++i)
         for (int p = 0; p < 3; ++p) TRY(launch_phase(h, p, i, s));
     CK(h, launch_advance_step(h->ctl, n, s));
@@ -252,7 +261,9 @@ int run_graph(MpmHandle* h, int n, cudaStream_t s) {
         drop_graphs(h);
         h->graphs_trac = h->has_trac;
     }
-    auto it = h->graphs.find(n);
+    TRY(classify_tiles(h, s));
+    const int64_t key = seq_key(h, n);
+    auto it = h->graphs.find(key);
     if (it == h->graphs.end()) {
         cudaGraph_t g = nullptr;
         CK(h, cudaStreamBeginCapture(h->cap, cudaStreamCaptureModeThreadLocal));
@@ -267,7 +278,7 @@ int run_graph(MpmHandle* h, int n, cudaStream_t s) {
         e = cudaGraphInstantiate(&ex, g, 0);
         cudaGraphDestroy(g);
         CK(h, e);
-        it = h->graphs.emplace(n, ex).first;
+        it = h->graphs.emplace(key, ex).first;
     }
     CK(h, cudaGraphLaunch(it->second, s));
     return MPM_OK;
@@ -428,6 +439,7 @@ int replay_block(MpmHandle* h, int64_t step0, int B, int& st, cudaStream_t s) {
     st = 0;
     for (int i = 0; i < B; ++i) {
         if (st & ST_DRIFTED) TRY(resort(h, s));
+        TRY(classify_tiles(h, s));
         TRY(launch_steps(h, 1, s));
         h->step++;
         TRY(read_ctl(h, s));
@@ -636,6 +648,7 @@ int mpm_create(const MpmDesc* d, MpmHandle** out) {
     A(&h->d_ptrs, 16);
 #undef A
     cudaError_t e = cudaMallocHost(&h->h_ctl, sizeof(Control));
+    if (e == cudaSuccess) e = cudaMallocHost(&h->h_tile_counts, 2 * sizeof(int));
     if (e != cudaSuccess) return failc(MPM_ERR_NOMEM, "cudaMallocHost failed");
     e = cudaStreamCreateWithFlags(&h->cap, cudaStreamNonBlocking);
     if (e != cudaSuccess) return failc(MPM_ERR_CUDA, "cudaStreamCreate failed");
@@ -678,7 +691,7 @@ int mpm_create(const MpmDesc* d, MpmHandle** out) {
     }
     up(h->dtiles, tiles.data(), sizeof(int4) * tiles.size());
     if (dalloc(h, &h->d_active, tiles.size()) != MPM_OK || dalloc(h, &h->d_empty, tiles.size()) != MPM_OK ||
-        dalloc(h, &h->d_tile_flags, tiles.size()) != MPM_OK) {
+        dalloc(h, &h->d_tile_flags, tiles.size()) != MPM_OK || dalloc(h, &h->d_tile_counts, 2) != MPM_OK) {
         g_create_error = h->err;
         return bail(MPM_ERR_NOMEM);
     }
@@ -687,6 +700,8 @@ int mpm_create(const MpmDesc* d, MpmHandle** out) {
         std::vector<int4> none(tiles.size(), make_int4(-1, 0, 0, 0));
         up(h->d_active, tiles.data(), sizeof(int4) * tiles.size());
         up(h->d_empty, none.data(), sizeof(int4) * tiles.size());
+        h->nact = (int)tiles.size();
+        h->nemp = 0;
     }
     if (r != MPM_OK) return failc(r, "tile upload failed");
 
@@ -720,6 +735,7 @@ int mpm_destroy(MpmHandle* h) {
     for (void* p : h->allocs) cudaFree(p);
     h->allocs.clear();
     if (h->h_ctl) cudaFreeHost(h->h_ctl);
+    if (h->h_tile_counts) cudaFreeHost(h->h_tile_counts);
     delete h;
     return MPM_OK;
 }

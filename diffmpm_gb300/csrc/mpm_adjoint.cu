@@ -92,7 +92,7 @@ struct AdjointState {
     // (keyed by length).  They hold the step descriptor and every buffer
     // pointer by value, so they are dropped when the handle's step graphs are
     // (g_gen != graph_gen) and whenever a buffer here is (re)allocated.
-    std::map<int, cudaGraphExec_t> g_rerun, g_rev;
+    std::map<int64_t, cudaGraphExec_t> g_rerun, g_rev;
     SegBuf g_tp[2], g_tn;      // tape copy tables of the re-run graphs
     uint64_t g_gen = ~0ull;
 };
@@ -338,7 +338,7 @@ int prepare_adj_graphs(MpmHandle* h, AdjointState* a, cudaStream_t s) {
 // Capture the launches that `body` issues on the handle's capture stream
 // into an executable graph stored at map[key] (if absent), then launch it.
 template <class F>
-int run_cached_graph(MpmHandle* h, std::map<int, cudaGraphExec_t>& map, int key, cudaStream_t s,
+int run_cached_graph(MpmHandle* h, std::map<int64_t, cudaGraphExec_t>& map, int64_t key, cudaStream_t s,
                      F&& body) {
     auto it = map.find(key);
     if (it == map.end()) {
@@ -366,9 +366,9 @@ int run_cached_graph(MpmHandle* h, std::map<int, cudaGraphExec_t>& map, int key,
 // t) and the tape copy of the nodal results; the step counter advances once.
 int rerun_graph(MpmHandle* h, AdjointState* a, int len, cudaStream_t s) {
     TRY(prepare_adj_graphs(h, a, s));
+    TRY(classify_tiles(h, s));   // the restored checkpoint's sort
     const int par0 = parity(h);
-    TRY(run_cached_graph(h, a->g_rerun, 2 * len + par0, s, [&](cudaStream_t c) -> int {
-        TRY(classify_tiles(h, c));   // the restored checkpoint's sort
+    TRY(run_cached_graph(h, a->g_rerun, seq_key(h, 2 * len + par0), s, [&](cudaStream_t c) -> int {
         for (int t = 0; t < len; ++t) {
             const SegBuf& tp = a->g_tp[(par0 + t) & 1];
             CK(h, launch_copy_segments(tp.segs, tp.first, tp.nseg, tp.nblocks, t, c));
@@ -414,6 +414,10 @@ int recompute_segment(MpmHandle* h, AdjointState* a, int seg, int len, cudaStrea
             r = upload_segments(h, tp, v, s);
             if (r != MPM_OK) break;
             tp_par = par;
+        }
+        if (t == 0 || resorts_at(a, first + t)) {   // the sort of the step (restored or re-sorted)
+            r = classify_tiles(h, s);
+            if (r != MPM_OK) break;
         }
         cudaError_t e = launch_copy_segments(tp.segs, tp.first, tp.nseg, tp.nblocks, t, s);
         if (e == cudaSuccess) {
@@ -711,7 +715,11 @@ int batch_recompute(MpmBatch* b, BatchAdjoint* x, int seg, int len, cudaStream_t
         BCK(b, launch_copy_segments(tp.segs, tp.first, tp.nseg, tp.nblocks, t, s));
         // the tile records hold the sort: refreshed at the segment start and
         // after a re-sort only
-        r = launch_batch_steps(b, 1, s, t == 0 || resorted);
+        if (t == 0 || resorted) {
+            r = prepare_tiles(b, s);
+            if (r != MPM_OK) return r;
+        }
+        r = launch_batch_steps(b, 1, s);
         if (r != MPM_OK) return r;
         for (MpmHandle* h : b->sims) h->step++;
         BCK(b, launch_copy_segments(x->tape_n.segs, x->tape_n.first, x->tape_n.nseg,

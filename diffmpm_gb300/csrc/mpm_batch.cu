@@ -54,23 +54,37 @@ void drop_batch_graphs(MpmBatch* b) {
     b->graphs.clear();
 }
 
-int launch_batch_steps(MpmBatch* b, int n, cudaStream_t s, bool gather) {
+int prepare_tiles(MpmBatch* b, cudaStream_t s) {
     // the descriptors and row starts change only between step blocks
     // (re-sorts, set-up calls): one record per tile and block lets a CTA fetch
     // its tile, descriptor, control pointer and row starts in one read
-    if (gather)
-        BCK(b, launch_gather_tiles(b->d_sims, b->d_ctls, b->d_tiles, b->ntiles, b->d_tdescs, s));
+    BCK(b, launch_classify_tiles_batch(b->d_sims, b->d_tiles, b->ntiles, b->d_tflags, b->d_act_list,
+                                       b->d_emp_list, b->d_tcounts, s));
+    BCK(b, launch_gather_tiles(b->d_sims, b->d_ctls, b->d_act_list, b->ntiles, b->d_tdescs, s));
+    BCK(b, launch_gather_tiles(b->d_sims, b->d_ctls, b->d_emp_list, b->ntiles, b->d_edescs, s));
+    BCK(b, cudaMemcpyAsync(b->h_tcounts, b->d_tcounts, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    BCK(b, cudaStreamSynchronize(s));
+    b->nact = b->h_tcounts[0];
+    b->nemp = b->h_tcounts[1];
+    return MPM_OK;
+}
+
+int launch_batch_steps(MpmBatch* b, int n, cudaStream_t s) {
     for (int i = 0; i < n; ++i) {
-        BCK(b, launch_nodal_kinematics_batch(b->cfg, b->d_tdescs, b->ntiles, i, s));
-        BCK(b, launch_forces_batch(b->cfg, b->d_tdescs, b->ntiles, i, s));
-        BCK(b, launch_particle_kinematics_batch(b->cfg, b->d_tdescs, b->ntiles, i, s));
+        BCK(b, launch_empty_nodes_batch(b->d_edescs, b->nemp, i, s));
+        BCK(b, launch_nodal_kinematics_batch(b->cfg, b->d_tdescs, b->nact, i, s));
+        BCK(b, launch_forces_batch(b->cfg, b->d_tdescs, b->nact, i, s));
+        BCK(b, launch_particle_kinematics_batch(b->cfg, b->d_tdescs, b->nact, i, s));
     }
     BCK(b, launch_advance_steps(b->d_ctls, (int)b->sims.size(), n, s));
     return MPM_OK;
 }
 
 int run_batch_graph(MpmBatch* b, int n, cudaStream_t s) {
-    auto it = b->graphs.find(n);
+    int r0 = prepare_tiles(b, s);
+    if (r0 != MPM_OK) return r0;
+    const int64_t key = (int64_t)n | ((int64_t)b->nact << 24) | ((int64_t)b->nemp << 44);
+    auto it = b->graphs.find(key);
     if (it == b->graphs.end()) {
         cudaGraph_t g = nullptr;
         BCK(b, cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal));
@@ -85,7 +99,7 @@ int run_batch_graph(MpmBatch* b, int n, cudaStream_t s) {
         e = cudaGraphInstantiate(&ex, g, 0);
         cudaGraphDestroy(g);
         BCK(b, e);
-        it = b->graphs.emplace(n, ex).first;
+        it = b->graphs.emplace(key, ex).first;
     }
     BCK(b, cudaGraphLaunch(it->second, s));
     return MPM_OK;
@@ -227,8 +241,14 @@ int mpm_batch_create(MpmHandle* const* sims, int n, MpmBatch** out) {
     };
     cudaError_t e;
     if ((e = cudaMalloc(&b->d_sims, sizeof(SimDev*) * n)) != cudaSuccess) return bail("cudaMalloc", e);
-    if ((e = cudaMalloc(&b->d_tdescs, sizeof(TileDesc) * tiles.size())) != cudaSuccess)
+    if ((e = cudaMalloc(&b->d_tdescs, sizeof(TileDesc) * tiles.size())) != cudaSuccess ||
+        (e = cudaMalloc(&b->d_edescs, sizeof(TileDesc) * tiles.size())) != cudaSuccess ||
+        (e = cudaMalloc(&b->d_act_list, sizeof(int4) * tiles.size())) != cudaSuccess ||
+        (e = cudaMalloc(&b->d_emp_list, sizeof(int4) * tiles.size())) != cudaSuccess ||
+        (e = cudaMalloc(&b->d_tflags, sizeof(int) * tiles.size())) != cudaSuccess ||
+        (e = cudaMalloc(&b->d_tcounts, sizeof(int) * 2)) != cudaSuccess)
         return bail("cudaMalloc", e);
+    if ((e = cudaMallocHost(&b->h_tcounts, sizeof(int) * 2)) != cudaSuccess) return bail("cudaMallocHost", e);
     if ((e = cudaMalloc(&b->d_ctls, sizeof(Control*) * n)) != cudaSuccess) return bail("cudaMalloc", e);
     if ((e = cudaMalloc(&b->d_tiles, sizeof(int4) * tiles.size())) != cudaSuccess) return bail("cudaMalloc", e);
     if ((e = cudaMalloc(&b->d_status, sizeof(Control) * n)) != cudaSuccess) return bail("cudaMalloc", e);
@@ -252,6 +272,12 @@ int mpm_batch_destroy(MpmBatch* b) {
     if (b->cap) cudaStreamDestroy(b->cap);
     cudaFree(b->d_sims);
     cudaFree(b->d_tdescs);
+    cudaFree(b->d_edescs);
+    cudaFree(b->d_act_list);
+    cudaFree(b->d_emp_list);
+    cudaFree(b->d_tflags);
+    cudaFree(b->d_tcounts);
+    if (b->h_tcounts) cudaFreeHost(b->h_tcounts);
     cudaFree(b->d_stage);
     cudaFree(b->d_ctls);
     cudaFree(b->d_tiles);

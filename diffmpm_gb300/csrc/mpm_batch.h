@@ -16,7 +16,14 @@ struct MpmBatch {
     std::vector<MpmHandle*> sims;
     mpm::StepConfig cfg{};
     const mpm::SimDev** d_sims = nullptr;
-    mpm::TileDesc* d_tdescs = nullptr;  // per-tile descriptor copies, refreshed per block
+    mpm::TileDesc* d_tdescs = nullptr;  // records of the active tiles, refreshed per block
+    mpm::TileDesc* d_edescs = nullptr;  // records of the empty tiles (node updates only)
+    int4* d_act_list = nullptr;         // the tile list split by launch_classify_tiles_batch
+    int4* d_emp_list = nullptr;
+    int* d_tflags = nullptr;
+    int* d_tcounts = nullptr;           // [active, empty]
+    int* h_tcounts = nullptr;           // pinned
+    int nact = 0, nemp = 0;
     void* d_stage = nullptr;            // staging of whole-batch field transfers
     size_t stage_bytes = 0;
     mpm::Control** d_ctls = nullptr;
@@ -28,7 +35,7 @@ struct MpmBatch {
     int resort_every = 1;               // re-sort a drifted simulation every this many blocks
     std::vector<int> since_resort;      // blocks each simulation has run since it drifted
     cudaStream_t cap = nullptr;
-    std::map<int, cudaGraphExec_t> graphs;
+    std::map<int64_t, cudaGraphExec_t> graphs;   // keyed by steps and tile counts
     mpm::SegBuf segbuf;
     std::vector<mpm::Checkpoint> tune;  // per-simulation state saved by the autotuner
     mpm::BatchAdjoint* badj = nullptr;
@@ -42,10 +49,14 @@ int bfail(MpmBatch* b, int code, const char* fmt, ...);
 // A failure reported on simulation i's handle, copied to the batch.
 int from_sim(MpmBatch* b, int i, int code);
 int check_ready(MpmBatch* b);
-// n steps of every simulation as 3n batched launches (no status handling),
-// after refreshing the tile records when `gather` (needed whenever a
-// descriptor or a sort changed since the last refresh).
-int launch_batch_steps(MpmBatch* b, int n, cudaStream_t s, bool gather = true);
+// Split the batch's tiles into active and empty ones and write their records
+// (descriptor, row starts, occupancy) for the current descriptors and sorts;
+// needed whenever a descriptor or a sort changed.  Waits for the counts, so
+// not inside a stream capture.
+int prepare_tiles(MpmBatch* b, cudaStream_t s);
+// n steps of every simulation as 3n batched launches over the active tiles
+// plus one over the empty tiles per step (no status handling).
+int launch_batch_steps(MpmBatch* b, int n, cudaStream_t s);
 // Gather every control block into b->h_status and clear the status words.
 int read_statuses(MpmBatch* b, cudaStream_t s);
 // Advance every simulation by nsteps steps in blocks (re-sorts, snapshots,

@@ -115,6 +115,9 @@ struct MpmHandle {
     int4* d_active = nullptr;
     int4* d_empty = nullptr;
     int* d_tile_flags = nullptr;
+    int* d_tile_counts = nullptr;    // [active, empty]
+    int* h_tile_counts = nullptr;    // pinned mirror
+    int nact = 0, nemp = 0;          // the step kernels' and the empty-node kernel's grids
     int64_t step = 0;
     // staging and pointer tables
     void* stage = nullptr;
@@ -130,7 +133,7 @@ struct MpmHandle {
     int64_t out_tickets = 0;
     // graphs
     cudaStream_t cap = nullptr;
-    std::map<int, cudaGraphExec_t> graphs;
+    std::map<int64_t, cudaGraphExec_t> graphs;   // keyed by steps and the tile counts
     bool graphs_trac = false;
     uint64_t graph_gen = 0;            // bumped whenever the step graphs are dropped
     bool has_pvc = false;              // particle velocity constraints set
@@ -199,8 +202,12 @@ int resort(MpmHandle* h, cudaStream_t s);
 int launch_steps(MpmHandle* h, int n, cudaStream_t s);
 // Phase `phase` (0 nodal kinematics, 1 forces, 2 G2P) of step ctl->step + k.
 int launch_phase(MpmHandle* h, int phase, int k, cudaStream_t s);
-// Active / empty tile lists for the current sort (before a sequence of launch_phase).
+// Active / empty tile lists and their counts (nact, nemp) for the current
+// sort; call before a sequence of launch_phase (it waits for the counts, so
+// not inside a stream capture).
 int classify_tiles(MpmHandle* h, cudaStream_t s);
+// Graph-cache key of a step sequence: its length and the tile counts it launches for.
+int64_t seq_key(const MpmHandle* h, int n);
 int check_status(MpmHandle* h, int& st);
 int take_snapshot(MpmHandle* h, cudaStream_t s);
 int replay_block(MpmHandle* h, int64_t step0, int B, int& st, cudaStream_t s);

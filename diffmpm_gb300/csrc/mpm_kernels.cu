@@ -16,6 +16,7 @@
 // the neighbouring sort-cells whose drift flag is set.  A particle that drifts
 // two cells away sets ST_DRIFT_VIOLATION and the host rolls the block back.
 #include <cuda_runtime.h>
+#include <cstddef>
 #include <cstdint>
 #include <type_traits>
 #include "mpm_device.cuh"
@@ -36,6 +37,10 @@ __global__ void k_gather_tiles(const SimDev* const* __restrict__ sims, Control* 
     if (t >= ntiles) return;
     const int4 T = tiles[t];
     TileDesc& d = out[t];
+    if (T.x < 0) {   // past the end of a classified list
+        if (lane == 0) d.T = T;
+        return;
+    }
     if (lane == 0) {
         d.T = T;
         d.ctl = ctls[T.x];
@@ -595,7 +600,15 @@ k_nodal_kinematics_batch(const TileDesc* __restrict__ td, int k) {
 // Nodal update shared by both schemes: concentrated forces (element.py:270-284),
 // a = nan_to_num(f/m), v += a dt, constraints, flush (element.py:305-329).
 // (fx, fy) is the summed internal plus external force of the particles.
-template <bool VD = false>
+// f / 0 after nan_to_num, exactly as nan_to_num(fdv(f, +0)) gives it
+// (+-FLT_MAX for a force of that sign, 0 for a zero or NaN force), without
+// the division's special-case path.
+__device__ __forceinline__ float massless_accel(float f) {
+    return f > 0.0f ? FLT_MAX : (f < 0.0f ? -FLT_MAX : 0.0f);
+}
+
+// MASSLESS: the node's mass is +0 (a node of an empty tile).
+template <bool VD = false, bool MASSLESS = false>
 __device__ __forceinline__ void nodal_update(const SimDev& S, int n, float t, float fx, float fy,
                                              float v0x, float v0y, float mass, uint16_t ncons) {
     if (rd<VD>(S.cnf_ptr)) {
@@ -609,8 +622,8 @@ __device__ __forceinline__ void nodal_update(const SimDev& S, int n, float t, fl
     }
     const float tx = fa(fx, 0.0f);   // + f_damp (zero, node.py:71)
     const float ty = fa(fy, 0.0f);
-    float ax = nan_to_num(fdv(tx, mass));
-    float ay = nan_to_num(fdv(ty, mass));
+    float ax = MASSLESS ? massless_accel(tx) : nan_to_num(fdv(tx, mass));
+    float ay = MASSLESS ? massless_accel(ty) : nan_to_num(fdv(ty, mass));
     const float dt = rd<VD>(S.dt);
     float vx = fa(v0x, fm(ax, dt));
     float vy = fa(v0y, fm(ay, dt));
@@ -1441,7 +1454,7 @@ __global__ void k_tile_flags(const __grid_constant__ SimDev S, const int4* __res
 
 __global__ void __launch_bounds__(1024)
 k_compact_tiles(const int* __restrict__ flags, const int4* __restrict__ tiles, int ntiles,
-                int4* __restrict__ active, int4* __restrict__ empty) {
+                int4* __restrict__ active, int4* __restrict__ empty, int* __restrict__ counts) {
     __shared__ int base[2];
     if (threadIdx.x == 0) base[0] = base[1] = 0;
     __syncthreads();
@@ -1466,13 +1479,17 @@ k_compact_tiles(const int* __restrict__ flags, const int4* __restrict__ tiles, i
     const int4 none = make_int4(-1, 0, 0, 0);
     for (int i = base[0] + (int)threadIdx.x; i < ntiles; i += 1024) active[i] = none;
     for (int i = base[1] + (int)threadIdx.x; i < ntiles; i += 1024) empty[i] = none;
+    if (threadIdx.x == 0 && counts) {
+        counts[0] = base[0];
+        counts[1] = base[1];
+    }
 }
 
 cudaError_t launch_classify_tiles(const SimDev& S, const int4* tiles, int ntiles, int* flags, int4* active,
-                                  int4* empty, cudaStream_t s) {
+                                  int4* empty, int* counts, cudaStream_t s) {
     if (ntiles > 0) {
         k_tile_flags<<<(ntiles + 7) / 8, 256, 0, s>>>(S, tiles, ntiles, flags);
-        k_compact_tiles<<<1, 1024, 0, s>>>(flags, tiles, ntiles, active, empty);
+        k_compact_tiles<<<1, 1024, 0, s>>>(flags, tiles, ntiles, active, empty, counts);
     }
     return cudaGetLastError();
 }
@@ -1482,29 +1499,136 @@ cudaError_t launch_classify_tiles(const SimDev& S, const int4* tiles, int ntiles
 // particle force (forces_tile's empty path), in one pass.  It runs before
 // the step's nodal-kinematics launch: no other tile reads these nodes' values
 // until the forces kernel (their velocity after nodal kinematics) and G2P
-// (their updated velocity and acceleration).
-__global__ void __launch_bounds__(TILE_THREADS)
-k_empty_nodes(const __grid_constant__ SimDev S, const int4* __restrict__ empty, Control* __restrict__ ctl,
-              int k) {
-    const int4 T = empty[blockIdx.x];
-    if (T.x < 0) return;
-    const int tid = threadIdx.x, lx = tid & (TILE_CX - 1), ly = tid / TILE_CX;
-    const int c0x = T.y * TILE_NX - 1, c0y = T.z * TILE_NY - 1;
-    if (!(lx < TILE_NX && ly < TILE_NY && c0x + 1 + lx <= S.nx && c0y + 1 + ly <= S.ny)) return;
-    const int node = (c0y + 1 + ly) * (S.nx + 1) + c0x + 1 + lx;
-    const uint16_t ncons = S.ncons[node];
-    float vx = flush(S.nvbx[node]), vy = flush(S.nvby[node]);
+// (their updated velocity and acceleration).  A CTA covers EMPTY_TILES tiles,
+// thread (lx, ly) the node (lx, ly) of each, with all loads of its nodes in
+// flight together: the kernel is a few loads and stores per node, so it is
+// latency that bounds it.
+constexpr int EMPTY_TILES = 4;
+
+__device__ __forceinline__ void empty_node_step(const SimDev& S, int node, uint16_t ncons, float vbx,
+                                                float vby, float t) {
+    float vx = flush(vbx), vy = flush(vby);
     apply_constraint(S, ncons, vx, vy, nullptr, nullptr);
     S.nm[node] = 0.0f;
     S.nvax[node] = vx;
     S.nvay[node] = vy;
-    const int step = load_step(ctl) + k;
-    nodal_update(S, node, step_time(step, S.dt), 0.0f, 0.0f, vx, vy, 0.0f, ncons);
+    nodal_update<false, true>(S, node, t, 0.0f, 0.0f, vx, vy, 0.0f, ncons);
+}
+
+__global__ void __launch_bounds__(TILE_THREADS)
+k_empty_nodes(const __grid_constant__ SimDev S, const int4* __restrict__ empty, int nempty,
+              Control* __restrict__ ctl, int k) {
+    const int tid = threadIdx.x, lx = tid & (TILE_CX - 1), ly = tid / TILE_CX;
+    const float t = step_time(load_step(ctl) + k, S.dt);
+    int node[EMPTY_TILES];
+    uint16_t nc[EMPTY_TILES];
+    float vbx[EMPTY_TILES], vby[EMPTY_TILES];
+    #pragma unroll
+    for (int e = 0; e < EMPTY_TILES; ++e) {
+        const int slot = blockIdx.x * EMPTY_TILES + e;
+        node[e] = -1;
+        if (slot < nempty) {
+            const int4 T = empty[slot];
+            const int c0x = T.y * TILE_NX - 1, c0y = T.z * TILE_NY - 1;
+            if (T.x >= 0 && lx < TILE_NX && ly < TILE_NY && c0x + 1 + lx <= S.nx && c0y + 1 + ly <= S.ny)
+                node[e] = (c0y + 1 + ly) * (S.nx + 1) + c0x + 1 + lx;
+        }
+    }
+    #pragma unroll
+    for (int e = 0; e < EMPTY_TILES; ++e)
+        if (node[e] >= 0) {
+            nc[e] = S.ncons[node[e]];
+            vbx[e] = S.nvbx[node[e]];
+            vby[e] = S.nvby[node[e]];
+        }
+    #pragma unroll
+    for (int e = 0; e < EMPTY_TILES; ++e)
+        if (node[e] >= 0) empty_node_step(S, node[e], nc[e], vbx[e], vby[e], t);
 }
 
 cudaError_t launch_empty_nodes(const SimDev& S, const int4* empty, int ntiles, Control* ctl, int k,
                                cudaStream_t s) {
-    if (ntiles > 0) k_empty_nodes<<<ntiles, TILE_THREADS, 0, s>>>(S, empty, ctl, k);
+    if (ntiles > 0)
+        k_empty_nodes<<<(ntiles + EMPTY_TILES - 1) / EMPTY_TILES, TILE_THREADS, 0, s>>>(S, empty, ntiles, ctl,
+                                                                                       k);
+    return cudaGetLastError();
+}
+
+// The same split for the tiles of a batch (each tile's simulation from sims).
+__global__ void k_tile_flags_batch(const SimDev* const* __restrict__ sims, const int4* __restrict__ tiles,
+                                   int ntiles, int* __restrict__ flags) {
+    const int t = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32, lane = threadIdx.x & 31;
+    if (t >= ntiles) return;
+    const int4 T = tiles[t];
+    const SimDev* S = sims[T.x];
+    const int nx = S->nx, ny = S->ny;
+    const int* __restrict__ cstart = S->cstart;
+    const int c0x = T.y * TILE_NX - 1, c0y = T.z * TILE_NY - 1;
+    const int x0 = max(c0x - 1, 0), x1 = min(c0x + TILE_CX + 1, nx);
+    const int y0 = max(c0y - 1, 0), y1 = min(c0y + TILE_CY + 1, ny);
+    int occ = 0;
+    if (x0 < x1)
+        for (int r = y0 + lane; r < y1; r += 32) occ |= cstart[r * nx + x1] != cstart[r * nx + x0];
+    occ = __any_sync(0xffffffffu, occ);
+    if (lane == 0) flags[t] = occ;
+}
+
+cudaError_t launch_classify_tiles_batch(const SimDev* const* sims, const int4* tiles, int ntiles, int* flags,
+                                        int4* active, int4* empty, int* counts, cudaStream_t s) {
+    if (ntiles > 0) {
+        k_tile_flags_batch<<<(ntiles + 7) / 8, 256, 0, s>>>(sims, tiles, ntiles, flags);
+        k_compact_tiles<<<1, 1024, 0, s>>>(flags, tiles, ntiles, active, empty, counts);
+    }
+    return cudaGetLastError();
+}
+
+// k_empty_nodes for the empty tiles of a batch, from their tile records (the
+// record's head: tile, control pointer and descriptor), EMPTY_TILES tiles per
+// CTA.
+__global__ void __launch_bounds__(TILE_THREADS)
+k_empty_nodes_batch(const TileDesc* __restrict__ td, int nempty, int k) {
+    constexpr int HEAD = (int)((offsetof(TileDesc, occ) + 15) / 16);   // tile, control, descriptor
+    __shared__ int4 s_head[EMPTY_TILES][HEAD];
+    const int first = blockIdx.x * EMPTY_TILES;
+    for (int i = threadIdx.x; i < EMPTY_TILES * HEAD; i += blockDim.x) {
+        const int e = i / HEAD, w = i - e * HEAD;
+        if (first + e < nempty) s_head[e][w] = reinterpret_cast<const int4*>(td + first + e)[w];
+    }
+    __syncthreads();
+    const int tid = threadIdx.x, lx = tid & (TILE_CX - 1), ly = tid / TILE_CX;
+    int node[EMPTY_TILES];
+    uint16_t nc[EMPTY_TILES];
+    float vbx[EMPTY_TILES], vby[EMPTY_TILES];
+    #pragma unroll
+    for (int e = 0; e < EMPTY_TILES; ++e) {
+        node[e] = -1;
+        if (first + e < nempty) {
+            const TileDesc& R = *reinterpret_cast<const TileDesc*>(s_head[e]);
+            const int4 T = R.T;
+            const int c0x = T.y * TILE_NX - 1, c0y = T.z * TILE_NY - 1;
+            if (T.x >= 0 && lx < TILE_NX && ly < TILE_NY && c0x + 1 + lx <= R.S.nx && c0y + 1 + ly <= R.S.ny)
+                node[e] = (c0y + 1 + ly) * (R.S.nx + 1) + c0x + 1 + lx;
+        }
+    }
+    #pragma unroll
+    for (int e = 0; e < EMPTY_TILES; ++e)
+        if (node[e] >= 0) {
+            const SimDev& S = reinterpret_cast<const TileDesc*>(s_head[e])->S;
+            nc[e] = S.ncons[node[e]];
+            vbx[e] = S.nvbx[node[e]];
+            vby[e] = S.nvby[node[e]];
+        }
+    #pragma unroll
+    for (int e = 0; e < EMPTY_TILES; ++e)
+        if (node[e] >= 0) {
+            const TileDesc& R = *reinterpret_cast<const TileDesc*>(s_head[e]);
+            empty_node_step(R.S, node[e], nc[e], vbx[e], vby[e], step_time(load_step(R.ctl) + k, R.S.dt));
+        }
+}
+
+cudaError_t launch_empty_nodes_batch(const TileDesc* td, int ntiles, int k, cudaStream_t s) {
+    if (ntiles > 0)
+        k_empty_nodes_batch<<<(ntiles + EMPTY_TILES - 1) / EMPTY_TILES, TILE_THREADS, 0, s>>>(td, ntiles, k);
     return cudaGetLastError();
 }
 

@@ -31,13 +31,19 @@ cudaError_t launch_particle_kinematics(const StepConfig& c, const SimDev& S, con
                                        int ntiles, Control* ctl, int k, cudaStream_t s);
 // Split the tile list into active tiles (cells or their ring store a
 // particle; the step kernels' grid) and empty ones (node updates only,
-// k_empty_nodes), both padded to ntiles entries with (-1, 0, 0, 0); flags is
-// ntiles ints of scratch.  Valid until the sort changes.
+// k_empty_nodes), in tile order, both padded to ntiles entries with
+// (-1, 0, 0, 0), and write their counts to counts[0..1]; flags is ntiles
+// ints of scratch.  Valid until the sort changes.
 cudaError_t launch_classify_tiles(const SimDev& S, const int4* tiles, int ntiles, int* flags, int4* active,
-                                  int4* empty, cudaStream_t s);
+                                  int4* empty, int* counts, cudaStream_t s);
 // The step's node updates of the empty tiles (before the nodal kinematics).
 cudaError_t launch_empty_nodes(const SimDev& S, const int4* empty, int ntiles, Control* ctl, int k,
                                cudaStream_t s);
+// The same for a batch: tiles of every simulation (sims[tile.x]); the empty
+// tiles' records (launch_gather_tiles of the empty list).
+cudaError_t launch_classify_tiles_batch(const SimDev* const* sims, const int4* tiles, int ntiles, int* flags,
+                                        int4* active, int4* empty, int* counts, cudaStream_t s);
+cudaError_t launch_empty_nodes_batch(const TileDesc* td, int ntiles, int k, cudaStream_t s);
 // The kernels above work on step (ctl->step + k); these advance the counter
 // once a sequence of steps has been launched.
 cudaError_t launch_advance_step(Control* ctl, int by, cudaStream_t s);
@@ -46,7 +52,8 @@ cudaError_t launch_advance_steps(Control* const* ctls, int n, int by, cudaStream
 // The same three phases for a batch of simulations in one launch each: tile
 // t works on simulation tiles[t].x, whose descriptor is sims[tiles[t].x] and
 // whose step counter and status are in ctls[tiles[t].x].
-// out[t] = {tiles[t], ctls[tiles[t].x], *sims[tiles[t].x]} for t < ntiles.
+// out[t] = {tiles[t], ctls[tiles[t].x], *sims[tiles[t].x], row starts,
+// occupancy} for t < ntiles (only out[t].T for a tile (-1, ...)).
 cudaError_t launch_gather_tiles(const SimDev* const* sims, Control* const* ctls, const int4* tiles,
                                 int ntiles, TileDesc* out, cudaStream_t s);
 cudaError_t launch_nodal_kinematics_batch(const StepConfig& c, const TileDesc* td, int ntiles,
