@@ -1313,7 +1313,7 @@ int mpm_set_kernel_variant(MpmHandle* h, int nk_ctas, int g2p_ctas, int forces_l
     if (!h) return MPM_ERR_INVALID;
     if ((nk_ctas != 2 && nk_ctas != 3) || (g2p_ctas != 2 && g2p_ctas != 3))
         return fail(h, MPM_ERR_INVALID, "kernel builds exist for 2 or 3 CTAs per SM");
-    if (forces_lpc != 0 && forces_lpc != 1) return fail(h, MPM_ERR_INVALID, "forces_lpc is 0 or 1");
+    if (forces_lpc < 0 || forces_lpc > 2) return fail(h, MPM_ERR_INVALID, "forces_lpc is 0, 1 or 2");
     if (nk_ctas != h->nk_ctas || g2p_ctas != h->g2p_ctas || forces_lpc != h->forces_lpc) {
         h->nk_ctas = nk_ctas;
         h->g2p_ctas = g2p_ctas;

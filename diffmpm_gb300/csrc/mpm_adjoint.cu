@@ -515,6 +515,20 @@ AdjStep base_args(MpmHandle* h, AdjointState* a, int epoch) {
     return A;
 }
 
+// The tiles the reverse node passes visit: the active tiles of the segment's
+// sort when the segment is one sort epoch (the classification of its re-run
+// holds for every step; an empty tile's node adjoints and cell counts are
+// read by no particle), else every tile.
+void reverse_tiles(MpmHandle* h, AdjointState* a, const int4*& tiles, int& ntiles) {
+    if (a->nep == 1) {
+        tiles = h->d_active;
+        ntiles = h->nact;
+    } else {
+        tiles = h->dtiles;
+        ntiles = h->ntiles;
+    }
+}
+
 int reverse_step(MpmHandle* h, AdjointState* a, int t, cudaStream_t s) {
     AdjStep A = base_args(h, a, a->epoch_of[t]);
     const size_t op = (size_t)t * A.sp, on = (size_t)t * A.sn, oc = (size_t)t * A.sc;
@@ -525,14 +539,22 @@ int reverse_step(MpmHandle* h, AdjointState* a, int t, cudaStream_t s) {
     A.cflag += oc;
     A.nm += on; A.nvax += on; A.nvay += on; A.nvbx += on; A.nvby += on; A.nax += on; A.nay += on;
     A.step += t;
-    CK(h, launch_rev_step(A, h->usl, h->has_trac, h->dtiles, h->ntiles, s));
+    const int4* tiles;
+    int ntiles;
+    reverse_tiles(h, a, tiles, ntiles);
+    CK(h, launch_rev_step(A, h->usl, h->has_trac, tiles, ntiles, s));
     return MPM_OK;
 }
 
-// The reverse steps of a segment of `len` steps in one sort epoch as one graph.
+// The reverse steps of a segment of `len` steps in one sort epoch as one
+// graph (keyed by the length and the number of tiles it launches).
 int reverse_graph(MpmHandle* h, AdjointState* a, int len, cudaStream_t s) {
     TRY(prepare_adj_graphs(h, a, s));
-    return run_cached_graph(h, a->g_rev, len, s, [&](cudaStream_t c) -> int {
+    const int4* tiles;
+    int ntiles;
+    reverse_tiles(h, a, tiles, ntiles);
+    const int64_t key = (int64_t)len | ((int64_t)ntiles << 24);
+    return run_cached_graph(h, a->g_rev, key, s, [&](cudaStream_t c) -> int {
         for (int t = len - 1; t >= 0; --t) TRY(reverse_step(h, a, t, c));
         return MPM_OK;
     });
@@ -906,6 +928,13 @@ int mpm_batch_adjoint(MpmBatch* b, const float* const* dl_dloc, const float* con
             cur[i] = a->epoch_of[len - 1];
         }
         BCK(b, cudaMemcpyAsync(x->d_bases, x->bases.data(), sizeof(AdjStep) * n, cudaMemcpyHostToDevice, s));
+        // the reverse node passes visit the active tiles of the re-run's
+        // classification when no simulation re-sorted in the segment (see
+        // reverse_tiles), else every tile
+        bool one_epoch = true;
+        for (MpmHandle* h : b->sims) one_epoch = one_epoch && h->adj->nep == 1;
+        const int4* rtiles = one_epoch ? b->d_act_list : b->d_tiles;
+        const int nrtiles = one_epoch ? b->nact : b->ntiles;
         for (int t = len - 1; t >= 0 && r == MPM_OK; --t) {
             for (int i = 0; i < n && r == MPM_OK; ++i) {
                 MpmHandle* h = b->sims[i];
@@ -925,7 +954,7 @@ int mpm_batch_adjoint(MpmBatch* b, const float* const* dl_dloc, const float* con
             if (r != MPM_OK) break;
             BCK(b, launch_adj_table(x->d_bases, n, t, x->d_table, s));
             BCK(b, launch_rev_batch(x->d_table, b->cfg.usl, b->cfg.traction, any_pvc, b->cfg.reinit,
-                                    any_newt, b->d_tiles, b->ntiles, x->part_blocks, x->n_part_blocks, s));
+                                    any_newt, rtiles, nrtiles, x->part_blocks, x->n_part_blocks, s));
         }
         for (int i = 0; i < n && r == MPM_OK; ++i) {
             MpmHandle* h = b->sims[i];

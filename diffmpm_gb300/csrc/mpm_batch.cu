@@ -440,9 +440,9 @@ int mpm_batch_step(MpmBatch* b, int nsteps, void* stream) {
 int mpm_batch_set_tuning(MpmBatch* b, const MpmTuning* t) {
     if (!b || !t) return MPM_ERR_INVALID;
     if (t->block_steps < 1 || t->resort_every < 1 || (t->nk_ctas != 2 && t->nk_ctas != 3) ||
-        (t->g2p_ctas != 2 && t->g2p_ctas != 3) || (t->forces_lpc != 0 && t->forces_lpc != 1))
+        (t->g2p_ctas != 2 && t->g2p_ctas != 3) || t->forces_lpc < 0 || t->forces_lpc > 2)
         return bfail(b, MPM_ERR_INVALID, "tuning out of range (block_steps >= 1, resort_every >= 1, "
-                                         "2 or 3 CTAs per SM, forces_lpc 0 or 1)");
+                                         "2 or 3 CTAs per SM, forces_lpc 0, 1 or 2)");
     if (t->nk_ctas != b->cfg.nk_ctas || t->g2p_ctas != b->cfg.g2p_ctas ||
         t->forces_lpc != b->cfg.forces_lpc) {
         b->cfg.nk_ctas = t->nk_ctas;
@@ -525,9 +525,12 @@ int mpm_batch_autotune(MpmBatch* b, int trial_steps, MpmTuning* best_out, void* 
             if (t.nk_ctas != best.nk_ctas || t.g2p_ctas != best.g2p_ctas) trial(t);
         }
     {
-        MpmTuning t = best;
-        t.forces_lpc = 1 - best.forces_lpc;
-        trial(t);
+        const int base_lpc = best.forces_lpc;
+        for (int m : {0, 1, 2}) {
+            MpmTuning t = best;
+            t.forces_lpc = m;
+            if (m != base_lpc) trial(t);
+        }
     }
     const int base_block = best.block_steps;
     for (int c : {10, 25, 50, 100, 200}) {

@@ -415,9 +415,61 @@ __device__ __forceinline__ ForceIn force_in_global(const SimDev& S, int q, int p
     return in;
 }
 
-// Per-particle work of phase 2: USF strain/volume/stress update (written back
-// when `write`) and the total-force contributions [f x, f y] x 4 corners,
-// internal plus external force (element.py:236-303, 842-901).
+// Per-particle work of phase 2 on a particle state held in registers: the
+// USF strain/volume/stress update of `p` and `V` (the particle's volume
+// before the step; element.py:236-303, 842-901 via particle.py:249-327) and
+// the total-force contributions [f x, f y] x 4 corners, internal plus
+// external force.  Returns the volume the forces use (the updated one under
+// USF).
+template <bool USL, bool REINIT, bool TRAC, bool VD = false>
+__device__ __forceinline__ float force_core(const SimDev& S, int q, float x, float y, PState& p, float V,
+                                            float cx, float rx, float cy, float ry, float size0,
+                                            const float nvx[4], const float nvy[4], float dvol,
+                                            float t, float* c) {
+    const float xi = natural(x, cx, rx);
+    const float eta = natural(y, cy, ry);
+    float N[4], Gx[4], Gy[4];
+    shape4(xi, eta, N);
+    dshape4(xi, eta, rx, ry, Gx, Gy);
+    const float mp = REINIT ? fm(V, p.rho) : rd<VD>(S.mass)[q];
+    if (!USL) {
+        float r0, r1, r3;
+        strain_rate4(Gx, Gy, nvx, nvy, r0, r1, r3);
+        const MatDev& M = rd<VD>(S.mats)[rd<VD>(S.mat)[q]];
+        const float* E = rd<VD>(S.E);
+        const float Ep = E ? E[q] : -1.0f;
+        V = fm(V, strain_stress_update(M, Ep, rd<VD>(S.dt), r0, r1, r3, dvol, p));
+    }
+    const float nV = -V;
+    const float mgx = fm(mp, rd<VD>(S.gx)), mgy = fm(mp, rd<VD>(S.gy));
+    #pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float fx = fa(fm(Gx[k], p.sxx), fm(Gy[k], p.sxy));
+        const float fy = fa(fm(Gy[k], p.syy), fm(Gx[k], p.sxy));
+        c[k] = fa(fm(nV, fx), fm(N[k], mgx));
+        c[4 + k] = fa(fm(nV, fy), fm(N[k], mgy));
+    }
+    add_traction<TRAC>(S, q, t, V, REINIT ? size0 : (S.psize ? S.psize[q] : 1.0f), N, c, c + 4);
+    return V;
+}
+
+// The USF state of particle q after the stress update (buffers `next`).
+template <bool REINIT, bool VD>
+__device__ __forceinline__ void store_state(const SimDev& S, int q, const PState& p, float V, int next) {
+    rd<VD>(S.sxx[next])[q] = p.sxx;
+    rd<VD>(S.syy[next])[q] = p.syy;
+    rd<VD>(S.szz[next])[q] = p.szz;
+    rd<VD>(S.sxy[next])[q] = p.sxy;
+    rd<VD>(S.exx)[q] = p.exx;
+    rd<VD>(S.eyy)[q] = p.eyy;
+    rd<VD>(S.exy)[q] = p.exy;
+    rd<VD>(S.rho[next])[q] = p.rho;
+    rd<VD>(S.vsc[next])[q] = p.vsc;
+    if (!REINIT) rd<VD>(S.vol[next])[q] = V;
+}
+
+// force_core on a particle read from global memory; the updated state is
+// written back when `write` (the particle's cell is owned by the tile).
 template <bool USL, bool REINIT, bool TRAC, bool VD = false>
 __device__ __forceinline__ void force_contrib(const SimDev& S, int q, const ForceIn& in, float cx,
                                               float rx, float cy, float ry, float V0, float size0,
@@ -432,48 +484,14 @@ __device__ __forceinline__ void force_contrib(const SimDev& S, int q, const Forc
         p.exy = rd<VD>(S.exy)[q];
         p.vsc = rd<VD>(S.vsc[parity])[q];
     }
-    const float xi = natural(in.x, cx, rx);
-    const float eta = natural(in.y, cy, ry);
-    float N[4], Gx[4], Gy[4];
-    shape4(xi, eta, N);
-    dshape4(xi, eta, rx, ry, Gx, Gy);
     p.sxx = in.sxx;
     p.syy = in.syy;
     p.szz = in.szz;
     p.sxy = in.sxy;
     p.rho = in.rho;
-    const float mp = REINIT ? fm(V0, p.rho) : rd<VD>(S.mass)[q];
-    float V = REINIT ? V0 : in.vol;
-    if (!USL) {
-        float r0, r1, r3;
-        strain_rate4(Gx, Gy, nvx, nvy, r0, r1, r3);
-        const MatDev& M = rd<VD>(S.mats)[rd<VD>(S.mat)[q]];
-        const float* E = rd<VD>(S.E);
-        const float Ep = E ? E[q] : -1.0f;
-        V = fm(V, strain_stress_update(M, Ep, rd<VD>(S.dt), r0, r1, r3, dvol, p));
-        if (write) {
-            rd<VD>(S.sxx[next])[q] = p.sxx;
-            rd<VD>(S.syy[next])[q] = p.syy;
-            rd<VD>(S.szz[next])[q] = p.szz;
-            rd<VD>(S.sxy[next])[q] = p.sxy;
-            rd<VD>(S.exx)[q] = p.exx;
-            rd<VD>(S.eyy)[q] = p.eyy;
-            rd<VD>(S.exy)[q] = p.exy;
-            rd<VD>(S.rho[next])[q] = p.rho;
-            rd<VD>(S.vsc[next])[q] = p.vsc;
-            if (!REINIT) rd<VD>(S.vol[next])[q] = V;
-        }
-    }
-    const float nV = -V;
-    const float mgx = fm(mp, rd<VD>(S.gx)), mgy = fm(mp, rd<VD>(S.gy));
-    #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const float fx = fa(fm(Gx[k], p.sxx), fm(Gy[k], p.sxy));
-        const float fy = fa(fm(Gy[k], p.syy), fm(Gx[k], p.sxy));
-        c[k] = fa(fm(nV, fx), fm(N[k], mgx));
-        c[4 + k] = fa(fm(nV, fy), fm(N[k], mgy));
-    }
-    add_traction<TRAC>(S, q, t, V, REINIT ? size0 : (S.psize ? S.psize[q] : 1.0f), N, c, c + 4);
+    const float V = force_core<USL, REINIT, TRAC, VD>(S, q, in.x, in.y, p, REINIT ? V0 : in.vol, cx, rx,
+                                                      cy, ry, size0, nvx, nvy, dvol, t, c);
+    if (!USL && write) store_state<REINIT, VD>(S, q, p, V, next);
 }
 
 // ---------------------------------------------------------------------------
@@ -646,28 +664,107 @@ constexpr int NV_W = TILE_CX + 1;   // node tile of the R cells: [c0x, c0x+33) x
 constexpr int NV_H = TILE_CY + 1;
 constexpr int K2_ROW_P = 128;   // particles of a row per pass (two CTAs per SM)
 
-// Row-pass buffers of the particle-per-lane forces path.
+// Fast paths of the forces kernel (StepConfig.forces_lpc):
+//   FM_ROW     a warp's lanes take consecutive particles of its cell row
+//              (coalesced global loads and stores); the contributions go
+//              through shared-memory slots and lane l adds the slots of its
+//              cell's particles in storage order.
+//   FM_LPC     lane per cell: every lane works through its own cell's
+//              particles in storage order, reading and writing them in
+//              global memory, with the cell's nodal velocities and values in
+//              registers, adding each contribution as it is formed.
+//   FM_STAGED  FM_ROW on the cell row staged in shared memory by 16-byte
+//              cp.async copies, one round trip per row instead of one per
+//              particle a lane takes; a particle's contributions go to its
+//              own staged slots once it has read them.
+// All three add the same contributions in the same order: the same bits.
+enum ForcesMode { FM_ROW = 0, FM_LPC = 1, FM_STAGED = 2 };
+
+// Row-pass buffers of FM_ROW.
 template <int NQ>
 struct ForceRows {
     float slot[TILE_CY][NQ][K2_ROW_P];    // contributions of a row's particles
     unsigned char cell[TILE_CY][K2_ROW_P];   // their cell within the row
     float cellv[TILE_CY][3][32];          // V0, size0, dvol per cell
 };
-struct NoForceRows {};
 
-// LPC (lane per cell): every lane works through its own cell's particles in
-// storage order, with the cell's nodal velocities and values in registers,
-// adding each contribution as it is formed -- the order of the
-// particle-per-lane path's slot sums, so both give the same bits.  Without
-// LPC, a warp's lanes take consecutive particles of the row (coalesced
-// loads and stores) and the contributions go through shared-memory slots.
-template <bool USL, bool REINIT, bool TRAC, bool VD, bool LPC = false>
+// Fields of the FM_STAGED row buffer: x, y and the stress state the forces
+// use, then (USF) the rest of the state the step updates.  Slots 0..7 take a
+// particle's eight contributions after it has read its fields.
+template <bool USL, bool REINIT>
+struct StagedFields {
+    static constexpr int X = 0, Y = 1, SXX = 2, SYY = 3, SXY = 4, RHO = 5;
+    static constexpr int SZZ = 6, EXX = 7, EYY = 8, EXY = 9, VSC = 10;   // USF only
+    static constexpr int NBASE = USL ? 6 : 11;
+    static constexpr int VOL = REINIT ? -1 : NBASE;   // solve semantics: persistent volume
+    static constexpr int NF = NBASE + (REINIT ? 0 : 1);
+    static constexpr int NBUF = NF > 8 ? NF : 8;
+    // slots of a row per pass: a row of 4 particles in each of 32 cells,
+    // starting anywhere in a 16-byte piece, fits one pass
+    static constexpr int P = 132;
+};
+
+// Shared memory of forces_tile by mode.  FM_STAGED overlays the per-cell
+// corner sums on the staged rows (they are formed after every row is done).
+template <int MODE, int NQ, bool USL, bool REINIT>
+struct ForceShared {
+    float c[NQ][SC_STRIDE];
+    ForceRows<NQ> rows;
+};
+template <int NQ, bool USL, bool REINIT>
+struct ForceShared<FM_LPC, NQ, USL, REINIT> {
+    float c[NQ][SC_STRIDE];
+};
+template <int NQ, bool USL, bool REINIT>
+struct ForceShared<FM_STAGED, NQ, USL, REINIT> {
+    using F = StagedFields<USL, REINIT>;
+    union {
+        float c[NQ][SC_STRIDE];
+        __align__(16) float buf[TILE_CY][F::NBUF][F::P];
+    };
+    unsigned char cell[TILE_CY][F::P];   // a staged particle's cell within the row
+    float cellv[TILE_CY][3][32];          // V0, size0, dvol per cell
+    const float* src[F::NF];              // the staged fields' arrays (this step's parity)
+};
+
+// The arrays of the FM_STAGED fields, one per thread tid < NF.
+template <bool USL, bool REINIT, bool VD>
+__device__ __forceinline__ void staged_arrays(const SimDev& S, int parity, int tid, const float** src) {
+    using F = StagedFields<USL, REINIT>;
+    if (tid >= F::NF) return;
+    const float* a = nullptr;
+    switch (tid) {
+        case F::X: a = rd<VD>(S.x); break;
+        case F::Y: a = rd<VD>(S.y); break;
+        case F::SXX: a = rd<VD>(S.sxx[parity]); break;
+        case F::SYY: a = rd<VD>(S.syy[parity]); break;
+        case F::SXY: a = rd<VD>(S.sxy[parity]); break;
+        case F::RHO: a = rd<VD>(S.rho[parity]); break;
+        default: break;
+    }
+    if constexpr (!USL) {
+        switch (tid) {
+            case F::SZZ: a = rd<VD>(S.szz[parity]); break;
+            case F::EXX: a = rd<VD>(S.exx); break;
+            case F::EYY: a = rd<VD>(S.eyy); break;
+            case F::EXY: a = rd<VD>(S.exy); break;
+            case F::VSC: a = rd<VD>(S.vsc[parity]); break;
+            default: break;
+        }
+    }
+    if constexpr (!REINIT) {
+        if (tid == F::VOL) a = rd<VD>(S.vol[parity]);
+    }
+    src[tid] = a;
+}
+
+template <bool USL, bool REINIT, bool TRAC, bool VD, int MODE = FM_ROW>
 __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
                                             Control* __restrict__ ctl, int k,
                                             const TileDesc* rec = nullptr) {
     constexpr int NQ = 8;
-    __shared__ float s_c[NQ][SC_STRIDE];               // [f x, f y] x corner, per cell
-    __shared__ std::conditional_t<LPC, NoForceRows, ForceRows<NQ>> s_rows;
+    __shared__ __align__(16) ForceShared<MODE, NQ, USL, REINIT> sh;
+    auto& s_c = sh.c;                                   // [f x, f y] x corner, per cell
     __shared__ int s_cs[TILE_CY][33];
     __shared__ float2 s_v[NV_W * NV_H];   // nodal velocity after phase 1 of the tile's nodes
     __shared__ TileGeo G;
@@ -703,13 +800,16 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
         return;
     }
     build_geo(S, c0x, c0y, G);
-    #pragma unroll
-    for (int q = 0; q < NQ; ++q) s_c[q][tid] = 0.0f;
+    if constexpr (MODE != FM_STAGED) {
+        #pragma unroll
+        for (int q = 0; q < NQ; ++q) s_c[q][tid] = 0.0f;
+    }
     s_cs[ly][lx] = L.cs;
     if (lx == 0) s_cs[ly][32] = L.cs32;
     #pragma unroll
     for (int e = 0; e < 2; ++e)
         if (tid + e * TILE_THREADS < NV_W * NV_H) s_v[tid + e * TILE_THREADS] = nv[e];
+    if constexpr (MODE == FM_STAGED) staged_arrays<USL, REINIT, VD>(S, parity, tid, sh.src);
     const bool slow = __syncthreads_or(L.drift) != 0;
 
     auto cell_velocities = [&](int li, int lj, float* vx, float* vy) {
@@ -724,7 +824,80 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
     };
 
     if (!slow) {
-      if constexpr (LPC) {
+      if constexpr (MODE == FM_STAGED) {
+        using F = StagedFields<USL, REINIT>;
+        float (*buf)[F::P] = sh.buf[ly];
+        auto& s_cell = sh.cell;
+        auto& s_cellv = sh.cellv;
+        const int* cs = s_cs[ly];
+        const int rb = cs[0], re = cs[32], cb = cs[lx], ce = cs[lx + 1];
+        {
+            float nvx[4], nvy[4], V0, size0, dvol;
+            if (!USL) cell_velocities(lx, ly, nvx, nvy);
+            force_cell_values<USL, REINIT, VD, TRAC>(S, ce - cb, geo_of(G, lx + 1, ly + 1), nvx, nvy, V0,
+                                                     size0, dvol);
+            s_cellv[ly][0][lx] = V0;
+            s_cellv[ly][1][lx] = size0;
+            s_cellv[ly][2][lx] = dvol;
+        }
+        const float cy = G.row[ly + 1].z, ry = G.row[ly + 1].w;   // row geometry (warp-uniform)
+        const int next = parity ^ 1;
+        float acc[NQ];
+        #pragma unroll
+        for (int q = 0; q < NQ; ++q) acc[q] = 0.0f;
+        #pragma unroll 1
+        for (int p0 = rb & ~3; p0 < re; p0 += F::P) {
+            const int p1 = min(p0 + F::P, re);
+            #pragma unroll
+            for (int f = 0; f < F::NF; ++f) {
+                #pragma unroll
+                for (int o = 4 * lx; o < F::P; o += 128)
+                    if (p0 + o < p1) cp_async16(&buf[f][o], sh.src[f] + p0 + o);
+            }
+            cp_async_commit();
+            for (int q = max(cb, p0); q < min(ce, p1); ++q) s_cell[ly][q - p0] = (unsigned char)lx;
+            cp_async_wait<0>();
+            __syncwarp();
+            #pragma unroll 1
+            for (int q = max(rb, p0) + lx; q < p1; q += 32) {
+                const int j = q - p0;
+                const int l = s_cell[ly][j];
+                float nvx[4], nvy[4];
+                if (!USL) cell_velocities(l, ly, nvx, nvy);
+                PState p;
+                p.sxx = buf[F::SXX][j];
+                p.syy = buf[F::SYY][j];
+                p.sxy = buf[F::SXY][j];
+                p.rho = buf[F::RHO][j];
+                p.szz = 0.0f;
+                if constexpr (!USL) {
+                    p.szz = buf[F::SZZ][j];
+                    p.exx = buf[F::EXX][j];
+                    p.eyy = buf[F::EYY][j];
+                    p.exy = buf[F::EXY][j];
+                    p.vsc = buf[F::VSC][j];
+                }
+                const float4 cg = G.col[l + 1];
+                float cc[NQ];
+                const float V = force_core<USL, REINIT, TRAC, VD>(
+                    S, q, buf[F::X][j], buf[F::Y][j], p, REINIT ? s_cellv[ly][0][l] : buf[REINIT ? 0 : F::VOL][j],
+                    cg.z, cg.w, cy, ry, s_cellv[ly][1][l], nvx, nvy, s_cellv[ly][2][l], t, cc);
+                if (!USL && l >= 1 && ly >= 1) store_state<REINIT, VD>(S, q, p, V, next);
+                #pragma unroll
+                for (int kk = 0; kk < NQ; ++kk) buf[kk][j] = cc[kk];
+            }
+            __syncwarp();
+            #pragma unroll 1
+            for (int q = max(cb, p0); q < min(ce, p1); ++q) {
+                #pragma unroll
+                for (int kk = 0; kk < NQ; ++kk) acc[kk] = fa(acc[kk], buf[kk][q - p0]);
+            }
+            __syncwarp();
+        }
+        __syncthreads();   // every row is done with the staged rows that s_c overlays
+        #pragma unroll
+        for (int q = 0; q < NQ; ++q) s_c[q][tid] = acc[q];
+      } else if constexpr (MODE == FM_LPC) {
         if (ci >= 0 && ci < S.nx && cj >= 0 && cj < S.ny) {
             const int cb = s_cs[ly][lx], ce = s_cs[ly][lx + 1];
             const CellGeo g = geo_of(G, lx + 1, ly + 1);
@@ -751,9 +924,9 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
         // particle per lane for the per-particle work (coalesced global loads
         // and stores), contributions to row slots, then lane per cell adds
         // the slots of its cell's particles in storage order
-        auto& s_slot = s_rows.slot;
-        auto& s_cell = s_rows.cell;
-        auto& s_cellv = s_rows.cellv;
+        auto& s_slot = sh.rows.slot;
+        auto& s_cell = sh.rows.cell;
+        auto& s_cellv = sh.rows.cellv;
         const int* cs = s_cs[ly];
         const int rb = cs[0], re = cs[32];
         const int cb = cs[lx], ce = cs[lx + 1];
@@ -800,21 +973,27 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
         #pragma unroll
         for (int k = 0; k < NQ; ++k) s_c[k][tid] = acc[k];
       }
-    } else if (ci >= 0 && ci < S.nx && cj >= 0 && cj < S.ny) {
-        const CellGeo g = geo_of(G, lx + 1, ly + 1);
-        const int cnt = REINIT ? count_cell(S, ci, cj, g) : 0;
-        float nvx[4], nvy[4], V0, size0, dvol;
-        if (!USL) cell_velocities(lx, ly, nvx, nvy);
-        force_cell_values<USL, REINIT, VD, TRAC>(S, cnt, g, nvx, nvy, V0, size0, dvol);
-        const bool own = lx >= 1 && ly >= 1;
-        visit_cell(S, ci, cj, g, [&](int q) {
-            float cc[NQ];
-            force_contrib<USL, REINIT, TRAC, VD>(S, q, force_in_global<VD>(S, q, parity, REINIT), g.cx,
-                                             g.rx, g.cy, g.ry, V0, size0, nvx, nvy, dvol, parity,
-                                             t, own, cc);
+    } else {
+        if constexpr (MODE == FM_STAGED) {
             #pragma unroll
-            for (int k = 0; k < NQ; ++k) s_c[k][tid] = fa(s_c[k][tid], cc[k]);
-        });
+            for (int q = 0; q < NQ; ++q) s_c[q][tid] = 0.0f;
+        }
+        if (ci >= 0 && ci < S.nx && cj >= 0 && cj < S.ny) {
+            const CellGeo g = geo_of(G, lx + 1, ly + 1);
+            const int cnt = REINIT ? count_cell(S, ci, cj, g) : 0;
+            float nvx[4], nvy[4], V0, size0, dvol;
+            if (!USL) cell_velocities(lx, ly, nvx, nvy);
+            force_cell_values<USL, REINIT, VD, TRAC>(S, cnt, g, nvx, nvy, V0, size0, dvol);
+            const bool own = lx >= 1 && ly >= 1;
+            visit_cell(S, ci, cj, g, [&](int q) {
+                float cc[NQ];
+                force_contrib<USL, REINIT, TRAC, VD>(S, q, force_in_global<VD>(S, q, parity, REINIT), g.cx,
+                                                 g.rx, g.cy, g.ry, V0, size0, nvx, nvy, dvol, parity,
+                                                 t, own, cc);
+                #pragma unroll
+                for (int k = 0; k < NQ; ++k) s_c[k][tid] = fa(s_c[k][tid], cc[k]);
+            });
+        }
     }
     __syncthreads();
     if (node_ok) {
@@ -824,21 +1003,21 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
     }
 }
 
-template <bool USL, bool REINIT, bool TRAC, bool LPC = false>
+template <bool USL, bool REINIT, bool TRAC, int MODE = FM_ROW>
 __global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
 k_forces(const __grid_constant__ SimDev S, const int4* __restrict__ tiles,
          Control* __restrict__ ctl, int k) {
     const int4 T = tiles[blockIdx.x];
     if (T.x < 0) return;
-    forces_tile<USL, REINIT, TRAC, false, LPC>(S, T, ctl, k);
+    forces_tile<USL, REINIT, TRAC, false, MODE>(S, T, ctl, k);
 }
 
-template <bool USL, bool REINIT, bool TRAC, bool LPC = false>
+template <bool USL, bool REINIT, bool TRAC, int MODE = FM_ROW>
 __global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
 k_forces_batch(const TileDesc* __restrict__ td, int k) {
     __shared__ TileDesc sT;
     load_tile(td + blockIdx.x, sT);
-    forces_tile<USL, REINIT, TRAC, true, LPC>(sT.S, sT.T, sT.ctl, k, &sT);
+    forces_tile<USL, REINIT, TRAC, true, MODE>(sT.S, sT.T, sT.ctl, k, &sT);
 }
 
 // ---------------------------------------------------------------------------
@@ -1244,20 +1423,23 @@ cudaError_t launch_nodal_kinematics(const StepConfig& c, const SimDev& S, const 
     return cudaGetLastError();
 }
 
+template <bool USL, bool REINIT, bool TRAC, int MODE>
+static void forces_mode(const SimDev& S, const int4* tiles, int ntiles, Control* ctl, int k,
+                        cudaStream_t s) {
+    prefer_shared(k_forces<USL, REINIT, TRAC, MODE>);
+    k_forces<USL, REINIT, TRAC, MODE><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl, k);
+}
+
 template <bool USL, bool REINIT, bool TRAC>
-static void forces_one(bool lpc, const SimDev& S, const int4* tiles, int ntiles, Control* ctl, int k,
+static void forces_one(int mode, const SimDev& S, const int4* tiles, int ntiles, Control* ctl, int k,
                        cudaStream_t s) {
-    if (lpc) {
-        prefer_shared(k_forces<USL, REINIT, TRAC, true>);
-        k_forces<USL, REINIT, TRAC, true><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl, k);
-    } else {
-        prefer_shared(k_forces<USL, REINIT, TRAC>);
-        k_forces<USL, REINIT, TRAC><<<ntiles, TILE_THREADS, 0, s>>>(S, tiles, ctl, k);
-    }
+    if (mode == FM_STAGED) forces_mode<USL, REINIT, TRAC, FM_STAGED>(S, tiles, ntiles, ctl, k, s);
+    else if (mode == FM_LPC) forces_mode<USL, REINIT, TRAC, FM_LPC>(S, tiles, ntiles, ctl, k, s);
+    else forces_mode<USL, REINIT, TRAC, FM_ROW>(S, tiles, ntiles, ctl, k, s);
 }
 
 template <bool USL, bool REINIT>
-static void forces_trac(bool trac, bool lpc, const SimDev& S, const int4* tiles, int ntiles,
+static void forces_trac(bool trac, int lpc, const SimDev& S, const int4* tiles, int ntiles,
                         Control* ctl, int k, cudaStream_t s) {
     if (trac) forces_one<USL, REINIT, true>(lpc, S, tiles, ntiles, ctl, k, s);
     else forces_one<USL, REINIT, false>(lpc, S, tiles, ntiles, ctl, k, s);
@@ -1265,7 +1447,7 @@ static void forces_trac(bool trac, bool lpc, const SimDev& S, const int4* tiles,
 
 cudaError_t launch_forces(const StepConfig& c, const SimDev& S, const int4* tiles, int ntiles,
                           Control* ctl, int k, cudaStream_t s) {
-    const bool lpc = c.forces_lpc != 0;
+    const int lpc = c.forces_lpc;
     if (c.usl) {
         if (c.reinit) forces_trac<true, true>(c.traction, lpc, S, tiles, ntiles, ctl, k, s);
         else forces_trac<true, false>(c.traction, lpc, S, tiles, ntiles, ctl, k, s);
@@ -1319,21 +1501,23 @@ cudaError_t launch_nodal_kinematics_batch(const StepConfig& c, const TileDesc* t
     return cudaGetLastError();
 }
 
+template <bool USL, bool REINIT, bool TRAC, int MODE>
+static void forces_batch_mode(const TileDesc* td, int ntiles, int k, cudaStream_t s) {
+    prefer_shared(k_forces_batch<USL, REINIT, TRAC, MODE>);
+    k_forces_batch<USL, REINIT, TRAC, MODE><<<ntiles, TILE_THREADS, 0, s>>>(td, k);
+}
+
 template <bool USL, bool REINIT, bool TRAC>
-static void forces_batch(bool lpc, const TileDesc* td, int ntiles, int k, cudaStream_t s) {
-    if (lpc) {
-        prefer_shared(k_forces_batch<USL, REINIT, TRAC, true>);
-        k_forces_batch<USL, REINIT, TRAC, true><<<ntiles, TILE_THREADS, 0, s>>>(td, k);
-    } else {
-        prefer_shared(k_forces_batch<USL, REINIT, TRAC>);
-        k_forces_batch<USL, REINIT, TRAC><<<ntiles, TILE_THREADS, 0, s>>>(td, k);
-    }
+static void forces_batch(int mode, const TileDesc* td, int ntiles, int k, cudaStream_t s) {
+    if (mode == FM_STAGED) forces_batch_mode<USL, REINIT, TRAC, FM_STAGED>(td, ntiles, k, s);
+    else if (mode == FM_LPC) forces_batch_mode<USL, REINIT, TRAC, FM_LPC>(td, ntiles, k, s);
+    else forces_batch_mode<USL, REINIT, TRAC, FM_ROW>(td, ntiles, k, s);
 }
 
 cudaError_t launch_forces_batch(const StepConfig& c, const TileDesc* td, int ntiles, int k,
                                 cudaStream_t s) {
     const int key = (c.usl ? 4 : 0) | (c.reinit ? 2 : 0) | (c.traction ? 1 : 0);
-    const bool lpc = c.forces_lpc != 0;
+    const int lpc = c.forces_lpc;
     switch (key) {
         case 0: forces_batch<false, false, false>(lpc, td, ntiles, k, s); break;
         case 1: forces_batch<false, false, true>(lpc, td, ntiles, k, s); break;

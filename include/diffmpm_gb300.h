@@ -318,7 +318,10 @@ int mpm_batch_set_block_steps(MpmBatch* b, int steps);
  *   forces_lpc    the forces kernel's fast path: 0, a warp's lanes take
  *                 consecutive particles of a cell row and add their
  *                 contributions through shared memory; 1, each lane works
- *                 through the particles of its own cell;
+ *                 through the particles of its own cell in global memory;
+ *                 2, the same on the cell row staged in shared memory by
+ *                 16-byte copies, with the updated state copied back the
+ *                 same way;
  *   ms_per_step   (output of mpm_batch_autotune) device time per step.
  * The builds and the re-sort cadence change no result beyond the last bits
  * of the re-sort schedule's summation order. */
@@ -333,7 +336,7 @@ typedef struct MpmTuning {
 
 /* Time `trial_steps` steps of the batch from its current state for
  * candidate tunings -- coordinate descent over the kernel builds
- * ({2, 3} x {2, 3} CTAs per SM, either forces path), the block length (10, 25, 50, 100, 200,
+ * ({2, 3} x {2, 3} CTAs per SM, each of the three forces paths), the block length (10, 25, 50, 100, 200,
  * capped at trial_steps) and the re-sort cadence (1, 2, 4 blocks) --, apply
  * the fastest, put every simulation back in the state it had, and return the
  * choice in *best (may be NULL). */

@@ -253,7 +253,7 @@ def test_kernel_builds_and_resort_cadence_keep_results(built):
     stays within the parity tolerance of the oracle."""
     spec = small_specs(k=1, seed=13)[0]
     ref = None
-    for nk, g2p, lpc in ((3, 3, 0), (2, 2, 1), (3, 2, 1), (2, 3, 0)):
+    for nk, g2p, lpc in ((3, 3, 0), (2, 2, 1), (3, 2, 2), (2, 3, 0)):
         _, sim, _ = member_sim(spec, 40)
         b = D.Batch([sim])
         b.set_tuning(block_steps=10, resort_every=1, nk_ctas=nk, g2p_ctas=g2p, forces_lpc=lpc)
@@ -279,11 +279,12 @@ def test_kernel_builds_and_resort_cadence_keep_results(built):
     (workloads.mixed_large, dict(n=48)),
 ])
 def test_forces_paths_give_the_same_bits(built, builder, kw):
-    """The forces kernel's two fast paths (particle per lane with slots, lane
-    per cell) add every cell's contributions in the same order: a single
-    simulation ends bit for bit in the same state with either."""
+    """The forces kernel's three fast paths (particle per lane with slots,
+    lane per cell in global memory, lane per cell on a staged row) add every
+    cell's contributions in the same order: a single simulation ends bit for
+    bit in the same state with each."""
     out = []
-    for lpc in (0, 1):
+    for lpc in (0, 1, 2):
         s, g, _ = builder(D, sim_steps=30, **kw)
         sim = s.simulation(g, reinit=True)
         s._upload(sim)
@@ -293,5 +294,6 @@ def test_forces_paths_give_the_same_bits(built, builder, kw):
         sim.step(30)
         out.append(state(sim))
         sim.close()
-    for k in FIELDS:
-        assert np.array_equal(out[0][k], out[1][k]), k
+    for o in out[1:]:
+        for k in FIELDS:
+            assert np.array_equal(out[0][k], o[k]), k
