@@ -107,6 +107,11 @@ struct BatchAdjoint {
     SegBuf tape_p[2], tape_n, misc;
     int* mismatch = nullptr;
     int* h_mismatch = nullptr;
+    // graphs of one-epoch segments: the re-run (keyed by length and tile
+    // counts) and the reverse steps (length, tiles, particle blocks); valid
+    // for the buffers and kernel builds in `gsig`
+    std::map<int64_t, cudaGraphExec_t> g_rerun, g_rev;
+    std::vector<uintptr_t> gsig;
 };
 
 namespace {
@@ -371,9 +376,9 @@ int rerun_graph(MpmHandle* h, AdjointState* a, int len, cudaStream_t s) {
     TRY(run_cached_graph(h, a->g_rerun, seq_key(h, 2 * len + par0), s, [&](cudaStream_t c) -> int {
         for (int t = 0; t < len; ++t) {
             const SegBuf& tp = a->g_tp[(par0 + t) & 1];
-            CK(h, launch_copy_segments(tp.segs, tp.first, tp.nseg, tp.nblocks, t, c));
+            CK(h, launch_copy_segments(tp.blk, tp.nblocks, t, c));
             for (int p = 0; p < 3; ++p) TRY(launch_phase(h, p, t, c));
-            CK(h, launch_copy_segments(a->g_tn.segs, a->g_tn.first, a->g_tn.nseg, a->g_tn.nblocks, t, c));
+            CK(h, launch_copy_segments(a->g_tn.blk, a->g_tn.nblocks, t, c));
         }
         CK(h, launch_advance_step(h->ctl, len, c));
         return MPM_OK;
@@ -419,13 +424,13 @@ int recompute_segment(MpmHandle* h, AdjointState* a, int seg, int len, cudaStrea
             r = classify_tiles(h, s);
             if (r != MPM_OK) break;
         }
-        cudaError_t e = launch_copy_segments(tp.segs, tp.first, tp.nseg, tp.nblocks, t, s);
+        cudaError_t e = launch_copy_segments(tp.blk, tp.nblocks, t, s);
         if (e == cudaSuccess) {
             r = launch_steps(h, 1, s);
             h->step++;
         }
         if (e == cudaSuccess && r == MPM_OK)
-            e = launch_copy_segments(tn.segs, tn.first, tn.nseg, tn.nblocks, t, s);
+            e = launch_copy_segments(tn.blk, tn.nblocks, t, s);
         if (e != cudaSuccess) r = fail(h, MPM_ERR_CUDA, "tape copy: %s", cudaGetErrorString(e));
         a->epoch_of[t] = a->nep - 1;
     }
@@ -441,7 +446,7 @@ int recompute_segment(MpmHandle* h, AdjointState* a, int seg, int len, cudaStrea
     r = upload_segments(h, cb, vc, s);
     if (r == MPM_OK) {
         cudaError_t e = cudaMemsetAsync(a->mismatch, 0, sizeof(int), s);
-        if (e == cudaSuccess) e = launch_compare_segments(cb.segs, cb.first, cb.nseg, cb.nblocks, a->mismatch, s);
+        if (e == cudaSuccess) e = launch_compare_segments(cb.blk, cb.nblocks, a->mismatch, s);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(a->h_mismatch, a->mismatch, sizeof(int), cudaMemcpyDeviceToHost, s);
         if (e != cudaSuccess) r = fail(h, MPM_ERR_CUDA, "re-run check: %s", cudaGetErrorString(e));
@@ -655,9 +660,34 @@ void adjoint_free(MpmHandle* h) {
     h->adj = nullptr;
 }
 
+void drop_batch_adj_graphs(BatchAdjoint* x) {
+    for (auto& kv : x->g_rerun) cudaGraphExecDestroy(kv.second);
+    for (auto& kv : x->g_rev) cudaGraphExecDestroy(kv.second);
+    x->g_rerun.clear();
+    x->g_rev.clear();
+}
+
+// The buffers and kernel builds the batched adjoint's graphs hold; the
+// cached graphs are dropped when any of them changed.
+void check_batch_adj_graphs(MpmBatch* b, BatchAdjoint* x) {
+    const std::vector<uintptr_t> sig = {
+        (uintptr_t)x->tape_p[0].segs, (uintptr_t)x->tape_p[0].blk, x->tape_p[0].nblocks,
+        (uintptr_t)x->tape_p[1].segs, (uintptr_t)x->tape_p[1].blk, x->tape_p[1].nblocks,
+        (uintptr_t)x->tape_n.segs, (uintptr_t)x->tape_n.blk, x->tape_n.nblocks,
+        (uintptr_t)x->d_bases, (uintptr_t)x->d_table, (uintptr_t)x->part_blocks,
+        (uintptr_t)x->n_part_blocks, (uintptr_t)b->d_tdescs, (uintptr_t)b->d_edescs,
+        (uintptr_t)b->d_act_list, (uintptr_t)b->d_tiles, (uintptr_t)b->d_ctls,
+        (uintptr_t)b->cfg.nk_ctas, (uintptr_t)b->cfg.g2p_ctas, (uintptr_t)b->cfg.forces_lpc};
+    if (sig != x->gsig) {
+        drop_batch_adj_graphs(x);
+        x->gsig = sig;
+    }
+}
+
 void batch_adjoint_free(MpmBatch* b) {
     BatchAdjoint* x = b->badj;
     if (!x) return;
+    drop_batch_adj_graphs(x);
     cudaFree(x->d_bases);
     cudaFree(x->d_table);
     cudaFree(x->part_blocks);
@@ -717,7 +747,29 @@ int batch_recompute(MpmBatch* b, BatchAdjoint* x, int seg, int len, cudaStream_t
     v.clear();
     for (MpmHandle* h : b->sims) tape_node_segments(h, h->adj, v);
     BTRY(b, 0, upload_segments(b->sims[0], x->tape_n, v, s));
-    for (int t = 0; t < len; ++t) {
+    bool resorts = false;
+    for (int i = 0; i < n && !resorts; ++i)
+        for (int t = 0; t < len && !resorts; ++t) resorts = resorts_at(b->sims[i]->adj, first[i] + t);
+    if (!resorts) {
+        // one sort epoch for every simulation: the segment's steps with their
+        // tape copies as one graph (the same launches as the loop below)
+        r = prepare_tiles(b, s);
+        if (r != MPM_OK) return r;
+        check_batch_adj_graphs(b, x);
+        const int64_t key = (int64_t)len | ((int64_t)b->nact << 20) | ((int64_t)b->nemp << 42);
+        BTRY(b, 0, run_cached_graph(b->sims[0], x->g_rerun, key, s, [&](cudaStream_t c) -> int {
+            for (int t = 0; t < len; ++t) {
+                const SegBuf& tp = x->tape_p[t & 1];
+                CK(b->sims[0], launch_copy_segments(tp.blk, tp.nblocks, t, c));
+                const int rr = launch_batch_steps(b, 1, c);
+                if (rr != MPM_OK) return fail(b->sims[0], MPM_ERR_CUDA, "%s", b->err.c_str());
+                CK(b->sims[0], launch_copy_segments(x->tape_n.blk, x->tape_n.nblocks, t, c));
+            }
+            return MPM_OK;
+        }));
+        for (MpmHandle* h : b->sims) h->step += len;
+    }
+    for (int t = 0; t < len && resorts; ++t) {
         bool resorted = false;
         for (int i = 0; i < n; ++i) {
             MpmHandle* h = b->sims[i];
@@ -734,7 +786,7 @@ int batch_recompute(MpmBatch* b, BatchAdjoint* x, int seg, int len, cudaStream_t
             if (r != MPM_OK) return r;
         }
         const SegBuf& tp = x->tape_p[t & 1];
-        BCK(b, launch_copy_segments(tp.segs, tp.first, tp.nseg, tp.nblocks, t, s));
+        BCK(b, launch_copy_segments(tp.blk, tp.nblocks, t, s));
         // the tile records hold the sort: refreshed at the segment start and
         // after a re-sort only
         if (t == 0 || resorted) {
@@ -744,8 +796,7 @@ int batch_recompute(MpmBatch* b, BatchAdjoint* x, int seg, int len, cudaStream_t
         r = launch_batch_steps(b, 1, s);
         if (r != MPM_OK) return r;
         for (MpmHandle* h : b->sims) h->step++;
-        BCK(b, launch_copy_segments(x->tape_n.segs, x->tape_n.first, x->tape_n.nseg,
-                                    x->tape_n.nblocks, t, s));
+        BCK(b, launch_copy_segments(x->tape_n.blk, x->tape_n.nblocks, t, s));
         for (MpmHandle* h : b->sims) h->adj->epoch_of[t] = h->adj->nep - 1;
     }
     r = read_statuses(b, s);
@@ -762,7 +813,7 @@ int batch_recompute(MpmBatch* b, BatchAdjoint* x, int seg, int len, cudaStream_t
     }
     BTRY(b, 0, upload_segments(b->sims[0], x->misc, v, s));
     BCK(b, cudaMemsetAsync(x->mismatch, 0, sizeof(int), s));
-    BCK(b, launch_compare_segments(x->misc.segs, x->misc.first, x->misc.nseg, x->misc.nblocks,
+    BCK(b, launch_compare_segments(x->misc.blk, x->misc.nblocks,
                                    x->mismatch, s));
     BCK(b, cudaMemcpyAsync(x->h_mismatch, x->mismatch, sizeof(int), cudaMemcpyDeviceToHost, s));
     BCK(b, cudaStreamSynchronize(s));
@@ -935,7 +986,22 @@ int mpm_batch_adjoint(MpmBatch* b, const float* const* dl_dloc, const float* con
         for (MpmHandle* h : b->sims) one_epoch = one_epoch && h->adj->nep == 1;
         const int4* rtiles = one_epoch ? b->d_act_list : b->d_tiles;
         const int nrtiles = one_epoch ? b->nact : b->ntiles;
-        for (int t = len - 1; t >= 0 && r == MPM_OK; --t) {
+        if (one_epoch) {
+            // no permutation between steps: the segment's reverse steps as one graph
+            check_batch_adj_graphs(b, x);
+            const int64_t key = (int64_t)len | ((int64_t)nrtiles << 20) | ((int64_t)x->n_part_blocks << 42);
+            r = run_cached_graph(b->sims[0], x->g_rev, key, s, [&](cudaStream_t c) -> int {
+                for (int t = len - 1; t >= 0; --t) {
+                    CK(b->sims[0], launch_adj_table(x->d_bases, n, t, x->d_table, c));
+                    CK(b->sims[0], launch_rev_batch(x->d_table, b->cfg.usl, b->cfg.traction, any_pvc,
+                                                    b->cfg.reinit, any_newt, rtiles, nrtiles, x->part_blocks,
+                                                    x->n_part_blocks, c));
+                }
+                return MPM_OK;
+            });
+            if (r != MPM_OK) r = from_sim(b, 0, r);
+        }
+        for (int t = len - 1; t >= 0 && r == MPM_OK && !one_epoch; --t) {
             for (int i = 0; i < n && r == MPM_OK; ++i) {
                 MpmHandle* h = b->sims[i];
                 AdjointState* a = h->adj;

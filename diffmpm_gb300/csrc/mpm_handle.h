@@ -53,7 +53,9 @@ struct Checkpoint {
 struct SegBuf {
     CopySeg* segs = nullptr;
     unsigned* first = nullptr;
+    CopyChunk* blk = nullptr; // chunk table of the copy kernels
     size_t cap = 0;
+    size_t blk_cap = 0;
     int nseg = 0;
     unsigned nblocks = 0;
 };

@@ -2101,8 +2101,11 @@ cudaError_t launch_node_momentum(const float* m, const float* vx, const float* v
 // ---------------------------------------------------------------------------
 // Segmented copy and status gather for batches
 // ---------------------------------------------------------------------------
-// Segment of block b: the last i with first[i] <= b.
-__device__ __forceinline__ int segment_of(const unsigned* __restrict__ first, int nseg, unsigned b) {
+// Chunk table: chunk b of segment i (the last i with first[i] <= b).
+__global__ void k_chunk_table(const CopySeg* __restrict__ segs, const unsigned* __restrict__ first,
+                              int nseg, unsigned nchunks, CopyChunk* __restrict__ chunks) {
+    const unsigned b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nchunks) return;
     int lo = 0, hi = nseg - 1;
     #pragma unroll 1
     while (lo < hi) {
@@ -2110,69 +2113,98 @@ __device__ __forceinline__ int segment_of(const unsigned* __restrict__ first, in
         if (first[mid] <= b) lo = mid;
         else hi = mid - 1;
     }
-    return lo;
+    const CopySeg sg = segs[lo];
+    const unsigned long long off = (unsigned long long)(b - first[lo]) * COPY_CHUNK;
+    CopyChunk c;
+    c.src = static_cast<const char*>(sg.src) + off;
+    c.dst = static_cast<char*>(sg.dst) + off;
+    c.dst_step = sg.dst_step;
+    c.bytes = off < sg.bytes ? min((unsigned long long)COPY_CHUNK, sg.bytes - off) : 0ull;
+    chunks[b] = c;
 }
 
-__global__ void __launch_bounds__(256)
-k_copy_segments(const CopySeg* __restrict__ segs, const unsigned* __restrict__ first, int nseg,
-                int t) {
-    const unsigned b = blockIdx.x;
-    const int i = segment_of(first, nseg, b);
-    const CopySeg sg = segs[i];
-    const unsigned long long off = (unsigned long long)(b - first[i]) * COPY_CHUNK;
-    if (off >= sg.bytes) return;
-    const unsigned long long end = min(off + COPY_CHUNK, sg.bytes);
-    const char* src = static_cast<const char*>(sg.src);
-    char* dst = static_cast<char*>(sg.dst) + (unsigned long long)t * sg.dst_step;
-    const bool vec = ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15) == 0;
-    unsigned long long k0 = off;
-    if (vec) {
-        const unsigned long long vend = off + ((end - off) & ~15ull);
-        for (unsigned long long k = off + 16ull * threadIdx.x; k < vend; k += 16ull * blockDim.x)
-            *reinterpret_cast<uint4*>(dst + k) = *reinterpret_cast<const uint4*>(src + k);
-        k0 = vend;
-    }
-    for (unsigned long long k = k0 + threadIdx.x; k < end; k += blockDim.x) dst[k] = src[k];
-}
-
-cudaError_t launch_copy_segments(const CopySeg* segs, const unsigned* first, int nseg,
-                                 unsigned nblocks, int t, cudaStream_t s) {
-    if (nseg > 0 && nblocks > 0) k_copy_segments<<<nblocks, 256, 0, s>>>(segs, first, nseg, t);
+cudaError_t launch_chunk_table(const CopySeg* segs, const unsigned* first, int nseg, unsigned nchunks,
+                               CopyChunk* chunks, cudaStream_t s) {
+    if (nseg > 0 && nchunks > 0)
+        k_chunk_table<<<(nchunks + 255) / 256, 256, 0, s>>>(segs, first, nseg, nchunks, chunks);
     return cudaGetLastError();
 }
 
-__global__ void __launch_bounds__(256)
-k_compare_segments(const CopySeg* __restrict__ segs, const unsigned* __restrict__ first, int nseg,
-                   int* __restrict__ mismatch) {
-    const unsigned b = blockIdx.x;
-    const int i = segment_of(first, nseg, b);
-    const CopySeg sg = segs[i];
-    const unsigned long long off = (unsigned long long)(b - first[i]) * COPY_CHUNK;
-    int diff = 0;
-    if (off < sg.bytes) {
-        const unsigned long long end = min(off + COPY_CHUNK, sg.bytes);
-        const char* a = static_cast<const char*>(sg.src);
-        const char* c = static_cast<const char*>(sg.dst);
-        const bool vec = ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(c)) & 15) == 0;
-        unsigned long long k0 = off;
-        if (vec) {
-            const unsigned long long vend = off + ((end - off) & ~15ull);
-            for (unsigned long long k = off + 16ull * threadIdx.x; k < vend; k += 16ull * blockDim.x) {
-                const uint4 x = *reinterpret_cast<const uint4*>(a + k);
-                const uint4 y = *reinterpret_cast<const uint4*>(c + k);
-                diff += (x.x != y.x) | (x.y != y.y) | (x.z != y.z) | (x.w != y.w);
-            }
-            k0 = vend;
-        }
-        for (unsigned long long k = k0 + threadIdx.x; k < end; k += blockDim.x) diff += a[k] != c[k];
+// A CTA of COPY_THREADS threads moves one chunk as COPY_VEC 16-byte words a
+// thread, all loaded before any is stored.  The destinations (tape slots,
+// checkpoints, snapshots) are not read again soon: streaming stores.
+constexpr int COPY_THREADS = 256;
+constexpr int COPY_VEC = COPY_CHUNK / (16 * COPY_THREADS);
+static_assert(COPY_VEC * 16 * COPY_THREADS == COPY_CHUNK, "a chunk is whole words of every thread");
+
+__device__ __forceinline__ CopyChunk load_chunk(const CopyChunk* __restrict__ chunks, unsigned b) {
+    const ulonglong2* p = reinterpret_cast<const ulonglong2*>(chunks + b);
+    const ulonglong2 u = p[0], w = p[1];
+    CopyChunk c;
+    c.src = reinterpret_cast<const char*>(u.x);
+    c.dst = reinterpret_cast<char*>(u.y);
+    c.dst_step = w.x;
+    c.bytes = w.y;
+    return c;
+}
+
+__global__ void __launch_bounds__(COPY_THREADS)
+k_copy_segments(const CopyChunk* __restrict__ chunks, int t) {
+    static_assert(sizeof(CopyChunk) == 32, "chunk entries are read as two 16-byte words");
+    const CopyChunk c = load_chunk(chunks, blockIdx.x);
+    const char* __restrict__ src = c.src;
+    char* __restrict__ dst = c.dst + (unsigned long long)t * c.dst_step;
+    const unsigned n = (unsigned)c.bytes;
+    const bool vec = ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15) == 0;
+    const unsigned n16 = vec ? n >> 4 : 0;
+    const uint4* __restrict__ s4 = reinterpret_cast<const uint4*>(src);
+    uint4* __restrict__ d4 = reinterpret_cast<uint4*>(dst);
+    uint4 v[COPY_VEC];
+    #pragma unroll
+    for (int u = 0; u < COPY_VEC; ++u) {
+        const unsigned k = threadIdx.x + u * COPY_THREADS;
+        if (k < n16) v[u] = s4[k];
     }
+    #pragma unroll
+    for (int u = 0; u < COPY_VEC; ++u) {
+        const unsigned k = threadIdx.x + u * COPY_THREADS;
+        if (k < n16) __stcs(d4 + k, v[u]);
+    }
+    for (unsigned k = 16 * n16 + threadIdx.x; k < n; k += COPY_THREADS) dst[k] = src[k];
+}
+
+cudaError_t launch_copy_segments(const CopyChunk* chunks, unsigned nchunks, int t, cudaStream_t s) {
+    if (nchunks > 0) k_copy_segments<<<nchunks, COPY_THREADS, 0, s>>>(chunks, t);
+    return cudaGetLastError();
+}
+
+__global__ void __launch_bounds__(COPY_THREADS)
+k_compare_segments(const CopyChunk* __restrict__ chunks, int* __restrict__ mismatch) {
+    const CopyChunk c = load_chunk(chunks, blockIdx.x);
+    const char* a = c.src;
+    const char* d = c.dst;
+    const unsigned n = (unsigned)c.bytes;
+    const bool vec = ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(d)) & 15) == 0;
+    const unsigned n16 = vec ? n >> 4 : 0;
+    int diff = 0;
+    const uint4* a4 = reinterpret_cast<const uint4*>(a);
+    const uint4* d4 = reinterpret_cast<const uint4*>(d);
+    #pragma unroll
+    for (int u = 0; u < COPY_VEC; ++u) {
+        const unsigned k = threadIdx.x + u * COPY_THREADS;
+        if (k < n16) {
+            const uint4 x = a4[k], y = d4[k];
+            diff += (x.x != y.x) | (x.y != y.y) | (x.z != y.z) | (x.w != y.w);
+        }
+    }
+    for (unsigned k = 16 * n16 + threadIdx.x; k < n; k += COPY_THREADS) diff += a[k] != d[k];
     const int total = __syncthreads_count(diff != 0);
     if (threadIdx.x == 0 && total) atomicAdd(mismatch, total);
 }
 
-cudaError_t launch_compare_segments(const CopySeg* segs, const unsigned* first, int nseg,
-                                    unsigned nblocks, int* mismatch, cudaStream_t s) {
-    if (nseg > 0 && nblocks > 0) k_compare_segments<<<nblocks, 256, 0, s>>>(segs, first, nseg, mismatch);
+cudaError_t launch_compare_segments(const CopyChunk* chunks, unsigned nchunks, int* mismatch,
+                                    cudaStream_t s) {
+    if (nchunks > 0) k_compare_segments<<<nchunks, COPY_THREADS, 0, s>>>(chunks, mismatch);
     return cudaGetLastError();
 }
 

@@ -117,21 +117,31 @@ cudaError_t launch_node_momentum(const float* m, const float* vx, const float* v
                                  float* out, cudaStream_t s);
 
 // Copy of many device-memory segments in one launch (snapshots and checkpoints
-// of whole batches, the adjoint's tape).  Segment i is copied by the CTAs
-// first[i] .. first[i+1]-1, COPY_CHUNK bytes each; first[nseg] is the grid
-// size.  The destination of a launch with slot t is dst + t * dst_step.
+// of whole batches, the adjoint's tape).  Segment i is cut into chunks of
+// COPY_CHUNK bytes, chunks first[i] .. first[i+1]-1, first[nseg] being their
+// number.  The chunk table (source, destination and length of every chunk)
+// is formed on the device once per upload (launch_chunk_table), so a CTA of
+// the copy kernel starts its chunk after one dependent load.  The
+// destination of a launch with slot t is dst + t * dst_step.
 struct CopySeg {
     const void* src;
     void* dst;
     unsigned long long bytes;
     unsigned long long dst_step;
 };
-constexpr unsigned COPY_CHUNK = 8192;
-cudaError_t launch_copy_segments(const CopySeg* segs, const unsigned* first, int nseg,
-                                 unsigned nblocks, int t, cudaStream_t s);
+struct CopyChunk {
+    const char* src;
+    char* dst;
+    unsigned long long dst_step;
+    unsigned long long bytes;
+};
+constexpr unsigned COPY_CHUNK = 16384;
+cudaError_t launch_chunk_table(const CopySeg* segs, const unsigned* first, int nseg, unsigned nchunks,
+                               CopyChunk* chunks, cudaStream_t s);
+cudaError_t launch_copy_segments(const CopyChunk* chunks, unsigned nchunks, int t, cudaStream_t s);
 // *mismatch += number of differing 16-byte words or tail bytes between src and dst.
-cudaError_t launch_compare_segments(const CopySeg* segs, const unsigned* first, int nseg,
-                                    unsigned nblocks, int* mismatch, cudaStream_t s);
+cudaError_t launch_compare_segments(const CopyChunk* chunks, unsigned nchunks, int* mismatch,
+                                    cudaStream_t s);
 
 // out[i] = *ctls[i], then ctls[i]->status = 0, for i < n.
 cudaError_t launch_gather_status(Control* const* ctls, int n, Control* out, cudaStream_t s);

@@ -96,6 +96,7 @@ void checkpoint_segments(MpmHandle* h, Checkpoint& c, bool save, std::vector<Cop
 void segbuf_free(SegBuf& buf) {
     if (buf.segs) cudaFree(buf.segs);
     if (buf.first) cudaFree(buf.first);
+    if (buf.blk) cudaFree(buf.blk);
     buf = SegBuf{};
 }
 
@@ -123,6 +124,15 @@ int upload_segments(MpmHandle* h, SegBuf& buf, const std::vector<CopySeg>& segs,
                           cudaMemcpyHostToDevice, s));
     CK(h, cudaMemcpyAsync(buf.first, first.data(), sizeof(unsigned) * first.size(),
                           cudaMemcpyHostToDevice, s));
+    if (buf.blk_cap < total) {
+        if (buf.blk) cudaFree(buf.blk);
+        buf.blk = nullptr;
+        buf.blk_cap = 0;
+        const size_t cap = total + total / 2;
+        CK(h, cudaMalloc(&buf.blk, sizeof(CopyChunk) * cap));
+        buf.blk_cap = cap;
+    }
+    CK(h, launch_chunk_table(buf.segs, buf.first, (int)segs.size(), (unsigned)total, buf.blk, s));
     buf.nseg = (int)segs.size();
     buf.nblocks = (unsigned)total;
     return MPM_OK;
@@ -130,7 +140,7 @@ int upload_segments(MpmHandle* h, SegBuf& buf, const std::vector<CopySeg>& segs,
 
 int run_segments(MpmHandle* h, SegBuf& buf, const std::vector<CopySeg>& segs, cudaStream_t s) {
     TRY(upload_segments(h, buf, segs, s));
-    CK(h, launch_copy_segments(buf.segs, buf.first, buf.nseg, buf.nblocks, 0, s));
+    CK(h, launch_copy_segments(buf.blk, buf.nblocks, 0, s));
     return MPM_OK;
 }
 
