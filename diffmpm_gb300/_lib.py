@@ -96,6 +96,7 @@ SIGNATURES = [
     ("mpm_time_phases", C.c_int, [_VP, C.c_int, _VP, _VP]),
     ("mpm_set_block_steps", C.c_int, [_VP, C.c_int]),
     ("mpm_set_kernel_variant", C.c_int, [_VP, C.c_int, C.c_int, C.c_int]),
+    ("mpm_set_empty_split", C.c_int, [_VP, C.c_int]),
     ("mpm_device_name", C.c_int, [C.c_int, C.c_char_p, C.c_int]),
     ("mpm_get_counters", C.c_int, [_VP, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     ("mpm_set_gravity", C.c_int, [_VP, C.c_double, C.c_double]),

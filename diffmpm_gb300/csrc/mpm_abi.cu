@@ -219,8 +219,18 @@ int classify_tiles(MpmHandle* h, cudaStream_t s) {
                                 h->d_tile_counts, s));
     CK(h, cudaMemcpyAsync(h->h_tile_counts, h->d_tile_counts, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(h, cudaStreamSynchronize(s));
-    h->nact = h->h_tile_counts[0];
-    h->nemp = h->h_tile_counts[1];
+    if (h->h_tile_counts[1] < h->empty_split_min) {
+        // too few empty tiles to pay for a launch of their own: the step
+        // kernels take every tile (an empty one costs a CTA that only
+        // updates its nodes, in a grid that is often under one wave)
+        h->step_tiles = h->dtiles;
+        h->nact = h->ntiles;
+        h->nemp = 0;
+    } else {
+        h->step_tiles = h->d_active;
+        h->nact = tile_grid(h->h_tile_counts[0], h->ntiles);
+        h->nemp = tile_grid(h->h_tile_counts[1], h->ntiles);
+    }
     return MPM_OK;
 }
 
@@ -237,11 +247,11 @@ int launch_phase(MpmHandle* h, int phase, int k, cudaStream_t s) {
     cudaError_t e = cudaSuccess;
     if (phase == 0) {
         CK(h, launch_empty_nodes(h->hs, h->d_empty, h->nemp, h->ctl, k, s));
-        e = launch_nodal_kinematics(c, h->hs, h->d_active, h->nact, h->ctl, k, s);
+        e = launch_nodal_kinematics(c, h->hs, h->step_tiles, h->nact, h->ctl, k, s);
     } else if (phase == 1) {
-        e = launch_forces(c, h->hs, h->d_active, h->nact, h->ctl, k, s);
+        e = launch_forces(c, h->hs, h->step_tiles, h->nact, h->ctl, k, s);
     } else {
-        e = launch_particle_kinematics(c, h->hs, h->d_active, h->nact, h->ctl, k, s);
+        e = launch_particle_kinematics(c, h->hs, h->step_tiles, h->nact, h->ctl, k, s);
     }
     CK(h, e);
     return MPM_OK;
@@ -702,6 +712,7 @@ int mpm_create(const MpmDesc* d, MpmHandle** out) {
         up(h->d_empty, none.data(), sizeof(int4) * tiles.size());
         h->nact = (int)tiles.size();
         h->nemp = 0;
+        h->step_tiles = h->d_active;
     }
     if (r != MPM_OK) return failc(r, "tile upload failed");
 
@@ -1306,6 +1317,13 @@ int mpm_device_name(int device, char* name, int len) {
     }
     snprintf(name, (size_t)len, "%s (sm_%d%d, %d SMs)", prop.name, prop.major, prop.minor,
              prop.multiProcessorCount);
+    return MPM_OK;
+}
+
+int mpm_set_empty_split(MpmHandle* h, int min_empty) {
+    if (!h) return MPM_ERR_INVALID;
+    if (min_empty < 0) return fail(h, MPM_ERR_INVALID, "min_empty is negative");
+    h->empty_split_min = min_empty;   // applies from the next classification
     return MPM_OK;
 }
 

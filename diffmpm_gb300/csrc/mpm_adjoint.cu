@@ -520,13 +520,13 @@ AdjStep base_args(MpmHandle* h, AdjointState* a, int epoch) {
     return A;
 }
 
-// The tiles the reverse node passes visit: the active tiles of the segment's
-// sort when the segment is one sort epoch (the classification of its re-run
-// holds for every step; an empty tile's node adjoints and cell counts are
-// read by no particle), else every tile.
+// The tiles the reverse node passes visit: the forward step kernels' tiles of
+// the segment's sort when the segment is one sort epoch (the classification
+// of its re-run holds for every step; an empty tile's node adjoints and cell
+// counts are read by no particle), else every tile.
 void reverse_tiles(MpmHandle* h, AdjointState* a, const int4*& tiles, int& ntiles) {
     if (a->nep == 1) {
-        tiles = h->d_active;
+        tiles = h->step_tiles;
         ntiles = h->nact;
     } else {
         tiles = h->dtiles;

@@ -250,7 +250,9 @@ __device__ __forceinline__ void rev_nodal_update_tile(const AdjStep& A, const in
 template <bool USL>
 __global__ void __launch_bounds__(TILE_THREADS, 2)
 k_rev_nodal_update(const __grid_constant__ AdjStep A, const int4* __restrict__ tiles) {
-    rev_nodal_update_tile<USL>(A, tiles[blockIdx.x]);
+    const int4 T = tiles[blockIdx.x];
+    if (T.x < 0) return;   // past the listed tiles
+    rev_nodal_update_tile<USL>(A, T);
 }
 
 template <bool USL>
@@ -258,6 +260,7 @@ __global__ void __launch_bounds__(TILE_THREADS, 2)
 k_rev_nodal_update_batch(const AdjStep* __restrict__ table, const int4* __restrict__ tiles) {
     __shared__ AdjStep sA;
     const int4 T = tiles[blockIdx.x];
+    if (T.x < 0) return;   // past the listed tiles
     load_step_args(table + T.x, sA);
     rev_nodal_update_tile<USL>(sA, T);
 }
@@ -750,8 +753,10 @@ __device__ __forceinline__ void rev_node_velocity_tile(const AdjStep& A, const i
 template <int MODE>
 __global__ void __launch_bounds__(TILE_THREADS, 2)
 k_rev_nodal_kinematics(const __grid_constant__ AdjStep A, const int4* __restrict__ tiles) {
-    if (MODE == RK_NODES) rev_node_velocity_tile(A, tiles[blockIdx.x]);
-    else rev_nodal_kinematics_tile<MODE>(A, tiles[blockIdx.x]);
+    const int4 T = tiles[blockIdx.x];
+    if (T.x < 0) return;   // past the listed tiles
+    if (MODE == RK_NODES) rev_node_velocity_tile(A, T);
+    else rev_nodal_kinematics_tile<MODE>(A, T);
 }
 
 template <int MODE>
@@ -759,6 +764,7 @@ __global__ void __launch_bounds__(TILE_THREADS, 2)
 k_rev_nodal_kinematics_batch(const AdjStep* __restrict__ table, const int4* __restrict__ tiles) {
     __shared__ AdjStep sA;
     const int4 T = tiles[blockIdx.x];
+    if (T.x < 0) return;   // past the listed tiles
     load_step_args(table + T.x, sA);
     if (MODE == RK_NODES) rev_node_velocity_tile(sA, T);
     else rev_nodal_kinematics_tile<MODE>(sA, T);

@@ -64,8 +64,8 @@ int prepare_tiles(MpmBatch* b, cudaStream_t s) {
     BCK(b, launch_gather_tiles(b->d_sims, b->d_ctls, b->d_emp_list, b->ntiles, b->d_edescs, s));
     BCK(b, cudaMemcpyAsync(b->h_tcounts, b->d_tcounts, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
     BCK(b, cudaStreamSynchronize(s));
-    b->nact = b->h_tcounts[0];
-    b->nemp = b->h_tcounts[1];
+    b->nact = tile_grid(b->h_tcounts[0], b->ntiles);
+    b->nemp = tile_grid(b->h_tcounts[1], b->ntiles);
     return MPM_OK;
 }
 

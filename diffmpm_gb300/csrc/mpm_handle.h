@@ -120,6 +120,7 @@ struct MpmHandle {
     int* d_tile_counts = nullptr;    // [active, empty]
     int* h_tile_counts = nullptr;    // pinned mirror
     int nact = 0, nemp = 0;          // the step kernels' and the empty-node kernel's grids
+    const int4* step_tiles = nullptr; // the step kernels' list: d_active after a split, else dtiles
     int64_t step = 0;
     // staging and pointer tables
     void* stage = nullptr;
@@ -144,6 +145,7 @@ struct MpmHandle {
     int block_steps = 100;
     int nk_ctas = 3, g2p_ctas = 2;     // kernel builds (StepConfig), set by mpm_set_kernel_variant
     int forces_lpc = 0;
+    int empty_split_min = mpm::EMPTY_SPLIT_MIN;   // mpm_set_empty_split
     int64_t resorts = 0, rollbacks = 0;
     // differentiation (null until mpm_record); gen counts state changes
     mpm::AdjointState* adj = nullptr;

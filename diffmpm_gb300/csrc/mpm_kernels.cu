@@ -612,6 +612,7 @@ __global__ void __launch_bounds__(TILE_THREADS, MINB)
 k_nodal_kinematics_batch(const TileDesc* __restrict__ td, int k) {
     __shared__ TileDesc sT;
     load_tile(td + blockIdx.x, sT);
+    if (sT.T.x < 0) return;   // past the listed tiles
     nodal_kinematics_tile<REINIT, true>(sT.S, sT.T, sT.ctl, k, &sT);
 }
 
@@ -1017,6 +1018,7 @@ __global__ void __launch_bounds__(TILE_THREADS, TILE_MIN_CTAS)
 k_forces_batch(const TileDesc* __restrict__ td, int k) {
     __shared__ TileDesc sT;
     load_tile(td + blockIdx.x, sT);
+    if (sT.T.x < 0) return;   // past the listed tiles
     forces_tile<USL, REINIT, TRAC, true, MODE>(sT.S, sT.T, sT.ctl, k, &sT);
 }
 
@@ -1379,6 +1381,7 @@ __global__ void __launch_bounds__(TILE_THREADS, MINB)
 k_particle_kinematics_batch(const TileDesc* __restrict__ td, int k) {
     __shared__ TileDesc sT;
     load_tile(td + blockIdx.x, sT);
+    if (sT.T.x < 0) return;   // past the listed tiles
     // no particle stored in the tile's sort-cells or around them: nothing
     // moves, and the sort-cells' drift flags are already clear (a flag is set
     // only for a sort-cell that stores a particle, and a re-sort clears all)

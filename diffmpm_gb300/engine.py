@@ -231,6 +231,11 @@ class Simulation:
         time step, scheme, particle count), for tuning-cache keys."""
         return dict(self._config, particles=int(self.n))
 
+    def set_empty_split(self, min_empty):
+        """Launch the empty tiles apart when there are at least ``min_empty``
+        of them (mpm_set_empty_split): the same results either way."""
+        self._ok(self._lib.mpm_set_empty_split(self._h, int(min_empty)))
+
     def set_kernel_variant(self, nk_ctas=3, g2p_ctas=2, forces_lpc=0):
         """Kernel builds of the step (mpm_set_kernel_variant): the same results,
         built for 2 or 3 resident CTAs per SM, and either forces path."""

@@ -229,6 +229,14 @@ int mpm_set_block_steps(MpmHandle* h, int steps);
  * way; only the speed differs (mpm_batch_autotune chooses them for a batch). */
 int mpm_set_kernel_variant(MpmHandle* h, int nk_ctas, int g2p_ctas, int forces_lpc);
 
+/* Tiles whose cells and ring of cells store no particle need only a node
+ * update per step.  When a simulation has at least `min_empty` such tiles
+ * (default 128), its step kernels are launched over the other tiles and one
+ * kernel updates the empty tiles' nodes; otherwise every tile goes through
+ * the step kernels.  Results are the same bits either way; 0 always splits,
+ * INT_MAX never does.  No counterpart in the reference. */
+int mpm_set_empty_split(MpmHandle* h, int min_empty);
+
 /* Name of CUDA device `device` with its compute capability and SM count
  * (NUL-terminated, truncated to len bytes), the GPU part of the key under
  * which tuning results are cached.  No counterpart in the reference. */
