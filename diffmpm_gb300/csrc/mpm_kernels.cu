@@ -415,6 +415,31 @@ __device__ __forceinline__ ForceIn force_in_global(const SimDev& S, int q, int p
     return in;
 }
 
+// The material table of the CTA's simulation, staged in shared memory at
+// tile set-up when it has at most MAT_SHARED entries: the stress updates read
+// a particle's material there (with one material, without loading the
+// particle's material id).
+constexpr int MAT_SHARED = 8;
+__shared__ MatDev s_mats[MAT_SHARED];
+
+template <bool VD>
+__device__ __forceinline__ void stage_materials(const SimDev& S) {
+    constexpr int W = (int)(sizeof(MatDev) / 4);
+    static_assert(W * 4 == (int)sizeof(MatDev), "material entries are whole words");
+    const int n = min(rd<VD>(S.nmat), MAT_SHARED);
+    const int* src = reinterpret_cast<const int*>(rd<VD>(S.mats));
+    int* dst = reinterpret_cast<int*>(s_mats);
+    for (int i = threadIdx.x; i < n * W; i += blockDim.x) dst[i] = src[i];
+}
+
+template <bool VD>
+__device__ __forceinline__ const MatDev& material_of(const SimDev& S, int q) {
+    const int n = rd<VD>(S.nmat);
+    if (n == 1) return s_mats[0];
+    const int m = rd<VD>(S.mat)[q];
+    return n <= MAT_SHARED ? s_mats[m] : rd<VD>(S.mats)[m];
+}
+
 // Per-particle work of phase 2 on a particle state held in registers: the
 // USF strain/volume/stress update of `p` and `V` (the particle's volume
 // before the step; element.py:236-303, 842-901 via particle.py:249-327) and
@@ -435,7 +460,7 @@ __device__ __forceinline__ float force_core(const SimDev& S, int q, float x, flo
     if (!USL) {
         float r0, r1, r3;
         strain_rate4(Gx, Gy, nvx, nvy, r0, r1, r3);
-        const MatDev& M = rd<VD>(S.mats)[rd<VD>(S.mat)[q]];
+        const MatDev& M = material_of<VD>(S, q);
         const float* E = rd<VD>(S.E);
         const float Ep = E ? E[q] : -1.0f;
         V = fm(V, strain_stress_update(M, Ep, rd<VD>(S.dt), r0, r1, r3, dvol, p));
@@ -811,6 +836,7 @@ __device__ __forceinline__ void forces_tile(const SimDev& S, const int4 T,
     for (int e = 0; e < 2; ++e)
         if (tid + e * TILE_THREADS < NV_W * NV_H) s_v[tid + e * TILE_THREADS] = nv[e];
     if constexpr (MODE == FM_STAGED) staged_arrays<USL, REINIT, VD>(S, parity, tid, sh.src);
+    if constexpr (!USL) stage_materials<VD>(S);
     const bool slow = __syncthreads_or(L.drift) != 0;
 
     auto cell_velocities = [&](int li, int lj, float* vx, float* vy) {
@@ -1169,7 +1195,7 @@ __device__ __forceinline__ float2 g2p_particle(const SimDev& S, int q, const flo
         p.exy = b[GF_EXY][lane];
         p.rho = b[GF_RHO][lane];
         p.vsc = b[GF_VSC][lane];
-        const MatDev& M = S.mats[S.mat[q]];
+        const MatDev& M = material_of<false>(S, q);
         const float Ep = S.E ? S.E[q] : -1.0f;
         const float f = strain_stress_update(M, Ep, dt, r0, r1, r3, dvol, p);
         S.sxx[next][q] = p.sxx;
@@ -1236,6 +1262,7 @@ __device__ __forceinline__ void particle_kinematics_tile(const SimDev& S, const 
     RowStage16<NF, DEPTH> st(&s_stage[w][0][0][0], src, rb, re, lane);
     const int rb4 = st.rb4;
     st.prime();
+    if constexpr (USL) stage_materials<false>(S);
     if (!__syncthreads_or(re > rb)) {
         // no particle stored in the tile's sort-cells: their drift flags clear
         if (row_ok && lane < TILE_NX && c0x + 1 + lane < S.nx) S.cflag[sj * S.nx + c0x + 1 + lane] = 0;
