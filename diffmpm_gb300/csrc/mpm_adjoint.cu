@@ -191,8 +191,14 @@ int restore_checkpoint(MpmHandle* h, Checkpoint& c, cudaStream_t s) {
     return sync(h, s);
 }
 
+// Particle slots between consecutive tape slots (np rounded up to 4).
+size_t tape_stride(const MpmHandle* h) { return ((size_t)h->np + 3) & ~(size_t)3; }
+
 int ensure_adjoint_buffers(MpmHandle* h, AdjointState* a, int slots, cudaStream_t s) {
-    const size_t np = (size_t)h->np, nn = (size_t)h->nn;
+    // particle arrays and tape slots hold a multiple of 4 slots, so that every
+    // slot starts on a 16-byte boundary for the reverse node passes' 16-byte
+    // row staging (which may read up to 3 slots past a row's end)
+    const size_t np = ((size_t)h->np + 3) & ~(size_t)3, nn = (size_t)h->nn;
     bool newtonian = false;
     for (const MatDev& m : h->mats) newtonian = newtonian || m.type == MAT_NEWTONIAN;
     if (a->tape_slots < slots || (!h->reinit && !a->tvol) || (newtonian && !a->tvsc)) {
@@ -296,12 +302,12 @@ int capture_epoch(MpmHandle* h, AdjointState* a, cudaStream_t s) {
 // state and drift flags (before the step) into slot 0 + t * stride.
 void tape_particle_segments(MpmHandle* h, AdjointState* a, int par, std::vector<CopySeg>& v) {
     const PSet& p = h->ps[h->pcur];
-    const size_t np = (size_t)h->np;
+    const size_t np = (size_t)h->np, stride = tape_stride(h);
     const float* src[NTP] = {p.x, p.y, p.vx, p.vy, p.sxx[par], p.syy[par], p.szz[par],
                              p.sxy[par], p.rho[par]};
-    for (int k = 0; k < NTP; ++k) add_seg(v, src[k], a->tp[k], sizeof(float) * np, sizeof(float) * np);
-    if (!h->reinit) add_seg(v, p.vol[par], a->tvol, sizeof(float) * np, sizeof(float) * np);
-    if (a->tvsc) add_seg(v, p.vsc[par], a->tvsc, sizeof(float) * np, sizeof(float) * np);
+    for (int k = 0; k < NTP; ++k) add_seg(v, src[k], a->tp[k], sizeof(float) * np, sizeof(float) * stride);
+    if (!h->reinit) add_seg(v, p.vol[par], a->tvol, sizeof(float) * np, sizeof(float) * stride);
+    if (a->tvsc) add_seg(v, p.vsc[par], a->tvsc, sizeof(float) * np, sizeof(float) * stride);
     add_seg(v, h->cflag, a->tflag, (size_t)h->ncell, (size_t)h->ncell);
 }
 
@@ -514,7 +520,7 @@ AdjStep base_args(MpmHandle* h, AdjointState* a, int epoch) {
     float** ns[NNS] = {&A.fbx, &A.fby, &A.mb, &A.vabx, &A.vaby, &A.qbx, &A.qby, &A.mbt};
     for (int k = 0; k < NNS; ++k) *ns[k] = a->nscr[k];
     A.cnt = a->cnt;
-    A.sp = h->np;
+    A.sp = (long long)tape_stride(h);
     A.sn = h->nn;
     A.sc = h->ncell;
     return A;

@@ -111,11 +111,17 @@ __device__ __forceinline__ void g2p_seeds(const AdjStep& A, int q, float& gx, fl
 // TILE_THREADS threads covers TILE_CX x TILE_CY cells and owns the nodes at
 // the upper-right corners of all but its first column and row), with each
 // thread summing the corner contributions of its cell's particles.  Fast
-// path: the cell rows are staged with coalesced copies (row_pass); slow path
+// path: the cell rows are staged with coalesced 16-byte copies (row_pass16); slow path
 // (a particle near the tile was outside its sort-cell at the step start): the
 // tape's drift flags and visit_tape_cell.  Tiles with no stored particle in
 // reach only write their nodes (all sums zero).
 // ---------------------------------------------------------------------------
+
+// Slots of a staged row per pass of the reverse node passes: a row of 4
+// particles in each of 32 cells, starting anywhere in a 16-byte piece, fits
+// one pass.  The staged arrays (tape slots, adjoint and scratch arrays) start
+// on 16-byte boundaries and hold a multiple of 4 slots.
+constexpr int REV_ROW_P = 132;
 
 // Tile set-up of the reverse node passes with every load issued before any is
 // consumed (one round trip): this thread's storage start of row cj (cs, and
@@ -180,7 +186,7 @@ template <bool USL>
 __device__ __forceinline__ void rev_nodal_update_tile(const AdjStep& A, const int4 T) {
     constexpr int NQ = 16;   // [v-hat bar x, y, a-hat bar x, y] x corner
     __shared__ float s_c[NQ][SC_STRIDE];
-    __shared__ float s_row[TILE_CY][6][ROW_P];
+    __shared__ __align__(16) float s_row[TILE_CY][6][REV_ROW_P];
     __shared__ int s_cs[TILE_CY][33];
     const int tid = threadIdx.x, tx = tid % TILE_CX, ty = tid / TILE_CX;
     const int c0x = T.y * TILE_NX - 1, c0y = T.z * TILE_NY - 1;
@@ -224,8 +230,8 @@ __device__ __forceinline__ void rev_nodal_update_tile(const AdjStep& A, const in
         if (!slow) {
             const int* cs = s_cs[ty];
             const float* const src[6] = {A.x, A.y, A.lx, A.ly, A.lvx, A.lvy};
-            float (*buf)[ROW_P] = s_row[ty];
-            row_pass<6>(buf, src, cs[0], cs[32], cs[tx], cs[tx + 1], tx, [&](int, int j) {
+            float (*buf)[REV_ROW_P] = s_row[ty];
+            row_pass16<6, REV_ROW_P>(buf, src, cs[0], cs[32], cs[tx], cs[tx + 1], tx, [&](int, int j) {
                 add(buf[0][j], buf[1][j], buf[2][j], buf[3][j], buf[4][j], buf[5][j]);
             });
         } else if (in_mesh) {
@@ -681,7 +687,7 @@ template <int MODE>
 __device__ __forceinline__ void rev_nodal_kinematics_tile(const AdjStep& A, const int4 T) {
     constexpr int NQ = 8;    // [vA-bar x, y] x corner
     __shared__ float s_c[NQ][SC_STRIDE];
-    __shared__ float s_row[TILE_CY][7][ROW_P];
+    __shared__ __align__(16) float s_row[TILE_CY][7][REV_ROW_P];
     __shared__ int s_cs[TILE_CY][33];
     const int tid = threadIdx.x, tx = tid % TILE_CX, ty = tid / TILE_CX;
     const int c0x = T.y * TILE_NX - 1, c0y = T.z * TILE_NY - 1;
@@ -714,8 +720,8 @@ __device__ __forceinline__ void rev_nodal_kinematics_tile(const AdjStep& A, cons
         if (!slow) {
             const int* cs = s_cs[ty];
             const float* const src[7] = {A.x, A.y, A.r0b, A.r1b, A.r3b, A.c0b, A.c1b};
-            float (*buf)[ROW_P] = s_row[ty];
-            row_pass<7>(buf, src, cs[0], cs[32], cs[tx], cs[tx + 1], tx, [&](int, int j) {
+            float (*buf)[REV_ROW_P] = s_row[ty];
+            row_pass16<7, REV_ROW_P>(buf, src, cs[0], cs[32], cs[tx], cs[tx + 1], tx, [&](int, int j) {
                 add(buf[0][j], buf[1][j], buf[2][j], buf[3][j], buf[4][j], buf[5][j], buf[6][j]);
             });
         } else if (in_mesh) {

@@ -263,41 +263,17 @@ __device__ __forceinline__ float node_sum(const float (*s)[SC_STRIDE], int tid) 
 }
 
 // Fast path of the particle-to-grid gathers (forward and reverse): warp w
-// stages the particles stored in sort-cell row w of a tile (storage range [rb, re)) into shared
-// memory with coalesced cp.async copies, ROW_P particles per pass, and lane l
-// then visits the particles of its own cell (storage range [cb, ce)) in storage
-// order, summing their corner contributions in registers: the same order and
-// the same roundings as the slow path's visit_cell, so both paths give the
-// same bits.
-constexpr int ROW_P = 160;
-
-template <int NF, int P = ROW_P, class F>
-__device__ __forceinline__ void row_pass(float (*buf)[P], const float* const (&src)[NF], int rb,
-                                         int re, int cb, int ce, int lane, F&& f) {
-    #pragma unroll 1
-    for (int p0 = rb; p0 < re; p0 += P) {
-        const int p1 = min(p0 + P, re);
-        for (int q = p0 + lane; q < p1; q += 32) {
-            #pragma unroll
-            for (int k = 0; k < NF; ++k)
-                if (src[k]) cp_async4(&buf[k][q - p0], src[k] + q);
-        }
-        cp_async_commit();
-        cp_async_wait<0>();
-        __syncwarp();
-        const int lo = max(cb, p0), hi = min(ce, p1);
-        #pragma unroll 1
-        for (int q = lo; q < hi; ++q) f(q, q - p0);
-        __syncwarp();
-    }
-}
-
-// row_pass with 16-byte copies: pass k stages storage slots
-// [rb4 + kP, rb4 + (k+1)P) (rb4 = rb rounded down to a multiple of 4, P a
-// multiple of 4) of every field with one cp.async.cg per 16-byte piece, and
-// f(q, j) finds slot q at buf[.][j], j = q - (rb4 + kP).  Every source array
-// must start on a 16-byte boundary and hold a multiple of 4 slots (the last
-// piece may read up to 3 slots past re).  Same visiting order as row_pass.
+// stages the particles stored in sort-cell row w of a tile (storage range
+// [rb, re)) into shared memory with coalesced copies, and lane l then visits
+// the particles of its own cell (storage range [cb, ce)) in storage order,
+// summing their corner contributions in registers: the same order and the
+// same roundings as the slow path's visit_cell, so both paths give the same
+// bits.  Pass k stages storage slots [rb4 + kP, rb4 + (k+1)P) (rb4 = rb
+// rounded down to a multiple of 4, P a multiple of 4) of every field with
+// one cp.async.cg per 16-byte piece, and f(q, j) finds slot q at buf[.][j],
+// j = q - (rb4 + kP).  Every source array must start on a 16-byte boundary
+// and hold a multiple of 4 slots (the last piece may read up to 3 slots past
+// re).
 template <int NF, int P, class F>
 __device__ __forceinline__ void row_pass16(float (*buf)[P], const float* const (&src)[NF], int rb,
                                            int re, int cb, int ce, int lane, F&& f) {
