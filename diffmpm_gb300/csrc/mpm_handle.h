@@ -203,14 +203,15 @@ int sync(MpmHandle* h, cudaStream_t s);
 int read_ctl(MpmHandle* h, cudaStream_t s);
 int clear_status(MpmHandle* h, cudaStream_t s);
 int resort(MpmHandle* h, cudaStream_t s);
+// n steps from ctl->step (the tiles classified for the current sort).
 int launch_steps(MpmHandle* h, int n, cudaStream_t s);
 // Phase `phase` (0 nodal kinematics, 1 forces, 2 G2P) of step ctl->step + k.
 int launch_phase(MpmHandle* h, int phase, int k, cudaStream_t s);
-// Active / empty tile lists and their counts (nact, nemp) for the current
-// sort; call before a sequence of launch_phase (it waits for the counts, so
-// not inside a stream capture).
+// The step kernels' tile list and grids (step_tiles, nact, nemp) for the
+// current sort; call before a sequence of launch_phase (it waits for the
+// counts, so not inside a stream capture).
 int classify_tiles(MpmHandle* h, cudaStream_t s);
-// Graph-cache key of a step sequence: its length and the tile counts it launches for.
+// Graph-cache key of a step sequence: its length and the grids it launches.
 int64_t seq_key(const MpmHandle* h, int n);
 int check_status(MpmHandle* h, int& st);
 int take_snapshot(MpmHandle* h, cudaStream_t s);

@@ -36,15 +36,15 @@ cudaError_t launch_particle_kinematics(const StepConfig& c, const SimDev& S, con
 // ints of scratch.  Valid until the sort changes.
 cudaError_t launch_classify_tiles(const SimDev& S, const int4* tiles, int ntiles, int* flags, int4* active,
                                   int4* empty, int* counts, cudaStream_t s);
+// A single simulation launches its empty tiles apart only when it has at
+// least this many (mpm_set_empty_split changes it per handle).
+constexpr int EMPTY_SPLIT_MIN = 128;
 // Grid of a launch over `count` tiles of such a list: the count rounded up to
 // a multiple of TILE_GRID_QUANTUM (at most the list's length), so that the
 // captured graphs, keyed by their grids, serve the small changes of the
 // counts that re-sorts bring; the CTAs past the count read a (-1, ...) entry
 // and return.
 constexpr int TILE_GRID_QUANTUM = 64;
-// A single simulation launches its empty tiles apart only when it has at
-// least this many.
-constexpr int EMPTY_SPLIT_MIN = 128;
 inline int tile_grid(int count, int ntiles) {
     if (count <= 0) return 0;
     const int q = (count + TILE_GRID_QUANTUM - 1) / TILE_GRID_QUANTUM * TILE_GRID_QUANTUM;
