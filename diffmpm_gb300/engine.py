@@ -70,6 +70,9 @@ def _out_arg(out, dtype, count):
 
 
 _TUNING_KEYS = ("block_steps", "resort_every", "nk_ctas", "g2p_ctas", "forces_lpc", "ms_per_step")
+# The candidates mpm_batch_autotune tries; part of the cache key, so that a
+# result chosen among other candidates is not read back.
+_TUNING_SPACE = "nk_ctas 2,3; g2p_ctas 2,3; forces_lpc 0,1,2; block_steps 10,25,50,100,200; resort_every 1,2,4"
 
 
 def device_name(device=None) -> str:
@@ -238,7 +241,8 @@ class Simulation:
 
     def set_kernel_variant(self, nk_ctas=3, g2p_ctas=2, forces_lpc=0):
         """Kernel builds of the step (mpm_set_kernel_variant): the same results,
-        built for 2 or 3 resident CTAs per SM, and either forces path."""
+        built for 2 or 3 resident CTAs per SM, and any of the three forces
+        paths (0 row slots, 1 lane per cell, 2 staged row)."""
         self._ok(self._lib.mpm_set_kernel_variant(self._h, int(nk_ctas), int(g2p_ctas),
                                                   int(forces_lpc)))
 
@@ -551,11 +555,12 @@ class Batch:
     def config_key(self, trial_steps) -> str:
         """Key of this batch's configuration in the tuning cache: the GPU's
         name and a hash of every member's mesh, time step, scheme and
-        particle count, and of the trial length."""
+        particle count, of the trial length and of the candidate set."""
         import hashlib
         import json
         desc = [s.config() for s in self.sims]
-        h = hashlib.sha256(json.dumps({"members": desc, "trial_steps": int(trial_steps)},
+        h = hashlib.sha256(json.dumps({"members": desc, "trial_steps": int(trial_steps),
+                                       "candidates": _TUNING_SPACE},
                                       sort_keys=True).encode()).hexdigest()[:20]
         return f"{device_name()}|{h}"
 
