@@ -591,18 +591,25 @@ def run_ours(args, world, rank, local):
 
     ps = npart * K
     value = world * ps / (fa_ms / 1000.0)
-    # kernels of ours launched in the timed region (record + adjoint)
-    nseg = (K + ckpt - 1) // ckpt
-    # record: 3 step kernels per step; per block a descriptor copy, a counter
-    # advance, a snapshot copy and a status gather; a checkpoint copy per
-    # segment.  adjoint: per step the 3 step kernels, a descriptor copy, a
-    # counter advance, 2 tape copies, the argument table and 4 reverse passes;
-    # per segment a restore, a check and the block-map set-up.  re-sorts: 9
-    # kernels each (counted over the record and the forward alone: halved).
+    # kernels of ours launched in the timed region (record + adjoint), as
+    # the code issues them (a 100-step run of this configuration counts
+    # 3164; ncu's launch list of the same region 3166):
+    # record: 4 step kernels per step (empty tiles' nodes, nodal kinematics,
+    #   forces, G2P); per block a counter advance, the tile split and records
+    #   (4), the snapshot (chunk table + copy) and the status gather; per
+    #   segment a checkpoint (chunk table + copy);
+    # adjoint: per segment restore (2), status, epoch copy (2), tape tables
+    #   (3), tile split and records (4), status and the re-run check (2);
+    #   per re-run step 2 tape copies, the 4 step kernels and a counter
+    #   advance; per reverse step the argument table and 4 passes; per
+    #   simulation the seeds in and the gradient out (3); the final restore
+    #   and status (3);
+    # re-sorts: 21 kernels each (counted over the record and the forward
+    #   alone: halved).
     nblk = (K + block - 1) // block
-    launches = (3 * K + 4 * nblk + (nseg + 1)
-                + K * (3 + 2 + 2 + 1 + 4) + nseg * 6
-                + 9 * counters["resorts"] // 2)
+    launches = (4 * K + nblk * 8 + nseg_count(K, ckpt) * 2
+                + nseg_count(K, ckpt) * 15 + K * (2 + 4 + 1) + K * 5 + 3 * args.nsims + 3
+                + 21 * counters["resorts"] // 2)
     if rank == 0:
         print(json.dumps({
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
@@ -661,6 +668,11 @@ def run_ours_plain(args, world, rank, local):
             "data": "synthetic", "config": {"workload": plain["workload"], "mesh": plain["mesh"],
                                             "particles": plain["particles"]},
             "roofline": roof, "plain_scaleup": plain}), flush=True)
+
+
+def nseg_count(steps, ckpt):
+    """Checkpoint segments of a recording of `steps` steps."""
+    return (steps + ckpt - 1) // ckpt
 
 
 def main():
