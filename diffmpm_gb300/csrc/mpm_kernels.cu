@@ -688,7 +688,7 @@ __device__ __forceinline__ void nodal_update(const SimDev& S, int n, float t, fl
 // ---------------------------------------------------------------------------
 constexpr int NV_W = TILE_CX + 1;   // node tile of the R cells: [c0x, c0x+33) x [c0y, c0y+17)
 constexpr int NV_H = TILE_CY + 1;
-constexpr int K2_ROW_P = 64;    // particles of a row per pass (measured against 128 and 136)
+constexpr int K2_ROW_P = 64;    // particles of a row per pass (measured against 32, 128 and 136)
 
 // Fast paths of the forces kernel (StepConfig.forces_lpc):
 //   FM_ROW     a warp's lanes take consecutive particles of its cell row
