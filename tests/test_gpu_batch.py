@@ -273,20 +273,23 @@ def test_kernel_builds_and_resort_cadence_keep_results(built):
     assert rel(sim.read("velocity"), exp["velocity"].reshape(-1, 2)) < 1e-4
 
 
-@pytest.mark.parametrize("builder,kw", [
-    (workloads.plain_scaleup, dict(n=64, scheme="usf")),
-    (workloads.plain_scaleup, dict(n=64, scheme="usl")),
-    (workloads.mixed_large, dict(n=48)),
+@pytest.mark.parametrize("builder,kw,reinit", [
+    (workloads.plain_scaleup, dict(n=64, scheme="usf"), True),
+    (workloads.plain_scaleup, dict(n=64, scheme="usl"), True),
+    (workloads.mixed_large, dict(n=48), True),
+    (workloads.plain_scaleup, dict(n=64, scheme="usf"), False),
+    (workloads.plain_scaleup, dict(n=64, scheme="usl"), False),
 ])
-def test_forces_paths_give_the_same_bits(built, builder, kw):
-    """The forces kernel's three fast paths (particle per lane with slots,
-    lane per cell in global memory, lane per cell on a staged row) add every
-    cell's contributions in the same order: a single simulation ends bit for
-    bit in the same state with each."""
+def test_forces_paths_give_the_same_bits(built, builder, kw, reinit):
+    """The forces kernel's three fast paths (particle per lane with row
+    slots, lane per cell in global memory, particle per lane on a staged
+    row) add every cell's contributions in the same order: a single
+    simulation ends bit for bit in the same state with each, with the
+    per-step volume set-up and under solve semantics (persistent volume)."""
     out = []
     for lpc in (0, 1, 2):
         s, g, _ = builder(D, sim_steps=30, **kw)
-        sim = s.simulation(g, reinit=True)
+        sim = s.simulation(g, reinit=reinit)
         s._upload(sim)
         sim.initialize()
         sim.set_kernel_variant(3, 2, lpc)
