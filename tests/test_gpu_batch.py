@@ -133,8 +133,8 @@ def test_batch_rejects_mixed_configurations(built):
 @pytest.mark.parametrize("scheme", ["usf", "usl"])
 @pytest.mark.parametrize("reinit", [True, False])
 def test_batch_variants_equal_single_runs(built, scheme, reinit):
-    """Every batched kernel variant (scheme x volume set-up) gives each member
-    the bits of its single run."""
+    """Every batched kernel variant (scheme x volume set-up x forces path)
+    gives each member the bits of its single run."""
     specs = small_specs(k=3, seed=21)
     steps = 30
 
@@ -147,16 +147,20 @@ def test_batch_variants_equal_single_runs(built, scheme, reinit):
         sim.set_block_steps(10)
         return sim
 
-    members = [make(sp) for sp in specs]
-    batch = D.Batch(members)
-    batch.set_block_steps(10)
-    batch.step(steps)
-    for sp, sim in zip(specs, members):
-        alone = make(sp)
-        alone.step(steps)
-        for k in FIELDS:
-            assert np.array_equal(sim.read(k), alone.read(k)), (sp["side"], k)
-    batch.close()
+    alone = []
+    for sp in specs:
+        sim = make(sp)
+        sim.step(steps)
+        alone.append(state(sim))
+    for lpc in (0, 1, 2):
+        members = [make(sp) for sp in specs]
+        batch = D.Batch(members)
+        batch.set_tuning(block_steps=10, resort_every=1, forces_lpc=lpc)
+        batch.step(steps)
+        for sp, sim, ref in zip(specs, members, alone):
+            for k in FIELDS:
+                assert np.array_equal(sim.read(k), ref[k]), (lpc, sp["side"], k)
+        batch.close()
 
 
 def test_batch_with_tractions_equals_single_runs(built):
