@@ -572,25 +572,35 @@ int reverse_graph(MpmHandle* h, AdjointState* a, int len, cudaStream_t s) {
 }
 
 // Zero the adjoint arrays; particle (n, 2) seeds in original order -> lam[0..3]
-// in the storage order `pid`.
+// in the storage order `pid`.  The zeros are one memset of the permutation
+// scratch gathered into all NLAM arrays (two launches instead of NLAM).
+// With wait == false the caller synchronises the stream before it returns
+// (a host seed may be staged in h->stage: the copies and gathers are
+// stream-ordered, so the second seed's copy follows the first one's gather).
 int seed(MpmHandle* h, AdjointState* a, const float* dl_dloc, const float* dl_dvel,
-         const int* pid, int on_device, cudaStream_t s) {
-    for (float* p : a->lam) CK(h, cudaMemsetAsync(p, 0, sizeof(float) * h->np, s));
+         const int* pid, int on_device, cudaStream_t s, bool wait = true) {
+    const int np = (int)h->np;
+    CK(h, cudaMemsetAsync(a->lam_tmp, 0, sizeof(float) * NLAM * (size_t)np, s));
+    CK(h, launch_gather_in(a->d_lam, NLAM, pid, np, a->lam_tmp, s));
     const float* src[2] = {dl_dloc, dl_dvel};
     for (int k = 0; k < 2; ++k) {
         if (!src[k]) continue;
         const void* d = nullptr;
         TRY(to_device(h, src[k], sizeof(float) * 2 * h->np, on_device, s, &d));
-        CK(h, launch_gather_in(a->d_lam + 2 * k, 2, pid, (int)h->np, static_cast<const float*>(d), s));
-        TRY(sync(h, s));
+        CK(h, launch_gather_in(a->d_lam + 2 * k, 2, pid, np, static_cast<const float*>(d), s));
+        if (wait) TRY(sync(h, s));
     }
     return MPM_OK;
 }
 
 // Adjoint arrays lam[first..] in storage order `pid` -> particle (n, ncomp)
-// array in original order.
+// array in original order.  With wait == false the caller synchronises the
+// stream before it returns (a host destination is written by an
+// asynchronous copy out of h->stage, which the next emit reuses in stream
+// order; a larger stage is allocated only after cudaFree has waited for the
+// device).
 int emit(MpmHandle* h, AdjointState* a, float* dst, int first, int ncomp, const int* pid,
-         int on_device, cudaStream_t s) {
+         int on_device, cudaStream_t s, bool wait = true) {
     if (!dst) return MPM_OK;
     const size_t bytes = sizeof(float) * ncomp * h->np;
     float* d = dst;
@@ -600,15 +610,15 @@ int emit(MpmHandle* h, AdjointState* a, float* dst, int first, int ncomp, const 
     }
     CK(h, launch_scatter_out(a->d_lam + first, ncomp, pid, (int)h->np, d, s));
     if (!on_device) CK(h, cudaMemcpyAsync(dst, d, bytes, cudaMemcpyDeviceToHost, s));
-    return sync(h, s);
+    return wait ? sync(h, s) : MPM_OK;
 }
 
 int emit_all(MpmHandle* h, AdjointState* a, float* dl_dE, float* dl_dloc0, float* dl_dvel0,
-             int on_device, cudaStream_t s) {
+             int on_device, cudaStream_t s, bool wait = true) {
     const int* pid = a->epochs[0].pid;   // the order of the first checkpoint
-    TRY(emit(h, a, dl_dE, 9, 1, pid, on_device, s));
-    TRY(emit(h, a, dl_dloc0, 0, 2, pid, on_device, s));
-    return emit(h, a, dl_dvel0, 2, 2, pid, on_device, s);
+    TRY(emit(h, a, dl_dE, 9, 1, pid, on_device, s, wait));
+    TRY(emit(h, a, dl_dloc0, 0, 2, pid, on_device, s, wait));
+    return emit(h, a, dl_dvel0, 2, 2, pid, on_device, s, wait);
 }
 
 int check_supported(MpmHandle* h) {
@@ -962,11 +972,17 @@ int mpm_batch_adjoint(MpmBatch* b, const float* const* dl_dloc, const float* con
     int r = ensure_batch_adjoint(b, s);
     if (r != MPM_OK) return r;
     BatchAdjoint* x = b->badj;
+    for (int i = 0; i < n; ++i) BTRY(b, i, ensure_adjoint_buffers(b->sims[i], b->sims[i]->adj, K, s));
     for (int i = 0; i < n; ++i) {
         MpmHandle* h = b->sims[i];
-        BTRY(b, i, ensure_adjoint_buffers(h, h->adj, K, s));
-        BTRY(b, i, seed(h, h->adj, dl_dloc[i], dl_dvel ? dl_dvel[i] : nullptr, h->ps[h->pcur].pid,
-                        on_device, s));
+        // (no wait per simulation: the segment loop synchronises the stream,
+        // and a failure here waits for the seeds already in flight)
+        const int e = seed(h, h->adj, dl_dloc[i], dl_dvel ? dl_dvel[i] : nullptr, h->ps[h->pcur].pid,
+                           on_device, s, false);
+        if (e != MPM_OK) {
+            cudaStreamSynchronize(s);
+            return from_sim(b, i, e);
+        }
     }
     x->bases.assign(n, AdjStep{});
     std::vector<int> cur(n, -1);   // epoch whose pointers bases[i] holds
@@ -1042,15 +1058,20 @@ int mpm_batch_adjoint(MpmBatch* b, const float* const* dl_dloc, const float* con
     for (int i = 0; i < n && r == MPM_OK; ++i) {
         MpmHandle* h = b->sims[i];
         const int e = emit_all(h, h->adj, dl_dE ? dl_dE[i] : nullptr, dl_dloc0 ? dl_dloc0[i] : nullptr,
-                               dl_dvel0 ? dl_dvel0[i] : nullptr, on_device, s);
+                               dl_dvel0 ? dl_dvel0[i] : nullptr, on_device, s, false);
         if (e != MPM_OK) r = from_sim(b, i, e);
     }
-    // leave every simulation at the recorded end state
+    // leave every simulation at the recorded end state (read_statuses
+    // synchronises the stream: the gradients' copies are complete on return)
     std::vector<CopySeg> v;
     for (MpmHandle* h : b->sims) checkpoint_segments(h, h->adj->ck[nseg], false, v);
     int r2 = run_segments(b->sims[0], x->misc, v, s);
-    if (r2 == MPM_OK) r2 = read_statuses(b, s);
-    else r2 = from_sim(b, 0, r2);
+    if (r2 == MPM_OK) {
+        r2 = read_statuses(b, s);
+    } else {
+        cudaStreamSynchronize(s);
+        r2 = from_sim(b, 0, r2);
+    }
     if (r != MPM_OK) return r;
     return r2;
 }
