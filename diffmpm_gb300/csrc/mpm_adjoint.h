@@ -103,17 +103,4 @@ cudaError_t launch_rev_batch(const AdjStep* table, bool usl, bool trac, bool pvc
                              const int4* tiles, int ntiles, const int2* part_blocks, int n_part_blocks,
                              cudaStream_t s);
 
-// *mismatch += number of i < n with a[i] != b[i] bitwise (4-byte words).
-cudaError_t launch_count_mismatch(const void* a, const void* b, int n, int* mismatch,
-                                  cudaStream_t s);
-
-// dst[k][i] = src[k][i] for k < count (count <= 9), i < n.
-struct CopyJob {
-    const void* src[9];
-    void* dst[9];
-    int count;
-    int n;
-};
-cudaError_t launch_copy_f32(const CopyJob& j, cudaStream_t s);
-
 }  // namespace mpm

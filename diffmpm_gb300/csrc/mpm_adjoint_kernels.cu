@@ -848,22 +848,6 @@ k_rev_mass_momentum_batch(const AdjStep* __restrict__ table, const int2* __restr
         rev_mass_momentum_at<REINIT>(sA, (bm.y * ADJ_ITER + k) * PART_THREADS + threadIdx.x, x[k], y[k]);
 }
 
-__global__ void k_copy_f32(const __grid_constant__ CopyJob j) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= j.n) return;
-    #pragma unroll 1
-    for (int k = 0; k < j.count; ++k)
-        static_cast<float*>(j.dst[k])[i] = static_cast<const float*>(j.src[k])[i];
-}
-
-__global__ void k_count_mismatch(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b,
-                                 int n, int* __restrict__ mismatch) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool diff = i < n && a[i] != b[i];
-    const int c = __syncthreads_count(diff);
-    if (threadIdx.x == 0 && c) atomicAdd(mismatch, c);
-}
-
 // table[i] = bases[i] with the tape pointers moved to slot t.
 __global__ void k_adj_table(const AdjStep* __restrict__ bases, int n, int t,
                             AdjStep* __restrict__ table) {
@@ -980,20 +964,6 @@ cudaError_t launch_rev_batch(const AdjStep* table, bool usl, bool trac, bool pvc
         if (reinit) k_rev_mass_momentum_batch<true><<<npb, PART_THREADS, 0, s>>>(table, part_blocks);
         else k_rev_mass_momentum_batch<false><<<npb, PART_THREADS, 0, s>>>(table, part_blocks);
     }
-    return cudaGetLastError();
-}
-
-cudaError_t launch_count_mismatch(const void* a, const void* b, int n, int* mismatch,
-                                  cudaStream_t s) {
-    if (n <= 0) return cudaSuccess;
-    k_count_mismatch<<<blocks_for(n, 256), 256, 0, s>>>(static_cast<const uint32_t*>(a),
-                                                         static_cast<const uint32_t*>(b), n, mismatch);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_copy_f32(const CopyJob& j, cudaStream_t s) {
-    if (j.n <= 0 || j.count <= 0) return cudaSuccess;
-    k_copy_f32<<<blocks_for(j.n, 256), 256, 0, s>>>(j);
     return cudaGetLastError();
 }
 
