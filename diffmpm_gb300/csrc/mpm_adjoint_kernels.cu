@@ -57,23 +57,6 @@ __device__ __forceinline__ void visit_tape_cell(const AdjStep& A, int ci, int cj
     }
 }
 
-// Shape function and gradient of corner k alone, with the same roundings as
-// shape4 / dshape4.
-__device__ __forceinline__ void corner_shape(int k, float xi, float eta, float rx, float ry,
-                                             float& N, float& Gx, float& Gy) {
-    const bool px = k == 1 || k == 2, py = k >= 2;
-    const float sx = px ? fa(1.0f, xi) : fs(1.0f, xi);
-    const float sy = py ? fa(1.0f, eta) : fs(1.0f, eta);
-    N = fm(fm(0.25f, sx), sy);
-    Gx = fm(fm(px ? 0.25f : -0.25f, sy), rx);
-    Gy = fm(fm(py ? 0.25f : -0.25f, sx), ry);
-}
-
-// Cell (ci, cj) and corner index of the node (I, J) for the four cells around
-// it, in the fixed order c = 0..3: (I-1, J-1) corner 2, (I, J-1) corner 3,
-// (I-1, J) corner 1, (I, J) corner 0.
-__device__ __forceinline__ int corner_of(int c) { return c == 0 ? 2 : c == 1 ? 3 : c == 2 ? 1 : 0; }
-
 __device__ __forceinline__ void particle_cell(const AdjStep& A, float x, float y, int& ci, int& cj) {
     ci = min(max(locate_axis(x, A.hx, A.nx), 0), A.nx - 1);
     cj = min(max(locate_axis(y, A.hy, A.ny), 0), A.ny - 1);

@@ -16,36 +16,6 @@ __device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); 
 __device__ __forceinline__ float fs(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float fdv(float a, float b) { return __fdiv_rn(a, b); }
 
-// Paired float32 arithmetic (sm_100+ add/sub/mul.rn.f32x2): one instruction
-// rounds each half to nearest like __fadd_rn / __fsub_rn / __fmul_rn, so a
-// pair of independent operations gives the same bits as the two scalar
-// operations in half the issue slots.
-__device__ __forceinline__ unsigned long long pk2(float2 a) {
-    unsigned long long r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
-    return r;
-}
-__device__ __forceinline__ float2 upk2(unsigned long long r) {
-    float2 a;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
-    return a;
-}
-__device__ __forceinline__ float2 fa2(float2 a, float2 b) {
-    unsigned long long d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk2(a)), "l"(pk2(b)));
-    return upk2(d);
-}
-__device__ __forceinline__ float2 fs2(float2 a, float2 b) {
-    unsigned long long d;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk2(a)), "l"(pk2(b)));
-    return upk2(d);
-}
-__device__ __forceinline__ float2 fm2(float2 a, float2 b) {
-    unsigned long long d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk2(a)), "l"(pk2(b)));
-    return upk2(d);
-}
-
 // Asynchronous 4-byte global -> shared copies (cp.async), committed in groups.
 __device__ __forceinline__ void cp_async4(void* smem_dst, const void* gmem_src) {
     const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
