@@ -52,15 +52,6 @@ void dfree(MpmHandle* h, void* p) {
     cudaFree(p);
 }
 
-// Element volume by the reference's formula in float32 (diffmpm/element.py:903-909).
-float element_volume(float hx, float hy) {
-    const float a = hy, c = hy, b = hx, d = hx;
-    const float p = std::sqrt(a * a + b * b), q = p;
-    const float t = ((a * a + c * c) - b * b) - d * d;
-    const float x = (((4.0f * p) * p) * q) * q - t * t;
-    return 0.25f * std::sqrt(x);
-}
-
 void drop_graphs(MpmHandle* h) {
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
     h->graphs.clear();

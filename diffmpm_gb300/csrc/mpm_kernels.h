@@ -2,10 +2,21 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <cmath>
 #include <string>
 #include "mpm_types.h"
 
 namespace mpm {
+
+// Element volume of an hx x hy Quadrilateral4Node element by the reference's
+// formula in float32 (diffmpm/element.py:903-909), on the host.
+inline float element_volume(float hx, float hy) {
+    const float a = hy, c = hy, b = hx, d = hx;
+    const float p = std::sqrt(a * a + b * b), q = p;
+    const float t = ((a * a + c * c) - b * b) - d * d;
+    const float x = (((4.0f * p) * p) * q) * q - t * t;
+    return 0.25f * std::sqrt(x);
+}
 
 struct StepConfig {
     bool usl;          // scheme: USL (else USF)
@@ -15,12 +26,13 @@ struct StepConfig {
     // built for: 3 (40 registers a thread) or 2 (up to 64)
     int nk_ctas = 3;
     int g2p_ctas = 2;
-    // forces kernel: particle per lane with shared-memory slots (0) or lane
-    // per cell (1); the same bits either way
+    // forces kernel fast path: particle per lane with row slots (0), lane
+    // per cell (1), particle per lane on a staged row (2); the same bits
+    // every way
     int forces_lpc = 0;
 };
 
-// One explicit step = three launches over the tile list.  The descriptor is
+// One explicit step = three launches over the (active) tile list.  The descriptor is
 // passed by value (a __grid_constant__ kernel parameter), so a captured graph
 // holds the descriptor current at capture time.
 cudaError_t launch_nodal_kinematics(const StepConfig& c, const SimDev& S, const int4* tiles,

@@ -65,15 +65,6 @@ int counters(int** out) {
     return MPM_OK;
 }
 
-// Element volume by the reference's formula in float32 (diffmpm/element.py:903-909).
-float q4_volume(float hx, float hy) {
-    const float a = hy, c = hy, b = hx, d = hx;
-    const float p = std::sqrt(a * a + b * b), q = p;
-    const float t = ((a * a + c * c) - b * b) - d * d;
-    const float x = (((4.0f * p) * p) * q) * q - t * t;
-    return 0.25f * std::sqrt(x);
-}
-
 __global__ void k_noalloc_count(const float* __restrict__ loc, int n, int nx, int ny, float hx,
                                 float hy, int* __restrict__ count, int32_t* __restrict__ eid) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -128,7 +119,7 @@ extern "C" int mpm_volume_setup_noalloc(int nx, int ny, double hx, double hy, in
     const float fhx = (float)hx, fhy = (float)hy;
     const int blocks = (int)((n + 255) / 256);
     k_noalloc_count<<<blocks, 256, 0, s>>>(loc, (int)n, nx, ny, fhx, fhy, count, element_id);
-    k_noalloc_volume<<<blocks, 256, 0, s>>>((int)n, element_id, count, q4_volume(fhx, fhy),
+    k_noalloc_volume<<<blocks, 256, 0, s>>>((int)n, element_id, count, mpm::element_volume(fhx, fhy),
                                             density, volume, mass);
     e = cudaGetLastError();
     if (e != cudaSuccess) return noalloc_fail(MPM_ERR_CUDA, cudaGetErrorString(e));
