@@ -1,8 +1,9 @@
 // C ABI of the GB300 explicit MPM step (declared in include/diffmpm_gb300.h).
 //
 // Host driver.  mpm_step advances in blocks of `block_steps` steps.  Each block
-// is one CUDA graph of 3 launches per step (nodal kinematics, forces + nodal
-// update, G2P).  Before a block the particles are re-sorted by cell if any
+// is one CUDA graph of three launches per step over the active tiles (nodal
+// kinematics, forces + nodal update, G2P), plus the empty tiles' node kernel
+// when the handle launches those tiles apart.  Before a block the particles are re-sorted by cell if any
 // particle changed cell during the previous block; the block's start state is
 // snapshotted, and if a particle drifted two cells from its sort-cell inside
 // the block (the cell gathers only look one cell away) the block is rolled back

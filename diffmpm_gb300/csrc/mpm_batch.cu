@@ -1,15 +1,18 @@
 // Batches: many independent simulations advanced together, one launch per
-// phase per step for all of them.
+// phase per step for all of them (and one for all their empty tiles).
 //
 // A batch groups simulation handles of one configuration (scheme, volume
 // set-up, tractions) on one GPU.  Their tiles form one tile list, each tile
-// tagged with its simulation's index; the batched kernels read that
-// simulation's descriptor (the handle's device copy, which a re-sort updates in
-// place) and control block through two pointer tables, so a captured graph of
-// a step block stays valid across re-sorts.  Per block: re-sort the
-// simulations that drifted, snapshot all of them (one segmented copy), run the
-// block graph, gather every status word in one copy; a simulation whose
-// particle drifted two cells is rolled back and replayed alone, step by step.
+// tagged with its simulation's index.  Before every step block one kernel
+// classifies the tiles (active / empty) and writes a record per tile: the
+// tile, its simulation's control pointer, a copy of the simulation's
+// descriptor (the handle's device copy, which a re-sort updates in place) and
+// the tile's row starts; the batched kernels read their tile's record, so a
+// captured graph of a step block stays valid across re-sorts.  Per block:
+// re-sort the simulations that drifted, snapshot all of them (one segmented
+// copy), refresh the records, run the block graph, gather every status word
+// in one copy; a simulation whose particle drifted two cells is rolled back
+// and replayed alone, step by step.
 // No counterpart in the reference, which runs one simulation per solve.
 #include <cuda_runtime.h>
 
