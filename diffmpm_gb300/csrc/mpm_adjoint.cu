@@ -5,10 +5,12 @@
 // state at the start of every segment of K steps (and at the end), plus the
 // steps before which the particles were re-sorted.  mpm_adjoint walks the
 // segments backwards: it restores the segment's checkpoint, re-runs its K
-// steps one at a time while copying each step's start state and nodal results
-// into a tape (re-sorting at the recorded steps, so the storage order of every
-// step matches the recorded run), then runs the four reverse passes of
-// mpm_adjoint.h for each step from the last to the first.  The adjoint arrays
+// steps while copying each step's start state and nodal results into a tape
+// (re-sorting at the recorded steps, so the storage order of every step
+// matches the recorded run), then runs the four reverse passes of
+// mpm_adjoint.h for each step from the last to the first.  A segment without
+// a re-sort re-runs and reverses as two cached CUDA graphs; one with a
+// re-sort goes step by step.  The adjoint arrays
 // follow the storage order of the step being reversed; where a re-sort
 // separates two steps they are permuted through the original particle order,
 // and after a segment they are left in the order of its checkpoint, which is
@@ -16,7 +18,9 @@
 // to reproduce the recorded state bit for bit).
 // Memory: one checkpoint per segment (the particle state, cell starts and
 // persistent nodal velocity) and a tape of K steps (9 floats per particle, 7
-// per node and 1 byte per cell per step).
+// per node and 1 byte per cell per step; one more float per particle for the
+// volume under solve semantics and one for the volumetric strain of a run
+// with Newtonian particles).
 //
 // mpm_batch_record / mpm_batch_adjoint do the same for every simulation of a
 // batch in lockstep: each re-run step, tape copy and reverse pass is one
