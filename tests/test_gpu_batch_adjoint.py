@@ -62,3 +62,25 @@ def test_batch_adjoint_equals_single(built, K, block, scheme, traction, reinit):
     for k in range(len(MEMBERS)):
         for key in again[k]:
             assert np.array_equal(again[k][key], got[k][key])
+
+
+def test_batch_adjoint_device_seeds_equal_host_seeds(built):
+    """Seeds and gradients as CUDA tensors (the device path of the seeding and
+    of the gradient output, with no synchronisation per member) give the bits
+    of the host-array call."""
+    torch = pytest.importorskip("torch")
+    steps = 24
+    sims, infos = zip(*[member(m, steps) for m in MEMBERS])
+    batch = D.Batch(list(sims))
+    batch.set_block_steps(100)
+    batch.record(steps, 10)
+    W = [seeds(inf["np"], k) for k, inf in enumerate(infos)]
+    host = batch.adjoint([w[0] for w in W], [w[1] for w in W])
+    dev = torch.device("cuda:0")
+    got = batch.adjoint([torch.from_numpy(w[0]).to(dev) for w in W],
+                        [torch.from_numpy(w[1]).to(dev) for w in W])
+    torch.cuda.synchronize()
+    for k in range(len(MEMBERS)):
+        for key in host[k]:
+            assert got[k][key].is_cuda
+            assert np.array_equal(got[k][key].cpu().numpy(), host[k][key]), (k, key)
