@@ -146,3 +146,26 @@ def test_output_enqueue_takes_the_destination_size():
     text = HEADER.read_text()
     decl = re.search(r"int mpm_output_enqueue\(([^)]*)\)", text, re.S).group(1)
     assert "size_t host_dst_bytes" in decl
+
+
+def test_every_entry_point_refuses_a_null_handle(built):
+    """Each call on a handle or batch checks the handle before it touches it or
+    the device: a NULL handle gives MPM_ERR_INVALID (destroying NULL is a
+    no-op, and the last-error calls of NULL give the creation error)."""
+    from diffmpm_gb300 import _lib
+    lib = _lib.load()
+    no_op = {"mpm_destroy", "mpm_batch_destroy"}
+    checked = 0
+    for name, restype, argtypes in _lib.SIGNATURES:
+        if restype is not ctypes.c_int or not argtypes or argtypes[0] is not ctypes.c_void_p:
+            continue
+        if name in ("mpm_host_free",):     # a host pointer, not a handle
+            continue
+        args = [None if t is ctypes.c_void_p or hasattr(t, "contents") or t is ctypes.c_char_p
+                else t(0) for t in argtypes]
+        rc = getattr(lib, name)(*args)
+        assert rc == (0 if name in no_op else 1), (name, rc)
+        checked += 1
+    assert checked >= 30
+    assert isinstance(lib.mpm_last_error(None), bytes)
+    assert isinstance(lib.mpm_batch_last_error(None), bytes)
