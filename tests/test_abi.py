@@ -169,3 +169,49 @@ def test_every_entry_point_refuses_a_null_handle(built):
     assert checked >= 30
     assert isinstance(lib.mpm_last_error(None), bytes)
     assert isinstance(lib.mpm_batch_last_error(None), bytes)
+
+
+def test_c_program_links_and_sees_the_python_struct_layouts(built, tmp_path):
+    """A plain C99 program (the shape of a cgo / FFI binding) compiles against
+    the header, links against the library and calls it without a GPU; the
+    layouts it reports for the descriptor, material and tuning structs are
+    the ones the Python binding declares."""
+    import shutil
+    import subprocess
+    from diffmpm_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = {"MpmDesc": _lib.MpmDesc, "MpmMaterial": _lib.MpmMaterial, "MpmTuning": _lib.MpmTuning}
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include <string.h>',
+             '#include "diffmpm_gb300.h"', 'int main(void) {',
+             '    if (mpm_abi_version() != MPM_ABI_VERSION) return 2;',
+             '    if (mpm_step(NULL, 1, NULL) != MPM_ERR_INVALID) return 3;',
+             '    MpmDesc d; memset(&d, 0, sizeof d);',
+             '    d.ndim = 2; d.nelements[0] = d.nelements[1] = 2;',
+             '    d.el_len[0] = d.el_len[1] = 0.5; d.scheme = 7;',
+             '    MpmHandle* h = NULL;',
+             '    if (mpm_create(&d, &h) != MPM_ERR_INVALID || h != NULL) return 4;',
+             '    if (!strstr(mpm_last_error(NULL), "scheme")) return 5;']
+    for s in structs:
+        lines.append(f'    printf("{s} size %zu\\n", sizeof({s}));')
+        for f, _ in structs[s]._fields_:
+            lines.append(f'    printf("{s} {f} %zu\\n", offsetof({s}, {f}));')
+    lines += ['    return 0;', '}']
+    src = tmp_path / "binding.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "binding"
+    lib_dir = _lib.LIB_PATH.parent
+    subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", str(HEADER.parent), str(src),
+                    "-L", str(lib_dir), f"-l:{_lib.LIB_PATH.name}", f"-Wl,-rpath,{lib_dir}",
+                    "-o", str(exe)], check=True, capture_output=True)
+    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert run.returncode == 0, (run.returncode, run.stderr)
+    seen = {}
+    for line in run.stdout.splitlines():
+        s, f, v = line.split()
+        seen[(s, f)] = int(v)
+    for s, cls in structs.items():
+        assert seen[(s, "size")] == ctypes.sizeof(cls), s
+        for f, _ in cls._fields_:
+            assert seen[(s, f)] == getattr(cls, f).offset, (s, f)
