@@ -593,7 +593,8 @@ def run_ours(args, world, rank, local):
     value = world * ps / (fa_ms / 1000.0)
     # kernels of ours launched in the timed region (record + adjoint), as
     # the code issues them (a 100-step run of this configuration counts
-    # 3164; ncu's launch list of the same region 3166):
+    # 3676; ncu's launch list of the same region counted 3166 before the
+    # adjoint arrays were zeroed by one gather per simulation, 512 more):
     # record: 4 step kernels per step (empty tiles' nodes, nodal kinematics,
     #   forces, G2P); per block a counter advance, the tile split and records
     #   (4), the snapshot (chunk table + copy) and the status gather; per
@@ -602,13 +603,14 @@ def run_ours(args, world, rank, local):
     #   (3), tile split and records (4), status and the re-run check (2);
     #   per re-run step 2 tape copies, the 4 step kernels and a counter
     #   advance; per reverse step the argument table and 4 passes; per
-    #   simulation the seeds in and the gradient out (3); the final restore
-    #   and status (3);
+    #   simulation the read of its positions for the seeds, the zeroing and
+    #   seed gathers and the gradient out (4); the final restore and status
+    #   (3);
     # re-sorts: 21 kernels each (counted over the record and the forward
     #   alone: halved).
     nblk = (K + block - 1) // block
     launches = (4 * K + nblk * 8 + nseg_count(K, ckpt) * 2
-                + nseg_count(K, ckpt) * 15 + K * (2 + 4 + 1) + K * 5 + 3 * args.nsims + 3
+                + nseg_count(K, ckpt) * 15 + K * (2 + 4 + 1) + K * 5 + 4 * args.nsims + 3
                 + 21 * counters["resorts"] // 2)
     if rank == 0:
         print(json.dumps({
