@@ -9,10 +9,12 @@ forward agrees with the NumPy oracle run in float64, and the adjoint tests also
 check it against central finite differences of that oracle.
 
 Scope: Quadrilateral4Node mesh, USF or USL, the per-step volume set-up of
-``solve_jit`` (diffmpm/solver.py:81-85, 100-111), LinearElastic (per-particle E
-or the material's) and SimpleMaterial, gravity, velocity constraints,
-concentrated nodal forces.  Particle cell ids and counts are piecewise constant
-in the positions and carry no gradient; so are the flush-to-zero masks.
+``solve_jit`` (diffmpm/solver.py:81-85, 100-111) or the carried volume and
+constant mass of ``solve`` (``reinit=False``; diffmpm/solver.py:116-157,
+particle.py:324-327), LinearElastic (per-particle E or the material's) and
+SimpleMaterial, gravity, velocity constraints, concentrated nodal forces.
+Particle cell ids and counts are piecewise constant in the positions and
+carry no gradient; so are the flush-to-zero masks.
 
 The float32 form is the gradient oracle of the float32 GPU adjoint: the
 reference's flush |a| < 1e-12 -> 0 has zero derivative, and a quantity that is
@@ -38,7 +40,8 @@ def _flush(a):
 class TorchMPM:
     """One simulation: mesh, materials, boundary conditions; ``run`` advances a
     state dict of tensors ``x (N,2), v (N,2), sig (N,4: xx yy zz xy),
-    eps (N,3: xx yy xy), rho (N,), vsc (N,)`` and the persistent nodal velocity."""
+    eps (N,3: xx yy xy), rho (N,), vsc (N,)``, the persistent nodal velocity
+    ``nv`` and, for solve semantics, ``vol (N,)`` and ``mass (N,)``."""
 
     def __init__(self, nx, ny, hx, hy, dt, gravity, constraints, materials, mat_ids,
                  scheme="usf", velocity_update=False, nodal_forces=(), dtype=torch.float64):
@@ -145,14 +148,20 @@ class TorchMPM:
         dvol = self.dt * (c0 + c1)
         return torch.stack([r0, r1, r3], dim=1), dvol
 
-    def step(self, st, i, E=None):
-        """One solve_jit step (R0 + scheme), returns the new state dict."""
+    def step(self, st, i, E=None, reinit=True):
+        """One step, returns the new state dict: solve_jit's (R0 + scheme:
+        volume V_el / count and mass V rho set up again) or, with ``reinit``
+        False, solve's (the state's carried ``vol`` and constant ``mass``;
+        the volume update V' = V (1 + dvol) is carried to the next step)."""
         x, v, s, eps, rho, vsc, nvo = (st[k] for k in ("x", "v", "sig", "eps", "rho", "vsc", "nv"))
         e, ids, N, Gx, Gy, Gcx, Gcy = self._geometry(x)
-        with torch.no_grad():
-            cnt = torch.bincount(e, minlength=self.nx * self.ny).to(self.dtype)
-        V0 = self.vol_el / cnt[e]
-        m = V0 * rho
+        if reinit:
+            with torch.no_grad():
+                cnt = torch.bincount(e, minlength=self.nx * self.ny).to(self.dtype)
+            V0 = self.vol_el / cnt[e]
+            m = V0 * rho
+        else:
+            V0, m = st["vol"], st["mass"]
         M = self._scatter(ids, m[:, None] * N)
         P = _flush(self._scatter(ids, (N[:, :, None] * (m[:, None] * v)[:, None, :])))
         safeM = torch.where(M == 0, torch.ones_like(M), M)
@@ -167,6 +176,7 @@ class TorchMPM:
             eps = eps + sr * self.dt
             V = V0 * (1 + dvol)
             rho = rho / (1 + dvol)
+        Vend = V
         fx = Gx * s[:, 0:1] + Gy * s[:, 3:4]
         fy = Gy * s[:, 1:2] + Gx * s[:, 3:4]
         fint = self._scatter(ids, torch.stack([-V[:, None] * fx, -V[:, None] * fy], dim=2))
@@ -192,13 +202,16 @@ class TorchMPM:
             vsc = vsc + dvol
             s = self._stress(s, E, sr, dvol, vsc)
             eps = eps + sr * self.dt
+            Vend = V0 * (1 + dvol)
             rho = rho / (1 + dvol)
         out.update(x=xp, v=vp, sig=s, eps=eps, rho=rho, vsc=vsc, nv=vb)
+        if not reinit:
+            out.update(vol=Vend, mass=m)
         return out
 
-    def run(self, st, nsteps, E=None, start=0):
+    def run(self, st, nsteps, E=None, start=0, reinit=True):
         for i in range(start, start + nsteps):
-            st = self.step(st, i, E)
+            st = self.step(st, i, E, reinit)
         return st
 
 
@@ -227,5 +240,8 @@ def from_solver(solver, gravity, dtype=torch.float64):
         "rho": torch.tensor(ps.density.reshape(n), dtype=f),
         "vsc": torch.tensor(ps.volumetric_strain_centroid.reshape(n), dtype=f),
         "nv": torch.tensor(el.nodes.velocity.reshape(-1, 2), dtype=f),
+        # the set-up of the constructor (solver.py:81-85), which solve carries
+        "vol": torch.tensor(ps.volume.reshape(n), dtype=f),
+        "mass": torch.tensor(ps.mass.reshape(n), dtype=f),
     }
     return sim, st

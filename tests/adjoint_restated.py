@@ -7,7 +7,9 @@ check that this restatement equals torch autograd of ``oracle.mpm_torch``, so
 the derivation the CUDA kernels implement is pinned without a GPU; the GPU
 tests then compare the kernels with autograd directly.
 
-Scope as the CUDA adjoint: USF or USL, per-step volume set-up, LinearElastic
+Scope as the CUDA adjoint: USF or USL, the per-step volume set-up of
+solve_jit or the carried volume and constant mass of solve (``reinit``
+False: V' = V f carries its own adjoint, and the mass none), LinearElastic
 with a per-particle E, gravity, velocity constraints.  USL reverses in six
 passes (the order of the CUDA launches): U, the stress update after G2P
 (strain-rate adjoints from the updated nodal velocities vB); G, their
@@ -29,8 +31,10 @@ def flush(a):
 
 
 class Restated:
-    def __init__(self, tsim):
-        """``tsim``: an ``oracle.mpm_torch.TorchMPM`` (mesh, constraints, material)."""
+    def __init__(self, tsim, reinit=True):
+        """``tsim``: an ``oracle.mpm_torch.TorchMPM`` (mesh, constraints,
+        material); ``reinit``: solve_jit semantics (else solve's)."""
+        self.reinit = reinit
         self.nx, self.ny = tsim.nx, tsim.ny
         self.node_x = tsim.node_x.numpy()
         self.node_y = tsim.node_y.numpy()
@@ -111,13 +115,17 @@ class Restated:
     # ------------------------------------------------------------------
     def forward(self, st, E):
         """One step; returns (new state, tape).  State: x (n,2), v (n,2),
-        sig (n,4: xx yy zz xy), rho (n,), nv (nn,2)."""
+        sig (n,4: xx yy zz xy), rho (n,), nv (nn,2); under solve semantics
+        also vol (n,) and mass (n,)."""
         x, v, s, rho, nvo = st["x"], st["v"], st["sig"], st["rho"], st["nv"]
         G = self.geometry(x)
         ids, N, Gx, Gy = G["ids"], G["N"], G["Gx"], G["Gy"]
-        cnt = np.bincount(G["e"], minlength=self.nx * self.ny).astype(float)
-        V0 = self.vol_el / cnt[G["e"]]
-        m = V0 * rho
+        if self.reinit:
+            cnt = np.bincount(G["e"], minlength=self.nx * self.ny).astype(float)
+            V0 = self.vol_el / cnt[G["e"]]
+            m = V0 * rho
+        else:
+            V0, m = st["vol"], st["mass"]
         M = self.scatter(ids, m[:, None] * N)
         P = flush(self.scatter(ids, N[:, :, None] * (m[:, None] * v)[:, None, :]))
         safe = np.where(M == 0, 1.0, M)
@@ -131,6 +139,7 @@ class Restated:
             s2 = self.stress(s, E, r0, r1, r3)
             V = V0 * f
             rho2 = rho / f
+        Vend = V
         fx = Gx * s2[:, 0:1] + Gy * s2[:, 3:4]
         fy = Gy * s2[:, 1:2] + Gx * s2[:, 3:4]
         F = self.scatter(ids, np.stack([-V[:, None] * fx, -V[:, None] * fy], 2))
@@ -148,13 +157,18 @@ class Restated:
             f = 1 + self.dt * (c0 + c1)
             s2 = self.stress(s, E, r0, r1, r3)
             rho2 = rho / f
-        tape = dict(x=x, v=v, sig=s, rho=rho, M=M, vA=vA, vB=vB, aB=aB)
-        return dict(x=x2, v=v2, sig=s2, rho=rho2, nv=vB), tape
+            Vend = V0 * f
+        tape = dict(x=x, v=v, sig=s, rho=rho, M=M, vA=vA, vB=vB, aB=aB, vol=V0, mass=m)
+        out = dict(x=x2, v=v2, sig=s2, rho=rho2, nv=vB)
+        if not self.reinit:
+            out.update(vol=Vend, mass=m)
+        return out, tape
 
     # ------------------------------------------------------------------
     def reverse(self, tape, lam, E):
         """Reverse of one step: ``lam`` (x, v, sig, rho adjoints of the step's
-        end state) -> adjoints of its start state; returns (lam, dL/dE part)."""
+        end state, and vol under solve semantics) -> adjoints of its start
+        state; returns (lam, dL/dE part)."""
         dt = self.dt
         x, v, s, rho = tape["x"], tape["v"], tape["sig"], tape["rho"]
         M, vA, vB, aB = tape["M"], tape["vA"], tape["vB"], tape["aB"]
@@ -162,9 +176,8 @@ class Restated:
         ids, N, Gx, Gy = G["ids"], G["N"], G["Gx"], G["Gy"]
         live = (M != 0)[:, None]
         safe = np.where(M == 0, 1.0, M)
-        cnt = np.bincount(G["e"], minlength=self.nx * self.ny).astype(float)
-        V0 = self.vol_el / cnt[G["e"]]
-        m = V0 * rho
+        V0, m = tape["vol"], tape["mass"]
+        lvol = None if self.reinit else lam["vol"]
         sb = lam["sig"].copy()
         vBb = np.zeros((self.nn, 2))
         if self.usl:
@@ -174,6 +187,9 @@ class Restated:
             f = 1 + dt * (c0 + c1)
             r0b, r1b, r3b, Eb = self.stress_reverse(sb, E, r0, r1, r3)
             fb = -lam["rho"] * (rho / f) / f
+            if not self.reinit:   # V' = V0 f carries the volume to the next step
+                fb = fb + lvol * V0
+                lvol = lvol * f
             rhob = lam["rho"] / f
             c0b = np.where(c0 != 0, fb * dt, 0.0)
             c1b = np.where(c1 != 0, fb * dt, 0.0)
@@ -210,11 +226,17 @@ class Restated:
         Gxb = -V[:, None] * (fbx * s2[:, 0:1] + fby * s2[:, 3:4])
         Gyb = -V[:, None] * (fbx * s2[:, 3:4] + fby * s2[:, 1:2])
         if self.usl:
-            rhob = rhob + V0 * mb
+            if self.reinit:
+                rhob = rhob + V0 * mb
+            else:   # the forces used the start volume
+                lvol = lvol + Vb
         else:
             r0b, r1b, r3b, Eb = self.stress_reverse(sb, E, r0, r1, r3)
-            fb = Vb * V0 - lam["rho"] * (rho / f) / f
-            rhob = lam["rho"] / f + V0 * mb
+            Vt = Vb if self.reinit else Vb + lvol
+            fb = Vt * V0 - lam["rho"] * (rho / f) / f
+            rhob = lam["rho"] / f + (V0 * mb if self.reinit else 0.0)
+            if not self.reinit:
+                lvol = Vt * f
             c0b = np.where(c0 != 0, fb * dt, 0.0)
             c1b = np.where(c1 != 0, fb * dt, 0.0)
         vx, vy = nvr[ids, 0], nvr[ids, 1]
@@ -235,10 +257,14 @@ class Restated:
         mb2 = (N * t).sum(1)
         vb = (0.0 if self.vu else lam["v"]) + m[:, None] * np.stack(
             [(N * Qb[ids, 0]).sum(1), (N * Qb[ids, 1]).sum(1)], 1)
-        rhob = rhob + V0 * mb2
+        if self.reinit:   # m = V0 rho (under solve semantics a constant)
+            rhob = rhob + V0 * mb2
         xb[:, 0] += (m[:, None] * t * Gx).sum(1)
         xb[:, 1] += (m[:, None] * t * Gy).sum(1)
-        return dict(x=xb, v=vb, sig=sb, rho=rhob), Eb
+        out = dict(x=xb, v=vb, sig=sb, rho=rhob)
+        if not self.reinit:
+            out["vol"] = lvol
+        return out, Eb
 
     def gradient(self, st0, E, nsteps, dl_dx, dl_dv=None):
         """Forward ``nsteps`` steps keeping every tape, then the reverse sweep;
@@ -251,6 +277,8 @@ class Restated:
         dt = st0["x"].dtype
         lam = dict(x=np.array(dl_dx, dt), v=np.zeros((n, 2), dt) if dl_dv is None else np.array(dl_dv, dt),
                    sig=np.zeros((n, 4), dt), rho=np.zeros(n, dt))
+        if not self.reinit:
+            lam["vol"] = np.zeros(n, dt)
         gE = np.zeros(n, dt)
         for tp in reversed(tapes):
             lam, Eb = self.reverse(tp, lam, E)

@@ -70,3 +70,29 @@ def test_autograd_matches_finite_differences():
 
     fd = (loss(E0 + h * u) - loss(E0 - h * u)) / (2 * h)
     assert abs(fd - grad @ u) <= 1e-5 * abs(fd) + 1e-30, (fd, grad @ u)
+
+
+def _sheared(p):
+    return np.stack([1.5 + 0.4 * p[:, 0] + 0.8 * p[:, 1], 0.6 + 0.5 * p[:, 0] - 0.3 * p[:, 1]],
+                    axis=1)
+
+
+@pytest.mark.parametrize("scheme", ["usf", "usl"])
+def test_forward_matches_numpy_oracle_solve_semantics(scheme):
+    """``solve`` semantics (volume carried from step to step, mass constant):
+    the restatement's ``reinit=False`` step against the oracle's."""
+    dt = 1e-3 if scheme == "usf" else 2.5e-4
+    o, g, _ = workloads.differentiation(O, n=16, sim_steps=24, dt=dt, velocity=_sheared,
+                                        dtype=np.float64, scheme=scheme)
+    sim, st = T.from_solver(o, g)
+    for i in range(24):
+        o.step(i, g, reinit=False)
+        st = sim.step(st, i, E=torch.tensor(o.mesh.particles[0].youngs_modulus, dtype=torch.float64),
+                      reinit=False)
+    p = o.mesh.particles[0]
+    assert rel(st["x"].numpy(), p.loc.reshape(-1, 2)) < 1e-13
+    assert rel(st["v"].numpy(), p.velocity.reshape(-1, 2)) < 1e-12
+    assert rel(st["sig"].numpy(), p.stress.reshape(-1, 6)[:, :4]) < 1e-12
+    assert rel(st["rho"].numpy(), p.density.reshape(-1)) < 1e-13
+    assert rel(st["vol"].numpy(), p.volume.reshape(-1)) < 1e-13
+    assert np.array_equal(st["mass"].numpy(), p.mass.reshape(-1))
