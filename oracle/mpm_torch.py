@@ -12,9 +12,10 @@ Scope: Quadrilateral4Node mesh, USF or USL, the per-step volume set-up of
 ``solve_jit`` (diffmpm/solver.py:81-85, 100-111) or the carried volume and
 constant mass of ``solve`` (``reinit=False``; diffmpm/solver.py:116-157,
 particle.py:324-327), LinearElastic (per-particle E or the material's) and
-SimpleMaterial, gravity, velocity constraints, concentrated nodal forces.
-Particle cell ids and counts are piecewise constant in the positions and
-carry no gradient; so are the flush-to-zero masks.
+SimpleMaterial, gravity, velocity constraints, concentrated nodal forces and
+particle tractions (t = f(t) tau V / size at force time, mesh.py:60-77,
+particle.py:329-343).  Particle cell ids and counts are piecewise constant in
+the positions and carry no gradient; so are the flush-to-zero masks.
 
 The float32 form is the gradient oracle of the float32 GPU adjoint: the
 reference's flush |a| < 1e-12 -> 0 has zero derivative, and a quantity that is
@@ -41,10 +42,12 @@ class TorchMPM:
     """One simulation: mesh, materials, boundary conditions; ``run`` advances a
     state dict of tensors ``x (N,2), v (N,2), sig (N,4: xx yy zz xy),
     eps (N,3: xx yy xy), rho (N,), vsc (N,)``, the persistent nodal velocity
-    ``nv`` and, for solve semantics, ``vol (N,)`` and ``mass (N,)``."""
+    ``nv`` and, for solve semantics, ``vol (N,)``, ``mass (N,)`` and
+    ``psize (N,)`` (the particle size of the set-up, which tractions divide by)."""
 
     def __init__(self, nx, ny, hx, hy, dt, gravity, constraints, materials, mat_ids,
-                 scheme="usf", velocity_update=False, nodal_forces=(), dtype=torch.float64):
+                 scheme="usf", velocity_update=False, nodal_forces=(), tractions=(),
+                 dtype=torch.float64):
         self.nx, self.ny = nx, ny
         f = self.dtype = dtype
         self.hx, self.hy = float(hx), float(hy)
@@ -65,6 +68,9 @@ class TorchMPM:
             self.cval[ids, d] = float(vel)
         self.cnf = [(torch.as_tensor(np.asarray(ids, dtype=np.int64).reshape(-1)), d, float(F), fn)
                     for ids, d, F, fn in nodal_forces]
+        # particle tractions (pids, dir, tau, function or None for Unit)
+        self.tractions = [(torch.as_tensor(np.asarray(ids, dtype=np.int64).reshape(-1)), int(d),
+                           float(tau), fn) for ids, d, tau, fn in tractions]
         a, b, c = self.hy, self.hx, self.hy
         p = np.sqrt(a * a + b * b)
         t = a * a + c * c - b * b - b * b
@@ -182,6 +188,15 @@ class TorchMPM:
         fint = self._scatter(ids, torch.stack([-V[:, None] * fx, -V[:, None] * fy], dim=2))
         fext = self._scatter(ids, N[:, :, None] * (m[:, None] * self.g[None, :])[:, None, :])
         t = float(np.float64(i) * self.dt)
+        if self.tractions:
+            size0 = torch.sqrt(V0) if reinit else st["psize"]
+            n = x.shape[0]
+            cols = [torch.zeros(n, dtype=self.dtype), torch.zeros(n, dtype=self.dtype)]
+            for pids, d, tau, fn in self.tractions:
+                fval = 1.0 if fn is None else float(np.interp(t, fn.xvalues, fn.fxvalues))
+                cols[d] = cols[d].index_add(0, pids, (fval * tau) * V[pids] / size0[pids])
+            trac = torch.stack(cols, dim=1)
+            fext = fext + self._scatter(ids, N[:, :, None] * trac[:, None, :])
         for nid, d, F, fn in self.cnf:
             fval = 1.0 if fn is None else float(np.interp(t, fn.xvalues, fn.fxvalues))
             col = torch.zeros(self.nn, 2, dtype=self.dtype)
@@ -225,9 +240,12 @@ def from_solver(solver, gravity, dtype=torch.float64):
     cons = [(ids, c.dir, c.velocity) for ids, c in el.constraints]
     nfs = [(f.node_ids, f.dir, f.force, None if type(f.function).__name__ == "Unit" else f.function)
            for f in el.concentrated_nodal_forces]
+    trs = [(t.pids, t.dir, t.traction, None if type(t.function).__name__ == "Unit" else t.function)
+           for t in solver.mesh.particle_tractions]
     sim = TorchMPM(nx, ny, float(el.el_len[0]), float(el.el_len[1]), solver.dt, gravity, cons,
                    ps.materials, ps.material_ids, scheme=solver.scheme,
-                   velocity_update=solver.velocity_update, nodal_forces=nfs, dtype=dtype)
+                   velocity_update=solver.velocity_update, nodal_forces=nfs, tractions=trs,
+                   dtype=dtype)
     f = dtype
     n = len(ps)
     s = ps.stress.reshape(n, 6)
@@ -243,5 +261,6 @@ def from_solver(solver, gravity, dtype=torch.float64):
         # the set-up of the constructor (solver.py:81-85), which solve carries
         "vol": torch.tensor(ps.volume.reshape(n), dtype=f),
         "mass": torch.tensor(ps.mass.reshape(n), dtype=f),
+        "psize": torch.tensor(ps.size.reshape(n, -1)[:, 0], dtype=f),
     }
     return sim, st

@@ -10,7 +10,9 @@ tests then compare the kernels with autograd directly.
 Scope as the CUDA adjoint: USF or USL, the per-step volume set-up of
 solve_jit or the carried volume and constant mass of solve (``reinit``
 False: V' = V f carries its own adjoint, and the mass none), LinearElastic
-with a per-particle E, gravity, velocity constraints.  USL reverses in six
+with a per-particle E, gravity, velocity constraints, particle tractions
+(t = f(t) tau V / size: the shape-function adjoint gains F-bar . t and, where
+the volume at force time varies, the volume adjoint N F-bar . t / V).  USL reverses in six
 passes (the order of the CUDA launches): U, the stress update after G2P
 (strain-rate adjoints from the updated nodal velocities vB); G, their
 transposed gather to the nodes; then passes 1-4 as for USF, with the forces
@@ -48,6 +50,7 @@ class Restated:
         assert tsim.scheme in ("usf", "usl") and len(tsim.materials) == 1
         self.usl = tsim.scheme == "usl"
         self.c1, self.c2, self.c3 = le_coefficients(float(tsim.materials[0].properties["poisson_ratio"]))
+        self.tractions = [(pids.numpy(), d, tau, fn) for pids, d, tau, fn in tsim.tractions]
 
     def geometry(self, x):
         i = np.searchsorted(self.node_x, x[:, 0], side="right") - 1
@@ -113,7 +116,7 @@ class Restated:
         return out
 
     # ------------------------------------------------------------------
-    def forward(self, st, E):
+    def forward(self, st, E, i=0):
         """One step; returns (new state, tape).  State: x (n,2), v (n,2),
         sig (n,4: xx yy zz xy), rho (n,), nv (nn,2); under solve semantics
         also vol (n,) and mass (n,)."""
@@ -144,6 +147,15 @@ class Restated:
         fy = Gy * s2[:, 1:2] + Gx * s2[:, 3:4]
         F = self.scatter(ids, np.stack([-V[:, None] * fx, -V[:, None] * fy], 2))
         F = F + self.scatter(ids, N[:, :, None] * (m[:, None] * self.g[None, :])[:, None, :])
+        # particle tractions at step i: tq = sum f(t) tau / size, t = tq V
+        tq = np.zeros_like(x)
+        if self.tractions:
+            size0 = np.sqrt(V0) if self.reinit else st["psize"]
+            t = float(np.float64(i) * self.dt)
+            for pids, d, tau, fn in self.tractions:
+                fval = 1.0 if fn is None else float(np.interp(t, fn.xvalues, fn.fxvalues))
+                np.add.at(tq[:, d], pids, (fval * tau) / size0[pids])
+            F = F + self.scatter(ids, N[:, :, None] * (tq * V[:, None])[:, None, :])
         a = np.where((M == 0)[:, None], 0.0, F / safe[:, None])
         vB = vA + a * self.dt
         vB = flush(np.where(self.cmask, self.cval, vB))
@@ -158,10 +170,12 @@ class Restated:
             s2 = self.stress(s, E, r0, r1, r3)
             rho2 = rho / f
             Vend = V0 * f
-        tape = dict(x=x, v=v, sig=s, rho=rho, M=M, vA=vA, vB=vB, aB=aB, vol=V0, mass=m)
+        tape = dict(x=x, v=v, sig=s, rho=rho, M=M, vA=vA, vB=vB, aB=aB, vol=V0, mass=m, tq=tq)
         out = dict(x=x2, v=v2, sig=s2, rho=rho2, nv=vB)
         if not self.reinit:
             out.update(vol=Vend, mass=m)
+            if "psize" in st:
+                out["psize"] = st["psize"]
         return out, tape
 
     # ------------------------------------------------------------------
@@ -220,6 +234,11 @@ class Restated:
         fx = Gx * s2[:, 0:1] + Gy * s2[:, 3:4]
         fy = Gy * s2[:, 1:2] + Gx * s2[:, 3:4]
         Vb = -(fbx * fx + fby * fy).sum(1)
+        if self.tractions:   # F-bar . t, t = tq V
+            tq = tape["tq"]
+            tr = tq * V[:, None]
+            Nb = Nb + fbx * tr[:, None, 0] + fby * tr[:, None, 1]
+            Vb = Vb + (N * (fbx * tq[:, None, 0] + fby * tq[:, None, 1])).sum(1)
         sb[:, 0] -= V * (fbx * Gx).sum(1)
         sb[:, 1] -= V * (fby * Gy).sum(1)
         sb[:, 3] -= V * (fbx * Gy + fby * Gx).sum(1)
@@ -270,8 +289,8 @@ class Restated:
         """Forward ``nsteps`` steps keeping every tape, then the reverse sweep;
         returns dict(E, x, v) of gradients at the start."""
         tapes, st = [], dict(st0)
-        for _ in range(nsteps):
-            st, tp = self.forward(st, E)
+        for i in range(nsteps):
+            st, tp = self.forward(st, E, i)
             tapes.append(tp)
         n = st0["x"].shape[0]
         dt = st0["x"].dtype

@@ -96,3 +96,23 @@ def test_forward_matches_numpy_oracle_solve_semantics(scheme):
     assert rel(st["rho"].numpy(), p.density.reshape(-1)) < 1e-13
     assert rel(st["vol"].numpy(), p.volume.reshape(-1)) < 1e-13
     assert np.array_equal(st["mass"].numpy(), p.mass.reshape(-1))
+
+
+@pytest.mark.parametrize("reinit", [True, False])
+@pytest.mark.parametrize("scheme", ["usf", "usl"])
+def test_forward_matches_numpy_oracle_with_particle_traction(scheme, reinit):
+    """A ramped particle traction on the top layer (t = f(t) tau V / size at
+    force time) under both volume semantics."""
+    dt = 1e-3 if scheme == "usf" else 2.5e-4
+    o, g, _ = workloads.differentiation(O, n=16, sim_steps=24, dt=dt, velocity=_sheared,
+                                        dtype=np.float64, scheme=scheme, traction=(1, -2.0e3))
+    sim, st = T.from_solver(o, g)
+    assert sim.tractions
+    E = torch.tensor(o.mesh.particles[0].youngs_modulus, dtype=torch.float64)
+    for i in range(24):
+        o.step(i, g, reinit=reinit)
+        st = sim.step(st, i, E=E, reinit=reinit)
+    p = o.mesh.particles[0]
+    assert rel(st["x"].numpy(), p.loc.reshape(-1, 2)) < 1e-13
+    assert rel(st["v"].numpy(), p.velocity.reshape(-1, 2)) < 1e-12
+    assert rel(st["sig"].numpy(), p.stress.reshape(-1, 6)[:, :4]) < 1e-12
