@@ -236,7 +236,8 @@ def test_adjoint_directional_derivative_vs_finite_differences(built, scheme):
 def test_adjoint_with_particle_tractions(built, scheme):
     """A ramped traction on the top particle layer (both directions in turn):
     directional derivatives in E, x_0 and v_0 against central differences of
-    the float64 oracle (the torch restatement has no tractions)."""
+    the float64 NumPy oracle (the restated reverse passes with tractions are
+    pinned against autograd on the CPU, tests/test_adjoint_restated.py)."""
     dt = 1e-3 if scheme == "usf" else 2.5e-4
     for d, val in ((1, -2.0e3), (0, 1.5e3)):
         kw = dict(n=16, sim_steps=24, dt=dt, velocity=sheared, scheme=scheme, traction=(d, val))
