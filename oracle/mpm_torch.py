@@ -12,9 +12,10 @@ Scope: Quadrilateral4Node mesh, USF or USL, the per-step volume set-up of
 ``solve_jit`` (diffmpm/solver.py:81-85, 100-111) or the carried volume and
 constant mass of ``solve`` (``reinit=False``; diffmpm/solver.py:116-157,
 particle.py:324-327), LinearElastic (per-particle E or the material's) and
-SimpleMaterial, gravity, velocity constraints, concentrated nodal forces and
+SimpleMaterial, gravity, velocity constraints, concentrated nodal forces,
 particle tractions (t = f(t) tau V / size at force time, mesh.py:60-77,
-particle.py:329-343).  Particle cell ids and counts are piecewise constant in
+particle.py:329-343) and the build's particle velocity constraints (set after
+the particle velocity update, in list order).  Particle cell ids and counts are piecewise constant in
 the positions and carry no gradient; so are the flush-to-zero masks.
 
 The float32 form is the gradient oracle of the float32 GPU adjoint: the
@@ -47,7 +48,7 @@ class TorchMPM:
 
     def __init__(self, nx, ny, hx, hy, dt, gravity, constraints, materials, mat_ids,
                  scheme="usf", velocity_update=False, nodal_forces=(), tractions=(),
-                 dtype=torch.float64):
+                 particle_constraints=(), dtype=torch.float64):
         self.nx, self.ny = nx, ny
         f = self.dtype = dtype
         self.hx, self.hy = float(hx), float(hy)
@@ -71,6 +72,9 @@ class TorchMPM:
         # particle tractions (pids, dir, tau, function or None for Unit)
         self.tractions = [(torch.as_tensor(np.asarray(ids, dtype=np.int64).reshape(-1)), int(d),
                            float(tau), fn) for ids, d, tau, fn in tractions]
+        # particle velocity constraints (pids, dir, velocity), later entries win
+        self.pcons = [(torch.as_tensor(np.asarray(ids, dtype=np.int64).reshape(-1)), int(d),
+                       float(vel)) for ids, d, vel in particle_constraints]
         a, b, c = self.hy, self.hx, self.hy
         p = np.sqrt(a * a + b * b)
         t = a * a + c * c - b * b - b * b
@@ -211,6 +215,13 @@ class TorchMPM:
         vhat = (N[:, :, None] * vb[ids]).sum(1)
         ahat = (N[:, :, None] * a[ids]).sum(1)
         vp = vhat if self.velocity_update else v + ahat * self.dt
+        if self.pcons:
+            pmask = torch.zeros_like(vp, dtype=torch.bool)
+            pval = torch.zeros_like(vp)
+            for pids, d, vel in self.pcons:
+                pmask[pids, d] = True
+                pval[pids, d] = vel
+            vp = torch.where(pmask, pval, vp)
         xp = x + vhat * self.dt
         if self.scheme == "usl":
             sr, dvol = self._strain(st, Gx, Gy, ids, vb, Gcx, Gcy)
@@ -242,10 +253,11 @@ def from_solver(solver, gravity, dtype=torch.float64):
            for f in el.concentrated_nodal_forces]
     trs = [(t.pids, t.dir, t.traction, None if type(t.function).__name__ == "Unit" else t.function)
            for t in solver.mesh.particle_tractions]
+    pcs = [(c.pids, c.dir, c.velocity) for c in solver.mesh.particle_velocity_constraints]
     sim = TorchMPM(nx, ny, float(el.el_len[0]), float(el.el_len[1]), solver.dt, gravity, cons,
                    ps.materials, ps.material_ids, scheme=solver.scheme,
                    velocity_update=solver.velocity_update, nodal_forces=nfs, tractions=trs,
-                   dtype=dtype)
+                   particle_constraints=pcs, dtype=dtype)
     f = dtype
     n = len(ps)
     s = ps.stress.reshape(n, 6)

@@ -12,7 +12,9 @@ solve_jit or the carried volume and constant mass of solve (``reinit``
 False: V' = V f carries its own adjoint, and the mass none), LinearElastic
 with a per-particle E, gravity, velocity constraints, particle tractions
 (t = f(t) tau V / size: the shape-function adjoint gains F-bar . t and, where
-the volume at force time varies, the volume adjoint N F-bar . t / V).  USL reverses in six
+the volume at force time varies, the volume adjoint N F-bar . t / V), and
+particle velocity constraints (a held component of the end-of-step velocity
+is a constant: its adjoint is cleared before the reverse passes).  USL reverses in six
 passes (the order of the CUDA launches): U, the stress update after G2P
 (strain-rate adjoints from the updated nodal velocities vB); G, their
 transposed gather to the nodes; then passes 1-4 as for USF, with the forces
@@ -51,6 +53,7 @@ class Restated:
         self.usl = tsim.scheme == "usl"
         self.c1, self.c2, self.c3 = le_coefficients(float(tsim.materials[0].properties["poisson_ratio"]))
         self.tractions = [(pids.numpy(), d, tau, fn) for pids, d, tau, fn in tsim.tractions]
+        self.pcons = [(pids.numpy(), d, vel) for pids, d, vel in tsim.pcons]
 
     def geometry(self, x):
         i = np.searchsorted(self.node_x, x[:, 0], side="right") - 1
@@ -163,6 +166,10 @@ class Restated:
         vhat = (N[:, :, None] * vB[ids]).sum(1)
         ahat = (N[:, :, None] * aB[ids]).sum(1)
         v2 = vhat if self.vu else v + ahat * self.dt
+        if self.pcons:
+            v2 = v2.copy()
+            for pids, d, vel in self.pcons:
+                v2[pids, d] = vel
         x2 = x + vhat * self.dt
         if self.usl:   # stress update from vB at the start-of-step positions
             r0, r1, r3, c0, c1 = self.rates(G, vB)
@@ -192,6 +199,10 @@ class Restated:
         safe = np.where(M == 0, 1.0, M)
         V0, m = tape["vol"], tape["mass"]
         lvol = None if self.reinit else lam["vol"]
+        if self.pcons:   # held velocity components are constants after G2P
+            lam = dict(lam, v=lam["v"].copy())
+            for pids, d, _ in self.pcons:
+                lam["v"][pids, d] = 0.0
         sb = lam["sig"].copy()
         vBb = np.zeros((self.nn, 2))
         if self.usl:

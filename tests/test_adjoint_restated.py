@@ -138,3 +138,38 @@ def test_restated_reverse_matches_autograd_with_particle_traction(scheme, reinit
     assert rel(got["E"], Et.grad.numpy()) < 1e-9
     assert rel(got["x"], x0.grad.numpy()) < 1e-9
     assert rel(got["v"], v0.grad.numpy()) < 1e-9
+
+
+@pytest.mark.parametrize("scheme", ["usf", "usl"])
+@pytest.mark.parametrize("vu", [False, True])
+def test_restated_reverse_matches_autograd_with_particle_velocity_constraints(vu, scheme):
+    """Overlapping particle velocity constraints: the cleared end-of-step
+    velocity adjoints against autograd."""
+    dt = 1e-3 if scheme == "usf" else 2.5e-4
+    o, g, info = workloads.differentiation(O, n=16, sim_steps=24, dt=dt, velocity=sheared,
+                                           dtype=np.float64, scheme=scheme)
+    o.velocity_update = vu
+    o.mpm_scheme.velocity_update = vu
+    n = info["np"]
+    o.mesh.particle_velocity_constraints = [
+        O.ParticleVelocityConstraint(pset=0, pids=np.arange(0, n, 7), dir=0, velocity=1.6),
+        O.ParticleVelocityConstraint(pset=0, pids=np.arange(3, n, 5), dir=1, velocity=0.5)]
+    tsim, st0 = T.from_solver(o, g)
+    rng = np.random.Generator(np.random.PCG64(11))
+    W = rng.normal(size=(n, 2))
+    U = rng.normal(size=(n, 2))
+    E = info["E"]
+    r = Restated(tsim)
+    got, end = r.gradient({k: st0[k].numpy().copy() for k in ("x", "v", "sig", "rho", "nv")},
+                          E, 24, W, U)
+    Et = torch.tensor(E, requires_grad=True)
+    x0 = st0["x"].clone().requires_grad_(True)
+    v0 = st0["v"].clone().requires_grad_(True)
+    end_t = tsim.run(dict(st0, x=x0, v=v0), 24, E=Et)
+    assert rel(end["x"], end_t["x"].detach().numpy()) < 1e-13
+    assert rel(end["v"], end_t["v"].detach().numpy()) < 1e-12
+    L = (end_t["x"] * torch.tensor(W)).sum() + (end_t["v"] * torch.tensor(U)).sum()
+    L.backward()
+    assert rel(got["E"], Et.grad.numpy()) < 1e-9
+    assert rel(got["x"], x0.grad.numpy()) < 1e-9
+    assert rel(got["v"], v0.grad.numpy()) < 1e-9

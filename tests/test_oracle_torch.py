@@ -116,3 +116,26 @@ def test_forward_matches_numpy_oracle_with_particle_traction(scheme, reinit):
     assert rel(st["x"].numpy(), p.loc.reshape(-1, 2)) < 1e-13
     assert rel(st["v"].numpy(), p.velocity.reshape(-1, 2)) < 1e-12
     assert rel(st["sig"].numpy(), p.stress.reshape(-1, 6)[:, :4]) < 1e-12
+
+
+@pytest.mark.parametrize("scheme", ["usf", "usl"])
+def test_forward_matches_numpy_oracle_with_particle_velocity_constraints(scheme):
+    """Particle velocity constraints, overlapping, later entries winning."""
+    dt = 1e-3 if scheme == "usf" else 2.5e-4
+    o, g, info = workloads.differentiation(O, n=16, sim_steps=24, dt=dt, velocity=_sheared,
+                                           dtype=np.float64, scheme=scheme)
+    n = info["np"]
+    o.mesh.particle_velocity_constraints = [
+        O.ParticleVelocityConstraint(pset=0, pids=np.arange(0, n, 7), dir=0, velocity=1.6),
+        O.ParticleVelocityConstraint(pset=0, pids=np.arange(3, n, 5), dir=1, velocity=0.5),
+        O.ParticleVelocityConstraint(pset=0, pids=np.arange(0, n, 14), dir=0, velocity=-0.2)]
+    sim, st = T.from_solver(o, g)
+    assert len(sim.pcons) == 3
+    E = torch.tensor(o.mesh.particles[0].youngs_modulus, dtype=torch.float64)
+    for i in range(24):
+        o.step(i, g)
+        st = sim.step(st, i, E=E)
+    p = o.mesh.particles[0]
+    assert rel(st["x"].numpy(), p.loc.reshape(-1, 2)) < 1e-13
+    assert np.array_equal(st["v"].numpy()[::14, 0], np.full(len(range(0, n, 14)), -0.2))
+    assert rel(st["v"].numpy(), p.velocity.reshape(-1, 2)) < 1e-12
