@@ -12,7 +12,9 @@ Scope: Quadrilateral4Node mesh, USF or USL, the per-step volume set-up of
 ``solve_jit`` (diffmpm/solver.py:81-85, 100-111) or the carried volume and
 constant mass of ``solve`` (``reinit=False``; diffmpm/solver.py:116-157,
 particle.py:324-327), LinearElastic (per-particle E or the material's) and
-SimpleMaterial, gravity, velocity constraints, concentrated nodal forces,
+SimpleMaterial and the build's Newtonian material (total stress from the
+rate and the accumulated centroid volumetric strain), gravity, velocity
+constraints, concentrated nodal forces,
 particle tractions (t = f(t) tau V / size at force time, mesh.py:60-77,
 particle.py:329-343) and the build's particle velocity constraints (set after
 the particle velocity update, in list order).  Particle cell ids and counts are piecewise constant in
@@ -143,6 +145,17 @@ class TorchMPM:
                 Es = float(mat.properties["E"])
                 ds = torch.stack([d0[sel] * Es, d1[sel] * Es, torch.zeros_like(d0[sel]),
                                   d3[sel] * Es], dim=1)
+            elif kind == "Newtonian":
+                # the build's total stress: K vsc' I + 2 mu dev(rate), rate_zz = 0,
+                # s_xy = mu rate_xy (oracle.mpm_oracle.Newtonian)
+                K = float(mat.properties["bulk_modulus"])
+                mu = float(mat.properties["dynamic_viscosity"])
+                kv = K * vsc_new[sel]
+                t3 = (sr[sel, 0] + sr[sel, 1]) / 3.0
+                tot = torch.stack([kv + 2.0 * mu * (sr[sel, 0] - t3), kv + 2.0 * mu * (sr[sel, 1] - t3),
+                                   kv - 2.0 * mu * t3, mu * sr[sel, 2]], dim=1)
+                out = out.index_put((sel.nonzero()[:, 0],), tot)
+                continue
             else:
                 raise NotImplementedError(kind)
             out = out.index_put((sel.nonzero()[:, 0],), s[sel] + ds)

@@ -49,9 +49,26 @@ class Restated:
         self.vol_el = float(tsim.vol_el)
         self.nn = tsim.nn
         self.vu = bool(tsim.velocity_update)
-        assert tsim.scheme in ("usf", "usl") and len(tsim.materials) == 1
+        assert tsim.scheme in ("usf", "usl")
         self.usl = tsim.scheme == "usl"
-        self.c1, self.c2, self.c3 = le_coefficients(float(tsim.materials[0].properties["poisson_ratio"]))
+        # per-particle material parameters: LinearElastic coefficients of E, or
+        # the Newtonian bulk modulus and viscosity (a total-stress material)
+        mid = tsim.mat_ids.numpy()
+        n = len(mid)
+        self.c1, self.c2, self.c3 = np.zeros(n), np.zeros(n), np.zeros(n)
+        self.newt, self.K, self.mu = np.zeros(n, bool), np.zeros(n), np.zeros(n)
+        for k, mat in enumerate(tsim.materials):
+            sel = mid == k
+            kind = type(mat).__name__
+            if kind == "LinearElastic":
+                c = le_coefficients(float(mat.properties["poisson_ratio"]))
+                self.c1[sel], self.c2[sel], self.c3[sel] = c
+            elif kind == "Newtonian":
+                self.newt[sel] = True
+                self.K[sel] = float(mat.properties["bulk_modulus"])
+                self.mu[sel] = float(mat.properties["dynamic_viscosity"])
+            else:
+                raise NotImplementedError(kind)
         self.tractions = [(pids.numpy(), d, tau, fn) for pids, d, tau, fn in tsim.tractions]
         self.pcons = [(pids.numpy(), d, vel) for pids, d, vel in tsim.pcons]
 
@@ -85,13 +102,38 @@ class Restated:
         c1 = flush((G["Gcy"] * vy).sum(1))
         return r0, r1, r3, c0, c1
 
-    def stress(self, s, E, r0, r1, r3):
+    def stress(self, s, E, r0, r1, r3, vsc2):
+        """Elastic increment, or the Newtonian total stress from the rates and
+        the updated centroid volumetric strain vsc2."""
         dt = self.dt
         d0, d1, d3 = r0 * dt, r1 * dt, r3 * dt
         a1, a2, Gm = E * self.c1, E * self.c2, E * self.c3
-        return s + np.stack([a1 * d0 + a2 * d1, a2 * d0 + a1 * d1, a2 * d0 + a2 * d1, Gm * d3], 1)
+        out = s + np.stack([a1 * d0 + a2 * d1, a2 * d0 + a1 * d1, a2 * d0 + a2 * d1, Gm * d3], 1)
+        if self.newt.any():
+            kv, t3, mu = self.K * vsc2, (r0 + r1) / 3.0, self.mu
+            tot = np.stack([kv + 2 * mu * (r0 - t3), kv + 2 * mu * (r1 - t3), kv - 2 * mu * t3,
+                            mu * r3], 1)
+            out = np.where(self.newt[:, None], tot, out)
+        return out
 
     def stress_reverse(self, sb, E, r0, r1, r3):
+        """Rate adjoints (masked where a rate was flushed), dL/dE, the adjoint
+        of the updated centroid volumetric strain and the particles whose
+        stress is total (their start-of-step stress passes no adjoint)."""
+        r0b, r1b, r3b, Eb = self.stress_reverse_elastic(sb, E, r0, r1, r3)
+        vscb = np.zeros_like(r0)
+        if self.newt.any():
+            tr = sb[:, 0] + sb[:, 1] + sb[:, 2]
+            t3b = -2 * self.mu * tr
+            nw = self.newt
+            r0b = np.where(nw, np.where(r0 != 0, 2 * self.mu * sb[:, 0] + t3b / 3, 0.0), r0b)
+            r1b = np.where(nw, np.where(r1 != 0, 2 * self.mu * sb[:, 1] + t3b / 3, 0.0), r1b)
+            r3b = np.where(nw, np.where(r3 != 0, self.mu * sb[:, 3], 0.0), r3b)
+            Eb = np.where(nw, 0.0, Eb)
+            vscb = np.where(nw, self.K * tr, 0.0)
+        return r0b, r1b, r3b, Eb, vscb, self.newt
+
+    def stress_reverse_elastic(self, sb, E, r0, r1, r3):
         """D^T sb dt (masked where a rate was flushed) and dL/dE."""
         dt = self.dt
         d0, d1, d3 = r0 * dt, r1 * dt, r3 * dt
@@ -137,12 +179,14 @@ class Restated:
         safe = np.where(M == 0, 1.0, M)
         vA = np.where((M == 0)[:, None], nvo, P / safe[:, None])
         vA = np.where(self.cmask, self.cval, flush(vA))
+        vsc = st["vsc"] if "vsc" in st else np.zeros_like(rho)
         if self.usl:   # forces on the start-of-step stress and volume
             s2, V, rho2 = s, V0, rho
         else:
             r0, r1, r3, c0, c1 = self.rates(G, vA)
             f = 1 + self.dt * (c0 + c1)
-            s2 = self.stress(s, E, r0, r1, r3)
+            vsc2 = vsc + self.dt * (c0 + c1)
+            s2 = self.stress(s, E, r0, r1, r3, vsc2)
             V = V0 * f
             rho2 = rho / f
         Vend = V
@@ -174,11 +218,13 @@ class Restated:
         if self.usl:   # stress update from vB at the start-of-step positions
             r0, r1, r3, c0, c1 = self.rates(G, vB)
             f = 1 + self.dt * (c0 + c1)
-            s2 = self.stress(s, E, r0, r1, r3)
+            vsc2 = vsc + self.dt * (c0 + c1)
+            s2 = self.stress(s, E, r0, r1, r3, vsc2)
             rho2 = rho / f
             Vend = V0 * f
-        tape = dict(x=x, v=v, sig=s, rho=rho, M=M, vA=vA, vB=vB, aB=aB, vol=V0, mass=m, tq=tq)
-        out = dict(x=x2, v=v2, sig=s2, rho=rho2, nv=vB)
+        tape = dict(x=x, v=v, sig=s, rho=rho, M=M, vA=vA, vB=vB, aB=aB, vol=V0, mass=m, tq=tq,
+                    vsc=vsc)
+        out = dict(x=x2, v=v2, sig=s2, rho=rho2, nv=vB, vsc=vsc2)
         if not self.reinit:
             out.update(vol=Vend, mass=m)
             if "psize" in st:
@@ -187,9 +233,9 @@ class Restated:
 
     # ------------------------------------------------------------------
     def reverse(self, tape, lam, E):
-        """Reverse of one step: ``lam`` (x, v, sig, rho adjoints of the step's
-        end state, and vol under solve semantics) -> adjoints of its start
-        state; returns (lam, dL/dE part)."""
+        """Reverse of one step: ``lam`` (x, v, sig, rho and vsc adjoints of the
+        step's end state, and vol under solve semantics) -> adjoints of its
+        start state; returns (lam, dL/dE part)."""
         dt = self.dt
         x, v, s, rho = tape["x"], tape["v"], tape["sig"], tape["rho"]
         M, vA, vB, aB = tape["M"], tape["vA"], tape["vB"], tape["aB"]
@@ -199,6 +245,7 @@ class Restated:
         safe = np.where(M == 0, 1.0, M)
         V0, m = tape["vol"], tape["mass"]
         lvol = None if self.reinit else lam["vol"]
+        lvsc = lam["vsc"] if "vsc" in lam else np.zeros_like(rho)
         if self.pcons:   # held velocity components are constants after G2P
             lam = dict(lam, v=lam["v"].copy())
             for pids, d, _ in self.pcons:
@@ -210,8 +257,10 @@ class Restated:
             # through to the start of the step
             r0, r1, r3, c0, c1 = self.rates(G, vB)
             f = 1 + dt * (c0 + c1)
-            r0b, r1b, r3b, Eb = self.stress_reverse(sb, E, r0, r1, r3)
-            fb = -lam["rho"] * (rho / f) / f
+            r0b, r1b, r3b, Eb, vscb, total = self.stress_reverse(sb, E, r0, r1, r3)
+            sb[total] = 0.0   # a total stress: the start-of-step stress passes none
+            lvsc = lvsc + vscb   # vsc' = vsc + dvol
+            fb = -lam["rho"] * (rho / f) / f + lvsc
             if not self.reinit:   # V' = V0 f carries the volume to the next step
                 fb = fb + lvol * V0
                 lvol = lvol * f
@@ -234,7 +283,7 @@ class Restated:
         if not self.usl:
             r0, r1, r3, c0, c1 = self.rates(G, vA)
             f = 1 + dt * (c0 + c1)
-            s2 = self.stress(s, E, r0, r1, r3)
+            s2 = self.stress(s, E, r0, r1, r3, tape["vsc"] + dt * (c0 + c1))
             V = V0 * f
             nvr = vA
         fbx, fby = Fb[ids, 0], Fb[ids, 1]
@@ -261,9 +310,11 @@ class Restated:
             else:   # the forces used the start volume
                 lvol = lvol + Vb
         else:
-            r0b, r1b, r3b, Eb = self.stress_reverse(sb, E, r0, r1, r3)
+            r0b, r1b, r3b, Eb, vscb, total = self.stress_reverse(sb, E, r0, r1, r3)
+            sb[total] = 0.0   # a total stress: the start-of-step stress passes none
+            lvsc = lvsc + vscb   # vsc' = vsc + dvol
             Vt = Vb if self.reinit else Vb + lvol
-            fb = Vt * V0 - lam["rho"] * (rho / f) / f
+            fb = Vt * V0 - lam["rho"] * (rho / f) / f + lvsc
             rhob = lam["rho"] / f + (V0 * mb if self.reinit else 0.0)
             if not self.reinit:
                 lvol = Vt * f
@@ -291,7 +342,7 @@ class Restated:
             rhob = rhob + V0 * mb2
         xb[:, 0] += (m[:, None] * t * Gx).sum(1)
         xb[:, 1] += (m[:, None] * t * Gy).sum(1)
-        out = dict(x=xb, v=vb, sig=sb, rho=rhob)
+        out = dict(x=xb, v=vb, sig=sb, rho=rhob, vsc=lvsc)
         if not self.reinit:
             out["vol"] = lvol
         return out, Eb

@@ -22,6 +22,7 @@ import pytest
 import diffmpm_gb300 as D
 from diffmpm_gb300 import workloads
 from oracle import mpm_oracle as O
+from mixed_cases import mixed_newtonian
 
 torch = pytest.importorskip("torch")
 from oracle import mpm_torch as T  # noqa: E402
@@ -381,29 +382,6 @@ def test_adjoint_needs_a_current_recording(built):
     with pytest.raises(D.MpmError) as e:
         sim.adjoint(np.zeros((info["np"], 2), np.float32))
     assert e.value.code == 6
-
-
-def mixed_newtonian(api, scheme, dtype=np.float32, E=None):
-    """16 x 16 mesh, Gauss-point particles over [0.1, 0.9] x [0, 0.6]: LinearElastic
-    (per-particle E) left of x = 0.5, Newtonian right of it, sheared initial
-    velocity, bottom fixed, gravity; USF at dt 1e-3 or USL at dt 2.5e-4, 24 steps."""
-    n, h = 16, 1.0 / 16
-    pts = workloads.gauss_points(2, 14, 0, 10, h)
-    mid = (pts[:, 0] >= 0.5).astype(np.int32)
-    mats = [api.LinearElastic({"density": 1000, "youngs_modulus": 1e6, "poisson_ratio": 0.3}),
-            api.Newtonian({"density": 1000, "bulk_modulus": 5e5, "dynamic_viscosity": 50.0})]
-    E0 = workloads.youngs_field(len(pts), 41) if E is None else E
-    bottom = workloads._node_ids(n, n, lambda i, j: j == 0)
-    cons = [(bottom, api.Constraint(0, 0.0)), (bottom, api.Constraint(1, 0.0))]
-    dk = {} if dtype == np.float32 else {"dtype": dtype}   # (the oracle's float64 runs)
-    el = api.Quadrilateral4Node((n, n), n * n, (h, h), cons, **dk)
-    ps = api.Particles(pts.reshape(-1, 1, 2), mats, np.zeros(len(pts), dtype=np.int32),
-                       material_ids=mid, youngs_modulus=E0, **dk)
-    ps.velocity[:] = sheared(pts).reshape(-1, 1, 2)
-    mesh = api.Mesh2D({"particles": [ps], "elements": el, "particle_surface_traction": []})
-    dt = 1e-3 if scheme == "usf" else 2.5e-4
-    solver = api.MPMExplicit(mesh, dt, scheme=scheme, sim_steps=24)
-    return solver, np.array([0.0, -9.81]), E0
 
 
 @pytest.mark.parametrize("scheme", ["usf", "usl"])

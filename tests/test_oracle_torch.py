@@ -139,3 +139,22 @@ def test_forward_matches_numpy_oracle_with_particle_velocity_constraints(scheme)
     assert rel(st["x"].numpy(), p.loc.reshape(-1, 2)) < 1e-13
     assert np.array_equal(st["v"].numpy()[::14, 0], np.full(len(range(0, n, 14)), -0.2))
     assert rel(st["v"].numpy(), p.velocity.reshape(-1, 2)) < 1e-12
+
+
+@pytest.mark.parametrize("reinit", [True, False])
+@pytest.mark.parametrize("scheme", ["usf", "usl"])
+def test_forward_matches_numpy_oracle_elastic_newtonian_mixture(scheme, reinit):
+    """Elastic and Newtonian particles in one population (the Newtonian stress
+    is total, from the rate and the accumulated centroid volumetric strain)."""
+    from mixed_cases import mixed_newtonian
+    o, g, E0 = mixed_newtonian(O, scheme, dtype=np.float64)
+    sim, st = T.from_solver(o, g)
+    E = torch.tensor(E0, dtype=torch.float64)
+    for i in range(24):
+        o.step(i, g, reinit=reinit)
+        st = sim.step(st, i, E=E, reinit=reinit)
+    p = o.mesh.particles[0]
+    assert rel(st["x"].numpy(), p.loc.reshape(-1, 2)) < 1e-13
+    assert rel(st["v"].numpy(), p.velocity.reshape(-1, 2)) < 1e-12
+    assert rel(st["sig"].numpy(), p.stress.reshape(-1, 6)[:, :4]) < 1e-12
+    assert rel(st["vsc"].numpy(), p.volumetric_strain_centroid.reshape(-1)) < 1e-12
