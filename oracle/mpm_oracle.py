@@ -79,6 +79,7 @@ class Unit:
         self.id = id
 
     def value(self, x, dtype=np.float32):
+        """functions.py:21-22"""
         return _c(1.0, dtype)
 
 
@@ -96,6 +97,7 @@ class Linear:
         self.fxvalues = np.asarray(fxvalues, dtype=np.float64)
 
     def value(self, x, dtype=np.float32):
+        """``jnp.interp(x, xvalues, fxvalues)`` (functions.py:40-41)."""
         xp = self.xvalues.astype(dtype)
         fp = self.fxvalues.astype(dtype)
         x = _c(x, dtype)
@@ -166,10 +168,13 @@ class ParticleVelocityConstraint(NamedTuple):
 # Materials (material.py:8-131) and the build's Newtonian definition
 # ----------------------------------------------------------------------------
 class _Material:
+    """Material base (material.py:8-52)."""
+
     _props: tuple = ()
     incremental = True
 
     def validate_props(self, props):
+        """KeyError naming a missing property (material.py:45-51)."""
         for key in self._props:
             if key not in props:
                 raise KeyError(
@@ -217,6 +222,7 @@ class LinearElastic(_Material):
         self.coeffs = (a1, a2, G)
 
     def de(self, dtype):
+        """The 6 x 6 elastic tensor of material.py:94-111 in ``dtype``."""
         return self._de64.astype(dtype)
 
     def compute_stress(self, dstrain):
@@ -247,6 +253,7 @@ class SimpleMaterial(_Material):
         self.properties = material_properties
 
     def compute_stress(self, dstrain):
+        """material.py:130-131"""
         return dstrain * _c(self.properties["E"], dstrain.dtype)
 
     def __repr__(self):
@@ -463,6 +470,8 @@ class Quadrilateral4Node(_Element):
         return self.element_node_ids(np.asarray(id)).reshape(4, 1)
 
     def element_node_ids(self, e):
+        """Node ids of elements ``e``, counter-clockwise from the lower left
+        (element.py:692-723, vectorised)."""
         e = np.asarray(e, dtype=np.int64)
         nx = self.nx
         ll = (e // nx) * (nx + 1) + e % nx
@@ -598,6 +607,7 @@ class Linear1D(_Element):
         return self.element_node_ids(np.asarray(id)).reshape(2, 1)
 
     def element_node_ids(self, e):
+        """Node ids (e, e + 1) of elements ``e`` (element.py:414-428, vectorised)."""
         e = np.asarray(e, dtype=np.int64)
         return np.stack([e, e + 1], axis=-1)
 
@@ -625,6 +635,7 @@ class Linear1D(_Element):
         return g * (_c(1, g.dtype) / J)
 
     def dn_dx(self, xi, element_ids):
+        """``shapefn_grad`` (element.py:488-515) with J = (x1 - x0)/2 exactly."""
         e = np.asarray(element_ids, dtype=np.int64)
         rx = _c(2, self.dtype) / (self.node_x[e + 1] - self.node_x[e])
         g = self._shapefn_natural_grad(xi)
@@ -638,10 +649,12 @@ class Linear1D(_Element):
         return np.where(ok, i, -1).astype(np.int32)
 
     def set_particle_element_ids(self, particles):
+        """element.py:517-541"""
         particles.element_ids = self.locate(particles.loc)
 
     def compute_volume(self, *args):
-        """Element length x_{e+1} - x_e (see the class docstring)."""
+        """Element length x_{e+1} - x_e in place of element.py:543-546 (see
+        the class docstring)."""
         self.volume[:, 0, 0] = self.node_x[1:] - self.node_x[:-1]
 
     def compute_internal_force(self, particles):
@@ -900,10 +913,14 @@ class _MeshBase:
 
 
 class Mesh1D(_MeshBase):
+    """mesh.py:96-109"""
+
     ndim = 1
 
 
 class Mesh2D(_MeshBase):
+    """mesh.py:113-126"""
+
     ndim = 2
 
 
@@ -911,6 +928,8 @@ class Mesh2D(_MeshBase):
 # Schemes (scheme.py:13-133)
 # ----------------------------------------------------------------------------
 class _MPMScheme:
+    """Phase order of scheme.py:16-75."""
+
     def __init__(self, mesh, dt, velocity_update):
         self.mesh = mesh
         self.dt = dt
@@ -955,9 +974,11 @@ class USF(_MPMScheme):
     """Stress update first (scheme.py:70-104)."""
 
     def precompute_stress_strain(self):
+        """scheme.py:98-100"""
         self.compute_stress_strain()
 
     def postcompute_stress_strain(self):
+        """scheme.py:102-104"""
         pass
 
 
@@ -965,9 +986,11 @@ class USL(_MPMScheme):
     """Stress update last (scheme.py:107-133)."""
 
     def precompute_stress_strain(self):
+        """scheme.py:127-129"""
         pass
 
     def postcompute_stress_strain(self):
+        """scheme.py:131-133"""
         self.compute_stress_strain()
 
 
