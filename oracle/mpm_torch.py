@@ -289,3 +289,176 @@ def from_solver(solver, gravity, dtype=torch.float64):
         "psize": torch.tensor(ps.size.reshape(n, -1)[:, 0], dtype=f),
     }
     return sim, st
+
+
+class TorchLine:
+    """The 1-D step (Linear1D elements on [0, nx h], one particle set) in the
+    same terms as ``TorchMPM``, for autograd of the 1-D runs: the oracle's
+    Linear1D semantics (element volume = its length, strain rate
+    ``[dN/dx . v, 0, 0, 0, 0, 0]``, centroid rate equal to it), USF or USL,
+    solve_jit or solve semantics, LinearElastic and SimpleMaterial (material or
+    per-particle E) and the build's Newtonian, gravity, node constraints,
+    concentrated nodal forces and particle velocity constraints.  State:
+    ``x, v (N,), sig (N,4), rho, vsc (N,), nv (nn,)`` and, for solve semantics,
+    ``vol, mass (N,)``."""
+
+    def __init__(self, nx, h, dt, gravity, constraints, materials, mat_ids, scheme="usf",
+                 velocity_update=False, nodal_forces=(), particle_constraints=(), dtype=torch.float64):
+        self.nx, self.dtype = nx, dtype
+        self.node_x = torch.arange(nx + 1, dtype=dtype) * torch.tensor(float(h), dtype=dtype)
+        self.dt = float(dt)
+        self.g = float(np.asarray(gravity, float).reshape(-1)[0])
+        self.nn = nx + 1
+        self.cmask = torch.zeros(self.nn, dtype=torch.bool)
+        self.cval = torch.zeros(self.nn, dtype=dtype)
+        for ids, d, vel in constraints:
+            ids = torch.as_tensor(np.asarray(ids, dtype=np.int64).reshape(-1))
+            self.cmask[ids] = True
+            self.cval[ids] = float(vel)
+        self.cnf = [(torch.as_tensor(np.asarray(ids, dtype=np.int64).reshape(-1)), float(F), fn)
+                    for ids, d, F, fn in nodal_forces]
+        self.pcons = [(torch.as_tensor(np.asarray(ids, dtype=np.int64).reshape(-1)), float(vel))
+                      for ids, d, vel in particle_constraints]
+        self.scheme, self.velocity_update = scheme, velocity_update
+        self.mat_ids = torch.as_tensor(np.asarray(mat_ids, dtype=np.int64))
+        self.materials = materials
+
+    def _geometry(self, x):
+        with torch.no_grad():
+            e = torch.searchsorted(self.node_x, x.contiguous(), right=True) - 1
+        if ((e < 0) | (e >= self.nx)).any():
+            raise ValueError("particle outside the mesh")
+        x0, x1 = self.node_x[e], self.node_x[e + 1]
+        r = 2.0 / (x1 - x0)
+        xi = (x - (x0 + x1) / 2) * r
+        N = torch.stack([0.5 * (1 - xi), 0.5 * (1 + xi)], dim=1)
+        dN = torch.stack([-0.5 * r, 0.5 * r], dim=1)
+        return e, torch.stack([e, e + 1], dim=1), N, dN, x1 - x0
+
+    def _scatter(self, ids, vals):
+        return torch.zeros(self.nn, dtype=vals.dtype).index_add(0, ids.reshape(-1), vals.reshape(-1))
+
+    def _stress(self, s, E, r, vsc_new):
+        dt = self.dt
+        d0 = r * dt
+        out = s.clone()
+        for k, mat in enumerate(self.materials):
+            sel = self.mat_ids == k
+            if not bool(sel.any()):
+                continue
+            kind = type(mat).__name__
+            if kind == "LinearElastic":
+                c1, c2, _ = le_coefficients(float(mat.properties["poisson_ratio"]))
+                Ek = E[sel] if E is not None else torch.full((int(sel.sum()),),
+                                                             float(mat.properties["youngs_modulus"]),
+                                                             dtype=self.dtype)
+                a1, a2 = Ek * c1, Ek * c2
+                new = s[sel] + torch.stack([a1 * d0[sel], a2 * d0[sel], a2 * d0[sel],
+                                            torch.zeros_like(d0[sel])], dim=1)
+            elif kind == "SimpleMaterial":
+                Es = E[sel] if E is not None else torch.full((int(sel.sum()),), float(mat.properties["E"]),
+                                                             dtype=self.dtype)
+                z = torch.zeros_like(d0[sel])
+                new = s[sel] + torch.stack([Es * d0[sel], z, z, z], dim=1)
+            elif kind == "Newtonian":
+                K = float(mat.properties["bulk_modulus"])
+                mu = float(mat.properties["dynamic_viscosity"])
+                kv, t3 = K * vsc_new[sel], r[sel] / 3.0
+                new = torch.stack([kv + 2.0 * mu * (r[sel] - t3), kv - 2.0 * mu * t3,
+                                   kv - 2.0 * mu * t3, torch.zeros_like(kv)], dim=1)
+            else:
+                raise NotImplementedError(kind)
+            out = out.index_put((sel.nonzero()[:, 0],), new)
+        return out
+
+    def step(self, st, i, E=None, reinit=True):
+        x, v, s, rho, vsc, nvo = (st[k] for k in ("x", "v", "sig", "rho", "vsc", "nv"))
+        e, ids, N, dN, length = self._geometry(x)
+        if reinit:
+            with torch.no_grad():
+                cnt = torch.bincount(e, minlength=self.nx).to(self.dtype)
+            V0 = length / cnt[e]
+            m = V0 * rho
+        else:
+            V0, m = st["vol"], st["mass"]
+        M = self._scatter(ids, m[:, None] * N)
+        P = _flush(self._scatter(ids, N * (m * v)[:, None]))
+        safeM = torch.where(M == 0, torch.ones_like(M), M)
+        vA = _flush(torch.where(M == 0, nvo, P / safeM))
+        vA = torch.where(self.cmask, self.cval, vA)
+
+        def rate(nvel):
+            return _flush((dN * nvel[ids]).sum(1))
+
+        V = V0
+        Vend = V0
+        if self.scheme == "usf":
+            r = rate(vA)
+            dvol = self.dt * r
+            vsc = vsc + dvol
+            s = self._stress(s, E, r, vsc)
+            V = V0 * (1 + dvol)
+            Vend = V
+            rho = rho / (1 + dvol)
+        fint = self._scatter(ids, (-V * s[:, 0])[:, None] * dN)
+        fext = self._scatter(ids, N * (m * self.g)[:, None])
+        t = float(np.float64(i) * self.dt)
+        for nid, F, fn in self.cnf:
+            fval = 1.0 if fn is None else float(np.interp(t, fn.xvalues, fn.fxvalues))
+            fext = fext + torch.zeros(self.nn, dtype=self.dtype).index_add(
+                0, nid, torch.full((nid.numel(),), fval * F, dtype=self.dtype))
+        tot = fint + fext
+        a = torch.where(M == 0, torch.zeros_like(tot), tot / safeM)
+        vb = vA + a * self.dt
+        vb = _flush(torch.where(self.cmask, self.cval, vb))
+        a = _flush(torch.where(self.cmask, torch.zeros_like(a), a))
+        vhat = (N * vb[ids]).sum(1)
+        ahat = (N * a[ids]).sum(1)
+        vp = vhat if self.velocity_update else v + ahat * self.dt
+        for pids, vel in self.pcons:
+            vp = vp.index_put((pids,), torch.full((pids.numel(),), vel, dtype=self.dtype))
+        xp = x + vhat * self.dt
+        if self.scheme == "usl":
+            r = rate(vb)
+            dvol = self.dt * r
+            vsc = vsc + dvol
+            s = self._stress(s, E, r, vsc)
+            Vend = V0 * (1 + dvol)
+            rho = rho / (1 + dvol)
+        out = dict(st, x=xp, v=vp, sig=s, rho=rho, vsc=vsc, nv=vb)
+        if not reinit:
+            out.update(vol=Vend, mass=m)
+        return out
+
+    def run(self, st, nsteps, E=None, start=0, reinit=True):
+        for i in range(start, start + nsteps):
+            st = self.step(st, i, E, reinit)
+        return st
+
+
+def from_line_solver(solver, gravity, dtype=torch.float64):
+    """TorchLine and initial state from an ``oracle.mpm_oracle`` MPMExplicit
+    on a Linear1D mesh with one particle set."""
+    el = solver.mesh.elements
+    ps = solver.mesh.particles[0]
+    cons = [(ids, c.dir, c.velocity) for ids, c in el.constraints]
+    nfs = [(f.node_ids, f.dir, f.force, None if type(f.function).__name__ == "Unit" else f.function)
+           for f in el.concentrated_nodal_forces]
+    pcs = [(c.pids, c.dir, c.velocity) for c in solver.mesh.particle_velocity_constraints]
+    sim = TorchLine(el.nx, float(el.el_len), solver.dt, gravity, cons, ps.materials, ps.material_ids,
+                    scheme=solver.scheme, velocity_update=solver.velocity_update, nodal_forces=nfs,
+                    particle_constraints=pcs, dtype=dtype)
+    n = len(ps)
+    s = ps.stress.reshape(n, 6)
+    f = dtype
+    st = {
+        "x": torch.tensor(ps.loc.reshape(n), dtype=f),
+        "v": torch.tensor(ps.velocity.reshape(n), dtype=f),
+        "sig": torch.tensor(np.stack([s[:, 0], s[:, 1], s[:, 2], s[:, 3]], 1), dtype=f),
+        "rho": torch.tensor(ps.density.reshape(n), dtype=f),
+        "vsc": torch.tensor(ps.volumetric_strain_centroid.reshape(n), dtype=f),
+        "nv": torch.tensor(el.nodes.velocity.reshape(-1), dtype=f),
+        "vol": torch.tensor(ps.volume.reshape(n), dtype=f),
+        "mass": torch.tensor(ps.mass.reshape(n), dtype=f),
+    }
+    return sim, st
