@@ -215,3 +215,25 @@ def test_c_program_links_and_sees_the_python_struct_layouts(built, tmp_path):
         assert seen[(s, "size")] == ctypes.sizeof(cls), s
         for f, _ in cls._fields_:
             assert seen[(s, f)] == getattr(cls, f).offset, (s, f)
+
+
+def test_tuning_cache_file_helpers(tmp_path, monkeypatch):
+    """The autotuner's JSON cache on the host: the path follows
+    $DIFFMPM_GB300_TUNING_CACHE, writes merge keys and replace the file
+    whole, and an unreadable or corrupt file reads as empty."""
+    from diffmpm_gb300 import engine
+    path = tmp_path / "sub" / "tuning.json"
+    monkeypatch.setenv("DIFFMPM_GB300_TUNING_CACHE", str(path))
+    assert engine.tuning_cache_path() == path
+    assert engine._read_tuning_cache(path) == {}
+    a = {"block_steps": 100, "resort_every": 1, "nk_ctas": 3, "g2p_ctas": 2, "forces_lpc": 0,
+         "ms_per_step": 1.2}
+    engine._write_tuning_cache(path, "gpu|k1", a)
+    engine._write_tuning_cache(path, "gpu|k2", dict(a, block_steps=50))
+    got = engine._read_tuning_cache(path)
+    assert got == {"gpu|k1": a, "gpu|k2": dict(a, block_steps=50)}
+    assert [p.name for p in path.parent.iterdir()] == ["tuning.json"]   # no temporaries left
+    path.write_text("{not json")
+    assert engine._read_tuning_cache(path) == {}
+    # the candidate set is part of every key's hash input
+    assert "forces_lpc 0,1,2" in engine._TUNING_SPACE
