@@ -32,6 +32,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -68,6 +69,9 @@ def parse():
                     help="steps of the 4096^2 elastic + Newtonian workload (0 skips it)")
     ap.add_argument("--diff-steps", type=int, default=2000,
                     help="steps of the differentiation workload (0 skips it)")
+    ap.add_argument("--cpu-configs", action="store_true",
+                    help="CPU only: time the float32 restatements of the reference step on a "
+                         "bounded sample of each configuration, one core, and print one JSON line")
     return ap.parse_args()
 
 
@@ -271,6 +275,49 @@ def run_reference(args, world, rank):
                          "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
+
+
+def run_cpu_configs():
+    """Per-configuration CPU figures beside the GPU ones: the float32 NumPy
+    restatement of the reference step (forward, ``np.add.at`` scatters in
+    particle order) on a bounded sample of steps of each configuration at its
+    full size, and the float32 torch restatement's forward + autograd adjoint
+    w.r.t. the per-particle E on the differentiation configuration; one
+    process on one core."""
+    import torch
+    from diffmpm_gb300 import workloads
+    from oracle import mpm_oracle as O
+    from oracle import mpm_torch as T
+    torch.set_num_threads(1)
+    out = {}
+
+    def forward(name, builder, steps, **kw):
+        solver, g, info = builder(O, sim_steps=steps, **kw)
+        t0 = time.perf_counter()
+        for i in range(steps):
+            solver.step(i, g)
+        sec = time.perf_counter() - t0
+        out[name] = {"what": "forward, NumPy float32", "particles": info["np"], "steps": steps,
+                     "seconds": sec, "value": info["np"] * steps / sec}
+
+    forward("plain_small_10x10_usf", workloads.plain_small, 1000)
+    forward("plain_scaleup_1024_usf", workloads.plain_scaleup, 2, n=1024, scheme="usf")
+    forward("plain_scaleup_1024_usl", workloads.plain_scaleup, 2, n=1024, scheme="usl")
+    forward("mixed_large_4096_usl", workloads.mixed_large, 1)
+    forward("differentiation_256_usf", workloads.differentiation, 20)
+    steps = 20
+    o, g, info = workloads.differentiation(O, sim_steps=steps)
+    sim, st0 = T.from_solver(o, g, dtype=torch.float32)
+    t0 = time.perf_counter()
+    E = torch.tensor(info["E"], dtype=torch.float32, requires_grad=True)
+    end = sim.run(dict(st0), steps, E=E)
+    ((end["x"] - st0["x"] - 1e-4) ** 2).sum(1).mean().backward()
+    sec = time.perf_counter() - t0
+    out["differentiation_256_usf_fwd_adjoint"] = {
+        "what": "forward + autograd adjoint w.r.t. E, torch float32", "particles": info["np"],
+        "steps": steps, "seconds": sec, "value": info["np"] * steps / sec}
+    print(json.dumps({"impl": "cpu-configs", "unit": UNIT, "cores": 1, "kind": "port",
+                      "host": platform.machine(), "configs": out}), flush=True)
 
 
 # ---------------------------------------------------------------------------
@@ -679,6 +726,9 @@ def nseg_count(steps, ckpt):
 
 def main():
     args = parse()
+    if args.cpu_configs:
+        run_cpu_configs()
+        return
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, world, rank)
