@@ -142,7 +142,9 @@ class TorchMPM:
                 ds = torch.stack([a1 * d0[sel] + a2 * d1[sel], a2 * d0[sel] + a1 * d1[sel],
                                   a2 * d0[sel] + a2 * d1[sel], G * d3[sel]], dim=1)
             elif kind == "SimpleMaterial":
-                Es = float(mat.properties["E"])
+                # a per-particle E replaces the material's (as in the oracle)
+                Es = E[sel] if E is not None else torch.full((int(sel.sum()),), float(mat.properties["E"]),
+                                                             dtype=self.dtype)
                 ds = torch.stack([d0[sel] * Es, d1[sel] * Es, torch.zeros_like(d0[sel]),
                                   d3[sel] * Es], dim=1)
             elif kind == "Newtonian":

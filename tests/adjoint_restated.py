@@ -7,19 +7,20 @@ check that this restatement equals torch autograd of ``oracle.mpm_torch``, so
 the derivation the CUDA kernels implement is pinned without a GPU; the GPU
 tests then compare the kernels with autograd directly.
 
-Scope as the CUDA adjoint: USF or USL, the per-step volume set-up of
+Scope as the CUDA adjoint: USF or USL; the per-step volume set-up of
 solve_jit or the carried volume and constant mass of solve (``reinit``
-False: V' = V f carries its own adjoint, and the mass none), LinearElastic
-with a per-particle E, gravity, velocity constraints, particle tractions
+False: V' = V f carries its own adjoint, and the mass none); LinearElastic
+or SimpleMaterial with a per-particle E and the build's Newtonian; gravity,
+velocity constraints, concentrated nodal forces; particle tractions
 (t = f(t) tau V / size: the shape-function adjoint gains F-bar . t and, where
-the volume at force time varies, the volume adjoint N F-bar . t / V), and
+the volume at force time varies, the volume adjoint N F-bar . t / V); and
 particle velocity constraints (a held component of the end-of-step velocity
-is a constant: its adjoint is cleared before the reverse passes).  USL reverses in six
-passes (the order of the CUDA launches): U, the stress update after G2P
-(strain-rate adjoints from the updated nodal velocities vB); G, their
-transposed gather to the nodes; then passes 1-4 as for USF, with the forces
-of pass 2 on the start-of-step stress and volume and no strain-rate gather in
-pass 3.
+is a constant: its adjoint is cleared before the reverse passes).  USL
+reverses in six passes (the order of the CUDA launches): U, the stress
+update after G2P (strain-rate adjoints from the updated nodal velocities
+vB); G, their transposed gather to the nodes; then passes 1-4 as for USF,
+with the forces of pass 2 on the start-of-step stress and volume and no
+strain-rate gather in pass 3.
 """
 from __future__ import annotations
 
@@ -57,12 +58,16 @@ class Restated:
         n = len(mid)
         self.c1, self.c2, self.c3 = np.zeros(n), np.zeros(n), np.zeros(n)
         self.newt, self.K, self.mu = np.zeros(n, bool), np.zeros(n), np.zeros(n)
+        self.simple, self.Es = np.zeros(n, bool), np.zeros(n)
         for k, mat in enumerate(tsim.materials):
             sel = mid == k
             kind = type(mat).__name__
             if kind == "LinearElastic":
                 c = le_coefficients(float(mat.properties["poisson_ratio"]))
                 self.c1[sel], self.c2[sel], self.c3[sel] = c
+            elif kind == "SimpleMaterial":   # sigma += E deps (E per particle if given)
+                self.simple[sel] = True
+                self.Es[sel] = float(mat.properties["E"])
             elif kind == "Newtonian":
                 self.newt[sel] = True
                 self.K[sel] = float(mat.properties["bulk_modulus"])
@@ -70,6 +75,7 @@ class Restated:
             else:
                 raise NotImplementedError(kind)
         self.tractions = [(pids.numpy(), d, tau, fn) for pids, d, tau, fn in tsim.tractions]
+        self.cnf = [(ids.numpy(), d, F, fn) for ids, d, F, fn in tsim.cnf]
         self.pcons = [(pids.numpy(), d, vel) for pids, d, vel in tsim.pcons]
 
     def geometry(self, x):
@@ -109,6 +115,10 @@ class Restated:
         d0, d1, d3 = r0 * dt, r1 * dt, r3 * dt
         a1, a2, Gm = E * self.c1, E * self.c2, E * self.c3
         out = s + np.stack([a1 * d0 + a2 * d1, a2 * d0 + a1 * d1, a2 * d0 + a2 * d1, Gm * d3], 1)
+        if self.simple.any():
+            Es = E if E is not None else self.Es
+            si = s + np.stack([Es * d0, Es * d1, 0 * d0, Es * d3], 1)
+            out = np.where(self.simple[:, None], si, out)
         if self.newt.any():
             kv, t3, mu = self.K * vsc2, (r0 + r1) / 3.0, self.mu
             tot = np.stack([kv + 2 * mu * (r0 - t3), kv + 2 * mu * (r1 - t3), kv - 2 * mu * t3,
@@ -121,6 +131,13 @@ class Restated:
         of the updated centroid volumetric strain and the particles whose
         stress is total (their start-of-step stress passes no adjoint)."""
         r0b, r1b, r3b, Eb = self.stress_reverse_elastic(sb, E, r0, r1, r3)
+        if self.simple.any():
+            Es = E if E is not None else self.Es
+            dt, sm = self.dt, self.simple
+            r0b = np.where(sm, np.where(r0 != 0, Es * sb[:, 0] * dt, 0.0), r0b)
+            r1b = np.where(sm, np.where(r1 != 0, Es * sb[:, 1] * dt, 0.0), r1b)
+            r3b = np.where(sm, np.where(r3 != 0, Es * sb[:, 3] * dt, 0.0), r3b)
+            Eb = np.where(sm, r0 * dt * sb[:, 0] + r1 * dt * sb[:, 1] + r3 * dt * sb[:, 3], Eb)
         vscb = np.zeros_like(r0)
         if self.newt.any():
             tr = sb[:, 0] + sb[:, 1] + sb[:, 2]
@@ -194,6 +211,11 @@ class Restated:
         fy = Gy * s2[:, 1:2] + Gx * s2[:, 3:4]
         F = self.scatter(ids, np.stack([-V[:, None] * fx, -V[:, None] * fy], 2))
         F = F + self.scatter(ids, N[:, :, None] * (m[:, None] * self.g[None, :])[:, None, :])
+        # concentrated nodal forces at step i (constants: no adjoint)
+        for nid, d, Fv, fn in self.cnf:
+            fval = 1.0 if fn is None else float(np.interp(float(np.float64(i) * self.dt), fn.xvalues,
+                                                          fn.fxvalues))
+            np.add.at(F[:, d], nid, fval * Fv)
         # particle tractions at step i: tq = sum f(t) tau / size, t = tq V
         tq = np.zeros_like(x)
         if self.tractions:

@@ -204,3 +204,32 @@ def test_restated_reverse_matches_autograd_elastic_newtonian_mixture(scheme, rei
     assert rel(got["x"], x0.grad.numpy()) < 1e-9
     assert rel(got["v"], v0.grad.numpy()) < 1e-9
     assert np.all(got["E"][r.newt] == 0.0)
+
+
+@pytest.mark.parametrize("reinit", [True, False])
+@pytest.mark.parametrize("scheme", ["usf", "usl"])
+def test_restated_reverse_matches_autograd_simple_material_nodal_force(scheme, reinit):
+    """SimpleMaterial with a per-particle E under a ramped concentrated nodal
+    force (a constant of the state: it changes the trajectory, not the
+    reverse passes)."""
+    from mixed_cases import simple_with_nodal_force
+    o, g, E0 = simple_with_nodal_force(O, scheme, dtype=np.float64)
+    tsim, st0 = T.from_solver(o, g)
+    n = len(E0)
+    rng = np.random.Generator(np.random.PCG64(17))
+    W = rng.normal(size=(n, 2))
+    U = rng.normal(size=(n, 2))
+    r = Restated(tsim, reinit=reinit)
+    assert r.simple.all() and r.cnf
+    keys = ("x", "v", "sig", "rho", "nv", "vsc") + (() if reinit else ("vol", "mass"))
+    got, end = r.gradient({k: st0[k].numpy().copy() for k in keys}, E0, 24, W, U)
+    Et = torch.tensor(E0, requires_grad=True)
+    x0 = st0["x"].clone().requires_grad_(True)
+    v0 = st0["v"].clone().requires_grad_(True)
+    end_t = tsim.run(dict(st0, x=x0, v=v0), 24, E=Et, reinit=reinit)
+    assert rel(end["x"], end_t["x"].detach().numpy()) < 1e-13
+    L = (end_t["x"] * torch.tensor(W)).sum() + (end_t["v"] * torch.tensor(U)).sum()
+    L.backward()
+    assert rel(got["E"], Et.grad.numpy()) < 1e-9
+    assert rel(got["x"], x0.grad.numpy()) < 1e-9
+    assert rel(got["v"], v0.grad.numpy()) < 1e-9

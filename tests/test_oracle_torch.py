@@ -158,3 +158,19 @@ def test_forward_matches_numpy_oracle_elastic_newtonian_mixture(scheme, reinit):
     assert rel(st["v"].numpy(), p.velocity.reshape(-1, 2)) < 1e-12
     assert rel(st["sig"].numpy(), p.stress.reshape(-1, 6)[:, :4]) < 1e-12
     assert rel(st["vsc"].numpy(), p.volumetric_strain_centroid.reshape(-1)) < 1e-12
+
+
+@pytest.mark.parametrize("scheme", ["usf", "usl"])
+def test_forward_matches_numpy_oracle_simple_material_nodal_force(scheme):
+    """SimpleMaterial with a per-particle E and a ramped concentrated nodal force."""
+    from mixed_cases import simple_with_nodal_force
+    o, g, E0 = simple_with_nodal_force(O, scheme, dtype=np.float64)
+    sim, st = T.from_solver(o, g)
+    E = torch.tensor(E0, dtype=torch.float64)
+    for i in range(24):
+        o.step(i, g)
+        st = sim.step(st, i, E=E)
+    p = o.mesh.particles[0]
+    assert rel(st["x"].numpy(), p.loc.reshape(-1, 2)) < 1e-13
+    assert rel(st["v"].numpy(), p.velocity.reshape(-1, 2)) < 1e-12
+    assert rel(st["sig"].numpy(), p.stress.reshape(-1, 6)[:, :4]) < 1e-12
