@@ -174,3 +174,21 @@ def test_forward_matches_numpy_oracle_simple_material_nodal_force(scheme):
     assert rel(st["x"].numpy(), p.loc.reshape(-1, 2)) < 1e-13
     assert rel(st["v"].numpy(), p.velocity.reshape(-1, 2)) < 1e-12
     assert rel(st["sig"].numpy(), p.stress.reshape(-1, 6)[:, :4]) < 1e-12
+
+
+@pytest.mark.parametrize("scheme", ["usf", "usl"])
+def test_float32_forward_tracks_the_float32_oracle(scheme):
+    """In float32 the torch restatement runs the oracle's float32 program (the
+    one the GPU adjoint is compared with) up to the order of its sums."""
+    dt = 1e-3 if scheme == "usf" else 2.5e-4
+    o, g, info = workloads.differentiation(O, n=16, sim_steps=24, dt=dt, velocity=_sheared,
+                                           scheme=scheme)
+    sim, st = T.from_solver(o, g, dtype=torch.float32)
+    E = torch.tensor(info["E"], dtype=torch.float32)
+    for i in range(24):
+        o.step(i, g)
+        st = sim.step(st, i, E=E)
+    p = o.mesh.particles[0]
+    assert rel(st["x"].numpy(), p.loc.reshape(-1, 2)) < 1e-6
+    assert rel(st["v"].numpy(), p.velocity.reshape(-1, 2)) < 1e-5
+    assert rel(st["sig"].numpy(), p.stress.reshape(-1, 6)[:, :4]) < 1e-5
