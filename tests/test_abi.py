@@ -237,3 +237,26 @@ def test_tuning_cache_file_helpers(tmp_path, monkeypatch):
     assert engine._read_tuning_cache(path) == {}
     # the candidate set is part of every key's hash input
     assert "forces_lpc 0,1,2" in engine._TUNING_SPACE
+
+
+def test_status_codes_map_to_python_exceptions(built):
+    """Non-zero statuses raise MpmError naming the status and carrying the
+    library's message; MPM_ERR_OUT_OF_MESH raises OutOfMeshError, which is
+    also a ValueError (the reference raises ValueError for bad inputs)."""
+    from diffmpm_gb300 import _lib
+    lib = _lib.load()
+    _lib.check(_lib.MPM_OK)
+    d = _lib.MpmDesc()
+    d.ndim, d.scheme = 2, 7
+    d.nelements[0] = d.nelements[1] = 2
+    d.el_len[0] = d.el_len[1] = 0.5
+    h = ctypes.c_void_p()
+    rc = lib.mpm_create(ctypes.byref(d), ctypes.byref(h))
+    with pytest.raises(_lib.MpmError, match="MPM_ERR_INVALID.*scheme"):
+        _lib.check(rc)
+    with pytest.raises(_lib.OutOfMeshError) as e:
+        _lib.check(3)
+    assert isinstance(e.value, ValueError) and e.value.code == 3
+    with pytest.raises(_lib.MpmError) as e:
+        _lib.check_batch(lib.mpm_batch_create(None, 0, ctypes.byref(ctypes.c_void_p())))
+    assert e.value.code == 1 and "at least one simulation" in str(e.value)
